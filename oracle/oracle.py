@@ -1,0 +1,376 @@
+"""Python side of the CPU oracle -- TEST INFRASTRUCTURE ONLY.
+
+Thin ctypes wrappers over ``liborc.so`` (the C restatement in
+``scalit_oracle.c``) plus the PIST outer loop, which is restated here in NumPy
+because its dense eigen-step is LAPACK ``DSYEV`` in the reference
+(``src/iterate/libiterate/pist/pist.f90:54,62``) and NumPy's ``eigvalsh`` is the
+same LAPACK family.  Only tests, the package's smoke check and the benchmark's
+CPU-baseline leg import this module.
+
+Parity status: pinned against the reference's known-answer test patterns and
+independent mathematics (see the header of ``scalit_oracle.c``); the reference
+itself cannot be built here, so no output of the reference is compared.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+from . import build as _build
+
+FMAX = 20
+_lib = None
+
+_dp = C.POINTER(C.c_double)
+_ip = C.POINTER(C.c_int)
+
+
+class OrcOSB(C.Structure):
+    _fields_ = [("sF", C.c_int), ("sN", C.c_int * FMAX), ("sDEP", C.c_int * FMAX),
+                ("sNDVR", C.c_int), ("H0", _dp), ("RES", _dp), ("DEP", _dp),
+                ("OUTH", _dp), ("E0", C.c_double)]
+
+
+_OP = C.CFUNCTYPE(None, C.c_void_p, C.c_int, _dp, _dp)
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        path = _build.build()
+        L = C.CDLL(path)
+        L.orc_h1x_xyz.argtypes = [C.c_int, C.c_int, C.c_int, _dp, _dp, _dp]
+        L.orc_h1tx_xyz.argtypes = [C.c_int, C.c_int, C.c_int, _dp, _dp, _dp]
+        L.orc_h1x_dep.argtypes = [C.c_int, C.c_int, C.c_int, _dp, _dp, _dp, _dp]
+        L.orc_h3x.argtypes = [C.c_int, C.c_int, _dp, _dp, _dp]
+        L.orc_vx.argtypes = [C.c_int, C.c_int, C.c_int, _dp, _dp]
+        L.orc_vtx.argtypes = [C.c_int, C.c_int, C.c_int, _dp, _dp]
+        L.orc_myhx.argtypes = [C.POINTER(OrcOSB), C.c_int, _dp, _dp, _dp]
+        L.orc_mypx.argtypes = [C.POINTER(OrcOSB), _dp, _dp, C.c_int, C.c_int, C.c_double,
+                               C.c_double, _dp, _dp]
+        L.orc_mypx.restype = C.c_int
+        L.orc_hosbinit_xyz.argtypes = [C.c_int, C.c_int, C.c_int, _dp, _dp, _dp]
+        L.orc_hosbinit_dep.argtypes = [C.c_int, C.c_int, C.c_int, _dp, _dp, _dp, _dp]
+        L.orc_mjacobi.argtypes = [C.c_int, C.c_int, C.c_int, C.c_int, _dp, _dp]
+        L.orc_mjacobi.restype = C.c_double
+        L.orc_sumoffdiag.argtypes = [C.c_int, C.c_int, _dp]
+        L.orc_sumoffdiag.restype = C.c_double
+        L.orc_sumdiag.argtypes = [C.c_int, C.c_int, _dp]
+        L.orc_sumdiag.restype = C.c_double
+        L.orc_hosbdiag.argtypes = [C.c_int, C.c_double, C.c_int, C.c_int, C.c_int, _dp, _dp,
+                                   _dp, _dp, _ip]
+        L.orc_mydiag.argtypes = [C.POINTER(OrcOSB), C.c_int, C.c_double, _dp, _dp, _dp]
+        L.orc_mydiag.restype = C.c_int
+        L.orc_qmr.argtypes = [C.c_int, C.c_int, C.c_double, C.c_int, _dp, _OP, C.c_void_p,
+                              _OP, C.c_void_p, _dp, _dp, C.c_int, _ip]
+        L.orc_qmr.restype = C.c_int
+        L.orc_osb_qmr.argtypes = [C.POINTER(OrcOSB), _dp, _dp, C.c_int, C.c_double, C.c_double,
+                                  C.c_int, C.c_int, C.c_double, _dp, _dp, _dp, C.c_int, _ip]
+        L.orc_osb_qmr.restype = C.c_int
+        L.orc_mgs_orth.argtypes = [C.c_int, _dp, C.c_int, _dp]
+        L.orc_mgs_orth.restype = C.c_int
+        L.orc_dot.argtypes = [C.c_longlong, _dp, _dp]
+        L.orc_dot.restype = C.c_double
+        L.orc_num_threads.restype = C.c_int
+        _lib = L
+    return _lib
+
+
+def _p(a: np.ndarray):
+    assert a.dtype == np.float64 and a.flags.c_contiguous
+    return a.ctypes.data_as(_dp)
+
+
+def _f64(a) -> np.ndarray:
+    return np.ascontiguousarray(a, dtype=np.float64)
+
+
+def num_threads() -> int:
+    return lib().orc_num_threads()
+
+
+# ----------------------------------------------------------------------------------
+# per-level contractions
+# ----------------------------------------------------------------------------------
+def h1x_xyz(nin, nout, blk, H, X):
+    H, X = _f64(H), _f64(X)
+    Y = np.empty_like(X)
+    lib().orc_h1x_xyz(nin, nout, blk, _p(H), _p(X), _p(Y))
+    return Y
+
+
+def h1tx_xyz(nin, nout, blk, H, X):
+    H, X = _f64(H), _f64(X)
+    Y = np.empty_like(X)
+    lib().orc_h1tx_xyz(nin, nout, blk, _p(H), _p(X), _p(Y))
+    return Y
+
+
+def h1x_dep(nin, nout, blk, H, corx, X):
+    H, corx, X = _f64(H), _f64(corx), _f64(X)
+    Y = np.empty_like(X)
+    lib().orc_h1x_dep(nin, nout, blk, _p(H), _p(corx), _p(X), _p(Y))
+    return Y
+
+
+def h3x(nin, nout, A, X):
+    A, X = _f64(A), _f64(X)
+    Y = np.empty_like(X)
+    lib().orc_h3x(nin, nout, _p(A), _p(X), _p(Y))
+    return Y
+
+
+def vx(nin, nout, blk, V, X):
+    V, X = _f64(V), _f64(X).copy()
+    lib().orc_vx(nin, nout, blk, _p(V), _p(X))
+    return X
+
+
+def vtx(nin, nout, blk, V, X):
+    V, X = _f64(V), _f64(X).copy()
+    lib().orc_vtx(nin, nout, blk, _p(V), _p(X))
+    return X
+
+
+# ----------------------------------------------------------------------------------
+# whole operator
+# ----------------------------------------------------------------------------------
+class Operator:
+    """The OSB operator state (module globals H0/RES/DEP/VOSB/EIG0 of the reference)."""
+
+    def __init__(self, sizes, dep, H0, RES, DEP, E0=0.0, ndvr=False, OUTH=None):
+        self.sizes = tuple(int(n) for n in sizes)
+        self.dep = tuple(bool(d) for d in dep)
+        self.H0, self.RES = _f64(H0), _f64(RES)
+        self.DEP = _f64(DEP if DEP is not None and len(DEP) else np.zeros(1))
+        self.OUTH = _f64(OUTH) if OUTH is not None else np.zeros(1)
+        self.E0 = float(E0)
+        self.ndvr = bool(ndvr)
+        self.N = int(np.prod(self.sizes))
+        self.VOSB = None
+        self.EIG0 = None
+        self._tmp = np.empty(self.N)
+        self._struct = OrcOSB()
+        self._sync()
+
+    @classmethod
+    def from_problem(cls, problem, E0=0.0):
+        return cls(problem.sizes, problem.dep, problem.H0, problem.RES, problem.DEP, E0)
+
+    def _sync(self):
+        s = self._struct
+        s.sF = len(self.sizes)
+        for i, n in enumerate(self.sizes):
+            s.sN[i] = n
+            s.sDEP[i] = int(self.dep[i])
+        s.sNDVR = int(self.ndvr)
+        s.H0, s.RES, s.DEP, s.OUTH = _p(self.H0), _p(self.RES), _p(self.DEP), _p(self.OUTH)
+        s.E0 = self.E0
+
+    def set_e0(self, e0):
+        self.E0 = float(e0)
+        self._sync()
+
+    @property
+    def vosb_len(self) -> int:
+        blk = np.cumprod((self.sizes[1:] + (1,))[::-1])[::-1]
+        return int(sum(int(b) * n * n for b, n in zip(blk, self.sizes)))
+
+    def hx(self, X, ntype=1):
+        X = _f64(X)
+        Y = np.empty_like(X)
+        lib().orc_myhx(C.byref(self._struct), int(ntype), _p(X), _p(Y), _p(self._tmp))
+        return Y
+
+    def build_osb(self, bjmax, bjtol):
+        """myDiag: returns per-level stats (the reference's eff(1:5))."""
+        self.VOSB = np.empty(self.vosb_len)
+        self.EIG0 = self.RES.copy()
+        stats = np.zeros(5 * len(self.sizes))
+        rc = lib().orc_mydiag(C.byref(self._struct), int(bjmax), float(bjtol), _p(self.VOSB),
+                              _p(self.EIG0), _p(stats))
+        if rc != 0:
+            raise MemoryError("oracle myDiag allocation failed")
+        return stats.reshape(len(self.sizes), 5)
+
+    def px(self, X, nosb=1, npc=1, de=0.0, beta=0.0):
+        X = _f64(X)
+        Y = np.empty_like(X)
+        rc = lib().orc_mypx(C.byref(self._struct), _p(self.VOSB), _p(self.EIG0), int(nosb),
+                            int(npc), float(de), float(beta), _p(X), _p(Y))
+        if rc != 0:
+            raise ValueError("unsupported preconditioner kind")
+        return Y
+
+    def qmr(self, B, qmrmax, qmrtol, nosb=1, de=0.0, beta=0.0, ntype=-1, mpi_codes=True):
+        """OSB_QMR: returns (status, X, RES, iterations)."""
+        B = _f64(B)
+        X = np.zeros_like(B)
+        res = C.c_double(0.0)
+        it = C.c_int(0)
+        rc = lib().orc_osb_qmr(C.byref(self._struct), _p(self.VOSB), _p(self.EIG0), int(nosb),
+                               float(de), float(beta), int(ntype), int(qmrmax), float(qmrtol),
+                               _p(B), _p(X), C.byref(res), int(bool(mpi_codes)), C.byref(it))
+        return rc, X, res.value, it.value
+
+
+def qmr_dense(H, B, qmrmax, qmrtol, ntype=0, mpi_codes=False):
+    """QMR on an explicit symmetric matrix with the Jacobi preconditioner
+    (the operators of src/iterate/libiterate/qmr/testing/qmr.drv.f90:56-119)."""
+
+    class Dense(C.Structure):
+        _fields_ = [("n", C.c_int), ("H", _dp)]
+
+    H = np.asfortranarray(H, dtype=np.float64)
+    Hc = np.ascontiguousarray(H.ravel(order="F"))
+    n = H.shape[0]
+    ctx = Dense(n, _p(Hc))
+    L = lib()
+    hx = _OP(("orc_dense_hx", L))
+    px = _OP(("orc_dense_jacobi_px", L))
+    B = _f64(B)
+    X = np.zeros(n)
+    res = C.c_double(0.0)
+    it = C.c_int(0)
+    rc = L.orc_qmr(int(ntype), int(qmrmax), float(qmrtol), n, _p(B), hx, C.byref(ctx), px,
+                   C.byref(ctx), _p(X), C.byref(res), int(bool(mpi_codes)), C.byref(it))
+    return rc, X, res.value
+
+
+def mgs_orth(W, m, VJ):
+    """MGS_ORTH in place on the Fortran-ordered (n, >=m+1) array ``VJ``."""
+    assert VJ.flags.f_contiguous
+    n = VJ.shape[0]
+    W = _f64(W)
+    flat = VJ.ravel(order="K")
+    ok = lib().orc_mgs_orth(n, _p(W), int(m), flat.ctypes.data_as(_dp))
+    return bool(ok)
+
+
+# ----------------------------------------------------------------------------------
+# PIST window / convergence helpers (src/libutil/serial/base/util.f90)
+# ----------------------------------------------------------------------------------
+def get_window(E0, vec, M):
+    """getWindow0 (util.f90:669-716): the M entries closest to E0, picked one
+    at a time; ties keep the lowest index."""
+    vec = np.asarray(vec, dtype=np.float64)
+    n = vec.size
+    if n < M:
+        out = np.empty(M)
+        out[:n] = vec
+        out[n:] = vec[n - 1]
+        return out
+    absv = np.abs(vec - E0)
+    label = np.ones(n, dtype=bool)
+    out = np.empty(M)
+    for i in range(M):
+        cand = np.where(label, absv, np.inf)
+        idx = int(np.argmin(cand))    # first minimum, as the strict '>' comparison
+        out[i] = vec[idx]
+        label[idx] = False
+    return out
+
+
+def get_diff_max(v1, v2):
+    """getDiffMax (util.f90:84-100)."""
+    return float(np.max(np.abs(np.asarray(v1) - np.asarray(v2))))
+
+
+def get_sep_max(v1, v2):
+    """getSepMax (util.f90:124-149)."""
+    v1, v2 = np.asarray(v1), np.asarray(v2)
+    return float(np.max(np.min(np.abs(v1[:, None] - v2[None, :]), axis=1)))
+
+
+def pist_conv(E0, etol, ntype, x, startcnt, stepcnt, stepeig, M, m_max, h0x, linsolv,
+              log=None):
+    """PIST_CONV (src/iterate/libiterate/pist/pist.f90:7-98) with pistH0
+    (pistHij.f90:70-125) and MGS_ORTH (gsorth.f90:42-72).
+
+    ``h0x(v) -> H v`` and ``linsolv(v) -> (status, w)`` are the operator callbacks.
+    Returns ``(status, eig[M] ascending, RES, info)``.
+    """
+    x = _f64(x)
+    N = x.size
+    if stepeig >= m_max or startcnt > m_max or M > m_max:
+        return 0, np.zeros(M), 0.0, {}
+    VJ = np.zeros((N, m_max), order="F")
+    HMAT = np.zeros((m_max, m_max))
+    cnt_low, cnt_high = 1, max(startcnt, M, stepeig + 1)
+    info = {"qmr_iters": [], "steps": []}
+    status = 0
+    res = 0.0
+    eig = np.zeros(M)
+
+    def pisth0(m_low, m_high):
+        if m_low < 1 or m_low >= m_high or m_high > m_max:
+            return 0
+        if m_low == 1:
+            m_start = 1
+            t = np.sqrt(lib().orc_dot(N, _p(x), _p(x)))
+            if t == 0.0:
+                return 0
+            VJ[:, 0] = x / t
+        else:
+            m_start = m_low - 1
+        for J in range(m_start, m_high):
+            num, W = linsolv(np.ascontiguousarray(VJ[:, J - 1]))
+            info["qmr_iters"].append(num)
+            if num <= 0:
+                return num
+            if not mgs_orth(W, J, VJ):
+                return -J
+        for J in range(m_low, m_high + 1):
+            vj = np.ascontiguousarray(VJ[:, J - 1])
+            W = _f64(h0x(vj))
+            for I in range(1, m_high + 1):
+                vi = np.ascontiguousarray(VJ[:, I - 1])
+                HMAT[I - 1, J - 1] = lib().orc_dot(N, _p(vi), _p(W))
+                HMAT[J - 1, I - 1] = HMAT[I - 1, J - 1]
+        return m_high
+
+    while cnt_high <= m_max:
+        rc = pisth0(cnt_low, cnt_high)
+        if rc < 0:
+            return -cnt_high, eig, res, info
+        num = cnt_high - stepeig
+        tmp = np.linalg.eigvalsh(HMAT[:num, :num], UPLO="U")
+        old = get_window(E0, tmp, M)
+        num = cnt_high
+        tmp = np.linalg.eigvalsh(HMAT[:num, :num], UPLO="U")
+        eig = get_window(E0, tmp, M)
+        res = get_diff_max(eig, old) if ntype <= 0 else get_sep_max(old, tmp[:cnt_high])
+        info["steps"].append((cnt_high, res))
+        if log:
+            log(f"Cnt1={cnt_high} Cnt2={cnt_high - stepeig} RES={res}")
+        if res <= etol:
+            status = cnt_high
+            break
+        status = -cnt_high
+        cnt_low = cnt_high + 1
+        if cnt_low >= m_max:
+            status = -m_max
+            break
+        cnt_high = min(cnt_high + stepcnt, m_max)
+    info["hmat"] = HMAT[:cnt_high, :cnt_high].copy()
+    return status, np.sort(eig), res, info
+
+
+def pist_params(M0, conv):
+    """setPISTConvParam (src/iterate/module/osbw.pistconv.h:303-333).
+
+    ``conv`` = (mE0, mTol, mStart, mStep, mMax, mNum, mGap)."""
+    mE0, mTol, mStart, mStep, mMax, _mNum, mGap = conv
+    start = 2 * M0 if mStart < M0 else mStart
+    step = 5 if mStep < 1 else mStep
+    eigstep = 1 if mGap < 1 else mGap
+    nmax = start + M0 if mMax < start else mMax
+    return dict(E0=mE0, etol=mTol, startcnt=start, stepcnt=step, stepeig=eigstep, m_max=nmax)
+
+
+def start_vector(N, seed=0):
+    """Seeded uniform(0,1) start vector standing in for ``random_number(X)``
+    (osbw.pistconv.h:35)."""
+    return np.random.default_rng(seed).random(N)
