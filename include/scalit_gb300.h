@@ -1,0 +1,269 @@
+/*
+ * scalit_gb300 -- GB300 (sm_103a) implementation of ScalIT's iterate hot path:
+ * the H*X product on a direct-product DVR grid, the OSB block-Jacobi
+ * preconditioner P*X, QMR inner solves and the PIST eigensolver.
+ *
+ * C ABI.  Plain pointers and sizes only.  Arrays are column-major with the
+ * reference's level order (level 1 varies fastest).  Unless a function name
+ * ends in _device, array arguments are HOST memory owned by the caller; the
+ * library copies them.  The _device variants take device pointers on the
+ * context's device and run on the context's stream.
+ *
+ * Status convention: functions returning int return 0 (or a positive count)
+ * on success and a negative SCALIT_E* code on failure, with a message
+ * available from scalit_last_error().  Solver entry points keep the
+ * reference's sign conventions (QMR: +iterations converged, -iterations not
+ * converged, -1..-4 breakdown; PIST: +Krylov size converged, -size not
+ * converged, 0 bad parameters).
+ */
+#ifndef SCALIT_GB300_H
+#define SCALIT_GB300_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define SCALIT_FMAX 20
+
+/* error codes */
+#define SCALIT_OK 0
+#define SCALIT_EINVAL (-101)     /* bad argument */
+#define SCALIT_ECUDA (-102)      /* CUDA runtime / library failure */
+#define SCALIT_ENOMEM (-103)     /* device allocation failed */
+#define SCALIT_ESTATE (-104)     /* call out of order (e.g. P*X before the build) */
+#define SCALIT_EUNSUP (-105)     /* option not supported */
+#define SCALIT_ENONFINITE (-106) /* NaN/Inf found in an input */
+
+/* operator kinds (sHC / sPC; src/iterate/module/osb.data.h TA0, TA1) */
+#define SCALIT_TA0 0 /* H*X (no shift)        */
+#define SCALIT_TA1 1 /* (H - E0)*X            */
+
+/* preconditioner kernels (sOSB; osb.data.h TOSB..TOSBD2) */
+#define SCALIT_TOSB 1   /* 1/(EIG0 - E0)                           */
+#define SCALIT_TOSBD1 2 /* +-1/DE inside the window |EIG0-E0| <= DE */
+#define SCALIT_TOSBD2 3 /* 1/(+-alpha + beta (EIG0-E0)) in window   */
+
+/* arithmetic of the QMR inner solves */
+#define SCALIT_PREC_FP64 0
+#define SCALIT_PREC_FP32 1
+
+typedef struct scalit_ctx scalit_ctx;
+
+/* ---------------------------------------------------------------- context --
+ * Replaces the module state set up by initOSB/calOSB + loadInitData
+ * (src/iterate/module/osb.f90:17-20, osb.init.h:2-49, osb.io.h:2-42) and the
+ * MPI counterparts initMOSB/loadInitData (mosb3.init.h:5-20, posb.io.h:6-70).
+ * nlevel = sF, sizes = sN(1:sF), dep = sDEP(1:sF) (dep[0] is forced false as
+ * in osb.print.h:198-199), ndvr = sNDVR.  device = CUDA ordinal.
+ */
+int scalit_create(scalit_ctx **ctx, int nlevel, const int *sizes, const int *dep, int ndvr,
+                  int device);
+void scalit_destroy(scalit_ctx *ctx);
+const char *scalit_last_error(void);
+long long scalit_npoints(const scalit_ctx *ctx);  /* myLen */
+long long scalit_h0_len(const scalit_ctx *ctx);   /* myH0%mLen */
+long long scalit_dep_len(const scalit_ctx *ctx);  /* myDEP%mLen */
+long long scalit_vosb_len(const scalit_ctx *ctx); /* myVOSB%mLen */
+
+/* Upload H0 (concatenated level matrices), RES (diagonal potential), DEP
+ * (concatenated dependent-level factors; may be NULL if no level depends)
+ * and OUTH (outermost per-point matrices when ndvr; else NULL).  EIG0 is
+ * initialised to RES (loadRESEig, osb.io.h:71-77).  Non-finite input values
+ * are rejected with SCALIT_ENONFINITE. */
+int scalit_load(scalit_ctx *ctx, const double *H0, const double *RES, const double *DEP,
+                const double *OUTH);
+/* The CUDA stream (cudaStream_t) all of the context's work is queued on.
+ * scalit_set_stream replaces it with a caller-owned stream (NULL restores
+ * the context's own); the _device entry points are then ordered on it. */
+void *scalit_get_stream(const scalit_ctx *ctx);
+int scalit_set_stream(scalit_ctx *ctx, void *stream);
+/* sOSBW%mE0: the shift of (H - E0) and of the preconditioner. */
+int scalit_set_shift(scalit_ctx *ctx, double e0);
+/* sOSB kernel kind with sOSBW%mDE and sOSBW%mBeta. */
+int scalit_set_precond(scalit_ctx *ctx, int osb_kind, double de, double beta);
+
+/* ---------------------------------------------------------------- H * X ---
+ * MYHX (src/iterate/module/osb.hx.h:71-110; MPI mosb3.hx.h:6-66):
+ *   Y = (RES - E0 [ntype==TA1]) .* X + sum_level H_level X
+ * for nvec vectors stored one after another (each npoints long).
+ * X and Y must not overlap. */
+int scalit_hx(scalit_ctx *ctx, int ntype, int nvec, const double *X, double *Y);
+int scalit_hx_device(scalit_ctx *ctx, int ntype, int nvec, const double *dX, double *dY);
+/* One level of MYHX on device vectors: Y (+)= H_level X (level is 1-based;
+ * a dependent level is scaled by its DEP factors, H1X_DEP / H2X, hpx.f90:21-35;
+ * otherwise H1X_XYZ, hpx.f90:5-18).  accumulate != 0 adds into Y. */
+int scalit_level_device(scalit_ctx *ctx, int level, int accumulate, const double *dX, double *dY);
+/* The same operator in FP32 (the QMR inner-solve arithmetic). */
+int scalit_hx_f32_device(scalit_ctx *ctx, int ntype, int nvec, const float *dX, float *dY);
+
+/* ------------------------------------------------- OSB preconditioner -----
+ * myDiag (src/iterate/module/osb.diag.h:53-151; MPI posb.diag.h:53-198):
+ * for level = sF..1 initialise HOSB (HOSBINIT_DEP/XYZ, hinitdep.f90:10-34,
+ * hinitxyz.f90:7-29), run the joint block-Jacobi sweeps of HosbDiag
+ * (hosbdiag.f90:5-75, jacobi.f90:2-83, vupdate.f90:4-36) until
+ * |d offdiag| <= bjtol * offdiag_0 or bjmax sweeps, and take EIG0 from the
+ * rotated diagonal.  stats (may be NULL) receives 5 numbers per level: min
+ * and max Jacobi efficiency, their sum, the sum of squared diagonals and the
+ * sum of sweep counters (the reference's eff(1:5)). */
+int scalit_build_osb(scalit_ctx *ctx, int bjmax, double bjtol, double *stats);
+/* Copy the preconditioner out (VOSB: scalit_vosb_len doubles, EIG0: npoints)
+ * or in (sVOSB < 0 path: loadVOSB/loadEig, osb.io.h:124-208). */
+int scalit_get_osb(scalit_ctx *ctx, double *VOSB, double *EIG0);
+int scalit_set_osb(scalit_ctx *ctx, const double *VOSB, const double *EIG0);
+
+/* MYPX (src/iterate/module/osb.px.h:125-219; MPI mosb3.px.h:7-132):
+ *   Y = V_sF..V_1 K^-1 V_1^T..V_sF^T X, K^-1 from the sOSB kind,
+ * E0 = 0 for npc == TA0, sOSBW%mE0 otherwise. */
+int scalit_px(scalit_ctx *ctx, int npc, int nvec, const double *X, double *Y);
+int scalit_px_device(scalit_ctx *ctx, int npc, int nvec, const double *dX, double *dY);
+int scalit_px_f32_device(scalit_ctx *ctx, int npc, int nvec, const float *dX, float *dY);
+
+/* ------------------------------------------------------------------ QMR ---
+ * OSB_QMR -> QMR / QMR_MPI (src/iterate/module/osbw.qmr.h:13-23,
+ * src/iterate/libiterate/qmr/qmr.f90:5-175,
+ * src/iterate/libiterate_mpi/qmr/qmr_mpi.f90:4-263) on HX = (H-E0)X and
+ * PX = MYPX(sOSB, TA1), with x0 = 0 when ntype <= 0.  ntype selects the
+ * convergence test: |1| uses |HX - B|/|HX| (one extra H*X per iteration),
+ * |2| the max of three ratios, otherwise |R|/|B|.  Returns the reference's
+ * QMR_MPI code; *res receives RES and *iters (may be NULL) the iteration
+ * count.  precision = SCALIT_PREC_FP64 or SCALIT_PREC_FP32 (vectors, H*X
+ * and P*X in FP32, reductions accumulated in FP64; B and X stay FP64 at the
+ * boundary). */
+int scalit_qmr(scalit_ctx *ctx, int ntype, int qmrmax, double qmrtol, int precision,
+               const double *B, double *X, double *res, int *iters);
+int scalit_qmr_device(scalit_ctx *ctx, int ntype, int qmrmax, double qmrtol, int precision,
+                      const double *dB, double *dX, double *res, int *iters);
+
+/* ----------------------------------------------------------------- PIST ---
+ * OSB_PISTCONV -> PIST_CONV / PIST_CONV_MPI
+ * (src/iterate/module/osbw.pistconv.h:16-50, setPISTConvParam :303-333;
+ * src/iterate/libiterate/pist/pist.f90:7-98, pistHij.f90:70-125;
+ * src/iterate/libiterate_mpi/pist/pist_mpi.f90:11-191, pistHij_mpi.f90:83-190).
+ * Krylov vectors from inexact QMR solves of (H-E0) w = v_J, full
+ * re-orthogonalisation in FP64, HMAT = V^T H V in FP64, Ritz values of HMAT
+ * on the device, window of m values nearest e0, convergence by the largest
+ * change (ntype <= 0) or separation (ntype > 0). */
+typedef struct {
+    double e0;        /* sConv%mE0: window centre                        */
+    double etol;      /* sConv%mTol                                      */
+    int ntype;        /* sPISTConvType (0: getDiffMax)                   */
+    int startcnt;     /* pistStart                                       */
+    int stepcnt;      /* pistStep                                        */
+    int stepeig;      /* pistEigStep                                     */
+    int m;            /* sConv%mNum: number of eigenvalues               */
+    int m_max;        /* pistNMax                                        */
+    int qmr_ntype;    /* sQMRConvType (-1)                               */
+    int qmr_max;      /* sQMR%mMax                                       */
+    double qmr_tol;   /* sQMR%mTol                                       */
+    int precision;    /* SCALIT_PREC_* of the QMR inner solves           */
+    int verbose;      /* print the reference's per-step lines to stdout  */
+} scalit_pist_params;
+
+typedef struct {
+    int krylov;        /* final cnt_high                                 */
+    int qmr_total;     /* sum of QMR iterations (num3)                   */
+    int qmr_solves;    /* number of QMR solves                           */
+    int checks;        /* number of Ritz checks                          */
+    double t_qmr;      /* seconds in QMR solves                          */
+    double t_orth;     /* seconds in re-orthogonalisation                */
+    double t_hmat;     /* seconds building HMAT columns                  */
+    double t_ritz;     /* seconds in the Ritz eigen-solves               */
+} scalit_pist_info;
+
+/* Fill params from the input-file values the way setPISTConvParam does:
+ * conv = (mE0, mTol, mStart, mStep, mMax, mNum, mGap), qmr = (mMax, mTol). */
+void scalit_pist_default_params(scalit_pist_params *p, int m0, double conv_e0, double conv_tol,
+                                int conv_start, int conv_step, int conv_max, int conv_gap,
+                                int qmr_max, double qmr_tol);
+/* x0: npoints start vector (host).  eig: m values ascending.  info may be NULL. */
+int scalit_pist(scalit_ctx *ctx, const scalit_pist_params *p, const double *x0, double *eig,
+                double *res, scalit_pist_info *info);
+
+/* -------------------------------------------- Fortran drop-in symbols -----
+ * The external routines the reference's modules call, with gfortran naming
+ * (lower case, trailing underscore) and every argument by reference.  They
+ * operate on caller HOST arrays and run on the GPU of the default context
+ * (device 0 unless scalit_fortran_device_ was called).  Operator callbacks:
+ * when qmr_/qmr_mpi_/pist_conv_/pist_conv_mpi_ receive this library's own
+ * scalit_ehx_/scalit_hx0_/scalit_epx_/scalit_osb_qmr_ they run
+ * device-resident on the context made by scalit_fortran_init_; any other
+ * callback is called with host vectors. */
+
+/* H1X_XYZ (src/iterate/libiterate/hpx/hpx.f90:5-18) and
+ * H1X_XYZ_Seq (src/iterate/libiterate_mpi/hpxseq/hpx_seq.f90:7-32). */
+void h1x_xyz_(const int *nin, const int *nout, const int *blk, const double *H1,
+              const double *X, double *Y);
+void h1x_xyz_seq_(const int *nin, const int *nout, const int *blk, const double *H1,
+                  const double *X, double *Y);
+/* H1TX_XYZ_Seq (hpx_seq.f90:36-60). */
+void h1tx_xyz_seq_(const int *nin, const int *nout, const int *blk, const double *H1,
+                   const double *X, double *Y);
+/* H1X_DEP (hpx.f90:21-35) and H2X_DEP_Seq (hpx_seq.f90:67-92). */
+void h1x_dep_(const int *nin, const int *nout, const int *blk, const double *H1,
+              const double *CORX, const double *X, double *Y);
+void h2x_dep_seq_(const int *nin, const int *nout, const int *blk, const double *H1,
+                  const double *DEPX, const double *X, double *Y);
+/* H3X_Out_Seq (hpx_seq.f90:129-154): per-point outer matrices. */
+void h3x_out_seq_(const int *nin, const int *nout, const int *blk, const double *OUTH,
+                  const double *X, double *Y);
+/* VX / VTX (hpx.f90:40-73) and VX_Seq / VTX_Seq (hpx_seq.f90:192-254), in place. */
+void vx_(const int *nin, const int *nout, const int *blk, const double *VOUT, double *X);
+void vtx_(const int *nin, const int *nout, const int *blk, const double *VOUT, double *X);
+void vx_seq_(const int *nin, const int *nout, const int *blk, const double *VOUT, double *X);
+void vtx_seq_(const int *nin, const int *nout, const int *blk, const double *VOUT, double *X);
+/* HosbDiag (src/iterate/libiterate/diag/hosbdiag.f90:5-75) and
+ * HosbDiag_Seq (src/iterate/libiterate_mpi/diagseq/hosbdiag_seq.f90:5-90). */
+void hosbdiag_(const int *bjmax, const double *bjtol, const int *blk, const int *mak,
+               const int *ndk, double *HOSB, double *VOSB, double *EIGVAL);
+void hosbdiag_seq_(const int *bjmax, const double *bjtol, const int *blk, const int *mak,
+                   const int *ndk, double *HOSB, double *VOSB, double *EIGVAL, const int *id);
+/* NORM_MPI / DOTPROD_MPI (src/libutil/parallel/p_base/vector_mpi.f90:8-27,110-124);
+ * comm is ignored: one device holds the whole vector. */
+double norm_mpi_(const int *comm, const int *nin, const double *X, int *ierr);
+double dotprod_mpi_(const int *comm, const int *nin, const double *X, const double *Y,
+                    int *ierr);
+/* MGS_ORTH (src/iterate/libiterate/orth/gsorth.f90:42-72) and MGS_ORTH_MPI
+ * (src/iterate/libiterate_mpi/orth/gsorth_mpi.f90:45-76): returns a Fortran
+ * logical (1 = .true.). */
+int mgs_orth_(const int *n, const double *WJ, const int *m, double *VJ);
+int mgs_orth_mpi_(const int *n, const double *WJ, const int *m, double *VJ, int *ierr);
+/* QMR (qmr.f90:5) and QMR_MPI (qmr_mpi.f90:4). */
+typedef void (*scalit_fortran_op)(const int *n, const double *x, double *y);
+typedef int (*scalit_fortran_linsolv)(const int *n, const double *b, double *x, double *res);
+int qmr_(const int *ntype, const int *qmrmax, const double *qmrtol, const int *n,
+         const double *B, scalit_fortran_op hx, scalit_fortran_op px, double *X, double *RES);
+int qmr_mpi_(const int *ntype, const int *qmrmax, const double *qmrtol, const int *n,
+             const double *B, scalit_fortran_op hx, scalit_fortran_op px, double *X,
+             double *RES, const int *myid);
+/* PIST_CONV (pist.f90:7) and PIST_CONV_MPI (pist_mpi.f90:11). */
+int pist_conv_(const double *e0, const double *etol, const int *ntype, const int *n,
+               const double *X, const int *startcnt, const int *stepcnt, const int *stepeig,
+               const int *m, const int *m_max, scalit_fortran_op h0x,
+               scalit_fortran_linsolv linsolv, double *EIG, double *RES);
+int pist_conv_mpi_(const int *myid, const int *rootid, const double *e0, const double *etol,
+                   const int *ntype, const int *n, const double *X, const int *startcnt,
+                   const int *stepcnt, const int *stepeig, const int *m, const int *m_max,
+                   scalit_fortran_op h0x, scalit_fortran_linsolv linsolv, double *EIG,
+                   double *RES);
+
+/* Module-state seam for the drivers: replaces loadInitData + progDiag and
+ * supplies the operator callbacks HX0 (TA0), EHX (TA1), EPX (MYPX TA1) and
+ * OSB_QMR (sQMRConvType, sQMR%mMax, sQMR%mTol).  A trailing IERR argument
+ * passed by the MPI library is tolerated. */
+void scalit_fortran_device_(const int *device);
+void scalit_fortran_init_(const int *sf, const int *sn, const int *sdep, const double *H0,
+                          const double *RES, const double *DEP, const double *e0, int *ierr);
+void scalit_fortran_precond_(const int *sosb, const double *de, const double *beta,
+                             const int *bjmax, const double *bjtol, int *ierr);
+void scalit_fortran_qmr_param_(const int *ntype, const int *qmrmax, const double *qmrtol,
+                               const int *precision);
+void scalit_fortran_final_(void);
+void scalit_hx0_(const int *n, const double *X, double *Y);
+void scalit_ehx_(const int *n, const double *X, double *Y);
+void scalit_epx_(const int *n, const double *X, double *Y);
+int scalit_osb_qmr_(const int *n, const double *B, double *X, double *ERES);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* SCALIT_GB300_H */

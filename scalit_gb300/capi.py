@@ -1,0 +1,287 @@
+"""ctypes bindings of libscalit_gb300.so (the C ABI in include/scalit_gb300.h).
+
+The library must have been built (``scalit_gb300.build.build()``); loading
+fails loudly otherwise -- there is no CPU fallback.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+from . import build as _build
+
+TA0, TA1 = 0, 1
+TOSB, TOSBD1, TOSBD2 = 1, 2, 3
+PREC_FP64, PREC_FP32 = 0, 1
+FMAX = 20
+
+_dp = C.POINTER(C.c_double)
+_ip = C.POINTER(C.c_int)
+_vp = C.c_void_p
+
+# Every function the header declares: name -> (restype, argtypes).
+SIGNATURES = {
+    "scalit_create": (C.c_int, [C.POINTER(C.c_void_p), C.c_int, _ip, _ip, C.c_int, C.c_int]),
+    "scalit_destroy": (None, [_vp]),
+    "scalit_last_error": (C.c_char_p, []),
+    "scalit_npoints": (C.c_longlong, [_vp]),
+    "scalit_h0_len": (C.c_longlong, [_vp]),
+    "scalit_dep_len": (C.c_longlong, [_vp]),
+    "scalit_vosb_len": (C.c_longlong, [_vp]),
+    "scalit_load": (C.c_int, [_vp, _dp, _dp, _dp, _dp]),
+    "scalit_get_stream": (C.c_void_p, [_vp]),
+    "scalit_set_stream": (C.c_int, [_vp, _vp]),
+    "scalit_set_shift": (C.c_int, [_vp, C.c_double]),
+    "scalit_set_precond": (C.c_int, [_vp, C.c_int, C.c_double, C.c_double]),
+    "scalit_hx": (C.c_int, [_vp, C.c_int, C.c_int, _dp, _dp]),
+    "scalit_hx_device": (C.c_int, [_vp, C.c_int, C.c_int, _vp, _vp]),
+    "scalit_hx_f32_device": (C.c_int, [_vp, C.c_int, C.c_int, _vp, _vp]),
+    "scalit_level_device": (C.c_int, [_vp, C.c_int, C.c_int, _vp, _vp]),
+    "scalit_build_osb": (C.c_int, [_vp, C.c_int, C.c_double, _dp]),
+    "scalit_get_osb": (C.c_int, [_vp, _dp, _dp]),
+    "scalit_set_osb": (C.c_int, [_vp, _dp, _dp]),
+    "scalit_px": (C.c_int, [_vp, C.c_int, C.c_int, _dp, _dp]),
+    "scalit_px_device": (C.c_int, [_vp, C.c_int, C.c_int, _vp, _vp]),
+    "scalit_px_f32_device": (C.c_int, [_vp, C.c_int, C.c_int, _vp, _vp]),
+    "scalit_qmr": (C.c_int, [_vp, C.c_int, C.c_int, C.c_double, C.c_int, _dp, _dp, _dp, _ip]),
+    "scalit_qmr_device": (C.c_int, [_vp, C.c_int, C.c_int, C.c_double, C.c_int, _vp, _vp, _dp, _ip]),
+    "scalit_pist_default_params": (None, [_vp, C.c_int, C.c_double, C.c_double, C.c_int, C.c_int,
+                                          C.c_int, C.c_int, C.c_int, C.c_double]),
+    "scalit_pist": (C.c_int, [_vp, _vp, _dp, _dp, _dp, _vp]),
+    # Fortran drop-ins (all arguments by reference)
+    "h1x_xyz_": (None, [_ip, _ip, _ip, _dp, _dp, _dp]),
+    "h1x_xyz_seq_": (None, [_ip, _ip, _ip, _dp, _dp, _dp]),
+    "h1tx_xyz_seq_": (None, [_ip, _ip, _ip, _dp, _dp, _dp]),
+    "h1x_dep_": (None, [_ip, _ip, _ip, _dp, _dp, _dp, _dp]),
+    "h2x_dep_seq_": (None, [_ip, _ip, _ip, _dp, _dp, _dp, _dp]),
+    "h3x_out_seq_": (None, [_ip, _ip, _ip, _dp, _dp, _dp]),
+    "vx_": (None, [_ip, _ip, _ip, _dp, _dp]),
+    "vtx_": (None, [_ip, _ip, _ip, _dp, _dp]),
+    "vx_seq_": (None, [_ip, _ip, _ip, _dp, _dp]),
+    "vtx_seq_": (None, [_ip, _ip, _ip, _dp, _dp]),
+    "hosbdiag_": (None, [_ip, _dp, _ip, _ip, _ip, _dp, _dp, _dp]),
+    "hosbdiag_seq_": (None, [_ip, _dp, _ip, _ip, _ip, _dp, _dp, _dp, _ip]),
+    "norm_mpi_": (C.c_double, [_ip, _ip, _dp, _ip]),
+    "dotprod_mpi_": (C.c_double, [_ip, _ip, _dp, _dp, _ip]),
+    "mgs_orth_": (C.c_int, [_ip, _dp, _ip, _dp]),
+    "mgs_orth_mpi_": (C.c_int, [_ip, _dp, _ip, _dp, _ip]),
+    "qmr_": (C.c_int, [_ip, _ip, _dp, _ip, _dp, _vp, _vp, _dp, _dp]),
+    "qmr_mpi_": (C.c_int, [_ip, _ip, _dp, _ip, _dp, _vp, _vp, _dp, _dp, _ip]),
+    "pist_conv_": (C.c_int, [_dp, _dp, _ip, _ip, _dp, _ip, _ip, _ip, _ip, _ip, _vp, _vp, _dp, _dp]),
+    "pist_conv_mpi_": (C.c_int, [_ip, _ip, _dp, _dp, _ip, _ip, _dp, _ip, _ip, _ip, _ip, _ip, _vp, _vp,
+                                 _dp, _dp]),
+    "scalit_fortran_device_": (None, [_ip]),
+    "scalit_fortran_init_": (None, [_ip, _ip, _ip, _dp, _dp, _dp, _dp, _ip]),
+    "scalit_fortran_precond_": (None, [_ip, _dp, _dp, _ip, _dp, _ip]),
+    "scalit_fortran_qmr_param_": (None, [_ip, _ip, _dp, _ip]),
+    "scalit_fortran_final_": (None, []),
+    "scalit_hx0_": (None, [_ip, _dp, _dp]),
+    "scalit_ehx_": (None, [_ip, _dp, _dp]),
+    "scalit_epx_": (None, [_ip, _dp, _dp]),
+    "scalit_osb_qmr_": (C.c_int, [_ip, _dp, _dp, _dp]),
+}
+
+
+class PistParams(C.Structure):
+    _fields_ = [("e0", C.c_double), ("etol", C.c_double), ("ntype", C.c_int),
+                ("startcnt", C.c_int), ("stepcnt", C.c_int), ("stepeig", C.c_int),
+                ("m", C.c_int), ("m_max", C.c_int), ("qmr_ntype", C.c_int),
+                ("qmr_max", C.c_int), ("qmr_tol", C.c_double), ("precision", C.c_int),
+                ("verbose", C.c_int)]
+
+
+class PistInfo(C.Structure):
+    _fields_ = [("krylov", C.c_int), ("qmr_total", C.c_int), ("qmr_solves", C.c_int),
+                ("checks", C.c_int), ("t_qmr", C.c_double), ("t_orth", C.c_double),
+                ("t_hmat", C.c_double), ("t_ritz", C.c_double)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+_lib = None
+
+
+def library_path() -> str:
+    return _build.LIB
+
+
+def load(build_if_missing: bool = False):
+    """Load the shared library (build it first when asked)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    path = _build.build() if build_if_missing else _build.LIB
+    if not os.path.exists(path):
+        raise RuntimeError(f"{path} is missing: run scalit_gb300.build.build() (nvcc, sm_103a)")
+    lib = C.CDLL(path)
+    for name, (res, args) in SIGNATURES.items():
+        f = getattr(lib, name)
+        f.restype = res
+        f.argtypes = args
+    _lib = lib
+    return lib
+
+
+class ScalitError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__(f"scalit error {code}: {msg}")
+        self.code = code
+
+
+def _check(rc):
+    if rc < -100:
+        raise ScalitError(rc, load().scalit_last_error().decode())
+    return rc
+
+
+def _p(a):
+    assert a.dtype == np.float64 and a.flags.c_contiguous
+    return a.ctypes.data_as(_dp)
+
+
+def _f64(a):
+    return np.ascontiguousarray(a, dtype=np.float64)
+
+
+def _ptr(t):
+    """Raw device pointer of a torch tensor or an int."""
+    if isinstance(t, int):
+        return C.c_void_p(t)
+    return C.c_void_p(t.data_ptr())
+
+
+class Context:
+    """One OSB operator on one GPU (the reference's module state)."""
+
+    def __init__(self, sizes, dep=None, ndvr=False, device=0):
+        self.lib = load()
+        sizes = [int(n) for n in sizes]
+        dep = [int(bool(d)) for d in (dep or [0] * len(sizes))]
+        n = (C.c_int * len(sizes))(*sizes)
+        d = (C.c_int * len(dep))(*dep)
+        h = C.c_void_p()
+        _check(self.lib.scalit_create(C.byref(h), len(sizes), n, d, int(bool(ndvr)), int(device)))
+        self.h = h
+        self.sizes = tuple(sizes)
+        self.N = int(self.lib.scalit_npoints(h))
+        self.vosb_len = int(self.lib.scalit_vosb_len(h))
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.scalit_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    @classmethod
+    def from_problem(cls, problem, e0=0.0, device=0):
+        ctx = cls(problem.sizes, problem.dep, device=device)
+        ctx.load(problem.H0, problem.RES, problem.DEP)
+        ctx.set_shift(e0)
+        return ctx
+
+    def load(self, H0, RES, DEP=None, OUTH=None):
+        self._keep = [_f64(H0), _f64(RES), _f64(DEP) if DEP is not None else None,
+                      _f64(OUTH) if OUTH is not None else None]
+        H0, RES, DEP, OUTH = self._keep
+        _check(self.lib.scalit_load(self.h, _p(H0), _p(RES), _p(DEP) if DEP is not None else None,
+                                    _p(OUTH) if OUTH is not None else None))
+
+    @property
+    def stream(self) -> int:
+        return int(self.lib.scalit_get_stream(self.h) or 0)
+
+    def set_stream(self, stream_ptr):
+        _check(self.lib.scalit_set_stream(self.h, C.c_void_p(int(stream_ptr) if stream_ptr else 0)))
+
+    def set_shift(self, e0):
+        _check(self.lib.scalit_set_shift(self.h, float(e0)))
+
+    def set_precond(self, kind=TOSB, de=0.0, beta=0.0):
+        _check(self.lib.scalit_set_precond(self.h, int(kind), float(de), float(beta)))
+
+    def hx(self, X, ntype=TA1):
+        X = _f64(X)
+        nvec = X.size // self.N
+        Y = np.empty_like(X)
+        _check(self.lib.scalit_hx(self.h, int(ntype), nvec, _p(X), _p(Y)))
+        return Y
+
+    def hx_device(self, dX, dY, nvec=1, ntype=TA1):
+        _check(self.lib.scalit_hx_device(self.h, int(ntype), int(nvec), _ptr(dX), _ptr(dY)))
+
+    def level_device(self, level, dX, dY, accumulate=False):
+        _check(self.lib.scalit_level_device(self.h, int(level), int(bool(accumulate)), _ptr(dX), _ptr(dY)))
+
+    def hx_f32_device(self, dX, dY, nvec=1, ntype=TA1):
+        _check(self.lib.scalit_hx_f32_device(self.h, int(ntype), int(nvec), _ptr(dX), _ptr(dY)))
+
+    def build_osb(self, bjmax, bjtol):
+        stats = np.zeros(5 * len(self.sizes))
+        _check(self.lib.scalit_build_osb(self.h, int(bjmax), float(bjtol), _p(stats)))
+        return stats.reshape(len(self.sizes), 5)
+
+    def get_osb(self):
+        V = np.empty(self.vosb_len)
+        E = np.empty(self.N)
+        _check(self.lib.scalit_get_osb(self.h, _p(V), _p(E)))
+        return V, E
+
+    def set_osb(self, VOSB, EIG0):
+        V, E = _f64(VOSB), _f64(EIG0)
+        _check(self.lib.scalit_set_osb(self.h, _p(V), _p(E)))
+
+    def px(self, X, npc=TA1):
+        X = _f64(X)
+        nvec = X.size // self.N
+        Y = np.empty_like(X)
+        _check(self.lib.scalit_px(self.h, int(npc), nvec, _p(X), _p(Y)))
+        return Y
+
+    def px_device(self, dX, dY, nvec=1, npc=TA1):
+        _check(self.lib.scalit_px_device(self.h, int(npc), int(nvec), _ptr(dX), _ptr(dY)))
+
+    def px_f32_device(self, dX, dY, nvec=1, npc=TA1):
+        _check(self.lib.scalit_px_f32_device(self.h, int(npc), int(nvec), _ptr(dX), _ptr(dY)))
+
+    def qmr(self, B, qmrmax, qmrtol, ntype=-1, precision=PREC_FP64, X0=None):
+        """OSB_QMR: returns (code, X, RES, iterations)."""
+        B = _f64(B)
+        X = np.zeros_like(B) if X0 is None else _f64(X0).copy()
+        res = C.c_double(0.0)
+        it = C.c_int(0)
+        code = _check(self.lib.scalit_qmr(self.h, int(ntype), int(qmrmax), float(qmrtol),
+                                          int(precision), _p(B), _p(X), C.byref(res), C.byref(it)))
+        return code, X, res.value, it.value
+
+    def pist(self, x0, m, e0, etol, startcnt=0, stepcnt=5, m_max=0, gap=1, qmr_max=2000,
+             qmr_tol=1e-4, qmr_ntype=-1, precision=PREC_FP64, ntype=0, verbose=False):
+        """OSB_PISTCONV: returns (status, eig[m], RES, info dict)."""
+        p = PistParams()
+        self.lib.scalit_pist_default_params(C.byref(p), int(m), float(e0), float(etol),
+                                            int(startcnt), int(stepcnt), int(m_max), int(gap),
+                                            int(qmr_max), float(qmr_tol))
+        p.qmr_ntype = int(qmr_ntype)
+        p.precision = int(precision)
+        p.ntype = int(ntype)
+        p.verbose = int(bool(verbose))
+        x0 = _f64(x0)
+        eig = np.zeros(int(m))
+        res = C.c_double(0.0)
+        info = PistInfo()
+        st = _check(self.lib.scalit_pist(self.h, C.byref(p), _p(x0), _p(eig), C.byref(res),
+                                         C.byref(info)))
+        return st, eig, res.value, dict(info.as_dict(), m_max=p.m_max, startcnt=p.startcnt)

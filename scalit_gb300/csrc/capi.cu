@@ -1,0 +1,1007 @@
+// The C ABI of libscalit_gb300: context management, the whole-operator entry
+// points and the Fortran drop-in symbols (gfortran naming, arguments by
+// reference, caller-owned host arrays).
+#include "internal.cuh"
+
+#include <cusolverDn.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdarg>
+#include <cstring>
+#include <mutex>
+#include <vector>
+
+namespace sc {
+
+static thread_local char g_err[512] = "";
+
+void set_error(const char *fmt, ...)
+{
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(g_err, sizeof(g_err), fmt, ap);
+    va_end(ap);
+}
+
+int cuda_fail(cudaError_t e, const char *what, const char *file, int line)
+{
+    set_error("%s failed: %s (%s:%d)", what, cudaGetErrorString(e), file, line);
+    if (e == cudaErrorMemoryAllocation) return SCALIT_ENOMEM;
+    return SCALIT_ECUDA;
+}
+
+void Layout::compute()
+{
+    dim[0] = 1;
+    for (int i = 0; i < nlev - 1; ++i) dim[i + 1] = dim[i] * n[i];
+    blk[nlev - 1] = 1;
+    for (int i = nlev - 1; i >= 1; --i) blk[i - 1] = blk[i] * n[i];
+    N = blk[0] * n[0];
+    i64 h = 0, d = 0, v = 0;
+    for (int i = 0; i < nlev; ++i) {
+        h0s[i] = h;
+        if (!(ndvr && i == nlev - 1)) h += (i64)n[i] * n[i];
+        deps[i] = d;
+        if (dep[i]) d += dim[i];
+        vs[i] = v;
+        v += blk[i] * (i64)n[i] * n[i];
+    }
+    h0len = h;
+    deplen = d;
+    vlen = v;
+    outhlen = ndvr ? (i64)n[nlev - 1] * N : 0;
+}
+
+int work_get(scalit_ctx *c, size_t bytes, void **out)
+{
+    if (c->work_bytes < bytes) {
+        if (c->work) {
+            cudaStreamSynchronize(c->stream);
+            cudaFree(c->work);
+            c->work = nullptr;
+            c->work_bytes = 0;
+        }
+        SC_CUDA(cudaMalloc(&c->work, bytes));
+        c->work_bytes = bytes;
+    }
+    *out = c->work;
+    return 0;
+}
+
+int sync_read_doubles(scalit_ctx *c, const double *dsrc, double *host, int count)
+{
+    SC_CUDA(cudaMemcpyAsync(c->h_pinned, dsrc, sizeof(double) * count, cudaMemcpyDeviceToHost, c->stream));
+    SC_CUDA(cudaStreamSynchronize(c->stream));
+    memcpy(host, c->h_pinned, sizeof(double) * count);
+    return 0;
+}
+
+// Scratch context for routines that need only a stream and reduction scratch.
+static int ctx_base_init(scalit_ctx *c, int device)
+{
+    c->device = device;
+    SC_CUDA(cudaSetDevice(device));
+    SC_CUDA(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
+    SC_CUDA(cudaMalloc(&c->red_partial, sizeof(double) * 4 * 152 * 4 + 64));
+    SC_CUDA(cudaMalloc(&c->red_counter, sizeof(unsigned int) * 4));
+    SC_CUDA(cudaMemset(c->red_counter, 0, sizeof(unsigned int) * 4));
+    SC_CUDA(cudaMalloc(&c->red_result, sizeof(double) * 16));
+    SC_CUDA(cudaMallocHost(&c->h_pinned, 4096));
+    cusolverDnHandle_t h = nullptr;
+    if (cusolverDnCreate(&h) != CUSOLVER_STATUS_SUCCESS) {
+        set_error("cusolverDnCreate failed");
+        return SCALIT_ECUDA;
+    }
+    c->cusolver = h;
+    return 0;
+}
+
+static bool all_finite(const double *a, i64 n)
+{
+    for (i64 i = 0; i < n; ++i)
+        if (!std::isfinite(a[i])) return false;
+    return true;
+}
+
+template <class T>
+static int hx_many(scalit_ctx *c, int ntype, int nvec, const T *dX, T *dY)
+{
+    if (!c->loaded) { set_error("H*X before scalit_load"); return SCALIT_ESTATE; }
+    if (nvec < 0) { set_error("nvec < 0"); return SCALIT_EINVAL; }
+    if (ntype != SCALIT_TA0 && ntype != SCALIT_TA1) { set_error("ntype must be TA0 or TA1"); return SCALIT_EINVAL; }
+    const T shift = ntype == SCALIT_TA0 ? T(0) : T(c->E0);
+    const i64 N = c->L.N;
+    for (int v = 0; v < nvec; ++v) {
+        int rc = hx_vec<T>(c, dX + (i64)v * N, dY + (i64)v * N, shift, T(1), nullptr, c->stream);
+        if (rc) return rc;
+    }
+    return 0;
+}
+
+template <class T>
+static int px_many(scalit_ctx *c, int npc, int nvec, const T *dX, T *dY)
+{
+    if (!c->osb_built) { set_error("P*X before the preconditioner was built or loaded"); return SCALIT_ESTATE; }
+    if (nvec < 0) { set_error("nvec < 0"); return SCALIT_EINVAL; }
+    const i64 N = c->L.N;
+    T *tmp = nullptr;
+    SC_CUDA(cudaMallocAsync(&tmp, sizeof(T) * (size_t)N, c->stream));
+    int rc = 0;
+    for (int v = 0; v < nvec && !rc; ++v)
+        rc = px_vec<T>(c, npc, dX + (i64)v * N, dY + (i64)v * N, tmp, T(1), nullptr, c->stream);
+    cudaFreeAsync(tmp, c->stream);
+    return rc;
+}
+
+}  // namespace sc
+
+using namespace sc;
+
+#define CTX_CHECK(c)                                                              \
+    do {                                                                          \
+        if (!(c)) { set_error("null context"); return SCALIT_EINVAL; }            \
+        if (cudaSetDevice((c)->device) != cudaSuccess) { set_error("cudaSetDevice failed"); return SCALIT_ECUDA; } \
+    } while (0)
+
+extern "C" {
+
+const char *scalit_last_error(void) { return g_err; }
+
+void scalit_destroy(scalit_ctx *c)
+{
+    if (!c) return;
+    cudaSetDevice(c->device);
+    if (c->stream) cudaStreamSynchronize(c->stream);
+    double *dptrs[] = {c->H0, c->RES, c->DEP, c->OUTH, c->EIG0, c->VOSB, c->red_partial, c->red_result};
+    for (double *p : dptrs) if (p) cudaFree(p);
+    float *fptrs[] = {c->H0f, c->RESf, c->DEPf, c->OUTHf, c->EIG0f, c->VOSBf};
+    for (float *p : fptrs) if (p) cudaFree(p);
+    if (c->red_counter) cudaFree(c->red_counter);
+    if (c->work) cudaFree(c->work);
+    if (c->h_pinned) cudaFreeHost(c->h_pinned);
+    if (c->cusolver) cusolverDnDestroy((cusolverDnHandle_t)c->cusolver);
+    if (c->own_stream) c->stream = c->own_stream;
+    if (c->stream) cudaStreamDestroy(c->stream);
+    delete c;
+}
+
+int scalit_create(scalit_ctx **out, int nlevel, const int *sizes, const int *dep, int ndvr, int device)
+{
+    if (!out) { set_error("null output pointer"); return SCALIT_EINVAL; }
+    *out = nullptr;
+    if (nlevel < 1 || nlevel > SCALIT_FMAX || !sizes) {
+        set_error("nlevel=%d out of range 1..%d", nlevel, SCALIT_FMAX);
+        return SCALIT_EINVAL;
+    }
+    scalit_ctx *c = new scalit_ctx();
+    Layout &L = c->L;
+    L.nlev = nlevel;
+    L.ndvr = ndvr ? 1 : 0;
+    i64 N = 1;
+    for (int i = 0; i < nlevel; ++i) {
+        if (sizes[i] < 1 || sizes[i] > 4096) {
+            set_error("level %d size %d out of range 1..4096", i + 1, sizes[i]);
+            delete c;
+            return SCALIT_EINVAL;
+        }
+        L.n[i] = sizes[i];
+        L.dep[i] = (dep && i > 0) ? (dep[i] != 0) : 0;   // sDEP(1) forced false
+        N *= sizes[i];
+        if (N > 2147483647LL) { set_error("grid of more than 2^31-1 points"); delete c; return SCALIT_EINVAL; }
+    }
+    if (L.ndvr) L.dep[nlevel - 1] = 0;
+    L.compute();
+    int rc = ctx_base_init(c, device);
+    if (rc) { scalit_destroy(c); return rc; }
+    auto alloc2 = [&](double **d, float **f, i64 n) -> int {
+        if (n <= 0) return 0;
+        SC_CUDA(cudaMalloc(d, sizeof(double) * (size_t)n));
+        SC_CUDA(cudaMalloc(f, sizeof(float) * (size_t)n));
+        return 0;
+    };
+    rc = alloc2(&c->H0, &c->H0f, L.h0len);
+    if (!rc) rc = alloc2(&c->RES, &c->RESf, L.N);
+    if (!rc) rc = alloc2(&c->DEP, &c->DEPf, L.deplen);
+    if (!rc) rc = alloc2(&c->OUTH, &c->OUTHf, L.outhlen);
+    if (!rc) rc = alloc2(&c->EIG0, &c->EIG0f, L.N);
+    if (!rc) rc = alloc2(&c->VOSB, &c->VOSBf, L.vlen);
+    if (rc) { scalit_destroy(c); return rc; }
+    *out = c;
+    return 0;
+}
+
+long long scalit_npoints(const scalit_ctx *c) { return c ? c->L.N : -1; }
+long long scalit_h0_len(const scalit_ctx *c) { return c ? c->L.h0len : -1; }
+long long scalit_dep_len(const scalit_ctx *c) { return c ? c->L.deplen : -1; }
+long long scalit_vosb_len(const scalit_ctx *c) { return c ? c->L.vlen : -1; }
+
+int scalit_load(scalit_ctx *c, const double *H0, const double *RES, const double *DEP, const double *OUTH)
+{
+    CTX_CHECK(c);
+    const Layout &L = c->L;
+    if (!H0 && L.h0len > 0) { set_error("H0 is required"); return SCALIT_EINVAL; }
+    if (!RES) { set_error("RES is required"); return SCALIT_EINVAL; }
+    if (L.deplen > 0 && !DEP) { set_error("DEP is required: a level depends on the coordinates"); return SCALIT_EINVAL; }
+    if (L.outhlen > 0 && !OUTH) { set_error("OUTH is required when the outer layer is per point"); return SCALIT_EINVAL; }
+    if (!all_finite(H0, L.h0len) || !all_finite(RES, L.N) || (L.deplen && !all_finite(DEP, L.deplen)) ||
+        (L.outhlen && !all_finite(OUTH, L.outhlen))) {
+        set_error("non-finite value in the Hamiltonian input");
+        return SCALIT_ENONFINITE;
+    }
+    cudaStream_t s = c->stream;
+    auto up = [&](double *d, float *f, const double *h, i64 n) -> int {
+        if (n <= 0) return 0;
+        SC_CUDA(cudaMemcpyAsync(d, h, sizeof(double) * (size_t)n, cudaMemcpyHostToDevice, s));
+        return to_f32(d, f, n, s);
+    };
+    int rc = up(c->H0, c->H0f, H0, L.h0len);
+    if (!rc) rc = up(c->RES, c->RESf, RES, L.N);
+    if (!rc) rc = up(c->DEP, c->DEPf, DEP, L.deplen);
+    if (!rc) rc = up(c->OUTH, c->OUTHf, OUTH, L.outhlen);
+    if (!rc) rc = up(c->EIG0, c->EIG0f, RES, L.N);
+    if (rc) return rc;
+    SC_CUDA(cudaStreamSynchronize(s));
+    c->loaded = true;
+    c->osb_built = false;
+    return 0;
+}
+
+void *scalit_get_stream(const scalit_ctx *c) { return c ? (void *)c->stream : nullptr; }
+
+int scalit_set_stream(scalit_ctx *c, void *stream)
+{
+    CTX_CHECK(c);
+    SC_CUDA(cudaStreamSynchronize(c->stream));
+    if (!c->own_stream) c->own_stream = c->stream;
+    c->stream = stream ? (cudaStream_t)stream : c->own_stream;
+    return 0;
+}
+
+int scalit_set_shift(scalit_ctx *c, double e0)
+{
+    if (!c) { set_error("null context"); return SCALIT_EINVAL; }
+    if (!std::isfinite(e0)) { set_error("non-finite shift"); return SCALIT_ENONFINITE; }
+    c->E0 = e0;
+    return 0;
+}
+
+int scalit_set_precond(scalit_ctx *c, int kind, double de, double beta)
+{
+    if (!c) { set_error("null context"); return SCALIT_EINVAL; }
+    if (kind == 4) { set_error("the OSBW window preconditioner (sOSB=4) is not supported"); return SCALIT_EUNSUP; }
+    if (kind < 1 || kind > 3) { set_error("unknown preconditioner kind %d", kind); return SCALIT_EINVAL; }
+    if ((kind == SCALIT_TOSBD1 || kind == SCALIT_TOSBD2) && !(fabs(de) > 0.0)) {
+        set_error("windowed preconditioner needs DE != 0");
+        return SCALIT_EINVAL;
+    }
+    c->osb_kind = kind;
+    c->osb_de = fabs(de);
+    c->osb_beta = beta;
+    return 0;
+}
+
+// --------------------------------------------------------------- H * X ---
+int scalit_hx_device(scalit_ctx *c, int ntype, int nvec, const double *dX, double *dY)
+{
+    CTX_CHECK(c);
+    return hx_many<double>(c, ntype, nvec, dX, dY);
+}
+
+int scalit_level_device(scalit_ctx *c, int level, int accumulate, const double *dX, double *dY)
+{
+    CTX_CHECK(c);
+    if (!c->loaded) { set_error("level product before scalit_load"); return SCALIT_ESTATE; }
+    if (level < 1 || level > c->L.nlev) { set_error("level %d out of range", level); return SCALIT_EINVAL; }
+    return level_apply<double>(c, level - 1, c->H0, c->DEP, c->OUTH, dX, dY, accumulate ? 1 : 0, nullptr,
+                               0.0, 1.0, nullptr, c->stream);
+}
+
+int scalit_hx_f32_device(scalit_ctx *c, int ntype, int nvec, const float *dX, float *dY)
+{
+    CTX_CHECK(c);
+    return hx_many<float>(c, ntype, nvec, dX, dY);
+}
+
+int scalit_hx(scalit_ctx *c, int ntype, int nvec, const double *X, double *Y)
+{
+    CTX_CHECK(c);
+    if (nvec <= 0) return nvec < 0 ? (set_error("nvec < 0"), SCALIT_EINVAL) : 0;
+    const i64 N = c->L.N;
+    double *w = nullptr;
+    int rc = work_get(c, sizeof(double) * 2 * (size_t)N, (void **)&w);
+    if (rc) return rc;
+    for (int v = 0; v < nvec; ++v) {
+        SC_CUDA(cudaMemcpyAsync(w, X + (i64)v * N, sizeof(double) * N, cudaMemcpyHostToDevice, c->stream));
+        rc = hx_many<double>(c, ntype, 1, w, w + N);
+        if (rc) return rc;
+        SC_CUDA(cudaMemcpyAsync(Y + (i64)v * N, w + N, sizeof(double) * N, cudaMemcpyDeviceToHost, c->stream));
+    }
+    SC_CUDA(cudaStreamSynchronize(c->stream));
+    return 0;
+}
+
+// --------------------------------------------------------------- P * X ---
+int scalit_px_device(scalit_ctx *c, int npc, int nvec, const double *dX, double *dY)
+{
+    CTX_CHECK(c);
+    return px_many<double>(c, npc, nvec, dX, dY);
+}
+
+int scalit_px_f32_device(scalit_ctx *c, int npc, int nvec, const float *dX, float *dY)
+{
+    CTX_CHECK(c);
+    return px_many<float>(c, npc, nvec, dX, dY);
+}
+
+int scalit_px(scalit_ctx *c, int npc, int nvec, const double *X, double *Y)
+{
+    CTX_CHECK(c);
+    if (nvec <= 0) return nvec < 0 ? (set_error("nvec < 0"), SCALIT_EINVAL) : 0;
+    const i64 N = c->L.N;
+    double *w = nullptr;
+    int rc = work_get(c, sizeof(double) * 2 * (size_t)N, (void **)&w);
+    if (rc) return rc;
+    for (int v = 0; v < nvec; ++v) {
+        SC_CUDA(cudaMemcpyAsync(w, X + (i64)v * N, sizeof(double) * N, cudaMemcpyHostToDevice, c->stream));
+        rc = px_many<double>(c, npc, 1, w, w + N);
+        if (rc) return rc;
+        SC_CUDA(cudaMemcpyAsync(Y + (i64)v * N, w + N, sizeof(double) * N, cudaMemcpyDeviceToHost, c->stream));
+    }
+    SC_CUDA(cudaStreamSynchronize(c->stream));
+    return 0;
+}
+
+// ---------------------------------------------------------- OSB build ---
+int scalit_build_osb(scalit_ctx *c, int bjmax, double bjtol, double *stats)
+{
+    CTX_CHECK(c);
+    if (!c->loaded) { set_error("build before scalit_load"); return SCALIT_ESTATE; }
+    if (bjmax < 0 || !(bjtol >= 0.0)) { set_error("bad block-Jacobi parameters"); return SCALIT_EINVAL; }
+    return osb_build(c, bjmax, bjtol, stats);
+}
+
+int scalit_get_osb(scalit_ctx *c, double *VOSB, double *EIG0)
+{
+    CTX_CHECK(c);
+    if (!c->osb_built) { set_error("no preconditioner built"); return SCALIT_ESTATE; }
+    if (VOSB) SC_CUDA(cudaMemcpyAsync(VOSB, c->VOSB, sizeof(double) * c->L.vlen, cudaMemcpyDeviceToHost, c->stream));
+    if (EIG0) SC_CUDA(cudaMemcpyAsync(EIG0, c->EIG0, sizeof(double) * c->L.N, cudaMemcpyDeviceToHost, c->stream));
+    SC_CUDA(cudaStreamSynchronize(c->stream));
+    return 0;
+}
+
+int scalit_set_osb(scalit_ctx *c, const double *VOSB, const double *EIG0)
+{
+    CTX_CHECK(c);
+    if (!c->loaded) { set_error("set_osb before scalit_load"); return SCALIT_ESTATE; }
+    if (!VOSB || !EIG0) { set_error("VOSB and EIG0 are required"); return SCALIT_EINVAL; }
+    if (!all_finite(VOSB, c->L.vlen) || !all_finite(EIG0, c->L.N)) { set_error("non-finite preconditioner"); return SCALIT_ENONFINITE; }
+    SC_CUDA(cudaMemcpyAsync(c->VOSB, VOSB, sizeof(double) * c->L.vlen, cudaMemcpyHostToDevice, c->stream));
+    SC_CUDA(cudaMemcpyAsync(c->EIG0, EIG0, sizeof(double) * c->L.N, cudaMemcpyHostToDevice, c->stream));
+    int rc = to_f32(c->VOSB, c->VOSBf, c->L.vlen, c->stream);
+    if (!rc) rc = to_f32(c->EIG0, c->EIG0f, c->L.N, c->stream);
+    if (rc) return rc;
+    SC_CUDA(cudaStreamSynchronize(c->stream));
+    c->osb_built = true;
+    return 0;
+}
+
+// ------------------------------------------------------------------ QMR --
+int scalit_qmr_device(scalit_ctx *c, int ntype, int qmrmax, double qmrtol, int precision,
+                      const double *dB, double *dX, double *res, int *iters)
+{
+    CTX_CHECK(c);
+    QmrResult r{};
+    int rc = qmr_run(c, ntype, qmrmax, qmrtol, precision, dB, dX, &r);
+    if (rc) return rc;
+    if (res) *res = r.res;
+    if (iters) *iters = r.iters;
+    return r.code;
+}
+
+int scalit_qmr(scalit_ctx *c, int ntype, int qmrmax, double qmrtol, int precision, const double *B,
+               double *X, double *res, int *iters)
+{
+    CTX_CHECK(c);
+    const i64 N = c->L.N;
+    double *bx = nullptr;
+    SC_CUDA(cudaMallocAsync(&bx, sizeof(double) * 2 * (size_t)N, c->stream));
+    SC_CUDA(cudaMemcpyAsync(bx, B, sizeof(double) * N, cudaMemcpyHostToDevice, c->stream));
+    if (ntype > 0) SC_CUDA(cudaMemcpyAsync(bx + N, X, sizeof(double) * N, cudaMemcpyHostToDevice, c->stream));
+    QmrResult r{};
+    int rc = qmr_run(c, ntype, qmrmax, qmrtol, precision, bx, bx + N, &r);
+    if (!rc) {
+        SC_CUDA(cudaMemcpyAsync(X, bx + N, sizeof(double) * N, cudaMemcpyDeviceToHost, c->stream));
+        SC_CUDA(cudaStreamSynchronize(c->stream));
+    }
+    cudaFreeAsync(bx, c->stream);
+    cudaStreamSynchronize(c->stream);
+    if (rc) return rc;
+    if (res) *res = r.res;
+    if (iters) *iters = r.iters;
+    return r.code;
+}
+
+// ----------------------------------------------------------------- PIST --
+void scalit_pist_default_params(scalit_pist_params *p, int m0, double conv_e0, double conv_tol,
+                                int conv_start, int conv_step, int conv_max, int conv_gap,
+                                int qmr_max, double qmr_tol)
+{
+    // setPISTConvParam (src/iterate/module/osbw.pistconv.h:303-333)
+    memset(p, 0, sizeof(*p));
+    p->e0 = conv_e0;
+    p->etol = conv_tol;
+    p->ntype = 0;
+    p->startcnt = (conv_start < m0) ? 2 * m0 : conv_start;
+    p->stepcnt = (conv_step < 1) ? 5 : conv_step;
+    p->stepeig = (conv_gap < 1) ? 1 : conv_gap;
+    p->m_max = (conv_max < p->startcnt) ? p->startcnt + m0 : conv_max;
+    p->m = m0;
+    p->qmr_ntype = -1;
+    p->qmr_max = qmr_max;
+    p->qmr_tol = qmr_tol;
+    p->precision = SCALIT_PREC_FP64;
+    p->verbose = 0;
+}
+
+int scalit_pist(scalit_ctx *c, const scalit_pist_params *p, const double *x0, double *eig, double *res,
+                scalit_pist_info *info)
+{
+    CTX_CHECK(c);
+    if (!p || !x0 || !eig || !res) { set_error("null argument"); return SCALIT_EINVAL; }
+    const i64 N = c->L.N;
+    double *dx = nullptr;
+    SC_CUDA(cudaMallocAsync(&dx, sizeof(double) * (size_t)N, c->stream));
+    SC_CUDA(cudaMemcpyAsync(dx, x0, sizeof(double) * N, cudaMemcpyHostToDevice, c->stream));
+    int rc = pist_ctx(c, p, dx, eig, res, info);
+    cudaFreeAsync(dx, c->stream);
+    cudaStreamSynchronize(c->stream);
+    return rc;
+}
+
+}  // extern "C"
+
+// ======================================================================
+// Fortran drop-in layer
+// ======================================================================
+namespace sc {
+
+static std::mutex g_fmu;
+static int g_fdev = 0;
+static scalit_ctx *g_fctx = nullptr;      // module state made by scalit_fortran_init_
+static scalit_ctx *g_scratch = nullptr;   // stream + scratch for stand-alone routines
+static struct { int ntype = -1, qmrmax = 2000; double tol = 1e-4; int precision = SCALIT_PREC_FP64; } g_fq;
+
+static scalit_ctx *scratch()
+{
+    if (g_scratch && g_scratch->device == g_fdev) return g_scratch;
+    if (g_scratch) { scalit_destroy(g_scratch); g_scratch = nullptr; }
+    scalit_ctx *c = new scalit_ctx();
+    if (ctx_base_init(c, g_fdev)) { scalit_destroy(c); return nullptr; }
+    g_scratch = c;
+    return c;
+}
+
+// Device buffers for a stand-alone call, freed on scope exit.
+struct Scoped {
+    std::vector<void *> ptrs;
+    cudaStream_t s;
+    explicit Scoped(cudaStream_t st) : s(st) {}
+    template <class T> T *get(i64 n)
+    {
+        void *p = nullptr;
+        if (cudaMalloc(&p, sizeof(T) * (size_t)std::max<i64>(n, 1)) != cudaSuccess) return nullptr;
+        ptrs.push_back(p);
+        return (T *)p;
+    }
+    ~Scoped()
+    {
+        cudaStreamSynchronize(s);
+        for (void *p : ptrs) cudaFree(p);
+    }
+};
+
+static void report(const char *who, int rc)
+{
+    if (rc) fprintf(stderr, "scalit_gb300: %s failed: %s\n", who, scalit_last_error());
+}
+
+// Y(nin, nout, blk) = per-level contraction; corx may be null; transpose uses H^T.
+static int level_host(int nin, int nout, int blk, const double *H, const double *corx, const double *X,
+                      double *Y, int transpose)
+{
+    scalit_ctx *c = scratch();
+    if (!c) return SCALIT_ECUDA;
+    const i64 n = (i64)nin * nout * blk;
+    Scoped sb(c->stream);
+    double *dH = sb.get<double>((i64)nout * nout), *dX = sb.get<double>(n), *dY = sb.get<double>(n);
+    double *dC = corx ? sb.get<double>(nin) : nullptr;
+    if (!dH || !dX || !dY || (corx && !dC)) { set_error("device allocation failed"); return SCALIT_ENOMEM; }
+    SC_CUDA(cudaMemcpyAsync(dH, H, sizeof(double) * nout * nout, cudaMemcpyHostToDevice, c->stream));
+    SC_CUDA(cudaMemcpyAsync(dX, X, sizeof(double) * n, cudaMemcpyHostToDevice, c->stream));
+    if (corx) SC_CUDA(cudaMemcpyAsync(dC, corx, sizeof(double) * nin, cudaMemcpyHostToDevice, c->stream));
+    GemmArgs<double> g{};
+    g.K = nout; g.batch = 1; g.alpha = 1.0; g.C = dY;
+    if (nin == 1) {
+        g.M = nout; g.N = blk; g.Mi = nout; g.s1 = 1; g.s2 = 0;
+        g.A = dH;
+        if (!transpose) { g.a_sk = nout; } else { g.s1 = nout; g.a_sk = 1; }
+        g.B = dX; g.b_sk = 1; g.b_sn = nout; g.c_sn = nout;
+        if (transpose) {
+            // moff is shared by A and C; use the batched GEMV for V^T-style products.
+            int rc = level_rotate<double>(1, nout, blk, dH, dX, dY, 1, nullptr, c->stream);
+            if (rc) return rc;
+            SC_CUDA(cudaMemcpyAsync(Y, dY, sizeof(double) * n, cudaMemcpyDeviceToHost, c->stream));
+            SC_CUDA(cudaStreamSynchronize(c->stream));
+            return 0;
+        }
+        (void)dC;
+    } else {
+        g.M = nin * blk; g.N = nout; g.Mi = nin; g.s1 = 1; g.s2 = (i64)nin * nout;
+        g.A = dX; g.a_sk = nin;
+        g.B = dH;
+        if (!transpose) { g.b_sk = nout; g.b_sn = 1; } else { g.b_sk = 1; g.b_sn = nout; }
+        g.c_sn = nin;
+        g.rowscale = dC;
+    }
+    int rc = launch_gemm<double>(g, c->stream);
+    if (rc) return rc;
+    SC_CUDA(cudaMemcpyAsync(Y, dY, sizeof(double) * n, cudaMemcpyDeviceToHost, c->stream));
+    SC_CUDA(cudaStreamSynchronize(c->stream));
+    return 0;
+}
+
+static int vx_host(int nin, int nout, int blk, const double *V, double *X, int transpose)
+{
+    scalit_ctx *c = scratch();
+    if (!c) return SCALIT_ECUDA;
+    const i64 n = (i64)nin * nout * blk;
+    Scoped sb(c->stream);
+    double *dV = sb.get<double>((i64)nout * nout * blk), *dX = sb.get<double>(n), *dY = sb.get<double>(n);
+    if (!dV || !dX || !dY) { set_error("device allocation failed"); return SCALIT_ENOMEM; }
+    SC_CUDA(cudaMemcpyAsync(dV, V, sizeof(double) * (size_t)nout * nout * blk, cudaMemcpyHostToDevice, c->stream));
+    SC_CUDA(cudaMemcpyAsync(dX, X, sizeof(double) * n, cudaMemcpyHostToDevice, c->stream));
+    int rc = level_rotate<double>(nin, nout, blk, dV, dX, dY, transpose, nullptr, c->stream);
+    if (rc) return rc;
+    SC_CUDA(cudaMemcpyAsync(X, dY, sizeof(double) * n, cudaMemcpyDeviceToHost, c->stream));
+    SC_CUDA(cudaStreamSynchronize(c->stream));
+    return 0;
+}
+
+template <class T>
+__global__ void h3x_blk_kernel(int nin, int nout, int blk, const T *Am, const T *X, T *Y)
+{
+    const i64 total = (i64)nin * nout * blk;
+    for (i64 e = blockIdx.x * (i64)blockDim.x + threadIdx.x; e < total; e += (i64)gridDim.x * blockDim.x) {
+        const i64 a = e % nin;
+        const i64 t = e / nin;
+        const int i = (int)(t % nout);
+        const i64 b = t / nout;
+        const T *xb = X + b * (i64)nin * nout;
+        T acc = T(0);
+        for (int j = 0; j < nout; ++j) acc = fma(Am[a + (i64)nin * (i + (i64)nout * j)], xb[a + (i64)nin * j], acc);
+        Y[e] = acc;
+    }
+}
+
+// Host-callback operators for the generic QMR / PIST drop-ins.
+struct HostQmrOps : QmrOps<double> {
+    scalit_ctx *c;
+    i64 n;
+    scalit_fortran_op fhx, fpx;
+    std::vector<double> hin, hout;
+    const int *state_done;
+    int call(scalit_fortran_op f, const double *in, double *out, const int *gate)
+    {
+        if (gate) {
+            int d = 0;
+            SC_CUDA(cudaMemcpyAsync(&d, gate, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+            SC_CUDA(cudaStreamSynchronize(c->stream));
+            if (d) return 0;
+        }
+        SC_CUDA(cudaMemcpyAsync(hin.data(), in, sizeof(double) * n, cudaMemcpyDeviceToHost, c->stream));
+        SC_CUDA(cudaStreamSynchronize(c->stream));
+        int ni = (int)n, ierr = 0;
+        // a trailing IERR argument (MPI callers) is harmless to pass
+        reinterpret_cast<void (*)(const int *, const double *, double *, int *)>(f)(&ni, hin.data(), hout.data(), &ierr);
+        SC_CUDA(cudaMemcpyAsync(out, hout.data(), sizeof(double) * n, cudaMemcpyHostToDevice, c->stream));
+        SC_CUDA(cudaStreamSynchronize(c->stream));
+        return 0;
+    }
+    int hx(const double *in, double *out, const int *gate) override { return call(fhx, in, out, gate); }
+    int px(const double *in, double *out, const int *gate) override { return call(fpx, in, out, gate); }
+    bool host_side() const override { return true; }
+};
+
+struct HostPistOps : PistOps {
+    scalit_ctx *c;
+    i64 n;
+    scalit_fortran_op fh0x;
+    scalit_fortran_linsolv flin;
+    std::vector<double> hin, hout;
+    int h0x(const double *dX, double *dY) override
+    {
+        SC_CUDA(cudaMemcpyAsync(hin.data(), dX, sizeof(double) * n, cudaMemcpyDeviceToHost, c->stream));
+        SC_CUDA(cudaStreamSynchronize(c->stream));
+        int ni = (int)n, ierr = 0;
+        reinterpret_cast<void (*)(const int *, const double *, double *, int *)>(fh0x)(&ni, hin.data(), hout.data(), &ierr);
+        SC_CUDA(cudaMemcpyAsync(dY, hout.data(), sizeof(double) * n, cudaMemcpyHostToDevice, c->stream));
+        SC_CUDA(cudaStreamSynchronize(c->stream));
+        return 0;
+    }
+    int linsolv(const double *dB, double *dX, int *num) override
+    {
+        SC_CUDA(cudaMemcpyAsync(hin.data(), dB, sizeof(double) * n, cudaMemcpyDeviceToHost, c->stream));
+        SC_CUDA(cudaStreamSynchronize(c->stream));
+        int ni = (int)n;
+        double r = 0.0;
+        *num = flin(&ni, hin.data(), hout.data(), &r);
+        SC_CUDA(cudaMemcpyAsync(dX, hout.data(), sizeof(double) * n, cudaMemcpyHostToDevice, c->stream));
+        SC_CUDA(cudaStreamSynchronize(c->stream));
+        return 0;
+    }
+};
+
+static int qmr_fortran(int ntype, int qmrmax, double tol, int n, const double *B, scalit_fortran_op hx,
+                       scalit_fortran_op px, double *X, double *RES, bool mpi_codes)
+{
+    std::lock_guard<std::mutex> lk(g_fmu);
+    *RES = 0.0;
+    if (hx == scalit_ehx_ && px == scalit_epx_ && g_fctx && g_fctx->L.N == n) {
+        scalit_ctx *f = g_fctx;
+        if (cudaSetDevice(f->device) != cudaSuccess) return -10;
+        Scoped sb(f->stream);
+        double *dB = sb.get<double>(n), *dX = sb.get<double>(n);
+        if (!dB || !dX) return -10;
+        cudaMemcpyAsync(dB, B, sizeof(double) * n, cudaMemcpyHostToDevice, f->stream);
+        if (ntype > 0) cudaMemcpyAsync(dX, X, sizeof(double) * n, cudaMemcpyHostToDevice, f->stream);
+        QmrResult r{};
+        int rc = qmr_run(f, ntype, qmrmax, tol, g_fq.precision, dB, dX, &r);
+        if (rc) { report("qmr (device)", rc); return -10; }
+        cudaMemcpyAsync(X, dX, sizeof(double) * n, cudaMemcpyDeviceToHost, f->stream);
+        cudaStreamSynchronize(f->stream);
+        *RES = r.res;
+        int code = r.code;
+        if (!mpi_codes && r.breakdown) code = (r.iters > 0) ? -r.iters : 0;
+        return code;
+    }
+    scalit_ctx *c = scratch();
+    if (!c) return -10;
+    Scoped sb(c->stream);
+    double *dB = sb.get<double>(n), *dX = sb.get<double>(n);
+    if (!dB || !dX) return -10;
+    if (cudaMemcpyAsync(dB, B, sizeof(double) * n, cudaMemcpyHostToDevice, c->stream) != cudaSuccess) return -10;
+    if (ntype > 0 && cudaMemcpyAsync(dX, X, sizeof(double) * n, cudaMemcpyHostToDevice, c->stream) != cudaSuccess) return -10;
+    HostQmrOps ops;
+    ops.c = c; ops.n = n; ops.fhx = hx; ops.fpx = px;
+    ops.hin.resize(n); ops.hout.resize(n);
+    QmrResult r{};
+    int rc = qmr_core<double>(c, n, ops, ntype, qmrmax, tol, dB, dX, &r);
+    if (rc) { report("qmr", rc); return -10; }
+    cudaMemcpyAsync(X, dX, sizeof(double) * n, cudaMemcpyDeviceToHost, c->stream);
+    cudaStreamSynchronize(c->stream);
+    *RES = r.res;
+    int code = r.code;
+    if (!mpi_codes && r.breakdown) code = (r.iters > 0) ? -r.iters : 0;
+    return code;
+}
+
+static int pist_fortran(double e0, double etol, int ntype, int n, const double *X, int startcnt, int stepcnt,
+                        int stepeig, int m, int m_max, scalit_fortran_op h0x, scalit_fortran_linsolv linsolv,
+                        double *EIG, double *RES)
+{
+    scalit_pist_params p{};
+    p.e0 = e0; p.etol = etol; p.ntype = ntype; p.startcnt = startcnt; p.stepcnt = stepcnt;
+    p.stepeig = stepeig; p.m = m; p.m_max = m_max;
+    p.qmr_ntype = g_fq.ntype; p.qmr_max = g_fq.qmrmax; p.qmr_tol = g_fq.tol; p.precision = g_fq.precision;
+    const bool own = (h0x == scalit_hx0_ && linsolv == scalit_osb_qmr_ && g_fctx && g_fctx->L.N == n);
+    if (own) {
+        int rc = scalit_pist(g_fctx, &p, X, EIG, RES, nullptr);
+        if (rc < -100) report("pist (device)", rc);
+        return rc;
+    }
+    scalit_ctx *c = scratch();
+    if (!c) return 0;
+    Scoped sb(c->stream);
+    double *dx = sb.get<double>(n);
+    if (!dx) return 0;
+    cudaMemcpyAsync(dx, X, sizeof(double) * n, cudaMemcpyHostToDevice, c->stream);
+    HostPistOps ops;
+    ops.c = c; ops.n = n; ops.fh0x = h0x; ops.flin = linsolv;
+    ops.hin.resize(n); ops.hout.resize(n);
+    int rc = pist_core(c, n, &p, dx, ops, EIG, RES, nullptr);
+    if (rc < -100) report("pist", rc);
+    return rc;
+}
+
+}  // namespace sc
+
+extern "C" {
+
+void h1x_xyz_(const int *nin, const int *nout, const int *blk, const double *H1, const double *X, double *Y)
+{
+    report("h1x_xyz", level_host(*nin, *nout, *blk, H1, nullptr, X, Y, 0));
+}
+
+void h1x_xyz_seq_(const int *nin, const int *nout, const int *blk, const double *H1, const double *X, double *Y)
+{
+    report("h1x_xyz_seq", level_host(*nin, *nout, *blk, H1, nullptr, X, Y, 0));
+}
+
+void h1tx_xyz_seq_(const int *nin, const int *nout, const int *blk, const double *H1, const double *X, double *Y)
+{
+    report("h1tx_xyz_seq", level_host(*nin, *nout, *blk, H1, nullptr, X, Y, 1));
+}
+
+void h1x_dep_(const int *nin, const int *nout, const int *blk, const double *H1, const double *CORX,
+              const double *X, double *Y)
+{
+    if (*nin == 1) {
+        // a one-point dependent factor is a scale of the whole product
+        std::vector<double> H(H1, H1 + (size_t)(*nout) * (*nout));
+        for (double &h : H) h *= CORX[0];
+        report("h1x_dep", level_host(*nin, *nout, *blk, H.data(), nullptr, X, Y, 0));
+        return;
+    }
+    report("h1x_dep", level_host(*nin, *nout, *blk, H1, CORX, X, Y, 0));
+}
+
+void h2x_dep_seq_(const int *nin, const int *nout, const int *blk, const double *H1, const double *DEPX,
+                  const double *X, double *Y)
+{
+    h1x_dep_(nin, nout, blk, H1, DEPX, X, Y);
+}
+
+void h3x_out_seq_(const int *nin, const int *nout, const int *blk, const double *OUTH, const double *X, double *Y)
+{
+    scalit_ctx *c = scratch();
+    if (!c) return;
+    const i64 n = (i64)(*nin) * (*nout) * (*blk);
+    const i64 na = (i64)(*nin) * (*nout) * (*nout);
+    Scoped sb(c->stream);
+    double *dA = sb.get<double>(na), *dX = sb.get<double>(n), *dY = sb.get<double>(n);
+    if (!dA || !dX || !dY) { report("h3x_out_seq", SCALIT_ENOMEM); return; }
+    cudaMemcpyAsync(dA, OUTH, sizeof(double) * na, cudaMemcpyHostToDevice, c->stream);
+    cudaMemcpyAsync(dX, X, sizeof(double) * n, cudaMemcpyHostToDevice, c->stream);
+    const int grid = (int)std::min<i64>((n + 255) / 256, 152 * 16);
+    h3x_blk_kernel<double><<<std::max(grid, 1), 256, 0, c->stream>>>(*nin, *nout, *blk, dA, dX, dY);
+    cudaMemcpyAsync(Y, dY, sizeof(double) * n, cudaMemcpyDeviceToHost, c->stream);
+    cudaError_t e = cudaStreamSynchronize(c->stream);
+    if (e != cudaSuccess) { set_error("h3x_out_seq: %s", cudaGetErrorString(e)); report("h3x_out_seq", SCALIT_ECUDA); }
+}
+
+void vx_(const int *nin, const int *nout, const int *blk, const double *VOUT, double *X)
+{
+    report("vx", vx_host(*nin, *nout, *blk, VOUT, X, 0));
+}
+
+void vtx_(const int *nin, const int *nout, const int *blk, const double *VOUT, double *X)
+{
+    report("vtx", vx_host(*nin, *nout, *blk, VOUT, X, 1));
+}
+
+void vx_seq_(const int *nin, const int *nout, const int *blk, const double *VOUT, double *X)
+{
+    vx_(nin, nout, blk, VOUT, X);
+}
+
+void vtx_seq_(const int *nin, const int *nout, const int *blk, const double *VOUT, double *X)
+{
+    vtx_(nin, nout, blk, VOUT, X);
+}
+
+static void hosbdiag_host(int bjmax, double bjtol, int blk, int mak, int ndk, double *HOSB, double *VOSB,
+                          double *EIG)
+{
+    scalit_ctx *c = scratch();
+    if (!c) return;
+    const i64 nh = (i64)ndk * mak * mak * blk, nv = (i64)mak * mak * blk, ne = (i64)ndk * mak * blk;
+    Scoped sb(c->stream);
+    double *dH = sb.get<double>(nh), *dV = sb.get<double>(nv), *dE = sb.get<double>(ne);
+    if (!dH || !dV || !dE) { report("hosbdiag", SCALIT_ENOMEM); return; }
+    cudaMemcpyAsync(dH, HOSB, sizeof(double) * nh, cudaMemcpyHostToDevice, c->stream);
+    double stats[5];
+    int rc = hosbdiag_device(c, bjmax, bjtol, blk, mak, ndk, dH, dV, dE, stats, c->stream);
+    if (rc) { report("hosbdiag", rc); return; }
+    cudaMemcpyAsync(HOSB, dH, sizeof(double) * nh, cudaMemcpyDeviceToHost, c->stream);
+    cudaMemcpyAsync(VOSB, dV, sizeof(double) * nv, cudaMemcpyDeviceToHost, c->stream);
+    cudaMemcpyAsync(EIG, dE, sizeof(double) * ne, cudaMemcpyDeviceToHost, c->stream);
+    cudaStreamSynchronize(c->stream);
+    // the reference's summary lines (hosbdiag.f90:67-71)
+    printf(" Aver. # of Sweeps:%10.5f.    Aver. OffDiag/Diag:%10.6f\n", stats[4] / blk, stats[2] / stats[4]);
+    printf(" Jacobi Effi: Min:%10.5f,   Max:%10.5f,  Mean:%10.5f\n", stats[0], stats[1], stats[2] / blk);
+}
+
+void hosbdiag_(const int *bjmax, const double *bjtol, const int *blk, const int *mak, const int *ndk,
+               double *HOSB, double *VOSB, double *EIGVAL)
+{
+    hosbdiag_host(*bjmax, *bjtol, *blk, *mak, *ndk, HOSB, VOSB, EIGVAL);
+}
+
+void hosbdiag_seq_(const int *bjmax, const double *bjtol, const int *blk, const int *mak, const int *ndk,
+                   double *HOSB, double *VOSB, double *EIGVAL, const int *id)
+{
+    (void)id;
+    hosbdiag_host(*bjmax, *bjtol, *blk, *mak, *ndk, HOSB, VOSB, EIGVAL);
+}
+
+static double dot_host(int n, const double *X, const double *Y, int *ierr)
+{
+    if (ierr) *ierr = 0;
+    scalit_ctx *c = scratch();
+    if (!c || n <= 0) { if (ierr && n > 0) *ierr = 1; return 0.0; }
+    Scoped sb(c->stream);
+    double *dX = sb.get<double>(n), *dY = (Y == X) ? dX : sb.get<double>(n), *dr = sb.get<double>(1);
+    if (!dX || !dY || !dr) { if (ierr) *ierr = 1; return 0.0; }
+    cudaMemcpyAsync(dX, X, sizeof(double) * n, cudaMemcpyHostToDevice, c->stream);
+    if (Y != X) cudaMemcpyAsync(dY, Y, sizeof(double) * n, cudaMemcpyHostToDevice, c->stream);
+    double r = 0.0;
+    if (dot_dev<double>(c, n, dX, dY, dr, c->stream) || sync_read_doubles(c, dr, &r, 1)) {
+        if (ierr) *ierr = 1;
+        return 0.0;
+    }
+    return r;
+}
+
+double norm_mpi_(const int *comm, const int *nin, const double *X, int *ierr)
+{
+    (void)comm;
+    return sqrt(dot_host(*nin, X, X, ierr));
+}
+
+double dotprod_mpi_(const int *comm, const int *nin, const double *X, const double *Y, int *ierr)
+{
+    (void)comm;
+    return dot_host(*nin, X, Y, ierr);
+}
+
+static int mgs_host(int n, const double *WJ, int m, double *VJ)
+{
+    // One-step modified Gram-Schmidt of WJ against VJ(:, 1:m) into VJ(:, m+1).
+    scalit_ctx *c = scratch();
+    if (!c) return 0;
+    Scoped sb(c->stream);
+    const i64 total = (i64)n * (m + 1);
+    double *dV = sb.get<double>(total), *dd = sb.get<double>(m + 2);
+    if (!dV || !dd) return 0;
+    if (m > 0) cudaMemcpyAsync(dV, VJ, sizeof(double) * (size_t)n * m, cudaMemcpyHostToDevice, c->stream);
+    cudaMemcpyAsync(dV + (i64)n * m, WJ, sizeof(double) * n, cudaMemcpyHostToDevice, c->stream);
+    double *v = dV + (i64)n * m;
+    double nrm2 = 0.0;
+    if (dot_dev<double>(c, n, v, v, dd + m, c->stream) || sync_read_doubles(c, dd + m, &nrm2, 1)) return 0;
+    if (nrm2 == 0.0) return 0;
+    // Projections one vector at a time in the reference's order.
+    for (int i = 0; i < m; ++i) {
+        const double *u = dV + (i64)n * i;
+        double d = 0.0;
+        if (dot_dev<double>(c, n, v, u, dd + i, c->stream) || sync_read_doubles(c, dd + i, &d, 1)) return 0;
+        if (axpy_dev(n, -d, u, v, c->stream)) return 0;   // v -= d u
+    }
+    double nv = 0.0;
+    if (dot_dev<double>(c, n, v, v, dd + m + 1, c->stream) || sync_read_doubles(c, dd + m + 1, &nv, 1)) return 0;
+    if (nv == 0.0) return 0;
+    if (scal_dev(n, 1.0 / sqrt(nv), v, c->stream)) return 0;
+    cudaMemcpyAsync(VJ + (i64)n * m, v, sizeof(double) * n, cudaMemcpyDeviceToHost, c->stream);
+    cudaStreamSynchronize(c->stream);
+    return 1;
+}
+
+int mgs_orth_(const int *n, const double *WJ, const int *m, double *VJ)
+{
+    std::lock_guard<std::mutex> lk(g_fmu);
+    return mgs_host(*n, WJ, *m, VJ);
+}
+
+int mgs_orth_mpi_(const int *n, const double *WJ, const int *m, double *VJ, int *ierr)
+{
+    if (ierr) *ierr = 0;
+    std::lock_guard<std::mutex> lk(g_fmu);
+    return mgs_host(*n, WJ, *m, VJ);
+}
+
+int qmr_(const int *ntype, const int *qmrmax, const double *qmrtol, const int *n, const double *B,
+         scalit_fortran_op hx, scalit_fortran_op px, double *X, double *RES)
+{
+    return qmr_fortran(*ntype, *qmrmax, *qmrtol, *n, B, hx, px, X, RES, false);
+}
+
+int qmr_mpi_(const int *ntype, const int *qmrmax, const double *qmrtol, const int *n, const double *B,
+             scalit_fortran_op hx, scalit_fortran_op px, double *X, double *RES, const int *myid)
+{
+    (void)myid;
+    return qmr_fortran(*ntype, *qmrmax, *qmrtol, *n, B, hx, px, X, RES, true);
+}
+
+int pist_conv_(const double *e0, const double *etol, const int *ntype, const int *n, const double *X,
+               const int *startcnt, const int *stepcnt, const int *stepeig, const int *m, const int *m_max,
+               scalit_fortran_op h0x, scalit_fortran_linsolv linsolv, double *EIG, double *RES)
+{
+    return pist_fortran(*e0, *etol, *ntype, *n, X, *startcnt, *stepcnt, *stepeig, *m, *m_max, h0x, linsolv,
+                        EIG, RES);
+}
+
+int pist_conv_mpi_(const int *myid, const int *rootid, const double *e0, const double *etol, const int *ntype,
+                   const int *n, const double *X, const int *startcnt, const int *stepcnt, const int *stepeig,
+                   const int *m, const int *m_max, scalit_fortran_op h0x, scalit_fortran_linsolv linsolv,
+                   double *EIG, double *RES)
+{
+    (void)myid; (void)rootid;
+    return pist_fortran(*e0, *etol, *ntype, *n, X, *startcnt, *stepcnt, *stepeig, *m, *m_max, h0x, linsolv,
+                        EIG, RES);
+}
+
+void scalit_fortran_device_(const int *device)
+{
+    std::lock_guard<std::mutex> lk(g_fmu);
+    g_fdev = *device;
+}
+
+void scalit_fortran_init_(const int *sf, const int *sn, const int *sdep, const double *H0, const double *RES,
+                          const double *DEP, const double *e0, int *ierr)
+{
+    std::lock_guard<std::mutex> lk(g_fmu);
+    if (g_fctx) { scalit_destroy(g_fctx); g_fctx = nullptr; }
+    int dep[SCALIT_FMAX] = {};
+    for (int i = 0; i < *sf && i < SCALIT_FMAX; ++i) dep[i] = sdep[i] != 0;
+    int rc = scalit_create(&g_fctx, *sf, sn, dep, 0, g_fdev);
+    if (!rc) rc = scalit_load(g_fctx, H0, RES, DEP, nullptr);
+    if (!rc) rc = scalit_set_shift(g_fctx, *e0);
+    if (rc) { report("scalit_fortran_init", rc); if (g_fctx) { scalit_destroy(g_fctx); g_fctx = nullptr; } }
+    if (ierr) *ierr = rc;
+}
+
+void scalit_fortran_precond_(const int *sosb, const double *de, const double *beta, const int *bjmax,
+                             const double *bjtol, int *ierr)
+{
+    std::lock_guard<std::mutex> lk(g_fmu);
+    int rc = g_fctx ? scalit_set_precond(g_fctx, *sosb, *de, *beta) : SCALIT_ESTATE;
+    if (!rc) rc = scalit_build_osb(g_fctx, *bjmax, *bjtol, nullptr);
+    if (rc) report("scalit_fortran_precond", rc);
+    if (ierr) *ierr = rc;
+}
+
+void scalit_fortran_qmr_param_(const int *ntype, const int *qmrmax, const double *qmrtol, const int *precision)
+{
+    std::lock_guard<std::mutex> lk(g_fmu);
+    g_fq.ntype = *ntype;
+    g_fq.qmrmax = *qmrmax;
+    g_fq.tol = *qmrtol;
+    g_fq.precision = *precision;
+}
+
+void scalit_fortran_final_(void)
+{
+    std::lock_guard<std::mutex> lk(g_fmu);
+    if (g_fctx) { scalit_destroy(g_fctx); g_fctx = nullptr; }
+    if (g_scratch) { scalit_destroy(g_scratch); g_scratch = nullptr; }
+}
+
+void scalit_hx0_(const int *n, const double *X, double *Y)
+{
+    if (!g_fctx || g_fctx->L.N != *n) { fprintf(stderr, "scalit_gb300: scalit_hx0 without a matching scalit_fortran_init\n"); return; }
+    report("scalit_hx0", scalit_hx(g_fctx, SCALIT_TA0, 1, X, Y));
+}
+
+void scalit_ehx_(const int *n, const double *X, double *Y)
+{
+    if (!g_fctx || g_fctx->L.N != *n) { fprintf(stderr, "scalit_gb300: scalit_ehx without a matching scalit_fortran_init\n"); return; }
+    report("scalit_ehx", scalit_hx(g_fctx, SCALIT_TA1, 1, X, Y));
+}
+
+void scalit_epx_(const int *n, const double *X, double *Y)
+{
+    if (!g_fctx || g_fctx->L.N != *n) { fprintf(stderr, "scalit_gb300: scalit_epx without a matching scalit_fortran_init\n"); return; }
+    report("scalit_epx", scalit_px(g_fctx, SCALIT_TA1, 1, X, Y));
+}
+
+int scalit_osb_qmr_(const int *n, const double *B, double *X, double *ERES)
+{
+    if (!g_fctx || g_fctx->L.N != *n) { fprintf(stderr, "scalit_gb300: scalit_osb_qmr without a matching scalit_fortran_init\n"); return -10; }
+    int iters = 0;
+    int code = scalit_qmr(g_fctx, g_fq.ntype, g_fq.qmrmax, g_fq.tol, g_fq.precision, B, X, ERES, &iters);
+    if (code < -100) { report("scalit_osb_qmr", code); return -10; }
+    return code;
+}
+
+}  // extern "C"

@@ -1,0 +1,308 @@
+// Per-level contractions of the H*X product and of the preconditioner
+// rotations, as one strided tiled GEMM kernel.
+//
+// Every level of MYHX (src/iterate/module/osb.hx.h:71-110) is a GEMM once the
+// grid vector is viewed through the level's strides:
+//   level with nin == 1   : Y(i, b)        = sum_j H(i, j) X(j, b)          (H1X, nin = 1)
+//   level with nin  > 1   : Y(a, i, b)     = s(a) sum_j H(i, j) X(a, j, b)   (H1X / H2X)
+// The first is C = H * X (M = nout, N = blk), the second folds (a, b) into M
+// (M = nin*blk, N = nout) with H^T as the B operand.  The diagonal potential
+// term of MYHX is fused into the epilogue of the first level.
+//
+// FP64 tiles are 64x64x16 with 4x4 outputs per thread, FP32 tiles 128x128x8
+// with 8x8 outputs per thread; A and B tiles are staged k-major in shared
+// memory with a register prefetch of the next K slab.
+#include "internal.cuh"
+
+namespace sc {
+
+template <class T> struct Tile;
+template <> struct Tile<double> { static constexpr int BM = 64, BN = 64, BK = 16, TM = 4, TN = 4; };
+template <> struct Tile<float> { static constexpr int BM = 128, BN = 128, BK = 8, TM = 8, TN = 8; };
+
+template <class T>
+__global__ void __launch_bounds__(256)
+gemm_kernel(GemmArgs<T> g)
+{
+    using TL = Tile<T>;
+    constexpr int BM = TL::BM, BN = TL::BN, BK = TL::BK, TM = TL::TM, TN = TL::TN;
+    constexpr int NT = 256;
+    constexpr int A_PER = BM * BK / NT;   // A elements each thread loads per slab
+    constexpr int B_PER = BN * BK / NT;
+    static_assert((BM / TM) * (BN / TN) == NT, "thread grid");
+
+    if (g.gate && *g.gate) return;
+
+    __shared__ T As[BK][BM];
+    __shared__ T Bs[BK][BN];
+
+    const int tid = threadIdx.x;
+    const int m0 = blockIdx.x * BM;
+    const int n0 = blockIdx.y * BN;
+    const int z = blockIdx.z;
+    const T *A = g.A + (i64)z * g.a_sz;
+    const T *B = g.B + (i64)z * g.b_sz;
+    T *Cp = g.C + (i64)z * g.c_sz;
+
+    // Loader mapping.  A: consecutive threads take consecutive m (coalesced
+    // along the contiguous grid axis).  B: consecutive threads take
+    // consecutive n when B's n-stride is 1, else consecutive k.
+    const bool b_n_fast = (g.b_sn == 1);
+    i64 a_moff[A_PER];
+    int a_m[A_PER], a_k[A_PER];
+    #pragma unroll
+    for (int r = 0; r < A_PER; ++r) {
+        const int e = tid + r * NT;
+        a_m[r] = e % BM;
+        a_k[r] = e / BM;
+        const int m = m0 + a_m[r];
+        a_moff[r] = (m < g.M) ? ((i64)(m % g.Mi) * g.s1 + (i64)(m / g.Mi) * g.s2) : -1;
+    }
+    int b_n[B_PER], b_k[B_PER];
+    #pragma unroll
+    for (int r = 0; r < B_PER; ++r) {
+        const int e = tid + r * NT;
+        if (b_n_fast) { b_n[r] = e % BN; b_k[r] = e / BN; }
+        else { b_k[r] = e % BK; b_n[r] = e / BK; }
+    }
+
+    T ra[A_PER], rb[B_PER];
+    auto load = [&](int k0) {
+        #pragma unroll
+        for (int r = 0; r < A_PER; ++r) {
+            const int k = k0 + a_k[r];
+            ra[r] = (a_moff[r] >= 0 && k < g.K) ? A[a_moff[r] + (i64)k * g.a_sk] : T(0);
+        }
+        #pragma unroll
+        for (int r = 0; r < B_PER; ++r) {
+            const int k = k0 + b_k[r], n = n0 + b_n[r];
+            rb[r] = (k < g.K && n < g.N) ? B[(i64)k * g.b_sk + (i64)n * g.b_sn] : T(0);
+        }
+    };
+    auto store = [&]() {
+        #pragma unroll
+        for (int r = 0; r < A_PER; ++r) As[a_k[r]][a_m[r]] = ra[r];
+        #pragma unroll
+        for (int r = 0; r < B_PER; ++r) Bs[b_k[r]][b_n[r]] = rb[r];
+    };
+
+    const int tm = (tid % (BM / TM)) * TM;   // this thread's rows within the tile
+    const int tn = (tid / (BM / TM)) * TN;   // this thread's columns
+    T acc[TM][TN];
+    #pragma unroll
+    for (int i = 0; i < TM; ++i)
+        #pragma unroll
+        for (int j = 0; j < TN; ++j) acc[i][j] = T(0);
+
+    load(0);
+    for (int k0 = 0; k0 < g.K; k0 += BK) {
+        __syncthreads();
+        store();
+        __syncthreads();
+        if (k0 + BK < g.K) load(k0 + BK);
+        #pragma unroll
+        for (int kk = 0; kk < BK; ++kk) {
+            T av[TM], bv[TN];
+            #pragma unroll
+            for (int i = 0; i < TM; ++i) av[i] = As[kk][tm + i];
+            #pragma unroll
+            for (int j = 0; j < TN; ++j) bv[j] = Bs[kk][tn + j];
+            #pragma unroll
+            for (int i = 0; i < TM; ++i)
+                #pragma unroll
+                for (int j = 0; j < TN; ++j) acc[i][j] = fma(av[i], bv[j], acc[i][j]);
+        }
+    }
+
+    // Epilogue.
+    #pragma unroll
+    for (int i = 0; i < TM; ++i) {
+        const int m = m0 + tm + i;
+        if (m >= g.M) continue;
+        const i64 mi = m % g.Mi;
+        const i64 moff = mi * g.s1 + (i64)(m / g.Mi) * g.s2;
+        const T sc = g.rowscale ? g.rowscale[mi] * g.alpha : g.alpha;
+        #pragma unroll
+        for (int j = 0; j < TN; ++j) {
+            const int n = n0 + tn + j;
+            if (n >= g.N) continue;
+            const i64 p = moff + (i64)n * g.c_sn;
+            T v = sc * acc[i][j];
+            if (g.diagV) v = fma(g.alpha * (g.diagV[p] - g.shift), g.diagX[p], v);
+            if (g.accumulate) v += Cp[p];
+            Cp[p] = v;
+        }
+    }
+}
+
+template <class T> int launch_gemm(const GemmArgs<T> &g, cudaStream_t s)
+{
+    using TL = Tile<T>;
+    if (g.M <= 0 || g.N <= 0 || g.batch <= 0) return 0;
+    if (g.batch > 65535) { set_error("gemm batch %d too large", g.batch); return SCALIT_EINVAL; }
+    dim3 grid((g.M + TL::BM - 1) / TL::BM, (g.N + TL::BN - 1) / TL::BN, g.batch);
+    if (grid.y > 65535) { set_error("gemm N=%d too large", g.N); return SCALIT_EINVAL; }
+    gemm_kernel<T><<<grid, 256, 0, s>>>(g);
+    SC_CHECK_LAUNCH();
+    return 0;
+}
+
+template int launch_gemm<double>(const GemmArgs<double> &, cudaStream_t);
+template int launch_gemm<float>(const GemmArgs<float> &, cudaStream_t);
+
+// ------------------------------------------------------------------------
+// H3X (src/libutil/serial/base/matrix.f90:188-203): outermost layer given as
+// per-point matrices A(nin, nout, nout): Y(a, i) (+)= sum_j A(a, i, j) X(a, j).
+template <class T>
+__global__ void h3x_kernel(int nin, int nout, const T *__restrict__ Am, const T *__restrict__ X,
+                           T *__restrict__ Y, int accumulate, T alpha, const int *gate)
+{
+    if (gate && *gate) return;
+    const i64 total = (i64)nin * nout;
+    for (i64 e = blockIdx.x * (i64)blockDim.x + threadIdx.x; e < total;
+         e += (i64)gridDim.x * blockDim.x) {
+        const i64 a = e % nin;
+        const int i = (int)(e / nin);
+        T acc = T(0);
+        for (int j = 0; j < nout; ++j)
+            acc = fma(Am[a + (i64)nin * (i + (i64)nout * j)], X[a + (i64)nin * j], acc);
+        const T v = alpha * acc;
+        Y[e] = accumulate ? Y[e] + v : v;
+    }
+}
+
+template <class T>
+int level_apply(const scalit_ctx *c, int l, const T *H0, const T *DEP, const T *OUTH, const T *X,
+                T *Y, int accumulate, const T *diagV, T shift, T alpha, const int *gate,
+                cudaStream_t s)
+{
+    const Layout &L = c->L;
+    const int nout = L.n[l];
+    const i64 nin = L.dim[l], blk = L.blk[l];
+    if (L.ndvr && l == L.nlev - 1) {
+        // Outer per-point matrices; the diagonal term, if requested, is a
+        // separate pass (the outermost level is never the first applied).
+        if (diagV) { set_error("diagonal fused into the outer layer"); return SCALIT_EINVAL; }
+        const i64 total = nin * nout;
+        const int threads = 256;
+        const int blocks = (int)((total + threads - 1) / threads < 152 * 16 ? (total + threads - 1) / threads : 152 * 16);
+        h3x_kernel<T><<<blocks, threads, 0, s>>>((int)nin, nout, OUTH, X, Y, accumulate, alpha, gate);
+        SC_CHECK_LAUNCH();
+        return 0;
+    }
+    GemmArgs<T> g{};
+    g.K = nout;
+    g.batch = 1;
+    g.accumulate = accumulate;
+    g.alpha = alpha;
+    g.diagV = diagV;
+    g.diagX = X;
+    g.shift = shift;
+    g.gate = gate;
+    g.C = Y;
+    g.c_sz = 0; g.a_sz = 0; g.b_sz = 0;
+    const T *H = H0 + L.h0s[l];
+    if (nin == 1) {
+        // Y(i, b) = sum_j H(i, j) X(j, b): A = H (col-major), B = X.
+        g.M = nout; g.N = (int)blk;
+        g.Mi = nout; g.s1 = 1; g.s2 = 0;
+        g.A = H; g.a_sk = nout;
+        g.B = X; g.b_sk = 1; g.b_sn = nout;
+        g.c_sn = nout;
+        g.rowscale = nullptr;
+        if (blk > 65535LL * Tile<T>::BN) { set_error("level %d too many blocks", l + 1); return SCALIT_EINVAL; }
+    } else {
+        // Y(a, i, b) = s(a) sum_j X(a, j, b) H(i, j): A = X with (a, b) folded, B = H^T.
+        const i64 M = nin * blk;
+        if (M > 2147483647LL) { set_error("level %d too large", l + 1); return SCALIT_EINVAL; }
+        g.M = (int)M; g.N = nout;
+        g.Mi = nin; g.s1 = 1; g.s2 = nin * nout;
+        g.A = X; g.a_sk = nin;
+        g.B = H; g.b_sk = nout; g.b_sn = 1;
+        g.c_sn = nin;
+        g.rowscale = L.dep[l] ? DEP + L.deps[l] : nullptr;
+    }
+    return launch_gemm<T>(g, s);
+}
+
+template <class T>
+__global__ void diag_kernel(i64 n, const T *__restrict__ V, T shift, T alpha,
+                            const T *__restrict__ X, T *__restrict__ Y, int accumulate,
+                            const int *gate)
+{
+    if (gate && *gate) return;
+    for (i64 i = blockIdx.x * (i64)blockDim.x + threadIdx.x; i < n; i += (i64)gridDim.x * blockDim.x) {
+        const T v = alpha * (V[i] - shift) * X[i];
+        Y[i] = accumulate ? Y[i] + v : v;
+    }
+}
+
+template <class T> static const T *pick(const scalit_ctx *c, const double *d, const float *f);
+template <> const double *pick<double>(const scalit_ctx *, const double *d, const float *) { return d; }
+template <> const float *pick<float>(const scalit_ctx *, const double *, const float *f) { return f; }
+
+template <class T>
+int hx_vec(const scalit_ctx *c, const T *X, T *Y, T shift, T alpha, const int *gate, cudaStream_t s)
+{
+    const Layout &L = c->L;
+    const T *H0 = pick<T>(c, c->H0, c->H0f);
+    const T *RES = pick<T>(c, c->RES, c->RESf);
+    const T *DEP = pick<T>(c, c->DEP, c->DEPf);
+    const T *OUTH = pick<T>(c, c->OUTH, c->OUTHf);
+    int rc;
+    int first = 0;
+    if (L.ndvr && L.nlev == 1) {
+        const int threads = 256;
+        diag_kernel<T><<<(int)((L.N + threads - 1) / threads), threads, 0, s>>>(L.N, RES, shift, alpha, X, Y, 0, gate);
+        SC_CHECK_LAUNCH();
+        first = 1;
+    }
+    for (int l = 0; l < L.nlev; ++l) {
+        const bool fuse_diag = (l == 0 && !first);
+        rc = level_apply<T>(c, l, H0, DEP, OUTH, X, Y, /*accumulate=*/l > 0 || first,
+                            fuse_diag ? RES : nullptr, shift, alpha, gate, s);
+        if (rc) return rc;
+    }
+    return 0;
+}
+
+template int hx_vec<double>(const scalit_ctx *, const double *, double *, double, double, const int *, cudaStream_t);
+template int hx_vec<float>(const scalit_ctx *, const float *, float *, float, float, const int *, cudaStream_t);
+template int level_apply<double>(const scalit_ctx *, int, const double *, const double *, const double *, const double *, double *, int, const double *, double, double, const int *, cudaStream_t);
+template int level_apply<float>(const scalit_ctx *, int, const float *, const float *, const float *, const float *, float *, int, const float *, float, float, const int *, cudaStream_t);
+
+// ------------------------------------------------------------------------
+// VX / VTX (src/iterate/libiterate/hpx/hpx.f90:40-73) out of place:
+// Y(:, i, b) = sum_j V(i, j, b) X(:, j, b)  (VX)   or  sum_j V(j, i, b) X(:, j, b)  (VTX).
+template <class T>
+int bgemv(int nout, int blk, const T *V, const T *X, T *Y, int transpose, const int *gate,
+          cudaStream_t s);
+
+template <class T>
+int level_rotate(int nin, int nout, int blk, const T *V, const T *X, T *Y, int transpose,
+                 const int *gate, cudaStream_t s)
+{
+    GemmArgs<T> g{};
+    g.K = nout;
+    g.accumulate = 0;
+    g.alpha = T(1);
+    g.gate = gate;
+    g.rowscale = nullptr;
+    g.diagV = nullptr;
+    g.C = Y;
+    if (nin == 1) return bgemv(nout, blk, V, X, Y, transpose, gate, s);
+    // per block b: Y_b(a, i) = sum_j X_b(a, j) V_b(i, j)  -> A = X_b, B = V_b^T (VX) or V_b (VTX)
+    g.M = nin; g.N = nout; g.batch = blk;
+    g.Mi = nin; g.s1 = 1; g.s2 = 0;
+    g.A = X; g.a_sk = nin; g.a_sz = (i64)nin * nout;
+    g.B = V; g.b_sz = (i64)nout * nout;
+    if (!transpose) { g.b_sk = nout; g.b_sn = 1; }
+    else { g.b_sk = 1; g.b_sn = nout; }
+    g.c_sn = nin; g.c_sz = (i64)nin * nout;
+    return launch_gemm<T>(g, s);
+}
+
+template int level_rotate<double>(int, int, int, const double *, const double *, double *, int, const int *, cudaStream_t);
+template int level_rotate<float>(int, int, int, const float *, const float *, float *, int, const int *, cudaStream_t);
+
+}  // namespace sc

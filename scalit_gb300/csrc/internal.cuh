@@ -1,0 +1,175 @@
+// Internal declarations shared by the translation units of libscalit_gb300.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <cstdint>
+#include <cstdio>
+#include <string>
+
+#include "../../include/scalit_gb300.h"
+
+typedef long long i64;
+
+namespace sc {
+
+// ------------------------------------------------------------------ errors --
+void set_error(const char *fmt, ...);
+int cuda_fail(cudaError_t e, const char *what, const char *file, int line);
+
+#define SC_CUDA(call)                                                         \
+    do {                                                                      \
+        cudaError_t _e = (call);                                              \
+        if (_e != cudaSuccess) return sc::cuda_fail(_e, #call, __FILE__, __LINE__); \
+    } while (0)
+
+#define SC_CHECK_LAUNCH() SC_CUDA(cudaGetLastError())
+
+// ------------------------------------------------------------------ layout --
+// calOSB (src/iterate/module/osb.init.h:2-49): per-level dimensions and the
+// start offsets of each level inside the concatenated H0 / DEP / VOSB arrays.
+struct Layout {
+    int nlev = 0;
+    int n[SCALIT_FMAX] = {};
+    int dep[SCALIT_FMAX] = {};
+    int ndvr = 0;
+    i64 dim[SCALIT_FMAX] = {};  // myDim: product of the faster levels' sizes
+    i64 blk[SCALIT_FMAX] = {};  // myBlk: product of the slower levels' sizes
+    i64 h0s[SCALIT_FMAX] = {};  // start of level l in H0
+    i64 deps[SCALIT_FMAX] = {}; // start of level l in DEP
+    i64 vs[SCALIT_FMAX] = {};   // start of level l in VOSB
+    i64 N = 0, h0len = 0, deplen = 0, vlen = 0, outhlen = 0;
+    void compute();
+};
+
+// Device vector with FP64 master and optional FP32 shadow.
+template <class T> struct DevBuf {
+    T *p = nullptr;
+    i64 n = 0;
+};
+
+}  // namespace sc
+
+// The opaque context of the C ABI.
+struct scalit_ctx {
+    sc::Layout L;
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    cudaStream_t own_stream = nullptr;   // the context's own stream while a caller's is set
+    // FP64 operator data (module globals H0/RES/DEP/OUTH/EIG0/VOSB in the reference)
+    double *H0 = nullptr, *RES = nullptr, *DEP = nullptr, *OUTH = nullptr;
+    double *EIG0 = nullptr, *VOSB = nullptr;
+    // FP32 shadows for the mixed-precision inner solves
+    float *H0f = nullptr, *RESf = nullptr, *DEPf = nullptr, *OUTHf = nullptr;
+    float *EIG0f = nullptr, *VOSBf = nullptr;
+    bool loaded = false, osb_built = false;
+    double E0 = 0.0;
+    int osb_kind = SCALIT_TOSB;
+    double osb_de = 0.0, osb_beta = 0.0;
+    // workspace (grown on demand)
+    void *work = nullptr;
+    size_t work_bytes = 0;
+    // reduction scratch: partial sums and a completion counter
+    double *red_partial = nullptr;
+    unsigned int *red_counter = nullptr;
+    double *red_result = nullptr;   // device scalars of the last reductions
+    double *h_pinned = nullptr;     // pinned host mirror for scalar readback
+    void *cusolver = nullptr;       // cusolverDnHandle_t
+};
+
+namespace sc {
+
+// Workspace: returns a device pointer with at least `bytes` bytes.
+int work_get(scalit_ctx *c, size_t bytes, void **out);
+
+// ----------------------------------------------------- contraction kernels --
+// C[m, n] (+)= rowscale[m % Mi] * sum_k A[m, k] * B[k, n]  with
+//   A(m,k) = A + moff(m) + k*a_sk,  B(k,n) = B + k*b_sk + n*b_sn,
+//   C(m,n) = C + moff(m) + n*c_sn,  moff(m) = (m % Mi)*s1 + (m / Mi)*s2,
+// per batch z: A += z*a_sz, B += z*b_sz, C += z*c_sz.
+// Epilogue: out = (accumulate ? C : 0) + alpha*scale*acc
+//           + (diagV ? (diagV[p] - shift) * diagX[p] : 0) with p = C offset.
+template <class T> struct GemmArgs {
+    int M, N, K, batch;
+    i64 Mi, s1, s2;
+    const T *A; i64 a_sk, a_sz;
+    const T *B; i64 b_sk, b_sn, b_sz;
+    T *C; i64 c_sn, c_sz;
+    const T *rowscale;     // may be null
+    int accumulate;
+    T alpha;
+    const T *diagV;        // may be null
+    const T *diagX;
+    T shift;
+    const int *gate;       // if non-null and *gate != 0 the kernel does nothing
+};
+
+template <class T> int launch_gemm(const GemmArgs<T> &g, cudaStream_t s);
+
+// One level of MYHX: out (+)= H_level X (dependent levels scaled by DEP).
+template <class T>
+int level_apply(const scalit_ctx *c, int level, const T *H0, const T *DEP, const T *OUTH,
+                const T *X, T *Y, int accumulate, const T *diagV, T shift, T alpha,
+                const int *gate, cudaStream_t s);
+
+// Whole operator for one vector: Y = alpha * ((V - shift) X + sum_l H_l X).
+template <class T>
+int hx_vec(const scalit_ctx *c, const T *X, T *Y, T shift, T alpha, const int *gate,
+           cudaStream_t s);
+
+// Whole preconditioner for one vector: Y = alpha * V K^-1 V^T X.  tmp: N elements.
+template <class T>
+int px_vec(const scalit_ctx *c, int npc, const T *X, T *Y, T *tmp, T alpha, const int *gate,
+           cudaStream_t s);
+
+// Generic per-level rotation (VX / VTX) on device arrays, out of place.
+template <class T>
+int level_rotate(int nin, int nout, int blk, const T *V, const T *X, T *Y, int transpose,
+                 const int *gate, cudaStream_t s);
+
+// ------------------------------------------------------------- OSB build --
+int osb_build(scalit_ctx *c, int bjmax, double bjtol, double *stats);
+// HosbDiag on a device HOSB(ndk, mak, mak, blk): fills VOSB and EIGVAL.
+int hosbdiag_device(scalit_ctx *c, int bjmax, double bjtol, int blk, int mak, int ndk,
+                    double *HOSB, double *VOSB, double *EIG, double *stats5, cudaStream_t s);
+
+// ------------------------------------------------------------ vector ops --
+// Deterministic FP64-accumulated dot product; writes the result to *out (device).
+template <class T>
+int dot_dev(scalit_ctx *c, i64 n, const T *x, const T *y, double *out, cudaStream_t s);
+int sync_read_doubles(scalit_ctx *c, const double *dsrc, double *host, int count);
+
+int axpy_dev(i64 n, double a, const double *x, double *y, cudaStream_t s);
+int scal_dev(i64 n, double a, double *x, cudaStream_t s);
+
+// Convert between precisions.
+int to_f32(const double *x, float *y, i64 n, cudaStream_t s);
+int to_f64(const float *x, double *y, i64 n, cudaStream_t s);
+
+// ------------------------------------------------------------------ QMR --
+struct QmrResult { int code; double res; int iters; int breakdown; };
+// Operator pair of a QMR solve.  hx/px write `out` from `in` on the context's
+// stream; device operators honour `gate` (skip when *gate != 0).
+template <class T> struct QmrOps {
+    virtual ~QmrOps() {}
+    virtual int hx(const T *in, T *out, const int *gate) = 0;
+    virtual int px(const T *in, T *out, const int *gate) = 0;
+    virtual bool host_side() const { return false; }
+};
+template <class T>
+int qmr_core(scalit_ctx *c, i64 n, QmrOps<T> &ops, int ntype, int qmrmax, double qmrtol,
+             const T *dB, T *dX, QmrResult *out);
+int qmr_run(scalit_ctx *c, int ntype, int qmrmax, double qmrtol, int precision,
+            const double *dB, double *dX, QmrResult *out);
+
+// ----------------------------------------------------------------- PIST --
+struct PistOps {
+    virtual ~PistOps() {}
+    virtual int h0x(const double *dX, double *dY) = 0;                  // H * x
+    virtual int linsolv(const double *dB, double *dX, int *num) = 0;   // (H - E0) x = b
+};
+int pist_core(scalit_ctx *c, i64 N, const scalit_pist_params *p, const double *dx0, PistOps &ops,
+              double *eig, double *res, scalit_pist_info *info);
+int pist_ctx(scalit_ctx *c, const scalit_pist_params *p, const double *dx0, double *eig,
+             double *res, scalit_pist_info *info);
+
+}  // namespace sc

@@ -1,0 +1,392 @@
+// PIST eigensolver on the device (PIST_CONV, src/iterate/libiterate/pist/pist.f90:7-98;
+// pistH0, pistHij.f90:70-125; MGS_ORTH, src/iterate/libiterate/orth/gsorth.f90:42-72;
+// window and convergence helpers, src/libutil/serial/base/util.f90:84-149,656-716).
+//
+// The Krylov basis VJ(N, M_MAX) and HMAT(M_MAX, M_MAX) stay in HBM in FP64.
+// Modified Gram-Schmidt keeps the reference's order: one fused launch per
+// previous vector applies the last projection and computes the next
+// coefficient (v -= d_{i-1} u_{i-1}; d_i = v . u_i), so the vector being
+// orthogonalised stays L2-resident and each basis vector is streamed once.
+// HMAT columns come from one FP64 H*X and one GEMV-T per new vector; the Ritz
+// values of the leading num x num block are computed by cuSOLVER's symmetric
+// eigensolver (the reference calls LAPACK DSYEV at the same point); window
+// selection and the convergence test run on the host over those few numbers.
+#include "internal.cuh"
+
+#include <cusolverDn.h>
+
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstdio>
+#include <vector>
+
+namespace sc {
+
+static constexpr int kT = 256;
+
+struct MgsState { unsigned int counter; int pad; };
+
+__device__ __forceinline__ bool last_block(double (&acc)[1], double *partial, unsigned int *counter)
+{
+    __shared__ double red[kT / 32];
+    __shared__ bool last;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    double a = acc[0];
+    #pragma unroll
+    for (int o = 16; o > 0; o >>= 1) a += __shfl_xor_sync(0xffffffffu, a, o);
+    if (lane == 0) red[warp] = a;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double s = 0.0;
+        for (int w = 0; w < kT / 32; ++w) s += red[w];
+        partial[blockIdx.x] = s;
+        __threadfence();
+        last = (atomicAdd(counter, 1u) == gridDim.x - 1);
+    }
+    __syncthreads();
+    return last;
+}
+
+// v -= dprev * uprev (when uprev != null); d[i] = v . u (when u != null).
+__global__ void __launch_bounds__(kT)
+mgs_kernel(i64 n, double *v, const double *uprev, const double *dprev, const double *u,
+           double *dout, double *partial, unsigned int *counter)
+{
+    const double dp = uprev ? *dprev : 0.0;
+    double acc[1] = {0.0};
+    for (i64 k = blockIdx.x * (i64)blockDim.x + threadIdx.x; k < n; k += (i64)gridDim.x * blockDim.x) {
+        double x = v[k];
+        if (uprev) { x = x - dp * uprev[k]; v[k] = x; }
+        const double y = u ? u[k] : x;
+        acc[0] = fma(x, y, acc[0]);
+    }
+    if (last_block(acc, partial, counter) && threadIdx.x == 0) {
+        *counter = 0;
+        double s = 0.0;
+        for (unsigned int b = 0; b < gridDim.x; ++b) s += partial[b];
+        *dout = s;
+    }
+}
+
+// v = v / sqrt(*nrm2) when nonzero.
+__global__ void scale_inv_sqrt_kernel(i64 n, double *v, const double *nrm2)
+{
+    const double s = sqrt(*nrm2);
+    if (s == 0.0) return;
+    for (i64 k = blockIdx.x * (i64)blockDim.x + threadIdx.x; k < n; k += (i64)gridDim.x * blockDim.x)
+        v[k] = v[k] / s;
+}
+
+__global__ void copy_scaled_kernel(i64 n, const double *x, double *y, const double *nrm2)
+{
+    const double s = sqrt(*nrm2);
+    for (i64 k = blockIdx.x * (i64)blockDim.x + threadIdx.x; k < n; k += (i64)gridDim.x * blockDim.x)
+        y[k] = x[k] / s;
+}
+
+// partial[I][chunk] = sum over the chunk of VJ(:, I) * w; then reduced in order.
+static constexpr int kGemvChunk = 8192;
+__global__ void __launch_bounds__(kT)
+gemvt_partial_kernel(i64 n, int m, const double *VJ, const double *w, double *partial, int nchunk)
+{
+    const int I = blockIdx.y;
+    const i64 k0 = (i64)blockIdx.x * kGemvChunk;
+    const i64 k1 = min(n, k0 + kGemvChunk);
+    const double *u = VJ + (i64)I * n;
+    double a = 0.0;
+    for (i64 k = k0 + threadIdx.x; k < k1; k += blockDim.x) a = fma(u[k], w[k], a);
+    __shared__ double red[kT / 32];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    #pragma unroll
+    for (int o = 16; o > 0; o >>= 1) a += __shfl_xor_sync(0xffffffffu, a, o);
+    if (lane == 0) red[warp] = a;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double s = 0.0;
+        for (int w2 = 0; w2 < kT / 32; ++w2) s += red[w2];
+        partial[(i64)I * nchunk + blockIdx.x] = s;
+    }
+    (void)m;
+}
+
+__global__ void gemvt_final_kernel(int m, int nchunk, const double *partial, double *HMAT, int ld,
+                                   int J)
+{
+    const int I = blockIdx.x * blockDim.x + threadIdx.x;
+    if (I >= m) return;
+    double s = 0.0;
+    for (int c = 0; c < nchunk; ++c) s += partial[(i64)I * nchunk + c];
+    HMAT[I + (i64)ld * J] = s;   // HMAT(I, J)
+    HMAT[J + (i64)ld * I] = s;   // HMAT(J, I)
+}
+
+// A (num x num, lda num) = symmetric matrix from the upper triangle of HMAT.
+__global__ void gather_upper_kernel(int num, const double *HMAT, int ld, double *A)
+{
+    const i64 total = (i64)num * num;
+    for (i64 e = blockIdx.x * (i64)blockDim.x + threadIdx.x; e < total; e += (i64)gridDim.x * blockDim.x) {
+        const int r = (int)(e % num), c = (int)(e / num);
+        A[e] = (r <= c) ? HMAT[r + (i64)ld * c] : HMAT[c + (i64)ld * r];
+    }
+}
+
+static int egrid(i64 n)
+{
+    i64 g = (n + kT * 4 - 1) / (kT * 4);
+    if (g > 152 * 4) g = 152 * 4;
+    if (g < 1) g = 1;
+    return (int)g;
+}
+
+// ------------------------------------------------------- host helpers --
+// getWindow0 (util.f90:669-716): M values nearest E0, chosen one at a time,
+// ties resolved to the lowest index (strict '>' comparison).
+static void get_window(double E0, const std::vector<double> &vec, int n, int M, double *out)
+{
+    if (n < M) {
+        for (int i = 0; i < n; ++i) out[i] = vec[i];
+        for (int i = n; i < M; ++i) out[i] = vec[n - 1];
+        return;
+    }
+    std::vector<char> label(n, 1);
+    for (int i = 0; i < M; ++i) {
+        int idx = -1;
+        double v0 = 0.0;
+        for (int j = 0; j < n; ++j) {
+            if (!label[j]) continue;
+            const double a = fabs(vec[j] - E0);
+            if (idx < 0 || v0 > a) { idx = j; v0 = a; }
+        }
+        out[i] = vec[idx];
+        label[idx] = 0;
+    }
+}
+
+static double diff_max(const double *a, const double *b, int n)
+{
+    double m = fabs(a[0] - b[0]);
+    for (int i = 1; i < n; ++i) m = std::max(m, fabs(a[i] - b[i]));
+    return m;
+}
+
+static double sep_max(const double *v1, int n1, const std::vector<double> &v2, int n2)
+{
+    double g = 0.0;
+    for (int i = 0; i < n1; ++i) {
+        double mm = fabs(v1[i] - v2[0]);
+        for (int j = 1; j < n2; ++j) mm = std::min(mm, fabs(v1[i] - v2[j]));
+        g = (i == 0) ? mm : std::max(g, mm);
+    }
+    return g;
+}
+
+static double now()
+{
+    return std::chrono::duration<double>(std::chrono::steady_clock::now().time_since_epoch()).count();
+}
+
+int pist_core(scalit_ctx *c, i64 N, const scalit_pist_params *p, const double *dx0, PistOps &ops,
+              double *eig, double *res, scalit_pist_info *info)
+{
+    cudaStream_t s = c->stream;
+    const int M = p->m, MM = p->m_max;
+    scalit_pist_info inf{};
+    *res = 0.0;
+    if (p->stepeig >= MM || p->startcnt > MM || M > MM || M < 1) {
+        if (info) *info = inf;
+        return 0;
+    }
+    const size_t vj_bytes = sizeof(double) * (size_t)N * MM;
+    double *VJ = nullptr, *W = nullptr, *HMAT = nullptr, *A = nullptr, *EV = nullptr, *D = nullptr;
+    double *partial = nullptr;
+    unsigned int *counter = nullptr;
+    int nchunk = (int)((N + kGemvChunk - 1) / kGemvChunk);
+    if (cudaMallocAsync(&VJ, vj_bytes, s) != cudaSuccess) {
+        set_error("PIST basis of %d vectors x %lld points does not fit", MM, N);
+        return SCALIT_ENOMEM;
+    }
+    SC_CUDA(cudaMallocAsync(&W, sizeof(double) * (size_t)N, s));
+    SC_CUDA(cudaMallocAsync(&HMAT, sizeof(double) * (size_t)MM * MM, s));
+    SC_CUDA(cudaMallocAsync(&A, sizeof(double) * (size_t)MM * MM, s));
+    SC_CUDA(cudaMallocAsync(&EV, sizeof(double) * (size_t)MM, s));
+    SC_CUDA(cudaMallocAsync(&D, sizeof(double) * ((size_t)MM + 8), s));
+    SC_CUDA(cudaMallocAsync(&partial, sizeof(double) * std::max((size_t)nchunk * MM, (size_t)kT * 152 * 4), s));
+    SC_CUDA(cudaMallocAsync(&counter, sizeof(unsigned int), s));
+    SC_CUDA(cudaMemsetAsync(counter, 0, sizeof(unsigned int), s));
+    SC_CUDA(cudaMemsetAsync(HMAT, 0, sizeof(double) * (size_t)MM * MM, s));
+
+    cusolverDnHandle_t sol = (cusolverDnHandle_t)c->cusolver;
+    int lwork = 0;
+    if (cusolverDnSetStream(sol, s) != CUSOLVER_STATUS_SUCCESS ||
+        cusolverDnDsyevd_bufferSize(sol, CUSOLVER_EIG_MODE_NOVECTOR, CUBLAS_FILL_MODE_UPPER, MM, A, MM, EV,
+                                    &lwork) != CUSOLVER_STATUS_SUCCESS) {
+        set_error("cusolverDnDsyevd_bufferSize failed");
+        return SCALIT_ECUDA;
+    }
+    double *work = nullptr;
+    int *devinfo = nullptr;
+    SC_CUDA(cudaMallocAsync(&work, sizeof(double) * (size_t)std::max(lwork, 1), s));
+    SC_CUDA(cudaMallocAsync(&devinfo, sizeof(int), s));
+
+    const int gr = egrid(N);
+    double *dnorm = D + MM;       // scratch scalars
+    auto vcol = [&](int J1) { return VJ + (i64)(J1 - 1) * N; };   // 1-based column
+    int status = 0;
+    int rc = 0;
+
+    // MGS_ORTH: orthogonalise W against columns 1..J into column J+1.
+    auto mgs = [&](int J, bool *ok) -> int {
+        double *v = vcol(J + 1);
+        SC_CUDA(cudaMemcpyAsync(v, W, sizeof(double) * (size_t)N, cudaMemcpyDeviceToDevice, s));
+        mgs_kernel<<<gr, kT, 0, s>>>(N, v, nullptr, nullptr, nullptr, dnorm, partial, counter);
+        for (int i = 1; i <= J; ++i) {
+            const double *uprev = (i > 1) ? vcol(i - 1) : nullptr;
+            mgs_kernel<<<gr, kT, 0, s>>>(N, v, uprev, D + (i - 2 >= 0 ? i - 2 : 0), vcol(i), D + (i - 1),
+                                         partial, counter);
+        }
+        // last projection and the norm
+        mgs_kernel<<<gr, kT, 0, s>>>(N, v, vcol(J), D + (J - 1), nullptr, dnorm + 1, partial, counter);
+        SC_CHECK_LAUNCH();
+        double h[2];
+        SC_CUDA(cudaMemcpyAsync(h, dnorm, 2 * sizeof(double), cudaMemcpyDeviceToHost, s));
+        SC_CUDA(cudaStreamSynchronize(s));
+        *ok = (h[0] != 0.0) && (h[1] != 0.0);
+        if (*ok) {
+            scale_inv_sqrt_kernel<<<gr, kT, 0, s>>>(N, v, dnorm + 1);
+            SC_CHECK_LAUNCH();
+        }
+        return 0;
+    };
+
+    auto pisth0 = [&](int m_low, int m_high, int *ret) -> int {
+        *ret = 0;
+        if (m_low < 1 || m_low >= m_high || m_high > MM) return 0;
+        int m_start;
+        if (m_low == 1) {
+            m_start = 1;
+            mgs_kernel<<<gr, kT, 0, s>>>(N, const_cast<double *>(dx0), nullptr, nullptr, nullptr, dnorm,
+                                         partial, counter);
+            SC_CHECK_LAUNCH();
+            double h;
+            SC_CUDA(cudaMemcpyAsync(&h, dnorm, sizeof(double), cudaMemcpyDeviceToHost, s));
+            SC_CUDA(cudaStreamSynchronize(s));
+            if (h == 0.0) return 0;
+            copy_scaled_kernel<<<gr, kT, 0, s>>>(N, dx0, vcol(1), dnorm);
+            SC_CHECK_LAUNCH();
+        } else {
+            m_start = m_low - 1;
+        }
+        *ret = m_high;
+        for (int J = m_start; J <= m_high - 1; ++J) {
+            int num = 0;
+            double t0 = now();
+            int r = ops.linsolv(vcol(J), W, &num);
+            if (r) return r;
+            inf.t_qmr += now() - t0;
+            inf.qmr_solves += 1;
+            if (num > 0) inf.qmr_total += num;
+            if (p->verbose) printf(" # of Lanczos iter.: %d . # of iter. for Linear Solver: %d\n", J, num);
+            if (num <= 0) { *ret = num; return 0; }
+            t0 = now();
+            bool ok = false;
+            r = mgs(J, &ok);
+            if (r) return r;
+            inf.t_orth += now() - t0;
+            if (!ok) { *ret = -J; return 0; }
+        }
+        const double t0 = now();
+        for (int J = m_low; J <= m_high; ++J) {
+            int r = ops.h0x(vcol(J), W);
+            if (r) return r;
+            gemvt_partial_kernel<<<dim3(nchunk, m_high), kT, 0, s>>>(N, m_high, VJ, W, partial, nchunk);
+            gemvt_final_kernel<<<(m_high + 127) / 128, 128, 0, s>>>(m_high, nchunk, partial, HMAT, MM, J - 1);
+            SC_CHECK_LAUNCH();
+        }
+        SC_CUDA(cudaStreamSynchronize(s));
+        inf.t_hmat += now() - t0;
+        return 0;
+    };
+
+    std::vector<double> tmp(MM), old(M), cur(M);
+    auto ritz = [&](int num) -> int {
+        const double t0 = now();
+        gather_upper_kernel<<<egrid((i64)num * num), kT, 0, s>>>(num, HMAT, MM, A);
+        SC_CHECK_LAUNCH();
+        cusolverStatus_t cs = cusolverDnDsyevd(sol, CUSOLVER_EIG_MODE_NOVECTOR, CUBLAS_FILL_MODE_UPPER, num, A,
+                                               num, EV, work, lwork, devinfo);
+        if (cs != CUSOLVER_STATUS_SUCCESS) { set_error("cusolverDnDsyevd failed (%d)", (int)cs); return SCALIT_ECUDA; }
+        int hinfo = 0;
+        SC_CUDA(cudaMemcpyAsync(tmp.data(), EV, sizeof(double) * num, cudaMemcpyDeviceToHost, s));
+        SC_CUDA(cudaMemcpyAsync(&hinfo, devinfo, sizeof(int), cudaMemcpyDeviceToHost, s));
+        SC_CUDA(cudaStreamSynchronize(s));
+        inf.t_ritz += now() - t0;
+        inf.checks += 1;
+        return hinfo == 0 ? 0 : 1;
+    };
+
+    int cnt_low = 1, cnt_high = std::max(std::max(p->startcnt, M), p->stepeig + 1);
+    while (cnt_high <= MM) {
+        int ret = 0;
+        rc = pisth0(cnt_low, cnt_high, &ret);
+        if (rc) break;
+        if (ret < 0) { status = -cnt_high; break; }
+        if (ret == 0 && cnt_low == 1) { status = 0; set_error("PIST start vector is zero"); break; }
+        int num = cnt_high - p->stepeig;
+        int lap = ritz(num);
+        if (lap < 0) { rc = lap; break; }
+        if (lap) { status = -num; break; }
+        get_window(p->e0, tmp, num, M, old.data());
+        num = cnt_high;
+        lap = ritz(num);
+        if (lap < 0) { rc = lap; break; }
+        if (lap) { status = -num; break; }
+        get_window(p->e0, tmp, num, M, cur.data());
+        *res = (p->ntype <= 0) ? diff_max(cur.data(), old.data(), M) : sep_max(old.data(), M, tmp, cnt_high);
+        if (p->verbose) printf(" Cnt1= %d  Cnt2= %d  RES= %.15e\n", cnt_high, cnt_high - p->stepeig, *res);
+        inf.krylov = cnt_high;
+        if (*res <= p->etol) { status = cnt_high; break; }
+        status = -cnt_high;
+        cnt_low = cnt_high + 1;
+        if (cnt_low >= MM) { status = -MM; break; }
+        cnt_high = std::min(cnt_high + p->stepcnt, MM);
+    }
+    std::sort(cur.begin(), cur.end());
+    for (int i = 0; i < M; ++i) eig[i] = cur[i];
+    cudaFreeAsync(VJ, s); cudaFreeAsync(W, s); cudaFreeAsync(HMAT, s); cudaFreeAsync(A, s);
+    cudaFreeAsync(EV, s); cudaFreeAsync(D, s); cudaFreeAsync(partial, s); cudaFreeAsync(counter, s);
+    cudaFreeAsync(work, s); cudaFreeAsync(devinfo, s);
+    cudaStreamSynchronize(s);
+    if (info) *info = inf;
+    return rc ? rc : status;
+}
+
+// Device-resident operators of the context: HX0 = MYHX(TA0), LinSolv = OSB_QMR.
+struct CtxOps : PistOps {
+    scalit_ctx *c;
+    const scalit_pist_params *p;
+    int h0x(const double *dX, double *dY) override
+    {
+        return hx_vec<double>(c, dX, dY, 0.0, 1.0, nullptr, c->stream);
+    }
+    int linsolv(const double *dB, double *dX, int *num) override
+    {
+        QmrResult r{};
+        int rc = qmr_run(c, p->qmr_ntype, p->qmr_max, p->qmr_tol, p->precision, dB, dX, &r);
+        if (rc) return rc;
+        *num = r.code;
+        return 0;
+    }
+};
+
+int pist_ctx(scalit_ctx *c, const scalit_pist_params *p, const double *dx0, double *eig, double *res,
+             scalit_pist_info *info)
+{
+    if (!c->osb_built) { set_error("PIST needs the preconditioner: build or load it first"); return SCALIT_ESTATE; }
+    CtxOps ops;
+    ops.c = c;
+    ops.p = p;
+    return pist_core(c, c->L.N, p, dx0, ops, eig, res, info);
+}
+
+}  // namespace sc

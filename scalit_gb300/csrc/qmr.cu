@@ -1,0 +1,514 @@
+// Device-resident preconditioned QMR (QMR, src/iterate/libiterate/qmr/qmr.f90:5-175;
+// breakdown codes of QMR_MPI, src/iterate/libiterate_mpi/qmr/qmr_mpi.f90:4-263).
+//
+// Every scalar of the recurrence lives in a device struct; the vector steps
+// are fused elementwise + reduction kernels whose last CTA to finish folds the
+// per-CTA partial sums in a fixed order (deterministic) and then advances the
+// scalar recurrence.  Every kernel first reads the struct's `done` flag and
+// returns when it is set, so the host can queue several iterations ahead and
+// only reads the flag back between batches.  The H*X and P*X launches take
+// the same flag as their gate.  FP32 mode keeps the vectors in FP32 and
+// accumulates every reduction in FP64.
+#include "internal.cuh"
+
+#include <cmath>
+
+namespace sc {
+
+static constexpr int kRedThreads = 256;
+static constexpr int kRedMaxBlocks = 152 * 4;
+
+struct QmrState {
+    double BNRM, ZNRM, VNRM, VNRMPO, ZVRAT, QSDOT, VZDOT, BETA, ETA;
+    double GAMAMO, GAMA, THETAMO, THETA, RES, XNRM;
+    double fq;        // Q = Z - fq * Q
+    double cq, cs, g; // UX = cq Q + g UX ; UR = cs S + g UR
+    double inv_zvrat;
+    double tol;
+    int i, code, done, qmrmax, ntype, iters, breakdown;
+    unsigned int counter;
+};
+
+// Sum of per-CTA partials (nv values per CTA) in CTA order by one thread.
+__device__ __forceinline__ void fold(const double *partial, int nblk, int nv, double *out)
+{
+    for (int v = 0; v < nv; ++v) out[v] = 0.0;
+    for (int b = 0; b < nblk; ++b)
+        for (int v = 0; v < nv; ++v) out[v] += partial[nv * b + v];
+}
+
+template <int NV>
+__device__ __forceinline__ bool block_reduce_store(double (&acc)[NV], double *partial,
+                                                   unsigned int *counter)
+{
+    __shared__ double red[NV][kRedThreads / 32];
+    __shared__ bool last;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    #pragma unroll
+    for (int v = 0; v < NV; ++v) {
+        double a = acc[v];
+        #pragma unroll
+        for (int o = 16; o > 0; o >>= 1) a += __shfl_xor_sync(0xffffffffu, a, o);
+        if (lane == 0) red[v][warp] = a;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        #pragma unroll
+        for (int v = 0; v < NV; ++v) {
+            double a = 0.0;
+            for (int w = 0; w < kRedThreads / 32; ++w) a += red[v][w];
+            partial[NV * blockIdx.x + v] = a;
+        }
+        __threadfence();
+        const unsigned int t = atomicAdd(counter, 1u);
+        last = (t == gridDim.x - 1);
+    }
+    __syncthreads();
+    return last;
+}
+
+// ----------------------------------------------------------------- steps --
+// step A: V /= VNRM, Z /= ZNRM, VZDOT = V.Z
+template <class T>
+__global__ void __launch_bounds__(kRedThreads)
+qmr_step_a(i64 n, T *V, T *Z, QmrState *st, double *partial)
+{
+    if (st->done) return;
+    const double vn = st->VNRM, zn = st->ZNRM;
+    if (vn == 0.0 || zn == 0.0) {
+        if (blockIdx.x == 0 && threadIdx.x == 0) { st->code = -1; st->breakdown = 1; st->done = 1; }
+        return;
+    }
+    const T tv = T(vn), tz = T(zn);
+    double acc[1] = {0.0};
+    for (i64 k = blockIdx.x * (i64)blockDim.x + threadIdx.x; k < n; k += (i64)gridDim.x * blockDim.x) {
+        const T v = V[k] / tv, z = Z[k] / tz;
+        V[k] = v; Z[k] = z;
+        acc[0] += (double)v * (double)z;
+    }
+    if (block_reduce_store<1>(acc, partial, &st->counter) && threadIdx.x == 0) {
+        st->counter = 0;
+        double d[1];
+        fold(partial, gridDim.x, 1, d);
+        st->ZVRAT = st->ZVRAT * st->ZNRM / st->VNRM;
+        st->VZDOT = d[0];
+        st->inv_zvrat = 1.0 / st->ZVRAT;
+        if (st->VZDOT == 0.0) { st->code = -2; st->breakdown = 1; st->done = 1; return; }
+        st->fq = (st->i == 1) ? 0.0 : st->VNRM * st->VZDOT / st->QSDOT;
+    }
+}
+
+// step B: Q = Z (i == 1) or Z - fq Q
+template <class T>
+__global__ void qmr_step_b(i64 n, const T *Z, T *Q, const QmrState *st)
+{
+    if (st->done) return;
+    const bool first = (st->i == 1);
+    const T f = T(st->fq);
+    for (i64 k = blockIdx.x * (i64)blockDim.x + threadIdx.x; k < n; k += (i64)gridDim.x * blockDim.x)
+        Q[k] = first ? Z[k] : Z[k] - f * Q[k];
+}
+
+// step C: S = ZVRAT S, QSDOT = Q.S, BETA = QSDOT / VZDOT
+template <class T>
+__global__ void __launch_bounds__(kRedThreads)
+qmr_step_c(i64 n, const T *Q, T *S, QmrState *st, double *partial)
+{
+    if (st->done) return;
+    const T zv = T(st->ZVRAT);
+    double acc[1] = {0.0};
+    for (i64 k = blockIdx.x * (i64)blockDim.x + threadIdx.x; k < n; k += (i64)gridDim.x * blockDim.x) {
+        const T sv = zv * S[k];
+        S[k] = sv;
+        acc[0] += (double)Q[k] * (double)sv;
+    }
+    if (block_reduce_store<1>(acc, partial, &st->counter) && threadIdx.x == 0) {
+        st->counter = 0;
+        double d[1];
+        fold(partial, gridDim.x, 1, d);
+        st->QSDOT = d[0];
+        st->BETA = st->QSDOT / st->VZDOT;
+        if (st->QSDOT == 0.0 || st->BETA == 0.0) { st->code = -3; st->breakdown = 1; st->done = 1; }
+    }
+}
+
+// step D: V = S - BETA V, VNRMPO = |V|
+template <class T>
+__global__ void __launch_bounds__(kRedThreads)
+qmr_step_d(i64 n, const T *S, T *V, QmrState *st, double *partial)
+{
+    if (st->done) return;
+    const T beta = T(st->BETA);
+    double acc[1] = {0.0};
+    for (i64 k = blockIdx.x * (i64)blockDim.x + threadIdx.x; k < n; k += (i64)gridDim.x * blockDim.x) {
+        const T v = S[k] - beta * V[k];
+        V[k] = v;
+        acc[0] += (double)v * (double)v;
+    }
+    if (block_reduce_store<1>(acc, partial, &st->counter) && threadIdx.x == 0) {
+        st->counter = 0;
+        double d[1];
+        fold(partial, gridDim.x, 1, d);
+        st->VNRMPO = sqrt(d[0]);
+    }
+}
+
+// step E: Z = Z / ZVRAT, ZNRM = |Z|, then THETA, GAMA, ETA and the X/R update coefficients
+template <class T>
+__global__ void __launch_bounds__(kRedThreads)
+qmr_step_e(i64 n, T *Z, QmrState *st, double *partial)
+{
+    if (st->done) return;
+    const T zv = T(st->ZVRAT);
+    double acc[1] = {0.0};
+    for (i64 k = blockIdx.x * (i64)blockDim.x + threadIdx.x; k < n; k += (i64)gridDim.x * blockDim.x) {
+        const T z = Z[k] / zv;
+        Z[k] = z;
+        acc[0] += (double)z * (double)z;
+    }
+    if (block_reduce_store<1>(acc, partial, &st->counter) && threadIdx.x == 0) {
+        st->counter = 0;
+        double d[1];
+        fold(partial, gridDim.x, 1, d);
+        st->ZNRM = sqrt(d[0]);
+        st->THETA = st->VNRMPO / (st->GAMAMO * fabs(st->BETA));
+        st->GAMA = 1.0 / sqrt(1.0 + st->THETA * st->THETA);
+        st->ETA = -st->ETA * st->VNRM * st->GAMA * st->GAMA / (st->BETA * st->GAMAMO * st->GAMAMO);
+        if (st->GAMA == 0.0) { st->code = -4; st->breakdown = 1; st->done = 1; return; }
+        st->cq = st->ETA * st->ZVRAT;
+        st->cs = st->ETA;
+        const double tg = st->THETAMO * st->GAMA;
+        st->g = (st->i == 1) ? 0.0 : tg * tg;
+    }
+}
+
+__device__ void qmr_advance(QmrState *st)
+{
+    if (fabs(st->RES) < st->tol) {
+        st->code = st->i;
+        st->iters = st->i;
+        st->done = 1;
+        return;
+    }
+    st->code = -st->i;
+    st->iters = st->i;
+    st->VNRM = st->VNRMPO;
+    st->GAMAMO = st->GAMA;
+    st->THETAMO = st->THETA;
+    st->i = st->i + 1;
+    if (st->i > st->qmrmax) st->done = 1;
+}
+
+// step F: UX, UR, X, R updates; for ntype != +-1 also the convergence test.
+template <class T>
+__global__ void __launch_bounds__(kRedThreads)
+qmr_step_f(i64 n, const T *Q, const T *S, T *UX, T *UR, T *X, T *R, QmrState *st, double *partial)
+{
+    if (st->done) return;
+    const bool first = (st->i == 1);
+    const T cq = T(st->cq), cs = T(st->cs), g = T(st->g);
+    const int conv = abs(st->ntype);
+    double acc[4] = {0.0, 0.0, 0.0, 0.0};
+    for (i64 k = blockIdx.x * (i64)blockDim.x + threadIdx.x; k < n; k += (i64)gridDim.x * blockDim.x) {
+        const T ux = first ? cq * Q[k] : cq * Q[k] + g * UX[k];
+        const T ur = first ? cs * S[k] : cs * S[k] + g * UR[k];
+        UX[k] = ux; UR[k] = ur;
+        const T x = X[k] + ux, r = R[k] - ur;
+        X[k] = x; R[k] = r;
+        acc[0] += (double)r * (double)r;
+        acc[1] += (double)ux * (double)ux;
+        acc[2] += (double)x * (double)x;
+        acc[3] += (double)ur * (double)ur;
+    }
+    if (conv == 1) return;  // the |HX-B|/|HX| test follows in step G
+    if (block_reduce_store<4>(acc, partial, &st->counter) && threadIdx.x == 0) {
+        st->counter = 0;
+        double d[4];
+        fold(partial, gridDim.x, 4, d);
+        if (conv == 2) {
+            const double r1 = sqrt(d[0]) / st->BNRM;
+            const double r2 = sqrt(d[1] / d[2]);
+            const double r3 = sqrt(d[3] / d[0]);
+            st->RES = fmax(fmax(r1, r2), r3);
+        } else {
+            st->RES = sqrt(d[0]) / st->BNRM;
+        }
+        qmr_advance(st);
+    }
+}
+
+// step G: XNRM = |HX0|, RES = |HX0 - B| / XNRM (HX0 = H X), then advance.
+template <class T>
+__global__ void __launch_bounds__(kRedThreads)
+qmr_step_g(i64 n, const T *HX0, const T *B, QmrState *st, double *partial)
+{
+    if (st->done) return;
+    double acc[2] = {0.0, 0.0};
+    for (i64 k = blockIdx.x * (i64)blockDim.x + threadIdx.x; k < n; k += (i64)gridDim.x * blockDim.x) {
+        const T h = HX0[k];
+        const T d = h - B[k];
+        acc[0] += (double)h * (double)h;
+        acc[1] += (double)d * (double)d;
+    }
+    if (block_reduce_store<2>(acc, partial, &st->counter) && threadIdx.x == 0) {
+        st->counter = 0;
+        double d[2];
+        fold(partial, gridDim.x, 2, d);
+        st->XNRM = sqrt(d[0]);
+        st->RES = sqrt(d[1]) / st->XNRM;
+        qmr_advance(st);
+    }
+}
+
+// initial norms: BNRM = VNRM = |B|, ZNRM = |Z|
+template <class T>
+__global__ void __launch_bounds__(kRedThreads)
+qmr_init_norms(i64 n, const T *B, const T *Z, QmrState *st, double *partial)
+{
+    double acc[2] = {0.0, 0.0};
+    for (i64 k = blockIdx.x * (i64)blockDim.x + threadIdx.x; k < n; k += (i64)gridDim.x * blockDim.x) {
+        acc[0] += (double)B[k] * (double)B[k];
+        acc[1] += (double)Z[k] * (double)Z[k];
+    }
+    if (block_reduce_store<2>(acc, partial, &st->counter) && threadIdx.x == 0) {
+        st->counter = 0;
+        double d[2];
+        fold(partial, gridDim.x, 2, d);
+        st->BNRM = sqrt(d[0]);
+        st->VNRM = st->BNRM;
+        st->ZNRM = sqrt(d[1]);
+        if (st->qmrmax < 1) st->done = 1;
+    }
+}
+
+template <class T>
+__global__ void copy_kernel(i64 n, const T *a, T *b, T *c)
+{
+    for (i64 k = blockIdx.x * (i64)blockDim.x + threadIdx.x; k < n; k += (i64)gridDim.x * blockDim.x) {
+        const T v = a[k];
+        b[k] = v;
+        if (c) c[k] = v;
+    }
+}
+
+__global__ void f64_to_f32_kernel(i64 n, const double *x, float *y)
+{
+    for (i64 k = blockIdx.x * (i64)blockDim.x + threadIdx.x; k < n; k += (i64)gridDim.x * blockDim.x)
+        y[k] = (float)x[k];
+}
+
+__global__ void f32_to_f64_kernel(i64 n, const float *x, double *y)
+{
+    for (i64 k = blockIdx.x * (i64)blockDim.x + threadIdx.x; k < n; k += (i64)gridDim.x * blockDim.x)
+        y[k] = (double)x[k];
+}
+
+static int red_grid(i64 n)
+{
+    i64 g = (n + kRedThreads * 4 - 1) / (kRedThreads * 4);
+    if (g > kRedMaxBlocks) g = kRedMaxBlocks;
+    if (g < 1) g = 1;
+    return (int)g;
+}
+
+static int ew_grid(i64 n)
+{
+    i64 g = (n + 255) / 256;
+    if (g > 152 * 16) g = 152 * 16;
+    if (g < 1) g = 1;
+    return (int)g;
+}
+
+int to_f32(const double *x, float *y, i64 n, cudaStream_t s)
+{
+    if (n <= 0) return 0;
+    f64_to_f32_kernel<<<ew_grid(n), 256, 0, s>>>(n, x, y);
+    SC_CHECK_LAUNCH();
+    return 0;
+}
+
+int to_f64(const float *x, double *y, i64 n, cudaStream_t s)
+{
+    if (n <= 0) return 0;
+    f32_to_f64_kernel<<<ew_grid(n), 256, 0, s>>>(n, x, y);
+    SC_CHECK_LAUNCH();
+    return 0;
+}
+
+__global__ void axpy_kernel(i64 n, double a, const double *x, double *y)
+{
+    for (i64 k = blockIdx.x * (i64)blockDim.x + threadIdx.x; k < n; k += (i64)gridDim.x * blockDim.x)
+        y[k] = y[k] + a * x[k];
+}
+
+__global__ void scal_kernel(i64 n, double a, double *x)
+{
+    for (i64 k = blockIdx.x * (i64)blockDim.x + threadIdx.x; k < n; k += (i64)gridDim.x * blockDim.x)
+        x[k] = a * x[k];
+}
+
+int axpy_dev(i64 n, double a, const double *x, double *y, cudaStream_t s)
+{
+    if (n <= 0) return 0;
+    axpy_kernel<<<ew_grid(n), 256, 0, s>>>(n, a, x, y);
+    SC_CHECK_LAUNCH();
+    return 0;
+}
+
+int scal_dev(i64 n, double a, double *x, cudaStream_t s)
+{
+    if (n <= 0) return 0;
+    scal_kernel<<<ew_grid(n), 256, 0, s>>>(n, a, x);
+    SC_CHECK_LAUNCH();
+    return 0;
+}
+
+// Plain deterministic dot for the API (NORM_MPI / DOTPROD_MPI drop-ins).
+template <class T>
+__global__ void __launch_bounds__(kRedThreads)
+dot_kernel(i64 n, const T *x, const T *y, double *partial, unsigned int *counter, double *out)
+{
+    double acc[1] = {0.0};
+    for (i64 k = blockIdx.x * (i64)blockDim.x + threadIdx.x; k < n; k += (i64)gridDim.x * blockDim.x)
+        acc[0] += (double)x[k] * (double)y[k];
+    if (block_reduce_store<1>(acc, partial, counter) && threadIdx.x == 0) {
+        *counter = 0;
+        double d[1];
+        fold(partial, gridDim.x, 1, d);
+        *out = d[0];
+    }
+}
+
+template <class T>
+int dot_dev(scalit_ctx *c, i64 n, const T *x, const T *y, double *out, cudaStream_t s)
+{
+    dot_kernel<T><<<red_grid(n), kRedThreads, 0, s>>>(n, x, y, c->red_partial, c->red_counter, out);
+    SC_CHECK_LAUNCH();
+    return 0;
+}
+
+template int dot_dev<double>(scalit_ctx *, i64, const double *, const double *, double *, cudaStream_t);
+template int dot_dev<float>(scalit_ctx *, i64, const float *, const float *, double *, cudaStream_t);
+
+// ------------------------------------------------------------------ driver --
+template <class T>
+int qmr_core(scalit_ctx *c, i64 n, QmrOps<T> &ops, int ntype, int qmrmax, double qmrtol,
+             const T *B, T *X, QmrResult *out)
+{
+    cudaStream_t s = c->stream;
+    // vectors: R UX UR Q S V Z HX0, then the scalar state
+    T *w = nullptr;
+    const size_t need = sizeof(T) * (size_t)n * 8 + sizeof(QmrState) + 64;
+    int rc = work_get(c, need, (void **)&w);
+    if (rc) return rc;
+    T *R = w, *UX = w + n, *UR = w + 2 * n, *Q = w + 3 * n, *S = w + 4 * n, *V = w + 5 * n;
+    T *Z = w + 6 * n, *HX0 = w + 7 * n;
+    QmrState *st = reinterpret_cast<QmrState *>(((uintptr_t)(w + 8 * n) + 63) & ~(uintptr_t)63);
+    QmrState h{};
+    h.ZVRAT = 1.0;
+    h.GAMAMO = 1.0;
+    h.ETA = -1.0;
+    h.i = 1;
+    h.qmrmax = qmrmax;
+    h.ntype = ntype;
+    h.tol = qmrtol;
+    SC_CUDA(cudaMemcpyAsync(st, &h, sizeof(h), cudaMemcpyHostToDevice, s));
+    const int *gate = &st->done;
+    double *partial = c->red_partial;
+    const int gr = red_grid(n), ge = ew_grid(n);
+
+    if (ntype <= 0) SC_CUDA(cudaMemsetAsync(X, 0, sizeof(T) * (size_t)n, s));
+    copy_kernel<T><<<ge, 256, 0, s>>>(n, B, R, V);
+    SC_CHECK_LAUNCH();
+    rc = ops.px(B, Z, nullptr);
+    if (rc) return rc;
+    qmr_init_norms<T><<<gr, kRedThreads, 0, s>>>(n, B, Z, st, partial);
+    SC_CHECK_LAUNCH();
+
+    const int batch = ops.host_side() ? 1 : 4;
+    int it = 0;
+    int *h_flag = reinterpret_cast<int *>(c->h_pinned);
+    while (true) {
+        for (int b = 0; b < batch; ++b) {
+            qmr_step_a<T><<<gr, kRedThreads, 0, s>>>(n, V, Z, st, partial);
+            qmr_step_b<T><<<ge, 256, 0, s>>>(n, Z, Q, st);
+            SC_CHECK_LAUNCH();
+            // S = (H - E0) Q; step C scales it by ZVRAT as the reference does
+            rc = ops.hx(Q, S, gate);
+            if (rc) return rc;
+            qmr_step_c<T><<<gr, kRedThreads, 0, s>>>(n, Q, S, st, partial);
+            qmr_step_d<T><<<gr, kRedThreads, 0, s>>>(n, S, V, st, partial);
+            SC_CHECK_LAUNCH();
+            rc = ops.px(V, Z, gate);
+            if (rc) return rc;
+            qmr_step_e<T><<<gr, kRedThreads, 0, s>>>(n, Z, st, partial);
+            qmr_step_f<T><<<gr, kRedThreads, 0, s>>>(n, Q, S, UX, UR, X, R, st, partial);
+            SC_CHECK_LAUNCH();
+            if (abs(ntype) == 1) {
+                rc = ops.hx(X, HX0, gate);
+                if (rc) return rc;
+                qmr_step_g<T><<<gr, kRedThreads, 0, s>>>(n, HX0, B, st, partial);
+                SC_CHECK_LAUNCH();
+            }
+            ++it;
+        }
+        SC_CUDA(cudaMemcpyAsync(h_flag, &st->done, sizeof(int), cudaMemcpyDeviceToHost, s));
+        SC_CUDA(cudaStreamSynchronize(s));
+        if (*h_flag) break;
+        if (it > qmrmax + batch) { set_error("QMR did not stop"); return SCALIT_ESTATE; }
+    }
+    SC_CUDA(cudaMemcpyAsync(&h, st, sizeof(h), cudaMemcpyDeviceToHost, s));
+    SC_CUDA(cudaStreamSynchronize(s));
+    out->code = h.code;
+    out->res = h.RES;
+    out->iters = h.iters;
+    out->breakdown = h.breakdown;
+    return 0;
+}
+
+template int qmr_core<double>(scalit_ctx *, i64, QmrOps<double> &, int, int, double, const double *, double *, QmrResult *);
+template int qmr_core<float>(scalit_ctx *, i64, QmrOps<float> &, int, int, double, const float *, float *, QmrResult *);
+
+// The context's own operator pair: HX = MYHX(TA1), PX = MYPX(sOSB, TA1).
+template <class T> struct CtxQmrOps : QmrOps<T> {
+    scalit_ctx *c;
+    T *tmp;
+    int hx(const T *in, T *out, const int *gate) override
+    {
+        return hx_vec<T>(c, in, out, T(c->E0), T(1), gate, c->stream);
+    }
+    int px(const T *in, T *out, const int *gate) override
+    {
+        return px_vec<T>(c, SCALIT_TA1, in, out, tmp, T(1), gate, c->stream);
+    }
+};
+
+int qmr_run(scalit_ctx *c, int ntype, int qmrmax, double qmrtol, int precision,
+            const double *dB, double *dX, QmrResult *out)
+{
+    if (!c->osb_built) { set_error("QMR needs the preconditioner: build or load it first"); return SCALIT_ESTATE; }
+    const i64 n = c->L.N;
+    if (precision == SCALIT_PREC_FP64) {
+        double *tmp = nullptr;
+        SC_CUDA(cudaMallocAsync(&tmp, sizeof(double) * (size_t)n, c->stream));
+        CtxQmrOps<double> ops;
+        ops.c = c;
+        ops.tmp = tmp;
+        int rc = qmr_core<double>(c, n, ops, ntype, qmrmax, qmrtol, dB, dX, out);
+        cudaFreeAsync(tmp, c->stream);
+        return rc;
+    }
+    if (precision != SCALIT_PREC_FP32) { set_error("unknown precision %d", precision); return SCALIT_EINVAL; }
+    float *bx = nullptr;
+    SC_CUDA(cudaMallocAsync(&bx, sizeof(float) * 3 * (size_t)n, c->stream));
+    CtxQmrOps<float> ops;
+    ops.c = c;
+    ops.tmp = bx + 2 * n;
+    int rc = to_f32(dB, bx, n, c->stream);
+    if (!rc) rc = qmr_core<float>(c, n, ops, ntype, qmrmax, qmrtol, bx, bx + n, out);
+    if (!rc) rc = to_f64(bx + n, dX, n, c->stream);
+    cudaFreeAsync(bx, c->stream);
+    return rc;
+}
+
+}  // namespace sc

@@ -1,0 +1,124 @@
+"""H*X on the GPU against the oracle (MYHX, src/iterate/module/osb.hx.h:71-110).
+
+Tolerance: norm-wise relative error 1e-12 in FP64 (elementwise relative error
+is ill-posed where the potential cancels the kinetic terms); 2e-6 in FP32.
+"""
+import numpy as np
+import pytest
+
+from scalit_gb300 import capi, hamiltonian as hm
+
+pytestmark = pytest.mark.gpu
+
+TOL64 = 1e-12
+TOL32 = 2e-6
+
+
+def rel(a, b):
+    return float(np.linalg.norm(a - b) / np.linalg.norm(b))
+
+
+@pytest.fixture(scope="module")
+def c0():
+    return hm.workload("tri-24x32x20")
+
+
+@pytest.mark.parametrize("ntype", [0, 1])
+def test_hx_c0_16_vectors(lib, orc, c0, ntype):
+    e0 = float(c0.RES.min())
+    ref = orc.Operator.from_problem(c0, E0=e0)
+    X = np.random.default_rng(0).standard_normal((16, c0.N))
+    with capi.Context.from_problem(c0, e0=e0) as ctx:
+        Y = ctx.hx(X, ntype)
+    for v in range(16):
+        assert rel(Y[v], ref.hx(X[v], ntype)) < TOL64
+
+
+@pytest.mark.parametrize("sizes", [(2, 3, 2), (5, 7, 3), (8, 8, 8), (13, 1, 9), (1, 6, 4),
+                                   (67, 3, 5), (3, 130, 2)])
+def test_hx_odd_shapes(lib, orc, sizes):
+    grid = hm.Grid3(*sizes)
+    p = hm.build_problem(grid, hm.PES())
+    ref = orc.Operator.from_problem(p, E0=0.01)
+    x = np.random.default_rng(1).standard_normal(p.N)
+    with capi.Context.from_problem(p, e0=0.01) as ctx:
+        y = ctx.hx(x, capi.TA1)
+    assert rel(y, ref.hx(x, 1)) < TOL64
+
+
+def test_hx_general_levels(lib, orc):
+    """A 4-level grid with two dependent levels (the layout is general in sF)."""
+    sizes = (4, 5, 3, 6)
+    dep = (False, True, False, True)
+    rng = np.random.default_rng(2)
+    H0 = []
+    for n in sizes:
+        a = rng.standard_normal((n, n))
+        H0.append(((a + a.T) / 2).ravel(order="F"))
+    H0 = np.concatenate(H0)
+    N = int(np.prod(sizes))
+    RES = rng.standard_normal(N)
+    dims = np.cumprod((1,) + sizes[:-1])
+    DEP = np.concatenate([rng.uniform(0.5, 1.5, int(dims[l])) for l in range(4) if dep[l]])
+    ref = orc.Operator(sizes, dep, H0, RES, DEP, E0=0.3)
+    x = rng.standard_normal(N)
+    with capi.Context(sizes, dep) as ctx:
+        ctx.load(H0, RES, DEP)
+        ctx.set_shift(0.3)
+        for nt in (0, 1):
+            assert rel(ctx.hx(x, nt), ref.hx(x, nt)) < TOL64
+
+
+def test_hx_f32_device(lib, orc, c0):
+    torch = pytest.importorskip("torch")
+    e0 = float(c0.RES.min())
+    ref = orc.Operator.from_problem(c0, E0=e0)
+    x = np.random.default_rng(3).standard_normal(c0.N)
+    with capi.Context.from_problem(c0, e0=e0) as ctx:
+        dx = torch.tensor(x, dtype=torch.float32, device="cuda")
+        dy = torch.empty_like(dx)
+        ctx.hx_f32_device(dx, dy, 1, capi.TA1)
+        torch.cuda.synchronize()
+        y = dy.double().cpu().numpy()
+    assert rel(y, ref.hx(x, 1)) < TOL32
+
+
+def test_hx_device_many(lib, orc, c0):
+    torch = pytest.importorskip("torch")
+    X = np.random.default_rng(4).standard_normal((3, c0.N))
+    ref = orc.Operator.from_problem(c0, E0=0.0)
+    with capi.Context.from_problem(c0, e0=0.0) as ctx:
+        dX = torch.tensor(X, device="cuda")
+        dY = torch.empty_like(dX)
+        ctx.hx_device(dX, dY, 3, capi.TA0)
+        torch.cuda.synchronize()
+        Y = dY.cpu().numpy()
+    for v in range(3):
+        assert rel(Y[v], ref.hx(X[v], 0)) < TOL64
+
+
+@pytest.mark.parametrize("name", ["tri-96x96x64", "tri-160x160x120"])
+def test_hx_large(lib, orc, name):
+    p = hm.workload(name)
+    e0 = float(p.RES.min())
+    ref = orc.Operator.from_problem(p, E0=e0)
+    x = np.random.default_rng(5).standard_normal(p.N)
+    with capi.Context.from_problem(p, e0=e0) as ctx:
+        y = ctx.hx(x, capi.TA1)
+    assert rel(y, ref.hx(x, 1)) < TOL64
+
+
+def test_hx_rejects_nonfinite(lib, c0):
+    bad = c0.RES.copy()
+    bad[7] = np.nan
+    with capi.Context(c0.sizes, c0.dep) as ctx:
+        with pytest.raises(capi.ScalitError) as e:
+            ctx.load(c0.H0, bad, c0.DEP)
+        assert e.value.code == -106
+
+
+def test_hx_before_load_is_an_error(lib, c0):
+    with capi.Context(c0.sizes, c0.dep) as ctx:
+        with pytest.raises(capi.ScalitError) as e:
+            ctx.hx(np.zeros(c0.N))
+        assert e.value.code == -104
