@@ -1,0 +1,379 @@
+"""Benchmark of the H*X hot path on GB300.
+
+One step = one FP64 H*X application (MYHX, TA1) to a block of 16 vectors on
+the 96 x 96 x 64 Jacobi-DVR grid (589,824 points) -- the "bare FP64 H*X on 1
+and 16 vectors" of the plain-FP64 GPU workload.  Inputs are seeded N(0,1)
+vectors already resident in HBM; two input/output sets (2 x 151 MB, larger
+than the 129 MB L2) alternate between steps.  `e2e` repeats the measurement
+through the host-buffer C ABI (scalit_hx), host<->device copies included.
+
+N > 1 (torchrun): replicas -- every rank runs the same workload on its own GPU,
+no collective on the data path; value = all ranks' applications / slowest rank.
+
+--impl reference: the oracle's FP64 restatement of the reference's serial
+MYHX (C, OpenMP over all host cores), timed on a bounded sample of the same
+workload; rank 0 only.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "H*X apps/s & %roofline; PIST time to 200 levels (mixed vs FP64 GPU)"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="tri-96x96x64")
+    ap.add_argument("--nvec", type=int, default=16)
+    ap.add_argument("--cpu-seconds", type=float, default=12.0)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    return ap.parse_args()
+
+
+# ---------------------------------------------------------------- helpers --
+def dist_env():
+    return (int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)),
+            int(os.environ.get("LOCAL_RANK", 0)))
+
+
+def reduce_max(value: float, world: int) -> float:
+    """Max of a per-rank float over all ranks (identity for one rank)."""
+    if world <= 1:
+        return value
+    import torch
+    import torch.distributed as dist
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([value], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def replicas_value(units_per_rank: float, world: int, max_seconds: float) -> float:
+    return units_per_rank * world / max_seconds
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled while the timed region runs."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device_index: int):
+        self.idx = device_index
+        self.samples = []
+        self._stop = threading.Event()
+        self._t = None
+
+    def _run(self):
+        while not self._stop.is_set():
+            try:
+                out = subprocess.run(["nvidia-smi", "-i", str(self.idx), f"--query-gpu={self.FIELDS}",
+                                      "--format=csv,noheader,nounits"], capture_output=True,
+                                     text=True, timeout=5).stdout.strip()
+                if out:
+                    self.samples.append([s.strip() for s in out.split(",")])
+            except Exception:
+                pass
+            self._stop.wait(0.2)
+
+    def __enter__(self):
+        self._t = threading.Thread(target=self._run, daemon=True)
+        self._t.start()
+        return self
+
+    def __exit__(self, *a):
+        self._stop.set()
+        if self._t:
+            self._t.join(timeout=10)
+
+    def summary(self):
+        if not self.samples:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [float(s[1]) for s in self.samples if s[1].replace(".", "").isdigit()]
+        smax = [float(s[2]) for s in self.samples if s[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for s in self.samples for i in range(4)
+                          if len(s) > 5 + i and s[5 + i].lower() == "active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(smax) if smax else None, "reasons": reasons,
+                "samples": len(self.samples)}
+
+
+def load_peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(path) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), float(d["bf16_tflops"]), "measured"
+    except Exception:
+        return 6800.0, 1900.0, "fallback"
+
+
+def hx_units(sizes):
+    """Algorithmic flops and bytes of one FP64 H*X application, and per level.
+
+    flops: 2 N n_l per level plus the diagonal (V - E0) X and the level sums (5N).
+    bytes of a level launch: read X, write Y, and read Y when accumulating
+    (levels 2..sF), plus the small level matrix; DEP and V where used.
+    """
+    n = list(sizes)
+    N = int(np.prod(n))
+    w = 8
+    levels = []
+    for l, nl in enumerate(n):
+        flops = 2.0 * N * nl
+        byts = (2 + (1 if l > 0 else 0)) * N * w + nl * nl * w
+        if l == 0:
+            byts += N * w            # V for the fused diagonal term
+            flops += 3.0 * N
+        if l == len(n) - 1:
+            byts += (N // nl) * w    # DEP factors c(r, R)
+            flops += N
+        levels.append({"flops": flops, "bytes": byts})
+    total_flops = sum(x["flops"] for x in levels) + N
+    total_bytes = 3 * N * w + sum(m * m for m in n) * w + (N // n[-1]) * w
+    return total_flops, total_bytes, levels
+
+
+# ------------------------------------------------------------- reference --
+def cpu_baseline(problem, e0, seconds, nvec_cap=64):
+    """The oracle's MYHX on the host cores: applications per second on a bounded sample."""
+    from oracle import oracle as orc
+    op = orc.Operator.from_problem(problem, E0=e0)
+    x = np.random.default_rng(0).standard_normal(problem.N)
+    op.hx(x, 1)
+    t0 = time.perf_counter()
+    op.hx(x, 1)
+    one = time.perf_counter() - t0
+    reps = max(1, min(nvec_cap, int(seconds / max(one, 1e-6))))
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        op.hx(x, 1)
+    dt = time.perf_counter() - t0
+    return {"value": reps / dt, "unit": "H*X apps/s", "cores": orc.num_threads(), "kind": "port",
+            "sample": f"{reps} FP64 H*X applications (TA1) on the {problem.sizes[0]}x"
+                      f"{problem.sizes[1]}x{problem.sizes[2]} grid, oracle C restatement of MYHX "
+                      f"(osb.hx.h:71-110), OpenMP over blocks"}
+
+
+def run_reference(args):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return 0
+    from scalit_gb300 import hamiltonian as hm
+    p = hm.workload(args.workload)
+    e0 = float(p.RES.min())
+    from oracle import oracle as orc
+    op = orc.Operator.from_problem(p, E0=e0)
+    x = np.random.default_rng(0).standard_normal(p.N)
+    op.hx(x, 1)
+    t0 = time.perf_counter()
+    op.hx(x, 1)
+    one = time.perf_counter() - t0
+    # each step is a bounded sample: nvec applications, capped so the run stays short
+    per_step = max(1, min(args.nvec, int(6.0 / max(one, 1e-6))))
+    for _ in range(args.warmup):
+        op.hx(x, 1)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        for _ in range(per_step):
+            op.hx(x, 1)
+    dt = time.perf_counter() - t0
+    value = args.steps * per_step / dt
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": "H*X apps/s",
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": dt / args.steps * 1e3, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": args.workload, "grid": list(p.sizes), "npoints": p.N,
+                   "vectors_per_step": per_step, "operator": "MYHX TA1"},
+        "cpu_baseline": {"value": value, "unit": "H*X apps/s", "cores": orc.num_threads(),
+                         "kind": "port",
+                         "sample": f"{per_step} applications per step, oracle C restatement of MYHX"},
+        "e2e": {"value": value, "unit": "H*X apps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+# ------------------------------------------------------------------- ours --
+def run_ours(args):
+    import torch
+    rank, world, local = dist_env()
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", init_method="env://")
+    torch.cuda.set_device(local)
+    from scalit_gb300 import capi, hamiltonian as hm
+    capi.load(build_if_missing=True)
+    p = hm.workload(args.workload)
+    e0 = float(p.RES.min())
+    N, nvec = p.N, args.nvec
+    ctx = capi.Context.from_problem(p, e0=e0, device=local)
+    stream = torch.cuda.ExternalStream(ctx.stream, device=local)
+    gen = torch.Generator(device=f"cuda:{local}").manual_seed(1234 + rank)
+    X = [torch.randn(nvec, N, dtype=torch.float64, device=f"cuda:{local}", generator=gen) for _ in range(2)]
+    Y = [torch.empty_like(X[0]) for _ in range(2)]
+    torch.cuda.synchronize()
+
+    def step(i):
+        ctx.hx_device(X[i % 2], Y[i % 2], nvec, capi.TA1)
+
+    for i in range(max(args.warmup, 3)):
+        step(i)
+    torch.cuda.synchronize()
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(local) as clk:
+        with torch.cuda.stream(stream):
+            ev0.record(stream)
+            for i in range(args.steps):
+                step(i)
+            ev1.record(stream)
+        torch.cuda.synchronize()
+    if world > 1:
+        torch.distributed.barrier()
+    ms = ev0.elapsed_time(ev1)
+    ms_max = reduce_max(ms, world)
+    value = replicas_value(args.steps * nvec, world, ms_max / 1e3)
+
+    # per-level kernel timing (the strided GEMM launches of one application)
+    total_flops, total_bytes, lv = hx_units(p.sizes)
+    level_ms = []
+    reps = 20
+    for l in range(len(p.sizes)):
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        with torch.cuda.stream(stream):
+            for i in range(3):
+                ctx.level_device(l + 1, X[i % 2][i], Y[i % 2][i], accumulate=l > 0)
+            a.record(stream)
+            for i in range(reps):
+                ctx.level_device(l + 1, X[i % 2][i % nvec], Y[i % 2][i % nvec], accumulate=l > 0)
+            b.record(stream)
+        torch.cuda.synchronize()
+        level_ms.append(a.elapsed_time(b) / reps)
+    dom = int(np.argmax(level_ms))
+    hbm, bf16, peak_src = load_peaks()
+    ach_gbs = lv[dom]["bytes"] / (level_ms[dom] / 1e3) / 1e9
+    ach_tf = lv[dom]["flops"] / (level_ms[dom] / 1e3) / 1e12
+
+    # FP64 reference rate: cuBLAS DGEMM measured live (the FP64 unit this path runs on)
+    fp64_peak = None
+    try:
+        m = 4096
+        A = torch.randn(m, m, dtype=torch.float64, device=f"cuda:{local}")
+        B = torch.randn(m, m, dtype=torch.float64, device=f"cuda:{local}")
+        for _ in range(2):
+            A @ B
+        torch.cuda.synchronize()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record()
+        for _ in range(3):
+            A @ B
+        b.record()
+        torch.cuda.synchronize()
+        fp64_peak = 2.0 * m ** 3 * 3 / (a.elapsed_time(b) / 1e3) / 1e12
+        del A, B
+    except Exception:
+        fp64_peak = None
+
+    # FP32 (the inner-solve arithmetic) on the same block
+    X32 = [x.float() for x in X]
+    Y32 = [torch.empty_like(x) for x in X32]
+    with torch.cuda.stream(stream):
+        for i in range(3):
+            ctx.hx_f32_device(X32[i % 2], Y32[i % 2], nvec, capi.TA1)
+    torch.cuda.synchronize()
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with torch.cuda.stream(stream):
+        a.record(stream)
+        for i in range(args.steps):
+            ctx.hx_f32_device(X32[i % 2], Y32[i % 2], nvec, capi.TA1)
+        b.record(stream)
+    torch.cuda.synchronize()
+    fp32_apps = args.steps * nvec / (a.elapsed_time(b) / 1e3)
+    del X32, Y32
+
+    # end to end through the host-buffer ABI (pinned host memory)
+    Xh = X[0].cpu().pin_memory()
+    Yh = torch.empty_like(Xh).pin_memory()
+    xh, yh = Xh.numpy(), Yh.numpy()
+    ctx.hx(xh, capi.TA1)
+    e2e_steps = max(3, args.steps // 4)
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        yh[...] = ctx.hx(xh, capi.TA1)
+    e2e_s = time.perf_counter() - t0
+    e2e_s = reduce_max(e2e_s, world)
+    e2e_value = replicas_value(e2e_steps * nvec, world, e2e_s)
+
+    base = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        base = cpu_baseline(p, e0, args.cpu_seconds)
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": "H*X apps/s", "n_gpus": world,
+            "steps": args.steps, "warmup": max(args.warmup, 3), "ms_per_step": ms_max / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic",
+            "config": {"workload": args.workload, "grid": list(p.sizes), "npoints": N,
+                       "vectors_per_step": nvec, "operator": "MYHX TA1 (H - E0) X",
+                       "parallelism": f"replicas{world}",
+                       "l2": "two alternating 2x151 MB input/output sets (> 129 MB L2)"},
+            "roofline": {"bound": "hbm", "achieved": ach_gbs, "peak": hbm, "unit": "GB/s",
+                         "frac": ach_gbs / hbm, "traffic": None,
+                         "kernel": f"gemm_kernel<double> level {dom + 1}",
+                         "peak_source": peak_src,
+                         "algorithmic_bytes_per_launch": lv[dom]["bytes"],
+                         "launch_ms": level_ms[dom]},
+            "fp64_roofline": {"bound": "fp64", "achieved": ach_tf, "unit": "TFLOP/s",
+                              "peak": fp64_peak, "frac": (ach_tf / fp64_peak) if fp64_peak else None,
+                              "peak_source": "cuBLAS DGEMM 4096^3 measured in this run",
+                              "algorithmic_flops_per_launch": lv[dom]["flops"]},
+            "level_ms": level_ms,
+            "hx_flops_per_app": total_flops, "hx_bytes_per_app": total_bytes,
+            "fp32_apps_per_s": fp32_apps,
+            "e2e": {"value": e2e_value, "unit": "H*X apps/s",
+                    "h2d_bytes_per_step": int(nvec * N * 8), "d2h_bytes_per_step": int(nvec * N * 8)},
+            "gpu_launches": args.steps * nvec * len(p.sizes),
+            "clocks": clk.summary(),
+        }
+        if base is not None:
+            line["cpu_baseline"] = base
+        print(json.dumps(line), flush=True)
+    ctx.close()
+    if world > 1:
+        torch.distributed.destroy_process_group()
+    return 0
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_ours(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

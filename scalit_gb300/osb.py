@@ -1,0 +1,128 @@
+"""Host-side mirror of the reference's OSB module and iterate driver.
+
+The serial driver ``prog_diag`` (src/iterate/prog/osb.drv.f90:3-38) and its MPI
+twin (posb2.drv.f90:5-44) do: read the stdin parameter file (myReadOSB), size
+the module (calOSB), load H0/RES/DEP (loadInitData), build the preconditioner
+(progDiag -> myDiag) and run PIST (progPistEig -> OSB_PISTCONV).  :class:`OSB`
+keeps the same steps and names; every numerical step runs on the GPU through
+the C ABI (``scalit_gb300.capi``).
+
+    python -m scalit_gb300.osb < input.txt
+"""
+from __future__ import annotations
+
+import sys
+import time
+
+import numpy as np
+
+from . import capi, refio
+
+
+class OSB:
+    """Module state: the parameter record plus the device context."""
+
+    def __init__(self, inp: refio.OSBInput, device: int = 0, precision: int = capi.PREC_FP64):
+        if inp.sCX:
+            raise ValueError("complex Hamiltonians (sCX) are not supported")
+        if inp.sOSB == refio.TOSBW:
+            raise ValueError("the OSBW window preconditioner (sOSB=4) is not supported")
+        self.inp = inp
+        self.device = device
+        self.precision = precision
+        self.ctx = None
+        self.stats = None
+
+    # readOSB (osb.print.h:2, 192-246)
+    @classmethod
+    def read(cls, text: str, **kw) -> "OSB":
+        return cls(refio.read_input(text), **kw)
+
+    # loadInitData (osb.io.h:2-42)
+    def load_init_data(self) -> bool:
+        inp = self.inp
+        H0 = refio.load_data(inp.H0File, inp.h0_len)
+        OUTH = None
+        if inp.sNDVR:
+            OUTH = refio.load_data_dir(inp.OUTHFile, inp.sN[inp.sF - 1] * inp.my_len)
+            RES = np.zeros(inp.my_len)
+        else:
+            RES = refio.load_data_dir(inp.RESFile, inp.my_len)
+        DEP = refio.load_data_dir(inp.DEPFile, inp.dep_len) if inp.dep_len else None
+        self.ctx = capi.Context(inp.sN[:inp.sF], inp.sDEP[:inp.sF], ndvr=inp.sNDVR, device=self.device)
+        self.ctx.load(H0, RES, DEP, OUTH)
+        self.ctx.set_shift(inp.sOSBW[0])
+        self.ctx.set_precond(inp.sOSB if inp.sOSB in (1, 2, 3) else 1, inp.sOSBW[1], inp.sOSBW[2])
+        return True
+
+    # progDiag (osb.progDiag.h:6-51): build, or load a saved preconditioner (sVOSB < 0)
+    def prog_diag(self, log=print):
+        inp = self.inp
+        t0 = time.perf_counter()
+        if inp.sVOSB < 0:
+            V = refio.load_data_dir(inp.VOSBFile, self.ctx.vosb_len)
+            E = refio.load_data_dir(inp.EigFile, inp.my_len)
+            self.ctx.set_osb(V, E)
+        else:
+            self.stats = self.ctx.build_osb(inp.sBJ[0], inp.sBJ[1])
+            if log:
+                for l in range(inp.sF - 1, -1, -1):
+                    eff = self.stats[l]
+                    blk = inp.my_blk[l]
+                    log(f"  BJ Diag.: Level:{l + 1:4d}.   Grid Size:{inp.sN[l]:6d}   # of Blocks:{blk:6d}")
+                    log(f" Aver. # of Sweeps:{eff[4] / blk:10.5f}.    Aver. OffDiag/Diag:{eff[2] / eff[4]:10.6f}")
+                    log(f" Jacobi Effi: Min:{eff[0]:10.5f},   Max:{eff[1]:10.5f},  Mean:{eff[2] / blk:10.5f}")
+            if inp.sVOSB > 0:
+                V, E = self.ctx.get_osb()
+                refio.save_data_dir(inp.VOSBFile, V)
+                refio.save_data_dir(inp.EigFile, E)
+        if log:
+            log(f" Time for block diagonalization (s): {time.perf_counter() - t0:.3f}")
+
+    # OSB_PISTCONV (osbw.pistconv.h:16-50) with setPISTConvParam (:303-333)
+    def pist(self, x0=None, seed=0, verbose=False):
+        inp = self.inp
+        mE0, mTol, mStart, mStep, mMax, mNum, mGap = inp.sConv
+        if x0 is None:
+            x0 = np.random.default_rng(seed).random(inp.my_len)   # random_number(X)
+        return self.ctx.pist(x0, mNum, mE0, mTol, startcnt=mStart, stepcnt=mStep, m_max=mMax,
+                             gap=mGap, qmr_max=inp.sQMR[0], qmr_tol=inp.sQMR[1], qmr_ntype=-1,
+                             precision=self.precision, ntype=0, verbose=verbose)
+
+    # progPistEig (osbw.progEig.h:6-98)
+    def prog_pist_eig(self, log=print, **kw):
+        t0 = time.perf_counter()
+        if log:
+            log(" ================================================")
+            log("      Get  Eigen Values Using PIST method        ")
+            log(" ================================================")
+            log(" ------  Bound states for Real Version of H0  -------")
+        st, eig, res, info = self.pist(**kw)
+        if log:
+            log(f" Max Lanczos Error: {res:.15E}  Eigen Values:")
+            for i in range(0, len(eig), 3):
+                log("  ".join(f"{e:25.15E}" for e in eig[i:i + 3]))
+            log(f" Time to get PIST Eigen values:(sec) {time.perf_counter() - t0:.3f}")
+        return st, eig, res, info
+
+    def close(self):
+        if self.ctx is not None:
+            self.ctx.close()
+            self.ctx = None
+
+
+def main(argv=None):
+    text = sys.stdin.read()
+    osb = OSB.read(text)
+    capi.load(build_if_missing=True)
+    if not osb.load_init_data():
+        print(" Error in loading data", file=sys.stderr)
+        return 1
+    osb.prog_diag()
+    st, eig, res, info = osb.prog_pist_eig(verbose=True)
+    osb.close()
+    return 0 if st > 0 else 2
+
+
+if __name__ == "__main__":
+    sys.exit(main())
