@@ -118,6 +118,23 @@ int scalit_px(scalit_ctx *ctx, int npc, int nvec, const double *X, double *Y);
 int scalit_px_device(scalit_ctx *ctx, int npc, int nvec, const double *dX, double *dY);
 int scalit_px_f32_device(scalit_ctx *ctx, int npc, int nvec, const float *dX, float *dY);
 
+/* P*X for one device vector that allocates nothing.  No counterpart in the
+ * reference: it exists for callers that cannot allocate device memory at call
+ * time -- a host code whose device memory is entirely owned by another
+ * allocator (a framework's caching pool or a preallocated arena), or a solver
+ * loop that must not trigger the implicit device synchronisation of
+ * cudaMalloc/cudaFree.  Same operator and kernels as scalit_px_device; its
+ * scratch vector is a file-scope device array of 2^20 doubles (8 MiB, held by
+ * every GPU that loads this library until the process exits), so grids larger
+ * than 1,048,576 points are rejected with SCALIT_EINVAL.  The first call on a
+ * device looks up that array's device address (cudaGetSymbolAddress) with the
+ * device current; make that first call before any stream capture.  All calls
+ * share the one array and it keeps the last call's contents (nothing in it
+ * needs to start at zero: every stage overwrites it before reading), so calls
+ * that overlap on the GPU -- two streams, or two contexts on one device --
+ * race on it. */
+int scalit_px_noalloc_device(scalit_ctx *ctx, int npc, const double *dX, double *dY);
+
 /* ------------------------------------------------------------------ QMR ---
  * OSB_QMR -> QMR / QMR_MPI (src/iterate/module/osbw.qmr.h:13-23,
  * src/iterate/libiterate/qmr/qmr.f90:5-175,

@@ -45,6 +45,7 @@ SIGNATURES = {
     "scalit_px": (C.c_int, [_vp, C.c_int, C.c_int, _dp, _dp]),
     "scalit_px_device": (C.c_int, [_vp, C.c_int, C.c_int, _vp, _vp]),
     "scalit_px_f32_device": (C.c_int, [_vp, C.c_int, C.c_int, _vp, _vp]),
+    "scalit_px_noalloc_device": (C.c_int, [_vp, C.c_int, _vp, _vp]),
     "scalit_qmr": (C.c_int, [_vp, C.c_int, C.c_int, C.c_double, C.c_int, _dp, _dp, _dp, _ip]),
     "scalit_qmr_device": (C.c_int, [_vp, C.c_int, C.c_int, C.c_double, C.c_int, _vp, _vp, _dp, _ip]),
     "scalit_pist_default_params": (None, [_vp, C.c_int, C.c_double, C.c_double, C.c_int, C.c_int,
@@ -253,6 +254,10 @@ class Context:
 
     def px_device(self, dX, dY, nvec=1, npc=TA1):
         _check(self.lib.scalit_px_device(self.h, int(npc), int(nvec), _ptr(dX), _ptr(dY)))
+
+    def px_noalloc_device(self, dX, dY, npc=TA1):
+        """P*X of one device vector with the library's static scratch (no allocation)."""
+        _check(self.lib.scalit_px_noalloc_device(self.h, int(npc), _ptr(dX), _ptr(dY)))
 
     def px_f32_device(self, dX, dY, nvec=1, npc=TA1):
         _check(self.lib.scalit_px_f32_device(self.h, int(npc), int(nvec), _ptr(dX), _ptr(dY)))
