@@ -44,6 +44,9 @@ def parse():
     ap.add_argument("--nvec", type=int, default=16)
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--pist-workload", default="tri-24x32x20",
+                    help="grid of the PIST leg ('none' skips it)")
+    ap.add_argument("--pist-levels", type=int, default=20)
     return ap.parse_args()
 
 
@@ -214,6 +217,35 @@ def run_reference(args):
     return 0
 
 
+# ------------------------------------------------------------------- PIST --
+def pist_leg(workload, levels, device, capi, hm):
+    """Wall time from the preconditioner build to converged eigenvalues, with
+    FP64 and with FP32 QMR inner solves (basis, HMAT and Ritz values in FP64)."""
+    p = hm.workload(workload)
+    e0 = float(p.RES.min())
+    x0 = np.random.default_rng(0).random(p.N)
+    out = {"workload": workload, "levels": levels}
+    eigs = {}
+    for name, prec in (("fp64", capi.PREC_FP64), ("fp32", capi.PREC_FP32)):
+        with capi.Context.from_problem(p, e0=e0, device=device) as ctx:
+            t0 = time.perf_counter()
+            ctx.build_osb(20, 1e-4)
+            t1 = time.perf_counter()
+            st, eig, res, info = ctx.pist(x0, levels, e0, 1e-11, m_max=max(20 * levels, 400),
+                                          qmr_max=2000, qmr_tol=1e-4, precision=prec)
+            t2 = time.perf_counter()
+        eigs[name] = eig
+        out[name] = {"status": st, "seconds": t2 - t0, "build_s": t1 - t0, "pist_s": t2 - t1,
+                     "levels_per_s": levels / (t2 - t0), "krylov": info["krylov"],
+                     "qmr_iterations": info["qmr_total"], "qmr_solves": info["qmr_solves"],
+                     "t_qmr": info["t_qmr"], "t_orth": info["t_orth"], "t_hmat": info["t_hmat"],
+                     "t_ritz": info["t_ritz"]}
+    out["speedup_fp32_inner"] = out["fp64"]["seconds"] / out["fp32"]["seconds"]
+    out["max_abs_diff_cm"] = float(np.abs(eigs["fp32"] - eigs["fp64"]).max() * hm.HARTREE_CM)
+    out["lowest_eigenvalues_eh"] = [float(v) for v in eigs["fp64"][:5]]
+    return out
+
+
 # ------------------------------------------------------------------- ours --
 def run_ours(args):
     import torch
@@ -322,7 +354,7 @@ def run_ours(args):
     e2e_steps = max(3, args.steps // 4)
     t0 = time.perf_counter()
     for _ in range(e2e_steps):
-        yh[...] = ctx.hx(xh, capi.TA1)
+        ctx.hx(xh, capi.TA1, out=yh)
     e2e_s = time.perf_counter() - t0
     e2e_s = reduce_max(e2e_s, world)
     e2e_value = replicas_value(e2e_steps * nvec, world, e2e_s)
@@ -330,6 +362,9 @@ def run_ours(args):
     base = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         base = cpu_baseline(p, e0, args.cpu_seconds)
+    pist = None
+    if args.pist_workload != "none" and args.pist_levels > 0:
+        pist = pist_leg(args.pist_workload, args.pist_levels, local, capi, hm)
 
     if rank == 0:
         line = {
@@ -361,6 +396,8 @@ def run_ours(args):
         }
         if base is not None:
             line["cpu_baseline"] = base
+        if pist is not None:
+            line["pist"] = pist
         print(json.dumps(line), flush=True)
     ctx.close()
     if world > 1:

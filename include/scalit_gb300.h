@@ -43,6 +43,11 @@ extern "C" {
 #define SCALIT_TOSBD1 2 /* +-1/DE inside the window |EIG0-E0| <= DE */
 #define SCALIT_TOSBD2 3 /* 1/(+-alpha + beta (EIG0-E0)) in window   */
 
+/* engine of the FP64 H*X level products */
+#define SCALIT_FP64_DFMA 0   /* FP64 pipe (strided GEMM on CUDA cores)                 */
+#define SCALIT_FP64_TENSOR 1 /* 7-bit digit slices on the BF16 tensor cores (tcgen05), */
+                             /* exact FP32 group sums, FP64 recombination (default)     */
+
 /* arithmetic of the QMR inner solves */
 #define SCALIT_PREC_FP64 0
 #define SCALIT_PREC_FP32 1
@@ -77,6 +82,10 @@ int scalit_load(scalit_ctx *ctx, const double *H0, const double *RES, const doub
  * the context's own); the _device entry points are then ordered on it. */
 void *scalit_get_stream(const scalit_ctx *ctx);
 int scalit_set_stream(scalit_ctx *ctx, void *stream);
+/* Engine of the FP64 H*X level products (SCALIT_FP64_DFMA or SCALIT_FP64_TENSOR).
+ * Levels with more than 256 points, and the per-point outer layer, always use
+ * the FP64 pipe. */
+int scalit_set_fp64_mode(scalit_ctx *ctx, int mode);
 /* sOSBW%mE0: the shift of (H - E0) and of the preconditioner. */
 int scalit_set_shift(scalit_ctx *ctx, double e0);
 /* sOSB kernel kind with sOSBW%mDE and sOSBW%mBeta. */

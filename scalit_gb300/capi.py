@@ -15,6 +15,7 @@ from . import build as _build
 TA0, TA1 = 0, 1
 TOSB, TOSBD1, TOSBD2 = 1, 2, 3
 PREC_FP64, PREC_FP32 = 0, 1
+FP64_DFMA, FP64_TENSOR = 0, 1
 FMAX = 20
 
 _dp = C.POINTER(C.c_double)
@@ -33,6 +34,7 @@ SIGNATURES = {
     "scalit_load": (C.c_int, [_vp, _dp, _dp, _dp, _dp]),
     "scalit_get_stream": (C.c_void_p, [_vp]),
     "scalit_set_stream": (C.c_int, [_vp, _vp]),
+    "scalit_set_fp64_mode": (C.c_int, [_vp, C.c_int]),
     "scalit_set_shift": (C.c_int, [_vp, C.c_double]),
     "scalit_set_precond": (C.c_int, [_vp, C.c_int, C.c_double, C.c_double]),
     "scalit_hx": (C.c_int, [_vp, C.c_int, C.c_int, _dp, _dp]),
@@ -208,16 +210,20 @@ class Context:
     def set_stream(self, stream_ptr):
         _check(self.lib.scalit_set_stream(self.h, C.c_void_p(int(stream_ptr) if stream_ptr else 0)))
 
+    def set_fp64_mode(self, mode):
+        _check(self.lib.scalit_set_fp64_mode(self.h, int(mode)))
+
     def set_shift(self, e0):
         _check(self.lib.scalit_set_shift(self.h, float(e0)))
 
     def set_precond(self, kind=TOSB, de=0.0, beta=0.0):
         _check(self.lib.scalit_set_precond(self.h, int(kind), float(de), float(beta)))
 
-    def hx(self, X, ntype=TA1):
+    def hx(self, X, ntype=TA1, out=None):
         X = _f64(X)
         nvec = X.size // self.N
-        Y = np.empty_like(X)
+        Y = np.empty_like(X) if out is None else out
+        assert Y.dtype == np.float64 and Y.flags.c_contiguous and Y.size == X.size
         _check(self.lib.scalit_hx(self.h, int(ntype), nvec, _p(X), _p(Y)))
         return Y
 

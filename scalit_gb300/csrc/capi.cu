@@ -83,6 +83,9 @@ static int ctx_base_init(scalit_ctx *c, int device)
     c->device = device;
     SC_CUDA(cudaSetDevice(device));
     SC_CUDA(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
+    SC_CUDA(cudaStreamCreateWithFlags(&c->s_in, cudaStreamNonBlocking));
+    SC_CUDA(cudaStreamCreateWithFlags(&c->s_out, cudaStreamNonBlocking));
+    for (int i = 0; i < 6; ++i) SC_CUDA(cudaEventCreateWithFlags(&c->ev[i], cudaEventDisableTiming));
     SC_CUDA(cudaMalloc(&c->red_partial, sizeof(double) * 4 * 152 * 4 + 64));
     SC_CUDA(cudaMalloc(&c->red_counter, sizeof(unsigned int) * 4));
     SC_CUDA(cudaMemset(c->red_counter, 0, sizeof(unsigned int) * 4));
@@ -112,8 +115,10 @@ static int hx_many(scalit_ctx *c, int ntype, int nvec, const T *dX, T *dY)
     if (ntype != SCALIT_TA0 && ntype != SCALIT_TA1) { set_error("ntype must be TA0 or TA1"); return SCALIT_EINVAL; }
     const T shift = ntype == SCALIT_TA0 ? T(0) : T(c->E0);
     const i64 N = c->L.N;
-    for (int v = 0; v < nvec; ++v) {
-        int rc = hx_vec<T>(c, dX + (i64)v * N, dY + (i64)v * N, shift, T(1), nullptr, c->stream);
+    // batches of at most 64 vectors per launch (grid z)
+    for (int v = 0; v < nvec; v += 64) {
+        const int nb = nvec - v < 64 ? nvec - v : 64;
+        int rc = hx_batch<T>(c, dX + (i64)v * N, dY + (i64)v * N, nb, shift, T(1), nullptr, c->stream);
         if (rc) return rc;
     }
     return 0;
@@ -157,12 +162,20 @@ void scalit_destroy(scalit_ctx *c)
     for (double *p : dptrs) if (p) cudaFree(p);
     float *fptrs[] = {c->H0f, c->RESf, c->DEPf, c->OUTHf, c->EIG0f, c->VOSBf};
     for (float *p : fptrs) if (p) cudaFree(p);
+    for (int l = 0; l < SCALIT_FMAX; ++l) {
+        if (c->tc[l].dig) cudaFree(c->tc[l].dig);
+        if (c->tc[l].exps) cudaFree(c->tc[l].exps);
+    }
+    if (c->tc_err) cudaFree(c->tc_err);
     if (c->red_counter) cudaFree(c->red_counter);
     if (c->work) cudaFree(c->work);
     if (c->h_pinned) cudaFreeHost(c->h_pinned);
     if (c->cusolver) cusolverDnDestroy((cusolverDnHandle_t)c->cusolver);
     if (c->own_stream) c->stream = c->own_stream;
     if (c->stream) cudaStreamDestroy(c->stream);
+    if (c->s_in) { cudaStreamSynchronize(c->s_in); cudaStreamDestroy(c->s_in); }
+    if (c->s_out) { cudaStreamSynchronize(c->s_out); cudaStreamDestroy(c->s_out); }
+    for (int i = 0; i < 6; ++i) if (c->ev[i]) cudaEventDestroy(c->ev[i]);
     delete c;
 }
 
@@ -242,8 +255,18 @@ int scalit_load(scalit_ctx *c, const double *H0, const double *RES, const double
     if (!rc) rc = up(c->EIG0, c->EIG0f, RES, L.N);
     if (rc) return rc;
     SC_CUDA(cudaStreamSynchronize(s));
+    rc = tc_prepare(c);
+    if (rc) return rc;
     c->loaded = true;
     c->osb_built = false;
+    return 0;
+}
+
+int scalit_set_fp64_mode(scalit_ctx *c, int mode)
+{
+    if (!c) { set_error("null context"); return SCALIT_EINVAL; }
+    if (mode != SCALIT_FP64_DFMA && mode != SCALIT_FP64_TENSOR) { set_error("unknown FP64 mode %d", mode); return SCALIT_EINVAL; }
+    c->fp64_mode = mode;
     return 0;
 }
 
@@ -307,18 +330,38 @@ int scalit_hx(scalit_ctx *c, int ntype, int nvec, const double *X, double *Y)
 {
     CTX_CHECK(c);
     if (nvec <= 0) return nvec < 0 ? (set_error("nvec < 0"), SCALIT_EINVAL) : 0;
+    if (!c->loaded) { set_error("H*X before scalit_load"); return SCALIT_ESTATE; }
+    // Chunks of vectors in two device buffer sets; the copy-in of chunk k+1 and
+    // the copy-out of chunk k-1 overlap the product of chunk k (three streams).
     const i64 N = c->L.N;
+    const i64 target = (64LL << 20) / (8 * N);
+    int G = (int)std::max<i64>(1, std::min<i64>(target, 64));
+    if (nvec >= 2) G = std::min(G, (nvec + 1) / 2);
+    G = std::min(G, nvec);
     double *w = nullptr;
-    int rc = work_get(c, sizeof(double) * 2 * (size_t)N, (void **)&w);
+    int rc = work_get(c, sizeof(double) * 4 * (size_t)G * N, (void **)&w);
     if (rc) return rc;
-    for (int v = 0; v < nvec; ++v) {
-        SC_CUDA(cudaMemcpyAsync(w, X + (i64)v * N, sizeof(double) * N, cudaMemcpyHostToDevice, c->stream));
-        rc = hx_many<double>(c, ntype, 1, w, w + N);
+    double *Xd[2] = {w, w + (i64)G * N}, *Yd[2] = {w + 2 * (i64)G * N, w + 3 * (i64)G * N};
+    cudaEvent_t *ev = c->ev;   // [in0, in1, comp0, comp1, out0, out1]
+    for (int v0 = 0, k = 0; v0 < nvec; v0 += G, ++k) {
+        const int b = k & 1;
+        const int nb = std::min(G, nvec - v0);
+        const size_t bytes = sizeof(double) * (size_t)nb * N;
+        SC_CUDA(cudaStreamWaitEvent(c->s_in, ev[2 + b], 0));
+        SC_CUDA(cudaMemcpyAsync(Xd[b], X + (i64)v0 * N, bytes, cudaMemcpyHostToDevice, c->s_in));
+        SC_CUDA(cudaEventRecord(ev[b], c->s_in));
+        SC_CUDA(cudaStreamWaitEvent(c->stream, ev[b], 0));
+        SC_CUDA(cudaStreamWaitEvent(c->stream, ev[4 + b], 0));
+        rc = hx_many<double>(c, ntype, nb, Xd[b], Yd[b]);
         if (rc) return rc;
-        SC_CUDA(cudaMemcpyAsync(Y + (i64)v * N, w + N, sizeof(double) * N, cudaMemcpyDeviceToHost, c->stream));
+        SC_CUDA(cudaEventRecord(ev[2 + b], c->stream));
+        SC_CUDA(cudaStreamWaitEvent(c->s_out, ev[2 + b], 0));
+        SC_CUDA(cudaMemcpyAsync(Y + (i64)v0 * N, Yd[b], bytes, cudaMemcpyDeviceToHost, c->s_out));
+        SC_CUDA(cudaEventRecord(ev[4 + b], c->s_out));
     }
+    SC_CUDA(cudaStreamSynchronize(c->s_out));
     SC_CUDA(cudaStreamSynchronize(c->stream));
-    return 0;
+    return tc_check_error(c);
 }
 
 // --------------------------------------------------------------- P * X ---
@@ -513,6 +556,15 @@ static int level_host(int nin, int nout, int blk, const double *H, const double 
 {
     scalit_ctx *c = scratch();
     if (!c) return SCALIT_ECUDA;
+    std::vector<double> Ht;
+    if (transpose && nin == 1) {
+        // H^T X for single-point blocks: transpose the small matrix on the host
+        Ht.resize((size_t)nout * nout);
+        for (int i = 0; i < nout; ++i)
+            for (int j = 0; j < nout; ++j) Ht[i + (size_t)nout * j] = H[j + (size_t)nout * i];
+        H = Ht.data();
+        transpose = 0;
+    }
     const i64 n = (i64)nin * nout * blk;
     Scoped sb(c->stream);
     double *dH = sb.get<double>((i64)nout * nout), *dX = sb.get<double>(n), *dY = sb.get<double>(n);
@@ -526,17 +578,9 @@ static int level_host(int nin, int nout, int blk, const double *H, const double 
     if (nin == 1) {
         g.M = nout; g.N = blk; g.Mi = nout; g.s1 = 1; g.s2 = 0;
         g.A = dH;
-        if (!transpose) { g.a_sk = nout; } else { g.s1 = nout; g.a_sk = 1; }
+        g.a_sk = nout;
         g.B = dX; g.b_sk = 1; g.b_sn = nout; g.c_sn = nout;
-        if (transpose) {
-            // moff is shared by A and C; use the batched GEMV for V^T-style products.
-            int rc = level_rotate<double>(1, nout, blk, dH, dX, dY, 1, nullptr, c->stream);
-            if (rc) return rc;
-            SC_CUDA(cudaMemcpyAsync(Y, dY, sizeof(double) * n, cudaMemcpyDeviceToHost, c->stream));
-            SC_CUDA(cudaStreamSynchronize(c->stream));
-            return 0;
-        }
-        (void)dC;
+        if (dC) { set_error("a dependent single-point level is a scaled product"); return SCALIT_EINVAL; }
     } else {
         g.M = nin * blk; g.N = nout; g.Mi = nin; g.s1 = 1; g.s2 = (i64)nin * nout;
         g.A = dX; g.a_sk = nin;

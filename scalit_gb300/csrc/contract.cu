@@ -14,17 +14,24 @@
 // memory with a register prefetch of the next K slab.
 #include "internal.cuh"
 
+#include <type_traits>
+
 namespace sc {
 
-template <class T> struct Tile;
-template <> struct Tile<double> { static constexpr int BM = 64, BN = 64, BK = 16, TM = 4, TN = 4; };
-template <> struct Tile<float> { static constexpr int BM = 128, BN = 128, BK = 8, TM = 8, TN = 8; };
+// Tile shapes: 256 threads, TM x TN outputs per thread.  The small tiles are
+// used when the large ones would give the launch fewer than about three waves
+// of CTAs on the 152 SMs (a single-vector level has only a few hundred tiles).
+template <int BM_, int BN_, int BK_, int TM_, int TN_> struct TileCfg {
+    static constexpr int BM = BM_, BN = BN_, BK = BK_, TM = TM_, TN = TN_;
+};
+template <class T> struct Tiles;
+template <> struct Tiles<double> { using Big = TileCfg<64, 64, 16, 4, 4>; using Small = TileCfg<32, 32, 16, 2, 2>; };
+template <> struct Tiles<float> { using Big = TileCfg<128, 128, 8, 8, 8>; using Small = TileCfg<64, 64, 8, 4, 4>; };
 
-template <class T>
+template <class T, class TL>
 __global__ void __launch_bounds__(256)
 gemm_kernel(GemmArgs<T> g)
 {
-    using TL = Tile<T>;
     constexpr int BM = TL::BM, BN = TL::BN, BK = TL::BK, TM = TL::TM, TN = TL::TN;
     constexpr int NT = 256;
     constexpr int A_PER = BM * BK / NT;   // A elements each thread loads per slab
@@ -128,23 +135,31 @@ gemm_kernel(GemmArgs<T> g)
             if (n >= g.N) continue;
             const i64 p = moff + (i64)n * g.c_sn;
             T v = sc * acc[i][j];
-            if (g.diagV) v = fma(g.alpha * (g.diagV[p] - g.shift), g.diagX[p], v);
+            if (g.diagV) v = fma(g.alpha * (g.diagV[p] - g.shift), g.diagX[p + (i64)z * g.dx_sz], v);
             if (g.accumulate) v += Cp[p];
             Cp[p] = v;
         }
     }
 }
 
-template <class T> int launch_gemm(const GemmArgs<T> &g, cudaStream_t s)
+template <class T, class TL> static int launch_tiles(const GemmArgs<T> &g, cudaStream_t s)
 {
-    using TL = Tile<T>;
-    if (g.M <= 0 || g.N <= 0 || g.batch <= 0) return 0;
-    if (g.batch > 65535) { set_error("gemm batch %d too large", g.batch); return SCALIT_EINVAL; }
     dim3 grid((g.M + TL::BM - 1) / TL::BM, (g.N + TL::BN - 1) / TL::BN, g.batch);
     if (grid.y > 65535) { set_error("gemm N=%d too large", g.N); return SCALIT_EINVAL; }
-    gemm_kernel<T><<<grid, 256, 0, s>>>(g);
+    gemm_kernel<T, TL><<<grid, 256, 0, s>>>(g);
     SC_CHECK_LAUNCH();
     return 0;
+}
+
+template <class T> int launch_gemm(const GemmArgs<T> &g, cudaStream_t s)
+{
+    using Big = typename Tiles<T>::Big;
+    using Small = typename Tiles<T>::Small;
+    if (g.M <= 0 || g.N <= 0 || g.batch <= 0) return 0;
+    if (g.batch > 65535) { set_error("gemm batch %d too large", g.batch); return SCALIT_EINVAL; }
+    const i64 big_ctas = (i64)((g.M + Big::BM - 1) / Big::BM) * ((g.N + Big::BN - 1) / Big::BN) * g.batch;
+    if (big_ctas < 3 * 2 * 152) return launch_tiles<T, Small>(g, s);
+    return launch_tiles<T, Big>(g, s);
 }
 
 template int launch_gemm<double>(const GemmArgs<double> &, cudaStream_t);
@@ -174,11 +189,12 @@ __global__ void h3x_kernel(int nin, int nout, const T *__restrict__ Am, const T 
 template <class T>
 int level_apply(const scalit_ctx *c, int l, const T *H0, const T *DEP, const T *OUTH, const T *X,
                 T *Y, int accumulate, const T *diagV, T shift, T alpha, const int *gate,
-                cudaStream_t s)
+                cudaStream_t s, int nvec)
 {
     const Layout &L = c->L;
     const int nout = L.n[l];
-    const i64 nin = L.dim[l], blk = L.blk[l];
+    const i64 nin = L.dim[l], blk = L.blk[l], N = L.N;
+    if (nvec < 1) return 0;
     if (L.ndvr && l == L.nlev - 1) {
         // Outer per-point matrices; the diagonal term, if requested, is a
         // separate pass (the outermost level is never the first applied).
@@ -186,39 +202,43 @@ int level_apply(const scalit_ctx *c, int l, const T *H0, const T *DEP, const T *
         const i64 total = nin * nout;
         const int threads = 256;
         const int blocks = (int)((total + threads - 1) / threads < 152 * 16 ? (total + threads - 1) / threads : 152 * 16);
-        h3x_kernel<T><<<blocks, threads, 0, s>>>((int)nin, nout, OUTH, X, Y, accumulate, alpha, gate);
-        SC_CHECK_LAUNCH();
+        for (int v = 0; v < nvec; ++v) {
+            h3x_kernel<T><<<blocks, threads, 0, s>>>((int)nin, nout, OUTH, X + (i64)v * N, Y + (i64)v * N,
+                                                     accumulate, alpha, gate);
+            SC_CHECK_LAUNCH();
+        }
         return 0;
     }
     GemmArgs<T> g{};
     g.K = nout;
-    g.batch = 1;
+    g.batch = nvec;
     g.accumulate = accumulate;
     g.alpha = alpha;
     g.diagV = diagV;
     g.diagX = X;
+    g.dx_sz = N;
     g.shift = shift;
     g.gate = gate;
     g.C = Y;
-    g.c_sz = 0; g.a_sz = 0; g.b_sz = 0;
+    g.c_sz = N;
     const T *H = H0 + L.h0s[l];
     if (nin == 1) {
         // Y(i, b) = sum_j H(i, j) X(j, b): A = H (col-major), B = X.
         g.M = nout; g.N = (int)blk;
         g.Mi = nout; g.s1 = 1; g.s2 = 0;
-        g.A = H; g.a_sk = nout;
-        g.B = X; g.b_sk = 1; g.b_sn = nout;
+        g.A = H; g.a_sk = nout; g.a_sz = 0;
+        g.B = X; g.b_sk = 1; g.b_sn = nout; g.b_sz = N;
         g.c_sn = nout;
         g.rowscale = nullptr;
-        if (blk > 65535LL * Tile<T>::BN) { set_error("level %d too many blocks", l + 1); return SCALIT_EINVAL; }
+        if (blk > 65535LL * Tiles<T>::Small::BN) { set_error("level %d too many blocks", l + 1); return SCALIT_EINVAL; }
     } else {
         // Y(a, i, b) = s(a) sum_j X(a, j, b) H(i, j): A = X with (a, b) folded, B = H^T.
         const i64 M = nin * blk;
         if (M > 2147483647LL) { set_error("level %d too large", l + 1); return SCALIT_EINVAL; }
         g.M = (int)M; g.N = nout;
         g.Mi = nin; g.s1 = 1; g.s2 = nin * nout;
-        g.A = X; g.a_sk = nin;
-        g.B = H; g.b_sk = nout; g.b_sn = 1;
+        g.A = X; g.a_sk = nin; g.a_sz = N;
+        g.B = H; g.b_sk = nout; g.b_sn = 1; g.b_sz = 0;
         g.c_sn = nin;
         g.rowscale = L.dep[l] ? DEP + L.deps[l] : nullptr;
     }
@@ -242,7 +262,8 @@ template <> const double *pick<double>(const scalit_ctx *, const double *d, cons
 template <> const float *pick<float>(const scalit_ctx *, const double *, const float *f) { return f; }
 
 template <class T>
-int hx_vec(const scalit_ctx *c, const T *X, T *Y, T shift, T alpha, const int *gate, cudaStream_t s)
+int hx_batch(const scalit_ctx *c, const T *X, T *Y, int nvec, T shift, T alpha, const int *gate,
+             cudaStream_t s)
 {
     const Layout &L = c->L;
     const T *H0 = pick<T>(c, c->H0, c->H0f);
@@ -253,23 +274,42 @@ int hx_vec(const scalit_ctx *c, const T *X, T *Y, T shift, T alpha, const int *g
     int first = 0;
     if (L.ndvr && L.nlev == 1) {
         const int threads = 256;
-        diag_kernel<T><<<(int)((L.N + threads - 1) / threads), threads, 0, s>>>(L.N, RES, shift, alpha, X, Y, 0, gate);
-        SC_CHECK_LAUNCH();
+        for (int v = 0; v < nvec; ++v) {
+            diag_kernel<T><<<(int)((L.N + threads - 1) / threads), threads, 0, s>>>(
+                L.N, RES, shift, alpha, X + (i64)v * L.N, Y + (i64)v * L.N, 0, gate);
+            SC_CHECK_LAUNCH();
+        }
         first = 1;
     }
     for (int l = 0; l < L.nlev; ++l) {
         const bool fuse_diag = (l == 0 && !first);
+        if constexpr (std::is_same<T, double>::value) {
+            if (c->fp64_mode == SCALIT_FP64_TENSOR && tc_usable(c, l)) {
+                rc = tc_level_apply(c, l, X, Y, l > 0 || first, fuse_diag ? RES : nullptr, shift, alpha,
+                                    gate, s, nvec);
+                if (rc) return rc;
+                continue;
+            }
+        }
         rc = level_apply<T>(c, l, H0, DEP, OUTH, X, Y, /*accumulate=*/l > 0 || first,
-                            fuse_diag ? RES : nullptr, shift, alpha, gate, s);
+                            fuse_diag ? RES : nullptr, shift, alpha, gate, s, nvec);
         if (rc) return rc;
     }
     return 0;
 }
 
+template <class T>
+int hx_vec(const scalit_ctx *c, const T *X, T *Y, T shift, T alpha, const int *gate, cudaStream_t s)
+{
+    return hx_batch<T>(c, X, Y, 1, shift, alpha, gate, s);
+}
+
+template int hx_batch<double>(const scalit_ctx *, const double *, double *, int, double, double, const int *, cudaStream_t);
+template int hx_batch<float>(const scalit_ctx *, const float *, float *, int, float, float, const int *, cudaStream_t);
 template int hx_vec<double>(const scalit_ctx *, const double *, double *, double, double, const int *, cudaStream_t);
 template int hx_vec<float>(const scalit_ctx *, const float *, float *, float, float, const int *, cudaStream_t);
-template int level_apply<double>(const scalit_ctx *, int, const double *, const double *, const double *, const double *, double *, int, const double *, double, double, const int *, cudaStream_t);
-template int level_apply<float>(const scalit_ctx *, int, const float *, const float *, const float *, const float *, float *, int, const float *, float, float, const int *, cudaStream_t);
+template int level_apply<double>(const scalit_ctx *, int, const double *, const double *, const double *, const double *, double *, int, const double *, double, double, const int *, cudaStream_t, int);
+template int level_apply<float>(const scalit_ctx *, int, const float *, const float *, const float *, const float *, float *, int, const float *, float, float, const int *, cudaStream_t, int);
 
 // ------------------------------------------------------------------------
 // VX / VTX (src/iterate/libiterate/hpx/hpx.f90:40-73) out of place:

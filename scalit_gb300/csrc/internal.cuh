@@ -49,12 +49,21 @@ template <class T> struct DevBuf {
 
 }  // namespace sc
 
+// Tensor-core plan of one level: the level matrix cut into 7 BF16 digit planes.
+struct TcLevelData {
+    uint16_t *dig = nullptr;   // [ntiles][KS][7][NT x 16] BF16 bits
+    int *exps = nullptr;       // [ntiles * NT] column exponents
+    int NT = 0, ntiles = 0, KS = 0, usable = 0;
+};
+
 // The opaque context of the C ABI.
 struct scalit_ctx {
     sc::Layout L;
     int device = 0;
     cudaStream_t stream = nullptr;
     cudaStream_t own_stream = nullptr;   // the context's own stream while a caller's is set
+    cudaStream_t s_in = nullptr, s_out = nullptr;   // host<->device copy streams
+    cudaEvent_t ev[6] = {};                          // copy/compute ordering events
     // FP64 operator data (module globals H0/RES/DEP/OUTH/EIG0/VOSB in the reference)
     double *H0 = nullptr, *RES = nullptr, *DEP = nullptr, *OUTH = nullptr;
     double *EIG0 = nullptr, *VOSB = nullptr;
@@ -74,6 +83,10 @@ struct scalit_ctx {
     double *red_result = nullptr;   // device scalars of the last reductions
     double *h_pinned = nullptr;     // pinned host mirror for scalar readback
     void *cusolver = nullptr;       // cusolverDnHandle_t
+    // FP64 H*X engine: SCALIT_FP64_DFMA (FP64 pipe) or SCALIT_FP64_TENSOR (digit-sliced tcgen05)
+    int fp64_mode = SCALIT_FP64_TENSOR;
+    TcLevelData tc[SCALIT_FMAX];
+    int *tc_err = nullptr;
 };
 
 namespace sc {
@@ -99,6 +112,7 @@ template <class T> struct GemmArgs {
     T alpha;
     const T *diagV;        // may be null
     const T *diagX;
+    i64 dx_sz;             // batch stride of diagX
     T shift;
     const int *gate;       // if non-null and *gate != 0 the kernel does nothing
 };
@@ -109,7 +123,12 @@ template <class T> int launch_gemm(const GemmArgs<T> &g, cudaStream_t s);
 template <class T>
 int level_apply(const scalit_ctx *c, int level, const T *H0, const T *DEP, const T *OUTH,
                 const T *X, T *Y, int accumulate, const T *diagV, T shift, T alpha,
-                const int *gate, cudaStream_t s);
+                const int *gate, cudaStream_t s, int nvec = 1);
+
+// The whole operator on nvec vectors stored back to back (one launch per level).
+template <class T>
+int hx_batch(const scalit_ctx *c, const T *X, T *Y, int nvec, T shift, T alpha, const int *gate,
+             cudaStream_t s);
 
 // Whole operator for one vector: Y = alpha * ((V - shift) X + sum_l H_l X).
 template <class T>
@@ -125,6 +144,14 @@ int px_vec(const scalit_ctx *c, int npc, const T *X, T *Y, T *tmp, T alpha, cons
 template <class T>
 int level_rotate(int nin, int nout, int blk, const T *V, const T *X, T *Y, int transpose,
                  const int *gate, cudaStream_t s);
+
+// ------------------------------------------------------- tensor-core FP64 --
+int tc_prepare(scalit_ctx *c);
+bool tc_usable(const scalit_ctx *c, int level);
+int tc_level_apply(const scalit_ctx *c, int level, const double *X, double *Y, int accumulate,
+                   const double *diagV, double shift, double alpha, const int *gate, cudaStream_t s,
+                   int nvec);
+int tc_check_error(scalit_ctx *c);
 
 // ------------------------------------------------------------- OSB build --
 int osb_build(scalit_ctx *c, int bjmax, double bjtol, double *stats);

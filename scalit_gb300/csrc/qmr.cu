@@ -463,7 +463,7 @@ int qmr_core(scalit_ctx *c, i64 n, QmrOps<T> &ops, int ntype, int qmrmax, double
     out->res = h.RES;
     out->iters = h.iters;
     out->breakdown = h.breakdown;
-    return 0;
+    return tc_check_error(c);
 }
 
 template int qmr_core<double>(scalit_ctx *, i64, QmrOps<double> &, int, int, double, const double *, double *, QmrResult *);

@@ -1,0 +1,415 @@
+// FP64-accurate level contractions of H*X on the tcgen05 tensor cores.
+//
+// GB300's FP64 pipe delivers ~1.1 TFLOP/s while its BF16 tensor cores deliver
+// ~2 PFLOP/s, so the FP64 level GEMMs  C(m, n) = sum_k A(m, k) B(k, n)
+// (A = the grid vector viewed through the level's strides, B(k, n) = H(n, k))
+// are computed exactly enough for FP64 from 7-bit integer digits:
+//
+//   A(m, k) = 2^e_m  sum_{s=0..6} a_s(m, k) 2^-7(s+1),   |a_s| <= 127   (e_m: row exponent)
+//   B(k, n) = 2^e_n  sum_{t=0..6} b_t(k, n) 2^-7(t+1),   |b_t| <= 127   (e_n: column exponent)
+//   C(m, n) = 2^(e_m+e_n-14) sum_{g=0..6} 2^-7g G_g(m, n),
+//   G_g = sum_{s+t=g} sum_k a_s b_t          (28 digit pairs)
+//
+// Every digit is an integer of at most 7 bits, exact in BF16; a product is at
+// most 2^14 and a group of g+1 pairs over K <= 160 stays below 2^24, so the
+// FP32 tensor-core accumulation of groups 0..5 is exact (group 6 sits 2^-42
+// below group 0, where FP32 rounding is immaterial).  The dropped digits and
+// pairs leave a relative error of ~2^-46 of |A||B|.  Each group accumulates
+// in its own TMEM accumulator; the epilogue reads them with tcgen05.ld and
+// recombines them in FP64.
+//
+// Structure of a CTA (128 threads, one M tile of 128 grid rows, one N tile):
+// each thread owns one row: it finds the row's exponent, then for every
+// 16-wide K step cuts its 16 values into 7 digit planes written to shared
+// memory in the K-major canonical layout (8x16-byte core matrices, no
+// swizzle); the K step's pre-cut B digit planes are copied next to them;
+// thread 0 issues the 28 tcgen05.mma (kind::f16, BF16 x BF16 -> FP32) and a
+// tcgen05.commit on the buffer's mbarrier.  Two buffers let the cutting of
+// step k+1 overlap the MMAs of step k.  Every mbarrier wait is bounded: on
+// expiry the kernel records an error, waits (bounded) for its MMAs, frees its
+// TMEM and returns.
+#include "internal.cuh"
+
+#include <cuda_bf16.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+namespace sc {
+
+static constexpr int kDigits = 7;
+static constexpr int kGroups = 7;
+static constexpr int kBM = 128;
+static constexpr int kThreadsTC = 128;
+static constexpr int kTmemCols = 512;
+static constexpr int kAStepBytes = kDigits * kBM * 16 * 2;    // 7 digit planes of 128 x 16 BF16
+static constexpr long long kWaitLimit = 1LL << 24;            // mbarrier polls before giving up
+
+struct TcArgs {
+    int M, N, K, KS, NT;
+    i64 Mi, s1, s2, a_sk, c_sn;
+    const double *A; i64 a_sz;
+    double *C; i64 c_sz;
+    const double *rowscale;
+    int accumulate;
+    double alpha;
+    const double *diagV;
+    const double *diagX;
+    i64 dx_sz;
+    double shift;
+    const int *gate;
+    int *err;
+    const uint4 *bdig;    // [ntile][ks][digit][NT x 16 BF16, canonical]
+    const int *bexp;      // [ntile * NT] column exponents
+};
+
+__device__ __forceinline__ uint32_t smem_addr(const void *p)
+{
+    return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+
+// Shared-memory matrix descriptor, K-major, no swizzle: start address, the
+// byte distance between core matrices along K (LBO) and along M/N (SBO).
+__device__ __forceinline__ uint64_t smem_desc(uint32_t saddr, uint32_t lbo, uint32_t sbo)
+{
+    uint64_t d = 0;
+    d |= (uint64_t)((saddr & 0x3FFFFu) >> 4);
+    d |= (uint64_t)((lbo >> 4) & 0x3FFFu) << 16;
+    d |= (uint64_t)((sbo >> 4) & 0x3FFFu) << 32;
+    d |= (uint64_t)1 << 46;   // descriptor version for tcgen05
+    return d;                 // base offset 0, relative LBO, no swizzle
+}
+
+// Instruction descriptor, kind::f16: D = F32, A = B = BF16, both K-major, M = 128.
+__host__ __device__ constexpr uint32_t idesc_bf16(int n)
+{
+    return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(n >> 3) << 17) | ((uint32_t)(kBM >> 4) << 24);
+}
+
+__device__ __forceinline__ void tc_mma(uint32_t d_tmem, uint64_t adesc, uint64_t bdesc, uint32_t idesc,
+                                       uint32_t accumulate)
+{
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "setp.ne.b32 p, %4, 0;\n\t"
+        "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}\n"
+        :: "r"(d_tmem), "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate));
+}
+
+__device__ __forceinline__ void tc_commit(uint64_t *mbar)
+{
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];"
+                 :: "r"(smem_addr(mbar)) : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try(uint64_t *mbar, uint32_t parity)
+{
+    uint32_t ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.b32 %0, 1, 0, p;\n\t}\n"
+        : "=r"(ok) : "r"(smem_addr(mbar)), "r"(parity) : "memory");
+    return ok != 0;
+}
+
+__device__ __forceinline__ bool mbar_wait(uint64_t *mbar, uint32_t parity)
+{
+    for (long long i = 0; i < kWaitLimit; ++i)
+        if (mbar_try(mbar, parity)) return true;
+    return false;
+}
+
+__device__ __forceinline__ void fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float (&v)[16])
+{
+    uint32_t r[16];
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x16.b32 "
+        "{%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, %15}, [%16];"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+          "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+        : "r"(taddr));
+    #pragma unroll
+    for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
+}
+
+__device__ __forceinline__ uint16_t bf16_bits(double d)
+{
+    return __bfloat16_as_ushort(__float2bfloat16_rn((float)d));
+}
+
+__global__ void __launch_bounds__(kThreadsTC, 1)
+tc_level_kernel(TcArgs g)
+{
+    if (g.gate && *g.gate) return;
+    extern __shared__ __align__(1024) unsigned char smem[];
+    const int NT = g.NT, KS = g.KS;
+    const int bstep = kDigits * NT * 32;                   // bytes of one K step of B digits
+    unsigned char *Abuf = smem;                            // 2 x kAStepBytes
+    unsigned char *Bbuf = smem + 2 * kAStepBytes;          // 2 x bstep
+    uint64_t *mbar = reinterpret_cast<uint64_t *>(Bbuf + 2 * bstep);
+    uint32_t *tslot = reinterpret_cast<uint32_t *>(mbar + 2);
+
+    const int tid = threadIdx.x, warp = tid >> 5;
+    const int m0 = blockIdx.x * kBM, ntile = blockIdx.y, z = blockIdx.z;
+    const double *A = g.A + (i64)z * g.a_sz;
+    double *C = g.C + (i64)z * g.c_sz;
+
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;"
+                     :: "r"(smem_addr(tslot)), "r"(kTmemCols) : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    if (tid == 0) {
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" :: "r"(smem_addr(&mbar[0])) : "memory");
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" :: "r"(smem_addr(&mbar[1])) : "memory");
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+
+    // this thread's grid row and its exponent
+    const int m = m0 + tid;
+    const bool mvalid = m < g.M;
+    const i64 moff = mvalid ? (i64)(m % g.Mi) * g.s1 + (i64)(m / g.Mi) * g.s2 : 0;
+    double mx = 0.0;
+    if (mvalid)
+        for (int k = 0; k < g.K; ++k) mx = fmax(mx, fabs(A[moff + (i64)k * g.a_sk]));
+    int em = 0;
+    if (mx > 0.0) frexp(mx, &em);
+    const double to_digits = ldexp(1.0, 7 - em);
+
+    fence_before();
+    __syncthreads();
+    fence_after();
+    const uint32_t tbase = *tslot;
+    const uint32_t idesc = idesc_bf16(NT);
+    bool ok = true;
+
+    for (int ks = 0; ks < KS; ++ks) {
+        const int buf = ks & 1;
+        if (ks >= 2 && !mbar_wait(&mbar[buf], ((ks - 2) >> 1) & 1)) { ok = false; break; }
+        unsigned char *Ab = Abuf + buf * kAStepBytes;
+        unsigned char *Bb = Bbuf + buf * bstep;
+        // cut this row's 16 values of the K step into 7 digit planes
+        double r[16];
+        #pragma unroll
+        for (int j = 0; j < 16; ++j) {
+            const int k = ks * 16 + j;
+            r[j] = (mvalid && k < g.K) ? A[moff + (i64)k * g.a_sk] * to_digits : 0.0;
+        }
+        const int rowoff = (tid >> 3) * 256 + (tid & 7) * 16;
+        #pragma unroll
+        for (int s = 0; s < kDigits; ++s) {
+            uint32_t w[8];
+            #pragma unroll
+            for (int j = 0; j < 16; j += 2) {
+                const double d0 = trunc(r[j]), d1 = trunc(r[j + 1]);
+                r[j] = (r[j] - d0) * 128.0;
+                r[j + 1] = (r[j + 1] - d1) * 128.0;
+                w[j >> 1] = (uint32_t)bf16_bits(d0) | ((uint32_t)bf16_bits(d1) << 16);
+            }
+            unsigned char *plane = Ab + s * (kBM * 32);
+            *reinterpret_cast<uint4 *>(plane + rowoff) = make_uint4(w[0], w[1], w[2], w[3]);
+            *reinterpret_cast<uint4 *>(plane + rowoff + 128) = make_uint4(w[4], w[5], w[6], w[7]);
+        }
+        // the K step's B digit planes (pre-cut, already in the canonical layout)
+        const uint4 *src = g.bdig + ((i64)ntile * KS + ks) * (bstep / 16);
+        uint4 *dst = reinterpret_cast<uint4 *>(Bb);
+        for (int i = tid; i < bstep / 16; i += kThreadsTC) dst[i] = src[i];
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        fence_before();
+        __syncthreads();
+        fence_after();
+        if (tid == 0) {
+            #pragma unroll 1
+            for (int s = 0; s < kDigits; ++s) {
+                const uint64_t ad = smem_desc(smem_addr(Ab + s * (kBM * 32)), 128, 256);
+                #pragma unroll 1
+                for (int t = 0; t + s < kGroups; ++t) {
+                    const uint64_t bd = smem_desc(smem_addr(Bb + t * (NT * 32)), 128, 256);
+                    const uint32_t acc = (ks > 0 || s > 0) ? 1u : 0u;
+                    tc_mma(tbase + (uint32_t)((s + t) * NT), ad, bd, idesc, acc);
+                }
+            }
+            tc_commit(&mbar[buf]);
+        }
+    }
+    if (ok) ok = mbar_wait(&mbar[(KS - 1) & 1], ((KS - 1) >> 1) & 1);
+    if (!ok) {
+        if (g.err) atomicExch(g.err, 1);
+        // give in-flight MMAs a bounded chance to drain before freeing TMEM
+        for (int b = 0; b < 2; ++b) mbar_wait(&mbar[b], 0) || mbar_wait(&mbar[b], 1);
+    }
+    fence_after();
+
+    if (ok) {
+        // epilogue: thread tid holds TMEM lane tid = grid row m
+        const double row_scale = ldexp(1.0, em - 14);
+        const double rs = (g.rowscale && mvalid) ? g.rowscale[m % g.Mi] : 1.0;
+        const double sc = g.alpha * rs;
+        const uint32_t lane_base = (uint32_t)(warp * 32) << 16;
+        for (int c0 = 0; c0 < NT; c0 += 16) {
+            float gv[kGroups][16];
+            #pragma unroll
+            for (int q = 0; q < kGroups; ++q) tmem_ld16(tbase + lane_base + (uint32_t)(q * NT + c0), gv[q]);
+            asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+            if (!mvalid) continue;
+            #pragma unroll
+            for (int j = 0; j < 16; ++j) {
+                const int n = ntile * NT + c0 + j;
+                if (n >= g.N) continue;
+                double acc = (double)gv[kGroups - 1][j];
+                #pragma unroll
+                for (int q = kGroups - 2; q >= 0; --q) acc = fma(acc, 0.0078125, (double)gv[q][j]);
+                const double val = acc * row_scale * ldexp(1.0, g.bexp[n]);
+                const i64 p = moff + (i64)n * g.c_sn;
+                double out = sc * val;
+                if (g.diagV) out = fma(g.alpha * (g.diagV[p] - g.shift), g.diagX[p + (i64)z * g.dx_sz], out);
+                if (g.accumulate) out += C[p];
+                C[p] = out;
+            }
+        }
+    }
+    fence_before();
+    __syncthreads();
+    if (warp == 0)
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" :: "r"(tbase), "r"(kTmemCols) : "memory");
+}
+
+// ------------------------------------------------------------------ host --
+// Digit planes of one level matrix: B(k, n) = H(n, k), per column n an
+// exponent e_n with |B(k, n)| < 2^e_n, then 7 digits per value.  Packed per
+// (N tile, K step, digit) as NT x 16 BF16 in the canonical K-major layout.
+static void cut_level_matrix(const double *H, int nout, int NT, int ntiles, int KS, std::vector<uint16_t> &dig,
+                             std::vector<int> &exps)
+{
+    const int KP = KS * 16;
+    dig.assign((size_t)ntiles * KS * kDigits * NT * 16, 0);
+    exps.assign((size_t)ntiles * NT, 0);
+    for (int n = 0; n < nout; ++n) {
+        double mx = 0.0;
+        for (int k = 0; k < nout; ++k) mx = std::max(mx, std::fabs(H[n + (size_t)nout * k]));
+        int e = 0;
+        if (mx > 0.0) std::frexp(mx, &e);
+        exps[n] = e;
+        const int tile = n / NT, nn = n % NT;
+        for (int k = 0; k < KP; ++k) {
+            double r = (k < nout) ? std::ldexp(H[n + (size_t)nout * k], 7 - e) : 0.0;
+            const int ks = k / 16, kk = k % 16;
+            for (int t = 0; t < kDigits; ++t) {
+                const double d = std::trunc(r);
+                r = (r - d) * 128.0;
+                const float f = (float)d;
+                uint32_t u;
+                std::memcpy(&u, &f, 4);
+                const uint16_t bits = (uint16_t)(u >> 16);   // exact: |d| <= 127
+                const size_t base = (((size_t)tile * KS + ks) * kDigits + t) * (size_t)NT * 16;
+                const size_t off = (size_t)(nn >> 3) * 128 + (size_t)(kk >> 3) * 64 + (size_t)(nn & 7) * 8 + (kk & 7);
+                dig[base + off] = bits;
+            }
+        }
+    }
+}
+
+int tc_prepare(scalit_ctx *c)
+{
+    const Layout &L = c->L;
+    for (int l = 0; l < L.nlev; ++l) {
+        TcLevelData &t = c->tc[l];
+        if (t.dig) { cudaFree(t.dig); t.dig = nullptr; }
+        if (t.exps) { cudaFree(t.exps); t.exps = nullptr; }
+        t.usable = 0;
+        if (L.ndvr && l == L.nlev - 1) continue;
+        const int nout = L.n[l];
+        if (nout > 256) continue;   // exactness of the FP32 groups needs K <= 256
+        const int NT = std::min(64, (nout + 15) / 16 * 16);
+        const int ntiles = (nout + NT - 1) / NT;
+        const int KS = (nout + 15) / 16;
+        std::vector<double> H(L.h0s[l] >= 0 ? (size_t)nout * nout : 0);
+        SC_CUDA(cudaMemcpy(H.data(), c->H0 + L.h0s[l], sizeof(double) * H.size(), cudaMemcpyDeviceToHost));
+        std::vector<uint16_t> dig;
+        std::vector<int> exps;
+        cut_level_matrix(H.data(), nout, NT, ntiles, KS, dig, exps);
+        SC_CUDA(cudaMalloc(&t.dig, dig.size() * sizeof(uint16_t)));
+        SC_CUDA(cudaMalloc(&t.exps, exps.size() * sizeof(int)));
+        SC_CUDA(cudaMemcpy(t.dig, dig.data(), dig.size() * sizeof(uint16_t), cudaMemcpyHostToDevice));
+        SC_CUDA(cudaMemcpy(t.exps, exps.data(), exps.size() * sizeof(int), cudaMemcpyHostToDevice));
+        t.NT = NT;
+        t.ntiles = ntiles;
+        t.KS = KS;
+        t.usable = 1;
+    }
+    if (!c->tc_err) SC_CUDA(cudaMalloc(&c->tc_err, sizeof(int)));
+    SC_CUDA(cudaMemset(c->tc_err, 0, sizeof(int)));
+    return 0;
+}
+
+bool tc_usable(const scalit_ctx *c, int l)
+{
+    return c->tc[l].usable != 0;
+}
+
+int tc_level_apply(const scalit_ctx *c, int l, const double *X, double *Y, int accumulate, const double *diagV,
+                   double shift, double alpha, const int *gate, cudaStream_t s, int nvec)
+{
+    const Layout &L = c->L;
+    const TcLevelData &t = c->tc[l];
+    if (!t.usable) { set_error("level %d has no tensor-core plan", l + 1); return SCALIT_EUNSUP; }
+    const int nout = L.n[l];
+    const i64 nin = L.dim[l], blk = L.blk[l], N = L.N;
+    TcArgs g{};
+    g.N = nout;
+    g.K = nout;
+    g.KS = t.KS;
+    g.NT = t.NT;
+    if (nin == 1) {
+        g.M = (int)blk; g.Mi = blk; g.s1 = nout; g.s2 = 0; g.a_sk = 1; g.c_sn = 1;
+        g.rowscale = nullptr;
+    } else {
+        const i64 M = nin * blk;
+        if (M > 2147483647LL) { set_error("level %d too large", l + 1); return SCALIT_EINVAL; }
+        g.M = (int)M; g.Mi = nin; g.s1 = 1; g.s2 = nin * nout; g.a_sk = nin; g.c_sn = nin;
+        g.rowscale = L.dep[l] ? c->DEP + L.deps[l] : nullptr;
+    }
+    g.A = X; g.a_sz = N;
+    g.C = Y; g.c_sz = N;
+    g.accumulate = accumulate;
+    g.alpha = alpha;
+    g.diagV = diagV;
+    g.diagX = X;
+    g.dx_sz = N;
+    g.shift = shift;
+    g.gate = gate;
+    g.err = c->tc_err;
+    g.bdig = reinterpret_cast<const uint4 *>(t.dig);
+    g.bexp = t.exps;
+    const size_t smem = 2 * (size_t)kAStepBytes + 2 * (size_t)kDigits * t.NT * 32 + 64;
+    // at least half of the SM's shared memory, so one CTA (and one TMEM owner) per SM
+    const size_t smem_req = std::max(smem, (size_t)(116 * 1024));
+    SC_CUDA(cudaFuncSetAttribute(tc_level_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_req));
+    dim3 grid((g.M + kBM - 1) / kBM, t.ntiles, nvec);
+    if (grid.z > 65535) { set_error("too many vectors"); return SCALIT_EINVAL; }
+    tc_level_kernel<<<grid, kThreadsTC, smem_req, s>>>(g);
+    SC_CHECK_LAUNCH();
+    return 0;
+}
+
+int tc_check_error(scalit_ctx *c)
+{
+    if (!c->tc_err) return 0;
+    int h = 0;
+    SC_CUDA(cudaMemcpyAsync(&h, c->tc_err, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+    SC_CUDA(cudaStreamSynchronize(c->stream));
+    if (h) {
+        set_error("tensor-core H*X: an mbarrier wait ran out (kernel aborted)");
+        cudaMemsetAsync(c->tc_err, 0, sizeof(int), c->stream);
+        return SCALIT_ECUDA;
+    }
+    return 0;
+}
+
+}  // namespace sc

@@ -23,12 +23,17 @@ def c0():
     return hm.workload("tri-24x32x20")
 
 
+ENGINES = [capi.FP64_TENSOR, capi.FP64_DFMA]
+
+
+@pytest.mark.parametrize("engine", ENGINES)
 @pytest.mark.parametrize("ntype", [0, 1])
-def test_hx_c0_16_vectors(lib, orc, c0, ntype):
+def test_hx_c0_16_vectors(lib, orc, c0, ntype, engine):
     e0 = float(c0.RES.min())
     ref = orc.Operator.from_problem(c0, E0=e0)
     X = np.random.default_rng(0).standard_normal((16, c0.N))
     with capi.Context.from_problem(c0, e0=e0) as ctx:
+        ctx.set_fp64_mode(engine)
         Y = ctx.hx(X, ntype)
     for v in range(16):
         assert rel(Y[v], ref.hx(X[v], ntype)) < TOL64
@@ -36,12 +41,14 @@ def test_hx_c0_16_vectors(lib, orc, c0, ntype):
 
 @pytest.mark.parametrize("sizes", [(2, 3, 2), (5, 7, 3), (8, 8, 8), (13, 1, 9), (1, 6, 4),
                                    (67, 3, 5), (3, 130, 2)])
-def test_hx_odd_shapes(lib, orc, sizes):
+@pytest.mark.parametrize("engine", ENGINES)
+def test_hx_odd_shapes(lib, orc, sizes, engine):
     grid = hm.Grid3(*sizes)
     p = hm.build_problem(grid, hm.PES())
     ref = orc.Operator.from_problem(p, E0=0.01)
     x = np.random.default_rng(1).standard_normal(p.N)
     with capi.Context.from_problem(p, e0=0.01) as ctx:
+        ctx.set_fp64_mode(engine)
         y = ctx.hx(x, capi.TA1)
     assert rel(y, ref.hx(x, 1)) < TOL64
 
@@ -97,15 +104,30 @@ def test_hx_device_many(lib, orc, c0):
         assert rel(Y[v], ref.hx(X[v], 0)) < TOL64
 
 
+@pytest.mark.parametrize("engine", ENGINES)
 @pytest.mark.parametrize("name", ["tri-96x96x64", "tri-160x160x120"])
-def test_hx_large(lib, orc, name):
+def test_hx_large(lib, orc, name, engine):
     p = hm.workload(name)
     e0 = float(p.RES.min())
     ref = orc.Operator.from_problem(p, E0=e0)
     x = np.random.default_rng(5).standard_normal(p.N)
     with capi.Context.from_problem(p, e0=e0) as ctx:
+        ctx.set_fp64_mode(engine)
         y = ctx.hx(x, capi.TA1)
     assert rel(y, ref.hx(x, 1)) < TOL64
+
+
+def test_hx_tensor_matches_dfma_elementwise(lib, c0):
+    """The digit-sliced tensor-core engine against the FP64 pipe, element by element
+    relative to the row scale (|Y| can cancel to zero, the row scale cannot)."""
+    x = np.random.default_rng(9).standard_normal(c0.N)
+    with capi.Context.from_problem(c0, e0=0.0) as ctx:
+        ctx.set_fp64_mode(capi.FP64_DFMA)
+        y0 = ctx.hx(x, capi.TA1)
+        ctx.set_fp64_mode(capi.FP64_TENSOR)
+        y1 = ctx.hx(x, capi.TA1)
+    scale = np.abs(y0).max()
+    assert np.abs(y1 - y0).max() / scale < 1e-13
 
 
 def test_hx_rejects_nonfinite(lib, c0):
