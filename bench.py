@@ -378,7 +378,7 @@ def run_ours(args):
                        "l2": "two alternating 2x151 MB input/output sets (> 129 MB L2)"},
             "roofline": {"bound": "hbm", "achieved": ach_gbs, "peak": hbm, "unit": "GB/s",
                          "frac": ach_gbs / hbm, "traffic": None,
-                         "kernel": f"gemm_kernel<double> level {dom + 1}",
+                         "kernel": f"tc_level_kernel level {dom + 1}",
                          "peak_source": peak_src,
                          "algorithmic_bytes_per_launch": lv[dom]["bytes"],
                          "launch_ms": level_ms[dom]},

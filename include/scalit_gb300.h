@@ -183,6 +183,10 @@ typedef struct {
     double qmr_tol;   /* sQMR%mTol                                       */
     int precision;    /* SCALIT_PREC_* of the QMR inner solves           */
     int verbose;      /* print the reference's per-step lines to stdout  */
+    int orth;         /* 0: one modified Gram-Schmidt pass in the        */
+                      /*    reference's order (MGS_ORTH);                */
+                      /* 1: classical Gram-Schmidt twice (default: keeps */
+                      /*    the basis orthonormal over long runs)        */
 } scalit_pist_params;
 
 typedef struct {
@@ -204,6 +208,32 @@ void scalit_pist_default_params(scalit_pist_params *p, int m0, double conv_e0, d
 /* x0: npoints start vector (host).  eig: m values ascending.  info may be NULL. */
 int scalit_pist(scalit_ctx *ctx, const scalit_pist_params *p, const double *x0, double *eig,
                 double *res, scalit_pist_info *info);
+
+/* ------------------------------------------------ Differentiation -------
+ * Adjoint of Y = MYHX(ntype) X for one vector: given the cotangent Ybar,
+ *   Xbar = H^T Ybar (the shifted operator with transposed level matrices),
+ *   Vbar = Ybar .* X (gradient with respect to the potential grid RES),
+ *   H0bar(level l) = sum over the other levels of s_l Ybar (x) X
+ *     (gradient with respect to each level matrix, laid out like H0; s_l is
+ *     the DEP factor of a dependent level).
+ * Any output pointer may be NULL.  No counterpart in the reference (which
+ * has no derivatives); it extends MYHX (osb.hx.h:71-110). */
+int scalit_hx_adjoint(scalit_ctx *ctx, int ntype, const double *X, const double *Ybar, double *Xbar,
+                      double *Vbar, double *H0bar);
+int scalit_hx_adjoint_device(scalit_ctx *ctx, int ntype, const double *dX, const double *dYbar,
+                             double *dXbar, double *dVbar, double *dH0bar);
+int scalit_hx_adjoint_f32_device(scalit_ctx *ctx, int ntype, const float *dX, const float *dYbar,
+                                 float *dXbar, float *dVbar, float *dH0bar);
+/* Hellmann-Feynman gradients dE_k/dp_j = <psi_k| dV/dp_j |psi_k> for m
+ * normalised eigenvectors psi (m x npoints) and np potential derivatives
+ * dvdp (np x npoints); grad receives m x np values (row k, column j). */
+int scalit_hf_gradients(scalit_ctx *ctx, int m, const double *psi, int np, const double *dvdp,
+                        double *grad);
+/* PIST as scalit_pist, also returning the m Ritz vectors of the converged
+ * levels (m x npoints, host, same order as eig): psi_k = V_basis y_k with y_k
+ * the eigenvector of HMAT (DSYEV 'V' in place of the reference's 'N'). */
+int scalit_pist_vectors(scalit_ctx *ctx, const scalit_pist_params *p, const double *x0, double *eig,
+                        double *res, scalit_pist_info *info, double *vectors);
 
 /* -------------------------------------------- Fortran drop-in symbols -----
  * The external routines the reference's modules call, with gfortran naming

@@ -284,12 +284,29 @@ def get_sep_max(v1, v2):
     return float(np.max(np.min(np.abs(v1[:, None] - v2[None, :]), axis=1)))
 
 
+def cgs2_orth(W, m, VJ):
+    """Classical Gram-Schmidt applied twice (the re-orthogonalising variant of
+    MGS_ORTH): W against VJ(:, 0:m) into VJ(:, m)."""
+    v = _f64(W).copy()
+    if np.sqrt(lib().orc_dot(v.size, _p(v), _p(v))) == 0.0:
+        return False
+    V = VJ[:, :m]
+    for _ in range(2):
+        v -= V @ (V.T @ v)
+    nrm = np.sqrt(lib().orc_dot(v.size, _p(v), _p(v)))
+    if nrm == 0.0:
+        return False
+    VJ[:, m] = v / nrm
+    return True
+
+
 def pist_conv(E0, etol, ntype, x, startcnt, stepcnt, stepeig, M, m_max, h0x, linsolv,
-              log=None):
+              log=None, orth=0):
     """PIST_CONV (src/iterate/libiterate/pist/pist.f90:7-98) with pistH0
     (pistHij.f90:70-125) and MGS_ORTH (gsorth.f90:42-72).
 
     ``h0x(v) -> H v`` and ``linsolv(v) -> (status, w)`` are the operator callbacks.
+    ``orth=1`` replaces the single MGS pass by classical Gram-Schmidt twice.
     Returns ``(status, eig[M] ascending, RES, info)``.
     """
     x = _f64(x)
@@ -320,7 +337,7 @@ def pist_conv(E0, etol, ntype, x, startcnt, stepcnt, stepeig, M, m_max, h0x, lin
             info["qmr_iters"].append(num)
             if num <= 0:
                 return num
-            if not mgs_orth(W, J, VJ):
+            if not (cgs2_orth(W, J, VJ) if orth else mgs_orth(W, J, VJ)):
                 return -J
         for J in range(m_low, m_high + 1):
             vj = np.ascontiguousarray(VJ[:, J - 1])

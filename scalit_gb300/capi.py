@@ -53,6 +53,11 @@ SIGNATURES = {
     "scalit_pist_default_params": (None, [_vp, C.c_int, C.c_double, C.c_double, C.c_int, C.c_int,
                                           C.c_int, C.c_int, C.c_int, C.c_double]),
     "scalit_pist": (C.c_int, [_vp, _vp, _dp, _dp, _dp, _vp]),
+    "scalit_hx_adjoint": (C.c_int, [_vp, C.c_int, _dp, _dp, _dp, _dp, _dp]),
+    "scalit_hx_adjoint_device": (C.c_int, [_vp, C.c_int, _vp, _vp, _vp, _vp, _vp]),
+    "scalit_hx_adjoint_f32_device": (C.c_int, [_vp, C.c_int, _vp, _vp, _vp, _vp, _vp]),
+    "scalit_hf_gradients": (C.c_int, [_vp, C.c_int, _dp, C.c_int, _dp, _dp]),
+    "scalit_pist_vectors": (C.c_int, [_vp, _vp, _dp, _dp, _dp, _vp, _dp]),
     # Fortran drop-ins (all arguments by reference)
     "h1x_xyz_": (None, [_ip, _ip, _ip, _dp, _dp, _dp]),
     "h1x_xyz_seq_": (None, [_ip, _ip, _ip, _dp, _dp, _dp]),
@@ -92,7 +97,7 @@ class PistParams(C.Structure):
                 ("startcnt", C.c_int), ("stepcnt", C.c_int), ("stepeig", C.c_int),
                 ("m", C.c_int), ("m_max", C.c_int), ("qmr_ntype", C.c_int),
                 ("qmr_max", C.c_int), ("qmr_tol", C.c_double), ("precision", C.c_int),
-                ("verbose", C.c_int)]
+                ("verbose", C.c_int), ("orth", C.c_int)]
 
 
 class PistInfo(C.Structure):
@@ -278,9 +283,37 @@ class Context:
                                           int(precision), _p(B), _p(X), C.byref(res), C.byref(it)))
         return code, X, res.value, it.value
 
+    def hx_adjoint(self, X, Ybar, ntype=TA1, want=("x", "v", "h")):
+        """Adjoint of H*X: returns (Xbar, Vbar, H0bar) (None for what is not wanted)."""
+        X, Ybar = _f64(X), _f64(Ybar)
+        Xb = np.empty(self.N) if "x" in want else None
+        Vb = np.empty(self.N) if "v" in want else None
+        Hb = np.empty(int(self.lib.scalit_h0_len(self.h))) if "h" in want else None
+        _check(self.lib.scalit_hx_adjoint(self.h, int(ntype), _p(X), _p(Ybar),
+                                          _p(Xb) if Xb is not None else None,
+                                          _p(Vb) if Vb is not None else None,
+                                          _p(Hb) if Hb is not None else None))
+        return Xb, Vb, Hb
+
+    def hx_adjoint_device(self, dX, dYbar, dXbar=None, dVbar=None, dHbar=None, ntype=TA1, f32=False):
+        f = self.lib.scalit_hx_adjoint_f32_device if f32 else self.lib.scalit_hx_adjoint_device
+        nul = C.c_void_p(0)
+        _check(f(self.h, int(ntype), _ptr(dX), _ptr(dYbar), _ptr(dXbar) if dXbar is not None else nul,
+                 _ptr(dVbar) if dVbar is not None else nul, _ptr(dHbar) if dHbar is not None else nul))
+
+    def hf_gradients(self, psi, dvdp):
+        """dE_k/dp_j = <psi_k| dV/dp_j |psi_k> for psi (m x N) and dvdp (np x N)."""
+        psi, dvdp = _f64(psi), _f64(dvdp)
+        m, npar = psi.size // self.N, dvdp.size // self.N
+        g = np.empty((m, npar))
+        _check(self.lib.scalit_hf_gradients(self.h, m, _p(psi), npar, _p(dvdp), _p(g)))
+        return g
+
     def pist(self, x0, m, e0, etol, startcnt=0, stepcnt=5, m_max=0, gap=1, qmr_max=2000,
-             qmr_tol=1e-4, qmr_ntype=-1, precision=PREC_FP64, ntype=0, verbose=False):
-        """OSB_PISTCONV: returns (status, eig[m], RES, info dict)."""
+             qmr_tol=1e-4, qmr_ntype=-1, precision=PREC_FP64, ntype=0, verbose=False, orth=1,
+             vectors=False):
+        """OSB_PISTCONV: returns (status, eig[m], RES, info dict); with vectors=True the
+        info dict also holds the m Ritz vectors ("vectors", m x N)."""
         p = PistParams()
         self.lib.scalit_pist_default_params(C.byref(p), int(m), float(e0), float(etol),
                                             int(startcnt), int(stepcnt), int(m_max), int(gap),
@@ -289,10 +322,16 @@ class Context:
         p.precision = int(precision)
         p.ntype = int(ntype)
         p.verbose = int(bool(verbose))
+        p.orth = int(orth)
         x0 = _f64(x0)
         eig = np.zeros(int(m))
         res = C.c_double(0.0)
         info = PistInfo()
+        if vectors:
+            vec = np.zeros((int(m), self.N))
+            st = _check(self.lib.scalit_pist_vectors(self.h, C.byref(p), _p(x0), _p(eig), C.byref(res),
+                                                     C.byref(info), _p(vec)))
+            return st, eig, res.value, dict(info.as_dict(), m_max=p.m_max, startcnt=p.startcnt, vectors=vec)
         st = _check(self.lib.scalit_pist(self.h, C.byref(p), _p(x0), _p(eig), C.byref(res),
                                          C.byref(info)))
         return st, eig, res.value, dict(info.as_dict(), m_max=p.m_max, startcnt=p.startcnt)

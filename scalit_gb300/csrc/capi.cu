@@ -316,6 +316,8 @@ int scalit_level_device(scalit_ctx *c, int level, int accumulate, const double *
     CTX_CHECK(c);
     if (!c->loaded) { set_error("level product before scalit_load"); return SCALIT_ESTATE; }
     if (level < 1 || level > c->L.nlev) { set_error("level %d out of range", level); return SCALIT_EINVAL; }
+    if (c->fp64_mode == SCALIT_FP64_TENSOR && tc_usable(c, level - 1))
+        return tc_level_apply(c, level - 1, dX, dY, accumulate ? 1 : 0, nullptr, 0.0, 1.0, nullptr, c->stream, 1);
     return level_apply<double>(c, level - 1, c->H0, c->DEP, c->OUTH, dX, dY, accumulate ? 1 : 0, nullptr,
                                0.0, 1.0, nullptr, c->stream);
 }
@@ -486,6 +488,7 @@ void scalit_pist_default_params(scalit_pist_params *p, int m0, double conv_e0, d
     p->qmr_tol = qmr_tol;
     p->precision = SCALIT_PREC_FP64;
     p->verbose = 0;
+    p->orth = 1;
 }
 
 int scalit_pist(scalit_ctx *c, const scalit_pist_params *p, const double *x0, double *eig, double *res,
@@ -503,6 +506,83 @@ int scalit_pist(scalit_ctx *c, const scalit_pist_params *p, const double *x0, do
     return rc;
 }
 
+int scalit_pist_vectors(scalit_ctx *c, const scalit_pist_params *p, const double *x0, double *eig, double *res,
+                        scalit_pist_info *info, double *vectors)
+{
+    CTX_CHECK(c);
+    if (!p || !x0 || !eig || !res) { set_error("null argument"); return SCALIT_EINVAL; }
+    const i64 N = c->L.N;
+    double *dx = nullptr;
+    SC_CUDA(cudaMallocAsync(&dx, sizeof(double) * (size_t)N, c->stream));
+    SC_CUDA(cudaMemcpyAsync(dx, x0, sizeof(double) * N, cudaMemcpyHostToDevice, c->stream));
+    int rc = pist_ctx(c, p, dx, eig, res, info, vectors);
+    cudaFreeAsync(dx, c->stream);
+    cudaStreamSynchronize(c->stream);
+    return rc;
+}
+
+// ------------------------------------------------------ differentiation --
+int scalit_hx_adjoint_device(scalit_ctx *c, int ntype, const double *dX, const double *dYbar, double *dXbar,
+                             double *dVbar, double *dH0bar)
+{
+    CTX_CHECK(c);
+    if (!c->loaded) { set_error("adjoint before scalit_load"); return SCALIT_ESTATE; }
+    if (!dX || !dYbar) { set_error("null input"); return SCALIT_EINVAL; }
+    return hx_adjoint<double>(c, ntype, dX, dYbar, dXbar, dVbar, dH0bar, c->stream);
+}
+
+int scalit_hx_adjoint_f32_device(scalit_ctx *c, int ntype, const float *dX, const float *dYbar, float *dXbar,
+                                 float *dVbar, float *dH0bar)
+{
+    CTX_CHECK(c);
+    if (!c->loaded) { set_error("adjoint before scalit_load"); return SCALIT_ESTATE; }
+    if (!dX || !dYbar) { set_error("null input"); return SCALIT_EINVAL; }
+    return hx_adjoint<float>(c, ntype, dX, dYbar, dXbar, dVbar, dH0bar, c->stream);
+}
+
+int scalit_hx_adjoint(scalit_ctx *c, int ntype, const double *X, const double *Ybar, double *Xbar, double *Vbar,
+                      double *H0bar)
+{
+    CTX_CHECK(c);
+    if (!c->loaded) { set_error("adjoint before scalit_load"); return SCALIT_ESTATE; }
+    if (!X || !Ybar) { set_error("null input"); return SCALIT_EINVAL; }
+    const i64 N = c->L.N, nh = std::max<i64>(c->L.h0len, 1);
+    double *w = nullptr;
+    cudaStream_t s = c->stream;
+    SC_CUDA(cudaMallocAsync(&w, sizeof(double) * (size_t)(4 * N + nh), s));
+    double *dX = w, *dY = w + N, *dXb = w + 2 * N, *dVb = w + 3 * N, *dHb = w + 4 * N;
+    SC_CUDA(cudaMemcpyAsync(dX, X, sizeof(double) * N, cudaMemcpyHostToDevice, s));
+    SC_CUDA(cudaMemcpyAsync(dY, Ybar, sizeof(double) * N, cudaMemcpyHostToDevice, s));
+    int rc = hx_adjoint<double>(c, ntype, dX, dY, Xbar ? dXb : nullptr, Vbar ? dVb : nullptr,
+                                H0bar ? dHb : nullptr, s);
+    if (!rc) {
+        if (Xbar) SC_CUDA(cudaMemcpyAsync(Xbar, dXb, sizeof(double) * N, cudaMemcpyDeviceToHost, s));
+        if (Vbar) SC_CUDA(cudaMemcpyAsync(Vbar, dVb, sizeof(double) * N, cudaMemcpyDeviceToHost, s));
+        if (H0bar) SC_CUDA(cudaMemcpyAsync(H0bar, dHb, sizeof(double) * c->L.h0len, cudaMemcpyDeviceToHost, s));
+    }
+    cudaFreeAsync(w, s);
+    SC_CUDA(cudaStreamSynchronize(s));
+    return rc;
+}
+
+int scalit_hf_gradients(scalit_ctx *c, int m, const double *psi, int np, const double *dvdp, double *grad)
+{
+    CTX_CHECK(c);
+    if (m < 1 || np < 1 || !psi || !dvdp || !grad) { set_error("bad Hellmann-Feynman arguments"); return SCALIT_EINVAL; }
+    const i64 N = c->L.N;
+    cudaStream_t s = c->stream;
+    double *w = nullptr;
+    SC_CUDA(cudaMallocAsync(&w, sizeof(double) * (size_t)((i64)(m + np) * N + (i64)m * np), s));
+    double *dpsi = w, *ddv = w + (i64)m * N, *dg = w + (i64)(m + np) * N;
+    SC_CUDA(cudaMemcpyAsync(dpsi, psi, sizeof(double) * (size_t)m * N, cudaMemcpyHostToDevice, s));
+    SC_CUDA(cudaMemcpyAsync(ddv, dvdp, sizeof(double) * (size_t)np * N, cudaMemcpyHostToDevice, s));
+    int rc = hf_gradients(c, m, dpsi, np, ddv, dg);
+    if (!rc) SC_CUDA(cudaMemcpyAsync(grad, dg, sizeof(double) * (size_t)m * np, cudaMemcpyDeviceToHost, s));
+    cudaFreeAsync(w, s);
+    SC_CUDA(cudaStreamSynchronize(s));
+    return rc;
+}
+
 }  // extern "C"
 
 // ======================================================================
@@ -514,7 +594,7 @@ static std::mutex g_fmu;
 static int g_fdev = 0;
 static scalit_ctx *g_fctx = nullptr;      // module state made by scalit_fortran_init_
 static scalit_ctx *g_scratch = nullptr;   // stream + scratch for stand-alone routines
-static struct { int ntype = -1, qmrmax = 2000; double tol = 1e-4; int precision = SCALIT_PREC_FP64; } g_fq;
+static struct { int ntype = -1, qmrmax = 2000; double tol = 1e-4; int precision = SCALIT_PREC_FP64; int orth = 1; } g_fq;
 
 static scalit_ctx *scratch()
 {
@@ -739,6 +819,7 @@ static int pist_fortran(double e0, double etol, int ntype, int n, const double *
     p.e0 = e0; p.etol = etol; p.ntype = ntype; p.startcnt = startcnt; p.stepcnt = stepcnt;
     p.stepeig = stepeig; p.m = m; p.m_max = m_max;
     p.qmr_ntype = g_fq.ntype; p.qmr_max = g_fq.qmrmax; p.qmr_tol = g_fq.tol; p.precision = g_fq.precision;
+    p.orth = g_fq.orth;
     const bool own = (h0x == scalit_hx0_ && linsolv == scalit_osb_qmr_ && g_fctx && g_fctx->L.N == n);
     if (own) {
         int rc = scalit_pist(g_fctx, &p, X, EIG, RES, nullptr);

@@ -122,12 +122,13 @@ gemm_kernel(GemmArgs<T> g)
     }
 
     // Epilogue.
+    const i64 cs1 = g.c_s1 >= 0 ? g.c_s1 : g.s1, cs2 = g.c_s2 >= 0 ? g.c_s2 : g.s2;
     #pragma unroll
     for (int i = 0; i < TM; ++i) {
         const int m = m0 + tm + i;
         if (m >= g.M) continue;
         const i64 mi = m % g.Mi;
-        const i64 moff = mi * g.s1 + (i64)(m / g.Mi) * g.s2;
+        const i64 moff = mi * cs1 + (i64)(m / g.Mi) * cs2;
         const T sc = g.rowscale ? g.rowscale[mi] * g.alpha : g.alpha;
         #pragma unroll
         for (int j = 0; j < TN; ++j) {

@@ -103,7 +103,8 @@ int work_get(scalit_ctx *c, size_t bytes, void **out);
 //           + (diagV ? (diagV[p] - shift) * diagX[p] : 0) with p = C offset.
 template <class T> struct GemmArgs {
     int M, N, K, batch;
-    i64 Mi, s1, s2;
+    i64 Mi, s1, s2;          // A's row offset (m % Mi) s1 + (m / Mi) s2
+    i64 c_s1 = -1, c_s2 = -1; // C's row strides; -1: the same as A's
     const T *A; i64 a_sk, a_sz;
     const T *B; i64 b_sk, b_sn, b_sz;
     T *C; i64 c_sn, c_sz;
@@ -144,6 +145,11 @@ int px_vec(const scalit_ctx *c, int npc, const T *X, T *Y, T *tmp, T alpha, cons
 template <class T>
 int level_rotate(int nin, int nout, int blk, const T *V, const T *X, T *Y, int transpose,
                  const int *gate, cudaStream_t s);
+
+// -------------------------------------------------------- differentiation --
+template <class T>
+int hx_adjoint(scalit_ctx *c, int ntype, const T *X, const T *Ybar, T *Xbar, T *Vbar, T *Hbar, cudaStream_t s);
+int hf_gradients(scalit_ctx *c, int m, const double *psi, int np, const double *dvdp, double *grad_dev);
 
 // ------------------------------------------------------- tensor-core FP64 --
 int tc_prepare(scalit_ctx *c);
@@ -195,8 +201,8 @@ struct PistOps {
     virtual int linsolv(const double *dB, double *dX, int *num) = 0;   // (H - E0) x = b
 };
 int pist_core(scalit_ctx *c, i64 N, const scalit_pist_params *p, const double *dx0, PistOps &ops,
-              double *eig, double *res, scalit_pist_info *info);
+              double *eig, double *res, scalit_pist_info *info, double *vectors_host = nullptr);
 int pist_ctx(scalit_ctx *c, const scalit_pist_params *p, const double *dx0, double *eig,
-             double *res, scalit_pist_info *info);
+             double *res, scalit_pist_info *info, double *vectors_host = nullptr);
 
 }  // namespace sc

@@ -61,12 +61,51 @@ mgs_kernel(i64 n, double *v, const double *uprev, const double *dprev, const dou
         const double y = u ? u[k] : x;
         acc[0] = fma(x, y, acc[0]);
     }
-    if (last_block(acc, partial, counter) && threadIdx.x == 0) {
-        *counter = 0;
+    if (last_block(acc, partial, counter)) {
+        // every thread of the last CTA folds a fixed strided share, then a fixed tree
+        __shared__ double fred[kT / 32];
         double s = 0.0;
-        for (unsigned int b = 0; b < gridDim.x; ++b) s += partial[b];
-        *dout = s;
+        for (unsigned int b = threadIdx.x; b < gridDim.x; b += blockDim.x) s += __ldcg(&partial[b]);
+        #pragma unroll
+        for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+        if ((threadIdx.x & 31) == 0) fred[threadIdx.x >> 5] = s;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            double t = 0.0;
+            for (int w = 0; w < kT / 32; ++w) t += fred[w];
+            *counter = 0;
+            *dout = t;
+        }
     }
+}
+
+// v -= V(:, 0:m) h  (the classical Gram-Schmidt update; h staged in shared memory)
+__global__ void __launch_bounds__(kT)
+gemv_sub_kernel(i64 n, int m, const double *VJ, const double *h, double *v)
+{
+    __shared__ double hs[1024];
+    for (int i0 = 0; i0 < m; i0 += 1024) {
+        const int cnt = min(1024, m - i0);
+        __syncthreads();
+        for (int i = threadIdx.x; i < cnt; i += blockDim.x) hs[i] = h[i0 + i];
+        __syncthreads();
+        for (i64 k = blockIdx.x * (i64)blockDim.x + threadIdx.x; k < n; k += (i64)gridDim.x * blockDim.x) {
+            double a = 0.0;
+            const double *col = VJ + (i64)i0 * n + k;
+            for (int i = 0; i < cnt; ++i) a = fma(col[(i64)i * n], hs[i], a);
+            v[k] -= a;
+        }
+    }
+}
+
+// h[I] = sum of the chunk partials of column I, in chunk order.
+__global__ void gemvt_vec_kernel(int m, int nchunk, const double *partial, double *h)
+{
+    const int I = blockIdx.x * blockDim.x + threadIdx.x;
+    if (I >= m) return;
+    double s = 0.0;
+    for (int c = 0; c < nchunk; ++c) s += partial[(i64)I * nchunk + c];
+    h[I] = s;
 }
 
 // v = v / sqrt(*nrm2) when nonzero.
@@ -181,13 +220,83 @@ static double sep_max(const double *v1, int n1, const std::vector<double> &v2, i
     return g;
 }
 
+// Ritz vectors of the M eigenvalues of HMAT(1:num, 1:num) nearest e0, ascending:
+// psi = VJ(:, 1:num) y, copied to the host as M x N.
+__global__ void select_columns_kernel(int num, int M, const double *Yall, const int *idx, double *Ysel)
+{
+    const i64 total = (i64)num * M;
+    for (i64 e = blockIdx.x * (i64)blockDim.x + threadIdx.x; e < total; e += (i64)gridDim.x * blockDim.x) {
+        const int r = (int)(e % num), k = (int)(e / num);
+        Ysel[e] = Yall[r + (i64)num * idx[k]];
+    }
+}
+
+static int ritz_vectors(scalit_ctx *c, i64 N, const double *VJ, const double *HMAT, int ld, int num, double e0,
+                        int M, double *A, double *EV, double *work, int lwork, int *devinfo, double *out_host)
+{
+    cudaStream_t s = c->stream;
+    cusolverDnHandle_t sol = (cusolverDnHandle_t)c->cusolver;
+    gather_upper_kernel<<<egrid((i64)num * num), kT, 0, s>>>(num, HMAT, ld, A);
+    SC_CHECK_LAUNCH();
+    int lw = 0;
+    if (cusolverDnDsyevd_bufferSize(sol, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_UPPER, num, A, num, EV, &lw) !=
+        CUSOLVER_STATUS_SUCCESS) { set_error("syevd buffer size"); return SCALIT_ECUDA; }
+    double *wk = work;
+    double *own = nullptr;
+    if (lw > lwork) { SC_CUDA(cudaMallocAsync(&own, sizeof(double) * (size_t)lw, s)); wk = own; }
+    if (cusolverDnDsyevd(sol, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_UPPER, num, A, num, EV, wk,
+                         std::max(lw, lwork), devinfo) != CUSOLVER_STATUS_SUCCESS) {
+        set_error("cusolverDnDsyevd (vectors) failed");
+        return SCALIT_ECUDA;
+    }
+    std::vector<double> ev(num);
+    SC_CUDA(cudaMemcpyAsync(ev.data(), EV, sizeof(double) * num, cudaMemcpyDeviceToHost, s));
+    SC_CUDA(cudaStreamSynchronize(s));
+    // the window's indices (getWindow0's choice), then ascending by eigenvalue
+    std::vector<char> label(num, 1);
+    std::vector<int> idx;
+    for (int i = 0; i < M && i < num; ++i) {
+        int best = -1;
+        double v0 = 0.0;
+        for (int j = 0; j < num; ++j) {
+            if (!label[j]) continue;
+            const double a = fabs(ev[j] - e0);
+            if (best < 0 || v0 > a) { best = j; v0 = a; }
+        }
+        idx.push_back(best);
+        label[best] = 0;
+    }
+    std::sort(idx.begin(), idx.end(), [&](int a, int b) { return ev[a] < ev[b]; });
+    const int Msel = (int)idx.size();
+    int *didx = nullptr;
+    double *Ysel = nullptr, *Psi = nullptr;
+    SC_CUDA(cudaMallocAsync(&didx, sizeof(int) * Msel, s));
+    SC_CUDA(cudaMallocAsync(&Ysel, sizeof(double) * (size_t)num * Msel, s));
+    SC_CUDA(cudaMallocAsync(&Psi, sizeof(double) * (size_t)N * Msel, s));
+    SC_CUDA(cudaMemcpyAsync(didx, idx.data(), sizeof(int) * Msel, cudaMemcpyHostToDevice, s));
+    select_columns_kernel<<<egrid((i64)num * Msel), kT, 0, s>>>(num, Msel, A, didx, Ysel);
+    GemmArgs<double> g{};
+    g.M = (int)N; g.N = Msel; g.K = num; g.batch = 1;
+    g.Mi = N; g.s1 = 1; g.s2 = 0;
+    g.A = VJ; g.a_sk = N;                 // A(p, k) = VJ[p + N k]
+    g.B = Ysel; g.b_sk = 1; g.b_sn = num; // B(k, j) = Ysel[k + num j]
+    g.C = Psi; g.c_sn = N;
+    g.alpha = 1.0;
+    int rc = launch_gemm<double>(g, s);
+    if (!rc) SC_CUDA(cudaMemcpyAsync(out_host, Psi, sizeof(double) * (size_t)N * Msel, cudaMemcpyDeviceToHost, s));
+    SC_CUDA(cudaStreamSynchronize(s));
+    cudaFreeAsync(didx, s); cudaFreeAsync(Ysel, s); cudaFreeAsync(Psi, s);
+    if (own) cudaFreeAsync(own, s);
+    return rc;
+}
+
 static double now()
 {
     return std::chrono::duration<double>(std::chrono::steady_clock::now().time_since_epoch()).count();
 }
 
 int pist_core(scalit_ctx *c, i64 N, const scalit_pist_params *p, const double *dx0, PistOps &ops,
-              double *eig, double *res, scalit_pist_info *info)
+              double *eig, double *res, scalit_pist_info *info, double *vectors_host)
 {
     cudaStream_t s = c->stream;
     const int M = p->m, MM = p->m_max;
@@ -236,17 +345,28 @@ int pist_core(scalit_ctx *c, i64 N, const scalit_pist_params *p, const double *d
     int rc = 0;
 
     // MGS_ORTH: orthogonalise W against columns 1..J into column J+1.
+    // orth == 0: modified Gram-Schmidt in the reference's order (one pass);
+    // orth == 1: classical Gram-Schmidt applied twice (GEMV-T then GEMV, x2).
     auto mgs = [&](int J, bool *ok) -> int {
         double *v = vcol(J + 1);
         SC_CUDA(cudaMemcpyAsync(v, W, sizeof(double) * (size_t)N, cudaMemcpyDeviceToDevice, s));
         mgs_kernel<<<gr, kT, 0, s>>>(N, v, nullptr, nullptr, nullptr, dnorm, partial, counter);
-        for (int i = 1; i <= J; ++i) {
-            const double *uprev = (i > 1) ? vcol(i - 1) : nullptr;
-            mgs_kernel<<<gr, kT, 0, s>>>(N, v, uprev, D + (i - 2 >= 0 ? i - 2 : 0), vcol(i), D + (i - 1),
-                                         partial, counter);
+        if (p->orth == 0) {
+            for (int i = 1; i <= J; ++i) {
+                const double *uprev = (i > 1) ? vcol(i - 1) : nullptr;
+                mgs_kernel<<<gr, kT, 0, s>>>(N, v, uprev, D + (i - 2 >= 0 ? i - 2 : 0), vcol(i), D + (i - 1),
+                                             partial, counter);
+            }
+            // last projection and the norm
+            mgs_kernel<<<gr, kT, 0, s>>>(N, v, vcol(J), D + (J - 1), nullptr, dnorm + 1, partial, counter);
+        } else {
+            for (int pass = 0; pass < 2; ++pass) {
+                gemvt_partial_kernel<<<dim3(nchunk, J), kT, 0, s>>>(N, J, VJ, v, partial, nchunk);
+                gemvt_vec_kernel<<<(J + 127) / 128, 128, 0, s>>>(J, nchunk, partial, D);
+                gemv_sub_kernel<<<gr, kT, 0, s>>>(N, J, VJ, D, v);
+            }
+            mgs_kernel<<<gr, kT, 0, s>>>(N, v, nullptr, nullptr, nullptr, dnorm + 1, partial, counter);
         }
-        // last projection and the norm
-        mgs_kernel<<<gr, kT, 0, s>>>(N, v, vcol(J), D + (J - 1), nullptr, dnorm + 1, partial, counter);
         SC_CHECK_LAUNCH();
         double h[2];
         SC_CUDA(cudaMemcpyAsync(h, dnorm, 2 * sizeof(double), cudaMemcpyDeviceToHost, s));
@@ -351,6 +471,10 @@ int pist_core(scalit_ctx *c, i64 N, const scalit_pist_params *p, const double *d
         if (cnt_low >= MM) { status = -MM; break; }
         cnt_high = std::min(cnt_high + p->stepcnt, MM);
     }
+    if (vectors_host && rc == 0 && status > 0) {
+        int r2 = ritz_vectors(c, N, VJ, HMAT, MM, status, p->e0, M, A, EV, work, lwork, devinfo, vectors_host);
+        if (r2) rc = r2;
+    }
     std::sort(cur.begin(), cur.end());
     for (int i = 0; i < M; ++i) eig[i] = cur[i];
     cudaFreeAsync(VJ, s); cudaFreeAsync(W, s); cudaFreeAsync(HMAT, s); cudaFreeAsync(A, s);
@@ -380,13 +504,13 @@ struct CtxOps : PistOps {
 };
 
 int pist_ctx(scalit_ctx *c, const scalit_pist_params *p, const double *dx0, double *eig, double *res,
-             scalit_pist_info *info)
+             scalit_pist_info *info, double *vectors_host)
 {
     if (!c->osb_built) { set_error("PIST needs the preconditioner: build or load it first"); return SCALIT_ESTATE; }
     CtxOps ops;
     ops.c = c;
     ops.p = p;
-    return pist_core(c, c->L.N, p, dx0, ops, eig, res, info);
+    return pist_core(c, c->L.N, p, dx0, ops, eig, res, info, vectors_host);
 }
 
 }  // namespace sc

@@ -29,12 +29,33 @@ struct QmrState {
     unsigned int counter;
 };
 
-// Sum of per-CTA partials (nv values per CTA) in CTA order by one thread.
-__device__ __forceinline__ void fold(const double *partial, int nblk, int nv, double *out)
+// Sum of the per-CTA partials (NV values per CTA), by every thread of the last
+// CTA: a fixed strided split, then a fixed warp/CTA tree -- the same order on
+// every run.  The result is valid in thread 0.
+template <int NV>
+__device__ __forceinline__ void fold(const double *partial, int nblk, double (&out)[NV])
 {
-    for (int v = 0; v < nv; ++v) out[v] = 0.0;
-    for (int b = 0; b < nblk; ++b)
-        for (int v = 0; v < nv; ++v) out[v] += partial[nv * b + v];
+    __shared__ double fred[NV][kRedThreads / 32];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    double a[NV];
+    #pragma unroll
+    for (int v = 0; v < NV; ++v) a[v] = 0.0;
+    for (int b = threadIdx.x; b < nblk; b += blockDim.x)
+        #pragma unroll
+        for (int v = 0; v < NV; ++v) a[v] += __ldcg(&partial[NV * b + v]);
+    #pragma unroll
+    for (int v = 0; v < NV; ++v) {
+        #pragma unroll
+        for (int o = 16; o > 0; o >>= 1) a[v] += __shfl_xor_sync(0xffffffffu, a[v], o);
+        if (lane == 0) fred[v][warp] = a[v];
+    }
+    __syncthreads();
+    #pragma unroll
+    for (int v = 0; v < NV; ++v) {
+        double s = 0.0;
+        for (int w = 0; w < kRedThreads / 32; ++w) s += fred[v][w];
+        out[v] = s;
+    }
 }
 
 template <int NV>
@@ -86,10 +107,11 @@ qmr_step_a(i64 n, T *V, T *Z, QmrState *st, double *partial)
         V[k] = v; Z[k] = z;
         acc[0] += (double)v * (double)z;
     }
-    if (block_reduce_store<1>(acc, partial, &st->counter) && threadIdx.x == 0) {
-        st->counter = 0;
+    if (block_reduce_store<1>(acc, partial, &st->counter)) {
         double d[1];
-        fold(partial, gridDim.x, 1, d);
+        fold<1>(partial, gridDim.x, d);
+        if (threadIdx.x != 0) return;
+        st->counter = 0;
         st->ZVRAT = st->ZVRAT * st->ZNRM / st->VNRM;
         st->VZDOT = d[0];
         st->inv_zvrat = 1.0 / st->ZVRAT;
@@ -122,10 +144,11 @@ qmr_step_c(i64 n, const T *Q, T *S, QmrState *st, double *partial)
         S[k] = sv;
         acc[0] += (double)Q[k] * (double)sv;
     }
-    if (block_reduce_store<1>(acc, partial, &st->counter) && threadIdx.x == 0) {
-        st->counter = 0;
+    if (block_reduce_store<1>(acc, partial, &st->counter)) {
         double d[1];
-        fold(partial, gridDim.x, 1, d);
+        fold<1>(partial, gridDim.x, d);
+        if (threadIdx.x != 0) return;
+        st->counter = 0;
         st->QSDOT = d[0];
         st->BETA = st->QSDOT / st->VZDOT;
         if (st->QSDOT == 0.0 || st->BETA == 0.0) { st->code = -3; st->breakdown = 1; st->done = 1; }
@@ -145,10 +168,11 @@ qmr_step_d(i64 n, const T *S, T *V, QmrState *st, double *partial)
         V[k] = v;
         acc[0] += (double)v * (double)v;
     }
-    if (block_reduce_store<1>(acc, partial, &st->counter) && threadIdx.x == 0) {
-        st->counter = 0;
+    if (block_reduce_store<1>(acc, partial, &st->counter)) {
         double d[1];
-        fold(partial, gridDim.x, 1, d);
+        fold<1>(partial, gridDim.x, d);
+        if (threadIdx.x != 0) return;
+        st->counter = 0;
         st->VNRMPO = sqrt(d[0]);
     }
 }
@@ -166,10 +190,11 @@ qmr_step_e(i64 n, T *Z, QmrState *st, double *partial)
         Z[k] = z;
         acc[0] += (double)z * (double)z;
     }
-    if (block_reduce_store<1>(acc, partial, &st->counter) && threadIdx.x == 0) {
-        st->counter = 0;
+    if (block_reduce_store<1>(acc, partial, &st->counter)) {
         double d[1];
-        fold(partial, gridDim.x, 1, d);
+        fold<1>(partial, gridDim.x, d);
+        if (threadIdx.x != 0) return;
+        st->counter = 0;
         st->ZNRM = sqrt(d[0]);
         st->THETA = st->VNRMPO / (st->GAMAMO * fabs(st->BETA));
         st->GAMA = 1.0 / sqrt(1.0 + st->THETA * st->THETA);
@@ -221,10 +246,11 @@ qmr_step_f(i64 n, const T *Q, const T *S, T *UX, T *UR, T *X, T *R, QmrState *st
         acc[3] += (double)ur * (double)ur;
     }
     if (conv == 1) return;  // the |HX-B|/|HX| test follows in step G
-    if (block_reduce_store<4>(acc, partial, &st->counter) && threadIdx.x == 0) {
-        st->counter = 0;
+    if (block_reduce_store<4>(acc, partial, &st->counter)) {
         double d[4];
-        fold(partial, gridDim.x, 4, d);
+        fold<4>(partial, gridDim.x, d);
+        if (threadIdx.x != 0) return;
+        st->counter = 0;
         if (conv == 2) {
             const double r1 = sqrt(d[0]) / st->BNRM;
             const double r2 = sqrt(d[1] / d[2]);
@@ -250,10 +276,11 @@ qmr_step_g(i64 n, const T *HX0, const T *B, QmrState *st, double *partial)
         acc[0] += (double)h * (double)h;
         acc[1] += (double)d * (double)d;
     }
-    if (block_reduce_store<2>(acc, partial, &st->counter) && threadIdx.x == 0) {
-        st->counter = 0;
+    if (block_reduce_store<2>(acc, partial, &st->counter)) {
         double d[2];
-        fold(partial, gridDim.x, 2, d);
+        fold<2>(partial, gridDim.x, d);
+        if (threadIdx.x != 0) return;
+        st->counter = 0;
         st->XNRM = sqrt(d[0]);
         st->RES = sqrt(d[1]) / st->XNRM;
         qmr_advance(st);
@@ -270,10 +297,11 @@ qmr_init_norms(i64 n, const T *B, const T *Z, QmrState *st, double *partial)
         acc[0] += (double)B[k] * (double)B[k];
         acc[1] += (double)Z[k] * (double)Z[k];
     }
-    if (block_reduce_store<2>(acc, partial, &st->counter) && threadIdx.x == 0) {
-        st->counter = 0;
+    if (block_reduce_store<2>(acc, partial, &st->counter)) {
         double d[2];
-        fold(partial, gridDim.x, 2, d);
+        fold<2>(partial, gridDim.x, d);
+        if (threadIdx.x != 0) return;
+        st->counter = 0;
         st->BNRM = sqrt(d[0]);
         st->VNRM = st->BNRM;
         st->ZNRM = sqrt(d[1]);
@@ -371,10 +399,11 @@ dot_kernel(i64 n, const T *x, const T *y, double *partial, unsigned int *counter
     double acc[1] = {0.0};
     for (i64 k = blockIdx.x * (i64)blockDim.x + threadIdx.x; k < n; k += (i64)gridDim.x * blockDim.x)
         acc[0] += (double)x[k] * (double)y[k];
-    if (block_reduce_store<1>(acc, partial, counter) && threadIdx.x == 0) {
-        *counter = 0;
+    if (block_reduce_store<1>(acc, partial, counter)) {
         double d[1];
-        fold(partial, gridDim.x, 1, d);
+        fold<1>(partial, gridDim.x, d);
+        if (threadIdx.x != 0) return;
+        *counter = 0;
         *out = d[0];
     }
 }

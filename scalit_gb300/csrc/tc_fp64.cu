@@ -138,9 +138,22 @@ __device__ __forceinline__ void tmem_ld16(uint32_t taddr, float (&v)[16])
     for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
 }
 
-__device__ __forceinline__ uint16_t bf16_bits(double d)
+// Binary exponent e with |x| < 2^e for x != 0 (frexp's exponent), read from the bits.
+__device__ __forceinline__ int exp_of(unsigned long long bits)
 {
-    return __bfloat16_as_ushort(__float2bfloat16_rn((float)d));
+    const int ex = (int)((bits >> 52) & 0x7FF);
+    if (ex) return ex - 1022;
+    const unsigned long long m = bits & 0x000FFFFFFFFFFFFFULL;   // subnormal
+    return m ? (64 - __clzll(m)) - 1074 : -100000;
+}
+
+// 49-bit fixed-point magnitude of |x| 2^(49 - e) (truncated), e >= exponent of x.
+__device__ __forceinline__ unsigned long long fixed49(unsigned long long bits, int e)
+{
+    const int ex = (int)((bits >> 52) & 0x7FF);
+    const unsigned long long m = (bits & 0x000FFFFFFFFFFFFFULL) | (ex ? (1ULL << 52) : 0ULL);
+    const int sh = (ex ? ex : 1) - 1075 + 49 - e;   // <= -4
+    return (sh <= -64) ? 0ULL : (m >> (-sh));
 }
 
 __global__ void __launch_bounds__(kThreadsTC, 1)
@@ -171,16 +184,22 @@ tc_level_kernel(TcArgs g)
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
 
-    // this thread's grid row and its exponent
+    // BF16 bit patterns of the digits -127..127 (all exact in BF16)
+    uint16_t *bf_tab = reinterpret_cast<uint16_t *>(tslot + 4);
+    for (int i = tid; i < 255; i += kThreadsTC)
+        bf_tab[i] = __bfloat16_as_ushort(__float2bfloat16_rn((float)(i - 127)));
+
+    // this thread's grid row and its exponent (integer arithmetic on the bits)
     const int m = m0 + tid;
     const bool mvalid = m < g.M;
     const i64 moff = mvalid ? (i64)(m % g.Mi) * g.s1 + (i64)(m / g.Mi) * g.s2 : 0;
-    double mx = 0.0;
+    int em = -100000;
     if (mvalid)
-        for (int k = 0; k < g.K; ++k) mx = fmax(mx, fabs(A[moff + (i64)k * g.a_sk]));
-    int em = 0;
-    if (mx > 0.0) frexp(mx, &em);
-    const double to_digits = ldexp(1.0, 7 - em);
+        for (int k = 0; k < g.K; ++k) {
+            const unsigned long long b = (unsigned long long)__double_as_longlong(A[moff + (i64)k * g.a_sk]);
+            if (b << 1) em = max(em, exp_of(b));
+        }
+    if (em < -2000) em = 0;   // an all-zero row
 
     fence_before();
     __syncthreads();
@@ -194,12 +213,17 @@ tc_level_kernel(TcArgs g)
         if (ks >= 2 && !mbar_wait(&mbar[buf], ((ks - 2) >> 1) & 1)) { ok = false; break; }
         unsigned char *Ab = Abuf + buf * kAStepBytes;
         unsigned char *Bb = Bbuf + buf * bstep;
-        // cut this row's 16 values of the K step into 7 digit planes
-        double r[16];
+        // cut this row's 16 values of the K step into 7 digit planes: the digits
+        // are the 7-bit fields of the 49-bit fixed-point magnitude, with x's sign
+        unsigned long long F[16];
+        int sgn[16];
         #pragma unroll
         for (int j = 0; j < 16; ++j) {
             const int k = ks * 16 + j;
-            r[j] = (mvalid && k < g.K) ? A[moff + (i64)k * g.a_sk] * to_digits : 0.0;
+            const unsigned long long b = (mvalid && k < g.K)
+                ? (unsigned long long)__double_as_longlong(A[moff + (i64)k * g.a_sk]) : 0ULL;
+            F[j] = fixed49(b, em);
+            sgn[j] = (int)(b >> 63);
         }
         const int rowoff = (tid >> 3) * 256 + (tid & 7) * 16;
         #pragma unroll
@@ -207,10 +231,11 @@ tc_level_kernel(TcArgs g)
             uint32_t w[8];
             #pragma unroll
             for (int j = 0; j < 16; j += 2) {
-                const double d0 = trunc(r[j]), d1 = trunc(r[j + 1]);
-                r[j] = (r[j] - d0) * 128.0;
-                r[j + 1] = (r[j + 1] - d1) * 128.0;
-                w[j >> 1] = (uint32_t)bf16_bits(d0) | ((uint32_t)bf16_bits(d1) << 16);
+                const int d0 = (int)((F[j] >> (42 - 7 * s)) & 127u);
+                const int d1 = (int)((F[j + 1] >> (42 - 7 * s)) & 127u);
+                const uint32_t b0 = bf_tab[127 + (sgn[j] ? -d0 : d0)];
+                const uint32_t b1 = bf_tab[127 + (sgn[j + 1] ? -d1 : d1)];
+                w[j >> 1] = b0 | (b1 << 16);
             }
             unsigned char *plane = Ab + s * (kBM * 32);
             *reinterpret_cast<uint4 *>(plane + rowoff) = make_uint4(w[0], w[1], w[2], w[3]);
@@ -247,10 +272,11 @@ tc_level_kernel(TcArgs g)
     fence_after();
 
     if (ok) {
-        // epilogue: thread tid holds TMEM lane tid = grid row m
-        const double row_scale = ldexp(1.0, em - 14);
+        // epilogue: thread tid holds TMEM lane tid = grid row m.  The exact group
+        // sums are recombined in 64-bit integers: T = sum_{g<=5} G_g 2^(7(5-g))
+        // + floor(G_6 / 2^7) < 2^60, so C = T 2^(e_m + e_n - 49), one conversion.
         const double rs = (g.rowscale && mvalid) ? g.rowscale[m % g.Mi] : 1.0;
-        const double sc = g.alpha * rs;
+        const double sc = g.alpha * rs * ldexp(1.0, em - 49);
         const uint32_t lane_base = (uint32_t)(warp * 32) << 16;
         for (int c0 = 0; c0 < NT; c0 += 16) {
             float gv[kGroups][16];
@@ -262,10 +288,13 @@ tc_level_kernel(TcArgs g)
             for (int j = 0; j < 16; ++j) {
                 const int n = ntile * NT + c0 + j;
                 if (n >= g.N) continue;
-                double acc = (double)gv[kGroups - 1][j];
+                long long T = ((long long)__float2int_rn(gv[kGroups - 1][j])) >> 7;
                 #pragma unroll
-                for (int q = kGroups - 2; q >= 0; --q) acc = fma(acc, 0.0078125, (double)gv[q][j]);
-                const double val = acc * row_scale * ldexp(1.0, g.bexp[n]);
+                for (int q = kGroups - 2; q >= 0; --q)
+                    T += (long long)__float2int_rn(gv[q][j]) << (7 * (kGroups - 2 - q));
+                double val = (double)T;
+                if (T != 0)   // times 2^e_n by an exponent add on the bits (no FP64 op)
+                    val = __longlong_as_double(__double_as_longlong(val) + ((long long)g.bexp[n] << 52));
                 const i64 p = moff + (i64)n * g.c_sn;
                 double out = sc * val;
                 if (g.diagV) out = fma(g.alpha * (g.diagV[p] - g.shift), g.diagX[p + (i64)z * g.dx_sz], out);
@@ -387,7 +416,7 @@ int tc_level_apply(const scalit_ctx *c, int l, const double *X, double *Y, int a
     g.err = c->tc_err;
     g.bdig = reinterpret_cast<const uint4 *>(t.dig);
     g.bexp = t.exps;
-    const size_t smem = 2 * (size_t)kAStepBytes + 2 * (size_t)kDigits * t.NT * 32 + 64;
+    const size_t smem = 2 * (size_t)kAStepBytes + 2 * (size_t)kDigits * t.NT * 32 + 64 + 512;
     // at least half of the SM's shared memory, so one CTA (and one TMEM owner) per SM
     const size_t smem_req = std::max(smem, (size_t)(116 * 1024));
     SC_CUDA(cudaFuncSetAttribute(tc_level_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_req));
