@@ -235,6 +235,15 @@ int scalit_hf_gradients(scalit_ctx *ctx, int m, const double *psi, int np, const
 int scalit_pist_vectors(scalit_ctx *ctx, const scalit_pist_params *p, const double *x0, double *eig,
                         double *res, scalit_pist_info *info, double *vectors);
 
+/* PIST followed by the output of PISTF_CONV (src/iterate/libiterate/pist/pistf.f90:98-104):
+ * on success *cnt receives the final Krylov size, ritz the cnt Ritz values of
+ * the last Rayleigh-Ritz step, hmat HMAT(1:cnt, 1:cnt) column-major and vj the
+ * basis VJ(1:N, 1:cnt).  Size the buffers for p->m_max (ritz: m_max, hmat:
+ * m_max^2, vj: npoints * m_max).  Any of ritz/hmat/vj may be NULL. */
+int scalit_pist_basis(scalit_ctx *ctx, const scalit_pist_params *p, const double *x0, double *eig,
+                      double *res, scalit_pist_info *info, int *cnt, double *ritz, double *hmat,
+                      double *vj);
+
 /* -------------------------------------------- Fortran drop-in symbols -----
  * The external routines the reference's modules call, with gfortran naming
  * (lower case, trailing underscore) and every argument by reference.  They

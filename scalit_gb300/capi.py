@@ -58,6 +58,7 @@ SIGNATURES = {
     "scalit_hx_adjoint_f32_device": (C.c_int, [_vp, C.c_int, _vp, _vp, _vp, _vp, _vp]),
     "scalit_hf_gradients": (C.c_int, [_vp, C.c_int, _dp, C.c_int, _dp, _dp]),
     "scalit_pist_vectors": (C.c_int, [_vp, _vp, _dp, _dp, _dp, _vp, _dp]),
+    "scalit_pist_basis": (C.c_int, [_vp, _vp, _dp, _dp, _dp, _vp, _ip, _dp, _dp, _dp]),
     # Fortran drop-ins (all arguments by reference)
     "h1x_xyz_": (None, [_ip, _ip, _ip, _dp, _dp, _dp]),
     "h1x_xyz_seq_": (None, [_ip, _ip, _ip, _dp, _dp, _dp]),
@@ -311,7 +312,7 @@ class Context:
 
     def pist(self, x0, m, e0, etol, startcnt=0, stepcnt=5, m_max=0, gap=1, qmr_max=2000,
              qmr_tol=1e-4, qmr_ntype=-1, precision=PREC_FP64, ntype=0, verbose=False, orth=1,
-             vectors=False):
+             vectors=False, basis=False):
         """OSB_PISTCONV: returns (status, eig[m], RES, info dict); with vectors=True the
         info dict also holds the m Ritz vectors ("vectors", m x N)."""
         p = PistParams()
@@ -327,6 +328,18 @@ class Context:
         eig = np.zeros(int(m))
         res = C.c_double(0.0)
         info = PistInfo()
+        if basis:
+            mm = int(p.m_max)
+            cnt = C.c_int(0)
+            ritz = np.zeros(mm)
+            hmat = np.zeros(mm * mm)
+            vj = np.zeros(mm * self.N)
+            st = _check(self.lib.scalit_pist_basis(self.h, C.byref(p), _p(x0), _p(eig), C.byref(res),
+                                                   C.byref(info), C.byref(cnt), _p(ritz), _p(hmat), _p(vj)))
+            k = cnt.value
+            return st, eig, res.value, dict(info.as_dict(), m_max=p.m_max, startcnt=p.startcnt, cnt=k,
+                                            ritz=ritz[:k], hmat=hmat[:k * k].reshape(k, k, order="F"),
+                                            vj=vj[:k * self.N].reshape(self.N, k, order="F"))
         if vectors:
             vec = np.zeros((int(m), self.N))
             st = _check(self.lib.scalit_pist_vectors(self.h, C.byref(p), _p(x0), _p(eig), C.byref(res),

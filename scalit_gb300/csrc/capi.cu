@@ -521,6 +521,23 @@ int scalit_pist_vectors(scalit_ctx *c, const scalit_pist_params *p, const double
     return rc;
 }
 
+int scalit_pist_basis(scalit_ctx *c, const scalit_pist_params *p, const double *x0, double *eig, double *res,
+                      scalit_pist_info *info, int *cnt, double *ritz, double *hmat, double *vj)
+{
+    CTX_CHECK(c);
+    if (!p || !x0 || !eig || !res) { set_error("null argument"); return SCALIT_EINVAL; }
+    const i64 N = c->L.N;
+    double *dx = nullptr;
+    SC_CUDA(cudaMallocAsync(&dx, sizeof(double) * (size_t)N, c->stream));
+    SC_CUDA(cudaMemcpyAsync(dx, x0, sizeof(double) * N, cudaMemcpyHostToDevice, c->stream));
+    PistBasisOut b;
+    b.cnt = cnt; b.ritz = ritz; b.hmat = hmat; b.vj = vj;
+    int rc = pist_ctx(c, p, dx, eig, res, info, nullptr, &b);
+    cudaFreeAsync(dx, c->stream);
+    cudaStreamSynchronize(c->stream);
+    return rc;
+}
+
 // ------------------------------------------------------ differentiation --
 int scalit_hx_adjoint_device(scalit_ctx *c, int ntype, const double *dX, const double *dYbar, double *dXbar,
                              double *dVbar, double *dH0bar)

@@ -200,9 +200,12 @@ struct PistOps {
     virtual int h0x(const double *dX, double *dY) = 0;                  // H * x
     virtual int linsolv(const double *dB, double *dX, int *num) = 0;   // (H - E0) x = b
 };
+struct PistBasisOut { int *cnt = nullptr; double *ritz = nullptr, *hmat = nullptr, *vj = nullptr; };
 int pist_core(scalit_ctx *c, i64 N, const scalit_pist_params *p, const double *dx0, PistOps &ops,
-              double *eig, double *res, scalit_pist_info *info, double *vectors_host = nullptr);
+              double *eig, double *res, scalit_pist_info *info, double *vectors_host = nullptr,
+              const PistBasisOut *basis = nullptr);
 int pist_ctx(scalit_ctx *c, const scalit_pist_params *p, const double *dx0, double *eig,
-             double *res, scalit_pist_info *info, double *vectors_host = nullptr);
+             double *res, scalit_pist_info *info, double *vectors_host = nullptr,
+             const PistBasisOut *basis = nullptr);
 
 }  // namespace sc

@@ -296,7 +296,8 @@ static double now()
 }
 
 int pist_core(scalit_ctx *c, i64 N, const scalit_pist_params *p, const double *dx0, PistOps &ops,
-              double *eig, double *res, scalit_pist_info *info, double *vectors_host)
+              double *eig, double *res, scalit_pist_info *info, double *vectors_host,
+              const PistBasisOut *basis)
 {
     cudaStream_t s = c->stream;
     const int M = p->m, MM = p->m_max;
@@ -471,6 +472,20 @@ int pist_core(scalit_ctx *c, i64 N, const scalit_pist_params *p, const double *d
         if (cnt_low >= MM) { status = -MM; break; }
         cnt_high = std::min(cnt_high + p->stepcnt, MM);
     }
+    if (basis && rc == 0 && status > 0) {
+        const int cnt = status;
+        if (basis->cnt) *basis->cnt = cnt;
+        if (basis->ritz) for (int i = 0; i < cnt; ++i) basis->ritz[i] = tmp[i];
+        if (basis->hmat) {
+            gather_upper_kernel<<<egrid((i64)cnt * cnt), kT, 0, s>>>(cnt, HMAT, MM, A);
+            if (cudaMemcpyAsync(basis->hmat, A, sizeof(double) * (size_t)cnt * cnt, cudaMemcpyDeviceToHost, s) != cudaSuccess)
+                rc = SCALIT_ECUDA;
+        }
+        if (basis->vj && cudaMemcpyAsync(basis->vj, VJ, sizeof(double) * (size_t)N * cnt, cudaMemcpyDeviceToHost, s) != cudaSuccess)
+            rc = SCALIT_ECUDA;
+        cudaStreamSynchronize(s);
+        if (rc) set_error("copying the PIST basis out failed");
+    }
     if (vectors_host && rc == 0 && status > 0) {
         int r2 = ritz_vectors(c, N, VJ, HMAT, MM, status, p->e0, M, A, EV, work, lwork, devinfo, vectors_host);
         if (r2) rc = r2;
@@ -504,13 +519,13 @@ struct CtxOps : PistOps {
 };
 
 int pist_ctx(scalit_ctx *c, const scalit_pist_params *p, const double *dx0, double *eig, double *res,
-             scalit_pist_info *info, double *vectors_host)
+             scalit_pist_info *info, double *vectors_host, const PistBasisOut *basis)
 {
     if (!c->osb_built) { set_error("PIST needs the preconditioner: build or load it first"); return SCALIT_ESTATE; }
     CtxOps ops;
     ops.c = c;
     ops.p = p;
-    return pist_core(c, c->L.N, p, dx0, ops, eig, res, info, vectors_host);
+    return pist_core(c, c->L.N, p, dx0, ops, eig, res, info, vectors_host, basis);
 }
 
 }  // namespace sc

@@ -18,11 +18,12 @@
 // in its own TMEM accumulator; the epilogue reads them with tcgen05.ld and
 // recombines them in FP64.
 //
-// Structure of a CTA (128 threads, one M tile of 128 grid rows, one N tile):
-// each thread owns one row: it finds the row's exponent, then for every
-// 16-wide K step cuts its 16 values into 7 digit planes written to shared
-// memory in the K-major canonical layout (8x16-byte core matrices, no
-// swizzle); the K step's pre-cut B digit planes are copied next to them;
+// Structure of a CTA (256 threads, one M tile of 128 grid rows, one N tile):
+// two threads own each row.  The FP64 operand streams through shared memory
+// in 16-wide K slabs by cp.async (a 3-deep ring), twice: the first pass finds
+// each row's exponent, the second cuts every slab into 7 digit planes written
+// to shared memory in the K-major canonical layout (8x16-byte core matrices,
+// no swizzle); the K step's pre-cut B digit planes are copied next to them;
 // thread 0 issues the 28 tcgen05.mma (kind::f16, BF16 x BF16 -> FP32) and a
 // tcgen05.commit on the buffer's mbarrier.  Two buffers let the cutting of
 // step k+1 overlap the MMAs of step k.  Every mbarrier wait is bounded: on
@@ -42,8 +43,9 @@ namespace sc {
 static constexpr int kDigits = 7;
 static constexpr int kGroups = 7;
 static constexpr int kBM = 128;
-static constexpr int kThreadsTC = 128;
+static constexpr int kThreadsTC = 256;   // two threads per grid row
 static constexpr int kTmemCols = 512;
+static constexpr int kStages = 3;                               // FP64 slab ring depth
 static constexpr int kAStepBytes = kDigits * kBM * 16 * 2;    // 7 digit planes of 128 x 16 BF16
 static constexpr long long kWaitLimit = 1LL << 24;            // mbarrier polls before giving up
 
@@ -125,17 +127,15 @@ __device__ __forceinline__ bool mbar_wait(uint64_t *mbar, uint32_t parity)
 __device__ __forceinline__ void fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
 __device__ __forceinline__ void fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
 
-__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float (&v)[16])
+__device__ __forceinline__ void tmem_ld8(uint32_t taddr, float (&v)[8])
 {
-    uint32_t r[16];
+    uint32_t r[8];
     asm volatile(
-        "tcgen05.ld.sync.aligned.32x32b.x16.b32 "
-        "{%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, %15}, [%16];"
-        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
-          "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+        "tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7])
         : "r"(taddr));
     #pragma unroll
-    for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
+    for (int i = 0; i < 8; ++i) v[i] = __uint_as_float(r[i]);
 }
 
 // Binary exponent e with |x| < 2^e for x != 0 (frexp's exponent), read from the bits.
@@ -165,7 +165,8 @@ tc_level_kernel(TcArgs g)
     const int bstep = kDigits * NT * 32;                   // bytes of one K step of B digits
     unsigned char *Abuf = smem;                            // 2 x kAStepBytes
     unsigned char *Bbuf = smem + 2 * kAStepBytes;          // 2 x bstep
-    uint64_t *mbar = reinterpret_cast<uint64_t *>(Bbuf + 2 * bstep);
+    double *slabs = reinterpret_cast<double *>(Bbuf + 2 * bstep);   // kStages x [16 k][128 rows]
+    uint64_t *mbar = reinterpret_cast<uint64_t *>(slabs + kStages * 16 * kBM);
     uint32_t *tslot = reinterpret_cast<uint32_t *>(mbar + 2);
 
     const int tid = threadIdx.x, warp = tid >> 5;
@@ -189,17 +190,57 @@ tc_level_kernel(TcArgs g)
     for (int i = tid; i < 255; i += kThreadsTC)
         bf_tab[i] = __bfloat16_as_ushort(__float2bfloat16_rn((float)(i - 127)));
 
-    // this thread's grid row and its exponent (integer arithmetic on the bits)
-    const int m = m0 + tid;
+    // this thread's grid row (two threads per row: half h takes the odd or even
+    // 8-wide halves of every K step) and the row's exponent (integer arithmetic)
+    int *em_row = reinterpret_cast<int *>(bf_tab + 256);
+    const int row = tid & (kBM - 1), half = tid >> 7;
+    const int m = m0 + row;
     const bool mvalid = m < g.M;
     const i64 moff = mvalid ? (i64)(m % g.Mi) * g.s1 + (i64)(m / g.Mi) * g.s2 : 0;
+    // FP64 operand slabs (16 K values x 128 rows) stream through a kStages ring by
+    // cp.async: pass 1 (slabs 0..KS-1) finds the row exponent, pass 2 (slabs
+    // KS..2KS-1) cuts the digits.  Thread (row, half) copies and reads the
+    // K values half, half+2, ..., half+14 of its row.
+    auto issue = [&](int t) {
+        if (t < 2 * KS) {
+            const int ks = t % KS;
+            double *st = slabs + (t % kStages) * 16 * kBM;
+            #pragma unroll
+            for (int i = 0; i < 8; ++i) {
+                const int j = half + 2 * i, k = ks * 16 + j;
+                double *dst = st + j * kBM + row;
+                if (mvalid && k < g.K) {
+                    const double *src = A + moff + (i64)k * g.a_sk;
+                    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;"
+                                 :: "r"(smem_addr(dst)), "l"(src) : "memory");
+                } else {
+                    *dst = 0.0;
+                }
+            }
+        }
+        asm volatile("cp.async.commit_group;" ::: "memory");
+    };
+    auto ready = [&]() {
+        asm volatile("cp.async.wait_group %0;" :: "n"(kStages - 2) : "memory");
+        __syncthreads();
+    };
+    for (int t = 0; t < kStages - 1; ++t) issue(t);
     int em = -100000;
-    if (mvalid)
-        for (int k = 0; k < g.K; ++k) {
-            const unsigned long long b = (unsigned long long)__double_as_longlong(A[moff + (i64)k * g.a_sk]);
+    for (int t = 0; t < KS; ++t) {
+        ready();
+        issue(t + kStages - 1);
+        const double *st = slabs + (t % kStages) * 16 * kBM;
+        #pragma unroll
+        for (int i = 0; i < 8; ++i) {
+            const unsigned long long b = (unsigned long long)__double_as_longlong(st[(half + 2 * i) * kBM + row]);
             if (b << 1) em = max(em, exp_of(b));
         }
-    if (em < -2000) em = 0;   // an all-zero row
+    }
+    if (half) em_row[row] = em;
+    __syncthreads();
+    if (!half) em_row[row] = max(em, em_row[row]) < -2000 ? 0 : max(em, em_row[row]);   // 0: all-zero row
+    __syncthreads();
+    em = em_row[row];
 
     fence_before();
     __syncthreads();
@@ -213,33 +254,35 @@ tc_level_kernel(TcArgs g)
         if (ks >= 2 && !mbar_wait(&mbar[buf], ((ks - 2) >> 1) & 1)) { ok = false; break; }
         unsigned char *Ab = Abuf + buf * kAStepBytes;
         unsigned char *Bb = Bbuf + buf * bstep;
-        // cut this row's 16 values of the K step into 7 digit planes: the digits
-        // are the 7-bit fields of the 49-bit fixed-point magnitude, with x's sign
-        unsigned long long F[16];
-        int sgn[16];
+        const int t = KS + ks;
+        ready();
+        issue(t + kStages - 1);
+        const double *st = slabs + (t % kStages) * 16 * kBM;
+        // cut this row's 8 values of the K step (this thread's half) into 7 digit
+        // planes: the digits are the 7-bit fields of the 49-bit fixed-point
+        // magnitude, with x's sign.  The slab holds K values half, half+2, ..;
+        // the digit layout wants half*8 .. half*8+7: read those from the slab.
+        unsigned long long F[8];
+        int sgn[8];
         #pragma unroll
-        for (int j = 0; j < 16; ++j) {
-            const int k = ks * 16 + j;
-            const unsigned long long b = (mvalid && k < g.K)
-                ? (unsigned long long)__double_as_longlong(A[moff + (i64)k * g.a_sk]) : 0ULL;
+        for (int j = 0; j < 8; ++j) {
+            const unsigned long long b = (unsigned long long)__double_as_longlong(st[(half * 8 + j) * kBM + row]);
             F[j] = fixed49(b, em);
             sgn[j] = (int)(b >> 63);
         }
-        const int rowoff = (tid >> 3) * 256 + (tid & 7) * 16;
+        const int rowoff = (row >> 3) * 256 + half * 128 + (row & 7) * 16;
         #pragma unroll
         for (int s = 0; s < kDigits; ++s) {
-            uint32_t w[8];
+            uint32_t w[4];
             #pragma unroll
-            for (int j = 0; j < 16; j += 2) {
+            for (int j = 0; j < 8; j += 2) {
                 const int d0 = (int)((F[j] >> (42 - 7 * s)) & 127u);
                 const int d1 = (int)((F[j + 1] >> (42 - 7 * s)) & 127u);
                 const uint32_t b0 = bf_tab[127 + (sgn[j] ? -d0 : d0)];
                 const uint32_t b1 = bf_tab[127 + (sgn[j + 1] ? -d1 : d1)];
                 w[j >> 1] = b0 | (b1 << 16);
             }
-            unsigned char *plane = Ab + s * (kBM * 32);
-            *reinterpret_cast<uint4 *>(plane + rowoff) = make_uint4(w[0], w[1], w[2], w[3]);
-            *reinterpret_cast<uint4 *>(plane + rowoff + 128) = make_uint4(w[4], w[5], w[6], w[7]);
+            *reinterpret_cast<uint4 *>(Ab + s * (kBM * 32) + rowoff) = make_uint4(w[0], w[1], w[2], w[3]);
         }
         // the K step's B digit planes (pre-cut, already in the canonical layout)
         const uint4 *src = g.bdig + ((i64)ntile * KS + ks) * (bstep / 16);
@@ -264,6 +307,7 @@ tc_level_kernel(TcArgs g)
         }
     }
     if (ok) ok = mbar_wait(&mbar[(KS - 1) & 1], ((KS - 1) >> 1) & 1);
+    asm volatile("cp.async.wait_all;" ::: "memory");   // no copy of this CTA stays in flight
     if (!ok) {
         if (g.err) atomicExch(g.err, 1);
         // give in-flight MMAs a bounded chance to drain before freeing TMEM
@@ -277,15 +321,18 @@ tc_level_kernel(TcArgs g)
         // + floor(G_6 / 2^7) < 2^60, so C = T 2^(e_m + e_n - 49), one conversion.
         const double rs = (g.rowscale && mvalid) ? g.rowscale[m % g.Mi] : 1.0;
         const double sc = g.alpha * rs * ldexp(1.0, em - 49);
-        const uint32_t lane_base = (uint32_t)(warp * 32) << 16;
-        for (int c0 = 0; c0 < NT; c0 += 16) {
-            float gv[kGroups][16];
+        // warp w reads TMEM lanes 32 (w % 4) .. (its rows) and the column half w / 4
+        const uint32_t lane_base = (uint32_t)((warp & 3) * 32) << 16;
+        const int chalf = (NT / 2 + 7) / 8 * 8;
+        const int cbeg = (warp >> 2) * chalf, cend = min(NT, cbeg + chalf);
+        for (int c0 = cbeg; c0 < cend; c0 += 8) {
+            float gv[kGroups][8];
             #pragma unroll
-            for (int q = 0; q < kGroups; ++q) tmem_ld16(tbase + lane_base + (uint32_t)(q * NT + c0), gv[q]);
+            for (int q = 0; q < kGroups; ++q) tmem_ld8(tbase + lane_base + (uint32_t)(q * NT + c0), gv[q]);
             asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
             if (!mvalid) continue;
             #pragma unroll
-            for (int j = 0; j < 16; ++j) {
+            for (int j = 0; j < 8; ++j) {
                 const int n = ntile * NT + c0 + j;
                 if (n >= g.N) continue;
                 long long T = ((long long)__float2int_rn(gv[kGroups - 1][j])) >> 7;
@@ -416,7 +463,8 @@ int tc_level_apply(const scalit_ctx *c, int l, const double *X, double *Y, int a
     g.err = c->tc_err;
     g.bdig = reinterpret_cast<const uint4 *>(t.dig);
     g.bexp = t.exps;
-    const size_t smem = 2 * (size_t)kAStepBytes + 2 * (size_t)kDigits * t.NT * 32 + 64 + 512;
+    const size_t smem = 2 * (size_t)kAStepBytes + 2 * (size_t)kDigits * t.NT * 32 + (size_t)kStages * 16 * kBM * 8 +
+                        64 + 1200;
     // at least half of the SM's shared memory, so one CTA (and one TMEM owner) per SM
     const size_t smem_req = std::max(smem, (size_t)(116 * 1024));
     SC_CUDA(cudaFuncSetAttribute(tc_level_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_req));

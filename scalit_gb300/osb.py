@@ -80,14 +80,14 @@ class OSB:
             log(f" Time for block diagonalization (s): {time.perf_counter() - t0:.3f}")
 
     # OSB_PISTCONV (osbw.pistconv.h:16-50) with setPISTConvParam (:303-333)
-    def pist(self, x0=None, seed=0, verbose=False):
+    def pist(self, x0=None, seed=0, verbose=False, basis=False):
         inp = self.inp
         mE0, mTol, mStart, mStep, mMax, mNum, mGap = inp.sConv
         if x0 is None:
             x0 = np.random.default_rng(seed).random(inp.my_len)   # random_number(X)
         return self.ctx.pist(x0, mNum, mE0, mTol, startcnt=mStart, stepcnt=mStep, m_max=mMax,
                              gap=mGap, qmr_max=inp.sQMR[0], qmr_tol=inp.sQMR[1], qmr_ntype=-1,
-                             precision=self.precision, ntype=0, verbose=verbose)
+                             precision=self.precision, ntype=0, verbose=verbose, basis=basis)
 
     # progPistEig (osbw.progEig.h:6-98)
     def prog_pist_eig(self, log=print, **kw):
@@ -97,7 +97,13 @@ class OSB:
             log("      Get  Eigen Values Using PIST method        ")
             log(" ================================================")
             log(" ------  Bound states for Real Version of H0  -------")
+        if self.inp.sPT != 0:
+            kw = dict(kw, basis=True)
         st, eig, res, info = self.pist(**kw)
+        if self.inp.sPT != 0 and st > 0:
+            refio.save_pist_basis(self.inp.PTFile, info["cnt"], info["ritz"], info["hmat"], info["vj"])
+            if log:
+                log(f" PIST basis and HMAT written to {self.inp.PTFile}")
         if log:
             log(f" Max Lanczos Error: {res:.15E}  Eigen Values:")
             for i in range(0, len(eig), 3):

@@ -250,6 +250,65 @@ def save_data(path, data: np.ndarray) -> None:
                 break
 
 
+def save_records(path, records) -> None:
+    """Several unformatted sequential records (bytes each), sub-records over 2 GiB."""
+    with open(path, "wb") as f:
+        for buf in records:
+            pos, n = 0, len(buf)
+            while True:
+                chunk = buf[pos:pos + _MAX_SUBRECORD]
+                more = pos + len(chunk) < n
+                f.write(struct.pack("<i", -len(chunk) if more else len(chunk)))
+                f.write(chunk)
+                f.write(struct.pack("<i", -len(chunk) if pos > 0 else len(chunk)))
+                pos += len(chunk)
+                if not more:
+                    break
+
+
+def load_records(path):
+    """All records of an unformatted sequential file as bytes."""
+    out = []
+    with open(path, "rb") as f:
+        while True:
+            hdr = f.read(4)
+            if not hdr:
+                return out
+            rec = bytearray()
+            while True:
+                if len(hdr) != 4:
+                    raise ValueError(f"{path}: truncated record marker")
+                lead = struct.unpack("<i", hdr)[0]
+                chunk = f.read(abs(lead))
+                if len(chunk) != abs(lead) or len(f.read(4)) != 4:
+                    raise ValueError(f"{path}: truncated record")
+                rec += chunk
+                if lead >= 0:
+                    break
+                hdr = f.read(4)
+            out.append(bytes(rec))
+
+
+def save_pist_basis(path, cnt, ritz, hmat, vj) -> None:
+    """The PT file of PISTF_CONV (src/iterate/libiterate/pist/pistf.f90:98-104):
+    (cnt, N) / Ritz values, HMAT(cnt, cnt) / VJ(N, cnt)."""
+    n = vj.shape[0]
+    save_records(path, [struct.pack("<ii", int(cnt), int(n)),
+                        np.ascontiguousarray(ritz[:cnt], dtype="<f8").tobytes()
+                        + np.asfortranarray(hmat[:cnt, :cnt], dtype="<f8").tobytes(order="F"),
+                        np.asfortranarray(vj[:, :cnt], dtype="<f8").tobytes(order="F")])
+
+
+def load_pist_basis(path):
+    r = load_records(path)
+    cnt, n = struct.unpack("<ii", r[0][:8])
+    a = np.frombuffer(r[1], dtype="<f8")
+    ritz = a[:cnt].copy()
+    hmat = a[cnt:cnt + cnt * cnt].reshape(cnt, cnt, order="F").copy()
+    vj = np.frombuffer(r[2], dtype="<f8").reshape(n, cnt, order="F").copy()
+    return cnt, ritz, hmat, vj
+
+
 def load_data(path, n: int) -> np.ndarray:
     """Read the first ``n`` doubles of an unformatted sequential record."""
     out = bytearray()

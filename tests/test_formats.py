@@ -112,3 +112,29 @@ def test_problem_files(tmp_path):
     np.testing.assert_array_equal(refio.load_data(back.H0File, back.h0_len), p.H0)
     np.testing.assert_array_equal(refio.load_data_dir(back.RESFile, back.my_len), p.RES)
     np.testing.assert_array_equal(refio.load_data_dir(back.DEPFile, back.dep_len), p.DEP)
+
+
+def test_records_and_subrecords(tmp_path, monkeypatch):
+    recs = [b"\x01\x02\x03\x04" * 5, b"", b"x" * 37]
+    path = tmp_path / "r.dat"
+    monkeypatch.setattr(refio, "_MAX_SUBRECORD", 8)       # force sub-records
+    refio.save_records(path, recs)
+    assert refio.load_records(path) == recs
+
+
+def test_pist_basis_file_roundtrip(tmp_path):
+    rng = np.random.default_rng(3)
+    cnt, n = 5, 11
+    ritz = rng.standard_normal(cnt)
+    hmat = rng.standard_normal((cnt, cnt))
+    vj = rng.standard_normal((n, cnt))
+    path = tmp_path / "PT.dat"
+    refio.save_pist_basis(path, cnt, ritz, hmat, vj)
+    raw = path.read_bytes()
+    assert int.from_bytes(raw[:4], "little") == 8                       # record 1: (cnt, N)
+    assert int.from_bytes(raw[4:8], "little") == cnt
+    c2, r2, h2, v2 = refio.load_pist_basis(path)
+    assert c2 == cnt
+    np.testing.assert_array_equal(r2, ritz)
+    np.testing.assert_array_equal(h2, hmat)
+    np.testing.assert_array_equal(v2, vj)
