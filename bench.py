@@ -231,7 +231,7 @@ def pist_leg(workload, levels, device, capi, hm):
             t0 = time.perf_counter()
             ctx.build_osb(20, 1e-4)
             t1 = time.perf_counter()
-            st, eig, res, info = ctx.pist(x0, levels, e0, 1e-11, m_max=max(20 * levels, 400),
+            st, eig, res, info = ctx.pist(x0, levels, e0, 1e-11, m_max=max(8 * levels, 400),
                                           qmr_max=2000, qmr_tol=1e-4, precision=prec)
             t2 = time.perf_counter()
         eigs[name] = eig

@@ -18,8 +18,8 @@
 // in its own TMEM accumulator; the epilogue reads them with tcgen05.ld and
 // recombines them in FP64.
 //
-// Structure of a CTA (256 threads, one M tile of 128 grid rows, one N tile):
-// two threads own each row.  The FP64 operand streams through shared memory
+// Structure of a CTA (512 threads, one M tile of 128 grid rows, one N tile):
+// four threads own each row.  The FP64 operand streams through shared memory
 // in 16-wide K slabs by cp.async (a 3-deep ring), twice: the first pass finds
 // each row's exponent, the second cuts every slab into 7 digit planes written
 // to shared memory in the K-major canonical layout (8x16-byte core matrices,
@@ -43,9 +43,10 @@ namespace sc {
 static constexpr int kDigits = 7;
 static constexpr int kGroups = 7;
 static constexpr int kBM = 128;
-static constexpr int kThreadsTC = 256;   // two threads per grid row
+static constexpr int kThreadsTC = 512;   // four threads per grid row
 static constexpr int kTmemCols = 512;
 static constexpr int kStages = 3;                               // FP64 slab ring depth
+static constexpr int kSlab = kBM * 17;                          // doubles per slab stage
 static constexpr int kAStepBytes = kDigits * kBM * 16 * 2;    // 7 digit planes of 128 x 16 BF16
 static constexpr long long kWaitLimit = 1LL << 24;            // mbarrier polls before giving up
 
@@ -127,6 +128,15 @@ __device__ __forceinline__ bool mbar_wait(uint64_t *mbar, uint32_t parity)
 __device__ __forceinline__ void fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
 __device__ __forceinline__ void fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
 
+__device__ __forceinline__ void tmem_ld4(uint32_t taddr, float (&v)[4])
+{
+    uint32_t r[4];
+    asm volatile("tcgen05.ld.sync.aligned.32x32b.x4.b32 {%0, %1, %2, %3}, [%4];"
+                 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]) : "r"(taddr));
+    #pragma unroll
+    for (int i = 0; i < 4; ++i) v[i] = __uint_as_float(r[i]);
+}
+
 __device__ __forceinline__ void tmem_ld8(uint32_t taddr, float (&v)[8])
 {
     uint32_t r[8];
@@ -165,8 +175,8 @@ tc_level_kernel(TcArgs g)
     const int bstep = kDigits * NT * 32;                   // bytes of one K step of B digits
     unsigned char *Abuf = smem;                            // 2 x kAStepBytes
     unsigned char *Bbuf = smem + 2 * kAStepBytes;          // 2 x bstep
-    double *slabs = reinterpret_cast<double *>(Bbuf + 2 * bstep);   // kStages x [16 k][128 rows]
-    uint64_t *mbar = reinterpret_cast<uint64_t *>(slabs + kStages * 16 * kBM);
+    double *slabs = reinterpret_cast<double *>(Bbuf + 2 * bstep);   // kStages x kSlab
+    uint64_t *mbar = reinterpret_cast<uint64_t *>(slabs + kStages * kSlab);
     uint32_t *tslot = reinterpret_cast<uint32_t *>(mbar + 2);
 
     const int tid = threadIdx.x, warp = tid >> 5;
@@ -189,28 +199,43 @@ tc_level_kernel(TcArgs g)
     uint16_t *bf_tab = reinterpret_cast<uint16_t *>(tslot + 4);
     for (int i = tid; i < 255; i += kThreadsTC)
         bf_tab[i] = __bfloat16_as_ushort(__float2bfloat16_rn((float)(i - 127)));
+    int *em4 = reinterpret_cast<int *>(bf_tab + 256);       // [4][kBM] partial row exponents
 
-    // this thread's grid row (two threads per row: half h takes the odd or even
-    // 8-wide halves of every K step) and the row's exponent (integer arithmetic)
-    int *em_row = reinterpret_cast<int *>(bf_tab + 256);
-    const int row = tid & (kBM - 1), half = tid >> 7;
+    // Four threads per grid row: quarter q handles K values 4q..4q+3 of every
+    // 16-wide K step.
+    const int row = tid & (kBM - 1), q = tid >> 7;
     const int m = m0 + row;
     const bool mvalid = m < g.M;
     const i64 moff = mvalid ? (i64)(m % g.Mi) * g.s1 + (i64)(m / g.Mi) * g.s2 : 0;
     // FP64 operand slabs (16 K values x 128 rows) stream through a kStages ring by
-    // cp.async: pass 1 (slabs 0..KS-1) finds the row exponent, pass 2 (slabs
-    // KS..2KS-1) cuts the digits.  Thread (row, half) copies and reads the
-    // K values half, half+2, ..., half+14 of its row.
+    // cp.async: pass 1 (slabs 0..KS-1) finds the row exponents, pass 2 (slabs
+    // KS..2KS-1) cuts the digits.  When K is the contiguous index (a_sk == 1) a
+    // slab is stored row by row (stride 17) and consecutive threads copy
+    // consecutive K values of a row; otherwise K by K (rows contiguous) and
+    // consecutive threads copy consecutive rows.  Both keep the copies coalesced.
+    const bool rowc = (g.a_sk == 1);
+    i64 lmoff[4];
+    bool lvalid[4];
+    #pragma unroll
+    for (int i = 0; i < 4; ++i) {
+        const int r = rowc ? ((tid >> 4) + 32 * i) : row;
+        const int mm = m0 + r;
+        lvalid[i] = mm < g.M;
+        lmoff[i] = lvalid[i] ? (i64)(mm % g.Mi) * g.s1 + (i64)(mm / g.Mi) * g.s2 : 0;
+    }
     auto issue = [&](int t) {
         if (t < 2 * KS) {
             const int ks = t % KS;
-            double *st = slabs + (t % kStages) * 16 * kBM;
+            double *st = slabs + (t % kStages) * kSlab;
             #pragma unroll
-            for (int i = 0; i < 8; ++i) {
-                const int j = half + 2 * i, k = ks * 16 + j;
-                double *dst = st + j * kBM + row;
-                if (mvalid && k < g.K) {
-                    const double *src = A + moff + (i64)k * g.a_sk;
+            for (int i = 0; i < 4; ++i) {
+                int r, j;
+                if (rowc) { j = tid & 15; r = (tid >> 4) + 32 * i; }
+                else { r = row; j = q + 4 * i; }
+                const int k = ks * 16 + j;
+                double *dst = rowc ? st + r * 17 + j : st + j * kBM + r;
+                if (lvalid[i] && k < g.K) {
+                    const double *src = A + lmoff[i] + (i64)k * g.a_sk;
                     asm volatile("cp.async.ca.shared.global [%0], [%1], 8;"
                                  :: "r"(smem_addr(dst)), "l"(src) : "memory");
                 } else {
@@ -224,23 +249,25 @@ tc_level_kernel(TcArgs g)
         asm volatile("cp.async.wait_group %0;" :: "n"(kStages - 2) : "memory");
         __syncthreads();
     };
+    auto slab_val = [&](const double *st, int j) -> unsigned long long {   // K value j of this row
+        return (unsigned long long)__double_as_longlong(rowc ? st[row * 17 + j] : st[j * kBM + row]);
+    };
     for (int t = 0; t < kStages - 1; ++t) issue(t);
     int em = -100000;
     for (int t = 0; t < KS; ++t) {
         ready();
         issue(t + kStages - 1);
-        const double *st = slabs + (t % kStages) * 16 * kBM;
+        const double *st = slabs + (t % kStages) * kSlab;
         #pragma unroll
-        for (int i = 0; i < 8; ++i) {
-            const unsigned long long b = (unsigned long long)__double_as_longlong(st[(half + 2 * i) * kBM + row]);
+        for (int jj = 0; jj < 4; ++jj) {
+            const unsigned long long b = slab_val(st, q * 4 + jj);
             if (b << 1) em = max(em, exp_of(b));
         }
     }
-    if (half) em_row[row] = em;
+    em4[q * kBM + row] = em;
     __syncthreads();
-    if (!half) em_row[row] = max(em, em_row[row]) < -2000 ? 0 : max(em, em_row[row]);   // 0: all-zero row
-    __syncthreads();
-    em = em_row[row];
+    em = max(max(em4[row], em4[kBM + row]), max(em4[2 * kBM + row], em4[3 * kBM + row]));
+    if (em < -2000) em = 0;   // an all-zero row
 
     fence_before();
     __syncthreads();
@@ -257,32 +284,31 @@ tc_level_kernel(TcArgs g)
         const int t = KS + ks;
         ready();
         issue(t + kStages - 1);
-        const double *st = slabs + (t % kStages) * 16 * kBM;
-        // cut this row's 8 values of the K step (this thread's half) into 7 digit
-        // planes: the digits are the 7-bit fields of the 49-bit fixed-point
-        // magnitude, with x's sign.  The slab holds K values half, half+2, ..;
-        // the digit layout wants half*8 .. half*8+7: read those from the slab.
-        unsigned long long F[8];
-        int sgn[8];
+        const double *st = slabs + (t % kStages) * kSlab;
+        // cut this row's 4 values of the K step (this thread's quarter) into 7
+        // digit planes: the digits are the 7-bit fields of the 49-bit fixed-point
+        // magnitude, with x's sign
+        unsigned long long F[4];
+        int sgn[4];
         #pragma unroll
-        for (int j = 0; j < 8; ++j) {
-            const unsigned long long b = (unsigned long long)__double_as_longlong(st[(half * 8 + j) * kBM + row]);
-            F[j] = fixed49(b, em);
-            sgn[j] = (int)(b >> 63);
+        for (int jj = 0; jj < 4; ++jj) {
+            const unsigned long long b = slab_val(st, q * 4 + jj);
+            F[jj] = fixed49(b, em);
+            sgn[jj] = (int)(b >> 63);
         }
-        const int rowoff = (row >> 3) * 256 + half * 128 + (row & 7) * 16;
+        const int rowoff = (row >> 3) * 256 + (q >> 1) * 128 + (row & 7) * 16 + (q & 1) * 8;
         #pragma unroll
         for (int s = 0; s < kDigits; ++s) {
-            uint32_t w[4];
+            uint32_t w[2];
             #pragma unroll
-            for (int j = 0; j < 8; j += 2) {
-                const int d0 = (int)((F[j] >> (42 - 7 * s)) & 127u);
-                const int d1 = (int)((F[j + 1] >> (42 - 7 * s)) & 127u);
-                const uint32_t b0 = bf_tab[127 + (sgn[j] ? -d0 : d0)];
-                const uint32_t b1 = bf_tab[127 + (sgn[j + 1] ? -d1 : d1)];
-                w[j >> 1] = b0 | (b1 << 16);
+            for (int jj = 0; jj < 4; jj += 2) {
+                const int d0 = (int)((F[jj] >> (42 - 7 * s)) & 127u);
+                const int d1 = (int)((F[jj + 1] >> (42 - 7 * s)) & 127u);
+                const uint32_t b0 = bf_tab[127 + (sgn[jj] ? -d0 : d0)];
+                const uint32_t b1 = bf_tab[127 + (sgn[jj + 1] ? -d1 : d1)];
+                w[jj >> 1] = b0 | (b1 << 16);
             }
-            *reinterpret_cast<uint4 *>(Ab + s * (kBM * 32) + rowoff) = make_uint4(w[0], w[1], w[2], w[3]);
+            *reinterpret_cast<uint2 *>(Ab + s * (kBM * 32) + rowoff) = make_uint2(w[0], w[1]);
         }
         // the K step's B digit planes (pre-cut, already in the canonical layout)
         const uint4 *src = g.bdig + ((i64)ntile * KS + ks) * (bstep / 16);
@@ -321,24 +347,24 @@ tc_level_kernel(TcArgs g)
         // + floor(G_6 / 2^7) < 2^60, so C = T 2^(e_m + e_n - 49), one conversion.
         const double rs = (g.rowscale && mvalid) ? g.rowscale[m % g.Mi] : 1.0;
         const double sc = g.alpha * rs * ldexp(1.0, em - 49);
-        // warp w reads TMEM lanes 32 (w % 4) .. (its rows) and the column half w / 4
+        // warp w reads TMEM lanes 32 (w % 4) .. (its rows) and the column quarter w / 4
         const uint32_t lane_base = (uint32_t)((warp & 3) * 32) << 16;
-        const int chalf = (NT / 2 + 7) / 8 * 8;
-        const int cbeg = (warp >> 2) * chalf, cend = min(NT, cbeg + chalf);
-        for (int c0 = cbeg; c0 < cend; c0 += 8) {
-            float gv[kGroups][8];
+        const int cq = NT / 4;                       // NT is a multiple of 16
+        const int cbeg = (warp >> 2) * cq, cend = cbeg + cq;
+        for (int c0 = cbeg; c0 < cend; c0 += 4) {
+            float gv[kGroups][4];
             #pragma unroll
-            for (int q = 0; q < kGroups; ++q) tmem_ld8(tbase + lane_base + (uint32_t)(q * NT + c0), gv[q]);
+            for (int gq = 0; gq < kGroups; ++gq) tmem_ld4(tbase + lane_base + (uint32_t)(gq * NT + c0), gv[gq]);
             asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
             if (!mvalid) continue;
             #pragma unroll
-            for (int j = 0; j < 8; ++j) {
+            for (int j = 0; j < 4; ++j) {
                 const int n = ntile * NT + c0 + j;
                 if (n >= g.N) continue;
                 long long T = ((long long)__float2int_rn(gv[kGroups - 1][j])) >> 7;
                 #pragma unroll
-                for (int q = kGroups - 2; q >= 0; --q)
-                    T += (long long)__float2int_rn(gv[q][j]) << (7 * (kGroups - 2 - q));
+                for (int gq = kGroups - 2; gq >= 0; --gq)
+                    T += (long long)__float2int_rn(gv[gq][j]) << (7 * (kGroups - 2 - gq));
                 double val = (double)T;
                 if (T != 0)   // times 2^e_n by an exponent add on the bits (no FP64 op)
                     val = __longlong_as_double(__double_as_longlong(val) + ((long long)g.bexp[n] << 52));
@@ -463,8 +489,8 @@ int tc_level_apply(const scalit_ctx *c, int l, const double *X, double *Y, int a
     g.err = c->tc_err;
     g.bdig = reinterpret_cast<const uint4 *>(t.dig);
     g.bexp = t.exps;
-    const size_t smem = 2 * (size_t)kAStepBytes + 2 * (size_t)kDigits * t.NT * 32 + (size_t)kStages * 16 * kBM * 8 +
-                        64 + 1200;
+    const size_t smem = 2 * (size_t)kAStepBytes + 2 * (size_t)kDigits * t.NT * 32 + (size_t)kStages * kSlab * 8 +
+                        64 + 3072;
     // at least half of the SM's shared memory, so one CTA (and one TMEM owner) per SM
     const size_t smem_req = std::max(smem, (size_t)(116 * 1024));
     SC_CUDA(cudaFuncSetAttribute(tc_level_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_req));
