@@ -115,6 +115,10 @@ int scalit_hx_f32_device(scalit_ctx *ctx, int ntype, int nvec, const float *dX, 
  * and max Jacobi efficiency, their sum, the sum of squared diagonals and the
  * sum of sweep counters (the reference's eff(1:5)). */
 int scalit_build_osb(scalit_ctx *ctx, int bjmax, double bjtol, double *stats);
+/* Wall seconds spent on each level (sF entries, level 1 first) by the last
+ * scalit_build_osb; the reference prints the whole build's time only
+ * (osb.progDiag.h:40-47). */
+int scalit_build_times(scalit_ctx *ctx, double *seconds);
 /* Copy the preconditioner out (VOSB: scalit_vosb_len doubles, EIG0: npoints)
  * or in (sVOSB < 0 path: loadVOSB/loadEig, osb.io.h:124-208). */
 int scalit_get_osb(scalit_ctx *ctx, double *VOSB, double *EIG0);
@@ -186,7 +190,10 @@ typedef struct {
     int orth;         /* 0: one modified Gram-Schmidt pass in the        */
                       /*    reference's order (MGS_ORTH);                */
                       /* 1: classical Gram-Schmidt twice (default: keeps */
-                      /*    the basis orthonormal over long runs)        */
+                      /*    the basis orthonormal over long runs);       */
+                      /* 2: as 1 with the first pass in FP32 against an  */
+                      /*    FP32 copy of the basis (N x m_max floats);   */
+                      /*    the second pass stays FP64                   */
 } scalit_pist_params;
 
 typedef struct {
@@ -197,7 +204,8 @@ typedef struct {
     double t_qmr;      /* seconds in QMR solves                          */
     double t_orth;     /* seconds in re-orthogonalisation                */
     double t_hmat;     /* seconds building HMAT columns                  */
-    double t_ritz;     /* seconds in the Ritz eigen-solves               */
+    double t_ritz;     /* seconds waiting for the Ritz eigen-solves      */
+    double t_resid;    /* seconds in the final Ritz-vector residual check */
 } scalit_pist_info;
 
 /* Fill params from the input-file values the way setPISTConvParam does:
@@ -234,6 +242,12 @@ int scalit_hf_gradients(scalit_ctx *ctx, int m, const double *psi, int np, const
  * the eigenvector of HMAT (DSYEV 'V' in place of the reference's 'N'). */
 int scalit_pist_vectors(scalit_ctx *ctx, const scalit_pist_params *p, const double *x0, double *eig,
                         double *res, scalit_pist_info *info, double *vectors);
+/* PIST as scalit_pist, followed by the final FP64 residual check of the
+ * converged levels: resid[k] = |H psi_k - eig_k psi_k|_2 for the normalised
+ * Ritz vector psi_k (H without shift, one batched FP64 H*X on the device).
+ * The reference reports no residuals (pist.f90 returns eigenvalues only). */
+int scalit_pist_residuals(scalit_ctx *ctx, const scalit_pist_params *p, const double *x0, double *eig,
+                          double *res, scalit_pist_info *info, double *resid);
 
 /* PIST followed by the output of PISTF_CONV (src/iterate/libiterate/pist/pistf.f90:98-104):
  * on success *cnt receives the final Krylov size, ritz the cnt Ritz values of

@@ -42,6 +42,7 @@ SIGNATURES = {
     "scalit_hx_f32_device": (C.c_int, [_vp, C.c_int, C.c_int, _vp, _vp]),
     "scalit_level_device": (C.c_int, [_vp, C.c_int, C.c_int, _vp, _vp]),
     "scalit_build_osb": (C.c_int, [_vp, C.c_int, C.c_double, _dp]),
+    "scalit_build_times": (C.c_int, [_vp, _dp]),
     "scalit_get_osb": (C.c_int, [_vp, _dp, _dp]),
     "scalit_set_osb": (C.c_int, [_vp, _dp, _dp]),
     "scalit_px": (C.c_int, [_vp, C.c_int, C.c_int, _dp, _dp]),
@@ -58,6 +59,7 @@ SIGNATURES = {
     "scalit_hx_adjoint_f32_device": (C.c_int, [_vp, C.c_int, _vp, _vp, _vp, _vp, _vp]),
     "scalit_hf_gradients": (C.c_int, [_vp, C.c_int, _dp, C.c_int, _dp, _dp]),
     "scalit_pist_vectors": (C.c_int, [_vp, _vp, _dp, _dp, _dp, _vp, _dp]),
+    "scalit_pist_residuals": (C.c_int, [_vp, _vp, _dp, _dp, _dp, _vp, _dp]),
     "scalit_pist_basis": (C.c_int, [_vp, _vp, _dp, _dp, _dp, _vp, _ip, _dp, _dp, _dp]),
     # Fortran drop-ins (all arguments by reference)
     "h1x_xyz_": (None, [_ip, _ip, _ip, _dp, _dp, _dp]),
@@ -104,7 +106,7 @@ class PistParams(C.Structure):
 class PistInfo(C.Structure):
     _fields_ = [("krylov", C.c_int), ("qmr_total", C.c_int), ("qmr_solves", C.c_int),
                 ("checks", C.c_int), ("t_qmr", C.c_double), ("t_orth", C.c_double),
-                ("t_hmat", C.c_double), ("t_ritz", C.c_double)]
+                ("t_hmat", C.c_double), ("t_ritz", C.c_double), ("t_resid", C.c_double)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}
@@ -247,6 +249,11 @@ class Context:
         _check(self.lib.scalit_build_osb(self.h, int(bjmax), float(bjtol), _p(stats)))
         return stats.reshape(len(self.sizes), 5)
 
+    def build_times(self):
+        t = np.zeros(len(self.sizes))
+        _check(self.lib.scalit_build_times(self.h, _p(t)))
+        return t
+
     def get_osb(self):
         V = np.empty(self.vosb_len)
         E = np.empty(self.N)
@@ -312,9 +319,10 @@ class Context:
 
     def pist(self, x0, m, e0, etol, startcnt=0, stepcnt=5, m_max=0, gap=1, qmr_max=2000,
              qmr_tol=1e-4, qmr_ntype=-1, precision=PREC_FP64, ntype=0, verbose=False, orth=1,
-             vectors=False, basis=False):
+             vectors=False, basis=False, residuals=False):
         """OSB_PISTCONV: returns (status, eig[m], RES, info dict); with vectors=True the
-        info dict also holds the m Ritz vectors ("vectors", m x N)."""
+        info dict also holds the m Ritz vectors ("vectors", m x N); with residuals=True
+        it holds the FP64 residual norms |H psi - E psi| of the levels ("resid", m)."""
         p = PistParams()
         self.lib.scalit_pist_default_params(C.byref(p), int(m), float(e0), float(etol),
                                             int(startcnt), int(stepcnt), int(m_max), int(gap),
@@ -340,6 +348,11 @@ class Context:
             return st, eig, res.value, dict(info.as_dict(), m_max=p.m_max, startcnt=p.startcnt, cnt=k,
                                             ritz=ritz[:k], hmat=hmat[:k * k].reshape(k, k, order="F"),
                                             vj=vj[:k * self.N].reshape(self.N, k, order="F"))
+        if residuals:
+            resid = np.zeros(int(m))
+            st = _check(self.lib.scalit_pist_residuals(self.h, C.byref(p), _p(x0), _p(eig), C.byref(res),
+                                                       C.byref(info), _p(resid)))
+            return st, eig, res.value, dict(info.as_dict(), m_max=p.m_max, startcnt=p.startcnt, resid=resid)
         if vectors:
             vec = np.zeros((int(m), self.N))
             st = _check(self.lib.scalit_pist_vectors(self.h, C.byref(p), _p(x0), _p(eig), C.byref(res),

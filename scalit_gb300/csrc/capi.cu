@@ -64,6 +64,7 @@ int work_get(scalit_ctx *c, size_t bytes, void **out)
         }
         SC_CUDA(cudaMalloc(&c->work, bytes));
         c->work_bytes = bytes;
+        c->gen++;
     }
     *out = c->work;
     return 0;
@@ -165,8 +166,10 @@ void scalit_destroy(scalit_ctx *c)
     for (int l = 0; l < SCALIT_FMAX; ++l) {
         if (c->tc[l].dig) cudaFree(c->tc[l].dig);
         if (c->tc[l].exps) cudaFree(c->tc[l].exps);
+        if (l == 0) tc_free_px(c);
     }
     if (c->tc_err) cudaFree(c->tc_err);
+    for (int i = 0; i < 2; ++i) if (c->qg[i].exec) cudaGraphExecDestroy(c->qg[i].exec);
     if (c->red_counter) cudaFree(c->red_counter);
     if (c->work) cudaFree(c->work);
     if (c->h_pinned) cudaFreeHost(c->h_pinned);
@@ -267,6 +270,7 @@ int scalit_set_fp64_mode(scalit_ctx *c, int mode)
     if (!c) { set_error("null context"); return SCALIT_EINVAL; }
     if (mode != SCALIT_FP64_DFMA && mode != SCALIT_FP64_TENSOR) { set_error("unknown FP64 mode %d", mode); return SCALIT_EINVAL; }
     c->fp64_mode = mode;
+    c->gen++;
     return 0;
 }
 
@@ -286,6 +290,7 @@ int scalit_set_shift(scalit_ctx *c, double e0)
     if (!c) { set_error("null context"); return SCALIT_EINVAL; }
     if (!std::isfinite(e0)) { set_error("non-finite shift"); return SCALIT_ENONFINITE; }
     c->E0 = e0;
+    c->gen++;
     return 0;
 }
 
@@ -299,6 +304,7 @@ int scalit_set_precond(scalit_ctx *c, int kind, double de, double beta)
         return SCALIT_EINVAL;
     }
     c->osb_kind = kind;
+    c->gen++;
     c->osb_de = fabs(de);
     c->osb_beta = beta;
     return 0;
@@ -406,6 +412,14 @@ int scalit_build_osb(scalit_ctx *c, int bjmax, double bjtol, double *stats)
     return osb_build(c, bjmax, bjtol, stats);
 }
 
+int scalit_build_times(scalit_ctx *c, double *seconds)
+{
+    CTX_CHECK(c);
+    if (!seconds) { set_error("null output"); return SCALIT_EINVAL; }
+    for (int l = 0; l < c->L.nlev; ++l) seconds[l] = c->build_s[l];
+    return 0;
+}
+
 int scalit_get_osb(scalit_ctx *c, double *VOSB, double *EIG0)
 {
     CTX_CHECK(c);
@@ -429,7 +443,8 @@ int scalit_set_osb(scalit_ctx *c, const double *VOSB, const double *EIG0)
     if (rc) return rc;
     SC_CUDA(cudaStreamSynchronize(c->stream));
     c->osb_built = true;
-    return 0;
+    c->gen++;
+    return tc_prepare_px(c);
 }
 
 // ------------------------------------------------------------------ QMR --
@@ -533,6 +548,21 @@ int scalit_pist_basis(scalit_ctx *c, const scalit_pist_params *p, const double *
     PistBasisOut b;
     b.cnt = cnt; b.ritz = ritz; b.hmat = hmat; b.vj = vj;
     int rc = pist_ctx(c, p, dx, eig, res, info, nullptr, &b);
+    cudaFreeAsync(dx, c->stream);
+    cudaStreamSynchronize(c->stream);
+    return rc;
+}
+
+int scalit_pist_residuals(scalit_ctx *c, const scalit_pist_params *p, const double *x0, double *eig, double *res,
+                          scalit_pist_info *info, double *resid)
+{
+    CTX_CHECK(c);
+    if (!p || !x0 || !eig || !res || !resid) { set_error("null argument"); return SCALIT_EINVAL; }
+    const i64 N = c->L.N;
+    double *dx = nullptr;
+    SC_CUDA(cudaMallocAsync(&dx, sizeof(double) * (size_t)N, c->stream));
+    SC_CUDA(cudaMemcpyAsync(dx, x0, sizeof(double) * N, cudaMemcpyHostToDevice, c->stream));
+    int rc = pist_ctx(c, p, dx, eig, res, info, nullptr, nullptr, resid);
     cudaFreeAsync(dx, c->stream);
     cudaStreamSynchronize(c->stream);
     return rc;

@@ -86,7 +86,16 @@ struct scalit_ctx {
     // FP64 H*X engine: SCALIT_FP64_DFMA (FP64 pipe) or SCALIT_FP64_TENSOR (digit-sliced tcgen05)
     int fp64_mode = SCALIT_FP64_TENSOR;
     TcLevelData tc[SCALIT_FMAX];
+    // digit planes of the preconditioner's rotations, levels >= 2: [level][VX, VTX]
+    TcLevelData pxtc[SCALIT_FMAX][2];
     int *tc_err = nullptr;
+    // Captured QMR iteration batches (one per precision); `gen` changes whenever
+    // anything baked into the captured launches changes (shift, preconditioner,
+    // engine, workspace), which invalidates them.
+    long long gen = 0;
+    // wall seconds per level of the last preconditioner build
+    double build_s[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+    struct QmrGraph { cudaGraphExec_t exec = nullptr; long long gen = -1; int ntype = 0; i64 n = 0; void *work = nullptr; } qg[2];
 };
 
 namespace sc {
@@ -153,6 +162,11 @@ int hf_gradients(scalit_ctx *c, int m, const double *psi, int np, const double *
 
 // ------------------------------------------------------- tensor-core FP64 --
 int tc_prepare(scalit_ctx *c);
+int tc_prepare_px(scalit_ctx *c);
+void tc_free_px(scalit_ctx *c);
+bool tc_px_usable(const scalit_ctx *c, int level);
+int tc_rot_apply(const scalit_ctx *c, int level, int transpose, const double *X, double *Y, const int *gate,
+                 cudaStream_t s);
 bool tc_usable(const scalit_ctx *c, int level);
 int tc_level_apply(const scalit_ctx *c, int level, const double *X, double *Y, int accumulate,
                    const double *diagV, double shift, double alpha, const int *gate, cudaStream_t s,
@@ -187,6 +201,7 @@ template <class T> struct QmrOps {
     virtual int hx(const T *in, T *out, const int *gate) = 0;
     virtual int px(const T *in, T *out, const int *gate) = 0;
     virtual bool host_side() const { return false; }
+    virtual void set_scratch(T *) {}   // an N-vector the preconditioner may use
 };
 template <class T>
 int qmr_core(scalit_ctx *c, i64 n, QmrOps<T> &ops, int ntype, int qmrmax, double qmrtol,
@@ -203,9 +218,9 @@ struct PistOps {
 struct PistBasisOut { int *cnt = nullptr; double *ritz = nullptr, *hmat = nullptr, *vj = nullptr; };
 int pist_core(scalit_ctx *c, i64 N, const scalit_pist_params *p, const double *dx0, PistOps &ops,
               double *eig, double *res, scalit_pist_info *info, double *vectors_host = nullptr,
-              const PistBasisOut *basis = nullptr);
+              const PistBasisOut *basis = nullptr, double *resid = nullptr);
 int pist_ctx(scalit_ctx *c, const scalit_pist_params *p, const double *dx0, double *eig,
              double *res, scalit_pist_info *info, double *vectors_host = nullptr,
-             const PistBasisOut *basis = nullptr);
+             const PistBasisOut *basis = nullptr, double *resid = nullptr);
 
 }  // namespace sc

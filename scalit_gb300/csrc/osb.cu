@@ -11,19 +11,27 @@
 // the rotated diagonal and the diagonal of HOSB is zeroed.
 //
 // The rotation order is the reference's, so V and EIG0 agree with it to
-// rounding.  Two device schedules:
-//  * many blocks (BLK >= 64): one CTA per block runs all its sweeps; the block
-//    is staged in shared memory when it fits (level 1: n x n matrices);
-//  * few blocks (the outermost levels, BLK = 1 for the angle): every rotation
-//    is spread over the whole GPU -- one launch computes the partial A,B,C
-//    sums, a second finishes the angle and rotates V, a third rotates HOSB.
+// rounding.  Within one offset i the rotations (j, j+i), (j+1, j+1+i), ...,
+// (j+m-1, j+m-1+i) with m <= i act on disjoint planes: none of them changes an
+// element another one reads for its angle, so their angles are the ones the
+// sequential order computes, and each element is touched by at most two of
+// them, applied here in the sequential order.  A sweep therefore runs as
+// about MAK ln MAK batches instead of MAK (MAK-1) / 2 single rotations.  Two
+// device schedules:
+//  * the block's stacked matrices fit in shared memory (level 1: one n x n
+//    matrix per block): one CTA per block runs all its sweeps in SMEM;
+//  * otherwise (the outer levels' stacks of NDK matrices): every batch is
+//    spread over the whole GPU and all blocks -- one launch forms the batch's
+//    angles and rotates V, a second rotates HOSB.
 // The angle is formed from A, B, C with square roots only (half-angle
 // identities for atan(B/(A-C))/4 and the +-pi/4 shifts), which equals the
 // reference's DATAN/DSIN/DCOS result to rounding.
 #include "internal.cuh"
 
 #include <algorithm>
+#include <chrono>
 #include <cmath>
+#include <type_traits>
 #include <vector>
 
 namespace sc {
@@ -91,63 +99,122 @@ __device__ void block_sum3(double &a, double &b, double &c, double *red)
     for (int w = 0; w < nw; ++w) { a += red[3 * w]; b += red[3 * w + 1]; c += red[3 * w + 2]; }
 }
 
-__device__ double block_offdiag(const double *H, int ndk, int mak, double *red)
+// Reductions over one block's stacked matrices; element (k, r, c) of the
+// stack sits at k + ndk (r + ldr c) (ldr = MAK, or MAK + 1 in shared memory
+// where the padding keeps row and column walks free of bank conflicts).
+__device__ double block_offdiag(const double *H, int ndk, int mak, int ldr, double *red)
 {
     double s = 0.0, z1 = 0.0, z2 = 0.0;
-    const i64 total = (i64)ndk * mak * mak;
-    for (i64 e = threadIdx.x; e < total; e += blockDim.x) {
-        const i64 rc = e / ndk;
-        const int r = (int)(rc % mak), col = (int)(rc / mak);
-        if (r < col) { const double h = H[e]; s = fma(h, h, s); }
+    const int per_col = ndk * mak;
+    for (int col = 1; col < mak; ++col) {
+        const int cnt = ndk * col;                 // rows 0..col-1 of every stacked matrix
+        const double *Hc = H + (i64)ndk * ldr * col;
+        for (int e = threadIdx.x; e < cnt; e += blockDim.x) { const double h = Hc[e]; s = fma(h, h, s); }
     }
+    (void)per_col;
     block_sum3(s, z1, z2, red);
     return 2.0 * s;
 }
 
-__device__ double block_sumdiag(const double *H, int ndk, int mak, double *red)
+__device__ double block_sumdiag(const double *H, int ndk, int mak, int ldr, double *red)
 {
     double s = 0.0, z1 = 0.0, z2 = 0.0;
-    const i64 total = (i64)ndk * mak;
-    for (i64 e = threadIdx.x; e < total; e += blockDim.x) {
-        const int k = (int)(e % ndk), i = (int)(e / ndk);
-        const double h = H[k + (i64)ndk * (i + (i64)mak * i)];
+    const int total = ndk * mak;
+    for (int e = threadIdx.x; e < total; e += blockDim.x) {
+        const int i = e / ndk, k = e - i * ndk;
+        const double h = H[k + (i64)ndk * (i + (i64)ldr * i)];
         s = fma(h, h, s);
     }
     block_sum3(s, z1, z2, red);
     return s;
 }
 
-// Rotate rows/columns p, q of every stacked matrix of one block (MJACOBI
-// update, jacobi.f90:62-80) for the (k, r) items [e0, e1) in steps of `step`.
-__device__ __forceinline__ void rotate_items(double *H, int ndk, int mak, int p, int q,
-                                             double cs, double sn, i64 e0, i64 e1, i64 step)
+// A batch: planes t = 0..m-1, (p_t, q_t) = (a + t, a + i + t), m <= i.
+// Its HOSB work items per stacked matrix: (MAK - 2m) * m pair updates of a row
+// outside the batch's planes, then an m x m grid of (t, t2) 2x2 blocks (t == t2:
+// the plane's own diagonal block; t < t2: the cross block, rotation t first).
+__host__ __device__ __forceinline__ int batch_items(int mak, int m)
 {
-    const double C2 = cs * cs, S2 = sn * sn, SC = sn * cs;
-    for (i64 e = e0; e < e1; e += step) {
-        const int k = (int)(e % ndk), r = (int)(e / ndk);
-        if (r == q) continue;
-        if (r == p) {
-            double *hpp = H + k + (i64)ndk * (p + (i64)mak * p);
-            double *hqq = H + k + (i64)ndk * (q + (i64)mak * q);
-            double *hpq = H + k + (i64)ndk * (p + (i64)mak * q);
-            double *hqp = H + k + (i64)ndk * (q + (i64)mak * p);
-            const double odg = *hpq;
-            const double ddg = 0.5 * *hpp - 0.5 * *hqq;
-            const double np_ = C2 * *hpp + S2 * *hqq - 2 * SC * odg;
-            const double nq_ = C2 * *hqq + S2 * *hpp + 2 * SC * odg;
-            const double nqp = (C2 - S2) * odg + 2 * SC * ddg;
-            *hpp = np_; *hqq = nq_; *hpq = nqp; *hqp = nqp;
-        } else {
-            double *hrp = H + k + (i64)ndk * (r + (i64)mak * p);
-            double *hrq = H + k + (i64)ndk * (r + (i64)mak * q);
-            double *hpr = H + k + (i64)ndk * (p + (i64)mak * r);
-            double *hqr = H + k + (i64)ndk * (q + (i64)mak * r);
-            const double a = *hrp, b = *hrq;
-            const double np_ = cs * a - sn * b;
-            const double nq_ = cs * b + sn * a;
-            *hrp = np_; *hpr = np_; *hrq = nq_; *hqr = nq_;
-        }
+    return (mak - 2 * m) * m + m * m;
+}
+
+__device__ __forceinline__ int free_row(int f, int a, int i, int m)
+{
+    if (f < a) return f;
+    f -= a;
+    if (f < i - m) return a + m + f;
+    return a + i + m + (f - (i - m));
+}
+
+// MJACOBI's update (jacobi.f90:62-80) of work item u of stacked matrix k.
+// ONE: a single matrix per block (ndk == 1) with 32-bit offsets.
+template <bool ONE>
+__device__ __forceinline__ void batch_item(double *H, int ndk_, int mak, int ldr, int a, int i, int m,
+                                           const double *__restrict__ cs, const double *__restrict__ sn,
+                                           int u, int k)
+{
+    using I = typename std::conditional<ONE, int, i64>::type;
+    const I ndk = ONE ? 1 : (I)ndk_;
+    const int nfree = (mak - 2 * m) * m;
+    const I ld = ndk * (I)ldr;
+    double *Hk = H + (ONE ? 0 : k);
+    if (u < nfree) {
+        const int f = u / m, t = u - f * m, r = free_row(f, a, i, m);
+        const int p = a + t, q = a + i + t;
+        double *hrp = Hk + ndk * r + ld * p, *hrq = Hk + ndk * r + ld * q;
+        double *hpr = Hk + ndk * p + ld * r, *hqr = Hk + ndk * q + ld * r;
+        const double c = cs[t], sv = sn[t];
+        const double x = *hrp, y = *hrq;
+        const double np_ = c * x - sv * y;
+        const double nq_ = c * y + sv * x;
+        *hrp = np_; *hpr = np_; *hrq = nq_; *hqr = nq_;
+        return;
     }
+    u -= nfree;
+    const int t = u / m, t2 = u - t * m;
+    if (t2 < t) return;
+    const int p = a + t, q = a + i + t;
+    const double c = cs[t], sv = sn[t];
+    if (t == t2) {
+        double *hpp = Hk + ndk * p + ld * p, *hqq = Hk + ndk * q + ld * q;
+        double *hpq = Hk + ndk * p + ld * q, *hqp = Hk + ndk * q + ld * p;
+        const double C2 = c * c, S2 = sv * sv, SC = sv * c;
+        const double odg = *hpq;
+        const double ddg = 0.5 * *hpp - 0.5 * *hqq;
+        const double np_ = C2 * *hpp + S2 * *hqq - 2 * SC * odg;
+        const double nq_ = C2 * *hqq + S2 * *hpp + 2 * SC * odg;
+        const double nqp = (C2 - S2) * odg + 2 * SC * ddg;
+        *hpp = np_; *hqq = nq_; *hpq = nqp; *hqp = nqp;
+        return;
+    }
+    const int p2 = a + t2, q2 = a + i + t2;
+    double *h00 = Hk + ndk * p + ld * p2, *h01 = Hk + ndk * p + ld * q2;
+    double *h10 = Hk + ndk * q + ld * p2, *h11 = Hk + ndk * q + ld * q2;
+    // rotation t acts on rows p2 and q2 as rows outside its plane ...
+    const double x00 = *h00, x01 = *h01, x10 = *h10, x11 = *h11;
+    const double a00 = c * x00 - sv * x10, a10 = c * x10 + sv * x00;
+    const double a01 = c * x01 - sv * x11, a11 = c * x11 + sv * x01;
+    // ... then rotation t2 on rows p and q
+    const double c2 = cs[t2], s2 = sn[t2];
+    const double b00 = c2 * a00 - s2 * a01, b01 = c2 * a01 + s2 * a00;
+    const double b10 = c2 * a10 - s2 * a11, b11 = c2 * a11 + s2 * a10;
+    *h00 = b00; *h01 = b01; *h10 = b10; *h11 = b11;
+    Hk[ndk * p2 + ld * p] = b00; Hk[ndk * q2 + ld * p] = b01;
+    Hk[ndk * p2 + ld * q] = b10; Hk[ndk * q2 + ld * q] = b11;
+}
+
+// VUPDATE (vupdate.f90:21-36) of item u = (t, row), rows fastest: columns
+// p_t, q_t of V.
+__device__ __forceinline__ void batch_vitem(double *V, int mak, int a, int i,
+                                            const double *__restrict__ cs, const double *__restrict__ sn,
+                                            int u)
+{
+    const int t = u / mak, row = u - t * mak;
+    double *vp = V + (i64)(a + t) * mak + row, *vq = V + (i64)(a + i + t) * mak + row;
+    const double c = cs[t], sv = sn[t];
+    const double x = *vp, y = *vq;
+    *vp = c * x - sv * y;
+    *vq = c * y + sv * x;
 }
 
 // ------------------------------------------------------------------ init --
@@ -170,78 +237,85 @@ __global__ void hosb_init_kernel(int blk, int mak, int ndk, const double *__rest
 }
 
 // ------------------------------------------------- schedule 1: CTA/block --
+static constexpr int kMaxBatch = 128;   // m <= MAK / 2
+
 __global__ void __launch_bounds__(kThreads)
-jacobi_block_kernel(int bjmax, double bjtol, int blk, int mak, int ndk, int stage,
+jacobi_block_kernel(int bjmax, double bjtol, int blk, int mak, int ndk,
                     double *__restrict__ HOSB, double *__restrict__ VOSB, double *__restrict__ EIG,
                     double *__restrict__ bstats)
 {
     extern __shared__ __align__(16) double smem[];
     double *red = smem;                 // 3 * 32
-    double *rot = smem + 96;            // cs, sn
-    double *Hs = smem + 128;            // staged block
-    const int tid = threadIdx.x, nt = blockDim.x;
-    const i64 bsz = (i64)ndk * mak * mak;
+    double *cs = smem + 96;             // kMaxBatch
+    double *sn = cs + kMaxBatch;        // kMaxBatch
+    double *H = sn + kMaxBatch;         // the block's stacked matrices, column stride ldr
+    const int tid = threadIdx.x, nt = blockDim.x, lane = tid & 31, warp = tid >> 5, nw = nt >> 5;
+    const int ldr = (ndk == 1) ? mak + 1 : mak;
+    const int col_g = ndk * mak, col_s = ndk * ldr;     // one column of the stack: global / shared
     for (int b = blockIdx.x; b < blk; b += gridDim.x) {
-        double *Hg = HOSB + (i64)b * bsz;
-        double *H = stage ? Hs : Hg;
+        double *Hg = HOSB + (i64)b * col_g * mak;
         double *V = VOSB + (i64)b * mak * mak;
         __syncthreads();
-        if (stage) for (i64 e = tid; e < bsz; e += nt) Hs[e] = Hg[e];
-        for (i64 e = tid; e < (i64)mak * mak; e += nt) V[e] = ((e % mak) == (e / mak)) ? 1.0 : 0.0;
+        for (int c = 0; c < mak; ++c)
+            for (int e = tid; e < col_g; e += nt) H[e + c * col_s] = Hg[e + (i64)c * col_g];
+        for (int e = tid; e < mak * mak; e += nt) { const int c = e / mak; V[e] = (e - c * mak == c) ? 1.0 : 0.0; }
         __syncthreads();
-        const double initye = block_offdiag(H, ndk, mak, red);
+        const double initye = block_offdiag(H, ndk, mak, ldr, red);
         double ye = initye, dye = initye;
         int k = 1;
         while (fabs(dye) > initye * bjtol && k <= bjmax) {
             for (int i = 1; i <= mak - 1; ++i) {
-                for (int j = 1; j <= mak - i; ++j) {
-                    const int p = j - 1, q = j + i - 1;
-                    double sA = 0.0, sB = 0.0, sC = 0.0;
-                    for (int kk = tid; kk < ndk; kk += nt) {
-                        const double o = H[kk + (i64)ndk * (p + (i64)mak * q)];
-                        const double d = 0.5 * H[kk + (i64)ndk * (p + (i64)mak * p)]
-                                       - 0.5 * H[kk + (i64)ndk * (q + (i64)mak * q)];
-                        sA = fma(o, o, sA); sB = fma(o, d, sB); sC = fma(d, d, sC);
-                    }
-                    if (ndk > 1) {
-                        block_sum3(sA, sB, sC, red);
-                    } else {
-                        __syncthreads();
-                        if (tid == 0) { red[0] = sA; red[1] = sB; red[2] = sC; }
-                        __syncthreads();
-                        sA = red[0]; sB = red[1]; sC = red[2];
-                    }
-                    if (tid == 0) {
-                        double cs, sn;
-                        jacobi_angle(sA, 2.0 * sB, sC, &cs, &sn);
-                        rot[0] = cs; rot[1] = sn;
+                for (int a = 0; a < mak - i; a += i) {
+                    const int m = min(i, mak - i - a);
+                    // angles of the batch: one warp per plane, lanes over the stack
+                    for (int t = warp; t < m; t += nw) {
+                        const int p = a + t, q = a + i + t;
+                        double sA = 0.0, sB = 0.0, sC = 0.0;
+                        for (int kk = lane; kk < ndk; kk += 32) {
+                            const double o = H[kk + ndk * (p + ldr * q)];
+                            const double d = 0.5 * H[kk + ndk * (p + ldr * p)]
+                                           - 0.5 * H[kk + ndk * (q + ldr * q)];
+                            sA = fma(o, o, sA); sB = fma(o, d, sB); sC = fma(d, d, sC);
+                        }
+                        if (ndk > 1) {
+                            #pragma unroll
+                            for (int o = 16; o > 0; o >>= 1) {
+                                sA += __shfl_xor_sync(0xffffffffu, sA, o);
+                                sB += __shfl_xor_sync(0xffffffffu, sB, o);
+                                sC += __shfl_xor_sync(0xffffffffu, sC, o);
+                            }
+                        }
+                        if (lane == 0) jacobi_angle(sA, 2.0 * sB, sC, cs + t, sn + t);
                     }
                     __syncthreads();
-                    const double cs = rot[0], sn = rot[1];
-                    rotate_items(H, ndk, mak, p, q, cs, sn, tid, (i64)ndk * mak, nt);
-                    for (int a = tid; a < mak; a += nt) {
-                        double *vp = V + (i64)p * mak, *vq = V + (i64)q * mak;
-                        const double t = cs * vp[a] - sn * vq[a];
-                        vq[a] = cs * vq[a] + sn * vp[a];
-                        vp[a] = t;
+                    const int nh = batch_items(mak, m);
+                    if (ndk == 1) {
+                        for (int u = tid; u < nh; u += nt) batch_item<true>(H, 1, mak, ldr, a, i, m, cs, sn, u, 0);
+                    } else {
+                        for (int e = tid; e < ndk * nh; e += nt) {
+                            const int u = e / ndk;
+                            batch_item<false>(H, ndk, mak, ldr, a, i, m, cs, sn, u, e - u * ndk);
+                        }
                     }
+                    for (int u = tid; u < mak * m; u += nt) batch_vitem(V, mak, a, i, cs, sn, u);
                     __syncthreads();
                 }
             }
-            dye = block_offdiag(H, ndk, mak, red) - ye;
+            dye = block_offdiag(H, ndk, mak, ldr, red) - ye;
             ye = ye + dye;
             k = k + 1;
         }
-        const double sd = block_sumdiag(H, ndk, mak, red);
+        const double sd = block_sumdiag(H, ndk, mak, ldr, red);
         __syncthreads();
-        for (i64 e = tid; e < (i64)ndk * mak; e += nt) {
-            const int kk = (int)(e % ndk), i = (int)(e / ndk);
-            const i64 di = kk + (i64)ndk * (i + (i64)mak * i);
+        for (int e = tid; e < ndk * mak; e += nt) {
+            const int i = e / ndk, kk = e - i * ndk;
+            const int di = kk + ndk * (i + ldr * i);
             EIG[kk + (i64)ndk * (i + (i64)mak * b)] = H[di];
             H[di] = 0.0;
         }
         __syncthreads();
-        if (stage) for (i64 e = tid; e < bsz; e += nt) Hg[e] = Hs[e];
+        for (int c = 0; c < mak; ++c)
+            for (int e = tid; e < col_g; e += nt) Hg[e + (i64)c * col_g] = H[e + c * col_s];
         if (tid == 0) {
             bstats[3 * (i64)b] = (double)k;
             bstats[3 * (i64)b + 1] = fabs(1.0 - ye / initye);
@@ -254,38 +328,25 @@ jacobi_block_kernel(int bjmax, double bjtol, int blk, int mak, int ndk, int stag
 // Per-block state of the sweep loop: [initye, ye, dye, k, done, sumdiag].
 struct SweepState { double initye, ye, dye; int k, done; double sumdiag; };
 
-static constexpr int kChunk = 8192;   // (k, r) items per CTA per rotation
-
 __global__ void __launch_bounds__(kThreads)
-gpu_partial_kernel(int mode, int mak, int ndk, int p, int q, const double *__restrict__ HOSB,
-                   double *__restrict__ partial, const SweepState *__restrict__ st)
+gpu_partial_kernel(int mode, int mak, int ndk, const double *__restrict__ HOSB, double *__restrict__ partial)
 {
-    // mode 0: A,B,C of plane (p,q); mode 1: sumOffDiag; mode 2: sumDiag.
+    // mode 1: sumOffDiag; mode 2: sumDiag.
     __shared__ double red[96];
     const int b = blockIdx.y;
-    if (mode == 0 && st[b].done) return;
     const double *H = HOSB + (i64)b * ndk * mak * mak;
     double sA = 0.0, sB = 0.0, sC = 0.0;
-    if (mode == 0) {
-        const i64 k0 = (i64)blockIdx.x * kChunk;
-        const i64 k1 = min((i64)ndk, k0 + kChunk);
-        for (i64 kk = k0 + threadIdx.x; kk < k1; kk += blockDim.x) {
-            const double o = H[kk + (i64)ndk * (p + (i64)mak * q)];
-            const double d = 0.5 * H[kk + (i64)ndk * (p + (i64)mak * p)]
-                           - 0.5 * H[kk + (i64)ndk * (q + (i64)mak * q)];
-            sA = fma(o, o, sA); sB = fma(o, d, sB); sC = fma(d, d, sC);
-        }
-    } else if (mode == 1) {
-        const i64 total = (i64)ndk * mak * mak;
-        for (i64 e = blockIdx.x * (i64)blockDim.x + threadIdx.x; e < total; e += (i64)gridDim.x * blockDim.x) {
-            const i64 rc = e / ndk;
-            const int r = (int)(rc % mak), col = (int)(rc / mak);
-            if (r < col) { const double h = H[e]; sA = fma(h, h, sA); }
+    if (mode == 1) {
+        // upper triangles: column col holds rows 0..col-1 contiguously (ndk * col numbers)
+        for (int col = 1 + blockIdx.x; col < mak; col += gridDim.x) {
+            const double *Hc = H + (i64)ndk * mak * col;
+            const int cnt = ndk * col;
+            for (int e = threadIdx.x; e < cnt; e += blockDim.x) { const double h = Hc[e]; sA = fma(h, h, sA); }
         }
     } else {
-        const i64 total = (i64)ndk * mak;
-        for (i64 e = blockIdx.x * (i64)blockDim.x + threadIdx.x; e < total; e += (i64)gridDim.x * blockDim.x) {
-            const int kk = (int)(e % ndk), i = (int)(e / ndk);
+        const int total = ndk * mak;
+        for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < total; e += gridDim.x * blockDim.x) {
+            const int i = e / ndk, kk = e - i * ndk;
             const double h = H[kk + (i64)ndk * (i + (i64)mak * i)];
             sA = fma(h, h, sA);
         }
@@ -297,47 +358,61 @@ gpu_partial_kernel(int mode, int mak, int ndk, int p, int q, const double *__res
     }
 }
 
-// One CTA per block: reduce the partials in order, form the angle, rotate V.
-__global__ void gpu_angle_kernel(int nchunk, int mak, int p, int q, const double *__restrict__ partial,
-                                 double *__restrict__ rot, double *__restrict__ VOSB,
-                                 const SweepState *__restrict__ st)
+// One CTA per (plane t of the batch, block b): A, B, C over the stack, the
+// angle, and V's columns p_t, q_t.
+__global__ void __launch_bounds__(kThreads)
+gpu_batch_angle_kernel(int mak, int ndk, int a, int i, int blk, int ms, const double *__restrict__ HOSB,
+                       double *__restrict__ rcs, double *__restrict__ rsn, double *__restrict__ VOSB,
+                       const SweepState *__restrict__ st)
 {
-    const int b = blockIdx.x;
-    if (st[b].done) return;
+    __shared__ double red[96];
     __shared__ double cssn[2];
-    if (threadIdx.x == 0) {
-        double A = 0.0, B = 0.0, C = 0.0;
-        for (int i = 0; i < nchunk; ++i) {
-            const double *pp = partial + 3 * ((i64)b * nchunk + i);
-            A += pp[0]; B += pp[1]; C += pp[2];
+    const int t = blockIdx.x, p = a + t, q = a + i + t;
+    for (int b = blockIdx.y; b < blk; b += gridDim.y) {
+        if (st[b].done) continue;
+        const double *H = HOSB + (i64)b * ndk * mak * mak;
+        double sA = 0.0, sB = 0.0, sC = 0.0;
+        for (int kk = threadIdx.x; kk < ndk; kk += blockDim.x) {
+            const double o = H[kk + (i64)ndk * (p + (i64)mak * q)];
+            const double d = 0.5 * H[kk + (i64)ndk * (p + (i64)mak * p)]
+                           - 0.5 * H[kk + (i64)ndk * (q + (i64)mak * q)];
+            sA = fma(o, o, sA); sB = fma(o, d, sB); sC = fma(d, d, sC);
         }
-        double cs, sn;
-        jacobi_angle(A, 2.0 * B, C, &cs, &sn);
-        cssn[0] = cs; cssn[1] = sn;
-        rot[2 * b] = cs; rot[2 * b + 1] = sn;
-    }
-    __syncthreads();
-    const double cs = cssn[0], sn = cssn[1];
-    double *V = VOSB + (i64)b * mak * mak;
-    for (int a = threadIdx.x; a < mak; a += blockDim.x) {
-        double *vp = V + (i64)p * mak, *vq = V + (i64)q * mak;
-        const double t = cs * vp[a] - sn * vq[a];
-        vq[a] = cs * vq[a] + sn * vp[a];
-        vp[a] = t;
+        block_sum3(sA, sB, sC, red);
+        if (threadIdx.x == 0) {
+            double c, sv;
+            jacobi_angle(sA, 2.0 * sB, sC, &c, &sv);
+            cssn[0] = c; cssn[1] = sv;
+            rcs[(i64)b * ms + t] = c;
+            rsn[(i64)b * ms + t] = sv;
+        }
+        __syncthreads();
+        const double c = cssn[0], sv = cssn[1];
+        double *V = VOSB + (i64)b * mak * mak;
+        for (int row = threadIdx.x; row < mak; row += blockDim.x) {
+            double *vp = V + (i64)p * mak + row, *vq = V + (i64)q * mak + row;
+            const double x = *vp, y = *vq;
+            *vp = c * x - sv * y;
+            *vq = c * y + sv * x;
+        }
     }
 }
 
 __global__ void __launch_bounds__(kThreads)
-gpu_rotate_kernel(int mak, int ndk, int p, int q, double *__restrict__ HOSB,
-                  const double *__restrict__ rot, const SweepState *__restrict__ st)
+gpu_batch_rotate_kernel(int mak, int ndk, int a, int i, int m, int blk, int ms, double *__restrict__ HOSB,
+                        const double *__restrict__ rcs, const double *__restrict__ rsn,
+                        const SweepState *__restrict__ st)
 {
-    const int b = blockIdx.y;
-    if (st[b].done) return;
-    double *H = HOSB + (i64)b * ndk * mak * mak;
-    const double cs = rot[2 * b], sn = rot[2 * b + 1];
-    const i64 total = (i64)ndk * mak;
-    rotate_items(H, ndk, mak, p, q, cs, sn, blockIdx.x * (i64)blockDim.x + threadIdx.x, total,
-                 (i64)gridDim.x * blockDim.x);
+    const int total = ndk * batch_items(mak, m);     // < 2^31 (checked on the host)
+    for (int b = blockIdx.y; b < blk; b += gridDim.y) {
+        if (st[b].done) continue;
+        double *H = HOSB + (i64)b * ndk * mak * mak;
+        const double *cs = rcs + (i64)b * ms, *sn = rsn + (i64)b * ms;
+        for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < total; e += gridDim.x * blockDim.x) {
+            const int u = e / ndk;
+            batch_item<false>(H, ndk, mak, mak, a, i, m, cs, sn, u, e - u * ndk);
+        }
+    }
 }
 
 // mode 0: initialise the sweep state from sumOffDiag; mode 1: end of a sweep.
@@ -406,66 +481,75 @@ int hosbdiag_device(scalit_ctx *c, int bjmax, double bjtol, int blk, int mak, in
                     double *HOSB, double *VOSB, double *EIG, double *stats5, cudaStream_t s)
 {
     if (blk <= 0 || mak <= 0 || ndk <= 0) { set_error("hosbdiag: bad sizes"); return SCALIT_EINVAL; }
-    if (blk > 65535 && blk < 64) { set_error("hosbdiag: bad block count"); return SCALIT_EINVAL; }
     std::vector<double> bstats(3 * (size_t)blk);
     double *d_bstats = nullptr;
     SC_CUDA(cudaMallocAsync(&d_bstats, sizeof(double) * 3 * (size_t)blk, s));
     int rc = 0;
-    const bool per_block = (blk >= 64) && ((i64)ndk * mak <= 262144);
+    const size_t fixed = (96 + 2 * kMaxBatch) * sizeof(double);
+    const size_t bytes = sizeof(double) * (size_t)ndk * mak * (ndk == 1 ? mak + 1 : mak);
+    const bool per_block = (bytes + fixed <= 225 * 1024) && mak / 2 <= kMaxBatch;
     if (per_block) {
-        const size_t bytes = sizeof(double) * (size_t)ndk * mak * mak;
-        const size_t fixed = 128 * sizeof(double);
-        const int stage = (bytes + fixed <= 225 * 1024) ? 1 : 0;
-        const size_t smem = fixed + (stage ? bytes : 0);
         SC_CUDA(cudaFuncSetAttribute(jacobi_block_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                      (int)(225 * 1024)));
         const int grid = blk < 152 * 8 ? blk : 152 * 8;
-        jacobi_block_kernel<<<grid, kThreads, smem, s>>>(bjmax, bjtol, blk, mak, ndk, stage, HOSB,
-                                                         VOSB, EIG, d_bstats);
+        jacobi_block_kernel<<<grid, kThreads, fixed + bytes, s>>>(bjmax, bjtol, blk, mak, ndk, HOSB, VOSB,
+                                                                  EIG, d_bstats);
         SC_CHECK_LAUNCH();
     } else {
-        if (blk > 65535) { set_error("hosbdiag: %d blocks too many for the spread schedule", blk); cudaFreeAsync(d_bstats, s); return SCALIT_EINVAL; }
-        const int nchunk = (int)((ndk + kChunk - 1) / kChunk);
+        const int gy = std::min(blk, 65535);
         const int npart_off = std::max(1, std::min(64, (int)(((i64)ndk * mak * mak + kThreads * 8 - 1) / (kThreads * 8))));
-        const int npart = std::max(nchunk, npart_off);
-        double *partial = nullptr, *rot = nullptr;
+        const int ms = std::max(1, mak / 2);
+        double *partial = nullptr, *rcs = nullptr;
         SweepState *st = nullptr;
-        SC_CUDA(cudaMallocAsync(&partial, sizeof(double) * 3 * (size_t)npart * blk, s));
-        SC_CUDA(cudaMallocAsync(&rot, sizeof(double) * 2 * (size_t)blk, s));
+        SC_CUDA(cudaMallocAsync(&partial, sizeof(double) * 3 * (size_t)npart_off * blk, s));
+        SC_CUDA(cudaMallocAsync(&rcs, sizeof(double) * 2 * (size_t)ms * blk, s));
         SC_CUDA(cudaMallocAsync(&st, sizeof(SweepState) * (size_t)blk, s));
+        double *rsn = rcs + (size_t)ms * blk;
         identity_kernel<<<gridsz((i64)mak * mak * blk), kThreads, 0, s>>>(mak, blk, VOSB);
+        if (blk > 65535) { set_error("hosbdiag: %d blocks too many for the spread schedule", blk); rc = SCALIT_EINVAL; }
+        if ((i64)ndk * mak * mak > 2147483647LL) { set_error("hosbdiag: a block of %d x %d x %d is too large", ndk, mak, mak); rc = SCALIT_EINVAL; }
         const dim3 goff(npart_off, blk);
-        gpu_partial_kernel<<<goff, kThreads, 0, s>>>(1, mak, ndk, 0, 0, HOSB, partial, st);
-        gpu_sweep_kernel<<<(blk + 127) / 128, 128, 0, s>>>(0, npart_off, bjmax, bjtol, partial, st, blk);
-        SC_CHECK_LAUNCH();
+        if (!rc) {
+            gpu_partial_kernel<<<goff, kThreads, 0, s>>>(1, mak, ndk, HOSB, partial);
+            gpu_sweep_kernel<<<(blk + 127) / 128, 128, 0, s>>>(0, npart_off, bjmax, bjtol, partial, st, blk);
+            SC_CHECK_LAUNCH();
+        }
         std::vector<SweepState> hst(blk);
-        const i64 items = (i64)ndk * mak;
-        const int grot = (int)std::min<i64>((items + kThreads - 1) / kThreads, 152 * 8);
-        for (int sweep = 0; sweep <= bjmax + 1; ++sweep) {
+        const int max_ctas = 152 * 16;
+        for (int sweep = 0; !rc && sweep <= bjmax + 1; ++sweep) {
             SC_CUDA(cudaMemcpyAsync(hst.data(), st, sizeof(SweepState) * blk, cudaMemcpyDeviceToHost, s));
             SC_CUDA(cudaStreamSynchronize(s));
             bool any = false;
             for (int b = 0; b < blk; ++b) any |= !hst[b].done;
             if (!any) break;
             for (int i = 1; i <= mak - 1; ++i) {
-                for (int j = 1; j <= mak - i; ++j) {
-                    const int p = j - 1, q = j + i - 1;
-                    gpu_partial_kernel<<<dim3(nchunk, blk), kThreads, 0, s>>>(0, mak, ndk, p, q, HOSB, partial, st);
-                    gpu_angle_kernel<<<blk, 128, 0, s>>>(nchunk, mak, p, q, partial, rot, VOSB, st);
-                    gpu_rotate_kernel<<<dim3(grot, blk), kThreads, 0, s>>>(mak, ndk, p, q, HOSB, rot, st);
+                for (int a = 0; a < mak - i; a += i) {
+                    const int m = std::min(i, mak - i - a);
+                    const i64 items = (i64)ndk * ((i64)(mak - 2 * m) * m + (i64)m * m);
+                    const int gx = (int)std::max<i64>(1, std::min<i64>((items + kThreads - 1) / kThreads,
+                                                                       std::max(1, max_ctas / gy)));
+                    gpu_batch_angle_kernel<<<dim3(m, gy), kThreads, 0, s>>>(mak, ndk, a, i, blk, ms, HOSB, rcs, rsn,
+                                                                            VOSB, st);
+                    gpu_batch_rotate_kernel<<<dim3(gx, gy), kThreads, 0, s>>>(mak, ndk, a, i, m, blk, ms, HOSB,
+                                                                              rcs, rsn, st);
                 }
             }
             SC_CHECK_LAUNCH();
-            gpu_partial_kernel<<<goff, kThreads, 0, s>>>(1, mak, ndk, 0, 0, HOSB, partial, st);
+            gpu_partial_kernel<<<goff, kThreads, 0, s>>>(1, mak, ndk, HOSB, partial);
             gpu_sweep_kernel<<<(blk + 127) / 128, 128, 0, s>>>(1, npart_off, bjmax, bjtol, partial, st, blk);
             SC_CHECK_LAUNCH();
         }
-        gpu_partial_kernel<<<goff, kThreads, 0, s>>>(2, mak, ndk, 0, 0, HOSB, partial, st);
-        gpu_finish_kernel<<<dim3(grot, blk), kThreads, 0, s>>>(npart_off, blk, mak, ndk, HOSB, EIG, partial, st, d_bstats);
-        SC_CHECK_LAUNCH();
+        if (!rc) {
+            const i64 items = (i64)ndk * mak;
+            const int grot = (int)std::min<i64>((items + kThreads - 1) / kThreads, 152 * 8);
+            gpu_partial_kernel<<<goff, kThreads, 0, s>>>(2, mak, ndk, HOSB, partial);
+            gpu_finish_kernel<<<dim3(grot, blk), kThreads, 0, s>>>(npart_off, blk, mak, ndk, HOSB, EIG, partial, st, d_bstats);
+            SC_CHECK_LAUNCH();
+        }
         cudaFreeAsync(partial, s);
-        cudaFreeAsync(rot, s);
+        cudaFreeAsync(rcs, s);
         cudaFreeAsync(st, s);
+        if (rc) { cudaFreeAsync(d_bstats, s); return rc; }
     }
     SC_CUDA(cudaMemcpyAsync(bstats.data(), d_bstats, sizeof(double) * 3 * (size_t)blk, cudaMemcpyDeviceToHost, s));
     SC_CUDA(cudaStreamSynchronize(s));
@@ -494,6 +578,7 @@ int osb_build(scalit_ctx *c, int bjmax, double bjtol, double *stats)
     SC_CUDA(cudaMemcpyAsync(c->EIG0, c->RES, sizeof(double) * (size_t)L.N, cudaMemcpyDeviceToDevice, s));
     int rc = 0;
     for (int l = L.nlev - 1; l >= 0 && rc == 0; --l) {
+        const auto t0 = std::chrono::steady_clock::now();
         const int mak = L.n[l];
         const i64 ndk = L.dim[l], blk = L.blk[l];
         if (ndk > 2147483647LL || blk > 2147483647LL) { set_error("level too large"); rc = SCALIT_EINVAL; break; }
@@ -507,13 +592,16 @@ int osb_build(scalit_ctx *c, int bjmax, double bjtol, double *stats)
         if (rc == 0)
             rc = hosbdiag_device(c, bjmax, bjtol, (int)blk, mak, (int)ndk, HOSB, c->VOSB + L.vs[l],
                                  c->EIG0, stats ? stats + 5 * l : nullptr, s);
+        if (rc == 0 && cudaStreamSynchronize(s) != cudaSuccess) { set_error("osb build level %d", l + 1); rc = SCALIT_ECUDA; }
+        c->build_s[l] = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
     }
     cudaFreeAsync(HOSB, s);
     if (rc) return rc;
     rc = to_f32(c->EIG0, c->EIG0f, L.N, s);
     if (!rc) rc = to_f32(c->VOSB, c->VOSBf, L.vlen, s);
-    if (!rc) c->osb_built = true;
+    if (!rc) { c->osb_built = true; c->gen++; }
     SC_CUDA(cudaStreamSynchronize(s));
+    if (!rc) rc = tc_prepare_px(c);
     return rc;
 }
 

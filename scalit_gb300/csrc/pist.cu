@@ -149,6 +149,58 @@ gemvt_partial_kernel(i64 n, int m, const double *VJ, const double *w, double *pa
     (void)m;
 }
 
+// FP32 first pass of the mixed classical Gram-Schmidt: partial[I][chunk] =
+// sum over the chunk of VJf(:, I) * wf in FP32 per thread, folded in FP64.
+__global__ void __launch_bounds__(kT)
+gemvt_partial_f32_kernel(i64 n, const float *VJf, const float *wf, double *partial, int nchunk)
+{
+    const int I = blockIdx.y;
+    const i64 k0 = (i64)blockIdx.x * kGemvChunk;
+    const i64 k1 = min(n, k0 + kGemvChunk);
+    const float *u = VJf + (i64)I * n;
+    float af = 0.0f;
+    for (i64 k = k0 + threadIdx.x; k < k1; k += blockDim.x) af = fmaf(u[k], wf[k], af);
+    double a = (double)af;
+    __shared__ double red[kT / 32];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    #pragma unroll
+    for (int o = 16; o > 0; o >>= 1) a += __shfl_xor_sync(0xffffffffu, a, o);
+    if (lane == 0) red[warp] = a;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double s = 0.0;
+        for (int w2 = 0; w2 < kT / 32; ++w2) s += red[w2];
+        partial[(i64)I * nchunk + blockIdx.x] = s;
+    }
+}
+
+// v -= VJf(:, 0:m) h with the products summed in FP32 (four interleaved
+// partial sums) and the update applied to the FP64 vector.
+__global__ void __launch_bounds__(kT)
+gemv_sub_f32_kernel(i64 n, int m, const float *VJf, const double *h, double *v)
+{
+    __shared__ float hs[2048];
+    for (int i0 = 0; i0 < m; i0 += 2048) {
+        const int cnt = min(2048, m - i0);
+        __syncthreads();
+        for (int i = threadIdx.x; i < cnt; i += blockDim.x) hs[i] = (float)h[i0 + i];
+        __syncthreads();
+        for (i64 k = blockIdx.x * (i64)blockDim.x + threadIdx.x; k < n; k += (i64)gridDim.x * blockDim.x) {
+            float a0 = 0.f, a1 = 0.f, a2 = 0.f, a3 = 0.f;
+            const float *col = VJf + (i64)i0 * n + k;
+            int i = 0;
+            for (; i + 3 < cnt; i += 4) {
+                a0 = fmaf(col[(i64)i * n], hs[i], a0);
+                a1 = fmaf(col[(i64)(i + 1) * n], hs[i + 1], a1);
+                a2 = fmaf(col[(i64)(i + 2) * n], hs[i + 2], a2);
+                a3 = fmaf(col[(i64)(i + 3) * n], hs[i + 3], a3);
+            }
+            for (; i < cnt; ++i) a0 = fmaf(col[(i64)i * n], hs[i], a0);
+            v[k] -= (double)((a0 + a1) + (a2 + a3));
+        }
+    }
+}
+
 __global__ void gemvt_final_kernel(int m, int nchunk, const double *partial, double *HMAT, int ld,
                                    int J)
 {
@@ -231,8 +283,36 @@ __global__ void select_columns_kernel(int num, int M, const double *Yall, const 
     }
 }
 
+// partial[j][chunk] = sum over the chunk of (HPsi(:, j) - theta_j Psi(:, j))^2
+__global__ void __launch_bounds__(kT)
+resid_partial_kernel(i64 n, const double *Psi, const double *HPsi, const double *theta, double *partial, int nchunk)
+{
+    const int j = blockIdx.y;
+    const i64 k0 = (i64)blockIdx.x * kGemvChunk;
+    const i64 k1 = min(n, k0 + kGemvChunk);
+    const double th = theta[j];
+    const double *u = Psi + (i64)j * n, *hu = HPsi + (i64)j * n;
+    double a = 0.0;
+    for (i64 k = k0 + threadIdx.x; k < k1; k += blockDim.x) { const double r = hu[k] - th * u[k]; a = fma(r, r, a); }
+    __shared__ double red[kT / 32];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    #pragma unroll
+    for (int o = 16; o > 0; o >>= 1) a += __shfl_xor_sync(0xffffffffu, a, o);
+    if (lane == 0) red[warp] = a;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double t = 0.0;
+        for (int w2 = 0; w2 < kT / 32; ++w2) t += red[w2];
+        partial[(i64)j * nchunk + blockIdx.x] = t;
+    }
+}
+
+// Ritz vectors of the window (ascending) into out_host (N x M, may be null),
+// and the FP64 residual norms |H psi - theta psi|_2 of the normalised Ritz
+// pairs into resid (M, may be null).
 static int ritz_vectors(scalit_ctx *c, i64 N, const double *VJ, const double *HMAT, int ld, int num, double e0,
-                        int M, double *A, double *EV, double *work, int lwork, int *devinfo, double *out_host)
+                        int M, double *A, double *EV, double *work, int lwork, int *devinfo, double *out_host,
+                        double *resid = nullptr)
 {
     cudaStream_t s = c->stream;
     cusolverDnHandle_t sol = (cusolverDnHandle_t)c->cusolver;
@@ -283,7 +363,32 @@ static int ritz_vectors(scalit_ctx *c, i64 N, const double *VJ, const double *HM
     g.C = Psi; g.c_sn = N;
     g.alpha = 1.0;
     int rc = launch_gemm<double>(g, s);
-    if (!rc) SC_CUDA(cudaMemcpyAsync(out_host, Psi, sizeof(double) * (size_t)N * Msel, cudaMemcpyDeviceToHost, s));
+    if (!rc && out_host)
+        SC_CUDA(cudaMemcpyAsync(out_host, Psi, sizeof(double) * (size_t)N * Msel, cudaMemcpyDeviceToHost, s));
+    if (!rc && resid) {
+        // H psi for all selected vectors in one batched FP64 application (HX0: no shift)
+        double *HPsi = nullptr, *theta = nullptr, *part = nullptr, *rn = nullptr;
+        const int nchunk = (int)((N + kGemvChunk - 1) / kGemvChunk);
+        SC_CUDA(cudaMallocAsync(&HPsi, sizeof(double) * (size_t)N * Msel, s));
+        SC_CUDA(cudaMallocAsync(&theta, sizeof(double) * Msel, s));
+        SC_CUDA(cudaMallocAsync(&part, sizeof(double) * (size_t)nchunk * Msel, s));
+        SC_CUDA(cudaMallocAsync(&rn, sizeof(double) * Msel, s));
+        std::vector<double> th(Msel);
+        for (int j = 0; j < Msel; ++j) th[j] = ev[idx[j]];
+        SC_CUDA(cudaMemcpyAsync(theta, th.data(), sizeof(double) * Msel, cudaMemcpyHostToDevice, s));
+        rc = hx_batch<double>(c, Psi, HPsi, Msel, 0.0, 1.0, nullptr, s);
+        if (!rc) {
+            resid_partial_kernel<<<dim3(nchunk, Msel), kT, 0, s>>>(N, Psi, HPsi, theta, part, nchunk);
+            gemvt_vec_kernel<<<(Msel + 127) / 128, 128, 0, s>>>(Msel, nchunk, part, rn);
+            SC_CHECK_LAUNCH();
+            std::vector<double> r2(Msel);
+            SC_CUDA(cudaMemcpyAsync(r2.data(), rn, sizeof(double) * Msel, cudaMemcpyDeviceToHost, s));
+            SC_CUDA(cudaStreamSynchronize(s));
+            for (int j = 0; j < Msel; ++j) resid[j] = std::sqrt(r2[j]);
+            for (int j = Msel; j < M; ++j) resid[j] = 0.0;
+        }
+        cudaFreeAsync(HPsi, s); cudaFreeAsync(theta, s); cudaFreeAsync(part, s); cudaFreeAsync(rn, s);
+    }
     SC_CUDA(cudaStreamSynchronize(s));
     cudaFreeAsync(didx, s); cudaFreeAsync(Ysel, s); cudaFreeAsync(Psi, s);
     if (own) cudaFreeAsync(own, s);
@@ -297,12 +402,13 @@ static double now()
 
 int pist_core(scalit_ctx *c, i64 N, const scalit_pist_params *p, const double *dx0, PistOps &ops,
               double *eig, double *res, scalit_pist_info *info, double *vectors_host,
-              const PistBasisOut *basis)
+              const PistBasisOut *basis, double *resid)
 {
     cudaStream_t s = c->stream;
     const int M = p->m, MM = p->m_max;
     scalit_pist_info inf{};
     *res = 0.0;
+    if (p->orth < 0 || p->orth > 2) { set_error("unknown orthogonalisation mode %d", p->orth); return SCALIT_EINVAL; }
     if (p->stepeig >= MM || p->startcnt > MM || M > MM || M < 1) {
         if (info) *info = inf;
         return 0;
@@ -317,6 +423,18 @@ int pist_core(scalit_ctx *c, i64 N, const scalit_pist_params *p, const double *d
         return SCALIT_ENOMEM;
     }
     SC_CUDA(cudaMallocAsync(&W, sizeof(double) * (size_t)N, s));
+    float *VJf = nullptr, *Wf = nullptr;   // FP32 copies for the mixed first pass (orth == 2)
+    if (p->orth == 2) {
+        if (cudaMallocAsync(&VJf, sizeof(float) * (size_t)N * MM, s) != cudaSuccess ||
+            cudaMallocAsync(&Wf, sizeof(float) * (size_t)N, s) != cudaSuccess) {
+            cudaGetLastError();
+            if (VJf) cudaFreeAsync(VJf, s);
+            cudaFreeAsync(VJ, s); cudaFreeAsync(W, s);
+            set_error("FP32 copy of the PIST basis (%d vectors x %lld points) does not fit", MM, N);
+            return SCALIT_ENOMEM;
+        }
+    }
+    auto vcolf = [&](int J1) { return VJf + (i64)(J1 - 1) * N; };
     SC_CUDA(cudaMallocAsync(&HMAT, sizeof(double) * (size_t)MM * MM, s));
     SC_CUDA(cudaMallocAsync(&A, sizeof(double) * (size_t)MM * MM, s));
     SC_CUDA(cudaMallocAsync(&EV, sizeof(double) * (size_t)MM, s));
@@ -347,7 +465,9 @@ int pist_core(scalit_ctx *c, i64 N, const scalit_pist_params *p, const double *d
 
     // MGS_ORTH: orthogonalise W against columns 1..J into column J+1.
     // orth == 0: modified Gram-Schmidt in the reference's order (one pass);
-    // orth == 1: classical Gram-Schmidt applied twice (GEMV-T then GEMV, x2).
+    // orth == 1: classical Gram-Schmidt applied twice (GEMV-T then GEMV, x2);
+    // orth == 2: the same with the first pass in FP32 against the basis' FP32
+    //            copy; the second pass (the re-orthogonalisation) in FP64.
     auto mgs = [&](int J, bool *ok) -> int {
         double *v = vcol(J + 1);
         SC_CUDA(cudaMemcpyAsync(v, W, sizeof(double) * (size_t)N, cudaMemcpyDeviceToDevice, s));
@@ -362,6 +482,14 @@ int pist_core(scalit_ctx *c, i64 N, const scalit_pist_params *p, const double *d
             mgs_kernel<<<gr, kT, 0, s>>>(N, v, vcol(J), D + (J - 1), nullptr, dnorm + 1, partial, counter);
         } else {
             for (int pass = 0; pass < 2; ++pass) {
+                if (pass == 0 && p->orth == 2) {
+                    int r2 = to_f32(v, Wf, N, s);
+                    if (r2) return r2;
+                    gemvt_partial_f32_kernel<<<dim3(nchunk, J), kT, 0, s>>>(N, VJf, Wf, partial, nchunk);
+                    gemvt_vec_kernel<<<(J + 127) / 128, 128, 0, s>>>(J, nchunk, partial, D);
+                    gemv_sub_f32_kernel<<<gr, kT, 0, s>>>(N, J, VJf, D, v);
+                    continue;
+                }
                 gemvt_partial_kernel<<<dim3(nchunk, J), kT, 0, s>>>(N, J, VJ, v, partial, nchunk);
                 gemvt_vec_kernel<<<(J + 127) / 128, 128, 0, s>>>(J, nchunk, partial, D);
                 gemv_sub_kernel<<<gr, kT, 0, s>>>(N, J, VJ, D, v);
@@ -376,6 +504,10 @@ int pist_core(scalit_ctx *c, i64 N, const scalit_pist_params *p, const double *d
         if (*ok) {
             scale_inv_sqrt_kernel<<<gr, kT, 0, s>>>(N, v, dnorm + 1);
             SC_CHECK_LAUNCH();
+            if (VJf) {
+                int r2 = to_f32(v, vcolf(J + 1), N, s);
+                if (r2) return r2;
+            }
         }
         return 0;
     };
@@ -395,6 +527,10 @@ int pist_core(scalit_ctx *c, i64 N, const scalit_pist_params *p, const double *d
             if (h == 0.0) return 0;
             copy_scaled_kernel<<<gr, kT, 0, s>>>(N, dx0, vcol(1), dnorm);
             SC_CHECK_LAUNCH();
+            if (VJf) {
+                int r2 = to_f32(vcol(1), vcolf(1), N, s);
+                if (r2) return r2;
+            }
         } else {
             m_start = m_low - 1;
         }
@@ -420,8 +556,9 @@ int pist_core(scalit_ctx *c, i64 N, const scalit_pist_params *p, const double *d
         for (int J = m_low; J <= m_high; ++J) {
             int r = ops.h0x(vcol(J), W);
             if (r) return r;
-            gemvt_partial_kernel<<<dim3(nchunk, m_high), kT, 0, s>>>(N, m_high, VJ, W, partial, nchunk);
-            gemvt_final_kernel<<<(m_high + 127) / 128, 128, 0, s>>>(m_high, nchunk, partial, HMAT, MM, J - 1);
+            // HMAT(1:J, J) and its mirror; the rows below J come from the later columns
+            gemvt_partial_kernel<<<dim3(nchunk, J), kT, 0, s>>>(N, J, VJ, W, partial, nchunk);
+            gemvt_final_kernel<<<(J + 127) / 128, 128, 0, s>>>(J, nchunk, partial, HMAT, MM, J - 1);
             SC_CHECK_LAUNCH();
         }
         SC_CUDA(cudaStreamSynchronize(s));
@@ -429,49 +566,85 @@ int pist_core(scalit_ctx *c, i64 N, const scalit_pist_params *p, const double *d
         return 0;
     };
 
-    std::vector<double> tmp(MM), old(M), cur(M);
-    auto ritz = [&](int num) -> int {
+    // Ritz checks.  The two DSYEV-equivalent solves of a check (leading
+    // cnt_high - stepeig and cnt_high blocks of HMAT) are queued on a second
+    // stream and their results read back into pinned memory; without verbose
+    // output the next batch of Krylov vectors is generated while they run, and
+    // the check is evaluated afterwards.  A converged check stops the solve at
+    // its own cnt_high, so the eigenvalues and basis are those of the
+    // sequential order; only the overlapped batch's work is spent in vain.
+    std::vector<double> tmp(MM), tmp1(MM), old(M), cur(M);
+    cudaStream_t s2 = c->s_out;
+    double *hbuf = nullptr;
+    SC_CUDA(cudaMallocHost(&hbuf, sizeof(double) * 2 * (size_t)MM + 64));
+    int *hinfo = reinterpret_cast<int *>(hbuf + 2 * (size_t)MM);
+    const bool overlap = !p->verbose;
+    int pend_high = 0;     // cnt_high of the check queued on s2 (0: none)
+
+    auto ritz_launch = [&](int high) -> int {
+        if (cusolverDnSetStream(sol, s2) != CUSOLVER_STATUS_SUCCESS) { set_error("cusolverDnSetStream failed"); return SCALIT_ECUDA; }
+        const int nums[2] = {high - p->stepeig, high};
+        for (int q = 0; q < 2; ++q) {
+            const int num = nums[q];
+            gather_upper_kernel<<<egrid((i64)num * num), kT, 0, s2>>>(num, HMAT, MM, A);
+            SC_CHECK_LAUNCH();
+            cusolverStatus_t cs = cusolverDnDsyevd(sol, CUSOLVER_EIG_MODE_NOVECTOR, CUBLAS_FILL_MODE_UPPER, num, A,
+                                                   num, EV, work, lwork, devinfo);
+            if (cs != CUSOLVER_STATUS_SUCCESS) { set_error("cusolverDnDsyevd failed (%d)", (int)cs); return SCALIT_ECUDA; }
+            SC_CUDA(cudaMemcpyAsync(hbuf + (size_t)q * MM, EV, sizeof(double) * num, cudaMemcpyDeviceToHost, s2));
+            SC_CUDA(cudaMemcpyAsync(hinfo + q, devinfo, sizeof(int), cudaMemcpyDeviceToHost, s2));
+        }
+        inf.checks += 2;
+        pend_high = high;
+        return 0;
+    };
+    // Evaluate the queued check (getWindow0 / getDiffMax / getSepMax on the host).
+    auto ritz_settle = [&](bool *stop) -> int {
         const double t0 = now();
-        gather_upper_kernel<<<egrid((i64)num * num), kT, 0, s>>>(num, HMAT, MM, A);
-        SC_CHECK_LAUNCH();
-        cusolverStatus_t cs = cusolverDnDsyevd(sol, CUSOLVER_EIG_MODE_NOVECTOR, CUBLAS_FILL_MODE_UPPER, num, A,
-                                               num, EV, work, lwork, devinfo);
-        if (cs != CUSOLVER_STATUS_SUCCESS) { set_error("cusolverDnDsyevd failed (%d)", (int)cs); return SCALIT_ECUDA; }
-        int hinfo = 0;
-        SC_CUDA(cudaMemcpyAsync(tmp.data(), EV, sizeof(double) * num, cudaMemcpyDeviceToHost, s));
-        SC_CUDA(cudaMemcpyAsync(&hinfo, devinfo, sizeof(int), cudaMemcpyDeviceToHost, s));
-        SC_CUDA(cudaStreamSynchronize(s));
+        SC_CUDA(cudaStreamSynchronize(s2));
         inf.t_ritz += now() - t0;
-        inf.checks += 1;
-        return hinfo == 0 ? 0 : 1;
+        const int high = pend_high, num1 = high - p->stepeig;
+        pend_high = 0;
+        *stop = false;
+        if (hinfo[0]) { status = -num1; *stop = true; return 0; }
+        std::copy(hbuf, hbuf + num1, tmp1.begin());
+        get_window(p->e0, tmp1, num1, M, old.data());
+        if (hinfo[1]) { status = -high; *stop = true; return 0; }
+        std::copy(hbuf + MM, hbuf + MM + high, tmp.begin());
+        get_window(p->e0, tmp, high, M, cur.data());
+        *res = (p->ntype <= 0) ? diff_max(cur.data(), old.data(), M) : sep_max(old.data(), M, tmp, high);
+        if (p->verbose) printf(" Cnt1= %d  Cnt2= %d  RES= %.15e\n", high, num1, *res);
+        inf.krylov = high;
+        if (*res <= p->etol) { status = high; *stop = true; return 0; }
+        status = -high;
+        return 0;
     };
 
     int cnt_low = 1, cnt_high = std::max(std::max(p->startcnt, M), p->stepeig + 1);
-    while (cnt_high <= MM) {
+    while (true) {
         int ret = 0;
+        bool stop = false;
         rc = pisth0(cnt_low, cnt_high, &ret);
         if (rc) break;
+        if (pend_high) {
+            rc = ritz_settle(&stop);
+            if (rc || stop) break;
+        }
         if (ret < 0) { status = -cnt_high; break; }
         if (ret == 0 && cnt_low == 1) { status = 0; set_error("PIST start vector is zero"); break; }
-        int num = cnt_high - p->stepeig;
-        int lap = ritz(num);
-        if (lap < 0) { rc = lap; break; }
-        if (lap) { status = -num; break; }
-        get_window(p->e0, tmp, num, M, old.data());
-        num = cnt_high;
-        lap = ritz(num);
-        if (lap < 0) { rc = lap; break; }
-        if (lap) { status = -num; break; }
-        get_window(p->e0, tmp, num, M, cur.data());
-        *res = (p->ntype <= 0) ? diff_max(cur.data(), old.data(), M) : sep_max(old.data(), M, tmp, cnt_high);
-        if (p->verbose) printf(" Cnt1= %d  Cnt2= %d  RES= %.15e\n", cnt_high, cnt_high - p->stepeig, *res);
-        inf.krylov = cnt_high;
-        if (*res <= p->etol) { status = cnt_high; break; }
-        status = -cnt_high;
+        rc = ritz_launch(cnt_high);
+        if (rc) break;
+        const bool last = cnt_high + 1 >= MM;
+        if (!overlap || last) {
+            rc = ritz_settle(&stop);
+            if (rc || stop) break;
+        }
         cnt_low = cnt_high + 1;
-        if (cnt_low >= MM) { status = -MM; break; }
+        if (last) { status = -MM; break; }
         cnt_high = std::min(cnt_high + p->stepcnt, MM);
     }
+    cudaStreamSynchronize(s2);
+    cusolverDnSetStream(sol, s);
     if (basis && rc == 0 && status > 0) {
         const int cnt = status;
         if (basis->cnt) *basis->cnt = cnt;
@@ -486,12 +659,18 @@ int pist_core(scalit_ctx *c, i64 N, const scalit_pist_params *p, const double *d
         cudaStreamSynchronize(s);
         if (rc) set_error("copying the PIST basis out failed");
     }
-    if (vectors_host && rc == 0 && status > 0) {
-        int r2 = ritz_vectors(c, N, VJ, HMAT, MM, status, p->e0, M, A, EV, work, lwork, devinfo, vectors_host);
+    if ((vectors_host || resid) && rc == 0 && status > 0) {
+        const double t0 = now();
+        cusolverDnSetStream(sol, s);
+        int r2 = ritz_vectors(c, N, VJ, HMAT, MM, status, p->e0, M, A, EV, work, lwork, devinfo, vectors_host,
+                              resid);
         if (r2) rc = r2;
+        inf.t_resid += now() - t0;
     }
     std::sort(cur.begin(), cur.end());
     for (int i = 0; i < M; ++i) eig[i] = cur[i];
+    cudaFreeHost(hbuf);
+    if (VJf) { cudaFreeAsync(VJf, s); cudaFreeAsync(Wf, s); }
     cudaFreeAsync(VJ, s); cudaFreeAsync(W, s); cudaFreeAsync(HMAT, s); cudaFreeAsync(A, s);
     cudaFreeAsync(EV, s); cudaFreeAsync(D, s); cudaFreeAsync(partial, s); cudaFreeAsync(counter, s);
     cudaFreeAsync(work, s); cudaFreeAsync(devinfo, s);
@@ -519,13 +698,13 @@ struct CtxOps : PistOps {
 };
 
 int pist_ctx(scalit_ctx *c, const scalit_pist_params *p, const double *dx0, double *eig, double *res,
-             scalit_pist_info *info, double *vectors_host, const PistBasisOut *basis)
+             scalit_pist_info *info, double *vectors_host, const PistBasisOut *basis, double *resid)
 {
     if (!c->osb_built) { set_error("PIST needs the preconditioner: build or load it first"); return SCALIT_ESTATE; }
     CtxOps ops;
     ops.c = c;
     ops.p = p;
-    return pist_core(c, c->L.N, p, dx0, ops, eig, res, info, vectors_host, basis);
+    return pist_core(c, c->L.N, p, dx0, ops, eig, res, info, vectors_host, basis, resid);
 }
 
 }  // namespace sc

@@ -9,6 +9,10 @@
 // level 1 is read from HBM exactly once per application.  The outer levels
 // are strided GEMMs (contract.cu).
 #include "internal.cuh"
+#include "ptx.cuh"
+
+#include <algorithm>
+#include <type_traits>
 
 namespace sc {
 
@@ -85,6 +89,143 @@ px_level1_fused(int n, i64 nblk, const T *__restrict__ V, const T *__restrict__ 
     }
 }
 
+// Streaming variant of the fused level-1 pass: a persistent CTA walks its
+// blocks while the blocks' matrices arrive as column chunks (kChunkCols
+// columns = kChunkCols * n contiguous numbers) through a ring of shared-memory
+// slots, each filled by one bulk copy that completes on the slot's mbarrier.
+// Phase 1 (t = V^T x, then K^-1) takes a chunk as soon as it lands; phase 2
+// (y = V t, one warp per column, every lane accumulating its own rows) frees
+// each slot once all warps are past it, and the slot is refilled right away
+// with the chunk `ring` positions ahead -- the next block's columns stream in
+// while this block finishes, so HBM sees one continuous read of VOSB level 1.
+static constexpr int kChunkCols = 16;
+static constexpr int kStreamThreads = 256;
+
+template <class T, int RPL>
+__global__ void __launch_bounds__(kStreamThreads)
+px_level1_stream(int n, i64 nblk, const T *__restrict__ V, const T *__restrict__ EIG,
+                 const T *__restrict__ X, T *__restrict__ Y, KernelParams kp, T alpha, int nc, int ring,
+                 const int *gate, int *err)
+{
+    if (gate && *gate) return;
+    extern __shared__ __align__(16) unsigned char smem_stream[];
+    __shared__ int abort_flag;
+    constexpr int NW = kStreamThreads / 32;
+    uint64_t *mbar = reinterpret_cast<uint64_t *>(smem_stream);
+    const size_t slot_elems = (size_t)kChunkCols * n;
+    T *slots = reinterpret_cast<T *>(smem_stream + (((size_t)ring * 8 + 127) & ~(size_t)127));
+    T *xs = slots + (size_t)ring * slot_elems;
+    T *ts = xs + n;
+    T *es = ts + n;                                     // the block's EIG0
+    T *part = es + n;                                   // NW x n
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const T e0 = T(kp.e0), de = T(fabs(kp.de)), rde = T(1.0 / fabs(kp.de));
+    const T beta_d = T(1.0 + kp.beta), alpha_d = T(-kp.beta * fabs(kp.de));
+
+    const i64 kblocks = (nblk - blockIdx.x + gridDim.x - 1) / gridDim.x;   // blocks of this CTA
+    const i64 G = kblocks * nc;                                            // its chunks
+    auto issue = [&](i64 g) {
+        const i64 b = blockIdx.x + (g / nc) * (i64)gridDim.x;
+        const int c0 = (int)(g % nc) * kChunkCols;
+        const int cols = min(kChunkCols, n - c0);
+        const uint32_t bytes = (uint32_t)(sizeof(T) * (size_t)cols * n);
+        const int slot = (int)(g % ring);
+        mbar_arrive_expect_tx(&mbar[slot], bytes);
+        bulk_g2s(slots + (size_t)slot * slot_elems, V + b * (i64)n * n + (i64)c0 * n, bytes, &mbar[slot]);
+    };
+    if (tid == 0) {
+        abort_flag = 0;
+        for (int i = 0; i < ring; ++i) mbar_init(&mbar[i], 1);
+        mbar_init_fence();
+        for (i64 g = 0; g < G && g < ring; ++g) issue(g);
+    }
+    // X and EIG0 of the first block; later blocks' are fetched during the
+    // previous block's phase 2 (one value per thread, n <= 256)
+    if (kblocks > 0 && tid < n) {
+        xs[tid] = X[(i64)blockIdx.x * n + tid];
+        es[tid] = EIG[(i64)blockIdx.x * n + tid];
+    }
+    __syncthreads();
+    i64 issued = G < ring ? G : ring;    // meaningful in thread 0
+    i64 k = 0;
+    for (; k < kblocks; ++k) {
+        const i64 b = blockIdx.x + k * (i64)gridDim.x;
+        // phase 1: t = K^-1 V^T x
+        for (int c = 0; c < nc; ++c) {
+            const i64 g = k * nc + c;
+            if (!mbar_wait(&mbar[g % ring], (uint32_t)((g / ring) & 1))) { abort_flag = 1; break; }
+            const T *chunk = slots + (size_t)(g % ring) * slot_elems;
+            const int c0 = c * kChunkCols, cols = min(kChunkCols, n - c0);
+            for (int j = warp; j < cols; j += NW) {
+                const T *col = chunk + (size_t)j * n;
+                T acc = T(0);
+                #pragma unroll
+                for (int r = 0; r < RPL; ++r) {
+                    const int row = lane + 32 * r;
+                    if (row < n) acc = fma(col[row], xs[row], acc);
+                }
+                #pragma unroll
+                for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+                if (lane == 0)
+                    ts[c0 + j] = kernel_div<T>(acc, es[c0 + j], e0, kp.kind, de, rde, alpha_d, beta_d);
+            }
+        }
+        __syncthreads();
+        if (abort_flag) break;
+        // phase 2: y = V t, releasing the slots in order; meanwhile the next
+        // block's X and EIG0 are on their way into registers
+        const bool more = k + 1 < kblocks && tid < n;
+        T xn = T(0), en = T(0);
+        if (more) {
+            const i64 bn = b + gridDim.x;
+            xn = X[bn * n + tid];
+            en = EIG[bn * n + tid];
+        }
+        T acc[RPL];
+        #pragma unroll
+        for (int r = 0; r < RPL; ++r) acc[r] = T(0);
+        for (int c = 0; c < nc; ++c) {
+            const i64 g = k * nc + c;
+            const T *chunk = slots + (size_t)(g % ring) * slot_elems;
+            const int c0 = c * kChunkCols, cols = min(kChunkCols, n - c0);
+            for (int j = warp; j < cols; j += NW) {
+                const T *col = chunk + (size_t)j * n;
+                const T tj = ts[c0 + j];
+                #pragma unroll
+                for (int r = 0; r < RPL; ++r) {
+                    const int row = lane + 32 * r;
+                    if (row < n) acc[r] = fma(col[row], tj, acc[r]);
+                }
+            }
+            __syncthreads();
+            if (tid == 0 && g + ring < G) {
+                fence_proxy_async_smem();
+                issue(g + ring);
+                issued = g + ring + 1;
+            }
+        }
+        #pragma unroll
+        for (int r = 0; r < RPL; ++r) {
+            const int row = lane + 32 * r;
+            if (row < n) part[warp * n + row] = acc[r];
+        }
+        __syncthreads();
+        for (int i = tid; i < n; i += kStreamThreads) {
+            T y = T(0);
+            #pragma unroll
+            for (int w = 0; w < NW; ++w) y += part[w * n + i];
+            Y[b * (i64)n + i] = alpha * y;
+        }
+        if (more) { xs[tid] = xn; es[tid] = en; }
+        __syncthreads();
+    }
+    if (abort_flag && tid == 0) {
+        if (err) atomicExch(err, 2);
+        // let every copy this CTA issued land before the CTA's shared memory is released
+        for (i64 g = k * nc; g < issued; ++g) mbar_wait(&mbar[g % ring], (uint32_t)((g / ring) & 1));
+    }
+}
+
 // Batched y_b = V_b x_b (transpose = 0) or V_b^T x_b (transpose = 1), one CTA per block.
 template <class T>
 __global__ void __launch_bounds__(256)
@@ -142,20 +283,60 @@ template int bgemv<float>(int, int, const float *, const float *, float *, int, 
 
 static constexpr size_t kMaxDynSmem = 220 * 1024;
 
+template <class T, int RPL>
+static int launch_px1_stream(int n, i64 nblk, const T *V, const T *EIG, const T *X, T *Y, KernelParams kp,
+                             T alpha, int nc, int ring, size_t smem, const int *gate, int *err, cudaStream_t s)
+{
+    static int configured = -1;
+    int dev = 0;
+    cudaGetDevice(&dev);
+    if (configured != dev) {
+        SC_CUDA(cudaFuncSetAttribute(px_level1_stream<T, RPL>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)kMaxDynSmem));
+        configured = dev;
+    }
+    const int grid = (int)std::min<i64>(nblk, 152);
+    px_level1_stream<T, RPL><<<grid, kStreamThreads, smem, s>>>(n, nblk, V, EIG, X, Y, kp, alpha, nc, ring,
+                                                                gate, err);
+    SC_CHECK_LAUNCH();
+    return 0;
+}
+
 template <class T>
 static int launch_px1(int n, i64 nblk, const T *V, const T *EIG, const T *X, T *Y,
-                      KernelParams kp, T alpha, const int *gate, cudaStream_t s)
+                      KernelParams kp, T alpha, const int *gate, int *err, cudaStream_t s)
 {
+    // the streaming kernel: whole blocks fit the ring, chunks and bases 16-byte aligned
+    const size_t chunk = sizeof(T) * (size_t)kChunkCols * n;
+    const int nc = (n + kChunkCols - 1) / kChunkCols;
+    const size_t fixed = sizeof(T) * (size_t)n * (3 + kStreamThreads / 32) + 256 + 64 * 8;
+    const int ring = (int)std::min<size_t>((kMaxDynSmem - fixed) / chunk, (size_t)3 * nc);
+    const bool aligned = ((reinterpret_cast<uintptr_t>(V) & 15) == 0) && ((sizeof(T) * (size_t)n * n) % 16 == 0);
+    if (n <= 256 && ring >= nc && nblk >= 1 && aligned) {
+        const size_t smem = (((size_t)ring * 8 + 127) & ~(size_t)127) + (size_t)ring * chunk +
+                            sizeof(T) * (size_t)n * (3 + kStreamThreads / 32);
+        switch ((n + 31) / 32) {
+        case 1: return launch_px1_stream<T, 1>(n, nblk, V, EIG, X, Y, kp, alpha, nc, ring, smem, gate, err, s);
+        case 2: return launch_px1_stream<T, 2>(n, nblk, V, EIG, X, Y, kp, alpha, nc, ring, smem, gate, err, s);
+        case 3: return launch_px1_stream<T, 3>(n, nblk, V, EIG, X, Y, kp, alpha, nc, ring, smem, gate, err, s);
+        case 4: return launch_px1_stream<T, 4>(n, nblk, V, EIG, X, Y, kp, alpha, nc, ring, smem, gate, err, s);
+        case 5: return launch_px1_stream<T, 5>(n, nblk, V, EIG, X, Y, kp, alpha, nc, ring, smem, gate, err, s);
+        case 6: return launch_px1_stream<T, 6>(n, nblk, V, EIG, X, Y, kp, alpha, nc, ring, smem, gate, err, s);
+        case 7: return launch_px1_stream<T, 7>(n, nblk, V, EIG, X, Y, kp, alpha, nc, ring, smem, gate, err, s);
+        default: return launch_px1_stream<T, 8>(n, nblk, V, EIG, X, Y, kp, alpha, nc, ring, smem, gate, err, s);
+        }
+    }
     const size_t vec = sizeof(T) * 2 * (size_t)n;
     const size_t mat = sizeof(T) * (size_t)n * n;
     const int v_in_smem = (vec + mat <= kMaxDynSmem) ? 1 : 0;
     const size_t sm = vec + (v_in_smem ? mat : 0);
-    static bool configured[2] = {false, false};
-    const int which = sizeof(T) == 8 ? 0 : 1;
-    if (!configured[which]) {
+    static int configured = -1;
+    int dev = 0;
+    cudaGetDevice(&dev);
+    if (configured != dev) {
         SC_CUDA(cudaFuncSetAttribute(px_level1_fused<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                      (int)kMaxDynSmem));
-        configured[which] = true;
+        configured = dev;
     }
     px_level1_fused<T><<<grid_for(nblk), 256, sm, s>>>(n, nblk, V, EIG, X, Y, kp, alpha, v_in_smem, gate);
     SC_CHECK_LAUNCH();
@@ -165,6 +346,19 @@ static int launch_px1(int n, i64 nblk, const T *V, const T *EIG, const T *X, T *
 template <class T> static const T *pickp(const double *d, const float *f);
 template <> const double *pickp<double>(const double *d, const float *) { return d; }
 template <> const float *pickp<float>(const double *, const float *f) { return f; }
+
+// VX / VTX of level l >= 2: FP64 on the tensor-core digit engine when it is
+// the context's FP64 engine, otherwise the strided GEMM.
+template <class T>
+static int rotate(const scalit_ctx *c, int l, int transpose, const T *V, const T *in, T *out, const int *gate,
+                  cudaStream_t s)
+{
+    const Layout &L = c->L;
+    if constexpr (std::is_same<T, double>::value) {
+        if (tc_px_usable(c, l)) return tc_rot_apply(c, l, transpose, in, out, gate, s);
+    }
+    return level_rotate<T>((int)L.dim[l], L.n[l], (int)L.blk[l], V + L.vs[l], in, out, transpose, gate, s);
+}
 
 template <class T>
 int px_vec(const scalit_ctx *c, int npc, const T *X, T *Y, T *tmp, T alpha, const int *gate,
@@ -183,21 +377,21 @@ int px_vec(const scalit_ctx *c, int npc, const T *X, T *Y, T *tmp, T alpha, cons
     for (int l = L.nlev - 1; l >= 1; --l) {
         ++stage;
         T *out = buf[(S - stage) % 2];
-        rc = level_rotate<T>((int)L.dim[l], L.n[l], (int)L.blk[l], V + L.vs[l], in, out, 1, gate, s);
+        rc = rotate<T>(c, l, 1, V, in, out, gate, s);
         if (rc) return rc;
         in = out;
     }
     ++stage;
     {
         T *out = buf[(S - stage) % 2];
-        rc = launch_px1<T>(L.n[0], L.blk[0], V + L.vs[0], EIG, in, out, kp, alpha, gate, s);
+        rc = launch_px1<T>(L.n[0], L.blk[0], V + L.vs[0], EIG, in, out, kp, alpha, gate, c->tc_err, s);
         if (rc) return rc;
         in = out;
     }
     for (int l = 1; l < L.nlev; ++l) {
         ++stage;
         T *out = buf[(S - stage) % 2];
-        rc = level_rotate<T>((int)L.dim[l], L.n[l], (int)L.blk[l], V + L.vs[l], in, out, 0, gate, s);
+        rc = rotate<T>(c, l, 0, V, in, out, gate, s);
         if (rc) return rc;
         in = out;
     }

@@ -425,14 +425,16 @@ int qmr_core(scalit_ctx *c, i64 n, QmrOps<T> &ops, int ntype, int qmrmax, double
              const T *B, T *X, QmrResult *out)
 {
     cudaStream_t s = c->stream;
-    // vectors: R UX UR Q S V Z HX0, then the scalar state
+    // vectors: R UX UR Q S V Z HX0, the right-hand side and solution copies,
+    // the preconditioner's scratch, then the scalar state
     T *w = nullptr;
-    const size_t need = sizeof(T) * (size_t)n * 8 + sizeof(QmrState) + 64;
+    const size_t need = sizeof(T) * (size_t)n * 11 + sizeof(QmrState) + 64;
     int rc = work_get(c, need, (void **)&w);
     if (rc) return rc;
     T *R = w, *UX = w + n, *UR = w + 2 * n, *Q = w + 3 * n, *S = w + 4 * n, *V = w + 5 * n;
-    T *Z = w + 6 * n, *HX0 = w + 7 * n;
-    QmrState *st = reinterpret_cast<QmrState *>(((uintptr_t)(w + 8 * n) + 63) & ~(uintptr_t)63);
+    T *Z = w + 6 * n, *HX0 = w + 7 * n, *Bw = w + 8 * n, *Xw = w + 9 * n, *Pt = w + 10 * n;
+    QmrState *st = reinterpret_cast<QmrState *>(((uintptr_t)(w + 11 * n) + 63) & ~(uintptr_t)63);
+    ops.set_scratch(Pt);
     QmrState h{};
     h.ZVRAT = 1.0;
     h.GAMAMO = 1.0;
@@ -446,47 +448,90 @@ int qmr_core(scalit_ctx *c, i64 n, QmrOps<T> &ops, int ntype, int qmrmax, double
     double *partial = c->red_partial;
     const int gr = red_grid(n), ge = ew_grid(n);
 
-    if (ntype <= 0) SC_CUDA(cudaMemsetAsync(X, 0, sizeof(T) * (size_t)n, s));
-    copy_kernel<T><<<ge, 256, 0, s>>>(n, B, R, V);
+    SC_CUDA(cudaMemcpyAsync(Bw, B, sizeof(T) * (size_t)n, cudaMemcpyDeviceToDevice, s));
+    if (ntype <= 0) SC_CUDA(cudaMemsetAsync(Xw, 0, sizeof(T) * (size_t)n, s));
+    else SC_CUDA(cudaMemcpyAsync(Xw, X, sizeof(T) * (size_t)n, cudaMemcpyDeviceToDevice, s));
+    copy_kernel<T><<<ge, 256, 0, s>>>(n, Bw, R, V);
     SC_CHECK_LAUNCH();
-    rc = ops.px(B, Z, nullptr);
+    rc = ops.px(Bw, Z, nullptr);
     if (rc) return rc;
-    qmr_init_norms<T><<<gr, kRedThreads, 0, s>>>(n, B, Z, st, partial);
+    qmr_init_norms<T><<<gr, kRedThreads, 0, s>>>(n, Bw, Z, st, partial);
     SC_CHECK_LAUNCH();
 
+    // one iteration; every launch is gated by st->done
+    auto iteration = [&]() -> int {
+        qmr_step_a<T><<<gr, kRedThreads, 0, s>>>(n, V, Z, st, partial);
+        qmr_step_b<T><<<ge, 256, 0, s>>>(n, Z, Q, st);
+        SC_CHECK_LAUNCH();
+        // S = (H - E0) Q; step C scales it by ZVRAT as the reference does
+        int r = ops.hx(Q, S, gate);
+        if (r) return r;
+        qmr_step_c<T><<<gr, kRedThreads, 0, s>>>(n, Q, S, st, partial);
+        qmr_step_d<T><<<gr, kRedThreads, 0, s>>>(n, S, V, st, partial);
+        SC_CHECK_LAUNCH();
+        r = ops.px(V, Z, gate);
+        if (r) return r;
+        qmr_step_e<T><<<gr, kRedThreads, 0, s>>>(n, Z, st, partial);
+        qmr_step_f<T><<<gr, kRedThreads, 0, s>>>(n, Q, S, UX, UR, Xw, R, st, partial);
+        SC_CHECK_LAUNCH();
+        if (abs(ntype) == 1) {
+            r = ops.hx(Xw, HX0, gate);
+            if (r) return r;
+            qmr_step_g<T><<<gr, kRedThreads, 0, s>>>(n, HX0, Bw, st, partial);
+            SC_CHECK_LAUNCH();
+        }
+        return 0;
+    };
+
     const int batch = ops.host_side() ? 1 : 4;
+    // Device-side operators: the batch of iterations is captured once as a CUDA
+    // graph per context and precision and replayed (all pointers live in the
+    // workspace; the launches read their scalars from the device state).
+    cudaGraphExec_t exec = nullptr;
+    if (!ops.host_side()) {
+        scalit_ctx::QmrGraph &qg = c->qg[sizeof(T) == 8 ? 0 : 1];
+        if (qg.exec && (qg.gen != c->gen || qg.ntype != ntype || qg.n != n || qg.work != c->work)) {
+            cudaGraphExecDestroy(qg.exec);
+            qg.exec = nullptr;
+        }
+        if (!qg.exec) {
+            cudaGraph_t graph = nullptr;
+            SC_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+            int r = 0;
+            for (int b = 0; b < batch && !r; ++b) r = iteration();
+            const cudaError_t ce = cudaStreamEndCapture(s, &graph);
+            if (r) { if (graph) cudaGraphDestroy(graph); return r; }
+            if (ce != cudaSuccess) return cuda_fail(ce, "cudaStreamEndCapture", __FILE__, __LINE__);
+            const cudaError_t ie = cudaGraphInstantiate(&qg.exec, graph, 0);
+            cudaGraphDestroy(graph);
+            if (ie != cudaSuccess) { qg.exec = nullptr; return cuda_fail(ie, "cudaGraphInstantiate", __FILE__, __LINE__); }
+            qg.gen = c->gen;
+            qg.ntype = ntype;
+            qg.n = n;
+            qg.work = c->work;
+        }
+        exec = qg.exec;
+    }
+
     int it = 0;
     int *h_flag = reinterpret_cast<int *>(c->h_pinned);
     while (true) {
-        for (int b = 0; b < batch; ++b) {
-            qmr_step_a<T><<<gr, kRedThreads, 0, s>>>(n, V, Z, st, partial);
-            qmr_step_b<T><<<ge, 256, 0, s>>>(n, Z, Q, st);
-            SC_CHECK_LAUNCH();
-            // S = (H - E0) Q; step C scales it by ZVRAT as the reference does
-            rc = ops.hx(Q, S, gate);
-            if (rc) return rc;
-            qmr_step_c<T><<<gr, kRedThreads, 0, s>>>(n, Q, S, st, partial);
-            qmr_step_d<T><<<gr, kRedThreads, 0, s>>>(n, S, V, st, partial);
-            SC_CHECK_LAUNCH();
-            rc = ops.px(V, Z, gate);
-            if (rc) return rc;
-            qmr_step_e<T><<<gr, kRedThreads, 0, s>>>(n, Z, st, partial);
-            qmr_step_f<T><<<gr, kRedThreads, 0, s>>>(n, Q, S, UX, UR, X, R, st, partial);
-            SC_CHECK_LAUNCH();
-            if (abs(ntype) == 1) {
-                rc = ops.hx(X, HX0, gate);
+        if (exec) {
+            SC_CUDA(cudaGraphLaunch(exec, s));
+        } else {
+            for (int b = 0; b < batch; ++b) {
+                rc = iteration();
                 if (rc) return rc;
-                qmr_step_g<T><<<gr, kRedThreads, 0, s>>>(n, HX0, B, st, partial);
-                SC_CHECK_LAUNCH();
             }
-            ++it;
         }
+        it += batch;
         SC_CUDA(cudaMemcpyAsync(h_flag, &st->done, sizeof(int), cudaMemcpyDeviceToHost, s));
         SC_CUDA(cudaStreamSynchronize(s));
         if (*h_flag) break;
         if (it > qmrmax + batch) { set_error("QMR did not stop"); return SCALIT_ESTATE; }
     }
     SC_CUDA(cudaMemcpyAsync(&h, st, sizeof(h), cudaMemcpyDeviceToHost, s));
+    SC_CUDA(cudaMemcpyAsync(X, Xw, sizeof(T) * (size_t)n, cudaMemcpyDeviceToDevice, s));
     SC_CUDA(cudaStreamSynchronize(s));
     out->code = h.code;
     out->res = h.RES;
@@ -501,7 +546,8 @@ template int qmr_core<float>(scalit_ctx *, i64, QmrOps<float> &, int, int, doubl
 // The context's own operator pair: HX = MYHX(TA1), PX = MYPX(sOSB, TA1).
 template <class T> struct CtxQmrOps : QmrOps<T> {
     scalit_ctx *c;
-    T *tmp;
+    T *tmp = nullptr;
+    void set_scratch(T *p) override { tmp = p; }
     int hx(const T *in, T *out, const int *gate) override
     {
         return hx_vec<T>(c, in, out, T(c->E0), T(1), gate, c->stream);
@@ -518,21 +564,15 @@ int qmr_run(scalit_ctx *c, int ntype, int qmrmax, double qmrtol, int precision,
     if (!c->osb_built) { set_error("QMR needs the preconditioner: build or load it first"); return SCALIT_ESTATE; }
     const i64 n = c->L.N;
     if (precision == SCALIT_PREC_FP64) {
-        double *tmp = nullptr;
-        SC_CUDA(cudaMallocAsync(&tmp, sizeof(double) * (size_t)n, c->stream));
         CtxQmrOps<double> ops;
         ops.c = c;
-        ops.tmp = tmp;
-        int rc = qmr_core<double>(c, n, ops, ntype, qmrmax, qmrtol, dB, dX, out);
-        cudaFreeAsync(tmp, c->stream);
-        return rc;
+        return qmr_core<double>(c, n, ops, ntype, qmrmax, qmrtol, dB, dX, out);
     }
     if (precision != SCALIT_PREC_FP32) { set_error("unknown precision %d", precision); return SCALIT_EINVAL; }
     float *bx = nullptr;
-    SC_CUDA(cudaMallocAsync(&bx, sizeof(float) * 3 * (size_t)n, c->stream));
+    SC_CUDA(cudaMallocAsync(&bx, sizeof(float) * 2 * (size_t)n, c->stream));
     CtxQmrOps<float> ops;
     ops.c = c;
-    ops.tmp = bx + 2 * n;
     int rc = to_f32(dB, bx, n, c->stream);
     if (!rc) rc = qmr_core<float>(c, n, ops, ntype, qmrmax, qmrtol, bx, bx + n, out);
     if (!rc) rc = to_f64(bx + n, dX, n, c->stream);

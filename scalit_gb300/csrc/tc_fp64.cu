@@ -30,6 +30,7 @@
 // expiry the kernel records an error, waits (bounded) for its MMAs, frees its
 // TMEM and returns.
 #include "internal.cuh"
+#include "ptx.cuh"
 
 #include <cuda_bf16.h>
 
@@ -48,7 +49,6 @@ static constexpr int kTmemCols = 512;
 static constexpr int kStages = 3;                               // FP64 slab ring depth
 static constexpr int kSlab = kBM * 17;                          // doubles per slab stage
 static constexpr int kAStepBytes = kDigits * kBM * 16 * 2;    // 7 digit planes of 128 x 16 BF16
-static constexpr long long kWaitLimit = 1LL << 24;            // mbarrier polls before giving up
 
 struct TcArgs {
     int M, N, K, KS, NT;
@@ -66,12 +66,12 @@ struct TcArgs {
     int *err;
     const uint4 *bdig;    // [ntile][ks][digit][NT x 16 BF16, canonical]
     const int *bexp;      // [ntile * NT] column exponents
+    // Per-block B (the preconditioner's rotations): every block of Mi grid rows
+    // has its own matrix; tpb M tiles cover one block and never straddle two.
+    int tpb;              // 0: one B for all rows
+    i64 bdig_blk;         // uint4 stride between the blocks' digit planes
+    int bexp_blk;         // int stride between the blocks' exponents
 };
-
-__device__ __forceinline__ uint32_t smem_addr(const void *p)
-{
-    return static_cast<uint32_t>(__cvta_generic_to_shared(p));
-}
 
 // Shared-memory matrix descriptor, K-major, no swizzle: start address, the
 // byte distance between core matrices along K (LBO) and along M/N (SBO).
@@ -105,24 +105,6 @@ __device__ __forceinline__ void tc_commit(uint64_t *mbar)
 {
     asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];"
                  :: "r"(smem_addr(mbar)) : "memory");
-}
-
-__device__ __forceinline__ bool mbar_try(uint64_t *mbar, uint32_t parity)
-{
-    uint32_t ok;
-    asm volatile(
-        "{\n\t.reg .pred p;\n\t"
-        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
-        "selp.b32 %0, 1, 0, p;\n\t}\n"
-        : "=r"(ok) : "r"(smem_addr(mbar)), "r"(parity) : "memory");
-    return ok != 0;
-}
-
-__device__ __forceinline__ bool mbar_wait(uint64_t *mbar, uint32_t parity)
-{
-    for (long long i = 0; i < kWaitLimit; ++i)
-        if (mbar_try(mbar, parity)) return true;
-    return false;
 }
 
 __device__ __forceinline__ void fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
@@ -180,7 +162,21 @@ tc_level_kernel(TcArgs g)
     uint32_t *tslot = reinterpret_cast<uint32_t *>(mbar + 2);
 
     const int tid = threadIdx.x, warp = tid >> 5;
-    const int m0 = blockIdx.x * kBM, ntile = blockIdx.y, z = blockIdx.z;
+    const int ntile = blockIdx.y, z = blockIdx.z;
+    // rows [m0, mlim) of this tile; with per-block B the tile stays inside block bsel
+    int m0, mlim;
+    const uint4 *bdig = g.bdig;
+    const int *bexp = g.bexp;
+    if (g.tpb > 0) {
+        const int bsel = blockIdx.x / g.tpb, lt = blockIdx.x - bsel * g.tpb;
+        m0 = bsel * (int)g.Mi + lt * kBM;
+        mlim = min(g.M, bsel * (int)g.Mi + (int)g.Mi);
+        bdig += (i64)bsel * g.bdig_blk;
+        bexp += (i64)bsel * g.bexp_blk;
+    } else {
+        m0 = blockIdx.x * kBM;
+        mlim = g.M;
+    }
     const double *A = g.A + (i64)z * g.a_sz;
     double *C = g.C + (i64)z * g.c_sz;
 
@@ -205,7 +201,7 @@ tc_level_kernel(TcArgs g)
     // 16-wide K step.
     const int row = tid & (kBM - 1), q = tid >> 7;
     const int m = m0 + row;
-    const bool mvalid = m < g.M;
+    const bool mvalid = m < mlim;
     const i64 moff = mvalid ? (i64)(m % g.Mi) * g.s1 + (i64)(m / g.Mi) * g.s2 : 0;
     // FP64 operand slabs (16 K values x 128 rows) stream through a kStages ring by
     // cp.async: pass 1 (slabs 0..KS-1) finds the row exponents, pass 2 (slabs
@@ -220,7 +216,7 @@ tc_level_kernel(TcArgs g)
     for (int i = 0; i < 4; ++i) {
         const int r = rowc ? ((tid >> 4) + 32 * i) : row;
         const int mm = m0 + r;
-        lvalid[i] = mm < g.M;
+        lvalid[i] = mm < mlim;
         lmoff[i] = lvalid[i] ? (i64)(mm % g.Mi) * g.s1 + (i64)(mm / g.Mi) * g.s2 : 0;
     }
     auto issue = [&](int t) {
@@ -311,7 +307,7 @@ tc_level_kernel(TcArgs g)
             *reinterpret_cast<uint2 *>(Ab + s * (kBM * 32) + rowoff) = make_uint2(w[0], w[1]);
         }
         // the K step's B digit planes (pre-cut, already in the canonical layout)
-        const uint4 *src = g.bdig + ((i64)ntile * KS + ks) * (bstep / 16);
+        const uint4 *src = bdig + ((i64)ntile * KS + ks) * (bstep / 16);
         uint4 *dst = reinterpret_cast<uint4 *>(Bb);
         for (int i = tid; i < bstep / 16; i += kThreadsTC) dst[i] = src[i];
         asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
@@ -367,7 +363,7 @@ tc_level_kernel(TcArgs g)
                     T += (long long)__float2int_rn(gv[gq][j]) << (7 * (kGroups - 2 - gq));
                 double val = (double)T;
                 if (T != 0)   // times 2^e_n by an exponent add on the bits (no FP64 op)
-                    val = __longlong_as_double(__double_as_longlong(val) + ((long long)g.bexp[n] << 52));
+                    val = __longlong_as_double(__double_as_longlong(val) + ((long long)bexp[n] << 52));
                 const i64 p = moff + (i64)n * g.c_sn;
                 double out = sc * val;
                 if (g.diagV) out = fma(g.alpha * (g.diagV[p] - g.shift), g.diagX[p + (i64)z * g.dx_sz], out);
@@ -447,6 +443,131 @@ int tc_prepare(scalit_ctx *c)
     }
     if (!c->tc_err) SC_CUDA(cudaMalloc(&c->tc_err, sizeof(int)));
     SC_CUDA(cudaMemset(c->tc_err, 0, sizeof(int)));
+    return 0;
+}
+
+// Digit planes of the preconditioner's rotations of level l (VOSB level l:
+// blk matrices V_b of n x n).  transpose = 0 plans V_b (VX), 1 plans V_b^T
+// (VTX).  One thread per (block, column n of B), B(k, n) = H(n, k) with H = V_b
+// or V_b^T; the digits, exponents and layout are those of cut_level_matrix.
+__global__ void cut_rot_kernel(int nout, int NT, int ntiles, int KS, int blk, const double *__restrict__ V,
+                               int transpose, uint16_t *__restrict__ dig, int *__restrict__ exps)
+{
+    const i64 idx = blockIdx.x * (i64)blockDim.x + threadIdx.x;
+    if (idx >= (i64)blk * nout) return;
+    const int b = (int)(idx / nout), n = (int)(idx - (i64)b * nout);
+    const double *Vb = V + (i64)b * nout * nout;
+    double mx = 0.0;
+    for (int k = 0; k < nout; ++k) {
+        const double v = transpose ? Vb[k + (i64)n * nout] : Vb[n + (i64)k * nout];
+        mx = fmax(mx, fabs(v));
+    }
+    int e = 0;
+    if (mx > 0.0) frexp(mx, &e);
+    exps[(i64)b * ntiles * NT + n] = e;
+    const int tile = n / NT, nn = n % NT;
+    for (int k = 0; k < nout; ++k) {
+        double r = ldexp(transpose ? Vb[k + (i64)n * nout] : Vb[n + (i64)k * nout], 7 - e);
+        const int ks = k / 16, kk = k % 16;
+        #pragma unroll
+        for (int t = 0; t < kDigits; ++t) {
+            const double d = trunc(r);
+            r = (r - d) * 128.0;
+            const size_t base = ((((size_t)b * ntiles + tile) * KS + ks) * kDigits + t) * (size_t)NT * 16;
+            const size_t off = (size_t)(nn >> 3) * 128 + (size_t)(kk >> 3) * 64 + (size_t)(nn & 7) * 8 + (kk & 7);
+            dig[base + off] = __bfloat16_as_ushort(__float2bfloat16_rn((float)d));   // |d| <= 127: exact
+        }
+    }
+}
+
+void tc_free_px(scalit_ctx *c)
+{
+    for (int l = 0; l < SCALIT_FMAX; ++l)
+        for (int d = 0; d < 2; ++d) {
+            TcLevelData &t = c->pxtc[l][d];
+            if (t.dig) cudaFree(t.dig);
+            if (t.exps) cudaFree(t.exps);
+            t = TcLevelData{};
+        }
+}
+
+int tc_prepare_px(scalit_ctx *c)
+{
+    const Layout &L = c->L;
+    tc_free_px(c);
+    for (int l = 1; l < L.nlev; ++l) {
+        const int nout = L.n[l];
+        if (nout > 256 || L.dim[l] < 2) continue;   // group exactness needs K <= 256
+        const int NT = std::min(64, (nout + 15) / 16 * 16);
+        const int ntiles = (nout + NT - 1) / NT;
+        const int KS = (nout + 15) / 16;
+        const i64 blk = L.blk[l];
+        const size_t ndig = (size_t)blk * ntiles * KS * kDigits * NT * 16;
+        const size_t nexp = (size_t)blk * ntiles * NT;
+        for (int d = 0; d < 2; ++d) {
+            TcLevelData &t = c->pxtc[l][d];
+            SC_CUDA(cudaMalloc(&t.dig, ndig * sizeof(uint16_t)));
+            SC_CUDA(cudaMalloc(&t.exps, nexp * sizeof(int)));
+            SC_CUDA(cudaMemsetAsync(t.dig, 0, ndig * sizeof(uint16_t), c->stream));
+            SC_CUDA(cudaMemsetAsync(t.exps, 0, nexp * sizeof(int), c->stream));
+            const i64 items = blk * nout;
+            cut_rot_kernel<<<(int)((items + 127) / 128), 128, 0, c->stream>>>(nout, NT, ntiles, KS, (int)blk,
+                                                                               c->VOSB + L.vs[l], d, t.dig, t.exps);
+            SC_CHECK_LAUNCH();
+            t.NT = NT;
+            t.ntiles = ntiles;
+            t.KS = KS;
+            t.usable = 1;
+        }
+    }
+    SC_CUDA(cudaStreamSynchronize(c->stream));
+    return 0;
+}
+
+bool tc_px_usable(const scalit_ctx *c, int l)
+{
+    return c->fp64_mode == SCALIT_FP64_TENSOR && c->pxtc[l][0].usable && c->pxtc[l][1].usable;
+}
+
+// VX (transpose = 0) / VTX (1) of level l >= 1 on the digit engine:
+// Y(a, i, b) = sum_j V_b(i, j) X(a, j, b)  or  sum_j V_b(j, i) X(a, j, b).
+int tc_rot_apply(const scalit_ctx *c, int l, int transpose, const double *X, double *Y, const int *gate,
+                 cudaStream_t s)
+{
+    const Layout &L = c->L;
+    const TcLevelData &t = c->pxtc[l][transpose ? 1 : 0];
+    if (!t.usable) { set_error("level %d has no tensor-core rotation plan", l + 1); return SCALIT_EUNSUP; }
+    const int nout = L.n[l];
+    const i64 nin = L.dim[l], blk = L.blk[l];
+    const i64 M = nin * blk;
+    if (M > 2147483647LL || nin > 2147483647LL) { set_error("level %d too large", l + 1); return SCALIT_EINVAL; }
+    TcArgs g{};
+    g.N = nout; g.K = nout; g.KS = t.KS; g.NT = t.NT;
+    g.M = (int)M; g.Mi = nin; g.s1 = 1; g.s2 = nin * nout; g.a_sk = nin; g.c_sn = nin;
+    g.A = X; g.a_sz = 0;
+    g.C = Y; g.c_sz = 0;
+    g.accumulate = 0;
+    g.alpha = 1.0;
+    g.gate = gate;
+    g.err = c->tc_err;
+    g.bdig = reinterpret_cast<const uint4 *>(t.dig);
+    g.bexp = t.exps;
+    i64 gx;
+    if (blk > 1) {
+        g.tpb = (int)((nin + kBM - 1) / kBM);
+        g.bdig_blk = (i64)t.ntiles * t.KS * kDigits * t.NT * 2;
+        g.bexp_blk = t.ntiles * t.NT;
+        gx = blk * g.tpb;
+    } else {
+        gx = (M + kBM - 1) / kBM;
+    }
+    if (gx > 2147483647LL) { set_error("level %d too large", l + 1); return SCALIT_EINVAL; }
+    const size_t smem = 2 * (size_t)kAStepBytes + 2 * (size_t)kDigits * t.NT * 32 + (size_t)kStages * kSlab * 8 +
+                        64 + 3072;
+    const size_t smem_req = std::max(smem, (size_t)(116 * 1024));
+    SC_CUDA(cudaFuncSetAttribute(tc_level_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_req));
+    tc_level_kernel<<<dim3((unsigned)gx, t.ntiles, 1), kThreadsTC, smem_req, s>>>(g);
+    SC_CHECK_LAUNCH();
     return 0;
 }
 

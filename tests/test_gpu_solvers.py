@@ -72,7 +72,7 @@ def test_qmr_zero_rhs_breakdown(lib, c0):
     assert not X.any()
 
 
-@pytest.mark.parametrize("orth", [0, 1])
+@pytest.mark.parametrize("orth", [0, 1, 2])
 def test_pist_c0_matches_oracle(lib, orc, c0, orth):
     e0 = float(c0.RES.min())
     ref = orc.Operator.from_problem(c0, E0=e0)
@@ -85,7 +85,7 @@ def test_pist_c0_matches_oracle(lib, orc, c0, orth):
         return rc, X
 
     st_r, eig_r, res_r, info_r = orc.pist_conv(e0, etol, 0, x0, 40, 5, 1, M, 400,
-                                               lambda v: ref.hx(v, 0), linsolv, orth=orth)
+                                               lambda v: ref.hx(v, 0), linsolv, orth=min(orth, 1))
     assert st_r > 0
     with capi.Context.from_problem(c0, e0=e0) as ctx:
         ctx.build_osb(20, 1e-4)
@@ -117,9 +117,13 @@ def test_pist_long_run_orthogonality(lib, orc):
         ctx.build_osb(20, 1e-4)
         st0, eig0, _, _ = ctx.pist(x0, 50, e0, 1e-11, m_max=1000, qmr_max=2000, qmr_tol=1e-4, orth=0)
         st1, eig1, _, info1 = ctx.pist(x0, 50, e0, 1e-11, m_max=1000, qmr_max=2000, qmr_tol=1e-4, orth=1)
+        # the mixed path: FP32 inner solves and an FP32 first Gram-Schmidt pass
+        st2, eig2, _, _ = ctx.pist(x0, 50, e0, 1e-11, m_max=1000, qmr_max=2000, qmr_tol=1e-4, orth=2,
+                                   precision=capi.PREC_FP32)
     assert st0 > 0 and eig0[0] < 1e-9            # the reference's MGS: spurious ~0 level
-    assert st1 > 0
+    assert st1 > 0 and st2 > 0
     assert np.abs(eig1 - eig_r).max() * hm.HARTREE_CM < CM_TOL
+    assert np.abs(eig2 - eig_r).max() * hm.HARTREE_CM < CM_TOL
 
 
 def test_pist_fp32_inner(lib, orc, c0):
@@ -143,8 +147,10 @@ def test_pist_bad_params(lib, c0):
     with capi.Context.from_problem(c0, e0=0.0) as ctx:
         ctx.build_osb(20, 1e-4)
         st, eig, res, info = ctx.pist(np.ones(c0.N), 5, 0.0, 1e-8, m_max=100, gap=200)
-    assert st == 0
-    assert info["qmr_solves"] == 0
+        assert st == 0
+        assert info["qmr_solves"] == 0
+        with pytest.raises(capi.ScalitError):
+            ctx.pist(np.ones(c0.N), 5, 0.0, 1e-8, m_max=100, orth=3)
 
 
 def test_qmr_matches_oracle_iteration_for_iteration(lib, orc, c0):
@@ -160,3 +166,21 @@ def test_qmr_matches_oracle_iteration_for_iteration(lib, orc, c0):
     code_r, X_r, res_r, it_r = ref.qmr(b, 300, 1e-9, ntype=-1)
     assert code == code_r
     assert rel(X, X_r) < 1e-8
+
+
+def test_pist_residuals_match_host_check(lib, orc, c0):
+    """The device residual check |H psi - E psi| equals the oracle's H*X applied
+    to the returned Ritz vectors, and is small for converged levels."""
+    e0 = float(c0.RES.min())
+    ref = orc.Operator.from_problem(c0, E0=e0)
+    x0 = orc.start_vector(c0.N, 0)
+    with capi.Context.from_problem(c0, e0=e0) as ctx:
+        ctx.build_osb(20, 1e-4)
+        st, eig, _, info = ctx.pist(x0, 20, e0, 1e-11, m_max=400, qmr_max=500, qmr_tol=1e-4, residuals=True)
+        st_v, eig_v, _, info_v = ctx.pist(x0, 20, e0, 1e-11, m_max=400, qmr_max=500, qmr_tol=1e-4, vectors=True)
+    assert st > 0 and st_v == st
+    np.testing.assert_array_equal(eig, eig_v)
+    psi = info_v["vectors"]
+    host = np.array([np.linalg.norm(ref.hx(psi[k], 0) - eig[k] * psi[k]) for k in range(20)])
+    np.testing.assert_allclose(info["resid"], host, rtol=1e-6, atol=1e-14)
+    assert info["resid"].max() < 1e-3
