@@ -47,6 +47,9 @@ def parse():
     ap.add_argument("--pist-workload", default="tri-24x32x20",
                     help="grid of the PIST leg ('none' skips it)")
     ap.add_argument("--pist-levels", type=int, default=20)
+    ap.add_argument("--batch-problems", type=int, default=0,
+                    help="shifted-QMR leg over this many uneven problems (0 skips it)")
+    ap.add_argument("--batch-shifts", type=int, default=16)
     return ap.parse_args()
 
 
@@ -128,6 +131,19 @@ def load_peaks():
         return float(d["hbm_gbs"]), float(d["bf16_tflops"]), "measured"
     except Exception:
         return 6800.0, 1900.0, "fallback"
+
+
+def profiled_traffic(workload, level):
+    """DRAM bytes per single-vector launch of the tensor-core level kernel, from
+    the committed ncu summary of this workload (None when not profiled)."""
+    import re
+    path = os.path.join(ROOT, "profiles", f"tc_level_kernel_{workload}.md")
+    try:
+        with open(path) as f:
+            m = re.search(rf"traffic_per_launch_level{level}_nvec1:\s*(\d+)", f.read())
+        return int(m.group(1)) if m else None
+    except OSError:
+        return None
 
 
 def hx_units(sizes):
@@ -257,6 +273,52 @@ def pist_leg(workload, levels, device, capi, hm):
     return out
 
 
+def batch_leg(nprob, nrhs, device, capi, hm):
+    """Uneven problems (n_R, n_r in [24, 96], n_theta in [16, 64], PES +-10%),
+    each with nrhs shifts over its lowest 0.02 Eh and one FP32 QMR on all of
+    them, every problem advanced by one CUDA graph; then the same problems one
+    after another for comparison."""
+    import torch
+    probs = hm.batched_problems(nprob, seed=0)
+    ctxs = [capi.Context.from_problem(p, e0=0.0, device=device) for p in probs]
+    try:
+        t0 = time.perf_counter()
+        for c in ctxs:
+            c.set_precond(capi.TOSBD1, 0.002, 0.0)
+            c.build_osb(20, 1e-4)
+        build_s = time.perf_counter() - t0
+        rng = np.random.default_rng(7)
+        shifts = np.stack([float(p.RES.min()) + 0.02 * (np.arange(nrhs) + 0.5) / nrhs for p in probs])
+        dBs = [torch.tensor(rng.standard_normal((nrhs, p.N)), device=f"cuda:{device}") for p in probs]
+        dXs = [torch.zeros_like(b) for b in dBs]
+        capi.qmr_shifts_batch(ctxs[:1], shifts[:1], dBs[:1], dXs[:1], 2000, 1e-4)      # warm-up
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        codes, res, dev_s = capi.qmr_shifts_batch(ctxs, shifts, dBs, dXs, 2000, 1e-4,
+                                                  precision=capi.PREC_FP32)
+        wall = time.perf_counter() - t0
+        its = np.abs(codes).astype(np.int64)
+        points = np.array([p.N for p in probs])
+        hx_apps = int((2 * its).sum())                      # QMR_MPI type -1: 2 H*X per iteration
+        hx_points = float((2 * its * points[:, None]).sum())
+        t0 = time.perf_counter()
+        for k, c in enumerate(ctxs):
+            c.qmr_shifts_device(dBs[k], torch.zeros_like(dBs[k]), shifts[k], 2000, 1e-4,
+                                precision=capi.PREC_FP32)
+        torch.cuda.synchronize()
+        seq = time.perf_counter() - t0
+        return {"problems": nprob, "shifts": nrhs, "points_total": int(points.sum()),
+                "points_min": int(points.min()), "points_max": int(points.max()),
+                "build_s": build_s, "solve_wall_s": wall, "solve_device_s": dev_s,
+                "converged": int((codes > 0).sum()), "systems": int(codes.size),
+                "qmr_iterations_total": int(its.sum()), "hx_apps": hx_apps,
+                "hx_apps_per_s": hx_apps / wall, "hx_points_per_s": hx_points / wall,
+                "one_by_one_wall_s": seq, "batch_speedup": seq / wall}
+    finally:
+        for c in ctxs:
+            c.close()
+
+
 # ------------------------------------------------------------------- ours --
 def run_ours(args):
     import torch
@@ -340,21 +402,30 @@ def run_ours(args):
     except Exception:
         fp64_peak = None
 
-    # FP32 (the inner-solve arithmetic) on the same block
+    # FP32 (the inner-solve arithmetic) on the same block, both FP32 engines
     X32 = [x.float() for x in X]
     Y32 = [torch.empty_like(x) for x in X32]
-    with torch.cuda.stream(stream):
-        for i in range(3):
-            ctx.hx_f32_device(X32[i % 2], Y32[i % 2], nvec, capi.TA1)
-    torch.cuda.synchronize()
-    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    with torch.cuda.stream(stream):
-        a.record(stream)
-        for i in range(args.steps):
-            ctx.hx_f32_device(X32[i % 2], Y32[i % 2], nvec, capi.TA1)
-        b.record(stream)
-    torch.cuda.synchronize()
-    fp32_apps = args.steps * nvec / (a.elapsed_time(b) / 1e3)
+
+    def time_f32(fn):
+        with torch.cuda.stream(stream):
+            for i in range(3):
+                fn(X32[i % 2], Y32[i % 2], nvec, capi.TA1)
+        torch.cuda.synchronize()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        with torch.cuda.stream(stream):
+            a.record(stream)
+            for i in range(args.steps):
+                fn(X32[i % 2], Y32[i % 2], nvec, capi.TA1)
+            b.record(stream)
+        torch.cuda.synchronize()
+        return args.steps * nvec / (a.elapsed_time(b) / 1e3)
+
+    fp32_engines = {}
+    for name, mode in (("simt", capi.FP32_SIMT), ("tensor_bf16x3", capi.FP32_TENSOR)):
+        ctx.set_fp32_mode(mode)
+        fp32_engines[name] = time_f32(ctx.hx_f32_device)
+    ctx.set_fp32_mode(capi.FP32_SIMT)
+    fp32_apps = max(fp32_engines.values())
 
     # P*X (MYPX, TA1) of the same block in FP64 and FP32, after one preconditioner build
     t0 = time.perf_counter()
@@ -375,6 +446,9 @@ def run_ours(args):
             b.record(stream)
         torch.cuda.synchronize()
         px_apps[name] = args.steps * nvec / (a.elapsed_time(b) / 1e3)
+    ctx.set_fp32_mode(capi.FP32_TENSOR)
+    px_apps["fp32_tensor_bf16x3"] = time_f32(ctx.px_f32_device)
+    ctx.set_fp32_mode(capi.FP32_SIMT)
     del X32, Y32
 
     # end to end through the host-buffer ABI (pinned host memory)
@@ -396,6 +470,9 @@ def run_ours(args):
     pist = None
     if args.pist_workload != "none" and args.pist_levels > 0:
         pist = pist_leg(args.pist_workload, args.pist_levels, local, capi, hm)
+    batch = None
+    if args.batch_problems > 0:
+        batch = batch_leg(args.batch_problems, args.batch_shifts, local, capi, hm)
 
     if rank == 0:
         line = {
@@ -408,7 +485,7 @@ def run_ours(args):
                        "parallelism": f"replicas{world}",
                        "l2": "two alternating 2x151 MB input/output sets (> 129 MB L2)"},
             "roofline": {"bound": "hbm", "achieved": ach_gbs, "peak": hbm, "unit": "GB/s",
-                         "frac": ach_gbs / hbm, "traffic": None,
+                         "frac": ach_gbs / hbm, "traffic": profiled_traffic(args.workload, dom + 1),
                          "kernel": f"tc_level_kernel level {dom + 1}",
                          "peak_source": peak_src,
                          "algorithmic_bytes_per_launch": lv[dom]["bytes"],
@@ -419,7 +496,7 @@ def run_ours(args):
                               "algorithmic_flops_per_launch": lv[dom]["flops"]},
             "level_ms": level_ms,
             "hx_flops_per_app": total_flops, "hx_bytes_per_app": total_bytes,
-            "fp32_apps_per_s": fp32_apps,
+            "fp32_apps_per_s": fp32_apps, "fp32_engines_apps_per_s": fp32_engines,
             "px_apps_per_s": px_apps,
             "osb_build": {"seconds": build_s, "levels_s": build_levels},
             "e2e": {"value": e2e_value, "unit": "H*X apps/s",
@@ -431,6 +508,8 @@ def run_ours(args):
             line["cpu_baseline"] = base
         if pist is not None:
             line["pist"] = pist
+        if batch is not None:
+            line["batch"] = batch
         print(json.dumps(line), flush=True)
     ctx.close()
     if world > 1:

@@ -48,6 +48,10 @@ extern "C" {
 #define SCALIT_FP64_TENSOR 1 /* 7-bit digit slices on the BF16 tensor cores (tcgen05), */
                              /* exact FP32 group sums, FP64 recombination (default)     */
 
+/* engine of the FP32 (inner-solve) level products and preconditioner rotations */
+#define SCALIT_FP32_SIMT 0   /* FP32 CUDA cores (strided GEMM)                         */
+#define SCALIT_FP32_TENSOR 1 /* split-BF16 x3 on the tensor cores (tcgen05), FP32 sums */
+
 /* arithmetic of the QMR inner solves */
 #define SCALIT_PREC_FP64 0
 #define SCALIT_PREC_FP32 1
@@ -86,6 +90,10 @@ int scalit_set_stream(scalit_ctx *ctx, void *stream);
  * Levels with more than 256 points, and the per-point outer layer, always use
  * the FP64 pipe. */
 int scalit_set_fp64_mode(scalit_ctx *ctx, int mode);
+/* Engine of the FP32 level products and preconditioner rotations
+ * (SCALIT_FP32_SIMT or SCALIT_FP32_TENSOR; levels above 256 points stay on
+ * the CUDA cores).  No reference counterpart: the reference has no FP32 path. */
+int scalit_set_fp32_mode(scalit_ctx *ctx, int mode);
 /* sOSBW%mE0: the shift of (H - E0) and of the preconditioner. */
 int scalit_set_shift(scalit_ctx *ctx, double e0);
 /* sOSB kernel kind with sOSBW%mDE and sOSBW%mBeta. */
@@ -115,6 +123,12 @@ int scalit_hx_f32_device(scalit_ctx *ctx, int ntype, int nvec, const float *dX, 
  * and max Jacobi efficiency, their sum, the sum of squared diagonals and the
  * sum of sweep counters (the reference's eff(1:5)). */
 int scalit_build_osb(scalit_ctx *ctx, int bjmax, double bjtol, double *stats);
+/* The CUDA-core GEMM tile the load-time autotuner picked for each level:
+ * picks[(prec * sF + level) * 2 + many], prec 0 = FP64 / 1 = FP32, many 0 = one
+ * vector / 1 = a block of 16; 0 = 128x128 (FP32) / 64x64 (FP64) tiles,
+ * 1 = the half-size tiles, -1 = not tuned (that engine is not used there).
+ * No reference counterpart (the reference has one loop order). */
+int scalit_tile_picks(scalit_ctx *ctx, int *picks);
 /* Wall seconds spent on each level (sF entries, level 1 first) by the last
  * scalit_build_osb; the reference prints the whole build's time only
  * (osb.progDiag.h:40-47). */
@@ -163,6 +177,28 @@ int scalit_qmr(scalit_ctx *ctx, int ntype, int qmrmax, double qmrtol, int precis
                const double *B, double *X, double *res, int *iters);
 int scalit_qmr_device(scalit_ctx *ctx, int ntype, int qmrmax, double qmrtol, int precision,
                       const double *dB, double *dX, double *res, int *iters);
+
+/* ----------------------------------------------- shifts and batches -----
+ * No reference counterpart: the reference solves one system per QMR call
+ * (qmr.f90:5-175).  QMR on nrhs right-hand sides at once: column v of dB / dX
+ * (npoints x nrhs, device, FP64) solves (H - shifts[v]) x = b with the
+ * preconditioner's kernel shifted to shifts[v] (the ctx's sOSB kind, TA1);
+ * all columns advance in lockstep through batched H*X / P*X launches, each
+ * with its own recurrence and stopping test (ntype, qmrmax, qmrtol as in
+ * scalit_qmr; precision SCALIT_PREC_FP32 runs the vectors and operators in
+ * FP32).  codes[v] (may be NULL) receives QMR_MPI's status of column v and
+ * res[v] (may be NULL) its final residual measure. */
+int scalit_qmr_shifts_device(scalit_ctx *ctx, int nrhs, const double *shifts, int ntype, int qmrmax,
+                             double qmrtol, int precision, const double *dB, double *dX, int *codes,
+                             double *res);
+/* The same for nprob independent problems on one GPU (each context loaded,
+ * preconditioned and with its own stream), advanced together by one CUDA graph
+ * with a branch per problem.  shifts, codes, res: nprob x nrhs (problem-major);
+ * dB[p], dX[p]: problem p's device arrays.  *seconds (may be NULL) receives the
+ * device time of the iterations. */
+int scalit_qmr_shifts_batch(scalit_ctx *const *ctxs, int nprob, int nrhs, const double *shifts, int ntype,
+                            int qmrmax, double qmrtol, int precision, const double *const *dB,
+                            double *const *dX, int *codes, double *res, double *seconds);
 
 /* ----------------------------------------------------------------- PIST ---
  * OSB_PISTCONV -> PIST_CONV / PIST_CONV_MPI

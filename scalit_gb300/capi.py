@@ -14,6 +14,7 @@ from . import build as _build
 
 TA0, TA1 = 0, 1
 TOSB, TOSBD1, TOSBD2 = 1, 2, 3
+FP32_SIMT, FP32_TENSOR = 0, 1
 PREC_FP64, PREC_FP32 = 0, 1
 FP64_DFMA, FP64_TENSOR = 0, 1
 FMAX = 20
@@ -43,6 +44,8 @@ SIGNATURES = {
     "scalit_level_device": (C.c_int, [_vp, C.c_int, C.c_int, _vp, _vp]),
     "scalit_build_osb": (C.c_int, [_vp, C.c_int, C.c_double, _dp]),
     "scalit_build_times": (C.c_int, [_vp, _dp]),
+    "scalit_set_fp32_mode": (C.c_int, [_vp, C.c_int]),
+    "scalit_tile_picks": (C.c_int, [_vp, _ip]),
     "scalit_get_osb": (C.c_int, [_vp, _dp, _dp]),
     "scalit_set_osb": (C.c_int, [_vp, _dp, _dp]),
     "scalit_px": (C.c_int, [_vp, C.c_int, C.c_int, _dp, _dp]),
@@ -60,6 +63,11 @@ SIGNATURES = {
     "scalit_hf_gradients": (C.c_int, [_vp, C.c_int, _dp, C.c_int, _dp, _dp]),
     "scalit_pist_vectors": (C.c_int, [_vp, _vp, _dp, _dp, _dp, _vp, _dp]),
     "scalit_pist_residuals": (C.c_int, [_vp, _vp, _dp, _dp, _dp, _vp, _dp]),
+    "scalit_qmr_shifts_device": (C.c_int, [_vp, C.c_int, _dp, C.c_int, C.c_int, C.c_double, C.c_int, _vp, _vp,
+                                           _ip, _dp]),
+    "scalit_qmr_shifts_batch": (C.c_int, [C.POINTER(C.c_void_p), C.c_int, C.c_int, _dp, C.c_int, C.c_int,
+                                          C.c_double, C.c_int, C.POINTER(C.c_void_p), C.POINTER(C.c_void_p),
+                                          _ip, _dp, _dp]),
     "scalit_pist_basis": (C.c_int, [_vp, _vp, _dp, _dp, _dp, _vp, _ip, _dp, _dp, _dp]),
     # Fortran drop-ins (all arguments by reference)
     "h1x_xyz_": (None, [_ip, _ip, _ip, _dp, _dp, _dp]),
@@ -221,6 +229,9 @@ class Context:
     def set_fp64_mode(self, mode):
         _check(self.lib.scalit_set_fp64_mode(self.h, int(mode)))
 
+    def set_fp32_mode(self, mode):
+        _check(self.lib.scalit_set_fp32_mode(self.h, int(mode)))
+
     def set_shift(self, e0):
         _check(self.lib.scalit_set_shift(self.h, float(e0)))
 
@@ -248,6 +259,12 @@ class Context:
         stats = np.zeros(5 * len(self.sizes))
         _check(self.lib.scalit_build_osb(self.h, int(bjmax), float(bjtol), _p(stats)))
         return stats.reshape(len(self.sizes), 5)
+
+    def tile_picks(self):
+        """Autotuned GEMM tiles, shape (precision [FP64, FP32], level, [one vector, many])."""
+        t = np.zeros(2 * len(self.sizes) * 2, dtype=np.int32)
+        _check(self.lib.scalit_tile_picks(self.h, t.ctypes.data_as(C.POINTER(C.c_int))))
+        return t.reshape(2, len(self.sizes), 2)
 
     def build_times(self):
         t = np.zeros(len(self.sizes))
@@ -280,6 +297,18 @@ class Context:
 
     def px_f32_device(self, dX, dY, nvec=1, npc=TA1):
         _check(self.lib.scalit_px_f32_device(self.h, int(npc), int(nvec), _ptr(dX), _ptr(dY)))
+
+    def qmr_shifts_device(self, dB, dX, shifts, qmrmax, qmrtol, ntype=-1, precision=PREC_FP64):
+        """QMR on len(shifts) right-hand sides at once (device arrays nrhs x N, FP64):
+        column v solves (H - shifts[v]) x = b_v.  Returns (codes, res)."""
+        shifts = _f64(shifts)
+        nrhs = shifts.size
+        codes = np.zeros(nrhs, dtype=np.int32)
+        res = np.zeros(nrhs)
+        _check(self.lib.scalit_qmr_shifts_device(self.h, nrhs, _p(shifts), int(ntype), int(qmrmax), float(qmrtol),
+                                                 int(precision), _ptr(dB), _ptr(dX),
+                                                 codes.ctypes.data_as(C.POINTER(C.c_int)), _p(res)))
+        return codes, res
 
     def qmr(self, B, qmrmax, qmrtol, ntype=-1, precision=PREC_FP64, X0=None):
         """OSB_QMR: returns (code, X, RES, iterations)."""
@@ -361,3 +390,22 @@ class Context:
         st = _check(self.lib.scalit_pist(self.h, C.byref(p), _p(x0), _p(eig), C.byref(res),
                                          C.byref(info)))
         return st, eig, res.value, dict(info.as_dict(), m_max=p.m_max, startcnt=p.startcnt)
+
+
+def qmr_shifts_batch(contexts, shifts, dBs, dXs, qmrmax, qmrtol, ntype=-1, precision=PREC_FP32):
+    """Shifted QMR of several problems advanced together by one CUDA graph.
+    shifts: nprob x nrhs; dBs / dXs: per problem device arrays nrhs x N (FP64).
+    Returns (codes, res, device_seconds)."""
+    lib = load()
+    shifts = np.ascontiguousarray(np.asarray(shifts, dtype=np.float64))
+    nprob, nrhs = shifts.shape
+    ctxs = (C.c_void_p * nprob)(*[c.h for c in contexts])
+    bs = (C.c_void_p * nprob)(*[_ptr(b) for b in dBs])
+    xs = (C.c_void_p * nprob)(*[_ptr(x) for x in dXs])
+    codes = np.zeros((nprob, nrhs), dtype=np.int32)
+    res = np.zeros((nprob, nrhs))
+    sec = C.c_double(0.0)
+    _check(lib.scalit_qmr_shifts_batch(ctxs, nprob, nrhs, _p(shifts), int(ntype), int(qmrmax), float(qmrtol),
+                                       int(precision), bs, xs, codes.ctypes.data_as(C.POINTER(C.c_int)), _p(res),
+                                       C.byref(sec)))
+    return codes, res, sec.value

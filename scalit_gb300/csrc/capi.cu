@@ -166,7 +166,7 @@ void scalit_destroy(scalit_ctx *c)
     for (int l = 0; l < SCALIT_FMAX; ++l) {
         if (c->tc[l].dig) cudaFree(c->tc[l].dig);
         if (c->tc[l].exps) cudaFree(c->tc[l].exps);
-        if (l == 0) tc_free_px(c);
+        if (l == 0) { tc_free_px(c); tc32_free(c, true, true); }
     }
     if (c->tc_err) cudaFree(c->tc_err);
     for (int i = 0; i < 2; ++i) if (c->qg[i].exec) cudaGraphExecDestroy(c->qg[i].exec);
@@ -259,9 +259,25 @@ int scalit_load(scalit_ctx *c, const double *H0, const double *RES, const double
     if (rc) return rc;
     SC_CUDA(cudaStreamSynchronize(s));
     rc = tc_prepare(c);
+    if (!rc) rc = tc32_prepare(c, false);
+    if (rc) return rc;
+    memset(c->tile_pick, -1, sizeof(c->tile_pick));
+    rc = gemm_autotune(c, 16);
     if (rc) return rc;
     c->loaded = true;
     c->osb_built = false;
+    c->gen++;
+    return 0;
+}
+
+int scalit_tile_picks(scalit_ctx *c, int *picks)
+{
+    CTX_CHECK(c);
+    if (!picks) { set_error("null output"); return SCALIT_EINVAL; }
+    int k = 0;
+    for (int p = 0; p < 2; ++p)
+        for (int l = 0; l < c->L.nlev; ++l)
+            for (int m = 0; m < 2; ++m) picks[k++] = c->tile_pick[p][l][m];
     return 0;
 }
 
@@ -270,6 +286,15 @@ int scalit_set_fp64_mode(scalit_ctx *c, int mode)
     if (!c) { set_error("null context"); return SCALIT_EINVAL; }
     if (mode != SCALIT_FP64_DFMA && mode != SCALIT_FP64_TENSOR) { set_error("unknown FP64 mode %d", mode); return SCALIT_EINVAL; }
     c->fp64_mode = mode;
+    c->gen++;
+    return 0;
+}
+
+int scalit_set_fp32_mode(scalit_ctx *c, int mode)
+{
+    if (!c) { set_error("null context"); return SCALIT_EINVAL; }
+    if (mode != SCALIT_FP32_SIMT && mode != SCALIT_FP32_TENSOR) { set_error("unknown FP32 mode %d", mode); return SCALIT_EINVAL; }
+    c->fp32_mode = mode;
     c->gen++;
     return 0;
 }
@@ -444,7 +469,9 @@ int scalit_set_osb(scalit_ctx *c, const double *VOSB, const double *EIG0)
     SC_CUDA(cudaStreamSynchronize(c->stream));
     c->osb_built = true;
     c->gen++;
-    return tc_prepare_px(c);
+    rc = tc_prepare_px(c);
+    if (!rc) rc = tc32_prepare(c, true);
+    return rc;
 }
 
 // ------------------------------------------------------------------ QMR --
@@ -566,6 +593,23 @@ int scalit_pist_residuals(scalit_ctx *c, const scalit_pist_params *p, const doub
     cudaFreeAsync(dx, c->stream);
     cudaStreamSynchronize(c->stream);
     return rc;
+}
+
+// ------------------------------------------------ shifts and batches ---
+int scalit_qmr_shifts_device(scalit_ctx *c, int nrhs, const double *shifts, int ntype, int qmrmax, double qmrtol,
+                             int precision, const double *dB, double *dX, int *codes, double *res)
+{
+    CTX_CHECK(c);
+    return shifted_qmr(c, nrhs, shifts, ntype, qmrmax, qmrtol, precision, dB, dX, codes, res);
+}
+
+int scalit_qmr_shifts_batch(scalit_ctx *const *ctxs, int nprob, int nrhs, const double *shifts, int ntype,
+                            int qmrmax, double qmrtol, int precision, const double *const *dB, double *const *dX,
+                            int *codes, double *res, double *seconds)
+{
+    if (!ctxs || nprob < 1) { set_error("empty batch"); return SCALIT_EINVAL; }
+    CTX_CHECK(ctxs[0]);
+    return batch_qmr(ctxs, nprob, nrhs, shifts, ntype, qmrmax, qmrtol, precision, dB, dX, codes, res, seconds);
 }
 
 // ------------------------------------------------------ differentiation --

@@ -136,7 +136,7 @@ gemm_kernel(GemmArgs<T> g)
             if (n >= g.N) continue;
             const i64 p = moff + (i64)n * g.c_sn;
             T v = sc * acc[i][j];
-            if (g.diagV) v = fma(g.alpha * (g.diagV[p] - g.shift), g.diagX[p + (i64)z * g.dx_sz], v);
+            if (g.diagV) v = fma(g.alpha * (g.diagV[p] - (g.shiftv ? g.shiftv[z] : g.shift)), g.diagX[p + (i64)z * g.dx_sz], v);
             if (g.accumulate) v += Cp[p];
             Cp[p] = v;
         }
@@ -158,6 +158,9 @@ template <class T> int launch_gemm(const GemmArgs<T> &g, cudaStream_t s)
     using Small = typename Tiles<T>::Small;
     if (g.M <= 0 || g.N <= 0 || g.batch <= 0) return 0;
     if (g.batch > 65535) { set_error("gemm batch %d too large", g.batch); return SCALIT_EINVAL; }
+    if (g.tile == 0) return launch_tiles<T, Big>(g, s);
+    if (g.tile == 1) return launch_tiles<T, Small>(g, s);
+    // untuned: the small tile unless the big one fills the GPU three times
     const i64 big_ctas = (i64)((g.M + Big::BM - 1) / Big::BM) * ((g.N + Big::BN - 1) / Big::BN) * g.batch;
     if (big_ctas < 3 * 2 * 152) return launch_tiles<T, Small>(g, s);
     return launch_tiles<T, Big>(g, s);
@@ -190,7 +193,7 @@ __global__ void h3x_kernel(int nin, int nout, const T *__restrict__ Am, const T 
 template <class T>
 int level_apply(const scalit_ctx *c, int l, const T *H0, const T *DEP, const T *OUTH, const T *X,
                 T *Y, int accumulate, const T *diagV, T shift, T alpha, const int *gate,
-                cudaStream_t s, int nvec)
+                cudaStream_t s, int nvec, const T *shiftv)
 {
     const Layout &L = c->L;
     const int nout = L.n[l];
@@ -219,9 +222,11 @@ int level_apply(const scalit_ctx *c, int l, const T *H0, const T *DEP, const T *
     g.diagX = X;
     g.dx_sz = N;
     g.shift = shift;
+    g.shiftv = shiftv;
     g.gate = gate;
     g.C = Y;
     g.c_sz = N;
+    g.tile = c->tile_pick[sizeof(T) == 8 ? 0 : 1][l][nvec > 1 ? 1 : 0];
     const T *H = H0 + L.h0s[l];
     if (nin == 1) {
         // Y(i, b) = sum_j H(i, j) X(j, b): A = H (col-major), B = X.
@@ -264,7 +269,7 @@ template <> const float *pick<float>(const scalit_ctx *, const double *, const f
 
 template <class T>
 int hx_batch(const scalit_ctx *c, const T *X, T *Y, int nvec, T shift, T alpha, const int *gate,
-             cudaStream_t s)
+             cudaStream_t s, const T *shiftv)
 {
     const Layout &L = c->L;
     const T *H0 = pick<T>(c, c->H0, c->H0f);
@@ -275,6 +280,7 @@ int hx_batch(const scalit_ctx *c, const T *X, T *Y, int nvec, T shift, T alpha, 
     int first = 0;
     if (L.ndvr && L.nlev == 1) {
         const int threads = 256;
+        if (shiftv) { set_error("per-vector shifts with a single outer layer"); return SCALIT_EUNSUP; }
         for (int v = 0; v < nvec; ++v) {
             diag_kernel<T><<<(int)((L.N + threads - 1) / threads), threads, 0, s>>>(
                 L.N, RES, shift, alpha, X + (i64)v * L.N, Y + (i64)v * L.N, 0, gate);
@@ -287,13 +293,20 @@ int hx_batch(const scalit_ctx *c, const T *X, T *Y, int nvec, T shift, T alpha, 
         if constexpr (std::is_same<T, double>::value) {
             if (c->fp64_mode == SCALIT_FP64_TENSOR && tc_usable(c, l)) {
                 rc = tc_level_apply(c, l, X, Y, l > 0 || first, fuse_diag ? RES : nullptr, shift, alpha,
-                                    gate, s, nvec);
+                                    gate, s, nvec, shiftv);
+                if (rc) return rc;
+                continue;
+            }
+        } else {
+            if (tc32_usable(c, l)) {
+                rc = tc32_level_apply(c, l, X, Y, l > 0 || first, fuse_diag ? RES : nullptr, shift, alpha,
+                                      gate, s, nvec, shiftv);
                 if (rc) return rc;
                 continue;
             }
         }
         rc = level_apply<T>(c, l, H0, DEP, OUTH, X, Y, /*accumulate=*/l > 0 || first,
-                            fuse_diag ? RES : nullptr, shift, alpha, gate, s, nvec);
+                            fuse_diag ? RES : nullptr, shift, alpha, gate, s, nvec, shiftv);
         if (rc) return rc;
     }
     return 0;
@@ -305,12 +318,12 @@ int hx_vec(const scalit_ctx *c, const T *X, T *Y, T shift, T alpha, const int *g
     return hx_batch<T>(c, X, Y, 1, shift, alpha, gate, s);
 }
 
-template int hx_batch<double>(const scalit_ctx *, const double *, double *, int, double, double, const int *, cudaStream_t);
-template int hx_batch<float>(const scalit_ctx *, const float *, float *, int, float, float, const int *, cudaStream_t);
+template int hx_batch<double>(const scalit_ctx *, const double *, double *, int, double, double, const int *, cudaStream_t, const double *);
+template int hx_batch<float>(const scalit_ctx *, const float *, float *, int, float, float, const int *, cudaStream_t, const float *);
 template int hx_vec<double>(const scalit_ctx *, const double *, double *, double, double, const int *, cudaStream_t);
 template int hx_vec<float>(const scalit_ctx *, const float *, float *, float, float, const int *, cudaStream_t);
-template int level_apply<double>(const scalit_ctx *, int, const double *, const double *, const double *, const double *, double *, int, const double *, double, double, const int *, cudaStream_t, int);
-template int level_apply<float>(const scalit_ctx *, int, const float *, const float *, const float *, const float *, float *, int, const float *, float, float, const int *, cudaStream_t, int);
+template int level_apply<double>(const scalit_ctx *, int, const double *, const double *, const double *, const double *, double *, int, const double *, double, double, const int *, cudaStream_t, int, const double *);
+template int level_apply<float>(const scalit_ctx *, int, const float *, const float *, const float *, const float *, float *, int, const float *, float, float, const int *, cudaStream_t, int, const float *);
 
 // ------------------------------------------------------------------------
 // VX / VTX (src/iterate/libiterate/hpx/hpx.f90:40-73) out of place:
@@ -344,6 +357,66 @@ int level_rotate(int nin, int nout, int blk, const T *V, const T *X, T *Y, int t
 }
 
 template int level_rotate<double>(int, int, int, const double *, const double *, double *, int, const int *, cudaStream_t);
+// Tile autotuner: for every level, both precisions of the CUDA-core GEMM and
+// one or many vectors, time the big and the small tile on the level's own
+// shapes (two launches each after one warm-up, CUDA events) and keep the
+// faster.  Scratch comes from the context's workspace.
+template <class T>
+static int tune_one(scalit_ctx *c, int l, int nvec, T *X, T *Y, cudaEvent_t e0, cudaEvent_t e1)
+{
+    const T *H0 = (sizeof(T) == 8) ? (const T *)c->H0 : (const T *)c->H0f;
+    const T *DEP = (sizeof(T) == 8) ? (const T *)c->DEP : (const T *)c->DEPf;
+    const T *OUTH = (sizeof(T) == 8) ? (const T *)c->OUTH : (const T *)c->OUTHf;
+    cudaStream_t s = c->stream;
+    float best = 0.f;
+    int pick = -1;
+    for (int tile = 0; tile < 2; ++tile) {
+        c->tile_pick[sizeof(T) == 8 ? 0 : 1][l][nvec > 1 ? 1 : 0] = (signed char)tile;
+        int rc = level_apply<T>(c, l, H0, DEP, OUTH, X, Y, 0, nullptr, T(0), T(1), nullptr, s, nvec);
+        if (rc) return rc;
+        SC_CUDA(cudaEventRecord(e0, s));
+        for (int r = 0; r < 2 && !rc; ++r)
+            rc = level_apply<T>(c, l, H0, DEP, OUTH, X, Y, 0, nullptr, T(0), T(1), nullptr, s, nvec);
+        if (rc) return rc;
+        SC_CUDA(cudaEventRecord(e1, s));
+        SC_CUDA(cudaEventSynchronize(e1));
+        float ms = 0.f;
+        SC_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+        if (pick < 0 || ms < best) { best = ms; pick = tile; }
+    }
+    c->tile_pick[sizeof(T) == 8 ? 0 : 1][l][nvec > 1 ? 1 : 0] = (signed char)pick;
+    return 0;
+}
+
+int gemm_autotune(scalit_ctx *c, int nvec_many)
+{
+    const Layout &L = c->L;
+    const i64 N = L.N;
+    if (nvec_many < 2) nvec_many = 2;
+    void *w = nullptr;
+    int rc = work_get(c, sizeof(double) * 2 * (size_t)N * nvec_many, &w);
+    if (rc) return rc;
+    SC_CUDA(cudaMemsetAsync(w, 0, sizeof(double) * 2 * (size_t)N * nvec_many, c->stream));
+    cudaEvent_t e0, e1;
+    SC_CUDA(cudaEventCreate(&e0));
+    SC_CUDA(cudaEventCreate(&e1));
+    for (int l = 0; l < L.nlev && !rc; ++l) {
+        if (L.ndvr && l == L.nlev - 1) continue;
+        for (int many = 0; many < 2 && !rc; ++many) {
+            const int nv = many ? nvec_many : 1;
+            double *X64 = reinterpret_cast<double *>(w), *Y64 = X64 + (size_t)N * nv;
+            float *X32 = reinterpret_cast<float *>(w), *Y32 = X32 + (size_t)N * nv;
+            // the FP64 CUDA-core GEMM serves single vectors in the bit-reproducible mode
+            if (!many) rc = tune_one<double>(c, l, nv, X64, Y64, e0, e1);
+            if (!rc) rc = tune_one<float>(c, l, nv, X32, Y32, e0, e1);
+        }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    return rc;
+}
+
+
 template int level_rotate<float>(int, int, int, const float *, const float *, float *, int, const int *, cudaStream_t);
 
 }  // namespace sc

@@ -85,6 +85,10 @@ struct scalit_ctx {
     void *cusolver = nullptr;       // cusolverDnHandle_t
     // FP64 H*X engine: SCALIT_FP64_DFMA (FP64 pipe) or SCALIT_FP64_TENSOR (digit-sliced tcgen05)
     int fp64_mode = SCALIT_FP64_TENSOR;
+    // FP32 engine: SCALIT_FP32_SIMT (CUDA cores) or SCALIT_FP32_TENSOR (split-BF16 x3)
+    int fp32_mode = SCALIT_FP32_SIMT;
+    TcLevelData tc32[SCALIT_FMAX];           // hi/lo planes of the level matrices
+    TcLevelData pxtc32[SCALIT_FMAX][2];      // of the preconditioner's rotations [VX, VTX]
     TcLevelData tc[SCALIT_FMAX];
     // digit planes of the preconditioner's rotations, levels >= 2: [level][VX, VTX]
     TcLevelData pxtc[SCALIT_FMAX][2];
@@ -93,9 +97,11 @@ struct scalit_ctx {
     // anything baked into the captured launches changes (shift, preconditioner,
     // engine, workspace), which invalidates them.
     long long gen = 0;
+    // CUDA-core GEMM tile per [FP64, FP32][level][one vector, many]: -1 untuned
+    signed char tile_pick[2][SCALIT_FMAX][2];
     // wall seconds per level of the last preconditioner build
     double build_s[8] = {0, 0, 0, 0, 0, 0, 0, 0};
-    struct QmrGraph { cudaGraphExec_t exec = nullptr; long long gen = -1; int ntype = 0; i64 n = 0; void *work = nullptr; } qg[2];
+    struct QmrGraph { cudaGraphExec_t exec = nullptr; long long gen = -1; int ntype = 0; i64 n = 0; void *work = nullptr; int nrhs = 0; } qg[2];
 };
 
 namespace sc {
@@ -124,6 +130,8 @@ template <class T> struct GemmArgs {
     const T *diagX;
     i64 dx_sz;             // batch stride of diagX
     T shift;
+    const T *shiftv = nullptr;   // per-batch shifts (batch index z), overriding shift
+    int tile = -1;               // 0: big tile, 1: small tile, -1: by the CTA count
     const int *gate;       // if non-null and *gate != 0 the kernel does nothing
 };
 
@@ -133,12 +141,12 @@ template <class T> int launch_gemm(const GemmArgs<T> &g, cudaStream_t s);
 template <class T>
 int level_apply(const scalit_ctx *c, int level, const T *H0, const T *DEP, const T *OUTH,
                 const T *X, T *Y, int accumulate, const T *diagV, T shift, T alpha,
-                const int *gate, cudaStream_t s, int nvec = 1);
+                const int *gate, cudaStream_t s, int nvec = 1, const T *shiftv = nullptr);
 
 // The whole operator on nvec vectors stored back to back (one launch per level).
 template <class T>
 int hx_batch(const scalit_ctx *c, const T *X, T *Y, int nvec, T shift, T alpha, const int *gate,
-             cudaStream_t s);
+             cudaStream_t s, const T *shiftv = nullptr);
 
 // Whole operator for one vector: Y = alpha * ((V - shift) X + sum_l H_l X).
 template <class T>
@@ -149,6 +157,10 @@ int hx_vec(const scalit_ctx *c, const T *X, T *Y, T shift, T alpha, const int *g
 template <class T>
 int px_vec(const scalit_ctx *c, int npc, const T *X, T *Y, T *tmp, T alpha, const int *gate,
            cudaStream_t s);
+// P*X of nvec vectors (stride npoints), vector v with kernel shift e0v[v] (device, TA1)
+template <class T>
+int px_multi(const scalit_ctx *c, const T *X, T *Y, T *tmp, int nvec, const double *e0v, const int *gate,
+             cudaStream_t s);
 
 // Generic per-level rotation (VX / VTX) on device arrays, out of place.
 template <class T>
@@ -161,6 +173,16 @@ int hx_adjoint(scalit_ctx *c, int ntype, const T *X, const T *Ybar, T *Xbar, T *
 int hf_gradients(scalit_ctx *c, int m, const double *psi, int np, const double *dvdp, double *grad_dev);
 
 // ------------------------------------------------------- tensor-core FP64 --
+int gemm_autotune(scalit_ctx *c, int nvec_many);
+int tc32_prepare(scalit_ctx *c, bool rotations);
+void tc32_free(scalit_ctx *c, bool levels, bool rotations);
+bool tc32_usable(const scalit_ctx *c, int level);
+bool tc32_px_usable(const scalit_ctx *c, int level);
+int tc32_level_apply(const scalit_ctx *c, int level, const float *X, float *Y, int accumulate, const float *diagV,
+                     float shift, float alpha, const int *gate, cudaStream_t s, int nvec,
+                     const float *shiftv = nullptr);
+int tc32_rot_apply(const scalit_ctx *c, int level, int transpose, const float *X, float *Y, const int *gate,
+                   cudaStream_t s, int nvec = 1);
 int tc_prepare(scalit_ctx *c);
 int tc_prepare_px(scalit_ctx *c);
 void tc_free_px(scalit_ctx *c);
@@ -170,7 +192,7 @@ int tc_rot_apply(const scalit_ctx *c, int level, int transpose, const double *X,
 bool tc_usable(const scalit_ctx *c, int level);
 int tc_level_apply(const scalit_ctx *c, int level, const double *X, double *Y, int accumulate,
                    const double *diagV, double shift, double alpha, const int *gate, cudaStream_t s,
-                   int nvec);
+                   int nvec, const double *shiftv = nullptr);
 int tc_check_error(scalit_ctx *c);
 
 // ------------------------------------------------------------- OSB build --
@@ -206,8 +228,42 @@ template <class T> struct QmrOps {
 template <class T>
 int qmr_core(scalit_ctx *c, i64 n, QmrOps<T> &ops, int ntype, int qmrmax, double qmrtol,
              const T *dB, T *dX, QmrResult *out);
+// nrhs right-hand sides in lockstep (dB, dX: n x nrhs; out[nrhs])
+template <class T>
+int qmr_core_n(scalit_ctx *c, i64 n, int nrhs, QmrOps<T> &ops, int ntype, int qmrmax, double qmrtol,
+               const T *dB, T *dX, QmrResult *out);
+struct QmrState;
+// The pieces of one solve, for callers that interleave several solves (one
+// CUDA graph over many problems): setup, one iteration's launches, results.
+template <class T> struct QmrSolve {
+    scalit_ctx *c = nullptr;
+    i64 n = 0;
+    int nrhs = 1;
+    QmrOps<T> *ops = nullptr;
+    int ntype = 0, qmrmax = 0;
+    double tol = 0.0;
+    cudaStream_t s = nullptr;
+    T *R = nullptr, *UX = nullptr, *UR = nullptr, *Q = nullptr, *S = nullptr, *V = nullptr, *Z = nullptr;
+    T *HX0 = nullptr, *Bw = nullptr, *Xw = nullptr, *Pt = nullptr;
+    QmrState *st = nullptr;
+    double *partial = nullptr;
+    int *alldone = nullptr;
+    const int *gate = nullptr;   // the flag that stops the operators (and the host loop)
+    int gr = 1, ge = 1;
+    int setup(scalit_ctx *ctx, i64 n, int nrhs, QmrOps<T> *ops, int ntype, int qmrmax, double tol,
+              const T *B, const T *X, cudaStream_t s);
+    int iteration();
+    int finish(T *X, QmrResult *out);
+};
 int qmr_run(scalit_ctx *c, int ntype, int qmrmax, double qmrtol, int precision,
             const double *dB, double *dX, QmrResult *out);
+
+// Shifted right-hand sides and batches of problems (multi.cu).
+int shifted_qmr(scalit_ctx *c, int nrhs, const double *shifts, int ntype, int qmrmax, double tol, int precision,
+                const double *dB, double *dX, int *codes, double *res);
+int batch_qmr(scalit_ctx *const *ctxs, int nprob, int nrhs, const double *shifts, int ntype, int qmrmax,
+              double tol, int precision, const double *const *dB, double *const *dX, int *codes, double *res,
+              double *seconds);
 
 // ----------------------------------------------------------------- PIST --
 struct PistOps {

@@ -248,7 +248,8 @@ jacobi_block_kernel(int bjmax, double bjtol, int blk, int mak, int ndk,
     double *red = smem;                 // 3 * 32
     double *cs = smem + 96;             // kMaxBatch
     double *sn = cs + kMaxBatch;        // kMaxBatch
-    double *H = sn + kMaxBatch;         // the block's stacked matrices, column stride ldr
+    double *abc_c = sn + kMaxBatch;     // kMaxBatch (C sums of a stacked batch)
+    double *H = abc_c + kMaxBatch;      // the block's stacked matrices, column stride ldr
     const int tid = threadIdx.x, nt = blockDim.x, lane = tid & 31, warp = tid >> 5, nw = nt >> 5;
     const int ldr = (ndk == 1) ? mak + 1 : mak;
     const int col_g = ndk * mak, col_s = ndk * ldr;     // one column of the stack: global / shared
@@ -267,25 +268,36 @@ jacobi_block_kernel(int bjmax, double bjtol, int blk, int mak, int ndk,
             for (int i = 1; i <= mak - 1; ++i) {
                 for (int a = 0; a < mak - i; a += i) {
                     const int m = min(i, mak - i - a);
-                    // angles of the batch: one warp per plane, lanes over the stack
-                    for (int t = warp; t < m; t += nw) {
-                        const int p = a + t, q = a + i + t;
-                        double sA = 0.0, sB = 0.0, sC = 0.0;
-                        for (int kk = lane; kk < ndk; kk += 32) {
-                            const double o = H[kk + ndk * (p + ldr * q)];
-                            const double d = 0.5 * H[kk + ndk * (p + ldr * p)]
-                                           - 0.5 * H[kk + ndk * (q + ldr * q)];
-                            sA = fma(o, o, sA); sB = fma(o, d, sB); sC = fma(d, d, sC);
+                    // angles of the batch: one thread per plane (the FP64 square
+                    // roots and divisions then fill whole warps); with a stack of
+                    // matrices one warp per plane first sums A, B, C over it
+                    if (ndk == 1) {
+                        for (int t = tid; t < m; t += nt) {
+                            const int p = a + t, q = a + i + t;
+                            const double o = H[p + ldr * q];
+                            const double d = 0.5 * H[p + ldr * p] - 0.5 * H[q + ldr * q];
+                            jacobi_angle(o * o, 2.0 * (o * d), d * d, cs + t, sn + t);
                         }
-                        if (ndk > 1) {
+                    } else {
+                        for (int t = warp; t < m; t += nw) {
+                            const int p = a + t, q = a + i + t;
+                            double sA = 0.0, sB = 0.0, sC = 0.0;
+                            for (int kk = lane; kk < ndk; kk += 32) {
+                                const double o = H[kk + ndk * (p + ldr * q)];
+                                const double d = 0.5 * H[kk + ndk * (p + ldr * p)]
+                                               - 0.5 * H[kk + ndk * (q + ldr * q)];
+                                sA = fma(o, o, sA); sB = fma(o, d, sB); sC = fma(d, d, sC);
+                            }
                             #pragma unroll
                             for (int o = 16; o > 0; o >>= 1) {
                                 sA += __shfl_xor_sync(0xffffffffu, sA, o);
                                 sB += __shfl_xor_sync(0xffffffffu, sB, o);
                                 sC += __shfl_xor_sync(0xffffffffu, sC, o);
                             }
+                            if (lane == 0) { cs[t] = sA; sn[t] = sB; abc_c[t] = sC; }
                         }
-                        if (lane == 0) jacobi_angle(sA, 2.0 * sB, sC, cs + t, sn + t);
+                        __syncthreads();
+                        for (int t = tid; t < m; t += nt) jacobi_angle(cs[t], 2.0 * sn[t], abc_c[t], cs + t, sn + t);
                     }
                     __syncthreads();
                     const int nh = batch_items(mak, m);
@@ -485,7 +497,7 @@ int hosbdiag_device(scalit_ctx *c, int bjmax, double bjtol, int blk, int mak, in
     double *d_bstats = nullptr;
     SC_CUDA(cudaMallocAsync(&d_bstats, sizeof(double) * 3 * (size_t)blk, s));
     int rc = 0;
-    const size_t fixed = (96 + 2 * kMaxBatch) * sizeof(double);
+    const size_t fixed = (96 + 3 * kMaxBatch) * sizeof(double);
     const size_t bytes = sizeof(double) * (size_t)ndk * mak * (ndk == 1 ? mak + 1 : mak);
     const bool per_block = (bytes + fixed <= 225 * 1024) && mak / 2 <= kMaxBatch;
     if (per_block) {
@@ -602,6 +614,7 @@ int osb_build(scalit_ctx *c, int bjmax, double bjtol, double *stats)
     if (!rc) { c->osb_built = true; c->gen++; }
     SC_CUDA(cudaStreamSynchronize(s));
     if (!rc) rc = tc_prepare_px(c);
+    if (!rc) rc = tc32_prepare(c, true);
     return rc;
 }
 

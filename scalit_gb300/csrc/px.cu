@@ -40,12 +40,13 @@ struct KernelParams {
 };
 
 // One CTA per level-1 block.  Dynamic shared memory: n*n matrix (if it fits)
-// plus two n-vectors.
+// plus two n-vectors.  nvec vectors (stride ldv) share the staged matrix; e0v
+// (may be null) gives each vector its own kernel shift.
 template <class T>
 __global__ void __launch_bounds__(256)
 px_level1_fused(int n, i64 nblk, const T *__restrict__ V, const T *__restrict__ EIG,
                 const T *__restrict__ X, T *__restrict__ Y, KernelParams kp, T alpha,
-                int v_in_smem, const int *gate)
+                int v_in_smem, const int *gate, int nvec, i64 ldv, const double *__restrict__ e0v)
 {
     if (gate && *gate) return;
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -54,37 +55,41 @@ px_level1_fused(int n, i64 nblk, const T *__restrict__ V, const T *__restrict__ 
     T *Vs = ts + n;
     const int tid = threadIdx.x, nt = blockDim.x;
     const int lane = tid & 31, warp = tid >> 5, nwarp = nt >> 5;
-    const T e0 = T(kp.e0), de = T(fabs(kp.de)), rde = T(1.0 / fabs(kp.de));
+    const T de = T(fabs(kp.de)), rde = T(1.0 / fabs(kp.de));
     const T beta_d = T(1.0 + kp.beta), alpha_d = T(-kp.beta * fabs(kp.de));
 
     for (i64 b = blockIdx.x; b < nblk; b += gridDim.x) {
         const T *Vb = V + b * (i64)n * n;
-        const T *xb = X + b * (i64)n;
-        __syncthreads();
-        for (int i = tid; i < n; i += nt) xs[i] = xb[i];
         const T *Vsrc = Vb;
+        __syncthreads();
         if (v_in_smem) {
             const i64 nn = (i64)n * n;
             for (i64 e = tid; e < nn; e += nt) Vs[e] = Vb[e];
             Vsrc = Vs;
         }
-        __syncthreads();
-        // t = V^T x: column i of V is contiguous; one warp per column.
-        for (int i = warp; i < n; i += nwarp) {
-            const T *col = Vsrc + (i64)i * n;
-            T acc = T(0);
-            for (int j = lane; j < n; j += 32) acc = fma(col[j], xs[j], acc);
-            #pragma unroll
-            for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
-            if (lane == 0)
-                ts[i] = kernel_div<T>(acc, EIG[b * (i64)n + i], e0, kp.kind, de, rde, alpha_d, beta_d);
-        }
-        __syncthreads();
-        // y = V t: one thread per row, consecutive rows are consecutive addresses.
-        for (int i = tid; i < n; i += nt) {
-            T acc = T(0);
-            for (int j = 0; j < n; ++j) acc = fma(Vsrc[i + (i64)j * n], ts[j], acc);
-            Y[b * (i64)n + i] = alpha * acc;
+        for (int v = 0; v < nvec; ++v) {
+            const T e0 = T(e0v ? e0v[v] : kp.e0);
+            const T *xb = X + (i64)v * ldv + b * (i64)n;
+            __syncthreads();
+            for (int i = tid; i < n; i += nt) xs[i] = xb[i];
+            __syncthreads();
+            // t = V^T x: column i of V is contiguous; one warp per column.
+            for (int i = warp; i < n; i += nwarp) {
+                const T *col = Vsrc + (i64)i * n;
+                T acc = T(0);
+                for (int j = lane; j < n; j += 32) acc = fma(col[j], xs[j], acc);
+                #pragma unroll
+                for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+                if (lane == 0)
+                    ts[i] = kernel_div<T>(acc, EIG[b * (i64)n + i], e0, kp.kind, de, rde, alpha_d, beta_d);
+            }
+            __syncthreads();
+            // y = V t: one thread per row, consecutive rows are consecutive addresses.
+            for (int i = tid; i < n; i += nt) {
+                T acc = T(0);
+                for (int j = 0; j < n; ++j) acc = fma(Vsrc[i + (i64)j * n], ts[j], acc);
+                Y[(i64)v * ldv + b * (i64)n + i] = alpha * acc;
+            }
         }
     }
 }
@@ -150,7 +155,9 @@ px_level1_stream(int n, i64 nblk, const T *__restrict__ V, const T *__restrict__
     i64 k = 0;
     for (; k < kblocks; ++k) {
         const i64 b = blockIdx.x + k * (i64)gridDim.x;
-        // phase 1: t = K^-1 V^T x
+        // phase 1: t = K^-1 V^T x.  One warp per column, lanes over rows; two
+        // shuffle levels leave 8 partial dots per column in part[], summed and
+        // divided by the kernel below with one thread per column.
         for (int c = 0; c < nc; ++c) {
             const i64 g = k * nc + c;
             if (!mbar_wait(&mbar[g % ring], (uint32_t)((g / ring) & 1))) { abort_flag = 1; break; }
@@ -164,14 +171,19 @@ px_level1_stream(int n, i64 nblk, const T *__restrict__ V, const T *__restrict__
                     const int row = lane + 32 * r;
                     if (row < n) acc = fma(col[row], xs[row], acc);
                 }
-                #pragma unroll
-                for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
-                if (lane == 0)
-                    ts[c0 + j] = kernel_div<T>(acc, es[c0 + j], e0, kp.kind, de, rde, alpha_d, beta_d);
+                acc += __shfl_xor_sync(0xffffffffu, acc, 16);
+                acc += __shfl_xor_sync(0xffffffffu, acc, 8);
+                if (lane < 8) part[(c0 + j) * 8 + lane] = acc;
             }
         }
         __syncthreads();
         if (abort_flag) break;
+        for (int i = tid; i < n; i += kStreamThreads) {
+            const T *pp = part + i * 8;
+            const T d = ((pp[0] + pp[1]) + (pp[2] + pp[3])) + ((pp[4] + pp[5]) + (pp[6] + pp[7]));
+            ts[i] = kernel_div<T>(d, es[i], e0, kp.kind, de, rde, alpha_d, beta_d);
+        }
+        __syncthreads();
         // phase 2: y = V t, releasing the slots in order; meanwhile the next
         // block's X and EIG0 are on their way into registers
         const bool more = k + 1 < kblocks && tid < n;
@@ -285,7 +297,8 @@ static constexpr size_t kMaxDynSmem = 220 * 1024;
 
 template <class T, int RPL>
 static int launch_px1_stream(int n, i64 nblk, const T *V, const T *EIG, const T *X, T *Y, KernelParams kp,
-                             T alpha, int nc, int ring, size_t smem, const int *gate, int *err, cudaStream_t s)
+                             T alpha, int nc, int ring, size_t smem, int per_sm, const int *gate, int *err,
+                             cudaStream_t s)
 {
     static int configured = -1;
     int dev = 0;
@@ -295,7 +308,7 @@ static int launch_px1_stream(int n, i64 nblk, const T *V, const T *EIG, const T 
                                      (int)kMaxDynSmem));
         configured = dev;
     }
-    const int grid = (int)std::min<i64>(nblk, 152);
+    const int grid = (int)std::min<i64>(nblk, 152 * per_sm);
     px_level1_stream<T, RPL><<<grid, kStreamThreads, smem, s>>>(n, nblk, V, EIG, X, Y, kp, alpha, nc, ring,
                                                                 gate, err);
     SC_CHECK_LAUNCH();
@@ -310,20 +323,26 @@ static int launch_px1(int n, i64 nblk, const T *V, const T *EIG, const T *X, T *
     const size_t chunk = sizeof(T) * (size_t)kChunkCols * n;
     const int nc = (n + kChunkCols - 1) / kChunkCols;
     const size_t fixed = sizeof(T) * (size_t)n * (3 + kStreamThreads / 32) + 256 + 64 * 8;
-    const int ring = (int)std::min<size_t>((kMaxDynSmem - fixed) / chunk, (size_t)3 * nc);
+    // two CTAs per SM when a ring of one block fits in half the shared memory
+    // (one CTA's barriers then overlap the other's copies), else one CTA with
+    // the deepest ring that fits
+    const size_t half = 113 * 1024;
+    const int ring2 = (half > fixed) ? (int)std::min<size_t>((half - fixed) / chunk, (size_t)nc) : 0;
+    const int per_sm = (ring2 >= nc) ? 2 : 1;
+    const int ring = (per_sm == 2) ? ring2 : (int)std::min<size_t>((kMaxDynSmem - fixed) / chunk, (size_t)3 * nc);
     const bool aligned = ((reinterpret_cast<uintptr_t>(V) & 15) == 0) && ((sizeof(T) * (size_t)n * n) % 16 == 0);
     if (n <= 256 && ring >= nc && nblk >= 1 && aligned) {
         const size_t smem = (((size_t)ring * 8 + 127) & ~(size_t)127) + (size_t)ring * chunk +
                             sizeof(T) * (size_t)n * (3 + kStreamThreads / 32);
         switch ((n + 31) / 32) {
-        case 1: return launch_px1_stream<T, 1>(n, nblk, V, EIG, X, Y, kp, alpha, nc, ring, smem, gate, err, s);
-        case 2: return launch_px1_stream<T, 2>(n, nblk, V, EIG, X, Y, kp, alpha, nc, ring, smem, gate, err, s);
-        case 3: return launch_px1_stream<T, 3>(n, nblk, V, EIG, X, Y, kp, alpha, nc, ring, smem, gate, err, s);
-        case 4: return launch_px1_stream<T, 4>(n, nblk, V, EIG, X, Y, kp, alpha, nc, ring, smem, gate, err, s);
-        case 5: return launch_px1_stream<T, 5>(n, nblk, V, EIG, X, Y, kp, alpha, nc, ring, smem, gate, err, s);
-        case 6: return launch_px1_stream<T, 6>(n, nblk, V, EIG, X, Y, kp, alpha, nc, ring, smem, gate, err, s);
-        case 7: return launch_px1_stream<T, 7>(n, nblk, V, EIG, X, Y, kp, alpha, nc, ring, smem, gate, err, s);
-        default: return launch_px1_stream<T, 8>(n, nblk, V, EIG, X, Y, kp, alpha, nc, ring, smem, gate, err, s);
+        case 1: return launch_px1_stream<T, 1>(n, nblk, V, EIG, X, Y, kp, alpha, nc, ring, smem, per_sm, gate, err, s);
+        case 2: return launch_px1_stream<T, 2>(n, nblk, V, EIG, X, Y, kp, alpha, nc, ring, smem, per_sm, gate, err, s);
+        case 3: return launch_px1_stream<T, 3>(n, nblk, V, EIG, X, Y, kp, alpha, nc, ring, smem, per_sm, gate, err, s);
+        case 4: return launch_px1_stream<T, 4>(n, nblk, V, EIG, X, Y, kp, alpha, nc, ring, smem, per_sm, gate, err, s);
+        case 5: return launch_px1_stream<T, 5>(n, nblk, V, EIG, X, Y, kp, alpha, nc, ring, smem, per_sm, gate, err, s);
+        case 6: return launch_px1_stream<T, 6>(n, nblk, V, EIG, X, Y, kp, alpha, nc, ring, smem, per_sm, gate, err, s);
+        case 7: return launch_px1_stream<T, 7>(n, nblk, V, EIG, X, Y, kp, alpha, nc, ring, smem, per_sm, gate, err, s);
+        default: return launch_px1_stream<T, 8>(n, nblk, V, EIG, X, Y, kp, alpha, nc, ring, smem, per_sm, gate, err, s);
         }
     }
     const size_t vec = sizeof(T) * 2 * (size_t)n;
@@ -338,7 +357,8 @@ static int launch_px1(int n, i64 nblk, const T *V, const T *EIG, const T *X, T *
                                      (int)kMaxDynSmem));
         configured = dev;
     }
-    px_level1_fused<T><<<grid_for(nblk), 256, sm, s>>>(n, nblk, V, EIG, X, Y, kp, alpha, v_in_smem, gate);
+    px_level1_fused<T><<<grid_for(nblk), 256, sm, s>>>(n, nblk, V, EIG, X, Y, kp, alpha, v_in_smem, gate, 1, 0,
+                                                       nullptr);
     SC_CHECK_LAUNCH();
     return 0;
 }
@@ -356,6 +376,8 @@ static int rotate(const scalit_ctx *c, int l, int transpose, const T *V, const T
     const Layout &L = c->L;
     if constexpr (std::is_same<T, double>::value) {
         if (tc_px_usable(c, l)) return tc_rot_apply(c, l, transpose, in, out, gate, s);
+    } else {
+        if (tc32_px_usable(c, l)) return tc32_rot_apply(c, l, transpose, in, out, gate, s, 1);
     }
     return level_rotate<T>((int)L.dim[l], L.n[l], (int)L.blk[l], V + L.vs[l], in, out, transpose, gate, s);
 }
@@ -399,6 +421,92 @@ int px_vec(const scalit_ctx *c, int npc, const T *X, T *Y, T *tmp, T alpha, cons
 }
 
 template int px_vec<double>(const scalit_ctx *, int, const double *, double *, double *, double, const int *, cudaStream_t);
+// P*X of nvec vectors (stride N) at once, vector v with its own kernel shift
+// e0v[v] (device): the level-1 matrices are staged once per block for all the
+// vectors, and the outer rotations fold the vectors into the GEMM rows.
+template <class T>
+int px_multi(const scalit_ctx *c, const T *X, T *Y, T *tmp, int nvec, const double *e0v, const int *gate,
+             cudaStream_t s)
+{
+    const Layout &L = c->L;
+    if (!c->osb_built) { set_error("P*X before the preconditioner was built or loaded"); return SCALIT_ESTATE; }
+    if (nvec < 1) return 0;
+    const T *V = pickp<T>(c->VOSB, c->VOSBf);
+    const T *EIG = pickp<T>(c->EIG0, c->EIG0f);
+    KernelParams kp{c->osb_kind, c->E0, c->osb_de, c->osb_beta};
+    const i64 N = L.N;
+    const int S = 2 * L.nlev - 1;
+    T *buf[2] = {Y, tmp};
+    const T *in = X;
+    int stage = 0, rc;
+    auto rot = [&](int l, int transpose, const T *a, T *o) -> int {
+        const i64 nin = L.dim[l];
+        const int nout = L.n[l];
+        if constexpr (std::is_same<T, double>::value) {
+            if (tc_px_usable(c, l)) {
+                for (int v = 0; v < nvec; ++v) {
+                    int r = tc_rot_apply(c, l, transpose, a + (i64)v * N, o + (i64)v * N, gate, s);
+                    if (r) return r;
+                }
+                return 0;
+            }
+        } else {
+            if (tc32_px_usable(c, l)) return tc32_rot_apply(c, l, transpose, a, o, gate, s, nvec);
+        }
+        if (nin * nvec > 2147483647LL) { set_error("level %d too large for %d vectors", l + 1, nvec); return SCALIT_EINVAL; }
+        GemmArgs<T> g{};
+        g.K = nout; g.accumulate = 0; g.alpha = T(1); g.gate = gate;
+        g.rowscale = nullptr; g.diagV = nullptr;
+        g.M = (int)(nin * nvec); g.N = nout; g.batch = (int)L.blk[l];
+        g.Mi = nin; g.s1 = 1; g.s2 = N;              // row m: a = m % nin of vector m / nin
+        g.A = a; g.a_sk = nin; g.a_sz = nin * nout;
+        g.B = V + L.vs[l]; g.b_sz = (i64)nout * nout;
+        if (!transpose) { g.b_sk = nout; g.b_sn = 1; }
+        else { g.b_sk = 1; g.b_sn = nout; }
+        g.C = o; g.c_sn = nin; g.c_sz = nin * nout;
+        return launch_gemm<T>(g, s);
+    };
+    for (int l = L.nlev - 1; l >= 1; --l) {
+        ++stage;
+        T *out = buf[(S - stage) % 2];
+        rc = rot(l, 1, in, out);
+        if (rc) return rc;
+        in = out;
+    }
+    ++stage;
+    {
+        T *out = buf[(S - stage) % 2];
+        const int n = L.n[0];
+        const size_t vec = sizeof(T) * 2 * (size_t)n;
+        const size_t mat = sizeof(T) * (size_t)n * n;
+        const int v_in_smem = (vec + mat <= kMaxDynSmem) ? 1 : 0;
+        const size_t sm = vec + (v_in_smem ? mat : 0);
+        static int configured = -1;
+        int dev = 0;
+        cudaGetDevice(&dev);
+        if (configured != dev) {
+            SC_CUDA(cudaFuncSetAttribute(px_level1_fused<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)kMaxDynSmem));
+            configured = dev;
+        }
+        px_level1_fused<T><<<grid_for(L.blk[0]), 256, sm, s>>>(n, L.blk[0], V + L.vs[0], EIG, in, out, kp, T(1),
+                                                               v_in_smem, gate, nvec, N, e0v);
+        SC_CHECK_LAUNCH();
+        in = out;
+    }
+    for (int l = 1; l < L.nlev; ++l) {
+        ++stage;
+        T *out = buf[(S - stage) % 2];
+        rc = rot(l, 0, in, out);
+        if (rc) return rc;
+        in = out;
+    }
+    return 0;
+}
+
+template int px_multi<double>(const scalit_ctx *, const double *, double *, double *, int, const double *, const int *, cudaStream_t);
+template int px_multi<float>(const scalit_ctx *, const float *, float *, float *, int, const double *, const int *, cudaStream_t);
+
 template int px_vec<float>(const scalit_ctx *, int, const float *, float *, float *, float, const int *, cudaStream_t);
 
 }  // namespace sc

@@ -12,11 +12,14 @@
 #include "internal.cuh"
 
 #include <cmath>
+#include <vector>
 
 namespace sc {
 
 static constexpr int kRedThreads = 256;
 static constexpr int kRedMaxBlocks = 152 * 4;
+// per right-hand side: room for 4 partial sums of every CTA of a reduction
+static constexpr i64 kPartStride = 4 * kRedMaxBlocks;
 
 struct QmrState {
     double BNRM, ZNRM, VNRM, VNRMPO, ZVRAT, QSDOT, VZDOT, BETA, ETA;
@@ -92,8 +95,9 @@ __device__ __forceinline__ bool block_reduce_store(double (&acc)[NV], double *pa
 // step A: V /= VNRM, Z /= ZNRM, VZDOT = V.Z
 template <class T>
 __global__ void __launch_bounds__(kRedThreads)
-qmr_step_a(i64 n, T *V, T *Z, QmrState *st, double *partial)
+qmr_step_a(i64 n, i64 ld, T *V, T *Z, QmrState *st, double *partial)
 {
+    { const int y = blockIdx.y; V += y * ld; Z += y * ld; st += y; partial += y * kPartStride; }
     if (st->done) return;
     const double vn = st->VNRM, zn = st->ZNRM;
     if (vn == 0.0 || zn == 0.0) {
@@ -122,8 +126,9 @@ qmr_step_a(i64 n, T *V, T *Z, QmrState *st, double *partial)
 
 // step B: Q = Z (i == 1) or Z - fq Q
 template <class T>
-__global__ void qmr_step_b(i64 n, const T *Z, T *Q, const QmrState *st)
+__global__ void qmr_step_b(i64 n, i64 ld, const T *Z, T *Q, const QmrState *st)
 {
+    { const int y = blockIdx.y; Z += y * ld; Q += y * ld; st += y; }
     if (st->done) return;
     const bool first = (st->i == 1);
     const T f = T(st->fq);
@@ -134,8 +139,9 @@ __global__ void qmr_step_b(i64 n, const T *Z, T *Q, const QmrState *st)
 // step C: S = ZVRAT S, QSDOT = Q.S, BETA = QSDOT / VZDOT
 template <class T>
 __global__ void __launch_bounds__(kRedThreads)
-qmr_step_c(i64 n, const T *Q, T *S, QmrState *st, double *partial)
+qmr_step_c(i64 n, i64 ld, const T *Q, T *S, QmrState *st, double *partial)
 {
+    { const int y = blockIdx.y; Q += y * ld; S += y * ld; st += y; partial += y * kPartStride; }
     if (st->done) return;
     const T zv = T(st->ZVRAT);
     double acc[1] = {0.0};
@@ -158,8 +164,9 @@ qmr_step_c(i64 n, const T *Q, T *S, QmrState *st, double *partial)
 // step D: V = S - BETA V, VNRMPO = |V|
 template <class T>
 __global__ void __launch_bounds__(kRedThreads)
-qmr_step_d(i64 n, const T *S, T *V, QmrState *st, double *partial)
+qmr_step_d(i64 n, i64 ld, const T *S, T *V, QmrState *st, double *partial)
 {
+    { const int y = blockIdx.y; S += y * ld; V += y * ld; st += y; partial += y * kPartStride; }
     if (st->done) return;
     const T beta = T(st->BETA);
     double acc[1] = {0.0};
@@ -180,8 +187,9 @@ qmr_step_d(i64 n, const T *S, T *V, QmrState *st, double *partial)
 // step E: Z = Z / ZVRAT, ZNRM = |Z|, then THETA, GAMA, ETA and the X/R update coefficients
 template <class T>
 __global__ void __launch_bounds__(kRedThreads)
-qmr_step_e(i64 n, T *Z, QmrState *st, double *partial)
+qmr_step_e(i64 n, i64 ld, T *Z, QmrState *st, double *partial)
 {
+    { const int y = blockIdx.y; Z += y * ld; st += y; partial += y * kPartStride; }
     if (st->done) return;
     const T zv = T(st->ZVRAT);
     double acc[1] = {0.0};
@@ -227,8 +235,13 @@ __device__ void qmr_advance(QmrState *st)
 // step F: UX, UR, X, R updates; for ntype != +-1 also the convergence test.
 template <class T>
 __global__ void __launch_bounds__(kRedThreads)
-qmr_step_f(i64 n, const T *Q, const T *S, T *UX, T *UR, T *X, T *R, QmrState *st, double *partial)
+qmr_step_f(i64 n, i64 ld, const T *Q, const T *S, T *UX, T *UR, T *X, T *R, QmrState *st, double *partial)
 {
+    {
+        const int y = blockIdx.y;
+        Q += y * ld; S += y * ld; UX += y * ld; UR += y * ld; X += y * ld; R += y * ld;
+        st += y; partial += y * kPartStride;
+    }
     if (st->done) return;
     const bool first = (st->i == 1);
     const T cq = T(st->cq), cs = T(st->cs), g = T(st->g);
@@ -266,8 +279,9 @@ qmr_step_f(i64 n, const T *Q, const T *S, T *UX, T *UR, T *X, T *R, QmrState *st
 // step G: XNRM = |HX0|, RES = |HX0 - B| / XNRM (HX0 = H X), then advance.
 template <class T>
 __global__ void __launch_bounds__(kRedThreads)
-qmr_step_g(i64 n, const T *HX0, const T *B, QmrState *st, double *partial)
+qmr_step_g(i64 n, i64 ld, const T *HX0, const T *B, QmrState *st, double *partial)
 {
+    { const int y = blockIdx.y; HX0 += y * ld; B += y * ld; st += y; partial += y * kPartStride; }
     if (st->done) return;
     double acc[2] = {0.0, 0.0};
     for (i64 k = blockIdx.x * (i64)blockDim.x + threadIdx.x; k < n; k += (i64)gridDim.x * blockDim.x) {
@@ -290,8 +304,9 @@ qmr_step_g(i64 n, const T *HX0, const T *B, QmrState *st, double *partial)
 // initial norms: BNRM = VNRM = |B|, ZNRM = |Z|
 template <class T>
 __global__ void __launch_bounds__(kRedThreads)
-qmr_init_norms(i64 n, const T *B, const T *Z, QmrState *st, double *partial)
+qmr_init_norms(i64 n, i64 ld, const T *B, const T *Z, QmrState *st, double *partial)
 {
+    { const int y = blockIdx.y; B += y * ld; Z += y * ld; st += y; partial += y * kPartStride; }
     double acc[2] = {0.0, 0.0};
     for (i64 k = blockIdx.x * (i64)blockDim.x + threadIdx.x; k < n; k += (i64)gridDim.x * blockDim.x) {
         acc[0] += (double)B[k] * (double)B[k];
@@ -307,6 +322,15 @@ qmr_init_norms(i64 n, const T *B, const T *Z, QmrState *st, double *partial)
         st->ZNRM = sqrt(d[1]);
         if (st->qmrmax < 1) st->done = 1;
     }
+}
+
+// all = 1 when every right-hand side's recurrence has stopped
+__global__ void qmr_all_done(const QmrState *st, int nrhs, int *all)
+{
+    int d = 1;
+    for (int v = threadIdx.x; v < nrhs; v += blockDim.x) d &= st[v].done ? 1 : 0;
+    d = __all_sync(0xffffffffu, d);
+    if (threadIdx.x == 0) *all = d;
 }
 
 template <class T>
@@ -420,21 +444,39 @@ template int dot_dev<double>(scalit_ctx *, i64, const double *, const double *, 
 template int dot_dev<float>(scalit_ctx *, i64, const float *, const float *, double *, cudaStream_t);
 
 // ------------------------------------------------------------------ driver --
+// One QMR solve of nrhs right-hand sides (B, X: n x nrhs, column v at v n)
+// advancing in lockstep: every vector kernel runs over all of them
+// (blockIdx.y = v), each with its own scalar state, and the operators are
+// applied to the whole block at once.  A right-hand side whose recurrence
+// stopped is skipped by the vector kernels; the operators stop when all have.
 template <class T>
-int qmr_core(scalit_ctx *c, i64 n, QmrOps<T> &ops, int ntype, int qmrmax, double qmrtol,
-             const T *B, T *X, QmrResult *out)
+int QmrSolve<T>::setup(scalit_ctx *ctx, i64 n_, int nrhs_, QmrOps<T> *ops_, int ntype_, int qmrmax_,
+                       double tol_, const T *B, const T *X, cudaStream_t stream)
 {
-    cudaStream_t s = c->stream;
-    // vectors: R UX UR Q S V Z HX0, the right-hand side and solution copies,
-    // the preconditioner's scratch, then the scalar state
-    T *w = nullptr;
-    const size_t need = sizeof(T) * (size_t)n * 11 + sizeof(QmrState) + 64;
+    c = ctx; n = n_; nrhs = nrhs_; ops = ops_; ntype = ntype_; qmrmax = qmrmax_; tol = tol_; s = stream;
+    const i64 nn = n * nrhs;
+    // vectors: R UX UR Q S V Z HX0, the right-hand sides and solution copies,
+    // the preconditioner's scratch; then the states, the partial sums and the
+    // all-stopped flag
+    const size_t vec_bytes = sizeof(T) * (size_t)nn * 11;
+    const size_t st_off = (vec_bytes + 255) & ~(size_t)255;
+    const size_t part_off = (st_off + sizeof(QmrState) * (size_t)nrhs + 255) & ~(size_t)255;
+    const size_t flag_off = part_off + sizeof(double) * (size_t)kPartStride * nrhs;
+    const size_t need = flag_off + 64;
+    unsigned char *w = nullptr;
     int rc = work_get(c, need, (void **)&w);
     if (rc) return rc;
-    T *R = w, *UX = w + n, *UR = w + 2 * n, *Q = w + 3 * n, *S = w + 4 * n, *V = w + 5 * n;
-    T *Z = w + 6 * n, *HX0 = w + 7 * n, *Bw = w + 8 * n, *Xw = w + 9 * n, *Pt = w + 10 * n;
-    QmrState *st = reinterpret_cast<QmrState *>(((uintptr_t)(w + 11 * n) + 63) & ~(uintptr_t)63);
-    ops.set_scratch(Pt);
+    T *v = reinterpret_cast<T *>(w);
+    R = v; UX = v + nn; UR = v + 2 * nn; Q = v + 3 * nn; S = v + 4 * nn; V = v + 5 * nn;
+    Z = v + 6 * nn; HX0 = v + 7 * nn; Bw = v + 8 * nn; Xw = v + 9 * nn; Pt = v + 10 * nn;
+    st = reinterpret_cast<QmrState *>(w + st_off);
+    partial = reinterpret_cast<double *>(w + part_off);
+    alldone = reinterpret_cast<int *>(w + flag_off);
+    gate = (nrhs == 1) ? &st->done : alldone;
+    gr = red_grid(n);
+    ge = ew_grid(n);
+    ops->set_scratch(Pt);
+
     QmrState h{};
     h.ZVRAT = 1.0;
     h.GAMAMO = 1.0;
@@ -442,55 +484,102 @@ int qmr_core(scalit_ctx *c, i64 n, QmrOps<T> &ops, int ntype, int qmrmax, double
     h.i = 1;
     h.qmrmax = qmrmax;
     h.ntype = ntype;
-    h.tol = qmrtol;
-    SC_CUDA(cudaMemcpyAsync(st, &h, sizeof(h), cudaMemcpyHostToDevice, s));
-    const int *gate = &st->done;
-    double *partial = c->red_partial;
-    const int gr = red_grid(n), ge = ew_grid(n);
-
-    SC_CUDA(cudaMemcpyAsync(Bw, B, sizeof(T) * (size_t)n, cudaMemcpyDeviceToDevice, s));
-    if (ntype <= 0) SC_CUDA(cudaMemsetAsync(Xw, 0, sizeof(T) * (size_t)n, s));
-    else SC_CUDA(cudaMemcpyAsync(Xw, X, sizeof(T) * (size_t)n, cudaMemcpyDeviceToDevice, s));
-    copy_kernel<T><<<ge, 256, 0, s>>>(n, Bw, R, V);
+    h.tol = tol;
+    std::vector<QmrState> hs((size_t)nrhs, h);
+    SC_CUDA(cudaMemcpyAsync(st, hs.data(), sizeof(QmrState) * (size_t)nrhs, cudaMemcpyHostToDevice, s));
+    SC_CUDA(cudaMemsetAsync(alldone, 0, sizeof(int), s));
+    SC_CUDA(cudaMemcpyAsync(Bw, B, sizeof(T) * (size_t)nn, cudaMemcpyDeviceToDevice, s));
+    if (ntype <= 0) SC_CUDA(cudaMemsetAsync(Xw, 0, sizeof(T) * (size_t)nn, s));
+    else SC_CUDA(cudaMemcpyAsync(Xw, X, sizeof(T) * (size_t)nn, cudaMemcpyDeviceToDevice, s));
+    copy_kernel<T><<<ew_grid(nn), 256, 0, s>>>(nn, Bw, R, V);
     SC_CHECK_LAUNCH();
-    rc = ops.px(Bw, Z, nullptr);
+    rc = ops->px(Bw, Z, nullptr);
     if (rc) return rc;
-    qmr_init_norms<T><<<gr, kRedThreads, 0, s>>>(n, Bw, Z, st, partial);
+    qmr_init_norms<T><<<dim3(gr, nrhs), kRedThreads, 0, s>>>(n, n, Bw, Z, st, partial);
+    if (nrhs > 1) qmr_all_done<<<1, 32, 0, s>>>(st, nrhs, alldone);
     SC_CHECK_LAUNCH();
+    return 0;
+}
 
-    // one iteration; every launch is gated by st->done
-    auto iteration = [&]() -> int {
-        qmr_step_a<T><<<gr, kRedThreads, 0, s>>>(n, V, Z, st, partial);
-        qmr_step_b<T><<<ge, 256, 0, s>>>(n, Z, Q, st);
-        SC_CHECK_LAUNCH();
-        // S = (H - E0) Q; step C scales it by ZVRAT as the reference does
-        int r = ops.hx(Q, S, gate);
+// One iteration; every launch is gated by the states' done flags.
+template <class T>
+int QmrSolve<T>::iteration()
+{
+    const dim3 gR(gr, nrhs), gE(ge, nrhs);
+    qmr_step_a<T><<<gR, kRedThreads, 0, s>>>(n, n, V, Z, st, partial);
+    qmr_step_b<T><<<gE, 256, 0, s>>>(n, n, Z, Q, st);
+    SC_CHECK_LAUNCH();
+    // S = (H - E0) Q; step C scales it by ZVRAT as the reference does
+    int r = ops->hx(Q, S, gate);
+    if (r) return r;
+    qmr_step_c<T><<<gR, kRedThreads, 0, s>>>(n, n, Q, S, st, partial);
+    qmr_step_d<T><<<gR, kRedThreads, 0, s>>>(n, n, S, V, st, partial);
+    SC_CHECK_LAUNCH();
+    r = ops->px(V, Z, gate);
+    if (r) return r;
+    qmr_step_e<T><<<gR, kRedThreads, 0, s>>>(n, n, Z, st, partial);
+    qmr_step_f<T><<<gR, kRedThreads, 0, s>>>(n, n, Q, S, UX, UR, Xw, R, st, partial);
+    SC_CHECK_LAUNCH();
+    if (abs(ntype) == 1) {
+        r = ops->hx(Xw, HX0, gate);
         if (r) return r;
-        qmr_step_c<T><<<gr, kRedThreads, 0, s>>>(n, Q, S, st, partial);
-        qmr_step_d<T><<<gr, kRedThreads, 0, s>>>(n, S, V, st, partial);
+        qmr_step_g<T><<<gR, kRedThreads, 0, s>>>(n, n, HX0, Bw, st, partial);
         SC_CHECK_LAUNCH();
-        r = ops.px(V, Z, gate);
-        if (r) return r;
-        qmr_step_e<T><<<gr, kRedThreads, 0, s>>>(n, Z, st, partial);
-        qmr_step_f<T><<<gr, kRedThreads, 0, s>>>(n, Q, S, UX, UR, Xw, R, st, partial);
+    }
+    if (nrhs > 1) {
+        qmr_all_done<<<1, 32, 0, s>>>(st, nrhs, alldone);
         SC_CHECK_LAUNCH();
-        if (abs(ntype) == 1) {
-            r = ops.hx(Xw, HX0, gate);
-            if (r) return r;
-            qmr_step_g<T><<<gr, kRedThreads, 0, s>>>(n, HX0, Bw, st, partial);
-            SC_CHECK_LAUNCH();
-        }
-        return 0;
-    };
+    }
+    return 0;
+}
 
+template <class T>
+int QmrSolve<T>::finish(T *X, QmrResult *out)
+{
+    std::vector<QmrState> hs((size_t)nrhs);
+    SC_CUDA(cudaMemcpyAsync(hs.data(), st, sizeof(QmrState) * (size_t)nrhs, cudaMemcpyDeviceToHost, s));
+    SC_CUDA(cudaMemcpyAsync(X, Xw, sizeof(T) * (size_t)n * nrhs, cudaMemcpyDeviceToDevice, s));
+    SC_CUDA(cudaStreamSynchronize(s));
+    for (int v = 0; v < nrhs; ++v) {
+        out[v].code = hs[v].code;
+        out[v].res = hs[v].RES;
+        out[v].iters = hs[v].iters;
+        out[v].breakdown = hs[v].breakdown;
+    }
+    return tc_check_error(c);
+}
+
+template <class T>
+int qmr_core_n(scalit_ctx *c, i64 n, int nrhs, QmrOps<T> &ops, int ntype, int qmrmax, double qmrtol,
+               const T *B, T *X, QmrResult *out)
+{
+    cudaStream_t s = c->stream;
+    QmrSolve<T> q;
+    int rc = q.setup(c, n, nrhs, &ops, ntype, qmrmax, qmrtol, B, X, s);
+    if (rc) return rc;
     const int batch = ops.host_side() ? 1 : 4;
     // Device-side operators: the batch of iterations is captured once as a CUDA
     // graph per context and precision and replayed (all pointers live in the
-    // workspace; the launches read their scalars from the device state).
-    cudaGraphExec_t exec = nullptr;
-    if (!ops.host_side()) {
+    // workspace; the launches read their scalars from the device states).
+    cudaGraphExec_t exec = nullptr, own_exec = nullptr;
+    if (!ops.host_side() && nrhs > 1) {
+        // several right-hand sides: the operators' shift arrays belong to this
+        // call, so the graph is captured for it alone
+        cudaGraph_t graph = nullptr;
+        SC_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+        int r = 0;
+        for (int b = 0; b < batch && !r; ++b) r = q.iteration();
+        const cudaError_t ce = cudaStreamEndCapture(s, &graph);
+        if (r) { if (graph) cudaGraphDestroy(graph); return r; }
+        if (ce != cudaSuccess) return cuda_fail(ce, "cudaStreamEndCapture", __FILE__, __LINE__);
+        const cudaError_t ie = cudaGraphInstantiate(&own_exec, graph, 0);
+        cudaGraphDestroy(graph);
+        if (ie != cudaSuccess) return cuda_fail(ie, "cudaGraphInstantiate", __FILE__, __LINE__);
+        exec = own_exec;
+    } else if (!ops.host_side()) {
         scalit_ctx::QmrGraph &qg = c->qg[sizeof(T) == 8 ? 0 : 1];
-        if (qg.exec && (qg.gen != c->gen || qg.ntype != ntype || qg.n != n || qg.work != c->work)) {
+        if (qg.exec && (qg.gen != c->gen || qg.ntype != ntype || qg.n != n || qg.work != c->work ||
+                        qg.nrhs != nrhs)) {
             cudaGraphExecDestroy(qg.exec);
             qg.exec = nullptr;
         }
@@ -498,7 +587,7 @@ int qmr_core(scalit_ctx *c, i64 n, QmrOps<T> &ops, int ntype, int qmrmax, double
             cudaGraph_t graph = nullptr;
             SC_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
             int r = 0;
-            for (int b = 0; b < batch && !r; ++b) r = iteration();
+            for (int b = 0; b < batch && !r; ++b) r = q.iteration();
             const cudaError_t ce = cudaStreamEndCapture(s, &graph);
             if (r) { if (graph) cudaGraphDestroy(graph); return r; }
             if (ce != cudaSuccess) return cuda_fail(ce, "cudaStreamEndCapture", __FILE__, __LINE__);
@@ -509,37 +598,42 @@ int qmr_core(scalit_ctx *c, i64 n, QmrOps<T> &ops, int ntype, int qmrmax, double
             qg.ntype = ntype;
             qg.n = n;
             qg.work = c->work;
+            qg.nrhs = nrhs;
         }
         exec = qg.exec;
     }
 
     int it = 0;
     int *h_flag = reinterpret_cast<int *>(c->h_pinned);
-    while (true) {
+    while (rc == 0) {
         if (exec) {
-            SC_CUDA(cudaGraphLaunch(exec, s));
+            if (cudaGraphLaunch(exec, s) != cudaSuccess) { rc = cuda_fail(cudaGetLastError(), "cudaGraphLaunch", __FILE__, __LINE__); break; }
         } else {
-            for (int b = 0; b < batch; ++b) {
-                rc = iteration();
-                if (rc) return rc;
-            }
+            for (int b = 0; b < batch && !rc; ++b) rc = q.iteration();
+            if (rc) break;
         }
         it += batch;
-        SC_CUDA(cudaMemcpyAsync(h_flag, &st->done, sizeof(int), cudaMemcpyDeviceToHost, s));
-        SC_CUDA(cudaStreamSynchronize(s));
+        if (cudaMemcpyAsync(h_flag, q.gate, sizeof(int), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+            cudaStreamSynchronize(s) != cudaSuccess) { rc = cuda_fail(cudaGetLastError(), "QMR poll", __FILE__, __LINE__); break; }
         if (*h_flag) break;
-        if (it > qmrmax + batch) { set_error("QMR did not stop"); return SCALIT_ESTATE; }
+        if (it > qmrmax + batch) { set_error("QMR did not stop"); rc = SCALIT_ESTATE; }
     }
-    SC_CUDA(cudaMemcpyAsync(&h, st, sizeof(h), cudaMemcpyDeviceToHost, s));
-    SC_CUDA(cudaMemcpyAsync(X, Xw, sizeof(T) * (size_t)n, cudaMemcpyDeviceToDevice, s));
-    SC_CUDA(cudaStreamSynchronize(s));
-    out->code = h.code;
-    out->res = h.RES;
-    out->iters = h.iters;
-    out->breakdown = h.breakdown;
-    return tc_check_error(c);
+    if (own_exec) cudaGraphExecDestroy(own_exec);
+    if (rc) return rc;
+    return q.finish(X, out);
 }
 
+template <class T>
+int qmr_core(scalit_ctx *c, i64 n, QmrOps<T> &ops, int ntype, int qmrmax, double qmrtol,
+             const T *B, T *X, QmrResult *out)
+{
+    return qmr_core_n<T>(c, n, 1, ops, ntype, qmrmax, qmrtol, B, X, out);
+}
+
+template struct QmrSolve<double>;
+template struct QmrSolve<float>;
+template int qmr_core_n<double>(scalit_ctx *, i64, int, QmrOps<double> &, int, int, double, const double *, double *, QmrResult *);
+template int qmr_core_n<float>(scalit_ctx *, i64, int, QmrOps<float> &, int, int, double, const float *, float *, QmrResult *);
 template int qmr_core<double>(scalit_ctx *, i64, QmrOps<double> &, int, int, double, const double *, double *, QmrResult *);
 template int qmr_core<float>(scalit_ctx *, i64, QmrOps<float> &, int, int, double, const float *, float *, QmrResult *);
 

@@ -62,6 +62,7 @@ struct TcArgs {
     const double *diagX;
     i64 dx_sz;
     double shift;
+    const double *shiftv;   // per-vector shifts (vector index z), overriding shift
     const int *gate;
     int *err;
     const uint4 *bdig;    // [ntile][ks][digit][NT x 16 BF16, canonical]
@@ -72,63 +73,6 @@ struct TcArgs {
     i64 bdig_blk;         // uint4 stride between the blocks' digit planes
     int bexp_blk;         // int stride between the blocks' exponents
 };
-
-// Shared-memory matrix descriptor, K-major, no swizzle: start address, the
-// byte distance between core matrices along K (LBO) and along M/N (SBO).
-__device__ __forceinline__ uint64_t smem_desc(uint32_t saddr, uint32_t lbo, uint32_t sbo)
-{
-    uint64_t d = 0;
-    d |= (uint64_t)((saddr & 0x3FFFFu) >> 4);
-    d |= (uint64_t)((lbo >> 4) & 0x3FFFu) << 16;
-    d |= (uint64_t)((sbo >> 4) & 0x3FFFu) << 32;
-    d |= (uint64_t)1 << 46;   // descriptor version for tcgen05
-    return d;                 // base offset 0, relative LBO, no swizzle
-}
-
-// Instruction descriptor, kind::f16: D = F32, A = B = BF16, both K-major, M = 128.
-__host__ __device__ constexpr uint32_t idesc_bf16(int n)
-{
-    return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(n >> 3) << 17) | ((uint32_t)(kBM >> 4) << 24);
-}
-
-__device__ __forceinline__ void tc_mma(uint32_t d_tmem, uint64_t adesc, uint64_t bdesc, uint32_t idesc,
-                                       uint32_t accumulate)
-{
-    asm volatile(
-        "{\n\t.reg .pred p;\n\t"
-        "setp.ne.b32 p, %4, 0;\n\t"
-        "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}\n"
-        :: "r"(d_tmem), "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate));
-}
-
-__device__ __forceinline__ void tc_commit(uint64_t *mbar)
-{
-    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];"
-                 :: "r"(smem_addr(mbar)) : "memory");
-}
-
-__device__ __forceinline__ void fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
-__device__ __forceinline__ void fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
-
-__device__ __forceinline__ void tmem_ld4(uint32_t taddr, float (&v)[4])
-{
-    uint32_t r[4];
-    asm volatile("tcgen05.ld.sync.aligned.32x32b.x4.b32 {%0, %1, %2, %3}, [%4];"
-                 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]) : "r"(taddr));
-    #pragma unroll
-    for (int i = 0; i < 4; ++i) v[i] = __uint_as_float(r[i]);
-}
-
-__device__ __forceinline__ void tmem_ld8(uint32_t taddr, float (&v)[8])
-{
-    uint32_t r[8];
-    asm volatile(
-        "tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];"
-        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7])
-        : "r"(taddr));
-    #pragma unroll
-    for (int i = 0; i < 8; ++i) v[i] = __uint_as_float(r[i]);
-}
 
 // Binary exponent e with |x| < 2^e for x != 0 (frexp's exponent), read from the bits.
 __device__ __forceinline__ int exp_of(unsigned long long bits)
@@ -366,7 +310,8 @@ tc_level_kernel(TcArgs g)
                     val = __longlong_as_double(__double_as_longlong(val) + ((long long)bexp[n] << 52));
                 const i64 p = moff + (i64)n * g.c_sn;
                 double out = sc * val;
-                if (g.diagV) out = fma(g.alpha * (g.diagV[p] - g.shift), g.diagX[p + (i64)z * g.dx_sz], out);
+                if (g.diagV) out = fma(g.alpha * (g.diagV[p] - (g.shiftv ? g.shiftv[z] : g.shift)),
+                                       g.diagX[p + (i64)z * g.dx_sz], out);
                 if (g.accumulate) out += C[p];
                 C[p] = out;
             }
@@ -577,7 +522,7 @@ bool tc_usable(const scalit_ctx *c, int l)
 }
 
 int tc_level_apply(const scalit_ctx *c, int l, const double *X, double *Y, int accumulate, const double *diagV,
-                   double shift, double alpha, const int *gate, cudaStream_t s, int nvec)
+                   double shift, double alpha, const int *gate, cudaStream_t s, int nvec, const double *shiftv)
 {
     const Layout &L = c->L;
     const TcLevelData &t = c->tc[l];
@@ -606,6 +551,7 @@ int tc_level_apply(const scalit_ctx *c, int l, const double *X, double *Y, int a
     g.diagX = X;
     g.dx_sz = N;
     g.shift = shift;
+    g.shiftv = shiftv;
     g.gate = gate;
     g.err = c->tc_err;
     g.bdig = reinterpret_cast<const uint4 *>(t.dig);

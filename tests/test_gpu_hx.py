@@ -144,3 +144,38 @@ def test_hx_before_load_is_an_error(lib, c0):
         with pytest.raises(capi.ScalitError) as e:
             ctx.hx(np.zeros(c0.N))
         assert e.value.code == -104
+
+
+def test_tile_autotuner_picks(lib, c0):
+    """The load-time autotuner picks a tile for every level GEMM it tuned."""
+    with capi.Context.from_problem(c0, e0=0.0) as ctx:
+        t = ctx.tile_picks()
+    assert t.shape == (2, 3, 2)
+    assert set(np.unique(t[1])) <= {0, 1}            # FP32: one vector and 16
+    assert set(np.unique(t[0, :, 0])) <= {0, 1}      # FP64 CUDA-core engine: one vector
+    assert (t[0, :, 1] == -1).all()
+
+
+TOL_BF16X3 = 3e-5   # split-BF16 x3: 16 significant bits per operand, FP32 sums
+
+
+@pytest.mark.parametrize("sizes", [(24, 32, 20), (13, 7, 5), (17, 33, 9)])
+def test_hx_f32_tensor_engine(lib, orc, sizes):
+    """FP32 H*X on the tensor cores (split-BF16 x3) against the FP64 oracle,
+    several vectors with their own shifts, odd sizes (partial tiles)."""
+    torch = pytest.importorskip("torch")
+    p = hm.build_problem(hm.Grid3(*sizes), hm.PES())
+    ref = orc.Operator.from_problem(p, E0=0.0)
+    X = np.random.default_rng(11).standard_normal((3, p.N))
+    shifts = float(p.RES.min()) + np.array([0.0, 0.004, 0.011])
+    with capi.Context.from_problem(p, e0=0.0) as ctx:
+        ctx.set_fp32_mode(capi.FP32_TENSOR)
+        dx = torch.tensor(X, dtype=torch.float32, device="cuda")
+        dy = torch.empty_like(dx)
+        ctx.hx_f32_device(dx, dy, 3, capi.TA0)
+        torch.cuda.synchronize()
+        Y = dy.double().cpu().numpy()
+    for v in range(3):
+        assert rel(Y[v], ref.hx(X[v], 0)) < TOL_BF16X3
+    # shifted systems through the multi-shift QMR use per-vector shifts; checked there
+    del shifts

@@ -95,3 +95,22 @@ def test_px_f32(lib, orc):
         torch.cuda.synchronize()
         z = dz.double().cpu().numpy()
     assert rel(z, ref.px(x)) < 1e-5
+
+
+def test_px_f32_tensor_engine(lib, orc):
+    """P*X in FP32 with the outer rotations on the tensor cores (split-BF16 x3)."""
+    torch = pytest.importorskip("torch")
+    p = hm.workload("tri-24x32x20")
+    e0 = float(p.RES.min()) - 1e-3
+    ref = orc.Operator.from_problem(p, E0=e0)
+    ref.build_osb(20, 1e-4)
+    x = np.random.default_rng(5).standard_normal(p.N)
+    with capi.Context.from_problem(p, e0=e0) as ctx:
+        ctx.set_fp32_mode(capi.FP32_TENSOR)
+        ctx.build_osb(20, 1e-4)
+        dx = torch.tensor(x, dtype=torch.float32, device="cuda")
+        dz = torch.empty_like(dx)
+        ctx.px_f32_device(dx, dz)
+        torch.cuda.synchronize()
+        z = dz.double().cpu().numpy()
+    assert rel(z, ref.px(x)) < 1e-4

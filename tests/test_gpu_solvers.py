@@ -184,3 +184,21 @@ def test_pist_residuals_match_host_check(lib, orc, c0):
     host = np.array([np.linalg.norm(ref.hx(psi[k], 0) - eig[k] * psi[k]) for k in range(20)])
     np.testing.assert_allclose(info["resid"], host, rtol=1e-6, atol=1e-14)
     assert info["resid"].max() < 1e-3
+
+
+def test_pist_mixed_tensor_fp32(lib, orc, c0):
+    """The mixed path with the FP32 tensor-core engine (split-BF16 x3 H*X and
+    rotations in the inner solves): eigenvalues still equal the exact ones."""
+    import scipy.sparse.linalg as sla
+    e0 = float(c0.RES.min())
+    ref = orc.Operator.from_problem(c0, E0=e0)
+    exact = np.sort(sla.eigsh(sla.LinearOperator((c0.N, c0.N), matvec=lambda v: ref.hx(v, 0)),
+                              k=20, which="SA", tol=1e-13)[0])
+    x0 = orc.start_vector(c0.N, 0)
+    with capi.Context.from_problem(c0, e0=e0) as ctx:
+        ctx.set_fp32_mode(capi.FP32_TENSOR)
+        ctx.build_osb(20, 1e-4)
+        st, eig, res, info = ctx.pist(x0, 20, e0, 1e-11, m_max=400, qmr_max=500, qmr_tol=1e-4,
+                                      precision=capi.PREC_FP32, orth=2)
+    assert st > 0
+    assert np.abs(eig - exact).max() * hm.HARTREE_CM < CM_TOL
