@@ -7,6 +7,11 @@ vectors already resident in HBM; two input/output sets (2 x 151 MB, larger
 than the 129 MB L2) alternate between steps.  `e2e` repeats the measurement
 through the host-buffer C ABI (scalit_hx), host<->device copies included.
 
+The PIST leg (default: the 200 lowest levels of the 160 x 160 x 120 problem,
+3,072,000 points) times preconditioner build + PIST to convergence + the FP64
+residual check twice: FP64 inner solves, and the mixed path (FP32 inner solves,
+FP32 first Gram-Schmidt pass), and reports every level's difference.
+
 N > 1 (torchrun): replicas -- every rank runs the same workload on its own GPU,
 no collective on the data path; value = all ranks' applications / slowest rank.
 
@@ -44,9 +49,9 @@ def parse():
     ap.add_argument("--nvec", type=int, default=16)
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--pist-workload", default="tri-24x32x20",
+    ap.add_argument("--pist-workload", default="tri-160x160x120",
                     help="grid of the PIST leg ('none' skips it)")
-    ap.add_argument("--pist-levels", type=int, default=20)
+    ap.add_argument("--pist-levels", type=int, default=200)
     ap.add_argument("--batch-problems", type=int, default=0,
                     help="shifted-QMR leg over this many uneven problems (0 skips it)")
     ap.add_argument("--batch-shifts", type=int, default=16)

@@ -39,6 +39,7 @@ gemm_kernel(GemmArgs<T> g)
     static_assert((BM / TM) * (BN / TN) == NT, "thread grid");
 
     if (g.gate && *g.gate) return;
+    if (g.vgate && g.vgate[(i64)(blockIdx.z / g.vgate_div) * g.vgate_stride]) return;
 
     __shared__ T As[BK][BM];
     __shared__ T Bs[BK][BN];
@@ -48,7 +49,7 @@ gemm_kernel(GemmArgs<T> g)
     const int n0 = blockIdx.y * BN;
     const int z = blockIdx.z;
     const T *A = g.A + (i64)z * g.a_sz;
-    const T *B = g.B + (i64)z * g.b_sz;
+    const T *B = g.B + (i64)(g.b_mod > 0 ? z % g.b_mod : z) * g.b_sz;
     T *Cp = g.C + (i64)z * g.c_sz;
 
     // Loader mapping.  A: consecutive threads take consecutive m (coalesced
@@ -193,7 +194,7 @@ __global__ void h3x_kernel(int nin, int nout, const T *__restrict__ Am, const T 
 template <class T>
 int level_apply(const scalit_ctx *c, int l, const T *H0, const T *DEP, const T *OUTH, const T *X,
                 T *Y, int accumulate, const T *diagV, T shift, T alpha, const int *gate,
-                cudaStream_t s, int nvec, const T *shiftv)
+                cudaStream_t s, int nvec, const T *shiftv, const int *vgate, int vstride)
 {
     const Layout &L = c->L;
     const int nout = L.n[l];
@@ -227,6 +228,8 @@ int level_apply(const scalit_ctx *c, int l, const T *H0, const T *DEP, const T *
     g.C = Y;
     g.c_sz = N;
     g.tile = c->tile_pick[sizeof(T) == 8 ? 0 : 1][l][nvec > 1 ? 1 : 0];
+    g.vgate = vgate;
+    g.vgate_stride = vstride;
     const T *H = H0 + L.h0s[l];
     if (nin == 1) {
         // Y(i, b) = sum_j H(i, j) X(j, b): A = H (col-major), B = X.
@@ -269,7 +272,7 @@ template <> const float *pick<float>(const scalit_ctx *, const double *, const f
 
 template <class T>
 int hx_batch(const scalit_ctx *c, const T *X, T *Y, int nvec, T shift, T alpha, const int *gate,
-             cudaStream_t s, const T *shiftv)
+             cudaStream_t s, const T *shiftv, const int *vgate, int vstride)
 {
     const Layout &L = c->L;
     const T *H0 = pick<T>(c, c->H0, c->H0f);
@@ -293,20 +296,20 @@ int hx_batch(const scalit_ctx *c, const T *X, T *Y, int nvec, T shift, T alpha, 
         if constexpr (std::is_same<T, double>::value) {
             if (c->fp64_mode == SCALIT_FP64_TENSOR && tc_usable(c, l)) {
                 rc = tc_level_apply(c, l, X, Y, l > 0 || first, fuse_diag ? RES : nullptr, shift, alpha,
-                                    gate, s, nvec, shiftv);
+                                    gate, s, nvec, shiftv, vgate, vstride);
                 if (rc) return rc;
                 continue;
             }
         } else {
             if (tc32_usable(c, l)) {
                 rc = tc32_level_apply(c, l, X, Y, l > 0 || first, fuse_diag ? RES : nullptr, shift, alpha,
-                                      gate, s, nvec, shiftv);
+                                      gate, s, nvec, shiftv, vgate, vstride);
                 if (rc) return rc;
                 continue;
             }
         }
         rc = level_apply<T>(c, l, H0, DEP, OUTH, X, Y, /*accumulate=*/l > 0 || first,
-                            fuse_diag ? RES : nullptr, shift, alpha, gate, s, nvec, shiftv);
+                            fuse_diag ? RES : nullptr, shift, alpha, gate, s, nvec, shiftv, vgate, vstride);
         if (rc) return rc;
     }
     return 0;
@@ -318,12 +321,12 @@ int hx_vec(const scalit_ctx *c, const T *X, T *Y, T shift, T alpha, const int *g
     return hx_batch<T>(c, X, Y, 1, shift, alpha, gate, s);
 }
 
-template int hx_batch<double>(const scalit_ctx *, const double *, double *, int, double, double, const int *, cudaStream_t, const double *);
-template int hx_batch<float>(const scalit_ctx *, const float *, float *, int, float, float, const int *, cudaStream_t, const float *);
+template int hx_batch<double>(const scalit_ctx *, const double *, double *, int, double, double, const int *, cudaStream_t, const double *, const int *, int);
+template int hx_batch<float>(const scalit_ctx *, const float *, float *, int, float, float, const int *, cudaStream_t, const float *, const int *, int);
 template int hx_vec<double>(const scalit_ctx *, const double *, double *, double, double, const int *, cudaStream_t);
 template int hx_vec<float>(const scalit_ctx *, const float *, float *, float, float, const int *, cudaStream_t);
-template int level_apply<double>(const scalit_ctx *, int, const double *, const double *, const double *, const double *, double *, int, const double *, double, double, const int *, cudaStream_t, int, const double *);
-template int level_apply<float>(const scalit_ctx *, int, const float *, const float *, const float *, const float *, float *, int, const float *, float, float, const int *, cudaStream_t, int, const float *);
+template int level_apply<double>(const scalit_ctx *, int, const double *, const double *, const double *, const double *, double *, int, const double *, double, double, const int *, cudaStream_t, int, const double *, const int *, int);
+template int level_apply<float>(const scalit_ctx *, int, const float *, const float *, const float *, const float *, float *, int, const float *, float, float, const int *, cudaStream_t, int, const float *, const int *, int);
 
 // ------------------------------------------------------------------------
 // VX / VTX (src/iterate/libiterate/hpx/hpx.f90:40-73) out of place:

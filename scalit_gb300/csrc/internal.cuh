@@ -132,6 +132,10 @@ template <class T> struct GemmArgs {
     T shift;
     const T *shiftv = nullptr;   // per-batch shifts (batch index z), overriding shift
     int tile = -1;               // 0: big tile, 1: small tile, -1: by the CTA count
+    int b_mod = 0;               // > 0: B of batch z is B + (z % b_mod) b_sz
+    const int *vgate = nullptr;  // per-vector stop flags: batch z is skipped when
+    int vgate_stride = 0;        //   vgate[(z / vgate_div) * vgate_stride] != 0
+    int vgate_div = 1;
     const int *gate;       // if non-null and *gate != 0 the kernel does nothing
 };
 
@@ -141,12 +145,13 @@ template <class T> int launch_gemm(const GemmArgs<T> &g, cudaStream_t s);
 template <class T>
 int level_apply(const scalit_ctx *c, int level, const T *H0, const T *DEP, const T *OUTH,
                 const T *X, T *Y, int accumulate, const T *diagV, T shift, T alpha,
-                const int *gate, cudaStream_t s, int nvec = 1, const T *shiftv = nullptr);
+                const int *gate, cudaStream_t s, int nvec = 1, const T *shiftv = nullptr,
+                const int *vgate = nullptr, int vstride = 0);
 
 // The whole operator on nvec vectors stored back to back (one launch per level).
 template <class T>
 int hx_batch(const scalit_ctx *c, const T *X, T *Y, int nvec, T shift, T alpha, const int *gate,
-             cudaStream_t s, const T *shiftv = nullptr);
+             cudaStream_t s, const T *shiftv = nullptr, const int *vgate = nullptr, int vstride = 0);
 
 // Whole operator for one vector: Y = alpha * ((V - shift) X + sum_l H_l X).
 template <class T>
@@ -160,7 +165,7 @@ int px_vec(const scalit_ctx *c, int npc, const T *X, T *Y, T *tmp, T alpha, cons
 // P*X of nvec vectors (stride npoints), vector v with kernel shift e0v[v] (device, TA1)
 template <class T>
 int px_multi(const scalit_ctx *c, const T *X, T *Y, T *tmp, int nvec, const double *e0v, const int *gate,
-             cudaStream_t s);
+             cudaStream_t s, const int *vgate = nullptr, int vstride = 0);
 
 // Generic per-level rotation (VX / VTX) on device arrays, out of place.
 template <class T>
@@ -180,9 +185,9 @@ bool tc32_usable(const scalit_ctx *c, int level);
 bool tc32_px_usable(const scalit_ctx *c, int level);
 int tc32_level_apply(const scalit_ctx *c, int level, const float *X, float *Y, int accumulate, const float *diagV,
                      float shift, float alpha, const int *gate, cudaStream_t s, int nvec,
-                     const float *shiftv = nullptr);
+                     const float *shiftv = nullptr, const int *vgate = nullptr, int vstride = 0);
 int tc32_rot_apply(const scalit_ctx *c, int level, int transpose, const float *X, float *Y, const int *gate,
-                   cudaStream_t s, int nvec = 1);
+                   cudaStream_t s, int nvec = 1, const int *vgate = nullptr, int vstride = 0);
 int tc_prepare(scalit_ctx *c);
 int tc_prepare_px(scalit_ctx *c);
 void tc_free_px(scalit_ctx *c);
@@ -192,7 +197,7 @@ int tc_rot_apply(const scalit_ctx *c, int level, int transpose, const double *X,
 bool tc_usable(const scalit_ctx *c, int level);
 int tc_level_apply(const scalit_ctx *c, int level, const double *X, double *Y, int accumulate,
                    const double *diagV, double shift, double alpha, const int *gate, cudaStream_t s,
-                   int nvec, const double *shiftv = nullptr);
+                   int nvec, const double *shiftv = nullptr, const int *vgate = nullptr, int vstride = 0);
 int tc_check_error(scalit_ctx *c);
 
 // ------------------------------------------------------------- OSB build --
@@ -233,6 +238,8 @@ template <class T>
 int qmr_core_n(scalit_ctx *c, i64 n, int nrhs, QmrOps<T> &ops, int ntype, int qmrmax, double qmrtol,
                const T *dB, T *dX, QmrResult *out);
 struct QmrState;
+const int *qmr_done_flag(const QmrState *st);   // &st->done; state v's flag at + v * qmr_state_stride()
+int qmr_state_stride();
 // The pieces of one solve, for callers that interleave several solves (one
 // CUDA graph over many problems): setup, one iteration's launches, results.
 template <class T> struct QmrSolve {

@@ -20,15 +20,17 @@ template <class T> struct CtxMultiOps : QmrOps<T> {
     int nrhs = 1;
     const T *shiftv = nullptr;     // device, nrhs
     const double *e0v = nullptr;   // device, nrhs
+    const int *vgate = nullptr;    // the right-hand sides' stop flags (set after setup)
+    int vstride = 0;
     T *tmp = nullptr;
     void set_scratch(T *p) override { tmp = p; }
     int hx(const T *in, T *out, const int *gate) override
     {
-        return hx_batch<T>(c, in, out, nrhs, T(0), T(1), gate, c->stream, shiftv);
+        return hx_batch<T>(c, in, out, nrhs, T(0), T(1), gate, c->stream, shiftv, vgate, vstride);
     }
     int px(const T *in, T *out, const int *gate) override
     {
-        return px_multi<T>(c, in, out, tmp, nrhs, e0v, gate, c->stream);
+        return px_multi<T>(c, in, out, tmp, nrhs, e0v, gate, c->stream, vgate, vstride);
     }
 };
 
@@ -64,7 +66,11 @@ struct ShiftedJob {
         SC_CUDA(cudaStreamSynchronize(s));   // the host shifts may go away after return
         if (prec == SCALIT_PREC_FP64) {
             ops64.c = c; ops64.nrhs = nrhs; ops64.shiftv = e0v; ops64.e0v = e0v;
-            return q64.setup(c, n, nrhs, &ops64, ntype, qmrmax, tol, dB, dX, s);
+            int r = q64.setup(c, n, nrhs, &ops64, ntype, qmrmax, tol, dB, dX, s);
+            // a right-hand side that stopped costs no more operator work
+            ops64.vgate = qmr_done_flag(q64.st);
+            ops64.vstride = qmr_state_stride();
+            return r;
         }
         SC_CUDA(cudaMallocAsync(&shiftf, sizeof(float) * nrhs, s));
         shifts_to_f32_kernel<<<(nrhs + 127) / 128, 128, 0, s>>>(nrhs, e0v, shiftf);
@@ -74,7 +80,10 @@ struct ShiftedJob {
         if (!rc && ntype > 0) rc = to_f32(dX, bx + nn, nn, s);
         if (rc) return rc;
         ops32.c = c; ops32.nrhs = nrhs; ops32.shiftv = shiftf; ops32.e0v = e0v;
-        return q32.setup(c, n, nrhs, &ops32, ntype, qmrmax, tol, bx, bx + nn, s);
+        rc = q32.setup(c, n, nrhs, &ops32, ntype, qmrmax, tol, bx, bx + nn, s);
+        ops32.vgate = qmr_done_flag(q32.st);
+        ops32.vstride = qmr_state_stride();
+        return rc;
     }
     int iteration() { return precision == SCALIT_PREC_FP64 ? q64.iteration() : q32.iteration(); }
     const int *gate() const { return precision == SCALIT_PREC_FP64 ? q64.gate : q32.gate; }

@@ -46,7 +46,8 @@ template <class T>
 __global__ void __launch_bounds__(256)
 px_level1_fused(int n, i64 nblk, const T *__restrict__ V, const T *__restrict__ EIG,
                 const T *__restrict__ X, T *__restrict__ Y, KernelParams kp, T alpha,
-                int v_in_smem, const int *gate, int nvec, i64 ldv, const double *__restrict__ e0v)
+                int v_in_smem, const int *gate, int nvec, i64 ldv, const double *__restrict__ e0v,
+                const int *__restrict__ vgate = nullptr, int vstride = 0)
 {
     if (gate && *gate) return;
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -68,6 +69,7 @@ px_level1_fused(int n, i64 nblk, const T *__restrict__ V, const T *__restrict__ 
             Vsrc = Vs;
         }
         for (int v = 0; v < nvec; ++v) {
+            if (vgate && vgate[(i64)v * vstride]) continue;   // uniform over the CTA
             const T e0 = T(e0v ? e0v[v] : kp.e0);
             const T *xb = X + (i64)v * ldv + b * (i64)n;
             __syncthreads();
@@ -426,7 +428,7 @@ template int px_vec<double>(const scalit_ctx *, int, const double *, double *, d
 // vectors, and the outer rotations fold the vectors into the GEMM rows.
 template <class T>
 int px_multi(const scalit_ctx *c, const T *X, T *Y, T *tmp, int nvec, const double *e0v, const int *gate,
-             cudaStream_t s)
+             cudaStream_t s, const int *vgate, int vstride)
 {
     const Layout &L = c->L;
     if (!c->osb_built) { set_error("P*X before the preconditioner was built or loaded"); return SCALIT_ESTATE; }
@@ -451,16 +453,19 @@ int px_multi(const scalit_ctx *c, const T *X, T *Y, T *tmp, int nvec, const doub
                 return 0;
             }
         } else {
-            if (tc32_px_usable(c, l)) return tc32_rot_apply(c, l, transpose, a, o, gate, s, nvec);
+            if (tc32_px_usable(c, l)) return tc32_rot_apply(c, l, transpose, a, o, gate, s, nvec, vgate, vstride);
         }
-        if (nin * nvec > 2147483647LL) { set_error("level %d too large for %d vectors", l + 1, nvec); return SCALIT_EINVAL; }
+        // batch z = v blk + b: vector v's block b sits at z nin nout (N = nin nout blk)
+        const i64 nb = L.blk[l] * nvec;
+        if (nb > 65535) { set_error("level %d: %lld blocks x vectors too many", l + 1, (long long)nb); return SCALIT_EINVAL; }
         GemmArgs<T> g{};
         g.K = nout; g.accumulate = 0; g.alpha = T(1); g.gate = gate;
         g.rowscale = nullptr; g.diagV = nullptr;
-        g.M = (int)(nin * nvec); g.N = nout; g.batch = (int)L.blk[l];
-        g.Mi = nin; g.s1 = 1; g.s2 = N;              // row m: a = m % nin of vector m / nin
+        g.M = (int)nin; g.N = nout; g.batch = (int)nb;
+        g.Mi = nin; g.s1 = 1; g.s2 = 0;
         g.A = a; g.a_sk = nin; g.a_sz = nin * nout;
-        g.B = V + L.vs[l]; g.b_sz = (i64)nout * nout;
+        g.B = V + L.vs[l]; g.b_sz = (i64)nout * nout; g.b_mod = (int)L.blk[l];
+        g.vgate = vgate; g.vgate_stride = vstride; g.vgate_div = (int)L.blk[l];
         if (!transpose) { g.b_sk = nout; g.b_sn = 1; }
         else { g.b_sk = 1; g.b_sn = nout; }
         g.C = o; g.c_sn = nin; g.c_sz = nin * nout;
@@ -490,7 +495,7 @@ int px_multi(const scalit_ctx *c, const T *X, T *Y, T *tmp, int nvec, const doub
             configured = dev;
         }
         px_level1_fused<T><<<grid_for(L.blk[0]), 256, sm, s>>>(n, L.blk[0], V + L.vs[0], EIG, in, out, kp, T(1),
-                                                               v_in_smem, gate, nvec, N, e0v);
+                                                               v_in_smem, gate, nvec, N, e0v, vgate, vstride);
         SC_CHECK_LAUNCH();
         in = out;
     }
@@ -504,8 +509,8 @@ int px_multi(const scalit_ctx *c, const T *X, T *Y, T *tmp, int nvec, const doub
     return 0;
 }
 
-template int px_multi<double>(const scalit_ctx *, const double *, double *, double *, int, const double *, const int *, cudaStream_t);
-template int px_multi<float>(const scalit_ctx *, const float *, float *, float *, int, const double *, const int *, cudaStream_t);
+template int px_multi<double>(const scalit_ctx *, const double *, double *, double *, int, const double *, const int *, cudaStream_t, const int *, int);
+template int px_multi<float>(const scalit_ctx *, const float *, float *, float *, int, const double *, const int *, cudaStream_t, const int *, int);
 
 template int px_vec<float>(const scalit_ctx *, int, const float *, float *, float *, float, const int *, cudaStream_t);
 

@@ -324,6 +324,10 @@ qmr_init_norms(i64 n, i64 ld, const T *B, const T *Z, QmrState *st, double *part
     }
 }
 
+// Stop flags of the right-hand sides' states, for per-vector gating of the operators.
+const int *qmr_done_flag(const QmrState *st) { return &st->done; }
+int qmr_state_stride() { return (int)(sizeof(QmrState) / sizeof(int)); }
+
 // all = 1 when every right-hand side's recurrence has stopped
 __global__ void qmr_all_done(const QmrState *st, int nrhs, int *all)
 {

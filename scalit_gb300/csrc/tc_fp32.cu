@@ -30,7 +30,8 @@
 namespace sc {
 
 static constexpr int kBM32 = 128;
-static constexpr int kThreads32 = 512;
+static constexpr int kThreads32 = 512;                      // cutting threads: four per grid row
+static constexpr int kBlock32 = 544;                        // plus one warp that issues the MMAs
 static constexpr int kStages32 = 3;
 static constexpr int kSlab32 = kBM32 * 17;                 // floats per slab stage (row stride 17)
 static constexpr int kAStep32 = 2 * kBM32 * 16 * 2;        // hi + lo planes of 128 x 16 BF16
@@ -48,6 +49,8 @@ struct Tc32Args {
     i64 dx_sz;
     float shift;
     const float *shiftv;
+    const int *vgate;      // per-vector stop flags vgate[z * vgate_stride] (may be null)
+    int vgate_stride;
     const int *gate;
     int *err;
     const uint4 *bsplit;   // [blocks][ntile][ks][hi, lo][NT x 16 BF16, canonical]
@@ -55,18 +58,20 @@ struct Tc32Args {
     i64 b_blk;             // uint4 stride between blocks' planes
 };
 
-__global__ void __launch_bounds__(kThreads32, 2)
+__global__ void __launch_bounds__(kBlock32, 2)
 tc32_level_kernel(Tc32Args g)
 {
     if (g.gate && *g.gate) return;
+    if (g.vgate && g.vgate[(i64)blockIdx.z * g.vgate_stride]) return;
     extern __shared__ __align__(1024) unsigned char smem[];
     const int NT = g.NT, KS = g.KS;
     const int bstep = 2 * NT * 32;                         // bytes of one K step of B (hi + lo)
     unsigned char *Bs = smem;                              // KS x bstep
     unsigned char *Abuf = Bs + (size_t)KS * bstep;         // 2 x kAStep32
     float *slabs = reinterpret_cast<float *>(Abuf + 2 * kAStep32);      // kStages32 x kSlab32
-    uint64_t *mbar = reinterpret_cast<uint64_t *>(slabs + kStages32 * kSlab32);
-    uint32_t *tslot = reinterpret_cast<uint32_t *>(mbar + 2);
+    uint64_t *mbar = reinterpret_cast<uint64_t *>(slabs + kStages32 * kSlab32);   // MMAs of a buffer done
+    uint64_t *cutb = mbar + 2;                                                      // a buffer's planes cut
+    uint32_t *tslot = reinterpret_cast<uint32_t *>(mbar + 4);
 
     const int tid = threadIdx.x, warp = tid >> 5;
     const int ntile = blockIdx.y, z = blockIdx.z;
@@ -93,7 +98,39 @@ tc32_level_kernel(Tc32Args g)
     if (tid == 0) {
         mbar_init(&mbar[0], 1);
         mbar_init(&mbar[1], 1);
+        mbar_init(&cutb[0], kThreads32);
+        mbar_init(&cutb[1], kThreads32);
         mbar_init_fence();
+    }
+    if (warp == kThreads32 / 32) {
+        // the MMA warp: per K step wait for the cut planes, issue the three
+        // MMAs (one lane), commit them to the buffer's barrier
+        fence_before();
+        __syncthreads();
+        fence_after();
+        const uint32_t tbase = *tslot;
+        const uint32_t idesc = idesc_bf16(NT);
+        for (int ks = 0; ks < KS; ++ks) {
+            const int buf = ks & 1;
+            if (!mbar_wait(&cutb[buf], (uint32_t)((ks >> 1) & 1))) break;
+            fence_after();
+            if ((tid & 31) == 0) {
+                const unsigned char *Ab = Abuf + buf * kAStep32;
+                const uint64_t a_hi = smem_desc(smem_addr(Ab), 128, 256);
+                const uint64_t a_lo = smem_desc(smem_addr(Ab + kBM32 * 32), 128, 256);
+                const unsigned char *Bk = Bs + (size_t)ks * bstep;
+                const uint64_t b_hi = smem_desc(smem_addr(Bk), 128, 256);
+                const uint64_t b_lo = smem_desc(smem_addr(Bk + NT * 32), 128, 256);
+                tc_mma(tbase, a_hi, b_hi, idesc, ks > 0 ? 1u : 0u);
+                tc_mma(tbase, a_hi, b_lo, idesc, 1u);
+                tc_mma(tbase, a_lo, b_hi, idesc, 1u);
+                tc_commit(&mbar[buf]);
+            }
+            __syncwarp();
+        }
+        fence_before();
+        __syncthreads();
+        return;   // warp 0 frees the TMEM
     }
     // the whole B tile, already split and in the canonical layout
     {
@@ -142,13 +179,12 @@ tc32_level_kernel(Tc32Args g)
     __syncthreads();
     fence_after();
     const uint32_t tbase = *tslot;
-    const uint32_t idesc = idesc_bf16(NT);
     bool ok = true;
     for (int ks = 0; ks < KS; ++ks) {
         const int buf = ks & 1;
         if (ks >= 2 && !mbar_wait(&mbar[buf], ((ks - 2) >> 1) & 1)) { ok = false; break; }
         asm volatile("cp.async.wait_group %0;" :: "n"(kStages32 - 2) : "memory");
-        __syncthreads();
+        asm volatile("bar.sync 1, %0;" :: "n"(kThreads32) : "memory");   // cutting threads only
         issue(ks + kStages32 - 1);
         const float *st = slabs + (ks % kStages32) * kSlab32;
         unsigned char *Ab = Abuf + buf * kAStep32;
@@ -167,21 +203,9 @@ tc32_level_kernel(Tc32Args g)
         const int rowoff = (row >> 3) * 256 + (q >> 1) * 128 + (row & 7) * 16 + (q & 1) * 8;
         *reinterpret_cast<uint2 *>(Ab + rowoff) = make_uint2(hw[0], hw[1]);
         *reinterpret_cast<uint2 *>(Ab + kBM32 * 32 + rowoff) = make_uint2(lw[0], lw[1]);
+        // make the planes (and the preloaded B tile) visible to the tensor cores
         fence_proxy_async_smem();
-        fence_before();
-        __syncthreads();
-        fence_after();
-        if (tid == 0) {
-            const uint64_t a_hi = smem_desc(smem_addr(Ab), 128, 256);
-            const uint64_t a_lo = smem_desc(smem_addr(Ab + kBM32 * 32), 128, 256);
-            const unsigned char *Bk = Bs + (size_t)ks * bstep;
-            const uint64_t b_hi = smem_desc(smem_addr(Bk), 128, 256);
-            const uint64_t b_lo = smem_desc(smem_addr(Bk + NT * 32), 128, 256);
-            tc_mma(tbase, a_hi, b_hi, idesc, ks > 0 ? 1u : 0u);
-            tc_mma(tbase, a_hi, b_lo, idesc, 1u);
-            tc_mma(tbase, a_lo, b_hi, idesc, 1u);
-            tc_commit(&mbar[buf]);
-        }
+        asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" :: "r"(smem_addr(&cutb[buf])) : "memory");
     }
     if (ok) ok = mbar_wait(&mbar[(KS - 1) & 1], ((KS - 1) >> 1) & 1);
     asm volatile("cp.async.wait_all;" ::: "memory");
@@ -302,7 +326,7 @@ int tc32_prepare(scalit_ctx *c, bool rotations)
 
 static size_t smem_bytes(int NT, int KS)
 {
-    return (size_t)KS * 2 * NT * 32 + 2 * (size_t)kAStep32 + (size_t)kStages32 * kSlab32 * 4 + 64;
+    return (size_t)KS * 2 * NT * 32 + 2 * (size_t)kAStep32 + (size_t)kStages32 * kSlab32 * 4 + 96;
 }
 
 static int launch32(const Tc32Args &g, i64 gx, int ntiles, int nvec, cudaStream_t s)
@@ -317,7 +341,7 @@ static int launch32(const Tc32Args &g, i64 gx, int ntiles, int nvec, cudaStream_
         configured = dev;
     }
     if (gx > 2147483647LL || nvec > 65535) { set_error("tensor-core FP32 grid too large"); return SCALIT_EINVAL; }
-    tc32_level_kernel<<<dim3((unsigned)gx, ntiles, nvec), kThreads32, smem, s>>>(g);
+    tc32_level_kernel<<<dim3((unsigned)gx, ntiles, nvec), kBlock32, smem, s>>>(g);
     SC_CHECK_LAUNCH();
     return 0;
 }
@@ -333,7 +357,8 @@ bool tc32_px_usable(const scalit_ctx *c, int l)
 }
 
 int tc32_level_apply(const scalit_ctx *c, int l, const float *X, float *Y, int accumulate, const float *diagV,
-                     float shift, float alpha, const int *gate, cudaStream_t s, int nvec, const float *shiftv)
+                     float shift, float alpha, const int *gate, cudaStream_t s, int nvec, const float *shiftv,
+                     const int *vgate, int vstride)
 {
     const Layout &L = c->L;
     const TcLevelData &t = c->tc32[l];
@@ -354,13 +379,14 @@ int tc32_level_apply(const scalit_ctx *c, int l, const float *X, float *Y, int a
     g.A = X; g.a_sz = N; g.C = Y; g.c_sz = N;
     g.accumulate = accumulate; g.alpha = alpha;
     g.diagV = diagV; g.diagX = X; g.dx_sz = N; g.shift = shift; g.shiftv = shiftv;
+    g.vgate = vgate; g.vgate_stride = vstride;
     g.gate = gate; g.err = c->tc_err;
     g.bsplit = reinterpret_cast<const uint4 *>(t.dig);
     return launch32(g, (g.M + kBM32 - 1) / kBM32, t.ntiles, nvec, s);
 }
 
 int tc32_rot_apply(const scalit_ctx *c, int l, int transpose, const float *X, float *Y, const int *gate,
-                   cudaStream_t s, int nvec)
+                   cudaStream_t s, int nvec, const int *vgate, int vstride)
 {
     const Layout &L = c->L;
     const TcLevelData &t = c->pxtc32[l][transpose ? 1 : 0];
@@ -374,6 +400,7 @@ int tc32_rot_apply(const scalit_ctx *c, int l, int transpose, const float *X, fl
     g.M = (int)M; g.Mi = nin; g.s1 = 1; g.s2 = nin * nout; g.a_sk = nin; g.c_sn = nin;
     g.A = X; g.a_sz = N; g.C = Y; g.c_sz = N;
     g.alpha = 1.0f; g.gate = gate; g.err = c->tc_err;
+    g.vgate = vgate; g.vgate_stride = vstride;
     g.bsplit = reinterpret_cast<const uint4 *>(t.dig);
     i64 gx;
     if (blk > 1) {

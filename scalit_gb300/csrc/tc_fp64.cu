@@ -44,7 +44,8 @@ namespace sc {
 static constexpr int kDigits = 7;
 static constexpr int kGroups = 7;
 static constexpr int kBM = 128;
-static constexpr int kThreadsTC = 512;   // four threads per grid row
+static constexpr int kThreadsTC = 512;   // cutting threads: four per grid row
+static constexpr int kBlockTC = 544;     // plus one warp that issues the MMAs
 static constexpr int kTmemCols = 512;
 static constexpr int kStages = 3;                               // FP64 slab ring depth
 static constexpr int kSlab = kBM * 17;                          // doubles per slab stage
@@ -63,6 +64,8 @@ struct TcArgs {
     i64 dx_sz;
     double shift;
     const double *shiftv;   // per-vector shifts (vector index z), overriding shift
+    const int *vgate;       // per-vector stop flags vgate[z * vgate_stride] (may be null)
+    int vgate_stride;
     const int *gate;
     int *err;
     const uint4 *bdig;    // [ntile][ks][digit][NT x 16 BF16, canonical]
@@ -92,18 +95,20 @@ __device__ __forceinline__ unsigned long long fixed49(unsigned long long bits, i
     return (sh <= -64) ? 0ULL : (m >> (-sh));
 }
 
-__global__ void __launch_bounds__(kThreadsTC, 1)
+__global__ void __launch_bounds__(kBlockTC, 1)
 tc_level_kernel(TcArgs g)
 {
     if (g.gate && *g.gate) return;
+    if (g.vgate && g.vgate[(i64)blockIdx.z * g.vgate_stride]) return;
     extern __shared__ __align__(1024) unsigned char smem[];
     const int NT = g.NT, KS = g.KS;
     const int bstep = kDigits * NT * 32;                   // bytes of one K step of B digits
     unsigned char *Abuf = smem;                            // 2 x kAStepBytes
     unsigned char *Bbuf = smem + 2 * kAStepBytes;          // 2 x bstep
     double *slabs = reinterpret_cast<double *>(Bbuf + 2 * bstep);   // kStages x kSlab
-    uint64_t *mbar = reinterpret_cast<uint64_t *>(slabs + kStages * kSlab);
-    uint32_t *tslot = reinterpret_cast<uint32_t *>(mbar + 2);
+    uint64_t *mbar = reinterpret_cast<uint64_t *>(slabs + kStages * kSlab);   // MMAs of a buffer done
+    uint64_t *cutb = mbar + 2;                                                  // a buffer's digits cut
+    uint32_t *tslot = reinterpret_cast<uint32_t *>(mbar + 4);
 
     const int tid = threadIdx.x, warp = tid >> 5;
     const int ntile = blockIdx.y, z = blockIdx.z;
@@ -130,9 +135,11 @@ tc_level_kernel(TcArgs g)
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
     }
     if (tid == 0) {
-        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" :: "r"(smem_addr(&mbar[0])) : "memory");
-        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" :: "r"(smem_addr(&mbar[1])) : "memory");
-        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        mbar_init(&mbar[0], 1);
+        mbar_init(&mbar[1], 1);
+        mbar_init(&cutb[0], kThreadsTC);
+        mbar_init(&cutb[1], kThreadsTC);
+        mbar_init_fence();
     }
 
     // BF16 bit patterns of the digits -127..127 (all exact in BF16)
@@ -141,8 +148,46 @@ tc_level_kernel(TcArgs g)
         bf_tab[i] = __bfloat16_as_ushort(__float2bfloat16_rn((float)(i - 127)));
     int *em4 = reinterpret_cast<int *>(bf_tab + 256);       // [4][kBM] partial row exponents
 
+    if (warp == kThreadsTC / 32) {
+        // The MMA warp: for every K step, wait until the cutting threads have
+        // written the step's digit planes, issue the 28 digit-pair MMAs (one
+        // lane) and commit them to the buffer's barrier; the cutting of the
+        // next step proceeds meanwhile.
+        fence_before();
+        __syncthreads();
+        fence_after();
+        const uint32_t tbase = *tslot;
+        const uint32_t idesc = idesc_bf16(NT);
+        const int lane = tid & 31;
+        for (int ks = 0; ks < KS; ++ks) {
+            const int buf = ks & 1;
+            if (!mbar_wait(&cutb[buf], (uint32_t)((ks >> 1) & 1))) break;
+            fence_after();
+            if (lane == 0) {
+                const unsigned char *Ab = Abuf + buf * kAStepBytes;
+                const unsigned char *Bb = Bbuf + buf * bstep;
+                #pragma unroll 1
+                for (int s = 0; s < kDigits; ++s) {
+                    const uint64_t ad = smem_desc(smem_addr(Ab + s * (kBM * 32)), 128, 256);
+                    #pragma unroll 1
+                    for (int t = 0; t + s < kGroups; ++t) {
+                        const uint64_t bd = smem_desc(smem_addr(Bb + t * (NT * 32)), 128, 256);
+                        const uint32_t acc = (ks > 0 || s > 0) ? 1u : 0u;
+                        tc_mma(tbase + (uint32_t)((s + t) * NT), ad, bd, idesc, acc);
+                    }
+                }
+                tc_commit(&mbar[buf]);
+            }
+            __syncwarp();
+        }
+        fence_before();
+        __syncthreads();
+        return;   // warp 0 frees the TMEM
+    }
+
     // Four threads per grid row: quarter q handles K values 4q..4q+3 of every
-    // 16-wide K step.
+    // 16-wide K step.  The cutting threads synchronise among themselves with
+    // named barrier 1 (the MMA warp never waits on it).
     const int row = tid & (kBM - 1), q = tid >> 7;
     const int m = m0 + row;
     const bool mvalid = m < mlim;
@@ -185,9 +230,10 @@ tc_level_kernel(TcArgs g)
         }
         asm volatile("cp.async.commit_group;" ::: "memory");
     };
+    auto cut_sync = [&]() { asm volatile("bar.sync 1, %0;" :: "n"(kThreadsTC) : "memory"); };
     auto ready = [&]() {
         asm volatile("cp.async.wait_group %0;" :: "n"(kStages - 2) : "memory");
-        __syncthreads();
+        cut_sync();
     };
     auto slab_val = [&](const double *st, int j) -> unsigned long long {   // K value j of this row
         return (unsigned long long)__double_as_longlong(rowc ? st[row * 17 + j] : st[j * kBM + row]);
@@ -205,15 +251,14 @@ tc_level_kernel(TcArgs g)
         }
     }
     em4[q * kBM + row] = em;
-    __syncthreads();
+    cut_sync();
     em = max(max(em4[row], em4[kBM + row]), max(em4[2 * kBM + row], em4[3 * kBM + row]));
     if (em < -2000) em = 0;   // an all-zero row
 
     fence_before();
-    __syncthreads();
+    __syncthreads();          // with the MMA warp: TMEM address and barriers ready
     fence_after();
     const uint32_t tbase = *tslot;
-    const uint32_t idesc = idesc_bf16(NT);
     bool ok = true;
 
     for (int ks = 0; ks < KS; ++ks) {
@@ -254,23 +299,9 @@ tc_level_kernel(TcArgs g)
         const uint4 *src = bdig + ((i64)ntile * KS + ks) * (bstep / 16);
         uint4 *dst = reinterpret_cast<uint4 *>(Bb);
         for (int i = tid; i < bstep / 16; i += kThreadsTC) dst[i] = src[i];
-        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-        fence_before();
-        __syncthreads();
-        fence_after();
-        if (tid == 0) {
-            #pragma unroll 1
-            for (int s = 0; s < kDigits; ++s) {
-                const uint64_t ad = smem_desc(smem_addr(Ab + s * (kBM * 32)), 128, 256);
-                #pragma unroll 1
-                for (int t = 0; t + s < kGroups; ++t) {
-                    const uint64_t bd = smem_desc(smem_addr(Bb + t * (NT * 32)), 128, 256);
-                    const uint32_t acc = (ks > 0 || s > 0) ? 1u : 0u;
-                    tc_mma(tbase + (uint32_t)((s + t) * NT), ad, bd, idesc, acc);
-                }
-            }
-            tc_commit(&mbar[buf]);
-        }
+        // make the planes visible to the tensor cores, then hand the step over
+        fence_proxy_async_smem();
+        asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" :: "r"(smem_addr(&cutb[buf])) : "memory");
     }
     if (ok) ok = mbar_wait(&mbar[(KS - 1) & 1], ((KS - 1) >> 1) & 1);
     asm volatile("cp.async.wait_all;" ::: "memory");   // no copy of this CTA stays in flight
@@ -318,7 +349,7 @@ tc_level_kernel(TcArgs g)
         }
     }
     fence_before();
-    __syncthreads();
+    __syncthreads();          // with the MMA warp
     if (warp == 0)
         asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" :: "r"(tbase), "r"(kTmemCols) : "memory");
 }
@@ -511,7 +542,7 @@ int tc_rot_apply(const scalit_ctx *c, int l, int transpose, const double *X, dou
                         64 + 3072;
     const size_t smem_req = std::max(smem, (size_t)(116 * 1024));
     SC_CUDA(cudaFuncSetAttribute(tc_level_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_req));
-    tc_level_kernel<<<dim3((unsigned)gx, t.ntiles, 1), kThreadsTC, smem_req, s>>>(g);
+    tc_level_kernel<<<dim3((unsigned)gx, t.ntiles, 1), kBlockTC, smem_req, s>>>(g);
     SC_CHECK_LAUNCH();
     return 0;
 }
@@ -522,7 +553,8 @@ bool tc_usable(const scalit_ctx *c, int l)
 }
 
 int tc_level_apply(const scalit_ctx *c, int l, const double *X, double *Y, int accumulate, const double *diagV,
-                   double shift, double alpha, const int *gate, cudaStream_t s, int nvec, const double *shiftv)
+                   double shift, double alpha, const int *gate, cudaStream_t s, int nvec, const double *shiftv,
+                   const int *vgate, int vstride)
 {
     const Layout &L = c->L;
     const TcLevelData &t = c->tc[l];
@@ -552,6 +584,8 @@ int tc_level_apply(const scalit_ctx *c, int l, const double *X, double *Y, int a
     g.dx_sz = N;
     g.shift = shift;
     g.shiftv = shiftv;
+    g.vgate = vgate;
+    g.vgate_stride = vstride;
     g.gate = gate;
     g.err = c->tc_err;
     g.bdig = reinterpret_cast<const uint4 *>(t.dig);
@@ -563,7 +597,7 @@ int tc_level_apply(const scalit_ctx *c, int l, const double *X, double *Y, int a
     SC_CUDA(cudaFuncSetAttribute(tc_level_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_req));
     dim3 grid((g.M + kBM - 1) / kBM, t.ntiles, nvec);
     if (grid.z > 65535) { set_error("too many vectors"); return SCALIT_EINVAL; }
-    tc_level_kernel<<<grid, kThreadsTC, smem_req, s>>>(g);
+    tc_level_kernel<<<grid, kBlockTC, smem_req, s>>>(g);
     SC_CHECK_LAUNCH();
     return 0;
 }
