@@ -32,7 +32,7 @@ namespace sc {
 static constexpr int kBM32 = 128;
 static constexpr int kThreads32 = 512;                      // cutting threads: four per grid row
 static constexpr int kBlock32 = 544;                        // plus one warp that issues the MMAs
-static constexpr int kStages32 = 3;
+static constexpr int kStages32 = 6;
 static constexpr int kSlab32 = kBM32 * 17;                 // floats per slab stage (row stride 17)
 static constexpr int kAStep32 = 2 * kBM32 * 16 * 2;        // hi + lo planes of 128 x 16 BF16
 
@@ -173,7 +173,15 @@ tc32_level_kernel(Tc32Args g)
         }
         asm volatile("cp.async.commit_group;" ::: "memory");
     };
-    for (int t = 0; t < kStages32 - 1; ++t) issue(t);
+    // K <= 16 kStages32: every slab in flight at once and resident; otherwise a
+    // ring with kStages32 - 1 slabs of look-ahead
+    const bool resident = (KS <= kStages32);
+    if (resident) {
+        for (int t = 0; t < KS; ++t) issue(t);
+        asm volatile("cp.async.wait_all;" ::: "memory");
+    } else {
+        for (int t = 0; t < kStages32 - 1; ++t) issue(t);
+    }
 
     fence_before();
     __syncthreads();
@@ -183,9 +191,11 @@ tc32_level_kernel(Tc32Args g)
     for (int ks = 0; ks < KS; ++ks) {
         const int buf = ks & 1;
         if (ks >= 2 && !mbar_wait(&mbar[buf], ((ks - 2) >> 1) & 1)) { ok = false; break; }
-        asm volatile("cp.async.wait_group %0;" :: "n"(kStages32 - 2) : "memory");
-        asm volatile("bar.sync 1, %0;" :: "n"(kThreads32) : "memory");   // cutting threads only
-        issue(ks + kStages32 - 1);
+        if (!resident) {
+            asm volatile("cp.async.wait_group %0;" :: "n"(kStages32 - 2) : "memory");
+            asm volatile("bar.sync 1, %0;" :: "n"(kThreads32) : "memory");   // cutting threads only
+            issue(ks + kStages32 - 1);
+        }
         const float *st = slabs + (ks % kStages32) * kSlab32;
         unsigned char *Ab = Abuf + buf * kAStep32;
         uint32_t hw[2], lw[2];

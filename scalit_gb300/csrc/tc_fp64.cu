@@ -47,7 +47,7 @@ static constexpr int kBM = 128;
 static constexpr int kThreadsTC = 512;   // cutting threads: four per grid row
 static constexpr int kBlockTC = 544;     // plus one warp that issues the MMAs
 static constexpr int kTmemCols = 512;
-static constexpr int kStages = 3;                               // FP64 slab ring depth
+static constexpr int kStages = 8;                               // FP64 slab ring depth
 static constexpr int kSlab = kBM * 17;                          // doubles per slab stage
 static constexpr int kAStepBytes = kDigits * kBM * 16 * 2;    // 7 digit planes of 128 x 16 BF16
 
@@ -238,11 +238,23 @@ tc_level_kernel(TcArgs g)
     auto slab_val = [&](const double *st, int j) -> unsigned long long {   // K value j of this row
         return (unsigned long long)__double_as_longlong(rowc ? st[row * 17 + j] : st[j * kBM + row]);
     };
-    for (int t = 0; t < kStages - 1; ++t) issue(t);
+    // With K <= 16 kStages all K slabs fit the ring: they are loaded once, all in
+    // flight together, and serve both passes; otherwise they stream twice with
+    // kStages - 1 slabs of look-ahead.
+    const bool resident = (KS <= kStages);
+    if (resident) {
+        for (int t = 0; t < KS; ++t) issue(t);
+        asm volatile("cp.async.wait_all;" ::: "memory");
+        cut_sync();
+    } else {
+        for (int t = 0; t < kStages - 1; ++t) issue(t);
+    }
     int em = -100000;
     for (int t = 0; t < KS; ++t) {
-        ready();
-        issue(t + kStages - 1);
+        if (!resident) {
+            ready();
+            issue(t + kStages - 1);
+        }
         const double *st = slabs + (t % kStages) * kSlab;
         #pragma unroll
         for (int jj = 0; jj < 4; ++jj) {
@@ -267,9 +279,11 @@ tc_level_kernel(TcArgs g)
         unsigned char *Ab = Abuf + buf * kAStepBytes;
         unsigned char *Bb = Bbuf + buf * bstep;
         const int t = KS + ks;
-        ready();
-        issue(t + kStages - 1);
-        const double *st = slabs + (t % kStages) * kSlab;
+        if (!resident) {
+            ready();
+            issue(t + kStages - 1);
+        }
+        const double *st = slabs + ((resident ? ks : t) % kStages) * kSlab;
         // cut this row's 4 values of the K step (this thread's quarter) into 7
         // digit planes: the digits are the 7-bit fields of the 49-bit fixed-point
         // magnitude, with x's sign
