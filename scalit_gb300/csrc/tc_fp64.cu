@@ -591,6 +591,7 @@ int tc_level_apply(const scalit_ctx *c, int l, const double *X, double *Y, int a
     }
     g.A = X; g.a_sz = N;
     g.C = Y; g.c_sz = N;
+    if (diagV && accumulate) { set_error("the diagonal term goes with the first level only"); return SCALIT_EINVAL; }
     g.accumulate = accumulate;
     g.alpha = alpha;
     g.diagV = diagV;
