@@ -45,11 +45,53 @@ __device__ __forceinline__ bool mbar_wait(uint64_t *mbar, uint32_t parity, long 
     return false;
 }
 
+__device__ __forceinline__ uint64_t globaltimer_ns()
+{
+    uint64_t t;
+    asm volatile("mov.u64 %0, %globaltimer;" : "=l"(t));
+    return t;
+}
+
+// try_wait that may suspend the thread for up to `hint_ns` while the phase is
+// incomplete (it wakes as soon as the phase completes), so waiting warps
+// leave the issue slots to the working ones.
+__device__ __forceinline__ bool mbar_try_suspend(uint64_t *mbar, uint32_t parity, uint32_t hint_ns)
+{
+    uint32_t ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n\t"
+        "selp.b32 %0, 1, 0, p;\n\t}\n"
+        : "=r"(ok) : "r"(smem_addr(mbar)), "r"(parity), "r"(hint_ns) : "memory");
+    return ok != 0;
+}
+
+// Wait bounded by wall time (the global timer) rather than by a poll count,
+// whatever the hardware makes of the suspend hint.
+static constexpr uint64_t kMbarWaitNs = 2000000000ull;   // 2 s
+
+__device__ __forceinline__ bool mbar_wait_timed(uint64_t *mbar, uint32_t parity, uint64_t limit_ns = kMbarWaitNs)
+{
+    if (mbar_try(mbar, parity)) return true;
+    const uint64_t t0 = globaltimer_ns();
+    for (;;) {
+        if (mbar_try_suspend(mbar, parity, 20000)) return true;
+        if (globaltimer_ns() - t0 > limit_ns) return false;
+    }
+}
+
 // One arrival that also announces `bytes` of transaction count.
 __device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t *mbar, uint32_t bytes)
 {
     asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;"
                  :: "r"(smem_addr(mbar)), "r"(bytes) : "memory");
+}
+
+// One plain arrival (release semantics: the caller's earlier reads of the
+// guarded buffer are ordered before whoever waits on the phase).
+__device__ __forceinline__ void mbar_arrive(uint64_t *mbar)
+{
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" :: "r"(smem_addr(mbar)) : "memory");
 }
 
 // Order earlier generic-proxy accesses of shared memory before later

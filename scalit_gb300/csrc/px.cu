@@ -12,6 +12,7 @@
 #include "ptx.cuh"
 
 #include <algorithm>
+#include <cstdlib>
 #include <type_traits>
 
 namespace sc {
@@ -96,20 +97,46 @@ px_level1_fused(int n, i64 nblk, const T *__restrict__ V, const T *__restrict__ 
     }
 }
 
-// Streaming variant of the fused level-1 pass: a persistent CTA walks its
-// blocks while the blocks' matrices arrive as column chunks (kChunkCols
-// columns = kChunkCols * n contiguous numbers) through a ring of shared-memory
-// slots, each filled by one bulk copy that completes on the slot's mbarrier.
-// Phase 1 (t = V^T x, then K^-1) takes a chunk as soon as it lands; phase 2
-// (y = V t, one warp per column, every lane accumulating its own rows) frees
-// each slot once all warps are past it, and the slot is refilled right away
-// with the chunk `ring` positions ahead -- the next block's columns stream in
-// while this block finishes, so HBM sees one continuous read of VOSB level 1.
-static constexpr int kChunkCols = 16;
+// Streaming variant of the fused level-1 pass.  A persistent CTA walks its
+// blocks while the blocks' matrices arrive as column chunks (CPW columns per
+// warp, CPW * 8 * n contiguous numbers) through a ring of shared-memory slots,
+// each filled by one bulk copy that completes on the slot's mbarrier.
+// Column j contributes t_j = f_j (v_j . x) and then t_j v_j to y, with f_j the
+// preconditioner kernel's factor for eigenvalue j, so a chunk is finished --
+// both products -- as soon as it lands: each warp takes CPW columns, reduces
+// their dot products together (a reduce-scatter over lane groups, then a
+// broadcast of t_j) and accumulates its own rows of y in registers.  The last
+// warp to finish a chunk (a shared-memory counter per slot) refills the slot
+// with the chunk `ring` positions ahead, so the ring need not hold a whole
+// block and HBM sees one continuous read of VOSB level 1.  The warps' partial
+// y meet once per block; partials, x and the factors are double-buffered by
+// block parity, so one CTA barrier per block suffices.
 static constexpr int kStreamThreads = 256;
+static constexpr int kStreamWarps = kStreamThreads / 32;
 
-template <class T, int RPL>
-__global__ void __launch_bounds__(kStreamThreads)
+// The factor f with K^-1 y = f y for eigenvalue `eig` (osb.px.h:156-189).
+template <class T>
+__device__ __forceinline__ T kernel_factor(T eig, T e0, int kind, T de, T rde, T alpha_d, T beta_d)
+{
+    const T ade = eig - e0;
+    if (kind == SCALIT_TOSBD1 && fabs(ade) <= de) return (ade < T(0)) ? -rde : rde;
+    if (kind == SCALIT_TOSBD2 && fabs(ade) <= de)
+        return T(1) / ((ade < T(0)) ? (-alpha_d + beta_d * ade) : (alpha_d + beta_d * ade));
+    return T(1) / ade;
+}
+
+// Shared memory of the streaming kernel: ring mbarriers, release counters and
+// last-issued chunk per slot, then the slots, then per block parity x, the
+// factors and NW partial y.
+__host__ __device__ constexpr size_t px1_stream_head(int ring)
+{
+    return (((size_t)ring * 16 + 127) & ~(size_t)127);
+}
+
+// FULL: n == 32 * RPL, every lane holds RPL rows and no row test is needed.
+// CPW (2 or 4): columns per warp and chunk.
+template <class T, int RPL, bool FULL, int CPW>
+__global__ void __launch_bounds__(kStreamThreads, sizeof(T) == 4 ? 4 : 2)
 px_level1_stream(int n, i64 nblk, const T *__restrict__ V, const T *__restrict__ EIG,
                  const T *__restrict__ X, T *__restrict__ Y, KernelParams kp, T alpha, int nc, int ring,
                  const int *gate, int *err)
@@ -117,77 +144,55 @@ px_level1_stream(int n, i64 nblk, const T *__restrict__ V, const T *__restrict__
     if (gate && *gate) return;
     extern __shared__ __align__(16) unsigned char smem_stream[];
     __shared__ int abort_flag;
-    constexpr int NW = kStreamThreads / 32;
-    uint64_t *mbar = reinterpret_cast<uint64_t *>(smem_stream);
-    const size_t slot_elems = (size_t)kChunkCols * n;
-    T *slots = reinterpret_cast<T *>(smem_stream + (((size_t)ring * 8 + 127) & ~(size_t)127));
-    T *xs = slots + (size_t)ring * slot_elems;
-    T *ts = xs + n;
-    T *es = ts + n;                                     // the block's EIG0
-    T *part = es + n;                                   // NW x n
+    constexpr int NW = kStreamWarps, kChunkCols = CPW * kStreamWarps;
+    static_assert(CPW == 2 || CPW == 4, "two or four columns per warp");
+    uint64_t *full = reinterpret_cast<uint64_t *>(smem_stream);
+    int *relcnt = reinterpret_cast<int *>(full + ring);         // warps done with the slot's chunks
+    int *last = relcnt + ring;                                  // the chunk last issued into the slot
+    const int slot_elems = kChunkCols * n;
+    T *slots = reinterpret_cast<T *>(smem_stream + px1_stream_head(ring));
+    T *vec0 = slots + ring * slot_elems;                        // per parity: x, f, NW partials
+    const int vstride = (2 + NW) * n;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const T e0 = T(kp.e0), de = T(fabs(kp.de)), rde = T(1.0 / fabs(kp.de));
     const T beta_d = T(1.0 + kp.beta), alpha_d = T(-kp.beta * fabs(kp.de));
 
-    const i64 kblocks = (nblk - blockIdx.x + gridDim.x - 1) / gridDim.x;   // blocks of this CTA
-    const i64 G = kblocks * nc;                                            // its chunks
-    auto issue = [&](i64 g) {
-        const i64 b = blockIdx.x + (g / nc) * (i64)gridDim.x;
-        const int c0 = (int)(g % nc) * kChunkCols;
+    // chunk and slot counters are plain ints advanced step by step: the loops
+    // hold no 64-bit division or remainder
+    const int kblocks = (int)((nblk - blockIdx.x + gridDim.x - 1) / gridDim.x);   // blocks of this CTA
+    const int G = kblocks * nc;                                                  // its chunks
+    auto issue = [&](int g, int slot) {
+        const int kk = g / nc, c0 = (g - kk * nc) * kChunkCols;
+        const i64 b = blockIdx.x + (i64)kk * gridDim.x;
         const int cols = min(kChunkCols, n - c0);
         const uint32_t bytes = (uint32_t)(sizeof(T) * (size_t)cols * n);
-        const int slot = (int)(g % ring);
-        mbar_arrive_expect_tx(&mbar[slot], bytes);
-        bulk_g2s(slots + (size_t)slot * slot_elems, V + b * (i64)n * n + (i64)c0 * n, bytes, &mbar[slot]);
+        last[slot] = g;
+        mbar_arrive_expect_tx(&full[slot], bytes);
+        bulk_g2s(slots + slot * slot_elems, V + b * (i64)n * n + (i64)c0 * n, bytes, &full[slot]);
     };
     if (tid == 0) {
         abort_flag = 0;
-        for (int i = 0; i < ring; ++i) mbar_init(&mbar[i], 1);
+        for (int i = 0; i < ring; ++i) {
+            mbar_init(&full[i], 1);
+            relcnt[i] = 0;
+            last[i] = -1;
+        }
         mbar_init_fence();
-        for (i64 g = 0; g < G && g < ring; ++g) issue(g);
+        for (int g = 0; g < G && g < ring; ++g) issue(g, g);
     }
-    // X and EIG0 of the first block; later blocks' are fetched during the
-    // previous block's phase 2 (one value per thread, n <= 256)
+    // x and the factors of the first block; each later block's are written
+    // into the other parity before the previous block's barrier
     if (kblocks > 0 && tid < n) {
-        xs[tid] = X[(i64)blockIdx.x * n + tid];
-        es[tid] = EIG[(i64)blockIdx.x * n + tid];
+        vec0[tid] = X[(i64)blockIdx.x * n + tid];
+        vec0[n + tid] = kernel_factor<T>(EIG[(i64)blockIdx.x * n + tid], e0, kp.kind, de, rde, alpha_d, beta_d);
     }
     __syncthreads();
-    i64 issued = G < ring ? G : ring;    // meaningful in thread 0
-    i64 k = 0;
+    int slot = 0;                                       // the current chunk's slot and phase
+    uint32_t par = 0;
+    int k = 0;
     for (; k < kblocks; ++k) {
-        const i64 b = blockIdx.x + k * (i64)gridDim.x;
-        // phase 1: t = K^-1 V^T x.  One warp per column, lanes over rows; two
-        // shuffle levels leave 8 partial dots per column in part[], summed and
-        // divided by the kernel below with one thread per column.
-        for (int c = 0; c < nc; ++c) {
-            const i64 g = k * nc + c;
-            if (!mbar_wait(&mbar[g % ring], (uint32_t)((g / ring) & 1))) { abort_flag = 1; break; }
-            const T *chunk = slots + (size_t)(g % ring) * slot_elems;
-            const int c0 = c * kChunkCols, cols = min(kChunkCols, n - c0);
-            for (int j = warp; j < cols; j += NW) {
-                const T *col = chunk + (size_t)j * n;
-                T acc = T(0);
-                #pragma unroll
-                for (int r = 0; r < RPL; ++r) {
-                    const int row = lane + 32 * r;
-                    if (row < n) acc = fma(col[row], xs[row], acc);
-                }
-                acc += __shfl_xor_sync(0xffffffffu, acc, 16);
-                acc += __shfl_xor_sync(0xffffffffu, acc, 8);
-                if (lane < 8) part[(c0 + j) * 8 + lane] = acc;
-            }
-        }
-        __syncthreads();
-        if (abort_flag) break;
-        for (int i = tid; i < n; i += kStreamThreads) {
-            const T *pp = part + i * 8;
-            const T d = ((pp[0] + pp[1]) + (pp[2] + pp[3])) + ((pp[4] + pp[5]) + (pp[6] + pp[7]));
-            ts[i] = kernel_div<T>(d, es[i], e0, kp.kind, de, rde, alpha_d, beta_d);
-        }
-        __syncthreads();
-        // phase 2: y = V t, releasing the slots in order; meanwhile the next
-        // block's X and EIG0 are on their way into registers
+        const i64 b = blockIdx.x + (i64)k * gridDim.x;
+        T *xs = vec0 + (k & 1) * vstride, *fs = xs + n, *part = fs + n;
         const bool more = k + 1 < kblocks && tid < n;
         T xn = T(0), en = T(0);
         if (more) {
@@ -195,48 +200,95 @@ px_level1_stream(int n, i64 nblk, const T *__restrict__ V, const T *__restrict__
             xn = X[bn * n + tid];
             en = EIG[bn * n + tid];
         }
-        T acc[RPL];
+        T xr[RPL], acc[RPL];
         #pragma unroll
-        for (int r = 0; r < RPL; ++r) acc[r] = T(0);
+        for (int r = 0; r < RPL; ++r) {
+            const int row = lane + 32 * r;
+            xr[r] = (FULL || row < n) ? xs[row] : T(0);
+            acc[r] = T(0);
+        }
         for (int c = 0; c < nc; ++c) {
-            const i64 g = k * nc + c;
-            const T *chunk = slots + (size_t)(g % ring) * slot_elems;
+            const int g = k * nc + c;
+            if (!__all_sync(0xffffffffu, mbar_wait_timed(&full[slot], par))) { abort_flag = 1; break; }
+            const T *chunk = slots + slot * slot_elems + lane;
             const int c0 = c * kChunkCols, cols = min(kChunkCols, n - c0);
-            for (int j = warp; j < cols; j += NW) {
-                const T *col = chunk + (size_t)j * n;
-                const T tj = ts[c0 + j];
+            // the warp's CPW columns, each element read once from shared
+            // memory (columns past the block's last are zero: warp-uniform)
+            T v[CPW][RPL], d[CPW];
+            #pragma unroll
+            for (int q = 0; q < CPW; ++q) {
+                const int j = warp + q * NW;
+                const T *col = chunk + j * n;
+                d[q] = T(0);
                 #pragma unroll
                 for (int r = 0; r < RPL; ++r) {
-                    const int row = lane + 32 * r;
-                    if (row < n) acc[r] = fma(col[row], tj, acc[r]);
+                    v[q][r] = (j < cols && (FULL || lane + 32 * r < n)) ? col[32 * r] : T(0);
+                    d[q] = fma(v[q][r], xr[r], d[q]);
                 }
             }
-            __syncthreads();
-            if (tid == 0 && g + ring < G) {
-                fence_proxy_async_smem();
-                issue(g + ring);
-                issued = g + ring + 1;
+            // reduce-scatter: at each of the first log2(CPW) shuffle levels
+            // the two lane groups swap the columns they do not keep, so lane
+            // group q = lane / (32 / CPW) ends with column q's full sum after
+            // five levels; t_q is then broadcast from the group's first lane
+            T keep;
+            if constexpr (CPW == 2) {
+                const bool h = lane & 16;
+                keep = (h ? d[1] : d[0]) + __shfl_xor_sync(0xffffffffu, h ? d[0] : d[1], 16);
+            } else {
+                const bool h1 = lane & 16, h2 = lane & 8;
+                const T k0 = (h1 ? d[2] : d[0]) + __shfl_xor_sync(0xffffffffu, h1 ? d[0] : d[2], 16);
+                const T k1 = (h1 ? d[3] : d[1]) + __shfl_xor_sync(0xffffffffu, h1 ? d[1] : d[3], 16);
+                keep = (h2 ? k1 : k0) + __shfl_xor_sync(0xffffffffu, h2 ? k0 : k1, 8);
             }
+            #pragma unroll
+            for (int o = 32 / CPW / 2; o > 0; o >>= 1) keep += __shfl_xor_sync(0xffffffffu, keep, o);
+            const int qh = lane / (32 / CPW), jh = warp + qh * NW;
+            const T th = jh < cols ? keep * fs[c0 + jh] : T(0);
+            #pragma unroll
+            for (int q = 0; q < CPW; ++q) {
+                const T tq = __shfl_sync(0xffffffffu, th, q * (32 / CPW));
+                #pragma unroll
+                for (int r = 0; r < RPL; ++r) acc[r] = fma(v[q][r], tq, acc[r]);
+            }
+            // release; the last warp out refills the slot
+            __syncwarp();
+            if (lane == 0) {
+                __threadfence_block();
+                if ((atomicAdd(&relcnt[slot], 1) + 1) % NW == 0) {      // counts NW per use of the slot
+                    __threadfence_block();
+                    if (g + ring < G) {
+                        fence_proxy_async_smem();
+                        issue(g + ring, slot);
+                    }
+                }
+            }
+            if (++slot == ring) { slot = 0; par ^= 1u; }
         }
         #pragma unroll
         for (int r = 0; r < RPL; ++r) {
             const int row = lane + 32 * r;
-            if (row < n) part[warp * n + row] = acc[r];
+            if (FULL || row < n) part[warp * n + row] = acc[r];
+        }
+        if (more) {
+            T *xo = vec0 + ((k + 1) & 1) * vstride;
+            xo[tid] = xn;
+            xo[n + tid] = kernel_factor<T>(en, e0, kp.kind, de, rde, alpha_d, beta_d);
         }
         __syncthreads();
+        if (abort_flag) break;
         for (int i = tid; i < n; i += kStreamThreads) {
             T y = T(0);
             #pragma unroll
             for (int w = 0; w < NW; ++w) y += part[w * n + i];
             Y[b * (i64)n + i] = alpha * y;
         }
-        if (more) { xs[tid] = xn; es[tid] = en; }
-        __syncthreads();
     }
     if (abort_flag && tid == 0) {
         if (err) atomicExch(err, 2);
-        // let every copy this CTA issued land before the CTA's shared memory is released
-        for (i64 g = k * nc; g < issued; ++g) mbar_wait(&mbar[g % ring], (uint32_t)((g / ring) & 1));
+        // every warp has stopped: let the latest copy into each slot land
+        // before the CTA's shared memory is released
+        for (int s = 0; s < ring; ++s)
+            if (last[s] >= 0) mbar_wait_timed(&full[s], (uint32_t)((last[s] / ring) & 1));
     }
 }
 
@@ -297,55 +349,111 @@ template int bgemv<float>(int, int, const float *, const float *, float *, int, 
 
 static constexpr size_t kMaxDynSmem = 220 * 1024;
 
-template <class T, int RPL>
-static int launch_px1_stream(int n, i64 nblk, const T *V, const T *EIG, const T *X, T *Y, KernelParams kp,
-                             T alpha, int nc, int ring, size_t smem, int per_sm, const int *gate, int *err,
-                             cudaStream_t s)
+// Shared memory of one SM and what each resident CTA loses to the runtime.
+static constexpr size_t kSmSmem = 228 * 1024;
+static constexpr size_t kCtaReserve = 1024 + 128;   // runtime reserve + static shared data
+
+// CTAs per SM for the streaming kernel: an explicit choice from the
+// environment (SCALIT_PX1_CTAS, a tuning override), else the most CTAs that
+// are resident at once (registers and shared memory) with a ring of at least
+// two chunks -- measured on GB300, more warps per SM beat a deeper ring.
+// Returns 0 when no count fits, else the count, with the deepest ring (up to
+// four blocks) that it leaves room for.
+static int px1_stream_shape(const void *fn, size_t chunk, int nc, size_t vecs, int &ring)
+{
+    static const int forced = [] {
+        const char *e = getenv("SCALIT_PX1_CTAS");
+        return e ? atoi(e) : 0;
+    }();
+    int best = 0, best_ring = 0;
+    for (int per_sm = 1; per_sm <= 8; ++per_sm) {
+        const size_t budget = std::min(kMaxDynSmem, kSmSmem / per_sm - kCtaReserve);
+        if (budget <= vecs + 128 + 2 * (chunk + 16)) break;
+        const int r = (int)std::min<size_t>((budget - vecs - 128) / (chunk + 16), (size_t)4 * nc);
+        int resident = 0;
+        const size_t smem = px1_stream_head(r) + (size_t)r * chunk + vecs;
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&resident, fn, kStreamThreads, smem) != cudaSuccess) {
+            cudaGetLastError();
+            break;
+        }
+        if (resident < per_sm) break;
+        best = per_sm;
+        best_ring = r;
+        if (per_sm == forced) break;
+    }
+    ring = best_ring;
+    return best;
+}
+
+// Launch of the streaming kernel; returns 1 when it does not apply (no ring
+// of two chunks fits), so the caller takes the one-CTA-per-block kernel.
+template <class T, int RPL, bool FULL, int CPW>
+static int launch_px1_stream_as(int n, i64 nblk, const T *V, const T *EIG, const T *X, T *Y, KernelParams kp,
+                                T alpha, const int *gate, int *err, cudaStream_t s)
 {
     static int configured = -1;
+    static int shape_n[257], shape_cta[257], shape_ring[257];   // per block size, filled on first use
     int dev = 0;
     cudaGetDevice(&dev);
     if (configured != dev) {
-        SC_CUDA(cudaFuncSetAttribute(px_level1_stream<T, RPL>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                     (int)kMaxDynSmem));
+        SC_CUDA(cudaFuncSetAttribute(px_level1_stream<T, RPL, FULL, CPW>,
+                                     cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kMaxDynSmem));
+        for (int i = 0; i <= 256; ++i) shape_n[i] = 0;
         configured = dev;
     }
+    constexpr int kChunkCols = CPW * kStreamWarps;
+    const size_t chunk = sizeof(T) * (size_t)kChunkCols * n;
+    const int nc = (n + kChunkCols - 1) / kChunkCols;
+    const size_t vecs = sizeof(T) * (size_t)n * 2 * (2 + kStreamWarps);
+    if (!shape_n[n]) {
+        int ring = 0;
+        shape_cta[n] = px1_stream_shape(reinterpret_cast<const void *>(px_level1_stream<T, RPL, FULL, CPW>),
+                                        chunk, nc, vecs, ring);
+        shape_ring[n] = ring;
+        shape_n[n] = 1;
+    }
+    const int per_sm = shape_cta[n], ring = shape_ring[n];
+    if (per_sm == 0) return 1;
+    if ((nblk / (152 * per_sm) + 1) * nc > 2147483647LL) return 1;   // a CTA counts its chunks in an int
+    const size_t smem = px1_stream_head(ring) + (size_t)ring * chunk + vecs;
     const int grid = (int)std::min<i64>(nblk, 152 * per_sm);
-    px_level1_stream<T, RPL><<<grid, kStreamThreads, smem, s>>>(n, nblk, V, EIG, X, Y, kp, alpha, nc, ring,
-                                                                gate, err);
+    px_level1_stream<T, RPL, FULL, CPW><<<grid, kStreamThreads, smem, s>>>(n, nblk, V, EIG, X, Y, kp, alpha,
+                                                                           nc, ring, gate, err);
     SC_CHECK_LAUNCH();
     return 0;
+}
+
+template <class T, int RPL>
+static int launch_px1_stream(int n, i64 nblk, const T *V, const T *EIG, const T *X, T *Y, KernelParams kp,
+                             T alpha, const int *gate, int *err, cudaStream_t s)
+{
+    // four columns per warp halve the per-chunk overhead; two keep the
+    // register footprint of long columns in bounds
+    constexpr int CPW = RPL <= 5 ? 4 : 2;
+    if (n == 32 * RPL)
+        return launch_px1_stream_as<T, RPL, true, CPW>(n, nblk, V, EIG, X, Y, kp, alpha, gate, err, s);
+    return launch_px1_stream_as<T, RPL, false, CPW>(n, nblk, V, EIG, X, Y, kp, alpha, gate, err, s);
 }
 
 template <class T>
 static int launch_px1(int n, i64 nblk, const T *V, const T *EIG, const T *X, T *Y,
                       KernelParams kp, T alpha, const int *gate, int *err, cudaStream_t s)
 {
-    // the streaming kernel: whole blocks fit the ring, chunks and bases 16-byte aligned
-    const size_t chunk = sizeof(T) * (size_t)kChunkCols * n;
-    const int nc = (n + kChunkCols - 1) / kChunkCols;
-    const size_t fixed = sizeof(T) * (size_t)n * (3 + kStreamThreads / 32) + 256 + 64 * 8;
-    // two CTAs per SM when a ring of one block fits in half the shared memory
-    // (one CTA's barriers then overlap the other's copies), else one CTA with
-    // the deepest ring that fits
-    const size_t half = 113 * 1024;
-    const int ring2 = (half > fixed) ? (int)std::min<size_t>((half - fixed) / chunk, (size_t)nc) : 0;
-    const int per_sm = (ring2 >= nc) ? 2 : 1;
-    const int ring = (per_sm == 2) ? ring2 : (int)std::min<size_t>((kMaxDynSmem - fixed) / chunk, (size_t)3 * nc);
+    // the streaming kernel: chunks and bases 16-byte aligned
     const bool aligned = ((reinterpret_cast<uintptr_t>(V) & 15) == 0) && ((sizeof(T) * (size_t)n * n) % 16 == 0);
-    if (n <= 256 && ring >= nc && nblk >= 1 && aligned) {
-        const size_t smem = (((size_t)ring * 8 + 127) & ~(size_t)127) + (size_t)ring * chunk +
-                            sizeof(T) * (size_t)n * (3 + kStreamThreads / 32);
+    if (n >= 1 && n <= 256 && nblk >= 1 && aligned) {
+        int rc = 1;
         switch ((n + 31) / 32) {
-        case 1: return launch_px1_stream<T, 1>(n, nblk, V, EIG, X, Y, kp, alpha, nc, ring, smem, per_sm, gate, err, s);
-        case 2: return launch_px1_stream<T, 2>(n, nblk, V, EIG, X, Y, kp, alpha, nc, ring, smem, per_sm, gate, err, s);
-        case 3: return launch_px1_stream<T, 3>(n, nblk, V, EIG, X, Y, kp, alpha, nc, ring, smem, per_sm, gate, err, s);
-        case 4: return launch_px1_stream<T, 4>(n, nblk, V, EIG, X, Y, kp, alpha, nc, ring, smem, per_sm, gate, err, s);
-        case 5: return launch_px1_stream<T, 5>(n, nblk, V, EIG, X, Y, kp, alpha, nc, ring, smem, per_sm, gate, err, s);
-        case 6: return launch_px1_stream<T, 6>(n, nblk, V, EIG, X, Y, kp, alpha, nc, ring, smem, per_sm, gate, err, s);
-        case 7: return launch_px1_stream<T, 7>(n, nblk, V, EIG, X, Y, kp, alpha, nc, ring, smem, per_sm, gate, err, s);
-        default: return launch_px1_stream<T, 8>(n, nblk, V, EIG, X, Y, kp, alpha, nc, ring, smem, per_sm, gate, err, s);
+        case 1: rc = launch_px1_stream<T, 1>(n, nblk, V, EIG, X, Y, kp, alpha, gate, err, s); break;
+        case 2: rc = launch_px1_stream<T, 2>(n, nblk, V, EIG, X, Y, kp, alpha, gate, err, s); break;
+        case 3: rc = launch_px1_stream<T, 3>(n, nblk, V, EIG, X, Y, kp, alpha, gate, err, s); break;
+        case 4: rc = launch_px1_stream<T, 4>(n, nblk, V, EIG, X, Y, kp, alpha, gate, err, s); break;
+        case 5: rc = launch_px1_stream<T, 5>(n, nblk, V, EIG, X, Y, kp, alpha, gate, err, s); break;
+        case 6: rc = launch_px1_stream<T, 6>(n, nblk, V, EIG, X, Y, kp, alpha, gate, err, s); break;
+        case 7: rc = launch_px1_stream<T, 7>(n, nblk, V, EIG, X, Y, kp, alpha, gate, err, s); break;
+        default: rc = launch_px1_stream<T, 8>(n, nblk, V, EIG, X, Y, kp, alpha, gate, err, s); break;
         }
+        if (rc <= 0) return rc;
     }
     const size_t vec = sizeof(T) * 2 * (size_t)n;
     const size_t mat = sizeof(T) * (size_t)n * n;
