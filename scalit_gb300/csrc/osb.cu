@@ -138,6 +138,19 @@ __host__ __device__ __forceinline__ int batch_items(int mak, int m)
     return (mak - 2 * m) * m + m * m;
 }
 
+// u / m and u % m for 0 <= u < 2^24, 1 <= m and a quotient below 2^20, from
+// rm = 1 / m in FP32: the product is then off by less than one, which the
+// single correction step fixes (integer division costs tens of instructions).
+__device__ __forceinline__ int quot_small(int u, int m, float rm, int &rem)
+{
+    int q = __float2int_rz(__int2float_rn(u) * rm);
+    int r = u - q * m;
+    if (r < 0) { --q; r += m; }
+    else if (r >= m) { ++q; r -= m; }
+    rem = r;
+    return q;
+}
+
 __device__ __forceinline__ int free_row(int f, int a, int i, int m)
 {
     if (f < a) return f;
@@ -151,7 +164,7 @@ __device__ __forceinline__ int free_row(int f, int a, int i, int m)
 template <bool ONE>
 __device__ __forceinline__ void batch_item(double *H, int ndk_, int mak, int ldr, int a, int i, int m,
                                            const double *__restrict__ cs, const double *__restrict__ sn,
-                                           int u, int k)
+                                           int u, int k, float rm)
 {
     using I = typename std::conditional<ONE, int, i64>::type;
     const I ndk = ONE ? 1 : (I)ndk_;
@@ -159,7 +172,8 @@ __device__ __forceinline__ void batch_item(double *H, int ndk_, int mak, int ldr
     const I ld = ndk * (I)ldr;
     double *Hk = H + (ONE ? 0 : k);
     if (u < nfree) {
-        const int f = u / m, t = u - f * m, r = free_row(f, a, i, m);
+        int t;
+        const int f = quot_small(u, m, rm, t), r = free_row(f, a, i, m);
         const int p = a + t, q = a + i + t;
         double *hrp = Hk + ndk * r + ld * p, *hrq = Hk + ndk * r + ld * q;
         double *hpr = Hk + ndk * p + ld * r, *hqr = Hk + ndk * q + ld * r;
@@ -171,7 +185,8 @@ __device__ __forceinline__ void batch_item(double *H, int ndk_, int mak, int ldr
         return;
     }
     u -= nfree;
-    const int t = u / m, t2 = u - t * m;
+    int t2;
+    const int t = quot_small(u, m, rm, t2);
     if (t2 < t) return;
     const int p = a + t, q = a + i + t;
     const double c = cs[t], sv = sn[t];
@@ -207,9 +222,10 @@ __device__ __forceinline__ void batch_item(double *H, int ndk_, int mak, int ldr
 // p_t, q_t of V.
 __device__ __forceinline__ void batch_vitem(double *V, int mak, int a, int i,
                                             const double *__restrict__ cs, const double *__restrict__ sn,
-                                            int u)
+                                            int u, float rmak)
 {
-    const int t = u / mak, row = u - t * mak;
+    int row;
+    const int t = quot_small(u, mak, rmak, row);
     double *vp = V + (i64)(a + t) * mak + row, *vq = V + (i64)(a + i + t) * mak + row;
     const double c = cs[t], sv = sn[t];
     const double x = *vp, y = *vq;
@@ -238,8 +254,12 @@ __global__ void hosb_init_kernel(int blk, int mak, int ndk, const double *__rest
 
 // ------------------------------------------------- schedule 1: CTA/block --
 static constexpr int kMaxBatch = 128;   // m <= MAK / 2
+// Large blocks leave room for one CTA per SM (the block's matrix fills shared
+// memory), so that CTA brings the warps that hide the FP64 pipe's and shared
+// memory's latencies: up to 1024 threads, about one per 16 matrix elements.
+static constexpr int kJacThreads = 1024;
 
-__global__ void __launch_bounds__(kThreads)
+__global__ void __launch_bounds__(kJacThreads, 1)
 jacobi_block_kernel(int bjmax, double bjtol, int blk, int mak, int ndk,
                     double *__restrict__ HOSB, double *__restrict__ VOSB, double *__restrict__ EIG,
                     double *__restrict__ bstats)
@@ -253,6 +273,7 @@ jacobi_block_kernel(int bjmax, double bjtol, int blk, int mak, int ndk,
     const int tid = threadIdx.x, nt = blockDim.x, lane = tid & 31, warp = tid >> 5, nw = nt >> 5;
     const int ldr = (ndk == 1) ? mak + 1 : mak;
     const int col_g = ndk * mak, col_s = ndk * ldr;     // one column of the stack: global / shared
+    const float rmak = 1.0f / (float)mak;
     for (int b = blockIdx.x; b < blk; b += gridDim.x) {
         double *Hg = HOSB + (i64)b * col_g * mak;
         double *V = VOSB + (i64)b * mak * mak;
@@ -301,15 +322,16 @@ jacobi_block_kernel(int bjmax, double bjtol, int blk, int mak, int ndk,
                     }
                     __syncthreads();
                     const int nh = batch_items(mak, m);
+                    const float rm = 1.0f / (float)m;
                     if (ndk == 1) {
-                        for (int u = tid; u < nh; u += nt) batch_item<true>(H, 1, mak, ldr, a, i, m, cs, sn, u, 0);
+                        for (int u = tid; u < nh; u += nt) batch_item<true>(H, 1, mak, ldr, a, i, m, cs, sn, u, 0, rm);
                     } else {
                         for (int e = tid; e < ndk * nh; e += nt) {
                             const int u = e / ndk;
-                            batch_item<false>(H, ndk, mak, ldr, a, i, m, cs, sn, u, e - u * ndk);
+                            batch_item<false>(H, ndk, mak, ldr, a, i, m, cs, sn, u, e - u * ndk, rm);
                         }
                     }
-                    for (int u = tid; u < mak * m; u += nt) batch_vitem(V, mak, a, i, cs, sn, u);
+                    for (int u = tid; u < mak * m; u += nt) batch_vitem(V, mak, a, i, cs, sn, u, rmak);
                     __syncthreads();
                 }
             }
@@ -416,13 +438,14 @@ gpu_batch_rotate_kernel(int mak, int ndk, int a, int i, int m, int blk, int ms, 
                         const SweepState *__restrict__ st)
 {
     const int total = ndk * batch_items(mak, m);     // < 2^31 (checked on the host)
+    const float rm = 1.0f / (float)m;
     for (int b = blockIdx.y; b < blk; b += gridDim.y) {
         if (st[b].done) continue;
         double *H = HOSB + (i64)b * ndk * mak * mak;
         const double *cs = rcs + (i64)b * ms, *sn = rsn + (i64)b * ms;
         for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < total; e += gridDim.x * blockDim.x) {
             const int u = e / ndk;
-            batch_item<false>(H, ndk, mak, mak, a, i, m, cs, sn, u, e - u * ndk);
+            batch_item<false>(H, ndk, mak, mak, a, i, m, cs, sn, u, e - u * ndk, rm);
         }
     }
 }
@@ -504,7 +527,9 @@ int hosbdiag_device(scalit_ctx *c, int bjmax, double bjtol, int blk, int mak, in
         SC_CUDA(cudaFuncSetAttribute(jacobi_block_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                      (int)(225 * 1024)));
         const int grid = blk < 152 * 8 ? blk : 152 * 8;
-        jacobi_block_kernel<<<grid, kThreads, fixed + bytes, s>>>(bjmax, bjtol, blk, mak, ndk, HOSB, VOSB,
+        int nt = 256;
+        while (nt < kJacThreads && nt * 16 < mak * mak) nt *= 2;
+        jacobi_block_kernel<<<grid, nt, fixed + bytes, s>>>(bjmax, bjtol, blk, mak, ndk, HOSB, VOSB,
                                                                   EIG, d_bstats);
         SC_CHECK_LAUNCH();
     } else {

@@ -201,6 +201,114 @@ gemv_sub_f32_kernel(i64 n, int m, const float *VJf, const double *h, double *v)
     }
 }
 
+// Vectorised forms of the two FP32 first-pass kernels, for n % 4 == 0 and
+// 16-byte aligned columns: float4 loads, and the projection takes kProjVecs
+// basis vectors per CTA against one register-resident chunk of wf, so the
+// basis streams at full HBM rate and wf is read once per kProjVecs vectors.
+static constexpr int kProjVecs = 4;
+__global__ void __launch_bounds__(kT)
+gemvt_partial_f32x4_kernel(i64 n, int m, const float *__restrict__ VJf, const float *__restrict__ wf,
+                           double *__restrict__ partial, int nchunk)
+{
+    constexpr int PER = kGemvChunk / kT / 4;             // float4s per thread
+    const int I0 = blockIdx.y * kProjVecs;
+    const i64 k0 = (i64)blockIdx.x * kGemvChunk;
+    float4 wv[PER];
+    #pragma unroll
+    for (int r = 0; r < PER; ++r) {
+        const i64 k = k0 + 4 * ((i64)threadIdx.x + (i64)r * kT);
+        wv[r] = (k < n) ? *reinterpret_cast<const float4 *>(wf + k) : make_float4(0.f, 0.f, 0.f, 0.f);
+    }
+    double a[kProjVecs];
+    #pragma unroll
+    for (int v = 0; v < kProjVecs; ++v) {
+        float af = 0.0f;
+        if (I0 + v < m) {
+            const float *u = VJf + (i64)(I0 + v) * n;
+            #pragma unroll
+            for (int r = 0; r < PER; ++r) {
+                const i64 k = k0 + 4 * ((i64)threadIdx.x + (i64)r * kT);
+                if (k < n) {
+                    const float4 x = *reinterpret_cast<const float4 *>(u + k);
+                    af = fmaf(x.x, wv[r].x, af);
+                    af = fmaf(x.y, wv[r].y, af);
+                    af = fmaf(x.z, wv[r].z, af);
+                    af = fmaf(x.w, wv[r].w, af);
+                }
+            }
+        }
+        a[v] = (double)af;
+    }
+    __shared__ double red[kT / 32][kProjVecs];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    #pragma unroll
+    for (int v = 0; v < kProjVecs; ++v) {
+        #pragma unroll
+        for (int o = 16; o > 0; o >>= 1) a[v] += __shfl_xor_sync(0xffffffffu, a[v], o);
+    }
+    if (lane == 0) {
+        #pragma unroll
+        for (int v = 0; v < kProjVecs; ++v) red[warp][v] = a[v];
+    }
+    __syncthreads();
+    if (threadIdx.x < kProjVecs && I0 + (int)threadIdx.x < m) {
+        double s = 0.0;
+        for (int w2 = 0; w2 < kT / 32; ++w2) s += red[w2][threadIdx.x];
+        partial[(i64)(I0 + threadIdx.x) * nchunk + blockIdx.x] = s;
+    }
+}
+
+// v -= VJf(:, 0:m) h as gemv_sub_f32_kernel (the same four interleaved FP32
+// partial sums per point, so the same result), four points per thread.
+__global__ void __launch_bounds__(kT)
+gemv_sub_f32x4_kernel(i64 n, int m, const float *__restrict__ VJf, const double *__restrict__ h,
+                      double *__restrict__ v)
+{
+    __shared__ float hs[2048];
+    const i64 k = 4 * (blockIdx.x * (i64)blockDim.x + threadIdx.x);
+    for (int i0 = 0; i0 < m; i0 += 2048) {
+        const int cnt = min(2048, m - i0);
+        __syncthreads();
+        for (int i = threadIdx.x; i < cnt; i += blockDim.x) hs[i] = (float)h[i0 + i];
+        __syncthreads();
+        if (k >= n) continue;
+        float a[4][4];
+        #pragma unroll
+        for (int e = 0; e < 4; ++e) a[e][0] = a[e][1] = a[e][2] = a[e][3] = 0.0f;
+        const float *col = VJf + (i64)i0 * n + k;
+        int i = 0;
+        for (; i + 3 < cnt; i += 4) {
+            float4 x[4];
+            #pragma unroll
+            for (int j = 0; j < 4; ++j) x[j] = *reinterpret_cast<const float4 *>(col + (i64)(i + j) * n);
+            #pragma unroll
+            for (int j = 0; j < 4; ++j) {
+                const float hj = hs[i + j];
+                a[0][j] = fmaf(x[j].x, hj, a[0][j]);
+                a[1][j] = fmaf(x[j].y, hj, a[1][j]);
+                a[2][j] = fmaf(x[j].z, hj, a[2][j]);
+                a[3][j] = fmaf(x[j].w, hj, a[3][j]);
+            }
+        }
+        for (; i < cnt; ++i) {
+            const float4 x = *reinterpret_cast<const float4 *>(col + (i64)i * n);
+            const float hj = hs[i];
+            a[0][0] = fmaf(x.x, hj, a[0][0]);
+            a[1][0] = fmaf(x.y, hj, a[1][0]);
+            a[2][0] = fmaf(x.z, hj, a[2][0]);
+            a[3][0] = fmaf(x.w, hj, a[3][0]);
+        }
+        double2 *vp = reinterpret_cast<double2 *>(v + k);
+        double2 v0 = vp[0], v1 = vp[1];
+        v0.x -= (double)((a[0][0] + a[0][1]) + (a[0][2] + a[0][3]));
+        v0.y -= (double)((a[1][0] + a[1][1]) + (a[1][2] + a[1][3]));
+        v1.x -= (double)((a[2][0] + a[2][1]) + (a[2][2] + a[2][3]));
+        v1.y -= (double)((a[3][0] + a[3][1]) + (a[3][2] + a[3][3]));
+        vp[0] = v0;
+        vp[1] = v1;
+    }
+}
+
 __global__ void gemvt_final_kernel(int m, int nchunk, const double *partial, double *HMAT, int ld,
                                    int J)
 {
@@ -435,6 +543,9 @@ int pist_core(scalit_ctx *c, i64 N, const scalit_pist_params *p, const double *d
         }
     }
     auto vcolf = [&](int J1) { return VJf + (i64)(J1 - 1) * N; };
+    // float4 / double2 access of every column in the mixed first pass
+    const bool vec4 = VJf && N % 4 == 0 && ((reinterpret_cast<uintptr_t>(VJf) | reinterpret_cast<uintptr_t>(VJ) |
+                                             reinterpret_cast<uintptr_t>(Wf)) & 15) == 0;
     SC_CUDA(cudaMallocAsync(&HMAT, sizeof(double) * (size_t)MM * MM, s));
     SC_CUDA(cudaMallocAsync(&A, sizeof(double) * (size_t)MM * MM, s));
     SC_CUDA(cudaMallocAsync(&EV, sizeof(double) * (size_t)MM, s));
@@ -485,9 +596,18 @@ int pist_core(scalit_ctx *c, i64 N, const scalit_pist_params *p, const double *d
                 if (pass == 0 && p->orth == 2) {
                     int r2 = to_f32(v, Wf, N, s);
                     if (r2) return r2;
-                    gemvt_partial_f32_kernel<<<dim3(nchunk, J), kT, 0, s>>>(N, VJf, Wf, partial, nchunk);
+                    if (vec4) {
+                        gemvt_partial_f32x4_kernel<<<dim3(nchunk, (J + kProjVecs - 1) / kProjVecs), kT, 0, s>>>(
+                            N, J, VJf, Wf, partial, nchunk);
+                    } else {
+                        gemvt_partial_f32_kernel<<<dim3(nchunk, J), kT, 0, s>>>(N, VJf, Wf, partial, nchunk);
+                    }
                     gemvt_vec_kernel<<<(J + 127) / 128, 128, 0, s>>>(J, nchunk, partial, D);
-                    gemv_sub_f32_kernel<<<gr, kT, 0, s>>>(N, J, VJf, D, v);
+                    if (vec4) {
+                        gemv_sub_f32x4_kernel<<<(int)((N / 4 + kT - 1) / kT), kT, 0, s>>>(N, J, VJf, D, v);
+                    } else {
+                        gemv_sub_f32_kernel<<<gr, kT, 0, s>>>(N, J, VJf, D, v);
+                    }
                     continue;
                 }
                 gemvt_partial_kernel<<<dim3(nchunk, J), kT, 0, s>>>(N, J, VJ, v, partial, nchunk);
