@@ -29,6 +29,7 @@
 #include "internal.cuh"
 
 #include <algorithm>
+#include <cstdlib>
 #include <chrono>
 #include <cmath>
 #include <type_traits>
@@ -256,7 +257,7 @@ __global__ void hosb_init_kernel(int blk, int mak, int ndk, const double *__rest
 static constexpr int kMaxBatch = 128;   // m <= MAK / 2
 // Large blocks leave room for one CTA per SM (the block's matrix fills shared
 // memory), so that CTA brings the warps that hide the FP64 pipe's and shared
-// memory's latencies: up to 1024 threads, about one per 16 matrix elements.
+// memory's latencies: up to 1024 threads.
 static constexpr int kJacThreads = 1024;
 
 __global__ void __launch_bounds__(kJacThreads, 1)
@@ -269,7 +270,9 @@ jacobi_block_kernel(int bjmax, double bjtol, int blk, int mak, int ndk,
     double *cs = smem + 96;             // kMaxBatch
     double *sn = cs + kMaxBatch;        // kMaxBatch
     double *abc_c = sn + kMaxBatch;     // kMaxBatch (C sums of a stacked batch)
-    double *H = abc_c + kMaxBatch;      // the block's stacked matrices, column stride ldr
+    double *cs_v = abc_c + kMaxBatch;   // kMaxBatch: the previous batch's angles, for
+    double *sn_v = cs_v + kMaxBatch;    // kMaxBatch  its deferred V update (one matrix)
+    double *H = sn_v + kMaxBatch;       // the block's stacked matrices, column stride ldr
     const int tid = threadIdx.x, nt = blockDim.x, lane = tid & 31, warp = tid >> 5, nw = nt >> 5;
     const int ldr = (ndk == 1) ? mak + 1 : mak;
     const int col_g = ndk * mak, col_s = ndk * ldr;     // one column of the stack: global / shared
@@ -285,6 +288,10 @@ jacobi_block_kernel(int bjmax, double bjtol, int blk, int mak, int ndk,
         const double initye = block_offdiag(H, ndk, mak, ldr, red);
         double ye = initye, dye = initye;
         int k = 1;
+        // one matrix: a batch's V update waits for the next batch's angle
+        // phase, so the FP64 pipe works on V while a few threads run the
+        // angles' divisions and square roots (V does not feed the angles)
+        int mv = 0, av = 0, iv = 0;
         while (fabs(dye) > initye * bjtol && k <= bjmax) {
             for (int i = 1; i <= mak - 1; ++i) {
                 for (int a = 0; a < mak - i; a += i) {
@@ -293,11 +300,15 @@ jacobi_block_kernel(int bjmax, double bjtol, int blk, int mak, int ndk,
                     // roots and divisions then fill whole warps); with a stack of
                     // matrices one warp per plane first sums A, B, C over it
                     if (ndk == 1) {
-                        for (int t = tid; t < m; t += nt) {
-                            const int p = a + t, q = a + i + t;
+                        const int t0 = (m + 31) & ~31;          // warps past the angle threads
+                        if (tid < m) {
+                            const int p = a + tid, q = a + i + tid;
                             const double o = H[p + ldr * q];
                             const double d = 0.5 * H[p + ldr * p] - 0.5 * H[q + ldr * q];
-                            jacobi_angle(o * o, 2.0 * (o * d), d * d, cs + t, sn + t);
+                            jacobi_angle(o * o, 2.0 * (o * d), d * d, cs + tid, sn + tid);
+                        } else if (tid >= t0) {                 // t0 <= kMaxBatch < nt
+                            for (int u = tid - t0; u < mak * mv; u += nt - t0)
+                                batch_vitem(V, mak, av, iv, cs_v, sn_v, u, rmak);
                         }
                     } else {
                         for (int t = warp; t < m; t += nw) {
@@ -325,13 +336,16 @@ jacobi_block_kernel(int bjmax, double bjtol, int blk, int mak, int ndk,
                     const float rm = 1.0f / (float)m;
                     if (ndk == 1) {
                         for (int u = tid; u < nh; u += nt) batch_item<true>(H, 1, mak, ldr, a, i, m, cs, sn, u, 0, rm);
+                        // keep this batch's angles for its V update
+                        if (tid < m) { cs_v[tid] = cs[tid]; sn_v[tid] = sn[tid]; }
+                        mv = m; av = a; iv = i;
                     } else {
                         for (int e = tid; e < ndk * nh; e += nt) {
                             const int u = e / ndk;
                             batch_item<false>(H, ndk, mak, ldr, a, i, m, cs, sn, u, e - u * ndk, rm);
                         }
+                        for (int u = tid; u < mak * m; u += nt) batch_vitem(V, mak, a, i, cs, sn, u, rmak);
                     }
-                    for (int u = tid; u < mak * m; u += nt) batch_vitem(V, mak, a, i, cs, sn, u, rmak);
                     __syncthreads();
                 }
             }
@@ -339,6 +353,8 @@ jacobi_block_kernel(int bjmax, double bjtol, int blk, int mak, int ndk,
             ye = ye + dye;
             k = k + 1;
         }
+        // the last batch's V update
+        for (int u = tid; u < mak * mv; u += nt) batch_vitem(V, mak, av, iv, cs_v, sn_v, u, rmak);
         const double sd = block_sumdiag(H, ndk, mak, ldr, red);
         __syncthreads();
         for (int e = tid; e < ndk * mak; e += nt) {
@@ -520,15 +536,28 @@ int hosbdiag_device(scalit_ctx *c, int bjmax, double bjtol, int blk, int mak, in
     double *d_bstats = nullptr;
     SC_CUDA(cudaMallocAsync(&d_bstats, sizeof(double) * 3 * (size_t)blk, s));
     int rc = 0;
-    const size_t fixed = (96 + 3 * kMaxBatch) * sizeof(double);
+    const size_t fixed = (96 + 5 * kMaxBatch) * sizeof(double);
     const size_t bytes = sizeof(double) * (size_t)ndk * mak * (ndk == 1 ? mak + 1 : mak);
     const bool per_block = (bytes + fixed <= 225 * 1024) && mak / 2 <= kMaxBatch;
     if (per_block) {
         SC_CUDA(cudaFuncSetAttribute(jacobi_block_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                      (int)(225 * 1024)));
         const int grid = blk < 152 * 8 ? blk : 152 * 8;
+        // threads: about 512 per SM shared by the CTAs that fit its shared
+        // memory -- several blocks in flight hide the per-batch barriers and
+        // angle latencies better than more warps in one.  Measured on GB300:
+        // 96 x 96 blocks (two CTAs per SM) 0.36 s at 256 threads, 0.53 s at
+        // 1024; 160 x 160 blocks (one) 5.39 s at 256, 4.76 s at 512, 4.89 s
+        // at 1024.
+        const int ctas = std::max(1, (int)((228 * 1024) / (fixed + bytes + 1024)));
         int nt = 256;
-        while (nt < kJacThreads && nt * 16 < mak * mak) nt *= 2;
+        while (nt < kJacThreads && 2 * nt * ctas <= 512) nt *= 2;
+        static const int forced = [] {                 // SCALIT_JAC_THREADS: a tuning override
+            const char *e = getenv("SCALIT_JAC_THREADS");
+            const int v = e ? atoi(e) : 0;
+            return (v >= 256 && v <= kJacThreads && v % 32 == 0) ? v : 0;   // above kMaxBatch
+        }();
+        if (forced) nt = forced;
         jacobi_block_kernel<<<grid, nt, fixed + bytes, s>>>(bjmax, bjtol, blk, mak, ndk, HOSB, VOSB,
                                                                   EIG, d_bstats);
         SC_CHECK_LAUNCH();
