@@ -242,6 +242,15 @@ def run_reference(args):
 def pist_leg(workload, levels, device, capi, hm):
     """Wall time from the preconditioner build to converged eigenvalues, with
     FP64 and with FP32 QMR inner solves (basis, HMAT and Ritz values in FP64)."""
+    # untimed warm-up on the small grid: the first solve of a process loads
+    # the solver library's kernels (lazy module loading, ~0.9 s), which would
+    # otherwise land on whichever arm runs first
+    pw = hm.workload("tri-24x32x20")
+    for prec, orth in ((capi.PREC_FP64, 1), (capi.PREC_FP32, 2)):
+        with capi.Context.from_problem(pw, e0=float(pw.RES.min()), device=device) as ctx:
+            ctx.build_osb(20, 1e-4)
+            ctx.pist(np.random.default_rng(0).random(pw.N), 20, float(pw.RES.min()), 1e-11, m_max=400,
+                     qmr_max=2000, qmr_tol=1e-4, precision=prec, orth=orth, residuals=True)
     p = hm.workload(workload)
     e0 = float(p.RES.min())
     x0 = np.random.default_rng(0).random(p.N)

@@ -199,6 +199,8 @@ int tc_level_apply(const scalit_ctx *c, int level, const double *X, double *Y, i
                    const double *diagV, double shift, double alpha, const int *gate, cudaStream_t s,
                    int nvec, const double *shiftv = nullptr, const int *vgate = nullptr, int vstride = 0);
 int tc_check_error(scalit_ctx *c);
+int tc_gemm_f64(const scalit_ctx *c, int M, int N, int K, const double *A, i64 lda, const double *B, i64 ldb,
+                double *C, i64 ldc, cudaStream_t s);
 
 // ------------------------------------------------------------- OSB build --
 int osb_build(scalit_ctx *c, int bjmax, double bjtol, double *stats);

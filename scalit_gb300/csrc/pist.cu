@@ -463,14 +463,20 @@ static int ritz_vectors(scalit_ctx *c, i64 N, const double *VJ, const double *HM
     SC_CUDA(cudaMallocAsync(&Psi, sizeof(double) * (size_t)N * Msel, s));
     SC_CUDA(cudaMemcpyAsync(didx, idx.data(), sizeof(int) * Msel, cudaMemcpyHostToDevice, s));
     select_columns_kernel<<<egrid((i64)num * Msel), kT, 0, s>>>(num, Msel, A, didx, Ysel);
-    GemmArgs<double> g{};
-    g.M = (int)N; g.N = Msel; g.K = num; g.batch = 1;
-    g.Mi = N; g.s1 = 1; g.s2 = 0;
-    g.A = VJ; g.a_sk = N;                 // A(p, k) = VJ[p + N k]
-    g.B = Ysel; g.b_sk = 1; g.b_sn = num; // B(k, j) = Ysel[k + num j]
-    g.C = Psi; g.c_sn = N;
-    g.alpha = 1.0;
-    int rc = launch_gemm<double>(g, s);
+    int rc = 0;
+    if (c->fp64_mode == SCALIT_FP64_TENSOR && N <= 2147483647LL) {
+        // the Ritz vectors on the digit engine (a 2 N num Msel FLOP product)
+        rc = tc_gemm_f64(c, (int)N, Msel, num, VJ, N, Ysel, num, Psi, N, s);
+    } else {
+        GemmArgs<double> g{};
+        g.M = (int)N; g.N = Msel; g.K = num; g.batch = 1;
+        g.Mi = N; g.s1 = 1; g.s2 = 0;
+        g.A = VJ; g.a_sk = N;                 // A(p, k) = VJ[p + N k]
+        g.B = Ysel; g.b_sk = 1; g.b_sn = num; // B(k, j) = Ysel[k + num j]
+        g.C = Psi; g.c_sn = N;
+        g.alpha = 1.0;
+        rc = launch_gemm<double>(g, s);
+    }
     if (!rc && out_host)
         SC_CUDA(cudaMemcpyAsync(out_host, Psi, sizeof(double) * (size_t)N * Msel, cudaMemcpyDeviceToHost, s));
     if (!rc && resid) {

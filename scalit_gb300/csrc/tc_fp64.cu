@@ -617,6 +617,82 @@ int tc_level_apply(const scalit_ctx *c, int l, const double *X, double *Y, int a
     return 0;
 }
 
+// Digit planes of B(k, n) = Bm[k0 + k + ldb n] for k < kc (a K chunk of a
+// general K x N matrix), one thread per column n: the chunk's column exponent,
+// then the digits, in the layout of cut_level_matrix.
+__global__ void cut_gen_kernel(int kc, int N, int NT, int KS, const double *__restrict__ Bm, i64 ldb,
+                               uint16_t *__restrict__ dig, int *__restrict__ exps)
+{
+    const int n = blockIdx.x * blockDim.x + threadIdx.x;
+    if (n >= N) return;
+    const double *col = Bm + (i64)n * ldb;
+    double mx = 0.0;
+    for (int k = 0; k < kc; ++k) mx = fmax(mx, fabs(col[k]));
+    int e = 0;
+    if (mx > 0.0) frexp(mx, &e);
+    exps[n] = e;
+    const int tile = n / NT, nn = n % NT;
+    for (int k = 0; k < kc; ++k) {
+        double r = ldexp(col[k], 7 - e);
+        const int ks = k / 16, kk = k % 16;
+        #pragma unroll
+        for (int t = 0; t < kDigits; ++t) {
+            const double d = trunc(r);
+            r = (r - d) * 128.0;
+            const size_t base = (((size_t)tile * KS + ks) * kDigits + t) * (size_t)NT * 16;
+            const size_t off = (size_t)(nn >> 3) * 128 + (size_t)(kk >> 3) * 64 + (size_t)(nn & 7) * 8 + (kk & 7);
+            dig[base + off] = __bfloat16_as_ushort(__float2bfloat16_rn((float)d));   // |d| <= 127: exact
+        }
+    }
+}
+
+// C (M x N, column stride ldc) = A (M x K, column stride lda) B (K x N, column
+// stride ldb), all FP64, on the digit engine: K in chunks of at most 256 (the
+// FP32 groups' exactness bound), each chunk's product accumulated into C.
+int tc_gemm_f64(const scalit_ctx *c, int M, int N, int K, const double *A, i64 lda, const double *B, i64 ldb,
+                double *C, i64 ldc, cudaStream_t s)
+{
+    if (M <= 0 || N <= 0 || K <= 0) return 0;
+    const int NT = std::min(64, (N + 15) / 16 * 16);
+    const int ntiles = (N + NT - 1) / NT;
+    const int kcmax = std::min(K, 256);
+    const int KSmax = (kcmax + 15) / 16;
+    const size_t ndig = (size_t)ntiles * KSmax * kDigits * NT * 16;
+    const size_t nexp = (size_t)ntiles * NT;
+    uint16_t *dig = nullptr;
+    int *exps = nullptr;
+    SC_CUDA(cudaMallocAsync(&dig, ndig * sizeof(uint16_t), s));
+    SC_CUDA(cudaMallocAsync(&exps, nexp * sizeof(int), s));
+    const size_t smem = 2 * (size_t)kAStepBytes + 2 * (size_t)kDigits * NT * 32 + (size_t)kStages * kSlab * 8 +
+                        64 + 3072;
+    const size_t smem_req = std::max(smem, (size_t)(116 * 1024));
+    int rc = 0;
+    if (cudaFuncSetAttribute(tc_level_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_req) !=
+        cudaSuccess) { set_error("tc_gemm_f64: shared memory attribute"); rc = SCALIT_ECUDA; }
+    for (int k0 = 0; k0 < K && !rc; k0 += 256) {
+        const int kc = std::min(256, K - k0);
+        const int KS = (kc + 15) / 16;
+        if (cudaMemsetAsync(dig, 0, ndig * sizeof(uint16_t), s) != cudaSuccess ||
+            cudaMemsetAsync(exps, 0, nexp * sizeof(int), s) != cudaSuccess) { rc = SCALIT_ECUDA; break; }
+        cut_gen_kernel<<<(N + 127) / 128, 128, 0, s>>>(kc, N, NT, KS, B + k0, ldb, dig, exps);
+        TcArgs g{};
+        g.M = M; g.N = N; g.K = kc; g.KS = KS; g.NT = NT;
+        g.Mi = M; g.s1 = 1; g.s2 = 0; g.a_sk = lda; g.c_sn = ldc;
+        g.A = A + (i64)k0 * lda; g.a_sz = 0;
+        g.C = C; g.c_sz = 0;
+        g.accumulate = k0 > 0;
+        g.alpha = 1.0;
+        g.err = c->tc_err;
+        g.bdig = reinterpret_cast<const uint4 *>(dig);
+        g.bexp = exps;
+        tc_level_kernel<<<dim3((M + kBM - 1) / kBM, ntiles, 1), kBlockTC, smem_req, s>>>(g);
+        if (cudaGetLastError() != cudaSuccess) { set_error("tc_gemm_f64 launch"); rc = SCALIT_ECUDA; }
+    }
+    cudaFreeAsync(dig, s);
+    cudaFreeAsync(exps, s);
+    return rc;
+}
+
 int tc_check_error(scalit_ctx *c)
 {
     if (!c->tc_err) return 0;

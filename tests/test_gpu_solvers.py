@@ -184,6 +184,12 @@ def test_pist_residuals_match_host_check(lib, orc, c0):
     host = np.array([np.linalg.norm(ref.hx(psi[k], 0) - eig[k] * psi[k]) for k in range(20)])
     np.testing.assert_allclose(info["resid"], host, rtol=1e-6, atol=1e-14)
     assert info["resid"].max() < 1e-3
+    # the Ritz vectors (basis x eigenvectors, an FP64 product on the digit
+    # engine) are orthonormal and reproduce the eigenvalues to FP64 accuracy
+    gram = psi @ psi.T
+    assert np.abs(gram - np.eye(len(psi))).max() < 1e-12
+    rq = np.array([psi[k] @ ref.hx(psi[k], 0) for k in range(20)])
+    np.testing.assert_allclose(rq, eig, rtol=1e-12, atol=0)
 
 
 def test_pist_mixed_tensor_fp32(lib, orc, c0):
