@@ -122,24 +122,36 @@ gemm_kernel(GemmArgs<T> g)
         }
     }
 
-    // Epilogue.
+    // Epilogue: every load (diagonal, accumulated output) before any store, so
+    // the thread's TM x TN loads are in flight together instead of one
+    // round trip per output (a store to C could alias a later load).
     const i64 cs1 = g.c_s1 >= 0 ? g.c_s1 : g.s1, cs2 = g.c_s2 >= 0 ? g.c_s2 : g.s2;
+    i64 moffs[TM];
     #pragma unroll
     for (int i = 0; i < TM; ++i) {
         const int m = m0 + tm + i;
-        if (m >= g.M) continue;
-        const i64 mi = m % g.Mi;
-        const i64 moff = mi * cs1 + (i64)(m / g.Mi) * cs2;
+        const i64 mi = m < g.M ? m % g.Mi : 0;
+        moffs[i] = mi * cs1 + (i64)(m < g.M ? m / g.Mi : 0) * cs2;
         const T sc = g.rowscale ? g.rowscale[mi] * g.alpha : g.alpha;
         #pragma unroll
         for (int j = 0; j < TN; ++j) {
             const int n = n0 + tn + j;
-            if (n >= g.N) continue;
-            const i64 p = moff + (i64)n * g.c_sn;
+            if (m >= g.M || n >= g.N) continue;
+            const i64 p = moffs[i] + (i64)n * g.c_sn;
             T v = sc * acc[i][j];
             if (g.diagV) v = fma(g.alpha * (g.diagV[p] - (g.shiftv ? g.shiftv[z] : g.shift)), g.diagX[p + (i64)z * g.dx_sz], v);
             if (g.accumulate) v += Cp[p];
-            Cp[p] = v;
+            acc[i][j] = v;
+        }
+    }
+    #pragma unroll
+    for (int i = 0; i < TM; ++i) {
+        const int m = m0 + tm + i;
+        #pragma unroll
+        for (int j = 0; j < TN; ++j) {
+            const int n = n0 + tn + j;
+            if (m >= g.M || n >= g.N) continue;
+            Cp[moffs[i] + (i64)n * g.c_sn] = acc[i][j];
         }
     }
 }

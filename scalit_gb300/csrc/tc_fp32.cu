@@ -33,7 +33,7 @@ static constexpr int kBM32 = 128;
 static constexpr int kThreads32 = 512;                      // cutting threads: four per grid row
 static constexpr int kBlock32 = 544;                        // plus one warp that issues the MMAs
 static constexpr int kStages32 = 6;
-static constexpr int kSlab32 = kBM32 * 17;                 // floats per slab stage (row stride 17)
+static constexpr int kSlab32 = kBM32 * 20;                 // floats per slab stage (row stride 20)
 static constexpr int kAStep32 = 2 * kBM32 * 16 * 2;        // hi + lo planes of 128 x 16 BF16
 
 struct Tc32Args {
@@ -53,6 +53,7 @@ struct Tc32Args {
     int vgate_stride;
     const int *gate;
     int *err;
+    int vec;               // 16-byte operand loads (aligned rows / row groups, K % 4 == 0)
     const uint4 *bsplit;   // [blocks][ntile][ks][hi, lo][NT x 16 BF16, canonical]
     int tpb;               // > 0: per-block B, tpb M tiles per block of Mi rows
     i64 b_blk;             // uint4 stride between blocks' planes
@@ -72,6 +73,7 @@ tc32_level_kernel(Tc32Args g)
     uint64_t *mbar = reinterpret_cast<uint64_t *>(slabs + kStages32 * kSlab32);   // MMAs of a buffer done
     uint64_t *cutb = mbar + 2;                                                      // a buffer's planes cut
     uint32_t *tslot = reinterpret_cast<uint32_t *>(mbar + 4);
+    uint64_t *bready = mbar + 5;                                                    // the B tile landed
 
     const int tid = threadIdx.x, warp = tid >> 5;
     const int ntile = blockIdx.y, z = blockIdx.z;
@@ -100,7 +102,13 @@ tc32_level_kernel(Tc32Args g)
         mbar_init(&mbar[1], 1);
         mbar_init(&cutb[0], kThreads32);
         mbar_init(&cutb[1], kThreads32);
+        mbar_init(bready, 1);
         mbar_init_fence();
+        // the whole B tile (already split, canonical layout) by bulk copies,
+        // one per K step, overlapping the grid operand's first loads
+        const unsigned char *bsrc_b = reinterpret_cast<const unsigned char *>(bsrc + (i64)ntile * KS * (bstep / 16));
+        mbar_arrive_expect_tx(bready, (uint32_t)(KS * bstep));
+        for (int ks = 0; ks < KS; ++ks) bulk_g2s(Bs + (size_t)ks * bstep, bsrc_b + (size_t)ks * bstep, bstep, bready);
     }
     if (warp == kThreads32 / 32) {
         // the MMA warp: per K step wait for the cut planes, issue the three
@@ -110,7 +118,8 @@ tc32_level_kernel(Tc32Args g)
         fence_after();
         const uint32_t tbase = *tslot;
         const uint32_t idesc = idesc_bf16(NT);
-        for (int ks = 0; ks < KS; ++ks) {
+        const bool bok = mbar_wait(bready, 0);
+        for (int ks = 0; ks < KS && bok; ++ks) {
             const int buf = ks & 1;
             if (!mbar_wait(&cutb[buf], (uint32_t)((ks >> 1) & 1))) break;
             fence_after();
@@ -132,12 +141,6 @@ tc32_level_kernel(Tc32Args g)
         __syncthreads();
         return;   // warp 0 frees the TMEM
     }
-    // the whole B tile, already split and in the canonical layout
-    {
-        const uint4 *src = bsrc + (i64)ntile * KS * (bstep / 16);
-        uint4 *dst = reinterpret_cast<uint4 *>(Bs);
-        for (int i = tid; i < KS * (bstep / 16); i += kThreads32) dst[i] = src[i];
-    }
 
     const int row = tid & (kBM32 - 1), q = tid >> 7;
     const int m = m0 + row;
@@ -153,8 +156,29 @@ tc32_level_kernel(Tc32Args g)
         lvalid[i] = mm < mlim;
         lmoff[i] = lvalid[i] ? (i64)(mm % g.Mi) * g.s1 + (i64)(mm / g.Mi) * g.s2 : 0;
     }
+    // 16-byte loads: K-major rows take four consecutive k per thread, M-major
+    // slabs four consecutive rows (one block: Mi % 4 == 0) at one k
+    const int vr = rowc ? (tid >> 2) : 4 * (tid & 31);
+    const int vj = rowc ? 4 * (tid & 3) : (tid >> 5);
+    bool vvalid = false;
+    i64 vmoff = 0;
+    if (g.vec) {
+        const int mm = m0 + vr;
+        vvalid = mm < mlim;
+        vmoff = vvalid ? (i64)(mm % g.Mi) * g.s1 + (i64)(mm / g.Mi) * g.s2 : 0;
+    }
     auto issue = [&](int t) {
-        if (t < KS) {
+        if (t < KS && g.vec) {
+            float *st = slabs + (t % kStages32) * kSlab32;
+            const int k = t * 16 + vj;
+            float *dst = rowc ? st + vr * 20 + vj : st + vj * kBM32 + vr;
+            if (vvalid && k < g.K) {
+                const float *src = A + vmoff + (i64)k * g.a_sk;
+                asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" :: "r"(smem_addr(dst)), "l"(src) : "memory");
+            } else {
+                *reinterpret_cast<float4 *>(dst) = make_float4(0.f, 0.f, 0.f, 0.f);
+            }
+        } else if (t < KS) {
             float *st = slabs + (t % kStages32) * kSlab32;
             #pragma unroll
             for (int i = 0; i < 4; ++i) {
@@ -162,7 +186,7 @@ tc32_level_kernel(Tc32Args g)
                 if (rowc) { j = tid & 15; r = (tid >> 4) + 32 * i; }
                 else { r = row; j = q + 4 * i; }
                 const int k = t * 16 + j;
-                float *dst = rowc ? st + r * 17 + j : st + j * kBM32 + r;
+                float *dst = rowc ? st + r * 20 + j : st + j * kBM32 + r;
                 if (lvalid[i] && k < g.K) {
                     const float *src = A + lmoff[i] + (i64)k * g.a_sk;
                     asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" :: "r"(smem_addr(dst)), "l"(src) : "memory");
@@ -202,8 +226,8 @@ tc32_level_kernel(Tc32Args g)
         #pragma unroll
         for (int jj = 0; jj < 4; jj += 2) {
             const int j0 = q * 4 + jj;
-            const float x0 = rowc ? st[row * 17 + j0] : st[j0 * kBM32 + row];
-            const float x1 = rowc ? st[row * 17 + j0 + 1] : st[(j0 + 1) * kBM32 + row];
+            const float x0 = rowc ? st[row * 20 + j0] : st[j0 * kBM32 + row];
+            const float x1 = rowc ? st[row * 20 + j0 + 1] : st[(j0 + 1) * kBM32 + row];
             const __nv_bfloat16 h0 = __float2bfloat16_rn(x0), h1 = __float2bfloat16_rn(x1);
             const __nv_bfloat16 l0 = __float2bfloat16_rn(x0 - __bfloat162float(h0));
             const __nv_bfloat16 l1 = __float2bfloat16_rn(x1 - __bfloat162float(h1));
@@ -232,23 +256,40 @@ tc32_level_kernel(Tc32Args g)
         const uint32_t lane_base = (uint32_t)((warp & 3) * 32) << 16;
         const int cq = NT / 4;
         const int cbeg = (warp >> 2) * cq, cend = cbeg + cq;
-        for (int c0 = cbeg; c0 < cend; c0 += 4) {
-            float v[4];
-            tmem_ld4(tbase + lane_base + (uint32_t)c0, v);
+        // 8 columns at a time: two TMEM loads, one wait, then every global
+        // load of the group (diagonal, accumulated output) before any store
+        for (int c0 = cbeg; c0 < cend; c0 += 8) {
+            float v[2][4];
+            #pragma unroll
+            for (int q = 0; q < 2; ++q)
+                if (c0 + 4 * q < cend) tmem_ld4(tbase + lane_base + (uint32_t)(c0 + 4 * q), v[q]);   // warp-uniform
             asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
             if (!mvalid) continue;
+            float outv[2][4];
             #pragma unroll
-            for (int j = 0; j < 4; ++j) {
-                const int n = ntile * NT + c0 + j;
-                if (n >= g.N) continue;
-                const i64 p = moff + (i64)n * g.c_sn;
-                float out = sc * v[j];
-                if (g.diagV) out = fmaf(g.alpha * (g.diagV[p] - shift), g.diagX[p + (i64)z * g.dx_sz], out);
-                if (g.accumulate) out += C[p];
-                C[p] = out;
-            }
+            for (int q = 0; q < 2; ++q)
+                #pragma unroll
+                for (int j = 0; j < 4; ++j) {
+                    const int n = ntile * NT + c0 + 4 * q + j;
+                    if (c0 + 4 * q >= cend || n >= g.N) continue;
+                    const i64 p = moff + (i64)n * g.c_sn;
+                    float out = sc * v[q][j];
+                    if (g.diagV) out = fmaf(g.alpha * (g.diagV[p] - shift), g.diagX[p + (i64)z * g.dx_sz], out);
+                    if (g.accumulate) out += C[p];
+                    outv[q][j] = out;
+                }
+            #pragma unroll
+            for (int q = 0; q < 2; ++q)
+                #pragma unroll
+                for (int j = 0; j < 4; ++j) {
+                    const int n = ntile * NT + c0 + 4 * q + j;
+                    if (c0 + 4 * q < cend && n < g.N) C[moff + (i64)n * g.c_sn] = outv[q][j];
+                }
         }
     }
+    // the B copies have landed before the CTA's shared memory goes (they
+    // have on every path that issued an MMA; this covers an early stop)
+    if (tid == 0) mbar_wait(bready, 0);
     fence_before();
     __syncthreads();
     if (warp == 0)
@@ -278,11 +319,25 @@ __global__ void split_b_kernel(int nout, int NT, int ntiles, int KS, int blk, co
     out[base + (size_t)NT * 16 + off] = __bfloat16_as_ushort(l);
 }
 
+// One N tile holds every output column up to 176 (the grid operand is then
+// loaded and split once; B, the ring and the A buffers fit one CTA's shared
+// memory); wider levels take two tiles.
 static void plan_dims(int nout, int &NT, int &ntiles, int &KS)
 {
-    NT = std::min(64, (nout + 15) / 16 * 16);
+    const int n16 = (nout + 15) / 16 * 16;
+    NT = n16 <= 176 ? n16 : ((nout + 1) / 2 + 15) / 16 * 16;
     ntiles = (nout + NT - 1) / NT;
     KS = (nout + 15) / 16;
+}
+
+// 16-byte loads of the grid operand: K-major rows (a_sk == 1) need K and the
+// row stride a multiple of 4; M-major slabs need blocks of a multiple of 4
+// rows and 4-aligned strides; both a 16-byte aligned base and vector stride.
+static int vec_ok(const Tc32Args &g)
+{
+    if ((reinterpret_cast<uintptr_t>(g.A) & 15) || (g.a_sz % 4)) return 0;
+    if (g.a_sk == 1) return (g.K % 4 == 0 && g.s1 % 4 == 0 && g.s2 % 4 == 0) ? 1 : 0;
+    return (g.s1 == 1 && g.Mi % 4 == 0 && g.s2 % 4 == 0 && g.a_sk % 4 == 0) ? 1 : 0;
 }
 
 static int split_into(scalit_ctx *c, TcLevelData &t, int nout, int blk, const float *Mt, int transpose)
@@ -351,7 +406,9 @@ static int launch32(const Tc32Args &g, i64 gx, int ntiles, int nvec, cudaStream_
         configured = dev;
     }
     if (gx > 2147483647LL || nvec > 65535) { set_error("tensor-core FP32 grid too large"); return SCALIT_EINVAL; }
-    tc32_level_kernel<<<dim3((unsigned)gx, ntiles, nvec), kBlock32, smem, s>>>(g);
+    Tc32Args gv = g;
+    gv.vec = vec_ok(g);
+    tc32_level_kernel<<<dim3((unsigned)gx, ntiles, nvec), kBlock32, smem, s>>>(gv);
     SC_CHECK_LAUNCH();
     return 0;
 }

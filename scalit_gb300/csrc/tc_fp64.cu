@@ -342,6 +342,9 @@ tc_level_kernel(TcArgs g)
             for (int gq = 0; gq < kGroups; ++gq) tmem_ld4(tbase + lane_base + (uint32_t)(gq * NT + c0), gv[gq]);
             asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
             if (!mvalid) continue;
+            // the four outputs with every load (exponents, diagonal,
+            // accumulated output) issued before the first store
+            double outv[4];
             #pragma unroll
             for (int j = 0; j < 4; ++j) {
                 const int n = ntile * NT + c0 + j;
@@ -358,7 +361,12 @@ tc_level_kernel(TcArgs g)
                 if (g.diagV) out = fma(g.alpha * (g.diagV[p] - (g.shiftv ? g.shiftv[z] : g.shift)),
                                        g.diagX[p + (i64)z * g.dx_sz], out);
                 if (g.accumulate) out += C[p];
-                C[p] = out;
+                outv[j] = out;
+            }
+            #pragma unroll
+            for (int j = 0; j < 4; ++j) {
+                const int n = ntile * NT + c0 + j;
+                if (n < g.N) C[moff + (i64)n * g.c_sn] = outv[j];
             }
         }
     }
