@@ -52,6 +52,10 @@ def parse():
     ap.add_argument("--pist-workload", default="tri-160x160x120",
                     help="grid of the PIST leg ('none' skips it)")
     ap.add_argument("--pist-levels", type=int, default=200)
+    ap.add_argument("--pist-arms", default="fp64,fp32",
+                    help="PIST arms to run: fp64 (FP64 inner solves), fp32 (mixed)")
+    ap.add_argument("--pist-warmup", type=int, default=1,
+                    help="untimed small-grid PIST before the timed arms (0 skips it)")
     ap.add_argument("--batch-problems", type=int, default=0,
                     help="shifted-QMR leg over this many uneven problems (0 skips it)")
     ap.add_argument("--batch-shifts", type=int, default=16)
@@ -239,27 +243,38 @@ def run_reference(args):
 
 
 # ------------------------------------------------------------------- PIST --
-def pist_leg(workload, levels, device, capi, hm):
+def pist_leg(workload, levels, device, capi, hm, arms=("fp64", "fp32"), warmup=True):
     """Wall time from the preconditioner build to converged eigenvalues, with
     FP64 and with FP32 QMR inner solves (basis, HMAT and Ritz values in FP64)."""
-    # untimed warm-up on the small grid: the first solve of a process loads
-    # the solver library's kernels (lazy module loading, ~0.9 s), which would
-    # otherwise land on whichever arm runs first
+    # untimed warm-up on the small grid with the same number of levels (so the
+    # same Krylov sizes): the first solve of a process loads the kernels of
+    # the eigensolver library for each matrix size class it meets (lazy module
+    # loading, seconds in all), which would otherwise land on whichever arm
+    # runs first
     pw = hm.workload("tri-24x32x20")
-    for prec, orth in ((capi.PREC_FP64, 1), (capi.PREC_FP32, 2)):
+    for prec, orth in ((capi.PREC_FP64, 1), (capi.PREC_FP32, 2)) if warmup else ():
         with capi.Context.from_problem(pw, e0=float(pw.RES.min()), device=device) as ctx:
             ctx.build_osb(20, 1e-4)
-            ctx.pist(np.random.default_rng(0).random(pw.N), 20, float(pw.RES.min()), 1e-11, m_max=400,
-                     qmr_max=2000, qmr_tol=1e-4, precision=prec, orth=orth, residuals=True)
+            if prec == capi.PREC_FP32:
+                ctx.set_fp32_mode(capi.FP32_TENSOR_PX)
+            ctx.pist(np.random.default_rng(0).random(pw.N), levels, float(pw.RES.min()), 1e-11,
+                     m_max=max(8 * levels, 400), qmr_max=2000, qmr_tol=1e-4, precision=prec, orth=orth,
+                     residuals=True)
     p = hm.workload(workload)
     e0 = float(p.RES.min())
     x0 = np.random.default_rng(0).random(p.N)
     out = {"workload": workload, "levels": levels}
     eigs = {}
-    # mixed leg: FP32 inner solves and an FP32 first Gram-Schmidt pass (the
-    # re-orthogonalisation pass, HMAT and the Ritz solves stay FP64)
+    # mixed leg: FP32 inner solves (H*X on the CUDA cores, the preconditioner's
+    # rotations in split-BF16 x3 on the tensor cores) and an FP32 first
+    # Gram-Schmidt pass (the re-orthogonalisation pass, HMAT and the Ritz
+    # solves stay FP64)
     for name, prec, orth in (("fp64", capi.PREC_FP64, 1), ("fp32", capi.PREC_FP32, 2)):
+        if name not in arms:
+            continue
         with capi.Context.from_problem(p, e0=e0, device=device) as ctx:
+            if prec == capi.PREC_FP32:
+                ctx.set_fp32_mode(capi.FP32_TENSOR_PX)
             t0 = time.perf_counter()
             stats = ctx.build_osb(20, 1e-4)
             t1 = time.perf_counter()
@@ -270,6 +285,8 @@ def pist_leg(workload, levels, device, capi, hm):
             t2 = time.perf_counter()
         eigs[name] = eig
         out[name] = {"status": st, "orth": orth, "seconds": t2 - t0, "build_s": t1 - t0, "pist_s": t2 - t1,
+                     "fp32_engine": ("H*X CUDA cores, preconditioner rotations split-BF16 x3 tensor cores"
+                                     if prec == capi.PREC_FP32 else None),
                      "build_levels_s": build_levels,
                      "sweeps_per_block": [float(stats[l, 4] / int(np.prod(p.sizes[l + 1:])))
                                           for l in range(len(p.sizes))],
@@ -278,12 +295,13 @@ def pist_leg(workload, levels, device, capi, hm):
                      "t_qmr": info["t_qmr"], "t_orth": info["t_orth"], "t_hmat": info["t_hmat"],
                      "t_ritz": info["t_ritz"], "t_resid": info["t_resid"],
                      "max_residual_eh": float(np.max(info["resid"]))}
-    out["speedup_fp32_inner"] = out["fp64"]["seconds"] / out["fp32"]["seconds"]
-    out["speedup_excluding_build"] = out["fp64"]["pist_s"] / out["fp32"]["pist_s"]
-    diff = np.abs(eigs["fp32"] - eigs["fp64"]) * hm.HARTREE_CM
-    out["max_abs_diff_cm"] = float(diff.max())
-    out["per_level_diff_cm"] = [float(f"{d:.3g}") for d in diff]
-    out["lowest_eigenvalues_eh"] = [float(v) for v in eigs["fp64"][:5]]
+    if "fp64" in eigs and "fp32" in eigs:
+        out["speedup_fp32_inner"] = out["fp64"]["seconds"] / out["fp32"]["seconds"]
+        out["speedup_excluding_build"] = out["fp64"]["pist_s"] / out["fp32"]["pist_s"]
+        diff = np.abs(eigs["fp32"] - eigs["fp64"]) * hm.HARTREE_CM
+        out["max_abs_diff_cm"] = float(diff.max())
+        out["per_level_diff_cm"] = [float(f"{d:.3g}") for d in diff]
+    out["lowest_eigenvalues_eh"] = [float(v) for v in next(iter(eigs.values()))[:5]] if eigs else []
     return out
 
 
@@ -483,7 +501,8 @@ def run_ours(args):
         base = cpu_baseline(p, e0, args.cpu_seconds)
     pist = None
     if args.pist_workload != "none" and args.pist_levels > 0:
-        pist = pist_leg(args.pist_workload, args.pist_levels, local, capi, hm)
+        pist = pist_leg(args.pist_workload, args.pist_levels, local, capi, hm,
+                        arms=tuple(a.strip() for a in args.pist_arms.split(",")), warmup=args.pist_warmup > 0)
     batch = None
     if args.batch_problems > 0:
         batch = batch_leg(args.batch_problems, args.batch_shifts, local, capi, hm)

@@ -51,6 +51,11 @@ extern "C" {
 /* engine of the FP32 (inner-solve) level products and preconditioner rotations */
 #define SCALIT_FP32_SIMT 0   /* FP32 CUDA cores (strided GEMM)                         */
 #define SCALIT_FP32_TENSOR 1 /* split-BF16 x3 on the tensor cores (tcgen05), FP32 sums */
+#define SCALIT_FP32_TENSOR_PX 2 /* preconditioner rotations on the tensor cores, H*X on
+                                   the CUDA cores: the operator keeps FP32 accuracy (the
+                                   QMR's attainable residual), the preconditioner, whose
+                                   accuracy only sets the convergence rate, takes the
+                                   faster engine                                         */
 
 /* arithmetic of the QMR inner solves */
 #define SCALIT_PREC_FP64 0
@@ -91,8 +96,10 @@ int scalit_set_stream(scalit_ctx *ctx, void *stream);
  * the FP64 pipe. */
 int scalit_set_fp64_mode(scalit_ctx *ctx, int mode);
 /* Engine of the FP32 level products and preconditioner rotations
- * (SCALIT_FP32_SIMT or SCALIT_FP32_TENSOR; levels above 256 points stay on
- * the CUDA cores).  No reference counterpart: the reference has no FP32 path. */
+ * (SCALIT_FP32_SIMT, SCALIT_FP32_TENSOR or SCALIT_FP32_TENSOR_PX; levels above
+ * 256 points stay on the CUDA cores).  Split-BF16 x3 carries ~16 significant
+ * bits (H*X relative error ~4e-6 against ~2e-7 on the CUDA cores).  No
+ * reference counterpart: the reference has no FP32 path. */
 int scalit_set_fp32_mode(scalit_ctx *ctx, int mode);
 /* sOSBW%mE0: the shift of (H - E0) and of the preconditioner. */
 int scalit_set_shift(scalit_ctx *ctx, double e0);

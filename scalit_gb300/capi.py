@@ -14,7 +14,7 @@ from . import build as _build
 
 TA0, TA1 = 0, 1
 TOSB, TOSBD1, TOSBD2 = 1, 2, 3
-FP32_SIMT, FP32_TENSOR = 0, 1
+FP32_SIMT, FP32_TENSOR, FP32_TENSOR_PX = 0, 1, 2
 PREC_FP64, PREC_FP32 = 0, 1
 FP64_DFMA, FP64_TENSOR = 0, 1
 FMAX = 20

@@ -293,7 +293,10 @@ int scalit_set_fp64_mode(scalit_ctx *c, int mode)
 int scalit_set_fp32_mode(scalit_ctx *c, int mode)
 {
     if (!c) { set_error("null context"); return SCALIT_EINVAL; }
-    if (mode != SCALIT_FP32_SIMT && mode != SCALIT_FP32_TENSOR) { set_error("unknown FP32 mode %d", mode); return SCALIT_EINVAL; }
+    if (mode != SCALIT_FP32_SIMT && mode != SCALIT_FP32_TENSOR && mode != SCALIT_FP32_TENSOR_PX) {
+        set_error("unknown FP32 mode %d", mode);
+        return SCALIT_EINVAL;
+    }
     c->fp32_mode = mode;
     c->gen++;
     return 0;

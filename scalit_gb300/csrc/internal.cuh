@@ -85,7 +85,8 @@ struct scalit_ctx {
     void *cusolver = nullptr;       // cusolverDnHandle_t
     // FP64 H*X engine: SCALIT_FP64_DFMA (FP64 pipe) or SCALIT_FP64_TENSOR (digit-sliced tcgen05)
     int fp64_mode = SCALIT_FP64_TENSOR;
-    // FP32 engine: SCALIT_FP32_SIMT (CUDA cores) or SCALIT_FP32_TENSOR (split-BF16 x3)
+    // FP32 engine: SCALIT_FP32_SIMT (CUDA cores), SCALIT_FP32_TENSOR (split-BF16 x3)
+    // or SCALIT_FP32_TENSOR_PX (split-BF16 x3 for the preconditioner's rotations only)
     int fp32_mode = SCALIT_FP32_SIMT;
     TcLevelData tc32[SCALIT_FMAX];           // hi/lo planes of the level matrices
     TcLevelData pxtc32[SCALIT_FMAX][2];      // of the preconditioner's rotations [VX, VTX]

@@ -54,6 +54,8 @@ struct Tc32Args {
     const int *gate;
     int *err;
     int vec;               // 16-byte operand loads (aligned rows / row groups, K % 4 == 0)
+    int resident;          // every K slab of the grid operand in shared memory at once
+    int cpre;              // accumulate: prefetch the output tile into the consumed slabs
     const uint4 *bsplit;   // [blocks][ntile][ks][hi, lo][NT x 16 BF16, canonical]
     int tpb;               // > 0: per-block B, tpb M tiles per block of Mi rows
     i64 b_blk;             // uint4 stride between blocks' planes
@@ -69,8 +71,11 @@ tc32_level_kernel(Tc32Args g)
     const int bstep = 2 * NT * 32;                         // bytes of one K step of B (hi + lo)
     unsigned char *Bs = smem;                              // KS x bstep
     unsigned char *Abuf = Bs + (size_t)KS * bstep;         // 2 x kAStep32
-    float *slabs = reinterpret_cast<float *>(Abuf + 2 * kAStep32);      // kStages32 x kSlab32
-    uint64_t *mbar = reinterpret_cast<uint64_t *>(slabs + kStages32 * kSlab32);   // MMAs of a buffer done
+    float *slabs = reinterpret_cast<float *>(Abuf + 2 * kAStep32);      // nslab x kSlab32
+    // resident: all KS slabs loaded at once; otherwise a ring of kStages32
+    const bool resident = g.resident != 0;
+    const int nslab = resident ? KS : kStages32;
+    uint64_t *mbar = reinterpret_cast<uint64_t *>(slabs + nslab * kSlab32);       // MMAs of a buffer done
     uint64_t *cutb = mbar + 2;                                                      // a buffer's planes cut
     uint32_t *tslot = reinterpret_cast<uint32_t *>(mbar + 4);
     uint64_t *bready = mbar + 5;                                                    // the B tile landed
@@ -142,10 +147,16 @@ tc32_level_kernel(Tc32Args g)
         return;   // warp 0 frees the TMEM
     }
 
+    // row offsets with 32-bit quotients (M < 2^31)
+    const int Mi32 = (int)g.Mi;
+    auto row_off = [&](int mm) -> i64 {
+        const int mq = mm / Mi32;
+        return (i64)(mm - mq * Mi32) * g.s1 + (i64)mq * g.s2;
+    };
     const int row = tid & (kBM32 - 1), q = tid >> 7;
     const int m = m0 + row;
     const bool mvalid = m < mlim;
-    const i64 moff = mvalid ? (i64)(m % g.Mi) * g.s1 + (i64)(m / g.Mi) * g.s2 : 0;
+    const i64 moff = mvalid ? row_off(m) : 0;
     const bool rowc = (g.a_sk == 1);
     i64 lmoff[4];
     bool lvalid[4];
@@ -154,7 +165,7 @@ tc32_level_kernel(Tc32Args g)
         const int r = rowc ? ((tid >> 4) + 32 * i) : row;
         const int mm = m0 + r;
         lvalid[i] = mm < mlim;
-        lmoff[i] = lvalid[i] ? (i64)(mm % g.Mi) * g.s1 + (i64)(mm / g.Mi) * g.s2 : 0;
+        lmoff[i] = (lvalid[i] && !g.vec) ? row_off(mm) : 0;
     }
     // 16-byte loads: K-major rows take four consecutive k per thread, M-major
     // slabs four consecutive rows (one block: Mi % 4 == 0) at one k
@@ -165,11 +176,11 @@ tc32_level_kernel(Tc32Args g)
     if (g.vec) {
         const int mm = m0 + vr;
         vvalid = mm < mlim;
-        vmoff = vvalid ? (i64)(mm % g.Mi) * g.s1 + (i64)(mm / g.Mi) * g.s2 : 0;
+        vmoff = vvalid ? row_off(mm) : 0;
     }
     auto issue = [&](int t) {
         if (t < KS && g.vec) {
-            float *st = slabs + (t % kStages32) * kSlab32;
+            float *st = slabs + (resident ? t : t % kStages32) * kSlab32;
             const int k = t * 16 + vj;
             float *dst = rowc ? st + vr * 20 + vj : st + vj * kBM32 + vr;
             if (vvalid && k < g.K) {
@@ -179,7 +190,7 @@ tc32_level_kernel(Tc32Args g)
                 *reinterpret_cast<float4 *>(dst) = make_float4(0.f, 0.f, 0.f, 0.f);
             }
         } else if (t < KS) {
-            float *st = slabs + (t % kStages32) * kSlab32;
+            float *st = slabs + (resident ? t : t % kStages32) * kSlab32;
             #pragma unroll
             for (int i = 0; i < 4; ++i) {
                 int r, j;
@@ -197,9 +208,8 @@ tc32_level_kernel(Tc32Args g)
         }
         asm volatile("cp.async.commit_group;" ::: "memory");
     };
-    // K <= 16 kStages32: every slab in flight at once and resident; otherwise a
-    // ring with kStages32 - 1 slabs of look-ahead
-    const bool resident = (KS <= kStages32);
+    // resident: every slab in flight at once; otherwise a ring with
+    // kStages32 - 1 slabs of look-ahead
     if (resident) {
         for (int t = 0; t < KS; ++t) issue(t);
         asm volatile("cp.async.wait_all;" ::: "memory");
@@ -220,7 +230,7 @@ tc32_level_kernel(Tc32Args g)
             asm volatile("bar.sync 1, %0;" :: "n"(kThreads32) : "memory");   // cutting threads only
             issue(ks + kStages32 - 1);
         }
-        const float *st = slabs + (ks % kStages32) * kSlab32;
+        const float *st = slabs + (resident ? ks : ks % kStages32) * kSlab32;
         unsigned char *Ab = Abuf + buf * kAStep32;
         uint32_t hw[2], lw[2];
         #pragma unroll
@@ -241,8 +251,26 @@ tc32_level_kernel(Tc32Args g)
         fence_proxy_async_smem();
         asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" :: "r"(smem_addr(&cutb[buf])) : "memory");
     }
+    // accumulating, resident, M-major output: once every slab is converted
+    // (a barrier of the cutting threads; the resident loop has none), the
+    // tile of C to add to streams into the consumed slabs while the last MMAs
+    // finish, so the epilogue reads it from shared memory
+    const float *Cs = slabs;                                  // [NT][kBM32]
+    if (g.cpre) {
+        asm volatile("bar.sync 1, %0;" :: "n"(kThreads32) : "memory");
+        const int rg = 4 * (tid & 31);
+        if (m0 + rg < mlim) {
+            const float *csrc = C + row_off(m0 + rg);
+            for (int n = tid >> 5; n < NT && ntile * NT + n < g.N; n += kThreads32 / 32)
+                asm volatile("cp.async.cg.shared.global [%0], [%1], 16;"
+                             :: "r"(smem_addr(Cs + n * kBM32 + rg)), "l"(csrc + (i64)(ntile * NT + n) * g.c_sn)
+                             : "memory");
+        }
+        asm volatile("cp.async.commit_group;" ::: "memory");
+    }
     if (ok) ok = mbar_wait(&mbar[(KS - 1) & 1], ((KS - 1) >> 1) & 1);
     asm volatile("cp.async.wait_all;" ::: "memory");
+    if (g.cpre) asm volatile("bar.sync 1, %0;" :: "n"(kThreads32) : "memory");
     if (!ok) {
         if (g.err) atomicExch(g.err, 3);
         for (int b = 0; b < 2; ++b) mbar_wait(&mbar[b], 0) || mbar_wait(&mbar[b], 1);
@@ -275,7 +303,7 @@ tc32_level_kernel(Tc32Args g)
                     const i64 p = moff + (i64)n * g.c_sn;
                     float out = sc * v[q][j];
                     if (g.diagV) out = fmaf(g.alpha * (g.diagV[p] - shift), g.diagX[p + (i64)z * g.dx_sz], out);
-                    if (g.accumulate) out += C[p];
+                    if (g.accumulate) out += g.cpre ? Cs[(c0 + 4 * q + j) * kBM32 + row] : C[p];
                     outv[q][j] = out;
                 }
             #pragma unroll
@@ -389,14 +417,16 @@ int tc32_prepare(scalit_ctx *c, bool rotations)
     return 0;
 }
 
-static size_t smem_bytes(int NT, int KS)
+static size_t smem_bytes(int NT, int KS, int nslab)
 {
-    return (size_t)KS * 2 * NT * 32 + 2 * (size_t)kAStep32 + (size_t)kStages32 * kSlab32 * 4 + 96;
+    return (size_t)KS * 2 * NT * 32 + 2 * (size_t)kAStep32 + (size_t)nslab * kSlab32 * 4 + 96;
 }
 
 static int launch32(const Tc32Args &g, i64 gx, int ntiles, int nvec, cudaStream_t s)
 {
-    const size_t smem = smem_bytes(g.NT, g.KS);
+    // all K slabs resident when they fit (every load in flight at once), else the ring
+    const int resident = (g.KS <= kStages32 || smem_bytes(g.NT, g.KS, g.KS) <= 220 * 1024) ? 1 : 0;
+    const size_t smem = smem_bytes(g.NT, g.KS, resident ? g.KS : kStages32);
     if (smem > 220 * 1024) { set_error("tensor-core FP32 tile too large"); return SCALIT_EUNSUP; }
     static int configured = -1;
     int dev = 0;
@@ -408,6 +438,11 @@ static int launch32(const Tc32Args &g, i64 gx, int ntiles, int nvec, cudaStream_
     if (gx > 2147483647LL || nvec > 65535) { set_error("tensor-core FP32 grid too large"); return SCALIT_EINVAL; }
     Tc32Args gv = g;
     gv.vec = vec_ok(g);
+    gv.resident = resident;
+    // output prefetch: 16-byte groups of four rows of one block at one column
+    gv.cpre = (resident && g.accumulate && g.s1 == 1 && g.Mi % 4 == 0 && g.s2 % 4 == 0 && g.c_sn % 4 == 0 &&
+               g.c_sz % 4 == 0 && (reinterpret_cast<uintptr_t>(g.C) & 15) == 0 &&
+               (size_t)g.NT * kBM32 <= (size_t)g.KS * kSlab32) ? 1 : 0;
     tc32_level_kernel<<<dim3((unsigned)gx, ntiles, nvec), kBlock32, smem, s>>>(gv);
     SC_CHECK_LAUNCH();
     return 0;
@@ -420,7 +455,8 @@ bool tc32_usable(const scalit_ctx *c, int l)
 
 bool tc32_px_usable(const scalit_ctx *c, int l)
 {
-    return c->fp32_mode == SCALIT_FP32_TENSOR && c->pxtc32[l][0].usable && c->pxtc32[l][1].usable;
+    return (c->fp32_mode == SCALIT_FP32_TENSOR || c->fp32_mode == SCALIT_FP32_TENSOR_PX) &&
+           c->pxtc32[l][0].usable && c->pxtc32[l][1].usable;
 }
 
 int tc32_level_apply(const scalit_ctx *c, int l, const float *X, float *Y, int accumulate, const float *diagV,

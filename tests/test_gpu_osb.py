@@ -114,3 +114,28 @@ def test_px_f32_tensor_engine(lib, orc):
         torch.cuda.synchronize()
         z = dz.double().cpu().numpy()
     assert rel(z, ref.px(x)) < 1e-4
+
+
+def test_fp32_tensor_px_mode(lib):
+    """SCALIT_FP32_TENSOR_PX: the preconditioner's rotations take the tensor
+    cores (the same results as SCALIT_FP32_TENSOR) while H*X stays on the CUDA
+    cores (the same results as SCALIT_FP32_SIMT)."""
+    torch = pytest.importorskip("torch")
+    p = hm.workload("tri-24x32x20")
+    x = np.random.default_rng(6).standard_normal(p.N)
+    out = {}
+    with capi.Context.from_problem(p, e0=float(p.RES.min()) - 1e-3) as ctx:
+        ctx.build_osb(20, 1e-4)
+        dx = torch.tensor(x, dtype=torch.float32, device="cuda")
+        for mode in (capi.FP32_SIMT, capi.FP32_TENSOR, capi.FP32_TENSOR_PX):
+            ctx.set_fp32_mode(mode)
+            hy, pz = torch.empty_like(dx), torch.empty_like(dx)
+            ctx.hx_f32_device(dx, hy)
+            ctx.px_f32_device(dx, pz)
+            torch.cuda.synchronize()
+            out[mode] = (hy.cpu(), pz.cpu())
+        with pytest.raises(capi.ScalitError):
+            ctx.set_fp32_mode(3)
+    assert torch.equal(out[capi.FP32_TENSOR_PX][0], out[capi.FP32_SIMT][0])
+    assert torch.equal(out[capi.FP32_TENSOR_PX][1], out[capi.FP32_TENSOR][1])
+    assert not torch.equal(out[capi.FP32_TENSOR][1], out[capi.FP32_SIMT][1])
