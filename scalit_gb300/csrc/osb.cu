@@ -374,6 +374,158 @@ jacobi_block_kernel(int bjmax, double bjtol, int blk, int mak, int ndk,
     }
 }
 
+// ------------------------------------- schedule 1b: CTA/block, packed --
+// One matrix per block (ndk == 1) kept as its upper triangle, column by
+// column (element (r, c), r <= c, at c (c + 1) / 2 + r): half the shared
+// memory of the full square, so two 160 x 160 blocks fit an SM and one CTA's
+// angle phases and barriers overlap the other's rotations.  Every element
+// update is the full-storage kernel's (the same formulas on the same values,
+// one stored copy instead of two mirrored ones), so H, V and the
+// eigenvalues evolve bit for bit alike; only the order of the sweep
+// reductions' sums differs.
+__device__ __forceinline__ int pk(int r, int c) { return ((c * (c + 1)) >> 1) + r; }   // r <= c
+__device__ __forceinline__ int pks(int a, int b) { return a <= b ? pk(a, b) : pk(b, a); }
+
+__device__ __forceinline__ void packed_item(double *H, int mak, int a, int i, int m,
+                                            const double *__restrict__ cs, const double *__restrict__ sn,
+                                            int u, float rm)
+{
+    const int nfree = (mak - 2 * m) * m;
+    if (u < nfree) {
+        int t;
+        const int f = quot_small(u, m, rm, t), r = free_row(f, a, i, m);
+        const int p = a + t, q = a + i + t;
+        const int ip = pks(r, p), iq = pks(r, q);
+        const double c = cs[t], sv = sn[t];
+        const double x = H[ip], y = H[iq];
+        H[ip] = c * x - sv * y;
+        H[iq] = c * y + sv * x;
+        return;
+    }
+    u -= nfree;
+    int t2;
+    const int t = quot_small(u, m, rm, t2);
+    if (t2 < t) return;
+    const int p = a + t, q = a + i + t;
+    const double c = cs[t], sv = sn[t];
+    if (t == t2) {
+        const int pp = pk(p, p), qq = pk(q, q), pq = pk(p, q);
+        const double C2 = c * c, S2 = sv * sv, SC = sv * c;
+        const double odg = H[pq];
+        const double ddg = 0.5 * H[pp] - 0.5 * H[qq];
+        const double np_ = C2 * H[pp] + S2 * H[qq] - 2 * SC * odg;
+        const double nq_ = C2 * H[qq] + S2 * H[pp] + 2 * SC * odg;
+        const double nqp = (C2 - S2) * odg + 2 * SC * ddg;
+        H[pp] = np_; H[qq] = nq_; H[pq] = nqp;
+        return;
+    }
+    const int p2 = a + t2, q2 = a + i + t2;
+    const int i00 = pks(p, p2), i01 = pks(p, q2), i10 = pks(q, p2), i11 = pks(q, q2);
+    const double x00 = H[i00], x01 = H[i01], x10 = H[i10], x11 = H[i11];
+    const double a00 = c * x00 - sv * x10, a10 = c * x10 + sv * x00;
+    const double a01 = c * x01 - sv * x11, a11 = c * x11 + sv * x01;
+    const double c2 = cs[t2], s2 = sn[t2];
+    H[i00] = c2 * a00 - s2 * a01;
+    H[i01] = c2 * a01 + s2 * a00;
+    H[i10] = c2 * a10 - s2 * a11;
+    H[i11] = c2 * a11 + s2 * a10;
+}
+
+// 2 sum over r < c of H(r, c)^2 and sum of H(c, c)^2, column by column.
+__device__ double packed_offdiag(const double *H, int mak, double *red)
+{
+    double s = 0.0, z1 = 0.0, z2 = 0.0;
+    for (int c = 1; c < mak; ++c) {
+        const double *Hc = H + pk(0, c);
+        for (int r = threadIdx.x; r < c; r += blockDim.x) { const double h = Hc[r]; s = fma(h, h, s); }
+    }
+    block_sum3(s, z1, z2, red);
+    return 2.0 * s;
+}
+
+__device__ double packed_sumdiag(const double *H, int mak, double *red)
+{
+    double s = 0.0, z1 = 0.0, z2 = 0.0;
+    for (int c = threadIdx.x; c < mak; c += blockDim.x) { const double h = H[pk(c, c)]; s = fma(h, h, s); }
+    block_sum3(s, z1, z2, red);
+    return s;
+}
+
+__global__ void __launch_bounds__(512, 2)
+jacobi_packed_kernel(int bjmax, double bjtol, int blk, int mak, double *__restrict__ HOSB,
+                     double *__restrict__ VOSB, double *__restrict__ EIG, double *__restrict__ bstats)
+{
+    extern __shared__ __align__(16) double smem[];
+    double *red = smem;                 // 3 * 32
+    double *cs = smem + 96;             // kMaxBatch
+    double *sn = cs + kMaxBatch;        // kMaxBatch
+    double *cs_v = sn + kMaxBatch;      // kMaxBatch: the previous batch's angles, for
+    double *sn_v = cs_v + kMaxBatch;    // kMaxBatch  its deferred V update
+    double *H = sn_v + kMaxBatch;       // upper triangle, mak (mak + 1) / 2
+    const int tid = threadIdx.x, nt = blockDim.x;
+    const float rmak = 1.0f / (float)mak;
+    for (int b = blockIdx.x; b < blk; b += gridDim.x) {
+        double *Hg = HOSB + (i64)b * mak * mak;
+        double *V = VOSB + (i64)b * mak * mak;
+        __syncthreads();
+        for (int e = tid; e < mak * mak; e += nt) {
+            int r;
+            const int c = quot_small(e, mak, rmak, r);
+            if (r <= c) H[pk(r, c)] = Hg[e];
+            V[e] = (r == c) ? 1.0 : 0.0;
+        }
+        __syncthreads();
+        const double initye = packed_offdiag(H, mak, red);
+        double ye = initye, dye = initye;
+        int k = 1;
+        int mv = 0, av = 0, iv = 0;
+        while (fabs(dye) > initye * bjtol && k <= bjmax) {
+            for (int i = 1; i <= mak - 1; ++i) {
+                for (int a = 0; a < mak - i; a += i) {
+                    const int m = min(i, mak - i - a);
+                    // angles (one thread per plane) while the warps past them
+                    // apply the previous batch's rotations to V
+                    const int t0 = (m + 31) & ~31;          // t0 <= kMaxBatch < nt
+                    if (tid < m) {
+                        const int p = a + tid, q = a + i + tid;
+                        const double o = H[pk(p, q)];
+                        const double d = 0.5 * H[pk(p, p)] - 0.5 * H[pk(q, q)];
+                        jacobi_angle(o * o, 2.0 * (o * d), d * d, cs + tid, sn + tid);
+                    } else if (tid >= t0) {
+                        for (int u = tid - t0; u < mak * mv; u += nt - t0)
+                            batch_vitem(V, mak, av, iv, cs_v, sn_v, u, rmak);
+                    }
+                    __syncthreads();
+                    const int nh = batch_items(mak, m);
+                    const float rm = 1.0f / (float)m;
+                    for (int u = tid; u < nh; u += nt) packed_item(H, mak, a, i, m, cs, sn, u, rm);
+                    if (tid < m) { cs_v[tid] = cs[tid]; sn_v[tid] = sn[tid]; }
+                    mv = m; av = a; iv = i;
+                    __syncthreads();
+                }
+            }
+            dye = packed_offdiag(H, mak, red) - ye;
+            ye = ye + dye;
+            k = k + 1;
+        }
+        for (int u = tid; u < mak * mv; u += nt) batch_vitem(V, mak, av, iv, cs_v, sn_v, u, rmak);
+        const double sd = packed_sumdiag(H, mak, red);
+        __syncthreads();
+        for (int e = tid; e < mak; e += nt) EIG[e + (i64)mak * b] = H[pk(e, e)];
+        // the rotated matrix back in full storage, its diagonal zeroed (as HOSB after HosbDiag)
+        for (int e = tid; e < mak * mak; e += nt) {
+            int r;
+            const int c = quot_small(e, mak, rmak, r);
+            Hg[e] = (r == c) ? 0.0 : H[pks(r, c)];
+        }
+        if (tid == 0) {
+            bstats[3 * (i64)b] = (double)k;
+            bstats[3 * (i64)b + 1] = fabs(1.0 - ye / initye);
+            bstats[3 * (i64)b + 2] = sd;
+        }
+    }
+}
+
 // --------------------------------------------- schedule 2: GPU/rotation --
 // Per-block state of the sweep loop: [initye, ye, dye, k, done, sumdiag].
 struct SweepState { double initye, ye, dye; int k, done; double sumdiag; };
@@ -558,8 +710,25 @@ int hosbdiag_device(scalit_ctx *c, int bjmax, double bjtol, int blk, int mak, in
             return (v >= 256 && v <= kJacThreads && v % 32 == 0) ? v : 0;   // above kMaxBatch
         }();
         if (forced) nt = forced;
-        jacobi_block_kernel<<<grid, nt, fixed + bytes, s>>>(bjmax, bjtol, blk, mak, ndk, HOSB, VOSB,
-                                                                  EIG, d_bstats);
+        static const int packed_off = [] {             // SCALIT_JAC_FULL=1: full storage (a comparison switch)
+            const char *e = getenv("SCALIT_JAC_FULL");
+            return e && atoi(e) == 1;
+        }();
+        if (ndk == 1 && !packed_off) {
+            // one matrix per block: the packed triangle, half the shared memory
+            const size_t pbytes = sizeof(double) * (size_t)mak * (mak + 1) / 2;
+            const int pctas = std::max(1, (int)((228 * 1024) / (fixed + pbytes + 1024)));
+            int pnt = 256;
+            while (pnt < 512 && 2 * pnt * pctas <= 512) pnt *= 2;
+            if (forced) pnt = std::min(forced, 512);
+            SC_CUDA(cudaFuncSetAttribute(jacobi_packed_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)(225 * 1024)));
+            jacobi_packed_kernel<<<grid, pnt, fixed + pbytes, s>>>(bjmax, bjtol, blk, mak, HOSB, VOSB, EIG,
+                                                                  d_bstats);
+        } else {
+            jacobi_block_kernel<<<grid, nt, fixed + bytes, s>>>(bjmax, bjtol, blk, mak, ndk, HOSB, VOSB, EIG,
+                                                                d_bstats);
+        }
         SC_CHECK_LAUNCH();
     } else {
         const int gy = std::min(blk, 65535);
