@@ -140,6 +140,12 @@ int scalit_tile_picks(scalit_ctx *ctx, int *picks);
  * scalit_build_osb; the reference prints the whole build's time only
  * (osb.progDiag.h:40-47). */
 int scalit_build_times(scalit_ctx *ctx, double *seconds);
+/* Self-test of the kernels' bounded waits: a one-CTA kernel waits `seconds`
+ * (0 < seconds <= 10) on an mbarrier that nothing completes, records the
+ * expiry in the context's error flag and returns; the call reports it as the
+ * product kernels' expiry is reported (SCALIT_ECUDA with a message) and the
+ * context stays usable.  No reference counterpart. */
+int scalit_selftest_wait(scalit_ctx *ctx, double seconds);
 /* Copy the preconditioner out (VOSB: scalit_vosb_len doubles, EIG0: npoints)
  * or in (sVOSB < 0 path: loadVOSB/loadEig, osb.io.h:124-208). */
 int scalit_get_osb(scalit_ctx *ctx, double *VOSB, double *EIG0);

@@ -44,6 +44,7 @@ SIGNATURES = {
     "scalit_level_device": (C.c_int, [_vp, C.c_int, C.c_int, _vp, _vp]),
     "scalit_build_osb": (C.c_int, [_vp, C.c_int, C.c_double, _dp]),
     "scalit_build_times": (C.c_int, [_vp, _dp]),
+    "scalit_selftest_wait": (C.c_int, [_vp, C.c_double]),
     "scalit_set_fp32_mode": (C.c_int, [_vp, C.c_int]),
     "scalit_tile_picks": (C.c_int, [_vp, _ip]),
     "scalit_get_osb": (C.c_int, [_vp, _dp, _dp]),
@@ -265,6 +266,10 @@ class Context:
         t = np.zeros(2 * len(self.sizes) * 2, dtype=np.int32)
         _check(self.lib.scalit_tile_picks(self.h, t.ctypes.data_as(C.POINTER(C.c_int))))
         return t.reshape(2, len(self.sizes), 2)
+
+    def selftest_wait(self, seconds):
+        """Run the bounded-wait self-test; returns the C call's status code."""
+        return int(self.lib.scalit_selftest_wait(self.h, float(seconds)))
 
     def build_times(self):
         t = np.zeros(len(self.sizes))

@@ -440,6 +440,12 @@ int scalit_build_osb(scalit_ctx *c, int bjmax, double bjtol, double *stats)
     return osb_build(c, bjmax, bjtol, stats);
 }
 
+int scalit_selftest_wait(scalit_ctx *c, double seconds)
+{
+    CTX_CHECK(c);
+    return wait_selftest(c, seconds);
+}
+
 int scalit_build_times(scalit_ctx *c, double *seconds)
 {
     CTX_CHECK(c);

@@ -200,6 +200,7 @@ int tc_level_apply(const scalit_ctx *c, int level, const double *X, double *Y, i
                    const double *diagV, double shift, double alpha, const int *gate, cudaStream_t s,
                    int nvec, const double *shiftv = nullptr, const int *vgate = nullptr, int vstride = 0);
 int tc_check_error(scalit_ctx *c);
+int wait_selftest(scalit_ctx *c, double seconds);
 int tc_gemm_f64(const scalit_ctx *c, int M, int N, int K, const double *A, i64 lda, const double *B, i64 ldb,
                 double *C, i64 ldc, cudaStream_t s);
 

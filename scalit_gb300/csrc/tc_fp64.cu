@@ -708,11 +708,38 @@ int tc_check_error(scalit_ctx *c)
     SC_CUDA(cudaMemcpyAsync(&h, c->tc_err, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
     SC_CUDA(cudaStreamSynchronize(c->stream));
     if (h) {
-        set_error("tensor-core H*X: an mbarrier wait ran out (kernel aborted)");
+        static const char *what[] = {"", "FP64 tensor-core level product", "level-1 P*X stream",
+                                     "FP32 tensor-core level product", "bounded-wait self-test"};
+        set_error("%s: an mbarrier wait ran out (kernel aborted, context usable)",
+                  (h >= 1 && h <= 4) ? what[h] : "device kernel");
         cudaMemsetAsync(c->tc_err, 0, sizeof(int), c->stream);
         return SCALIT_ECUDA;
     }
     return 0;
+}
+
+// Self-test of the bounded waits: one CTA waits on an mbarrier whose expected
+// transaction bytes never arrive (nothing is copied), the wait runs out after
+// limit_ns, the kernel records code 4 in the context's error flag and returns
+// -- the path every streaming and tensor-core kernel takes on expiry.
+__global__ void wait_selftest_kernel(uint64_t limit_ns, int *err)
+{
+    __shared__ __align__(8) uint64_t mbar;
+    if (threadIdx.x == 0) {
+        mbar_init(&mbar, 1);
+        mbar_init_fence();
+        mbar_arrive_expect_tx(&mbar, 16);      // 16 bytes that no copy delivers
+        if (!mbar_wait_timed(&mbar, 0, limit_ns) && err) atomicExch(err, 4);
+    }
+}
+
+int wait_selftest(scalit_ctx *c, double seconds)
+{
+    if (!(seconds > 0.0 && seconds <= 10.0)) { set_error("self-test wait of %g s out of (0, 10]", seconds); return SCALIT_EINVAL; }
+    if (!c->tc_err) SC_CUDA(cudaMalloc(&c->tc_err, sizeof(int)));
+    wait_selftest_kernel<<<1, 32, 0, c->stream>>>((uint64_t)(seconds * 1e9), c->tc_err);
+    SC_CHECK_LAUNCH();
+    return tc_check_error(c);
 }
 
 }  // namespace sc
