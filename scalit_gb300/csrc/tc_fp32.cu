@@ -33,7 +33,11 @@ static constexpr int kBM32 = 128;
 static constexpr int kThreads32 = 512;                      // cutting threads: four per grid row
 static constexpr int kBlock32 = 544;                        // plus one warp that issues the MMAs
 static constexpr int kStages32 = 6;
-static constexpr int kSlab32 = kBM32 * 20;                 // floats per slab stage (row stride 20)
+// Floats per slab stage: K-major rows (level 1) with a padded row stride of 20
+// (16-byte aligned, conflict-free reads), M-major slabs 16 rows of 128 packed.
+static constexpr int kSlab32 = kBM32 * 20;
+static constexpr int kSlab32M = kBM32 * 16;
+__host__ __device__ constexpr int slab_floats(bool kmajor) { return kmajor ? kSlab32 : kSlab32M; }
 static constexpr int kAStep32 = 2 * kBM32 * 16 * 2;        // hi + lo planes of 128 x 16 BF16
 
 struct Tc32Args {
@@ -71,11 +75,12 @@ tc32_level_kernel(Tc32Args g)
     const int bstep = 2 * NT * 32;                         // bytes of one K step of B (hi + lo)
     unsigned char *Bs = smem;                              // KS x bstep
     unsigned char *Abuf = Bs + (size_t)KS * bstep;         // 2 x kAStep32
-    float *slabs = reinterpret_cast<float *>(Abuf + 2 * kAStep32);      // nslab x kSlab32
+    float *slabs = reinterpret_cast<float *>(Abuf + 2 * kAStep32);      // nslab x slab
     // resident: all KS slabs loaded at once; otherwise a ring of kStages32
     const bool resident = g.resident != 0;
     const int nslab = resident ? KS : kStages32;
-    uint64_t *mbar = reinterpret_cast<uint64_t *>(slabs + nslab * kSlab32);       // MMAs of a buffer done
+    const int slab = slab_floats(g.a_sk == 1);
+    uint64_t *mbar = reinterpret_cast<uint64_t *>(slabs + nslab * slab);          // MMAs of a buffer done
     uint64_t *cutb = mbar + 2;                                                      // a buffer's planes cut
     uint32_t *tslot = reinterpret_cast<uint32_t *>(mbar + 4);
     uint64_t *bready = mbar + 5;                                                    // the B tile landed
@@ -180,7 +185,7 @@ tc32_level_kernel(Tc32Args g)
     }
     auto issue = [&](int t) {
         if (t < KS && g.vec) {
-            float *st = slabs + (resident ? t : t % kStages32) * kSlab32;
+            float *st = slabs + (resident ? t : t % kStages32) * slab;
             const int k = t * 16 + vj;
             float *dst = rowc ? st + vr * 20 + vj : st + vj * kBM32 + vr;
             if (vvalid && k < g.K) {
@@ -190,7 +195,7 @@ tc32_level_kernel(Tc32Args g)
                 *reinterpret_cast<float4 *>(dst) = make_float4(0.f, 0.f, 0.f, 0.f);
             }
         } else if (t < KS) {
-            float *st = slabs + (resident ? t : t % kStages32) * kSlab32;
+            float *st = slabs + (resident ? t : t % kStages32) * slab;
             #pragma unroll
             for (int i = 0; i < 4; ++i) {
                 int r, j;
@@ -230,7 +235,7 @@ tc32_level_kernel(Tc32Args g)
             asm volatile("bar.sync 1, %0;" :: "n"(kThreads32) : "memory");   // cutting threads only
             issue(ks + kStages32 - 1);
         }
-        const float *st = slabs + (resident ? ks : ks % kStages32) * kSlab32;
+        const float *st = slabs + (resident ? ks : ks % kStages32) * slab;
         unsigned char *Ab = Abuf + buf * kAStep32;
         uint32_t hw[2], lw[2];
         #pragma unroll
@@ -417,16 +422,17 @@ int tc32_prepare(scalit_ctx *c, bool rotations)
     return 0;
 }
 
-static size_t smem_bytes(int NT, int KS, int nslab)
+static size_t smem_bytes(int NT, int KS, int nslab, int slab)
 {
-    return (size_t)KS * 2 * NT * 32 + 2 * (size_t)kAStep32 + (size_t)nslab * kSlab32 * 4 + 96;
+    return (size_t)KS * 2 * NT * 32 + 2 * (size_t)kAStep32 + (size_t)nslab * slab * 4 + 96;
 }
 
 static int launch32(const Tc32Args &g, i64 gx, int ntiles, int nvec, cudaStream_t s)
 {
     // all K slabs resident when they fit (every load in flight at once), else the ring
-    const int resident = (g.KS <= kStages32 || smem_bytes(g.NT, g.KS, g.KS) <= 220 * 1024) ? 1 : 0;
-    const size_t smem = smem_bytes(g.NT, g.KS, resident ? g.KS : kStages32);
+    const int slab = slab_floats(g.a_sk == 1);
+    const int resident = (g.KS <= kStages32 || smem_bytes(g.NT, g.KS, g.KS, slab) <= 220 * 1024) ? 1 : 0;
+    const size_t smem = smem_bytes(g.NT, g.KS, resident ? g.KS : kStages32, slab);
     if (smem > 220 * 1024) { set_error("tensor-core FP32 tile too large"); return SCALIT_EUNSUP; }
     static int configured = -1;
     int dev = 0;
@@ -442,7 +448,7 @@ static int launch32(const Tc32Args &g, i64 gx, int ntiles, int nvec, cudaStream_
     // output prefetch: 16-byte groups of four rows of one block at one column
     gv.cpre = (resident && g.accumulate && g.s1 == 1 && g.Mi % 4 == 0 && g.s2 % 4 == 0 && g.c_sn % 4 == 0 &&
                g.c_sz % 4 == 0 && (reinterpret_cast<uintptr_t>(g.C) & 15) == 0 &&
-               (size_t)g.NT * kBM32 <= (size_t)g.KS * kSlab32) ? 1 : 0;
+               (size_t)g.NT * kBM32 <= (size_t)g.KS * slab_floats(false)) ? 1 : 0;
     tc32_level_kernel<<<dim3((unsigned)gx, ntiles, nvec), kBlock32, smem, s>>>(gv);
     SC_CHECK_LAUNCH();
     return 0;
