@@ -710,11 +710,7 @@ int hosbdiag_device(scalit_ctx *c, int bjmax, double bjtol, int blk, int mak, in
             return (v >= 256 && v <= kJacThreads && v % 32 == 0) ? v : 0;   // above kMaxBatch
         }();
         if (forced) nt = forced;
-        static const int packed_off = [] {             // SCALIT_JAC_FULL=1: full storage (a comparison switch)
-            const char *e = getenv("SCALIT_JAC_FULL");
-            return e && atoi(e) == 1;
-        }();
-        if (ndk == 1 && !packed_off) {
+        if (ndk == 1) {
             // one matrix per block: the packed triangle, half the shared memory
             const size_t pbytes = sizeof(double) * (size_t)mak * (mak + 1) / 2;
             const int pctas = std::max(1, (int)((228 * 1024) / (fixed + pbytes + 1024)));
