@@ -91,6 +91,21 @@ __device__ __forceinline__ bool block_reduce_store(double (&acc)[NV], double *pa
     return last;
 }
 
+// FP32 steps on float4 groups (n % 4 == 0): the group's products are summed
+// in FP32 and the group sum is added to the FP64 accumulator -- one
+// conversion and one FP64 add per four points instead of per point (on this
+// part FP64 arithmetic and conversions share the slow FP64 pipe).
+template <class T> __device__ __forceinline__ bool use_vec4(i64 n)
+{
+    return sizeof(T) == 4 && (n & 3) == 0;
+}
+__device__ __forceinline__ float dot4(const float4 a, const float4 b)
+{
+    return fmaf(a.x, b.x, a.y * b.y) + fmaf(a.z, b.z, a.w * b.w);
+}
+#define SC_GRID_LOOP4(k4, n4) \
+    for (i64 k4 = blockIdx.x * (i64)blockDim.x + threadIdx.x; k4 < (n4); k4 += (i64)gridDim.x * blockDim.x)
+
 // ----------------------------------------------------------------- steps --
 // step A: V /= VNRM, Z /= ZNRM, VZDOT = V.Z
 template <class T>
@@ -106,10 +121,22 @@ qmr_step_a(i64 n, i64 ld, T *V, T *Z, QmrState *st, double *partial)
     }
     const T tv = T(vn), tz = T(zn);
     double acc[1] = {0.0};
-    for (i64 k = blockIdx.x * (i64)blockDim.x + threadIdx.x; k < n; k += (i64)gridDim.x * blockDim.x) {
-        const T v = V[k] / tv, z = Z[k] / tz;
-        V[k] = v; Z[k] = z;
-        acc[0] += (double)v * (double)z;
+    if (use_vec4<T>(n)) {
+        float4 *V4 = reinterpret_cast<float4 *>(V), *Z4 = reinterpret_cast<float4 *>(Z);
+        const float fv = (float)tv, fz = (float)tz;
+        SC_GRID_LOOP4(k4, n >> 2) {
+            float4 v = V4[k4], z = Z4[k4];
+            v.x /= fv; v.y /= fv; v.z /= fv; v.w /= fv;
+            z.x /= fz; z.y /= fz; z.z /= fz; z.w /= fz;
+            V4[k4] = v; Z4[k4] = z;
+            acc[0] += (double)dot4(v, z);
+        }
+    } else {
+        for (i64 k = blockIdx.x * (i64)blockDim.x + threadIdx.x; k < n; k += (i64)gridDim.x * blockDim.x) {
+            const T v = V[k] / tv, z = Z[k] / tz;
+            V[k] = v; Z[k] = z;
+            acc[0] += (double)v * (double)z;
+        }
     }
     if (block_reduce_store<1>(acc, partial, &st->counter)) {
         double d[1];
@@ -145,10 +172,22 @@ qmr_step_c(i64 n, i64 ld, const T *Q, T *S, QmrState *st, double *partial)
     if (st->done) return;
     const T zv = T(st->ZVRAT);
     double acc[1] = {0.0};
-    for (i64 k = blockIdx.x * (i64)blockDim.x + threadIdx.x; k < n; k += (i64)gridDim.x * blockDim.x) {
-        const T sv = zv * S[k];
-        S[k] = sv;
-        acc[0] += (double)Q[k] * (double)sv;
+    if (use_vec4<T>(n)) {
+        const float4 *Q4 = reinterpret_cast<const float4 *>(Q);
+        float4 *S4 = reinterpret_cast<float4 *>(S);
+        const float f = (float)zv;
+        SC_GRID_LOOP4(k4, n >> 2) {
+            float4 sv = S4[k4];
+            sv.x *= f; sv.y *= f; sv.z *= f; sv.w *= f;
+            S4[k4] = sv;
+            acc[0] += (double)dot4(Q4[k4], sv);
+        }
+    } else {
+        for (i64 k = blockIdx.x * (i64)blockDim.x + threadIdx.x; k < n; k += (i64)gridDim.x * blockDim.x) {
+            const T sv = zv * S[k];
+            S[k] = sv;
+            acc[0] += (double)Q[k] * (double)sv;
+        }
     }
     if (block_reduce_store<1>(acc, partial, &st->counter)) {
         double d[1];
@@ -170,10 +209,23 @@ qmr_step_d(i64 n, i64 ld, const T *S, T *V, QmrState *st, double *partial)
     if (st->done) return;
     const T beta = T(st->BETA);
     double acc[1] = {0.0};
-    for (i64 k = blockIdx.x * (i64)blockDim.x + threadIdx.x; k < n; k += (i64)gridDim.x * blockDim.x) {
-        const T v = S[k] - beta * V[k];
-        V[k] = v;
-        acc[0] += (double)v * (double)v;
+    if (use_vec4<T>(n)) {
+        const float4 *S4 = reinterpret_cast<const float4 *>(S);
+        float4 *V4 = reinterpret_cast<float4 *>(V);
+        const float b = (float)beta;
+        SC_GRID_LOOP4(k4, n >> 2) {
+            const float4 sv = S4[k4];
+            float4 v = V4[k4];
+            v.x = sv.x - b * v.x; v.y = sv.y - b * v.y; v.z = sv.z - b * v.z; v.w = sv.w - b * v.w;
+            V4[k4] = v;
+            acc[0] += (double)dot4(v, v);
+        }
+    } else {
+        for (i64 k = blockIdx.x * (i64)blockDim.x + threadIdx.x; k < n; k += (i64)gridDim.x * blockDim.x) {
+            const T v = S[k] - beta * V[k];
+            V[k] = v;
+            acc[0] += (double)v * (double)v;
+        }
     }
     if (block_reduce_store<1>(acc, partial, &st->counter)) {
         double d[1];
@@ -193,10 +245,21 @@ qmr_step_e(i64 n, i64 ld, T *Z, QmrState *st, double *partial)
     if (st->done) return;
     const T zv = T(st->ZVRAT);
     double acc[1] = {0.0};
-    for (i64 k = blockIdx.x * (i64)blockDim.x + threadIdx.x; k < n; k += (i64)gridDim.x * blockDim.x) {
-        const T z = Z[k] / zv;
-        Z[k] = z;
-        acc[0] += (double)z * (double)z;
+    if (use_vec4<T>(n)) {
+        float4 *Z4 = reinterpret_cast<float4 *>(Z);
+        const float f = (float)zv;
+        SC_GRID_LOOP4(k4, n >> 2) {
+            float4 z = Z4[k4];
+            z.x /= f; z.y /= f; z.z /= f; z.w /= f;
+            Z4[k4] = z;
+            acc[0] += (double)dot4(z, z);
+        }
+    } else {
+        for (i64 k = blockIdx.x * (i64)blockDim.x + threadIdx.x; k < n; k += (i64)gridDim.x * blockDim.x) {
+            const T z = Z[k] / zv;
+            Z[k] = z;
+            acc[0] += (double)z * (double)z;
+        }
     }
     if (block_reduce_store<1>(acc, partial, &st->counter)) {
         double d[1];
@@ -247,16 +310,47 @@ qmr_step_f(i64 n, i64 ld, const T *Q, const T *S, T *UX, T *UR, T *X, T *R, QmrS
     const T cq = T(st->cq), cs = T(st->cs), g = T(st->g);
     const int conv = abs(st->ntype);
     double acc[4] = {0.0, 0.0, 0.0, 0.0};
-    for (i64 k = blockIdx.x * (i64)blockDim.x + threadIdx.x; k < n; k += (i64)gridDim.x * blockDim.x) {
-        const T ux = first ? cq * Q[k] : cq * Q[k] + g * UX[k];
-        const T ur = first ? cs * S[k] : cs * S[k] + g * UR[k];
-        UX[k] = ux; UR[k] = ur;
-        const T x = X[k] + ux, r = R[k] - ur;
-        X[k] = x; R[k] = r;
-        acc[0] += (double)r * (double)r;
-        acc[1] += (double)ux * (double)ux;
-        acc[2] += (double)x * (double)x;
-        acc[3] += (double)ur * (double)ur;
+    if (use_vec4<T>(n)) {
+        const float4 *Q4 = reinterpret_cast<const float4 *>(Q), *S4 = reinterpret_cast<const float4 *>(S);
+        float4 *UX4 = reinterpret_cast<float4 *>(UX), *UR4 = reinterpret_cast<float4 *>(UR);
+        float4 *X4 = reinterpret_cast<float4 *>(X), *R4 = reinterpret_cast<float4 *>(R);
+        const float fq = (float)cq, fs = (float)cs, fg = (float)g;
+        SC_GRID_LOOP4(k4, n >> 2) {
+            const float4 q = Q4[k4], sv = S4[k4];
+            float4 ux, ur;
+            if (first) {
+                ux = make_float4(fq * q.x, fq * q.y, fq * q.z, fq * q.w);
+                ur = make_float4(fs * sv.x, fs * sv.y, fs * sv.z, fs * sv.w);
+            } else {
+                const float4 u0 = UX4[k4], u1 = UR4[k4];
+                ux = make_float4(fq * q.x + fg * u0.x, fq * q.y + fg * u0.y, fq * q.z + fg * u0.z, fq * q.w + fg * u0.w);
+                ur = make_float4(fs * sv.x + fg * u1.x, fs * sv.y + fg * u1.y, fs * sv.z + fg * u1.z,
+                                 fs * sv.w + fg * u1.w);
+            }
+            UX4[k4] = ux; UR4[k4] = ur;
+            float4 x = X4[k4], r = R4[k4];
+            x.x += ux.x; x.y += ux.y; x.z += ux.z; x.w += ux.w;
+            r.x -= ur.x; r.y -= ur.y; r.z -= ur.z; r.w -= ur.w;
+            X4[k4] = x; R4[k4] = r;
+            if (conv != 1) {
+                acc[0] += (double)dot4(r, r);
+                acc[1] += (double)dot4(ux, ux);
+                acc[2] += (double)dot4(x, x);
+                acc[3] += (double)dot4(ur, ur);
+            }
+        }
+    } else {
+        for (i64 k = blockIdx.x * (i64)blockDim.x + threadIdx.x; k < n; k += (i64)gridDim.x * blockDim.x) {
+            const T ux = first ? cq * Q[k] : cq * Q[k] + g * UX[k];
+            const T ur = first ? cs * S[k] : cs * S[k] + g * UR[k];
+            UX[k] = ux; UR[k] = ur;
+            const T x = X[k] + ux, r = R[k] - ur;
+            X[k] = x; R[k] = r;
+            acc[0] += (double)r * (double)r;
+            acc[1] += (double)ux * (double)ux;
+            acc[2] += (double)x * (double)x;
+            acc[3] += (double)ur * (double)ur;
+        }
     }
     if (conv == 1) return;  // the |HX-B|/|HX| test follows in step G
     if (block_reduce_store<4>(acc, partial, &st->counter)) {
@@ -284,11 +378,21 @@ qmr_step_g(i64 n, i64 ld, const T *HX0, const T *B, QmrState *st, double *partia
     { const int y = blockIdx.y; HX0 += y * ld; B += y * ld; st += y; partial += y * kPartStride; }
     if (st->done) return;
     double acc[2] = {0.0, 0.0};
-    for (i64 k = blockIdx.x * (i64)blockDim.x + threadIdx.x; k < n; k += (i64)gridDim.x * blockDim.x) {
-        const T h = HX0[k];
-        const T d = h - B[k];
-        acc[0] += (double)h * (double)h;
-        acc[1] += (double)d * (double)d;
+    if (use_vec4<T>(n)) {
+        const float4 *H4 = reinterpret_cast<const float4 *>(HX0), *B4 = reinterpret_cast<const float4 *>(B);
+        SC_GRID_LOOP4(k4, n >> 2) {
+            const float4 h = H4[k4], b = B4[k4];
+            const float4 d = make_float4(h.x - b.x, h.y - b.y, h.z - b.z, h.w - b.w);
+            acc[0] += (double)dot4(h, h);
+            acc[1] += (double)dot4(d, d);
+        }
+    } else {
+        for (i64 k = blockIdx.x * (i64)blockDim.x + threadIdx.x; k < n; k += (i64)gridDim.x * blockDim.x) {
+            const T h = HX0[k];
+            const T d = h - B[k];
+            acc[0] += (double)h * (double)h;
+            acc[1] += (double)d * (double)d;
+        }
     }
     if (block_reduce_store<2>(acc, partial, &st->counter)) {
         double d[2];
@@ -308,9 +412,18 @@ qmr_init_norms(i64 n, i64 ld, const T *B, const T *Z, QmrState *st, double *part
 {
     { const int y = blockIdx.y; B += y * ld; Z += y * ld; st += y; partial += y * kPartStride; }
     double acc[2] = {0.0, 0.0};
-    for (i64 k = blockIdx.x * (i64)blockDim.x + threadIdx.x; k < n; k += (i64)gridDim.x * blockDim.x) {
-        acc[0] += (double)B[k] * (double)B[k];
-        acc[1] += (double)Z[k] * (double)Z[k];
+    if (use_vec4<T>(n)) {
+        const float4 *B4 = reinterpret_cast<const float4 *>(B), *Z4 = reinterpret_cast<const float4 *>(Z);
+        SC_GRID_LOOP4(k4, n >> 2) {
+            const float4 b = B4[k4], z = Z4[k4];
+            acc[0] += (double)dot4(b, b);
+            acc[1] += (double)dot4(z, z);
+        }
+    } else {
+        for (i64 k = blockIdx.x * (i64)blockDim.x + threadIdx.x; k < n; k += (i64)gridDim.x * blockDim.x) {
+            acc[0] += (double)B[k] * (double)B[k];
+            acc[1] += (double)Z[k] * (double)Z[k];
+        }
     }
     if (block_reduce_store<2>(acc, partial, &st->counter)) {
         double d[2];
