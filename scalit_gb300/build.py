@@ -57,7 +57,7 @@ def build(force: bool = False, verbose: bool = False) -> str:
     with cf.ThreadPoolExecutor(max_workers=len(SOURCES)) as ex:
         objs = list(ex.map(compile_one, SOURCES))
     tmp = LIB + f".tmp{os.getpid()}"
-    cmd = [nvcc, *ARCH, "-shared", "-o", tmp, *objs, "-lcusolver",
+    cmd = [nvcc, *ARCH, "-shared", "-o", tmp, *objs, "-lcusolver", "-lpthread",
            "-Xlinker", "-rpath=/usr/local/cuda/lib64"]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:

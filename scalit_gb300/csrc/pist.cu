@@ -19,6 +19,8 @@
 #include <chrono>
 #include <cmath>
 #include <cstdio>
+#include <string>
+#include <thread>
 #include <vector>
 
 namespace sc {
@@ -707,7 +709,16 @@ int pist_core(scalit_ctx *c, i64 N, const scalit_pist_params *p, const double *d
     const bool overlap = !p->verbose;
     int pend_high = 0;     // cnt_high of the check queued on s2 (0: none)
 
-    auto ritz_launch = [&](int high) -> int {
+    // The check's launches are issued by a worker thread: cuSOLVER's host side
+    // takes ~8 ms a check at Krylov size ~500, during which the main thread
+    // already queues the next batch's QMR solves (the leading high x high
+    // block of HMAT that the check reads is final; later columns write rows
+    // and columns beyond it).  The worker is joined before the check is
+    // evaluated and before the solve returns.
+    std::thread ritz_worker;
+    int ritz_rc = 0;
+    std::string ritz_err;
+    auto ritz_launch_body = [&](int high) -> int {
         if (cusolverDnSetStream(sol, s2) != CUSOLVER_STATUS_SUCCESS) { set_error("cusolverDnSetStream failed"); return SCALIT_ECUDA; }
         const int nums[2] = {high - p->stepeig, high};
         for (int q = 0; q < 2; ++q) {
@@ -721,12 +732,35 @@ int pist_core(scalit_ctx *c, i64 N, const scalit_pist_params *p, const double *d
             SC_CUDA(cudaMemcpyAsync(hinfo + q, devinfo, sizeof(int), cudaMemcpyDeviceToHost, s2));
         }
         inf.checks += 2;
+        return 0;
+    };
+    auto ritz_join = [&]() -> int {
+        if (ritz_worker.joinable()) ritz_worker.join();
+        if (!ritz_rc) return 0;
+        set_error("%s", ritz_err.c_str());     // the worker's message (errors are per thread)
+        const int r = ritz_rc;
+        ritz_rc = 0;
+        return r;
+    };
+    auto ritz_launch = [&](int high) -> int {
+        const int r = ritz_join();
+        if (r) return r;
         pend_high = high;
+        const int dev = c->device;
+        ritz_worker = std::thread([&, high, dev] {
+            if (cudaSetDevice(dev) != cudaSuccess) { ritz_rc = SCALIT_ECUDA; ritz_err = "cudaSetDevice failed"; return; }
+            ritz_rc = ritz_launch_body(high);
+            if (ritz_rc) ritz_err = scalit_last_error();
+        });
         return 0;
     };
     // Evaluate the queued check (getWindow0 / getDiffMax / getSepMax on the host).
     auto ritz_settle = [&](bool *stop) -> int {
         const double t0 = now();
+        {
+            const int r = ritz_join();
+            if (r) { pend_high = 0; return r; }
+        }
         SC_CUDA(cudaStreamSynchronize(s2));
         inf.t_ritz += now() - t0;
         const int high = pend_high, num1 = high - p->stepeig;
@@ -768,6 +802,10 @@ int pist_core(scalit_ctx *c, i64 N, const scalit_pist_params *p, const double *d
         cnt_low = cnt_high + 1;
         if (last) { status = -MM; break; }
         cnt_high = std::min(cnt_high + p->stepcnt, MM);
+    }
+    {
+        const int r = ritz_join();
+        if (r && !rc) rc = r;
     }
     cudaStreamSynchronize(s2);
     cusolverDnSetStream(sol, s);
