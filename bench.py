@@ -267,8 +267,9 @@ def pist_leg(workload, levels, device, capi, hm, arms=("fp64", "fp32"), warmup=T
     eigs = {}
     # mixed leg: FP32 inner solves (H*X on the CUDA cores, the preconditioner's
     # rotations in split-BF16 x3 on the tensor cores) and an FP32 first
-    # Gram-Schmidt pass (the re-orthogonalisation pass, HMAT and the Ritz
-    # solves stay FP64)
+    # Gram-Schmidt pass (the re-orthogonalisation's projections, HMAT and the
+    # Ritz solves stay FP64; its update streams the basis' FP32 copy with
+    # coefficients split into two FP32 parts)
     for name, prec, orth in (("fp64", capi.PREC_FP64, 1), ("fp32", capi.PREC_FP32, 2)):
         if name not in arms:
             continue

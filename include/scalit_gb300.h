@@ -242,7 +242,10 @@ typedef struct {
                       /*    the basis orthonormal over long runs);       */
                       /* 2: as 1 with the first pass in FP32 against an  */
                       /*    FP32 copy of the basis (N x m_max floats);   */
-                      /*    the second pass stays FP64                   */
+                      /*    the second pass projects in FP64 and applies */
+                      /*    its (tiny) coefficients, split into two FP32 */
+                      /*    parts, over the FP32 copy: orthonormal to    */
+                      /*    FP64 round-off                               */
 } scalit_pist_params;
 
 typedef struct {

@@ -177,28 +177,51 @@ gemvt_partial_f32_kernel(i64 n, const float *VJf, const float *wf, double *parti
 }
 
 // v -= VJf(:, 0:m) h with the products summed in FP32 (four interleaved
-// partial sums) and the update applied to the FP64 vector.
+// partial sums) and the update applied to the FP64 vector.  SPLIT: h is taken
+// as hi + lo, two FP32 numbers (hi = fl32(h), lo = fl32(h - hi)), and the lo
+// products get their own FP32 sum, so rounding h to FP32 puts no error into
+// the span of the basis (the re-orthogonalisation's update, where h is tiny).
+template <bool SPLIT>
 __global__ void __launch_bounds__(kT)
 gemv_sub_f32_kernel(i64 n, int m, const float *VJf, const double *h, double *v)
 {
     __shared__ float hs[2048];
+    __shared__ float hl[SPLIT ? 2048 : 1];
     for (int i0 = 0; i0 < m; i0 += 2048) {
         const int cnt = min(2048, m - i0);
         __syncthreads();
-        for (int i = threadIdx.x; i < cnt; i += blockDim.x) hs[i] = (float)h[i0 + i];
+        for (int i = threadIdx.x; i < cnt; i += blockDim.x) {
+            const double hd = h[i0 + i];
+            const float hh = (float)hd;
+            hs[i] = hh;
+            if (SPLIT) hl[i] = (float)(hd - (double)hh);
+        }
         __syncthreads();
         for (i64 k = blockIdx.x * (i64)blockDim.x + threadIdx.x; k < n; k += (i64)gridDim.x * blockDim.x) {
-            float a0 = 0.f, a1 = 0.f, a2 = 0.f, a3 = 0.f;
+            float a0 = 0.f, a1 = 0.f, a2 = 0.f, a3 = 0.f, b = 0.f;
             const float *col = VJf + (i64)i0 * n + k;
             int i = 0;
             for (; i + 3 < cnt; i += 4) {
-                a0 = fmaf(col[(i64)i * n], hs[i], a0);
-                a1 = fmaf(col[(i64)(i + 1) * n], hs[i + 1], a1);
-                a2 = fmaf(col[(i64)(i + 2) * n], hs[i + 2], a2);
-                a3 = fmaf(col[(i64)(i + 3) * n], hs[i + 3], a3);
+                const float x0 = col[(i64)i * n], x1 = col[(i64)(i + 1) * n];
+                const float x2 = col[(i64)(i + 2) * n], x3 = col[(i64)(i + 3) * n];
+                a0 = fmaf(x0, hs[i], a0);
+                a1 = fmaf(x1, hs[i + 1], a1);
+                a2 = fmaf(x2, hs[i + 2], a2);
+                a3 = fmaf(x3, hs[i + 3], a3);
+                if (SPLIT) {
+                    b = fmaf(x0, hl[i], b);
+                    b = fmaf(x1, hl[i + 1], b);
+                    b = fmaf(x2, hl[i + 2], b);
+                    b = fmaf(x3, hl[i + 3], b);
+                }
             }
-            for (; i < cnt; ++i) a0 = fmaf(col[(i64)i * n], hs[i], a0);
-            v[k] -= (double)((a0 + a1) + (a2 + a3));
+            for (; i < cnt; ++i) {
+                const float x0 = col[(i64)i * n];
+                a0 = fmaf(x0, hs[i], a0);
+                if (SPLIT) b = fmaf(x0, hl[i], b);
+            }
+            if (SPLIT) v[k] -= (double)((a0 + a1) + (a2 + a3)) + (double)b;
+            else v[k] -= (double)((a0 + a1) + (a2 + a3));
         }
     }
 }
@@ -261,20 +284,29 @@ gemvt_partial_f32x4_kernel(i64 n, int m, const float *__restrict__ VJf, const fl
 }
 
 // v -= VJf(:, 0:m) h as gemv_sub_f32_kernel (the same four interleaved FP32
-// partial sums per point, so the same result), four points per thread.
+// partial sums per point and the same SPLIT form, so the same result), four
+// points per thread.
+template <bool SPLIT>
 __global__ void __launch_bounds__(kT)
 gemv_sub_f32x4_kernel(i64 n, int m, const float *__restrict__ VJf, const double *__restrict__ h,
                       double *__restrict__ v)
 {
     __shared__ float hs[2048];
+    __shared__ float hl[SPLIT ? 2048 : 1];
     const i64 k = 4 * (blockIdx.x * (i64)blockDim.x + threadIdx.x);
     for (int i0 = 0; i0 < m; i0 += 2048) {
         const int cnt = min(2048, m - i0);
         __syncthreads();
-        for (int i = threadIdx.x; i < cnt; i += blockDim.x) hs[i] = (float)h[i0 + i];
+        for (int i = threadIdx.x; i < cnt; i += blockDim.x) {
+            const double hd = h[i0 + i];
+            const float hh = (float)hd;
+            hs[i] = hh;
+            if (SPLIT) hl[i] = (float)(hd - (double)hh);
+        }
         __syncthreads();
         if (k >= n) continue;
         float a[4][4];
+        float bl[4] = {0.0f, 0.0f, 0.0f, 0.0f};
         #pragma unroll
         for (int e = 0; e < 4; ++e) a[e][0] = a[e][1] = a[e][2] = a[e][3] = 0.0f;
         const float *col = VJf + (i64)i0 * n + k;
@@ -290,6 +322,13 @@ gemv_sub_f32x4_kernel(i64 n, int m, const float *__restrict__ VJf, const double 
                 a[1][j] = fmaf(x[j].y, hj, a[1][j]);
                 a[2][j] = fmaf(x[j].z, hj, a[2][j]);
                 a[3][j] = fmaf(x[j].w, hj, a[3][j]);
+                if (SPLIT) {
+                    const float lj = hl[i + j];
+                    bl[0] = fmaf(x[j].x, lj, bl[0]);
+                    bl[1] = fmaf(x[j].y, lj, bl[1]);
+                    bl[2] = fmaf(x[j].z, lj, bl[2]);
+                    bl[3] = fmaf(x[j].w, lj, bl[3]);
+                }
             }
         }
         for (; i < cnt; ++i) {
@@ -299,13 +338,27 @@ gemv_sub_f32x4_kernel(i64 n, int m, const float *__restrict__ VJf, const double 
             a[1][0] = fmaf(x.y, hj, a[1][0]);
             a[2][0] = fmaf(x.z, hj, a[2][0]);
             a[3][0] = fmaf(x.w, hj, a[3][0]);
+            if (SPLIT) {
+                const float lj = hl[i];
+                bl[0] = fmaf(x.x, lj, bl[0]);
+                bl[1] = fmaf(x.y, lj, bl[1]);
+                bl[2] = fmaf(x.z, lj, bl[2]);
+                bl[3] = fmaf(x.w, lj, bl[3]);
+            }
         }
         double2 *vp = reinterpret_cast<double2 *>(v + k);
         double2 v0 = vp[0], v1 = vp[1];
-        v0.x -= (double)((a[0][0] + a[0][1]) + (a[0][2] + a[0][3]));
-        v0.y -= (double)((a[1][0] + a[1][1]) + (a[1][2] + a[1][3]));
-        v1.x -= (double)((a[2][0] + a[2][1]) + (a[2][2] + a[2][3]));
-        v1.y -= (double)((a[3][0] + a[3][1]) + (a[3][2] + a[3][3]));
+        if (SPLIT) {
+            v0.x -= (double)((a[0][0] + a[0][1]) + (a[0][2] + a[0][3])) + (double)bl[0];
+            v0.y -= (double)((a[1][0] + a[1][1]) + (a[1][2] + a[1][3])) + (double)bl[1];
+            v1.x -= (double)((a[2][0] + a[2][1]) + (a[2][2] + a[2][3])) + (double)bl[2];
+            v1.y -= (double)((a[3][0] + a[3][1]) + (a[3][2] + a[3][3])) + (double)bl[3];
+        } else {
+            v0.x -= (double)((a[0][0] + a[0][1]) + (a[0][2] + a[0][3]));
+            v0.y -= (double)((a[1][0] + a[1][1]) + (a[1][2] + a[1][3]));
+            v1.x -= (double)((a[2][0] + a[2][1]) + (a[2][2] + a[2][3]));
+            v1.y -= (double)((a[3][0] + a[3][1]) + (a[3][2] + a[3][3]));
+        }
         vp[0] = v0;
         vp[1] = v1;
     }
@@ -586,7 +639,11 @@ int pist_core(scalit_ctx *c, i64 N, const scalit_pist_params *p, const double *d
     // orth == 0: modified Gram-Schmidt in the reference's order (one pass);
     // orth == 1: classical Gram-Schmidt applied twice (GEMV-T then GEMV, x2);
     // orth == 2: the same with the first pass in FP32 against the basis' FP32
-    //            copy; the second pass (the re-orthogonalisation) in FP64.
+    //            copy; the second pass (the re-orthogonalisation) projects in
+    //            FP64, and its update v -= V h also streams the FP32 copy: h is
+    //            ~1e-7 |v| after the first pass, and the copy's rounding error
+    //            (2^-24 per element, random in sign) projects onto the basis at
+    //            ~1e-11, so V^T v after the update stays at FP64 round-off.
     auto mgs = [&](int J, bool *ok) -> int {
         double *v = vcol(J + 1);
         SC_CUDA(cudaMemcpyAsync(v, W, sizeof(double) * (size_t)N, cudaMemcpyDeviceToDevice, s));
@@ -612,15 +669,21 @@ int pist_core(scalit_ctx *c, i64 N, const scalit_pist_params *p, const double *d
                     }
                     gemvt_vec_kernel<<<(J + 127) / 128, 128, 0, s>>>(J, nchunk, partial, D);
                     if (vec4) {
-                        gemv_sub_f32x4_kernel<<<(int)((N / 4 + kT - 1) / kT), kT, 0, s>>>(N, J, VJf, D, v);
+                        gemv_sub_f32x4_kernel<false><<<(int)((N / 4 + kT - 1) / kT), kT, 0, s>>>(N, J, VJf, D, v);
                     } else {
-                        gemv_sub_f32_kernel<<<gr, kT, 0, s>>>(N, J, VJf, D, v);
+                        gemv_sub_f32_kernel<false><<<gr, kT, 0, s>>>(N, J, VJf, D, v);
                     }
                     continue;
                 }
                 gemvt_partial_kernel<<<dim3(nchunk, J), kT, 0, s>>>(N, J, VJ, v, partial, nchunk);
                 gemvt_vec_kernel<<<(J + 127) / 128, 128, 0, s>>>(J, nchunk, partial, D);
-                gemv_sub_kernel<<<gr, kT, 0, s>>>(N, J, VJ, D, v);
+                if (p->orth == 2 && vec4) {
+                    gemv_sub_f32x4_kernel<true><<<(int)((N / 4 + kT - 1) / kT), kT, 0, s>>>(N, J, VJf, D, v);
+                } else if (p->orth == 2) {
+                    gemv_sub_f32_kernel<true><<<gr, kT, 0, s>>>(N, J, VJf, D, v);
+                } else {
+                    gemv_sub_kernel<<<gr, kT, 0, s>>>(N, J, VJ, D, v);
+                }
             }
             mgs_kernel<<<gr, kT, 0, s>>>(N, v, nullptr, nullptr, nullptr, dnorm + 1, partial, counter);
         }

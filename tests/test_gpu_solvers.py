@@ -126,6 +126,28 @@ def test_pist_long_run_orthogonality(lib, orc):
     assert np.abs(eig2 - eig_r).max() * hm.HARTREE_CM < CM_TOL
 
 
+ORTH_TOL = 3e-15   # max |V^T V - I|: FP64 round-off; an FP32-rounded update coefficient gives ~1e-14
+
+
+@pytest.mark.parametrize("orth", [1, 2])
+def test_pist_basis_orthogonality(lib, orc, c0, orth):
+    """The Krylov basis after classical Gram-Schmidt twice is orthonormal to FP64
+    round-off, in FP64 (orth=1) and in the mixed form (orth=2: FP32 first pass,
+    FP64 projections and an FP32-streamed update with split coefficients)."""
+    e0 = float(c0.RES.min())
+    x0 = orc.start_vector(c0.N, 0)
+    with capi.Context.from_problem(c0, e0=e0) as ctx:
+        ctx.build_osb(20, 1e-4)
+        st, eig, res, info = ctx.pist(x0, 20, e0, 1e-11, m_max=400, qmr_max=500, qmr_tol=1e-4,
+                                      precision=capi.PREC_FP32, orth=orth, basis=True)
+    V = info["vj"]
+    assert st > 0 and V.shape[1] > 40
+    G = V.T @ V
+    err = np.abs(G - np.eye(G.shape[0])).max()
+    print(f"orth={orth} basis {V.shape[1]} vectors: max|V^T V - I| = {err:.3e}")
+    assert err < ORTH_TOL
+
+
 def test_pist_fp32_inner(lib, orc, c0):
     """Mixed precision: FP32 QMR inner solves, FP64 basis / HMAT / Ritz."""
     import scipy.sparse.linalg as sla
