@@ -391,3 +391,181 @@ def start_vector(N, seed=0):
     """Seeded uniform(0,1) start vector standing in for ``random_number(X)``
     (osbw.pistconv.h:35)."""
     return np.random.default_rng(seed).random(N)
+
+
+# ----------------------------------------------------------------------------------
+# OSBW window preconditioner (sOSB = TOSBW = 4), bound-state (real) form
+# ----------------------------------------------------------------------------------
+TOSBW = 4
+
+
+def osbw_size(EIG0, E0, DE):
+    """getOSBWSize (src/iterate/module/osb.osbw.h:62-73): states with |EIG0 - E0| <= DE."""
+    return int(np.count_nonzero(np.abs(np.asarray(EIG0) - E0) <= DE))
+
+
+def osbw_adjust(EIG0, E0, count, de, max_iter=2000):
+    """adjustWinSize (osb.osbw.h:118-145): doubles DE while the window holds
+    fewer than ``count`` states and bisects between the last two widths while
+    it holds more, until it holds exactly ``count``.  The reference loops
+    without a bound (forever when no width gives exactly ``count`` states,
+    e.g. tied EIG0 values, or when DE starts at 0); this restatement raises
+    ValueError after ``max_iter`` steps instead."""
+    EIG0 = np.asarray(EIG0, dtype=np.float64)
+    de1 = 0.0
+    cnt0 = osbw_size(EIG0, E0, de)
+    it = 0
+    while cnt0 != count:
+        if cnt0 < count:
+            de1 = de
+            de = 2.0 * de
+        else:
+            de = 0.5 * (de1 + de)
+        cnt0 = osbw_size(EIG0, E0, de)
+        it += 1
+        if it > max_iter:
+            raise ValueError(f"no window width holds exactly {count} states")
+    return de
+
+
+def osbw_index(EIG0, E0, DE):
+    """getOSBWIndex (osb.osbw.h:76-92): the window's grid indices in ascending
+    order (0-based here; the reference's are 1-based)."""
+    return np.nonzero(np.abs(np.asarray(EIG0) - E0) <= DE)[0]
+
+
+def osbw_level_index(sizes, ind):
+    """getLevelIndex (src/iterate/module/osb.vi.h:11-27): per level l the block
+    bk (the combined coordinates of the slower levels) and the column col
+    (the level-l coordinate) of each window state, both 0-based, shape
+    (len(sizes), len(ind))."""
+    sizes = np.asarray(sizes, dtype=np.int64)
+    dim = np.cumprod(np.concatenate(([1], sizes[:-1])))
+    clen = dim * sizes
+    ind = np.asarray(ind, dtype=np.int64)
+    bk = ind[None, :] // clen[:, None]
+    col = (ind[None, :] - bk * clen[:, None]) // dim[:, None]
+    return bk, col
+
+
+def vosb_starts(sizes):
+    """myVOSB%mStart (src/iterate/module/osb.init.h:37): level l's blocks of
+    sN(l) x sN(l) start after the lower levels' myBlk(l) sN(l)^2 entries."""
+    sizes = list(sizes)
+    vs, v = [], 0
+    for l, n in enumerate(sizes):
+        vs.append(v)
+        v += int(np.prod(sizes[l + 1:], dtype=np.int64)) * n * n
+    return vs
+
+
+def osbw_vi(sizes, VOSB, bk, col):
+    """getLevelVi / getVi (osb.vi.h:38-80): the preconditioner's basis vector of
+    one state, V_sF..V_1 applied to the unit vector -- a Kronecker product of
+    one column per level, v_sF x ... x v_1 (level 1 fastest), built in the
+    reference's order (level 1 first, each level multiplying the previous)."""
+    vs = vosb_starts(sizes)
+    Vi = np.ones(1)
+    for l, n in enumerate(sizes):
+        off = vs[l] + int(bk[l]) * n * n + int(col[l]) * n
+        Vi = np.kron(VOSB[off:off + n], Vi)
+    return Vi
+
+
+def osbw_hij(op, ind):
+    """getVOSBH0 (src/iterate/module/osb.hij.h:128-159): Hij(I, J) = Vi . (H Vj)
+    for I < J with H = MYHX(TA0) (HijX, osb.hx.h:29-36), mirrored, and
+    Hij(I, I) = EIG0(ind(I)).  H Vj is formed once per J (the reference forms
+    it again for every I; the values are the same)."""
+    m = len(ind)
+    bk, col = osbw_level_index(op.sizes, ind)
+    vec = [osbw_vi(op.sizes, op.VOSB, bk[:, i], col[:, i]) for i in range(m)]
+    H = np.zeros((m, m))
+    for J in range(m):
+        hv = op.hx(vec[J], 0)
+        for I in range(J):
+            H[I, J] = lib().orc_dot(op.N, _p(vec[I]), _p(hv))
+            H[J, I] = H[I, J]
+    for I in range(m):
+        H[I, I] = op.EIG0[ind[I]]
+    return H
+
+
+class OSBW:
+    """initOSBW for the bound-state job (osb.osbw.h:2-50 with getOSBWH through
+    getVOSBH0, and createWH, src/iterate/module/osb.pij.h:6-45): the window
+    of ``count`` states around E0, its matrix HW, and HWR = HW - shift I
+    (shift = E0 for TA1, 0 for TA0) factored by LAPACK DSYTRF('U')."""
+
+    def __init__(self, op, E0, count, de, npc=1, HW=None):
+        from scipy.linalg import lapack
+        if de <= 0.0:
+            raise ValueError("window width must be positive")
+        self.E0 = float(E0)
+        self.de = osbw_adjust(op.EIG0, E0, int(count), float(de))
+        self.ind = osbw_index(op.EIG0, E0, self.de)
+        if self.ind.size == 0:
+            raise ValueError("empty window")
+        self.HW = osbw_hij(op, self.ind) if HW is None else np.array(HW, dtype=np.float64)
+        HWR = self.HW.copy()
+        if npc != 0:
+            HWR[np.diag_indices_from(HWR)] -= self.E0
+        m = self.ind.size
+        self.ldu, self.ipiv, info = lapack.dsytrf(HWR, lower=0, lwork=6 * m)
+        if info != 0:
+            raise ValueError(f"DSYTRF info={info}")
+        self.HWR = HWR
+
+    def solve(self, wy):
+        """DSYTRS('U', hwLen, 1, HWR, WIPIV, WY) (osb.px.h:196-199)."""
+        from scipy.linalg import lapack
+        x, info = lapack.dsytrs(self.ldu, self.ipiv, np.asarray(wy, dtype=np.float64), lower=0)
+        if info != 0:
+            raise ValueError(f"DSYTRS info={info}")
+        return x
+
+
+def osbw_px(op, win, X, npc=1):
+    """MYPX with the TOSBW kernel (src/iterate/module/osb.px.h:125-148,191-206,
+    213-219): V^T of levels sF..1, the window entries WY = Y(WIND) solved
+    with the factored HWR, every other entry divided by EIG0 - E0, then V of
+    levels 1..sF."""
+    sizes = op.sizes
+    vs = vosb_starts(sizes)
+    dims = np.cumprod((1,) + sizes[:-1])
+    Y = _f64(X).copy()
+    nlev = len(sizes)
+    for l in range(nlev - 1, -1, -1):
+        blk = int(np.prod(sizes[l + 1:], dtype=np.int64))
+        lib().orc_vtx(int(dims[l]), sizes[l], blk, _p(op.VOSB[vs[l]:]), _p(Y))
+    E0 = 0.0 if npc == 0 else op.E0
+    wy = win.solve(Y[win.ind])
+    Y = Y / (op.EIG0 - E0)
+    Y[win.ind] = wy
+    for l in range(nlev):
+        blk = int(np.prod(sizes[l + 1:], dtype=np.int64))
+        lib().orc_vx(int(dims[l]), sizes[l], blk, _p(op.VOSB[vs[l]:]), _p(Y))
+    return Y
+
+
+def osbw_qmr(op, win, B, qmrmax, qmrtol, ntype=-1, mpi_codes=True):
+    """OSB_QMR with HX = MYHX(TA1) and PX = MYPX(TOSBW, TA1): returns
+    (status, X, RES, iterations)."""
+    N = op.N
+
+    def hx(_ctx, n, x, y):
+        xv = np.ctypeslib.as_array(x, shape=(N,))
+        np.ctypeslib.as_array(y, shape=(N,))[:] = op.hx(xv.copy(), 1)
+
+    def px(_ctx, n, x, y):
+        xv = np.ctypeslib.as_array(x, shape=(N,))
+        np.ctypeslib.as_array(y, shape=(N,))[:] = osbw_px(op, win, xv.copy(), 1)
+
+    fh, fp = _OP(hx), _OP(px)
+    B = _f64(B)
+    X = np.zeros_like(B)
+    res = C.c_double(0.0)
+    it = C.c_int(0)
+    rc = lib().orc_qmr(int(ntype), int(qmrmax), float(qmrtol), N, _p(B), fh, None, fp, None, _p(X),
+                       C.byref(res), int(bool(mpi_codes)), C.byref(it))
+    return rc, X, res.value, it.value
