@@ -42,6 +42,7 @@ extern "C" {
 #define SCALIT_TOSB 1   /* 1/(EIG0 - E0)                           */
 #define SCALIT_TOSBD1 2 /* +-1/DE inside the window |EIG0-E0| <= DE */
 #define SCALIT_TOSBD2 3 /* 1/(+-alpha + beta (EIG0-E0)) in window   */
+#define SCALIT_TOSBW 4  /* exact (H - E0)^-1 on a window of states    */
 
 /* engine of the FP64 H*X level products */
 #define SCALIT_FP64_DFMA 0   /* FP64 pipe (strided GEMM on CUDA cores)                 */
@@ -103,7 +104,9 @@ int scalit_set_fp64_mode(scalit_ctx *ctx, int mode);
 int scalit_set_fp32_mode(scalit_ctx *ctx, int mode);
 /* sOSBW%mE0: the shift of (H - E0) and of the preconditioner. */
 int scalit_set_shift(scalit_ctx *ctx, double e0);
-/* sOSB kernel kind with sOSBW%mDE and sOSBW%mBeta. */
+/* sOSB kernel kind with sOSBW%mDE and sOSBW%mBeta.  SCALIT_TOSBW needs a
+ * window made by scalit_build_osbw / scalit_set_osbw for the current
+ * preconditioner (SCALIT_ESTATE otherwise). */
 int scalit_set_precond(scalit_ctx *ctx, int osb_kind, double de, double beta);
 
 /* ---------------------------------------------------------------- H * X ---
@@ -151,9 +154,39 @@ int scalit_selftest_wait(scalit_ctx *ctx, double seconds);
 int scalit_get_osb(scalit_ctx *ctx, double *VOSB, double *EIG0);
 int scalit_set_osb(scalit_ctx *ctx, const double *VOSB, const double *EIG0);
 
+/* OSBW window preconditioner, bound-state job: initOSBW
+ * (src/iterate/module/osb.osbw.h:2-50) after the preconditioner build.
+ * The window width is adjusted (adjustWinSize, osb.osbw.h:118-145) until
+ * exactly `count` states satisfy |EIG0 - e0| <= de; *de is the starting width
+ * on entry and the final width on return.  HW(i, j) = <V_i | H | V_j> over the
+ * window's basis vectors with H = MYHX(TA0) and EIG0 on the diagonal
+ * (getVOSBH0, osb.hij.h:128-159); HWR = HW - shift I, shift = e0 for
+ * npc == SCALIT_TA1 and 0 for SCALIT_TA0, is factored (createWH,
+ * osb.pij.h:6-45) and the TOSBW kernel is selected for P*X (osb.px.h:191-206).
+ * *hwlen (may be null) receives the window size.  Errors: SCALIT_ESTATE
+ * before the preconditioner exists; SCALIT_EINVAL for count outside 1..N,
+ * de <= 0, no width holding exactly count states within 2000 steps (tied
+ * EIG0 values: the reference loops forever there) or a singular HWR (DSYTRF
+ * info > 0: createWH fails); SCALIT_ENOMEM when the count basis vectors
+ * (count x npoints doubles) do not fit.  Building the preconditioner again,
+ * set_osb or load leaves the window stale: P*X with TOSBW then returns
+ * SCALIT_ESTATE until the window is made again.  scalit_set_shift does not
+ * refactor HWR (the reference factors it once, at initOSBW). */
+int scalit_build_osbw(scalit_ctx *ctx, double e0, int count, double *de, int npc, int *hwlen);
+/* The last window: its size, its grid points (0-based, ascending: WIND - 1)
+ * and HW (hwlen x hwlen, column-major: the array saveHW writes,
+ * osb.io.h:297-319).  Any output pointer may be null. */
+int scalit_get_osbw(scalit_ctx *ctx, int *hwlen, int *ind, double *hw);
+/* loadHW (osb.io.h:240-264) then createWH: the window is selected as
+ * scalit_build_osbw selects it, HW (count x count, column-major) is taken
+ * from the caller instead of being formed, and HWR is factored. */
+int scalit_set_osbw(scalit_ctx *ctx, double e0, int count, double *de, int npc, const double *hw);
+
 /* MYPX (src/iterate/module/osb.px.h:125-219; MPI mosb3.px.h:7-132):
  *   Y = V_sF..V_1 K^-1 V_1^T..V_sF^T X, K^-1 from the sOSB kind,
- * E0 = 0 for npc == TA0, sOSBW%mE0 otherwise. */
+ * E0 = 0 for npc == TA0, sOSBW%mE0 otherwise.  With SCALIT_TOSBW the
+ * window's entries take HWR^-1 (factored once, with the shift given to
+ * scalit_build_osbw) and the others 1/(EIG0 - E0). */
 int scalit_px(scalit_ctx *ctx, int npc, int nvec, const double *X, double *Y);
 int scalit_px_device(scalit_ctx *ctx, int npc, int nvec, const double *dX, double *dY);
 int scalit_px_f32_device(scalit_ctx *ctx, int npc, int nvec, const float *dX, float *dY);
@@ -386,6 +419,11 @@ void scalit_fortran_init_(const int *sf, const int *sn, const int *sdep, const d
                           const double *RES, const double *DEP, const double *e0, int *ierr);
 void scalit_fortran_precond_(const int *sosb, const double *de, const double *beta,
                              const int *bjmax, const double *bjtol, int *ierr);
+/* initOSBW (osb.osbw.h:2-50) on the module state, after scalit_fortran_precond_
+ * with sOSB = 4 (which builds the preconditioner only): the window of
+ * sOSBW%mCnt states around sOSBW%mE0 from the width sOSBW%mDE (updated in
+ * place, as adjustWinSize updates it), factored for sPC = npc; selects TOSBW. */
+void scalit_fortran_osbw_(const double *e0, const int *cnt, double *de, const int *npc, int *ierr);
 void scalit_fortran_qmr_param_(const int *ntype, const int *qmrmax, const double *qmrtol,
                                const int *precision);
 void scalit_fortran_final_(void);

@@ -13,7 +13,7 @@ import numpy as np
 from . import build as _build
 
 TA0, TA1 = 0, 1
-TOSB, TOSBD1, TOSBD2 = 1, 2, 3
+TOSB, TOSBD1, TOSBD2, TOSBW = 1, 2, 3, 4
 FP32_SIMT, FP32_TENSOR, FP32_TENSOR_PX = 0, 1, 2
 PREC_FP64, PREC_FP32 = 0, 1
 FP64_DFMA, FP64_TENSOR = 0, 1
@@ -49,6 +49,9 @@ SIGNATURES = {
     "scalit_tile_picks": (C.c_int, [_vp, _ip]),
     "scalit_get_osb": (C.c_int, [_vp, _dp, _dp]),
     "scalit_set_osb": (C.c_int, [_vp, _dp, _dp]),
+    "scalit_build_osbw": (C.c_int, [_vp, C.c_double, C.c_int, _dp, C.c_int, _ip]),
+    "scalit_set_osbw": (C.c_int, [_vp, C.c_double, C.c_int, _dp, C.c_int, _dp]),
+    "scalit_get_osbw": (C.c_int, [_vp, _ip, _ip, _dp]),
     "scalit_px": (C.c_int, [_vp, C.c_int, C.c_int, _dp, _dp]),
     "scalit_px_device": (C.c_int, [_vp, C.c_int, C.c_int, _vp, _vp]),
     "scalit_px_f32_device": (C.c_int, [_vp, C.c_int, C.c_int, _vp, _vp]),
@@ -95,6 +98,7 @@ SIGNATURES = {
     "scalit_fortran_device_": (None, [_ip]),
     "scalit_fortran_init_": (None, [_ip, _ip, _ip, _dp, _dp, _dp, _dp, _ip]),
     "scalit_fortran_precond_": (None, [_ip, _dp, _dp, _ip, _dp, _ip]),
+    "scalit_fortran_osbw_": (None, [_dp, _ip, _dp, _ip, _ip]),
     "scalit_fortran_qmr_param_": (None, [_ip, _ip, _dp, _ip]),
     "scalit_fortran_final_": (None, []),
     "scalit_hx0_": (None, [_ip, _dp, _dp]),
@@ -285,6 +289,31 @@ class Context:
     def set_osb(self, VOSB, EIG0):
         V, E = _f64(VOSB), _f64(EIG0)
         _check(self.lib.scalit_set_osb(self.h, _p(V), _p(E)))
+
+    def build_osbw(self, e0, count, de, npc=TA1):
+        """initOSBW: the window of ``count`` states around ``e0`` (starting width
+        ``de``), its matrix HW and factor; selects TOSBW.  Returns (hwlen, de)."""
+        d = C.c_double(float(de))
+        m = C.c_int(0)
+        _check(self.lib.scalit_build_osbw(self.h, float(e0), int(count), C.byref(d), int(npc), C.byref(m)))
+        return m.value, d.value
+
+    def set_osbw(self, e0, count, de, HW, npc=TA1):
+        """loadHW + createWH: the window selected as build_osbw selects it, HW
+        (count x count) given.  Returns the final width."""
+        d = C.c_double(float(de))
+        hw = np.ascontiguousarray(np.asarray(HW, dtype=np.float64).ravel(order="F"))
+        _check(self.lib.scalit_set_osbw(self.h, float(e0), int(count), C.byref(d), int(npc), _p(hw)))
+        return d.value
+
+    def get_osbw(self):
+        """(ind, HW): the window's grid points (0-based) and its matrix."""
+        m = C.c_int(0)
+        _check(self.lib.scalit_get_osbw(self.h, C.byref(m), None, None))
+        ind = np.zeros(m.value, dtype=np.int32)
+        hw = np.zeros(m.value * m.value)
+        _check(self.lib.scalit_get_osbw(self.h, None, ind.ctypes.data_as(_ip), _p(hw)))
+        return ind.astype(np.int64), hw.reshape(m.value, m.value, order="F")
 
     def px(self, X, npc=TA1):
         X = _f64(X)

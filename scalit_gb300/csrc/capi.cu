@@ -169,6 +169,7 @@ void scalit_destroy(scalit_ctx *c)
         if (l == 0) { tc_free_px(c); tc32_free(c, true, true); }
     }
     if (c->tc_err) cudaFree(c->tc_err);
+    osbw_free(c);
     for (int i = 0; i < 2; ++i) if (c->qg[i].exec) cudaGraphExecDestroy(c->qg[i].exec);
     if (c->red_counter) cudaFree(c->red_counter);
     if (c->work) cudaFree(c->work);
@@ -266,6 +267,7 @@ int scalit_load(scalit_ctx *c, const double *H0, const double *RES, const double
     if (rc) return rc;
     c->loaded = true;
     c->osb_built = false;
+    osbw_invalidate(c);
     c->gen++;
     return 0;
 }
@@ -325,8 +327,11 @@ int scalit_set_shift(scalit_ctx *c, double e0)
 int scalit_set_precond(scalit_ctx *c, int kind, double de, double beta)
 {
     if (!c) { set_error("null context"); return SCALIT_EINVAL; }
-    if (kind == 4) { set_error("the OSBW window preconditioner (sOSB=4) is not supported"); return SCALIT_EUNSUP; }
-    if (kind < 1 || kind > 3) { set_error("unknown preconditioner kind %d", kind); return SCALIT_EINVAL; }
+    if (kind < 1 || kind > 4) { set_error("unknown preconditioner kind %d", kind); return SCALIT_EINVAL; }
+    if (kind == SCALIT_TOSBW && !(c->osbw_len > 0 && c->osbw_valid)) {
+        set_error("TOSBW needs a window for the current preconditioner: call scalit_build_osbw or scalit_set_osbw");
+        return SCALIT_ESTATE;
+    }
     if ((kind == SCALIT_TOSBD1 || kind == SCALIT_TOSBD2) && !(fabs(de) > 0.0)) {
         set_error("windowed preconditioner needs DE != 0");
         return SCALIT_EINVAL;
@@ -477,10 +482,39 @@ int scalit_set_osb(scalit_ctx *c, const double *VOSB, const double *EIG0)
     if (rc) return rc;
     SC_CUDA(cudaStreamSynchronize(c->stream));
     c->osb_built = true;
+    osbw_invalidate(c);
     c->gen++;
     rc = tc_prepare_px(c);
     if (!rc) rc = tc32_prepare(c, true);
     return rc;
+}
+
+// ---------------------------------------------------------- OSBW window ---
+int scalit_build_osbw(scalit_ctx *c, double e0, int count, double *de, int npc, int *hwlen)
+{
+    CTX_CHECK(c);
+    return osbw_make(c, e0, count, de, npc, nullptr, hwlen);
+}
+
+int scalit_set_osbw(scalit_ctx *c, double e0, int count, double *de, int npc, const double *hw)
+{
+    CTX_CHECK(c);
+    if (!hw) { set_error("HW is required"); return SCALIT_EINVAL; }
+    if (count < 1) { set_error("OSBW window size %d < 1", count); return SCALIT_EINVAL; }
+    if (!all_finite(hw, (i64)count * count)) { set_error("non-finite HW"); return SCALIT_ENONFINITE; }
+    return osbw_make(c, e0, count, de, npc, hw, nullptr);
+}
+
+int scalit_get_osbw(scalit_ctx *c, int *hwlen, int *ind, double *hw)
+{
+    CTX_CHECK(c);
+    if (c->osbw_len <= 0) { set_error("no OSBW window"); return SCALIT_ESTATE; }
+    const int m = c->osbw_len;
+    if (hwlen) *hwlen = m;
+    if (ind) SC_CUDA(cudaMemcpyAsync(ind, c->osbw_ind, sizeof(int) * (size_t)m, cudaMemcpyDeviceToHost, c->stream));
+    if (hw) SC_CUDA(cudaMemcpyAsync(hw, c->osbw_hw, sizeof(double) * (size_t)m * m, cudaMemcpyDeviceToHost, c->stream));
+    SC_CUDA(cudaStreamSynchronize(c->stream));
+    return 0;
 }
 
 // ------------------------------------------------------------------ QMR --
@@ -1180,9 +1214,20 @@ void scalit_fortran_precond_(const int *sosb, const double *de, const double *be
                              const double *bjtol, int *ierr)
 {
     std::lock_guard<std::mutex> lk(g_fmu);
-    int rc = g_fctx ? scalit_set_precond(g_fctx, *sosb, *de, *beta) : SCALIT_ESTATE;
+    // sOSB = TOSBW: the drivers call initOSBW after progDiag (osb.progPX.h:28-35),
+    // here scalit_fortran_osbw_, which selects TOSBW once the window exists.
+    const int kind = (*sosb == SCALIT_TOSBW) ? SCALIT_TOSB : *sosb;
+    int rc = g_fctx ? scalit_set_precond(g_fctx, kind, *de, *beta) : SCALIT_ESTATE;
     if (!rc) rc = scalit_build_osb(g_fctx, *bjmax, *bjtol, nullptr);
     if (rc) report("scalit_fortran_precond", rc);
+    if (ierr) *ierr = rc;
+}
+
+void scalit_fortran_osbw_(const double *e0, const int *cnt, double *de, const int *npc, int *ierr)
+{
+    std::lock_guard<std::mutex> lk(g_fmu);
+    const int rc = g_fctx ? scalit_build_osbw(g_fctx, *e0, *cnt, de, *npc, nullptr) : SCALIT_ESTATE;
+    if (rc) report("scalit_fortran_osbw", rc);
     if (ierr) *ierr = rc;
 }
 

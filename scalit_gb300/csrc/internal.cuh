@@ -74,6 +74,17 @@ struct scalit_ctx {
     double E0 = 0.0;
     int osb_kind = SCALIT_TOSB;
     double osb_de = 0.0, osb_beta = 0.0;
+    // OSBW window (sOSB = TOSBW): its grid points, HW (column-major), the
+    // inverse of HW - shift I in FP64 and FP32 (both triangles), and room for
+    // the gathered window entries of one P*X.  osbw_valid turns false when
+    // the preconditioner the window was made from changes.
+    int osbw_len = 0;
+    bool osbw_valid = false;
+    int *osbw_ind = nullptr;
+    double *osbw_hw = nullptr, *osbw_inv = nullptr;
+    float *osbw_invf = nullptr;
+    void *osbw_wy = nullptr;
+    double osbw_e0 = 0.0, osbw_de = 0.0;
     // workspace (grown on demand)
     void *work = nullptr;
     size_t work_bytes = 0;
@@ -203,6 +214,17 @@ int tc_check_error(scalit_ctx *c);
 int wait_selftest(scalit_ctx *c, double seconds);
 int tc_gemm_f64(const scalit_ctx *c, int M, int N, int K, const double *A, i64 lda, const double *B, i64 ldb,
                 double *C, i64 ldc, cudaStream_t s);
+
+// ---------------------------------------------------------- OSBW window --
+// initOSBW for the bound-state job: window width and points, HW (formed, or
+// taken from hw_host), the inverse of HW - shift I; selects TOSBW.
+int osbw_make(scalit_ctx *c, double e0, int count, double *de, int npc, const double *hw_host, int *hwlen);
+void osbw_free(scalit_ctx *c);
+void osbw_invalidate(scalit_ctx *c);
+// The TOSBW kernel step of P*X in place on Z = V^T X: the window entries
+// solved with the window matrix, all others divided by EIG0 - e0, times alpha.
+template <class T>
+int osbw_window_apply(const scalit_ctx *c, T *Z, const T *EIG, double e0, T alpha, const int *gate, cudaStream_t s);
 
 // ------------------------------------------------------------- OSB build --
 int osb_build(scalit_ctx *c, int bjmax, double bjtol, double *stats);

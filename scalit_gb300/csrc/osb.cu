@@ -830,7 +830,7 @@ int osb_build(scalit_ctx *c, int bjmax, double bjtol, double *stats)
     if (rc) return rc;
     rc = to_f32(c->EIG0, c->EIG0f, L.N, s);
     if (!rc) rc = to_f32(c->VOSB, c->VOSBf, L.vlen, s);
-    if (!rc) { c->osb_built = true; c->gen++; }
+    if (!rc) { c->osb_built = true; osbw_invalidate(c); c->gen++; }
     SC_CUDA(cudaStreamSynchronize(s));
     if (!rc) rc = tc_prepare_px(c);
     if (!rc) rc = tc32_prepare(c, true);

@@ -492,12 +492,52 @@ static int rotate(const scalit_ctx *c, int l, int transpose, const T *V, const T
     return level_rotate<T>((int)L.dim[l], L.n[l], (int)L.blk[l], V + L.vs[l], in, out, transpose, gate, s);
 }
 
+// MYPX with the TOSBW kernel (osb.px.h:191-206): the level-1 rotations are
+// not fused with the kernel step, whose window entries couple blocks.
+// Stages: V^T of levels sF..1, the window step in place, V of levels 1..sF.
+template <class T>
+static int px_vec_window(const scalit_ctx *c, int npc, const T *X, T *Y, T *tmp, T alpha, const int *gate,
+                         cudaStream_t s)
+{
+    const Layout &L = c->L;
+    if (!(c->osbw_len > 0 && c->osbw_valid)) {
+        set_error("TOSBW P*X without a window for the current preconditioner: call scalit_build_osbw again");
+        return SCALIT_ESTATE;
+    }
+    const T *V = pickp<T>(c->VOSB, c->VOSBf);
+    const T *EIG = pickp<T>(c->EIG0, c->EIG0f);
+    const int S = 2 * L.nlev;
+    T *buf[2] = {Y, tmp};
+    const T *in = X;
+    int stage = 0, rc;
+    for (int l = L.nlev - 1; l >= 0; --l) {
+        ++stage;
+        T *out = buf[(S - stage) % 2];
+        rc = (l == 0) ? level_rotate<T>(1, L.n[0], (int)L.blk[0], V + L.vs[0], in, out, 1, gate, s)
+                      : rotate<T>(c, l, 1, V, in, out, gate, s);
+        if (rc) return rc;
+        in = out;
+    }
+    rc = osbw_window_apply<T>(c, const_cast<T *>(in), EIG, npc == SCALIT_TA0 ? 0.0 : c->E0, alpha, gate, s);
+    if (rc) return rc;
+    for (int l = 0; l < L.nlev; ++l) {
+        ++stage;
+        T *out = buf[(S - stage) % 2];
+        rc = (l == 0) ? level_rotate<T>(1, L.n[0], (int)L.blk[0], V + L.vs[0], in, out, 0, gate, s)
+                      : rotate<T>(c, l, 0, V, in, out, gate, s);
+        if (rc) return rc;
+        in = out;
+    }
+    return 0;
+}
+
 template <class T>
 int px_vec(const scalit_ctx *c, int npc, const T *X, T *Y, T *tmp, T alpha, const int *gate,
            cudaStream_t s)
 {
     const Layout &L = c->L;
     if (!c->osb_built) { set_error("P*X before the preconditioner was built or loaded"); return SCALIT_ESTATE; }
+    if (c->osb_kind == SCALIT_TOSBW) return px_vec_window<T>(c, npc, X, Y, tmp, alpha, gate, s);
     const T *V = pickp<T>(c->VOSB, c->VOSBf);
     const T *EIG = pickp<T>(c->EIG0, c->EIG0f);
     KernelParams kp{c->osb_kind, npc == SCALIT_TA0 ? 0.0 : c->E0, c->osb_de, c->osb_beta};
@@ -540,6 +580,10 @@ int px_multi(const scalit_ctx *c, const T *X, T *Y, T *tmp, int nvec, const doub
 {
     const Layout &L = c->L;
     if (!c->osb_built) { set_error("P*X before the preconditioner was built or loaded"); return SCALIT_ESTATE; }
+    if (c->osb_kind == SCALIT_TOSBW) {
+        set_error("the OSBW window is factored for one shift: per-vector shifts need TOSB, TOSBD1 or TOSBD2");
+        return SCALIT_EUNSUP;
+    }
     if (nvec < 1) return 0;
     const T *V = pickp<T>(c->VOSB, c->VOSBf);
     const T *EIG = pickp<T>(c->EIG0, c->EIG0f);

@@ -25,8 +25,6 @@ class OSB:
     def __init__(self, inp: refio.OSBInput, device: int = 0, precision: int = capi.PREC_FP64):
         if inp.sCX:
             raise ValueError("complex Hamiltonians (sCX) are not supported")
-        if inp.sOSB == refio.TOSBW:
-            raise ValueError("the OSBW window preconditioner (sOSB=4) is not supported")
         self.inp = inp
         self.device = device
         self.precision = precision
@@ -78,6 +76,28 @@ class OSB:
                 refio.save_data_dir(inp.EigFile, E)
         if log:
             log(f" Time for block diagonalization (s): {time.perf_counter() - t0:.3f}")
+        if inp.sOSB == refio.TOSBW:
+            self.init_osbw(log)
+
+    # initOSBW (osb.osbw.h:2-50), bound-state job: sHW >= 0 forms the window
+    # matrix (sHW > 0 also writes it, saveHW), sHW < 0 reads it (loadHW)
+    def init_osbw(self, log=print):
+        inp = self.inp
+        mE0, mDE, mBeta, mCnt = inp.sOSBW
+        t0 = time.perf_counter()
+        if log:
+            log(f" original window width: {mDE}  size: {mCnt}")
+        if inp.sHW >= 0:
+            _, de = self.ctx.build_osbw(mE0, mCnt, mDE, capi.TA1)
+            if inp.sHW > 0:
+                _, HW = self.ctx.get_osbw()
+                refio.save_hw(inp.HWFile, HW)
+        else:
+            de = self.ctx.set_osbw(mE0, mCnt, mDE, refio.load_hw(inp.HWFile, mCnt), capi.TA1)
+        inp.sOSBW = (mE0, de, mBeta, mCnt)             # adjustWinSize updates sOSBW%mDE
+        if log:
+            log(f" final window width: {de}  window size: {mCnt}")
+            log(f" Time to calculate Hij for Energy Window: {time.perf_counter() - t0:.3f}")
 
     # OSB_PISTCONV (osbw.pistconv.h:16-50) with setPISTConvParam (:303-333)
     def pist(self, x0=None, seed=0, verbose=False, basis=False):

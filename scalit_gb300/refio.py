@@ -309,6 +309,57 @@ def load_pist_basis(path):
     return cnt, ritz, hmat, vj
 
 
+def save_hw(path, hw, binary: bool = True) -> None:
+    """The HW file of the OSBW window (saveHW, src/iterate/module/osb.io.h:297-319):
+    unformatted sequential records (count) / HW(count, count), or with
+    ``binary=False`` the list-directed text form (count, then HW column by
+    column)."""
+    hw = np.asarray(hw, dtype=np.float64)
+    cnt = hw.shape[0]
+    if hw.shape != (cnt, cnt):
+        raise ValueError("HW must be square")
+    if binary:
+        save_records(path, [struct.pack("<i", cnt), np.asfortranarray(hw, dtype="<f8").tobytes(order="F")])
+        return
+    with open(path, "w") as f:
+        f.write(f" {cnt}\n")
+        flat = hw.ravel(order="F")
+        for i in range(0, flat.size, 3):
+            f.write(" " + " ".join(repr(float(v)) for v in flat[i:i + 3]) + "\n")
+
+
+def load_hw(path, count: int, binary: bool = True) -> np.ndarray:
+    """loadHW (osb.io.h:240-264): the HW file of a window of ``count`` states;
+    ValueError when the file holds another count (loadHW returns .false.).
+    The text form accepts Fortran list-directed repeats (``r*value``)."""
+    if binary:
+        r = load_records(path)
+        if len(r) < 2 or len(r[0]) < 4:
+            raise ValueError(f"{path}: not an HW file")
+        cnt = struct.unpack("<i", r[0][:4])[0]
+        if cnt != count:
+            raise ValueError(f"{path}: window of {cnt} states, expected {count}")
+        a = np.frombuffer(r[1], dtype="<f8")
+        if a.size != cnt * cnt:
+            raise ValueError(f"{path}: truncated HW")
+        return a.reshape(cnt, cnt, order="F").copy()
+    with open(path) as f:
+        toks = f.read().replace(",", " ").split()
+    vals = []
+    for t in toks:
+        if "*" in t:
+            rep, v = t.split("*", 1)
+            vals.extend([_real(v)] * int(rep))
+        else:
+            vals.append(_real(t))
+    if not vals or int(vals[0]) != count:
+        raise ValueError(f"{path}: window of {int(vals[0]) if vals else 0} states, expected {count}")
+    a = np.array(vals[1:1 + count * count], dtype=np.float64)
+    if a.size != count * count:
+        raise ValueError(f"{path}: truncated HW")
+    return a.reshape(count, count, order="F")
+
+
 def load_data(path, n: int) -> np.ndarray:
     """Read the first ``n`` doubles of an unformatted sequential record."""
     out = bytearray()

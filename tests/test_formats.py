@@ -138,3 +138,21 @@ def test_pist_basis_file_roundtrip(tmp_path):
     np.testing.assert_array_equal(r2, ritz)
     np.testing.assert_array_equal(h2, hmat)
     np.testing.assert_array_equal(v2, vj)
+
+
+def test_hw_file_roundtrip(tmp_path):
+    """saveHW / loadHW (osb.io.h:240-319), both forms; a file of another window size is refused."""
+    rng = np.random.default_rng(4)
+    a = rng.standard_normal((6, 6))
+    hw = (a + a.T) / 2
+    for binary in (True, False):
+        path = tmp_path / f"hw_{binary}.dat"
+        refio.save_hw(path, hw, binary=binary)
+        np.testing.assert_array_equal(refio.load_hw(path, 6, binary=binary), hw)
+        with pytest.raises(ValueError):
+            refio.load_hw(path, 5, binary=binary)
+    raw = (tmp_path / "hw_True.dat").read_bytes()
+    assert int.from_bytes(raw[:4], "little") == 4 and int.from_bytes(raw[4:8], "little") == 6
+    txt = tmp_path / "hw_rep.txt"                       # list-directed repeats: r*value, D exponents
+    txt.write_text(" 2\n 2*1.5D0 0.25\n -3.0\n")
+    np.testing.assert_array_equal(refio.load_hw(txt, 2, binary=False), [[1.5, 0.25], [1.5, -3.0]])
