@@ -161,13 +161,16 @@ int scalit_set_osb(scalit_ctx *ctx, const double *VOSB, const double *EIG0);
  * on entry and the final width on return.  HW(i, j) = <V_i | H | V_j> over the
  * window's basis vectors with H = MYHX(TA0) and EIG0 on the diagonal
  * (getVOSBH0, osb.hij.h:128-159); HWR = HW - shift I, shift = e0 for
- * npc == SCALIT_TA1 and 0 for SCALIT_TA0, is factored (createWH,
- * osb.pij.h:6-45) and the TOSBW kernel is selected for P*X (osb.px.h:191-206).
+ * npc == SCALIT_TA1 and 0 for SCALIT_TA0, is inverted once (createWH,
+ * osb.pij.h:6-45, factors it for DSYTRS; here its symmetric eigen-decomposition
+ * gives HWR^-1, equal to the factor's solve to rounding) and the TOSBW kernel
+ * is selected for P*X (osb.px.h:191-206).
  * *hwlen (may be null) receives the window size.  Errors: SCALIT_ESTATE
  * before the preconditioner exists; SCALIT_EINVAL for count outside 1..N,
  * de <= 0, no width holding exactly count states within 2000 steps (tied
- * EIG0 values: the reference loops forever there) or a singular HWR (DSYTRF
- * info > 0: createWH fails); SCALIT_ENOMEM when the count basis vectors
+ * EIG0 values: the reference loops forever there) or a singular HWR (an
+ * exactly zero eigenvalue, where DSYTRF reports info > 0 and createWH fails);
+ * SCALIT_ENOMEM when the count basis vectors
  * (count x npoints doubles) do not fit.  Building the preconditioner again,
  * set_osb or load leaves the window stale: P*X with TOSBW then returns
  * SCALIT_ESTATE until the window is made again.  scalit_set_shift does not
@@ -179,7 +182,7 @@ int scalit_build_osbw(scalit_ctx *ctx, double e0, int count, double *de, int npc
 int scalit_get_osbw(scalit_ctx *ctx, int *hwlen, int *ind, double *hw);
 /* loadHW (osb.io.h:240-264) then createWH: the window is selected as
  * scalit_build_osbw selects it, HW (count x count, column-major) is taken
- * from the caller instead of being formed, and HWR is factored. */
+ * from the caller instead of being formed, and HWR is inverted. */
 int scalit_set_osbw(scalit_ctx *ctx, double e0, int count, double *de, int npc, const double *hw);
 
 /* MYPX (src/iterate/module/osb.px.h:125-219; MPI mosb3.px.h:7-132):

@@ -15,10 +15,11 @@
 // their Gram product, split over the grid points and reduced in a fixed
 // order.  The reference forms H V_j again for every i < j (count^2 / 2
 // H*X); here each H V_j is formed once.  HWR is factored by cuSOLVER's
-// Bunch-Kaufman DSYTRF and inverted by DSYTRI once per window; P*X applies
-// the inverse as a dense symmetric product (one warp per window row), which
-// equals DSYTRS's solve to rounding times the condition of HWR and keeps
-// every P*X launch library-free (capturable in the QMR's CUDA graphs).
+// symmetric eigen-decomposition (syevd) once per window and inverted as
+// Q diag(1/w) Q^T; P*X applies the inverse as a dense symmetric product (one
+// warp per window row), which equals the reference's DSYTRF/DSYTRS solve to
+// rounding times the condition of HWR and keeps every P*X launch
+// library-free (capturable in the QMR's CUDA graphs).
 #include "internal.cuh"
 
 #include <cusolverDn.h>
@@ -161,13 +162,17 @@ __global__ void osbw_shift_kernel(int m, const double *__restrict__ HW, double s
     A[e] = HW[e] - (i == j ? shift : 0.0);
 }
 
-// DSYTRI leaves the inverse in the upper triangle: mirror it to the lower.
-__global__ void osbw_mirror_kernel(int m, double *A)
+// A(i, j) = sum_k Q(i, k) Q(j, k) r(k), r = 1/w: the inverse from the
+// eigenpairs, the same sum for (i, j) and (j, i), so A is exactly symmetric.
+__global__ void osbw_inverse_kernel(int m, const double *__restrict__ Q, const double *__restrict__ r,
+                                    double *__restrict__ A)
 {
     const i64 e = blockIdx.x * (i64)blockDim.x + threadIdx.x;
     if (e >= (i64)m * m) return;
     const int i = (int)(e % m), j = (int)(e / m);
-    if (i > j) A[e] = A[j + (i64)i * m];
+    double acc = 0.0;
+    for (int k = 0; k < m; ++k) acc = fma(Q[i + (i64)k * m] * Q[j + (i64)k * m], r[k], acc);
+    A[e] = acc;
 }
 
 // P*X window step, in place on Z = V^T X (osb.px.h:191-206):
@@ -292,68 +297,87 @@ static int form_hw(scalit_ctx *c, int m, const int *d_ind, const std::vector<i64
     return rc;
 }
 
-// HWR = HW - shift I -> its inverse (both triangles, FP64 and FP32).
+// HWR = HW - shift I -> its inverse (both triangles, FP64 and FP32) from the
+// symmetric eigen-decomposition HWR = Q diag(w) Q^T (cuSOLVER syevd):
+// HWR^-1 = Q diag(1/w) Q^T.  An exactly zero eigenvalue is the singular case
+// DSYTRF reports with info > 0 (createWH fails).
 static int invert_hwr(scalit_ctx *c, int m, double shift, cudaStream_t s)
 {
     const i64 mm = (i64)m * m;
     const int g = (int)((mm + kT - 1) / kT);
-    osbw_shift_kernel<<<g, kT, 0, s>>>(m, c->osbw_hw, shift, c->osbw_inv);
-    SC_CHECK_LAUNCH();
     cusolverDnHandle_t sol = (cusolverDnHandle_t)c->cusolver;
     if (cusolverDnSetStream(sol, s) != CUSOLVER_STATUS_SUCCESS) { set_error("cusolverDnSetStream failed"); return SCALIT_ECUDA; }
-    int lw1 = 0, lw2 = 0;
-    int *ipiv = nullptr, *info = nullptr;
-    double *work = nullptr;
-    SC_CUDA(cudaMallocAsync(&ipiv, sizeof(int) * (size_t)m, s));
-    SC_CUDA(cudaMallocAsync(&info, sizeof(int) * 2, s));
+    double *Q = nullptr, *w = nullptr, *work = nullptr;
+    int *info = nullptr;
+    auto release = [&]() {
+        if (Q) cudaFreeAsync(Q, s);
+        if (w) cudaFreeAsync(w, s);
+        if (work) cudaFreeAsync(work, s);
+        if (info) cudaFreeAsync(info, s);
+    };
+    if (cudaMallocAsync(&Q, sizeof(double) * (size_t)mm, s) != cudaSuccess ||
+        cudaMallocAsync(&w, sizeof(double) * (size_t)m, s) != cudaSuccess ||
+        cudaMallocAsync(&info, sizeof(int), s) != cudaSuccess) {
+        cudaGetLastError();
+        release();
+        set_error("OSBW: factor workspace does not fit");
+        return SCALIT_ENOMEM;
+    }
+    osbw_shift_kernel<<<g, kT, 0, s>>>(m, c->osbw_hw, shift, Q);
     int rc = 0;
-    if (cusolverDnDsytrf_bufferSize(sol, m, c->osbw_inv, m, &lw1) != CUSOLVER_STATUS_SUCCESS ||
-        cusolverDnDsytri_bufferSize(sol, CUBLAS_FILL_MODE_UPPER, m, c->osbw_inv, m, ipiv, &lw2) !=
-            CUSOLVER_STATUS_SUCCESS) {
-        set_error("cuSOLVER sytrf/sytri buffer size failed");
+    if (cudaGetLastError() != cudaSuccess) { set_error("OSBW shift launch failed"); rc = SCALIT_ECUDA; }
+    int lw = 0;
+    if (!rc && cusolverDnDsyevd_bufferSize(sol, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_UPPER, m, Q, m, w, &lw) !=
+                   CUSOLVER_STATUS_SUCCESS) {
+        set_error("cusolverDnDsyevd_bufferSize failed");
         rc = SCALIT_ECUDA;
     }
-    const int lw = std::max(std::max(lw1, lw2), 1);
-    if (!rc && cudaMallocAsync(&work, sizeof(double) * (size_t)lw, s) != cudaSuccess) {
+    if (!rc && cudaMallocAsync(&work, sizeof(double) * (size_t)std::max(lw, 1), s) != cudaSuccess) {
         cudaGetLastError();
-        set_error("OSBW: factor workspace does not fit");
+        set_error("OSBW: eigensolver workspace does not fit");
         rc = SCALIT_ENOMEM;
     }
-    int hinfo[2] = {0, 0};
-    if (!rc && cusolverDnDsytrf(sol, CUBLAS_FILL_MODE_UPPER, m, c->osbw_inv, m, ipiv, work, lw, info) !=
-                   CUSOLVER_STATUS_SUCCESS) {
-        set_error("cusolverDnDsytrf failed");
+    if (!rc && cudaMemsetAsync(info, 0, sizeof(int), s) != cudaSuccess) { set_error("memset failed"); rc = SCALIT_ECUDA; }
+    if (!rc && cusolverDnDsyevd(sol, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_UPPER, m, Q, m, w, work, std::max(lw, 1),
+                                info) != CUSOLVER_STATUS_SUCCESS) {
+        set_error("cusolverDnDsyevd failed");
         rc = SCALIT_ECUDA;
     }
-    if (!rc && (cudaMemcpyAsync(hinfo, info, sizeof(int), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+    int hinfo = 0;
+    std::vector<double> hw((size_t)m);
+    if (!rc && (cudaMemcpyAsync(&hinfo, info, sizeof(int), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+                cudaMemcpyAsync(hw.data(), w, sizeof(double) * (size_t)m, cudaMemcpyDeviceToHost, s) != cudaSuccess ||
                 cudaStreamSynchronize(s) != cudaSuccess)) {
-        set_error("OSBW factor read-back failed");
+        set_error("OSBW eigenvalue read-back failed");
         rc = SCALIT_ECUDA;
     }
-    if (!rc && hinfo[0] != 0) {
-        set_error("OSBW window matrix HW - E0 is singular or invalid (DSYTRF info=%d)", hinfo[0]);
+    if (!rc && hinfo != 0) {
+        set_error("OSBW window matrix eigen-decomposition failed (syevd info=%d)", hinfo);
         rc = SCALIT_EINVAL;
     }
-    if (!rc && cusolverDnDsytri(sol, CUBLAS_FILL_MODE_UPPER, m, c->osbw_inv, m, ipiv, work, lw, info + 1) !=
-                   CUSOLVER_STATUS_SUCCESS) {
-        set_error("cusolverDnDsytri failed");
-        rc = SCALIT_ECUDA;
+    if (!rc) {
+        for (int k = 0; k < m; ++k) {
+            if (hw[(size_t)k] == 0.0 || !std::isfinite(hw[(size_t)k])) {
+                set_error("OSBW window matrix HW - E0 is singular (eigenvalue %d is %g)", k + 1, hw[(size_t)k]);
+                rc = SCALIT_EINVAL;
+                break;
+            }
+        }
     }
-    if (!rc && (cudaMemcpyAsync(hinfo + 1, info + 1, sizeof(int), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
-                cudaStreamSynchronize(s) != cudaSuccess)) {
-        set_error("OSBW inverse read-back failed");
-        rc = SCALIT_ECUDA;
+    if (!rc) {
+        for (int k = 0; k < m; ++k) hw[(size_t)k] = 1.0 / hw[(size_t)k];
+        if (cudaMemcpyAsync(w, hw.data(), sizeof(double) * (size_t)m, cudaMemcpyHostToDevice, s) != cudaSuccess ||
+            cudaStreamSynchronize(s) != cudaSuccess) {
+            set_error("OSBW reciprocal upload failed");
+            rc = SCALIT_ECUDA;
+        }
     }
-    if (!rc && hinfo[1] != 0) {
-        set_error("OSBW window matrix inverse failed (DSYTRI info=%d)", hinfo[1]);
-        rc = SCALIT_EINVAL;
+    if (!rc) {
+        osbw_inverse_kernel<<<g, kT, 0, s>>>(m, Q, w, c->osbw_inv);
+        if (cudaGetLastError() != cudaSuccess) { set_error("OSBW inverse launch failed"); rc = SCALIT_ECUDA; }
     }
-    if (work) cudaFreeAsync(work, s);
-    cudaFreeAsync(ipiv, s);
-    cudaFreeAsync(info, s);
+    release();
     if (rc) return rc;
-    osbw_mirror_kernel<<<g, kT, 0, s>>>(m, c->osbw_inv);
-    SC_CHECK_LAUNCH();
     return to_f32(c->osbw_inv, c->osbw_invf, mm, s);
 }
 

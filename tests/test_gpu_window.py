@@ -6,8 +6,8 @@ The context takes the oracle's VOSB / EIG0 (set_osb), so both sides select
 the window from identical EIG0.  Tolerances: the window width and points are
 the same host arithmetic (bit-exact); HW's off-diagonal entries are FP64
 sums in another order (1e-12 of max |HW|) and its diagonal is EIG0 (exact);
-P*X applies HWR^-1 where the oracle solves with DSYTRS (1e-9 norm-wise in
-FP64, 1e-4 in FP32).
+P*X applies HWR^-1 (from the eigen-decomposition of HWR) where the oracle
+solves with DSYTRF/DSYTRS (1e-9 norm-wise in FP64, 1e-4 in FP32).
 """
 import numpy as np
 import pytest
@@ -115,7 +115,7 @@ def test_set_osbw_from_saved_hw(lib, case):
     assert de2 == de
     np.testing.assert_array_equal(ind2, ind)
     np.testing.assert_array_equal(HW2, HW)
-    np.testing.assert_array_equal(z2, z)
+    assert rel(z2, z) < 1e-12           # the same HW factored again
 
 
 def test_pist_with_window_preconditioner(lib, orc):
@@ -193,7 +193,7 @@ def test_module_seam_osbw(lib):
         m, de_c = ctx.build_osbw(e0, 50, 1e-4)
         z = ctx.px(b)
     assert m == 50 and de.value == de_c
-    assert rel(y, z) < 1e-14
+    assert rel(y, z) < 1e-12
 
 
 def test_driver_flow_with_window(lib, tmp_path):
@@ -224,5 +224,5 @@ def test_driver_flow_with_window(lib, tmp_path):
     o2 = osb.OSB(inp2)
     o2.load_init_data()
     o2.prog_diag(log=None)
-    np.testing.assert_array_equal(o2.ctx.px(x), z)
+    assert rel(o2.ctx.px(x), z) < 1e-12
     o2.close()
