@@ -569,3 +569,162 @@ def osbw_qmr(op, win, B, qmrmax, qmrtol, ntype=-1, mpi_codes=True):
     rc = lib().orc_qmr(int(ntype), int(qmrmax), float(qmrtol), N, _p(B), fh, None, fp, None, _p(X),
                        C.byref(res), int(bool(mpi_codes)), C.byref(it))
     return rc, X, res.value, it.value
+
+
+# ----------------------------------------------------------------------------------
+# Complex forms with absorbing potentials (resonances JOB_RES1/2, CRP)
+# ----------------------------------------------------------------------------------
+# nType codes (src/iterate/module/osb.data.h:18-22)
+TA0, TA1, TAAP0, TMAP0 = 0, 1, 2, 3
+TAAP, TAAPP, TAAPR = 100, 101, 102
+TMAP, TMAPP, TMAPR = 200, 201, 202
+
+_CX_DIAG = {TA0: (False, 0, None), TA1: (True, 0, None),
+            TAAP0: (False, 1, "AP"), TMAP0: (False, -1, "AP"),
+            TAAP: (True, 1, "AP"), TAAPP: (True, 1, "APP"), TAAPR: (True, 1, "APR"),
+            TMAP: (True, -1, "AP"), TMAPP: (True, -1, "APP"), TMAPR: (True, -1, "APR")}
+
+
+def cx_terms(ntype):
+    """(E0 used?, sign of i, absorbing array) of the nType: MYHX_DX's diagonal
+    (src/iterate/module/osb.hxdx.h:178-215); unknown codes are (H - E0) X."""
+    return _CX_DIAG.get(int(ntype), (True, 0, None))
+
+
+class CxOperator:
+    """The real operator with absorbing potentials: AP = APP (JOB_RES1/2,
+    APR = 0) or APP + APR (JOB_CRP) (loadInitData, osb.io.h:18-30,92-112)."""
+
+    def __init__(self, op, APP, APR=None):
+        self.op = op
+        self.APP = _f64(APP)
+        self.APR = np.zeros_like(self.APP) if APR is None else _f64(APR)
+        self.AP = self.APP + self.APR if APR is not None else self.APP.copy()
+
+    def _absorb(self, which):
+        return {"AP": self.AP, "APP": self.APP, "APR": self.APR}[which]
+
+    def hx(self, X, ntype):
+        """MYHX_DX (osb.hxdx.h:178-240): Y = (RES - E0 [+-] i A) X + sum_level H_level X
+        with the real level matrices applied to the real and imaginary parts."""
+        use_e0, sign, which = cx_terms(ntype)
+        X = np.asarray(X, dtype=np.complex128)
+        nt = 1 if use_e0 else 0
+        Y = self.op.hx(X.real.copy(), nt) + 1j * self.op.hx(X.imag.copy(), nt)
+        if sign:
+            Y = Y + 1j * sign * self._absorb(which) * X
+        return Y
+
+    def _kernel(self, ntype, E0):
+        use_e0, sign, which = cx_terms(ntype)
+        e0 = E0 if ntype not in (TA0, TAAP0, TMAP0) else 0.0
+        return e0, sign, (self._absorb(which) if sign else None)
+
+    def px(self, X, nosb=1, ntype=TA1, de=0.0, beta=0.0):
+        """MYPX_DX (src/iterate/module/osb.mypxdx.h): V^T of levels sF..1 on the
+        real and imaginary parts, the complex kernel, V of levels 1..sF.
+        TOSB divides by EIG0 - E0 [+-] i A; TOSBD1 clamps |EIG0 - E0| <= DE to
+        +-DE first; TOSBD2 maps it to alpha + beta (EIG0 - E0) on both sides of
+        E0 (the complex form has the same expression in both branches, unlike
+        the real TOSBD2 of osb.px.h:174-189)."""
+        op = self.op
+        sizes = op.sizes
+        vs = vosb_starts(sizes)
+        dims = np.cumprod((1,) + sizes[:-1])
+        nlev = len(sizes)
+
+        def rot(y, transpose):
+            yr, yi = _f64(y.real).copy(), _f64(y.imag).copy()
+            order = range(nlev - 1, -1, -1) if transpose else range(nlev)
+            for l in order:
+                blk = int(np.prod(sizes[l + 1:], dtype=np.int64))
+                f = lib().orc_vtx if transpose else lib().orc_vx
+                f(int(dims[l]), sizes[l], blk, _p(op.VOSB[vs[l]:]), _p(yr))
+                f(int(dims[l]), sizes[l], blk, _p(op.VOSB[vs[l]:]), _p(yi))
+            return yr + 1j * yi
+
+        Y = rot(np.asarray(X, dtype=np.complex128), True)
+        e0, sign, A = self._kernel(ntype, op.E0)
+        ade = op.EIG0 - e0
+        DE = abs(de)
+        if nosb == 2:                                   # TOSBD1
+            inside = np.abs(ade) <= DE
+            ade = np.where(inside, np.where(ade < 0.0, -DE, DE), ade)
+        elif nosb == 3:                                 # TOSBD2
+            b1 = beta + 1.0
+            alpha = -beta * DE
+            inside = np.abs(ade) <= DE
+            ade = np.where(inside, alpha + b1 * ade, ade)
+        elif nosb == TOSBW:
+            raise ValueError("the complex window preconditioner is not restated")
+        den = ade + 1j * sign * A if sign else ade
+        Y = Y / den
+        return rot(Y, False)
+
+
+def qmr_cx(hx, px, B, qmrmax, qmrtol, ntype=0, X0=None):
+    """QMR_CX (src/iterate/libiterate/qmr/qmrcx.f90:4-175): QMR for complex
+    symmetric systems, bilinear products DOT_CX = X^T Y (vector_cx.f90:227-234),
+    norms from the conjugated dot_product.  Returns (code, X, RES)."""
+    B = np.asarray(B, dtype=np.complex128)
+    n = B.size
+    X = np.zeros(n, np.complex128) if (ntype <= 0 or X0 is None) else np.asarray(X0, np.complex128).copy()
+    nrm = lambda v: np.sqrt(abs(np.vdot(v, v)))
+    zvrat = 1.0
+    R = B.copy()
+    V = B.copy()
+    bnrm = nrm(B)
+    vnrm = bnrm
+    Z = px(B)
+    znrm = nrm(Z)
+    gamamo, eta = 1.0, -1.0
+    code, res = 0, 0.0
+    Q = S = UX = UR = None
+    qsdot = 0.0
+    thetamo = 0.0
+    for i in range(1, qmrmax + 1):
+        if vnrm == 0.0 or znrm == 0.0:
+            break
+        zvrat = zvrat * znrm / vnrm
+        V = V / vnrm
+        Z = Z / znrm
+        vzdot = np.sum(V * Z)
+        if abs(vzdot) == 0.0:
+            break
+        Q = Z.copy() if i == 1 else Z - (vnrm * vzdot) / qsdot * Q
+        S = zvrat * hx(Q)
+        qsdot = np.sum(Q * S)
+        beta = qsdot / vzdot
+        if abs(qsdot) == 0.0 or abs(beta) == 0.0:
+            break
+        V = S - beta * V
+        vnrmpo = nrm(V)
+        Z = px(V) / zvrat
+        znrm = nrm(Z)
+        theta = vnrmpo / (gamamo * abs(beta))
+        gama = 1.0 / np.sqrt(1.0 + theta * theta)
+        eta = -eta * vnrm * gama * gama / (beta * gamamo * gamamo)
+        if gama == 0.0:
+            break
+        if i == 1:
+            UX = eta * zvrat * Q
+            UR = eta * S
+        else:
+            UX = (eta * zvrat) * Q + ((thetamo * gama) ** 2) * UX
+            UR = eta * S + ((thetamo * gama) ** 2) * UR
+        X = X + UX
+        R = R - UR
+        if abs(ntype) == 1:
+            HX0 = hx(X)
+            res = nrm(HX0 - B) / nrm(HX0)
+        elif abs(ntype) == 2:
+            res = max(nrm(R) / bnrm, np.sqrt(abs(np.vdot(UX, UX) / np.vdot(X, X))),
+                      np.sqrt(abs(np.vdot(UR, UR) / np.vdot(R, R))))
+        else:
+            res = nrm(R) / bnrm
+        if abs(res) < qmrtol:
+            code = i
+            break
+        code = -i
+        vnrm, gamamo, thetamo = vnrmpo, gama, theta
+    return code, X, res
