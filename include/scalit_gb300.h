@@ -37,6 +37,16 @@ extern "C" {
 /* operator kinds (sHC / sPC; src/iterate/module/osb.data.h TA0, TA1) */
 #define SCALIT_TA0 0 /* H*X (no shift)        */
 #define SCALIT_TA1 1 /* (H - E0)*X            */
+/* nType codes of the complex forms with absorbing potentials
+ * (src/iterate/module/osb.data.h:18-22) */
+#define SCALIT_TAAP0 2   /* (H + i AP) X          */
+#define SCALIT_TMAP0 3   /* (H - i AP) X          */
+#define SCALIT_TAAP 100  /* (H - E0 + i AP) X     */
+#define SCALIT_TAAPP 101 /* (H - E0 + i APP) X    */
+#define SCALIT_TAAPR 102 /* (H - E0 + i APR) X    */
+#define SCALIT_TMAP 200  /* (H - E0 - i AP) X     */
+#define SCALIT_TMAPP 201 /* (H - E0 - i APP) X    */
+#define SCALIT_TMAPR 202 /* (H - E0 - i APR) X    */
 
 /* preconditioner kernels (sOSB; osb.data.h TOSB..TOSBD2) */
 #define SCALIT_TOSB 1   /* 1/(EIG0 - E0)                           */
@@ -210,6 +220,37 @@ int scalit_px_f32_device(scalit_ctx *ctx, int npc, int nvec, const float *dX, fl
  * that overlap on the GPU -- two streams, or two contexts on one device --
  * race on it. */
 int scalit_px_noalloc_device(scalit_ctx *ctx, int npc, const double *dX, double *dY);
+
+/* ------------------------------------------------ complex (absorbing) forms --
+ * The resonance and CRP jobs: complex vectors (the reference's COMPLEX*16,
+ * interleaved real/imaginary, npoints complex values per vector), real H, V
+ * and EIG0, complex diagonal.  scalit_set_absorbing loads APP and APR
+ * (loadInitData, osb.io.h:18-30,92-112): APR may be null (JOB_RES1/2: APR = 0,
+ * AP = APP); otherwise AP = APP + APR (JOB_CRP). */
+int scalit_set_absorbing(scalit_ctx *ctx, const double *APP, const double *APR);
+/* MYHX_DX (src/iterate/module/osb.hxdx.h:178-240):
+ *   Y = (RES - E0 [ntype uses E0] + sign i A) X + sum_level H_level X
+ * with sign and A (AP, APP or APR) from the ntype (SCALIT_TA0 .. SCALIT_TMAPR;
+ * unknown codes act as TA1, as the reference's default does). */
+int scalit_hx_cx(scalit_ctx *ctx, int ntype, int nvec, const double *X, double *Y);
+int scalit_hx_cx_device(scalit_ctx *ctx, int ntype, int nvec, const double *dX, double *dY);
+/* MYPX_DX (src/iterate/module/osb.mypxdx.h): V^T of every level, the kernel
+ * 1/(EIG0 - E0 + sign i A) (E0 = 0 for TA0, TAAP0, TMAP0; TOSBD1 clamps
+ * |EIG0 - E0| <= DE to +-DE; TOSBD2 uses alpha + (1 + beta)(EIG0 - E0) on both
+ * sides of E0, as the complex reference does), V of every level.  The complex
+ * window preconditioner (TOSBW) returns SCALIT_EUNSUP. */
+int scalit_px_cx(scalit_ctx *ctx, int ntype, int nvec, const double *X, double *Y);
+int scalit_px_cx_device(scalit_ctx *ctx, int ntype, int nvec, const double *dX, double *dY);
+/* QMR_CX (src/iterate/libiterate/qmr/qmrcx.f90:4-175): QMR for the complex
+ * symmetric system MYHX_DX(ntype) X = B preconditioned by MYPX_DX(sOSB, ntype),
+ * bilinear products X^T Y.  conv selects the convergence test as QMR's ntype
+ * does (|1|: |HX - B|/|HX|, |2|: the max of three ratios, else |R|/|B|; X is
+ * zeroed when conv <= 0, otherwise X is the start).  *code receives QMR_CX's
+ * result (+iterations converged, -iterations not, 0 or -1 on breakdown before
+ * the first step) and *res (may be null) RES; the function returns 0 or a
+ * library error. */
+int scalit_qmr_cx(scalit_ctx *ctx, int conv, int qmrmax, double qmrtol, int ntype, const double *B,
+                  double *X, int *code, double *res);
 
 /* ------------------------------------------------------------------ QMR ---
  * OSB_QMR -> QMR / QMR_MPI (src/iterate/module/osbw.qmr.h:13-23,

@@ -14,6 +14,8 @@ from . import build as _build
 
 TA0, TA1 = 0, 1
 TOSB, TOSBD1, TOSBD2, TOSBW = 1, 2, 3, 4
+# nType codes of the complex forms (osb.data.h:18-22)
+TAAP0, TMAP0, TAAP, TAAPP, TAAPR, TMAP, TMAPP, TMAPR = 2, 3, 100, 101, 102, 200, 201, 202
 FP32_SIMT, FP32_TENSOR, FP32_TENSOR_PX = 0, 1, 2
 PREC_FP64, PREC_FP32 = 0, 1
 FP64_DFMA, FP64_TENSOR = 0, 1
@@ -50,6 +52,12 @@ SIGNATURES = {
     "scalit_get_osb": (C.c_int, [_vp, _dp, _dp]),
     "scalit_set_osb": (C.c_int, [_vp, _dp, _dp]),
     "scalit_build_osbw": (C.c_int, [_vp, C.c_double, C.c_int, _dp, C.c_int, _ip]),
+    "scalit_set_absorbing": (C.c_int, [_vp, _dp, _dp]),
+    "scalit_hx_cx": (C.c_int, [_vp, C.c_int, C.c_int, _dp, _dp]),
+    "scalit_hx_cx_device": (C.c_int, [_vp, C.c_int, C.c_int, _vp, _vp]),
+    "scalit_px_cx": (C.c_int, [_vp, C.c_int, C.c_int, _dp, _dp]),
+    "scalit_px_cx_device": (C.c_int, [_vp, C.c_int, C.c_int, _vp, _vp]),
+    "scalit_qmr_cx": (C.c_int, [_vp, C.c_int, C.c_int, C.c_double, C.c_int, _dp, _dp, _ip, _dp]),
     "scalit_set_osbw": (C.c_int, [_vp, C.c_double, C.c_int, _dp, C.c_int, _dp]),
     "scalit_get_osbw": (C.c_int, [_vp, _ip, _ip, _dp]),
     "scalit_px": (C.c_int, [_vp, C.c_int, C.c_int, _dp, _dp]),
@@ -305,6 +313,39 @@ class Context:
         hw = np.ascontiguousarray(np.asarray(HW, dtype=np.float64).ravel(order="F"))
         _check(self.lib.scalit_set_osbw(self.h, float(e0), int(count), C.byref(d), int(npc), _p(hw)))
         return d.value
+
+    def set_absorbing(self, APP, APR=None):
+        """The absorbing potentials: AP = APP (APR None) or APP + APR."""
+        self._ap = [_f64(APP), None if APR is None else _f64(APR)]
+        _check(self.lib.scalit_set_absorbing(self.h, _p(self._ap[0]),
+                                             None if self._ap[1] is None else _p(self._ap[1])))
+
+    def _cx_apply(self, fn, X, ntype):
+        Z = np.ascontiguousarray(X, dtype=np.complex128)
+        nvec = Z.size // self.N
+        out = np.empty_like(Z)
+        zf, of = Z.view(np.float64), out.view(np.float64)
+        _check(fn(self.h, int(ntype), nvec, _p(zf), _p(of)))
+        return out
+
+    def hx_cx(self, X, ntype=TAAP):
+        """MYHX_DX on complex vectors (N or nvec x N)."""
+        return self._cx_apply(self.lib.scalit_hx_cx, X, ntype)
+
+    def px_cx(self, X, ntype=TAAP):
+        """MYPX_DX on complex vectors."""
+        return self._cx_apply(self.lib.scalit_px_cx, X, ntype)
+
+    def qmr_cx(self, B, qmrmax, qmrtol, ntype=TAAP, conv=0, X0=None):
+        """QMR_CX: returns (code, X, RES)."""
+        Bc = np.ascontiguousarray(B, dtype=np.complex128)
+        X = np.zeros_like(Bc) if X0 is None else np.ascontiguousarray(X0, dtype=np.complex128).copy()
+        code = C.c_int(0)
+        res = C.c_double(0.0)
+        _check(self.lib.scalit_qmr_cx(self.h, int(conv), int(qmrmax), float(qmrtol), int(ntype),
+                                      _p(Bc.view(np.float64)), _p(X.view(np.float64)), C.byref(code),
+                                      C.byref(res)))
+        return code.value, X, res.value
 
     def get_osbw(self):
         """(ind, HW): the window's grid points (0-based) and its matrix."""

@@ -170,6 +170,8 @@ void scalit_destroy(scalit_ctx *c)
     }
     if (c->tc_err) cudaFree(c->tc_err);
     osbw_free(c);
+    double *aptrs[] = {c->APP, c->APR, c->AP};
+    for (double *p : aptrs) if (p) cudaFree(p);
     for (int i = 0; i < 2; ++i) if (c->qg[i].exec) cudaGraphExecDestroy(c->qg[i].exec);
     if (c->red_counter) cudaFree(c->red_counter);
     if (c->work) cudaFree(c->work);

@@ -1,0 +1,486 @@
+// Complex forms with absorbing potentials (the reference's resonance and CRP
+// jobs): MYHX_DX (src/iterate/module/osb.hxdx.h:178-240), MYPX_DX
+// (src/iterate/module/osb.mypxdx.h) and QMR_CX
+// (src/iterate/libiterate/qmr/qmrcx.f90:4-175).
+//
+// H, V and EIG0 are real; the vectors and the diagonal are complex.  On the
+// device a complex vector is planar (N real parts, then N imaginary parts),
+// so the real level products run on both halves as one batch of two vectors
+// through the FP64 engines of the real path, and the preconditioner's real
+// rotations run on each half.  The C ABI takes and returns the reference's
+// interleaved COMPLEX*16 arrays.
+#include "internal.cuh"
+
+#include <algorithm>
+#include <cmath>
+#include <complex>
+#include <cstring>
+#include <vector>
+
+namespace sc {
+
+static constexpr int kT = 256;
+
+static int cgrid(i64 n)
+{
+    const i64 g = (n + kT - 1) / kT;
+    return (int)std::max<i64>(1, std::min<i64>(g, 152LL * 16));
+}
+
+// nType of the complex forms (osb.data.h:18-22): whether E0 shifts the real
+// diagonal, the sign of i A, and which absorbing potential A is.
+struct CxTerms {
+    bool use_e0;
+    int sign;
+    const double *A;
+};
+
+static int cx_terms(const scalit_ctx *c, int ntype, CxTerms *t)
+{
+    int which = 0;   // 0: none, 1: AP, 2: APP, 3: APR
+    switch (ntype) {
+    case SCALIT_TA0: *t = {false, 0, nullptr}; break;
+    case SCALIT_TA1: *t = {true, 0, nullptr}; break;
+    case SCALIT_TAAP0: *t = {false, 1, nullptr}; which = 1; break;
+    case SCALIT_TMAP0: *t = {false, -1, nullptr}; which = 1; break;
+    case SCALIT_TAAP: *t = {true, 1, nullptr}; which = 1; break;
+    case SCALIT_TAAPP: *t = {true, 1, nullptr}; which = 2; break;
+    case SCALIT_TAAPR: *t = {true, 1, nullptr}; which = 3; break;
+    case SCALIT_TMAP: *t = {true, -1, nullptr}; which = 1; break;
+    case SCALIT_TMAPP: *t = {true, -1, nullptr}; which = 2; break;
+    case SCALIT_TMAPR: *t = {true, -1, nullptr}; which = 3; break;
+    default: *t = {true, 0, nullptr}; break;   // the reference's default: (H - E0) X
+    }
+    if (which) {
+        if (!c->AP) { set_error("nType %d needs the absorbing potentials: call scalit_set_absorbing", ntype); return SCALIT_ESTATE; }
+        t->A = which == 1 ? c->AP : which == 2 ? c->APP : c->APR;
+    }
+    return 0;
+}
+
+// E0 of the preconditioner's kernel (MYPX_DX: 0 for TA0, TAAP0, TMAP0)
+static double cx_kernel_e0(const scalit_ctx *c, int ntype)
+{
+    return (ntype == SCALIT_TA0 || ntype == SCALIT_TAAP0 || ntype == SCALIT_TMAP0) ? 0.0 : c->E0;
+}
+
+// --------------------------------------------------------------- kernels --
+__global__ void cx_split_kernel(i64 n, const double *__restrict__ z, double *__restrict__ re, double *__restrict__ im)
+{
+    for (i64 p = blockIdx.x * (i64)blockDim.x + threadIdx.x; p < n; p += (i64)gridDim.x * blockDim.x) {
+        const double2 v = reinterpret_cast<const double2 *>(z)[p];
+        re[p] = v.x;
+        im[p] = v.y;
+    }
+}
+
+__global__ void cx_join_kernel(i64 n, const double *__restrict__ re, const double *__restrict__ im, double *__restrict__ z)
+{
+    for (i64 p = blockIdx.x * (i64)blockDim.x + threadIdx.x; p < n; p += (i64)gridDim.x * blockDim.x)
+        reinterpret_cast<double2 *>(z)[p] = make_double2(re[p], im[p]);
+}
+
+// Y += i sign A X on planar vectors (the imaginary part of MYHX_DX's diagonal).
+__global__ void cx_absorb_kernel(i64 n, const double *__restrict__ X, double *__restrict__ Y, const double *__restrict__ A,
+                                 double sign)
+{
+    for (i64 p = blockIdx.x * (i64)blockDim.x + threadIdx.x; p < n; p += (i64)gridDim.x * blockDim.x) {
+        const double a = sign * A[p];
+        const double xr = X[p], xi = X[n + p];
+        Y[p] = Y[p] - a * xi;
+        Y[n + p] = Y[n + p] + a * xr;
+    }
+}
+
+// MYPX_DX's kernel on planar Z in place: Z / (ade + i sign A), ade = EIG0 - e0,
+// clamped to +-DE inside the window for TOSBD1, alpha + (1 + beta) ade there
+// for TOSBD2 (the complex form uses that expression on both sides of E0).
+__global__ void cx_kernel_step(i64 n, double *__restrict__ Z, const double *__restrict__ EIG,
+                               const double *__restrict__ A, double e0, double sign, int nosb, double de, double beta)
+{
+    for (i64 p = blockIdx.x * (i64)blockDim.x + threadIdx.x; p < n; p += (i64)gridDim.x * blockDim.x) {
+        double ade = EIG[p] - e0;
+        if (nosb == SCALIT_TOSBD1 && fabs(ade) <= de) ade = (ade < 0.0) ? -de : de;
+        else if (nosb == SCALIT_TOSBD2 && fabs(ade) <= de) ade = -beta * de + (beta + 1.0) * ade;
+        const double zr = Z[p], zi = Z[n + p];
+        if (A) {
+            const double ai = sign * A[p];
+            const double d = ade * ade + ai * ai;
+            Z[p] = (zr * ade + zi * ai) / d;
+            Z[n + p] = (zi * ade - zr * ai) / d;
+        } else {
+            Z[p] = zr / ade;
+            Z[n + p] = zi / ade;
+        }
+    }
+}
+
+// y = a x + b y (complex a, b) on planar vectors; overwrite: y = a x.
+__global__ void cx_axpby_kernel(i64 n, double ar, double ai, const double *__restrict__ x, double br, double bi,
+                                double *__restrict__ y, int overwrite)
+{
+    for (i64 p = blockIdx.x * (i64)blockDim.x + threadIdx.x; p < n; p += (i64)gridDim.x * blockDim.x) {
+        const double xr = x[p], xi = x[n + p];
+        double yr = ar * xr - ai * xi, yi = ar * xi + ai * xr;
+        if (!overwrite) {
+            const double vr = y[p], vi = y[n + p];
+            yr += br * vr - bi * vi;
+            yi += br * vi + bi * vr;
+        }
+        y[p] = yr;
+        y[n + p] = yi;
+    }
+}
+
+__global__ void real_div_kernel(i64 n, double *__restrict__ x, double d)
+{
+    for (i64 p = blockIdx.x * (i64)blockDim.x + threadIdx.x; p < n; p += (i64)gridDim.x * blockDim.x) x[p] = x[p] / d;
+}
+
+__global__ void real_mul_kernel(i64 n, double *__restrict__ x, double a)
+{
+    for (i64 p = blockIdx.x * (i64)blockDim.x + threadIdx.x; p < n; p += (i64)gridDim.x * blockDim.x) x[p] = a * x[p];
+}
+
+// -------------------------------------------------------- planar operators --
+// MYHX_DX on a planar complex vector.
+static int hx_cx_planar(const scalit_ctx *c, int ntype, const double *X, double *Y, cudaStream_t s)
+{
+    CxTerms t;
+    int rc = cx_terms(c, ntype, &t);
+    if (rc) return rc;
+    rc = hx_batch<double>(c, X, Y, 2, t.use_e0 ? c->E0 : 0.0, 1.0, nullptr, s);
+    if (rc) return rc;
+    if (t.sign) {
+        cx_absorb_kernel<<<cgrid(c->L.N), kT, 0, s>>>(c->L.N, X, Y, t.A, (double)t.sign);
+        SC_CHECK_LAUNCH();
+    }
+    return 0;
+}
+
+// MYPX_DX on a planar complex vector: V^T of levels sF..1 on each half, the
+// complex kernel, V of levels 1..sF (tmp: 2N).  The stages alternate between
+// Y and tmp so that the last one writes Y.
+static int px_cx_planar(const scalit_ctx *c, int ntype, const double *X, double *Y, double *tmp, cudaStream_t s)
+{
+    const Layout &L = c->L;
+    const i64 N = L.N;
+    if (!c->osb_built) { set_error("P*X before the preconditioner was built or loaded"); return SCALIT_ESTATE; }
+    if (c->osb_kind == SCALIT_TOSBW) {
+        set_error("the complex window preconditioner (ZHETRF/ZGETRF of createWH_DXCX) is not supported");
+        return SCALIT_EUNSUP;
+    }
+    CxTerms t;
+    int rc = cx_terms(c, ntype, &t);
+    if (rc) return rc;
+    const int S = 2 * L.nlev;
+    for (int q = 0; q < 2; ++q) {
+        double *buf[2] = {Y + q * N, tmp + q * N};
+        const double *in = X + q * N;
+        int stage = 0;
+        for (int l = L.nlev - 1; l >= 0; --l) {
+            ++stage;
+            double *out = buf[(S - stage) % 2];
+            rc = px_rotate(c, l, 1, in, out, nullptr, s);
+            if (rc) return rc;
+            in = out;
+        }
+    }
+    double *Z = (L.nlev % 2 == 0) ? Y : tmp;   // where both halves' V^T stages ended
+    cx_kernel_step<<<cgrid(N), kT, 0, s>>>(N, Z, c->EIG0, t.sign ? t.A : nullptr, cx_kernel_e0(c, ntype),
+                                           (double)t.sign, c->osb_kind, c->osb_de, c->osb_beta);
+    SC_CHECK_LAUNCH();
+    for (int q = 0; q < 2; ++q) {
+        double *buf[2] = {Y + q * N, tmp + q * N};
+        const double *in = Z + q * N;
+        int stage = L.nlev;
+        for (int l = 0; l < L.nlev; ++l) {
+            ++stage;
+            double *out = buf[(S - stage) % 2];
+            rc = px_rotate(c, l, 0, in, out, nullptr, s);
+            if (rc) return rc;
+            in = out;
+        }
+    }
+    return 0;
+}
+
+// ------------------------------------------------------------------ QMR_CX --
+// QMR for the complex symmetric system (H - E0 [+-] i A) X = B with the
+// complex OSB preconditioner, in the reference's order (qmrcx.f90:4-175).
+// Bilinear products X^T Y (DOT_CX, vector_cx.f90:227-234) and the norms of
+// the conjugated dot_product are deterministic FP64 device reductions read
+// back per use; the scalar recurrence runs on the host as in the reference.
+static int qmr_cx_run(scalit_ctx *c, int conv, int qmrmax, double tol, int ntype, const double *B, double *X,
+                      int *code_out, double *res_out)
+{
+    typedef std::complex<double> cplx;
+    const i64 N = c->L.N, N2 = 2 * N;
+    cudaStream_t s = c->stream;
+    double *w = nullptr, *dd = nullptr;
+    const bool full_res = std::abs(conv) == 1;
+    if (cudaMallocAsync(&w, sizeof(double) * (size_t)N2 * 10, s) != cudaSuccess) {
+        cudaGetLastError();
+        set_error("QMR_CX workspace (%lld complex points x 10) does not fit", N);
+        return SCALIT_ENOMEM;
+    }
+    if (cudaMallocAsync(&dd, sizeof(double) * 16, s) != cudaSuccess) {
+        cudaGetLastError();
+        cudaFreeAsync(w, s);
+        set_error("QMR_CX scalars do not fit");
+        return SCALIT_ENOMEM;
+    }
+    double *R = w, *UX = w + N2, *UR = w + 2 * N2, *Q = w + 3 * N2, *Sv = w + 4 * N2, *V = w + 5 * N2;
+    double *Z = w + 6 * N2, *HX0 = w + 7 * N2, *T = w + 8 * N2;   // T: the preconditioner's scratch (2N)
+    const int g = cgrid(N), g2 = cgrid(N2);
+    int rc = 0;
+    auto nrm = [&](const double *x, double *out) -> int {
+        int r = dot_dev<double>(c, N2, x, x, dd, s);
+        if (r) return r;
+        double h;
+        r = sync_read_doubles(c, dd, &h, 1);
+        if (r) return r;
+        *out = std::sqrt(std::fabs(h));
+        return 0;
+    };
+    auto bil = [&](const double *x, const double *y, cplx *out) -> int {
+        int r = dot_dev<double>(c, N, x, y, dd, s);
+        if (!r) r = dot_dev<double>(c, N, x + N, y + N, dd + 1, s);
+        if (!r) r = dot_dev<double>(c, N, x, y + N, dd + 2, s);
+        if (!r) r = dot_dev<double>(c, N, x + N, y, dd + 3, s);
+        if (r) return r;
+        double h[4];
+        r = sync_read_doubles(c, dd, h, 4);
+        if (r) return r;
+        *out = cplx(h[0] - h[1], h[2] + h[3]);
+        return 0;
+    };
+    auto axpby = [&](cplx a, const double *x, cplx b, double *y, int overwrite) -> int {
+        cx_axpby_kernel<<<g, kT, 0, s>>>(N, a.real(), a.imag(), x, b.real(), b.imag(), y, overwrite);
+        SC_CHECK_LAUNCH();
+        return 0;
+    };
+    auto rdiv = [&](double *x, double d) -> int {
+        real_div_kernel<<<g2, kT, 0, s>>>(N2, x, d);
+        SC_CHECK_LAUNCH();
+        return 0;
+    };
+    int code = -1;
+    double res = 0.0;
+    do {
+        double zvrat = 1.0, bnrm = 0.0, vnrm = 0.0, znrm = 0.0, gamamo = 1.0, thetamo = 0.0;
+        cplx eta(-1.0, 0.0), qsdot(0.0, 0.0);
+        if (conv <= 0 && cudaMemsetAsync(X, 0, sizeof(double) * (size_t)N2, s) != cudaSuccess) { set_error("memset failed"); rc = SCALIT_ECUDA; break; }
+        if (cudaMemcpyAsync(R, B, sizeof(double) * (size_t)N2, cudaMemcpyDeviceToDevice, s) != cudaSuccess ||
+            cudaMemcpyAsync(V, B, sizeof(double) * (size_t)N2, cudaMemcpyDeviceToDevice, s) != cudaSuccess) {
+            set_error("QMR_CX copy failed");
+            rc = SCALIT_ECUDA;
+            break;
+        }
+        if ((rc = nrm(B, &bnrm))) break;
+        vnrm = bnrm;
+        if ((rc = px_cx_planar(c, ntype, B, Z, T, s))) break;
+        if ((rc = nrm(Z, &znrm))) break;
+        code = 0;
+        for (int i = 1; i <= qmrmax; ++i) {
+            if (vnrm == 0.0 || znrm == 0.0) break;
+            zvrat = zvrat * znrm / vnrm;
+            if ((rc = rdiv(V, vnrm)) || (rc = rdiv(Z, znrm))) break;
+            cplx vzdot;
+            if ((rc = bil(V, Z, &vzdot))) break;
+            if (std::abs(vzdot) == 0.0) break;
+            if (i == 1) rc = axpby(cplx(1.0, 0.0), Z, cplx(0.0, 0.0), Q, 1);
+            else rc = axpby(cplx(1.0, 0.0), Z, -(vnrm * vzdot) / qsdot, Q, 0);
+            if (rc) break;
+            if ((rc = hx_cx_planar(c, ntype, Q, Sv, s))) break;
+            real_mul_kernel<<<g2, kT, 0, s>>>(N2, Sv, zvrat);
+            if (cudaGetLastError() != cudaSuccess) { set_error("QMR_CX scale launch failed"); rc = SCALIT_ECUDA; break; }
+            if ((rc = bil(Q, Sv, &qsdot))) break;
+            const cplx beta = qsdot / vzdot;
+            if (std::abs(qsdot) == 0.0 || std::abs(beta) == 0.0) break;
+            if ((rc = axpby(cplx(1.0, 0.0), Sv, -beta, V, 0))) break;
+            double vnrmpo;
+            if ((rc = nrm(V, &vnrmpo))) break;
+            if ((rc = px_cx_planar(c, ntype, V, Z, T, s))) break;
+            if ((rc = rdiv(Z, zvrat))) break;
+            if ((rc = nrm(Z, &znrm))) break;
+            const double theta = vnrmpo / (gamamo * std::abs(beta));
+            const double gama = 1.0 / std::sqrt(1.0 + theta * theta);
+            eta = -eta * vnrm * gama * gama / (beta * gamamo * gamamo);
+            if (gama == 0.0) break;
+            if (i == 1) {
+                if ((rc = axpby(eta * zvrat, Q, cplx(0.0, 0.0), UX, 1))) break;
+                if ((rc = axpby(eta, Sv, cplx(0.0, 0.0), UR, 1))) break;
+            } else {
+                const double tg = (thetamo * gama) * (thetamo * gama);
+                if ((rc = axpby(eta * zvrat, Q, cplx(tg, 0.0), UX, 0))) break;
+                if ((rc = axpby(eta, Sv, cplx(tg, 0.0), UR, 0))) break;
+            }
+            if ((rc = axpby(cplx(1.0, 0.0), UX, cplx(1.0, 0.0), X, 0))) break;
+            if ((rc = axpby(cplx(-1.0, 0.0), UR, cplx(1.0, 0.0), R, 0))) break;
+            if (full_res) {
+                double xnrm, r1;
+                if ((rc = hx_cx_planar(c, ntype, X, HX0, s))) break;
+                if ((rc = nrm(HX0, &xnrm))) break;
+                if ((rc = axpby(cplx(-1.0, 0.0), B, cplx(1.0, 0.0), HX0, 0))) break;
+                if ((rc = nrm(HX0, &r1))) break;
+                res = r1 / xnrm;
+            } else if (std::abs(conv) == 2) {
+                double rn, uxn, xn, urn;
+                if ((rc = nrm(R, &rn)) || (rc = nrm(UX, &uxn)) || (rc = nrm(X, &xn)) || (rc = nrm(UR, &urn))) break;
+                res = std::max(rn / bnrm, std::max(uxn / xn, urn / rn));
+            } else {
+                double rn;
+                if ((rc = nrm(R, &rn))) break;
+                res = rn / bnrm;
+            }
+            if (std::fabs(res) < tol) { code = i; break; }
+            code = -i;
+            vnrm = vnrmpo;
+            gamamo = gama;
+            thetamo = theta;
+        }
+    } while (0);
+    (void)HX0;
+    cudaFreeAsync(w, s);
+    cudaFreeAsync(dd, s);
+    cudaStreamSynchronize(s);
+    if (rc) return rc;
+    *code_out = code;
+    if (res_out) *res_out = res;
+    return 0;
+}
+
+// ------------------------------------------------------------------- C ABI --
+// Interleaved COMPLEX*16 in (host or device) -> planar device P (2N).
+static int to_planar(scalit_ctx *c, const double *Z, bool host, double *stage, double *P)
+{
+    const i64 N = c->L.N;
+    const double *src = Z;
+    if (host) {
+        SC_CUDA(cudaMemcpyAsync(stage, Z, sizeof(double) * 2 * (size_t)N, cudaMemcpyHostToDevice, c->stream));
+        src = stage;
+    }
+    cx_split_kernel<<<cgrid(N), kT, 0, c->stream>>>(N, src, P, P + N);
+    SC_CHECK_LAUNCH();
+    return 0;
+}
+
+static int from_planar(scalit_ctx *c, const double *P, bool host, double *stage, double *Z)
+{
+    const i64 N = c->L.N;
+    double *dst = host ? stage : Z;
+    cx_join_kernel<<<cgrid(N), kT, 0, c->stream>>>(N, P, P + N, dst);
+    SC_CHECK_LAUNCH();
+    if (host) SC_CUDA(cudaMemcpyAsync(Z, stage, sizeof(double) * 2 * (size_t)N, cudaMemcpyDeviceToHost, c->stream));
+    return 0;
+}
+
+static int cx_apply(scalit_ctx *c, int which, int ntype, int nvec, const double *X, double *Y, bool host)
+{
+    const Layout &L = c->L;
+    const i64 N = L.N;
+    if (!c->loaded) { set_error("complex H*X / P*X before scalit_load"); return SCALIT_ESTATE; }
+    if (nvec < 0) { set_error("nvec < 0"); return SCALIT_EINVAL; }
+    if (nvec == 0) return 0;
+    if (!X || !Y) { set_error("null vector"); return SCALIT_EINVAL; }
+    double *w = nullptr;
+    if (cudaMallocAsync(&w, sizeof(double) * 2 * (size_t)N * 4, c->stream) != cudaSuccess) {
+        cudaGetLastError();
+        set_error("complex workspace does not fit");
+        return SCALIT_ENOMEM;
+    }
+    double *stage = w, *P = w + 2 * N, *Qv = w + 4 * N, *T = w + 6 * N;
+    int rc = 0;
+    for (int v = 0; v < nvec && !rc; ++v) {
+        rc = to_planar(c, X + (i64)v * 2 * N, host, stage, P);
+        if (!rc) rc = which == 0 ? hx_cx_planar(c, ntype, P, Qv, c->stream) : px_cx_planar(c, ntype, P, Qv, T, c->stream);
+        if (!rc) rc = from_planar(c, Qv, host, stage, Y + (i64)v * 2 * N);
+    }
+    cudaFreeAsync(w, c->stream);
+    if (cudaStreamSynchronize(c->stream) != cudaSuccess && !rc) { set_error("complex apply failed"); rc = SCALIT_ECUDA; }
+    return rc;
+}
+
+}  // namespace sc
+
+using namespace sc;
+
+#define CX_CTX_CHECK(c)                                                           \
+    do {                                                                          \
+        if (!(c)) { set_error("null context"); return SCALIT_EINVAL; }            \
+        if (cudaSetDevice((c)->device) != cudaSuccess) { set_error("cudaSetDevice failed"); return SCALIT_ECUDA; } \
+    } while (0)
+
+extern "C" {
+
+int scalit_set_absorbing(scalit_ctx *c, const double *APP, const double *APR)
+{
+    CX_CTX_CHECK(c);
+    if (!c->loaded) { set_error("scalit_set_absorbing before scalit_load"); return SCALIT_ESTATE; }
+    if (!APP) { set_error("APP is required"); return SCALIT_EINVAL; }
+    const i64 N = c->L.N;
+    for (i64 p = 0; p < N; ++p) {
+        if (!std::isfinite(APP[p]) || (APR && !std::isfinite(APR[p]))) { set_error("non-finite absorbing potential"); return SCALIT_ENONFINITE; }
+    }
+    if (!c->AP) {
+        SC_CUDA(cudaMalloc(&c->APP, sizeof(double) * (size_t)N));
+        SC_CUDA(cudaMalloc(&c->APR, sizeof(double) * (size_t)N));
+        SC_CUDA(cudaMalloc(&c->AP, sizeof(double) * (size_t)N));
+    }
+    // loadInitData (osb.io.h:18-30): JOB_RES1/2 read APP with APR = 0 and
+    // AP = APP; JOB_CRP reads both and AP = APP + APR.
+    std::vector<double> ap(APP, APP + N);
+    if (APR) for (i64 p = 0; p < N; ++p) ap[(size_t)p] = APP[p] + APR[p];
+    SC_CUDA(cudaMemcpyAsync(c->APP, APP, sizeof(double) * (size_t)N, cudaMemcpyHostToDevice, c->stream));
+    if (APR) SC_CUDA(cudaMemcpyAsync(c->APR, APR, sizeof(double) * (size_t)N, cudaMemcpyHostToDevice, c->stream));
+    else SC_CUDA(cudaMemsetAsync(c->APR, 0, sizeof(double) * (size_t)N, c->stream));
+    SC_CUDA(cudaMemcpyAsync(c->AP, ap.data(), sizeof(double) * (size_t)N, cudaMemcpyHostToDevice, c->stream));
+    SC_CUDA(cudaStreamSynchronize(c->stream));
+    return 0;
+}
+
+int scalit_hx_cx(scalit_ctx *c, int ntype, int nvec, const double *X, double *Y)
+{
+    CX_CTX_CHECK(c);
+    return cx_apply(c, 0, ntype, nvec, X, Y, true);
+}
+
+int scalit_hx_cx_device(scalit_ctx *c, int ntype, int nvec, const double *dX, double *dY)
+{
+    CX_CTX_CHECK(c);
+    return cx_apply(c, 0, ntype, nvec, dX, dY, false);
+}
+
+int scalit_px_cx(scalit_ctx *c, int ntype, int nvec, const double *X, double *Y)
+{
+    CX_CTX_CHECK(c);
+    return cx_apply(c, 1, ntype, nvec, X, Y, true);
+}
+
+int scalit_px_cx_device(scalit_ctx *c, int ntype, int nvec, const double *dX, double *dY)
+{
+    CX_CTX_CHECK(c);
+    return cx_apply(c, 1, ntype, nvec, dX, dY, false);
+}
+
+int scalit_qmr_cx(scalit_ctx *c, int conv, int qmrmax, double qmrtol, int ntype, const double *B, double *X,
+                  int *code, double *res)
+{
+    CX_CTX_CHECK(c);
+    if (!c->osb_built) { set_error("QMR_CX needs the preconditioner: build or load it first"); return SCALIT_ESTATE; }
+    if (!B || !X || !code) { set_error("B, X and code are required"); return SCALIT_EINVAL; }
+    const i64 N = c->L.N;
+    double *w = nullptr;
+    SC_CUDA(cudaMallocAsync(&w, sizeof(double) * 2 * (size_t)N * 3, c->stream));
+    double *stage = w, *Bp = w + 2 * N, *Xp = w + 4 * N;
+    int rc = to_planar(c, B, true, stage, Bp);
+    if (!rc && conv > 0) rc = to_planar(c, X, true, stage, Xp);
+    if (!rc) rc = qmr_cx_run(c, conv, qmrmax, qmrtol, ntype, Bp, Xp, code, res);
+    if (!rc) rc = from_planar(c, Xp, true, stage, X);
+    cudaFreeAsync(w, c->stream);
+    if (cudaStreamSynchronize(c->stream) != cudaSuccess && !rc) { set_error("QMR_CX failed"); rc = SCALIT_ECUDA; }
+    return rc;
+}
+
+}  // extern "C"

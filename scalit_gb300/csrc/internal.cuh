@@ -85,6 +85,8 @@ struct scalit_ctx {
     float *osbw_invf = nullptr;
     void *osbw_wy = nullptr;
     double osbw_e0 = 0.0, osbw_de = 0.0;
+    // absorbing potentials of the complex forms: APP, APR and AP = APP + APR
+    double *APP = nullptr, *APR = nullptr, *AP = nullptr;
     // workspace (grown on demand)
     void *work = nullptr;
     size_t work_bytes = 0;
@@ -214,6 +216,10 @@ int tc_check_error(scalit_ctx *c);
 int wait_selftest(scalit_ctx *c, double seconds);
 int tc_gemm_f64(const scalit_ctx *c, int M, int N, int K, const double *A, i64 lda, const double *B, i64 ldb,
                 double *C, i64 ldc, cudaStream_t s);
+
+// VX / VTX of level l (0-based) in FP64, out of place (the real P*X engines).
+int px_rotate(const scalit_ctx *c, int l, int transpose, const double *in, double *out, const int *gate,
+              cudaStream_t s);
 
 // ---------------------------------------------------------- OSBW window --
 // initOSBW for the bound-state job: window width and points, HW (formed, or

@@ -492,6 +492,16 @@ static int rotate(const scalit_ctx *c, int l, int transpose, const T *V, const T
     return level_rotate<T>((int)L.dim[l], L.n[l], (int)L.blk[l], V + L.vs[l], in, out, transpose, gate, s);
 }
 
+// VX (transpose = 0) or VTX (transpose = 1) of one level, FP64, out of place:
+// the engines of the real P*X (level 1 by the batched block GEMV).
+int px_rotate(const scalit_ctx *c, int l, int transpose, const double *in, double *out, const int *gate,
+              cudaStream_t s)
+{
+    const Layout &L = c->L;
+    if (l == 0) return level_rotate<double>(1, L.n[0], (int)L.blk[0], c->VOSB + L.vs[0], in, out, transpose, gate, s);
+    return rotate<double>(c, l, transpose, c->VOSB, in, out, gate, s);
+}
+
 // MYPX with the TOSBW kernel (osb.px.h:191-206): the level-1 rotations are
 // not fused with the kernel step, whose window entries couple blocks.
 // Stages: V^T of levels sF..1, the window step in place, V of levels 1..sF.

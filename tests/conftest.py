@@ -25,3 +25,18 @@ def orc():
     from oracle import oracle
     oracle.lib()
     return oracle
+
+
+# GPU modules whose device path has not yet passed on a GB300 run after the
+# others, so that under -x a failure in one of them does not hide the rest;
+# test_zz_no_alloc.py stays last (its docstring says why).
+_NOT_YET_VALIDATED = ("test_gpu_window.py", "test_gpu_complex.py")
+
+
+def pytest_collection_modifyitems(config, items):
+    def rank(item):
+        name = os.path.basename(str(item.fspath))
+        if name == "test_zz_no_alloc.py":
+            return 2
+        return 1 if name in _NOT_YET_VALIDATED else 0
+    items.sort(key=rank)

@@ -1,0 +1,112 @@
+"""Complex forms with absorbing potentials on the GPU against the oracle
+(MYHX_DX, src/iterate/module/osb.hxdx.h:178-240; MYPX_DX,
+src/iterate/module/osb.mypxdx.h; QMR_CX, src/iterate/libiterate/qmr/qmrcx.f90:4-175).
+
+The context takes the oracle's VOSB / EIG0 (set_osb).  Tolerances: complex
+H*X 1e-12 norm-wise (the real level products of the FP64 engine, 1e-16, on
+both halves); P*X 1e-9 as the real P*X; QMR_CX's solution 1e-7 of the
+oracle's and its residual against the dense operator 1e-8.
+"""
+import numpy as np
+import pytest
+
+from scalit_gb300 import capi, hamiltonian as hm
+
+pytestmark = pytest.mark.gpu
+
+
+def rel(a, b):
+    return float(np.linalg.norm(a - b) / np.linalg.norm(b))
+
+
+@pytest.fixture(scope="module")
+def case(orc):
+    p = hm.build_problem(hm.Grid3(12, 10, 8), hm.PES())
+    ref = orc.Operator.from_problem(p, E0=0.0)
+    ref.build_osb(20, 1e-4)
+    e0 = float(np.sort(ref.EIG0)[15]) + 2e-4
+    ref.set_e0(e0)
+    rng = np.random.default_rng(0)
+    app = rng.uniform(0.0, 2e-3, p.N)
+    apr = rng.uniform(0.0, 1e-3, p.N)
+    return p, ref, e0, app, apr
+
+
+def context(p, ref, e0, app, apr):
+    ctx = capi.Context.from_problem(p, e0=e0)
+    ctx.set_osb(ref.VOSB, ref.EIG0)
+    ctx.set_absorbing(app, apr)
+    return ctx
+
+
+def cvec(rng, shape):
+    return rng.standard_normal(shape) + 1j * rng.standard_normal(shape)
+
+
+@pytest.mark.parametrize("ntype", [0, 1, 2, 3, 100, 101, 102, 200, 201, 202])
+def test_hx_cx_matches_oracle(lib, orc, case, ntype):
+    p, ref, e0, app, apr = case
+    cx = orc.CxOperator(ref, app, apr)
+    X = cvec(np.random.default_rng(1), (2, p.N))
+    with context(p, ref, e0, app, apr) as ctx:
+        Y = ctx.hx_cx(X, ntype)
+    for v in range(2):
+        assert rel(Y[v], cx.hx(X[v], ntype)) < 1e-12
+
+
+@pytest.mark.parametrize("kind,ntype", [(1, 1), (1, 0), (1, 2), (1, 100), (1, 202), (2, 101), (3, 200)])
+def test_px_cx_matches_oracle(lib, orc, case, kind, ntype):
+    p, ref, e0, app, apr = case
+    cx = orc.CxOperator(ref, app, apr)
+    de, beta = 3e-3, 0.5
+    x = cvec(np.random.default_rng(2), p.N)
+    with context(p, ref, e0, app, apr) as ctx:
+        ctx.set_precond(kind, de, beta)
+        z = ctx.px_cx(x, ntype)
+    assert rel(z, cx.px(x, nosb=kind, ntype=ntype, de=de, beta=beta)) < 1e-9
+
+
+def test_resonance_job_uses_app_only(lib, orc, case):
+    """JOB_RES1/2: APR = 0 and AP = APP."""
+    p, ref, e0, app, apr = case
+    cx = orc.CxOperator(ref, app)
+    x = cvec(np.random.default_rng(3), p.N)
+    with capi.Context.from_problem(p, e0=e0) as ctx:
+        ctx.set_osb(ref.VOSB, ref.EIG0)
+        ctx.set_absorbing(app)
+        y = ctx.hx_cx(x, capi.TAAP)
+        y0 = ctx.hx_cx(x, capi.TAAPR)
+    assert rel(y, cx.hx(x, capi.TAAP)) < 1e-12
+    assert rel(y0, cx.hx(x, capi.TA1)) < 1e-12        # APR = 0
+
+
+def test_qmr_cx_matches_oracle(lib, orc, case):
+    p, ref, e0, app, apr = case
+    cx = orc.CxOperator(ref, app, apr)
+    b = cvec(np.random.default_rng(4), p.N)
+    code_r, x_r, res_r = orc.qmr_cx(lambda v: cx.hx(v, orc.TAAP), lambda v: cx.px(v, 1, orc.TAAP), b, 500, 1e-10)
+    with context(p, ref, e0, app, apr) as ctx:
+        ctx.set_fp64_mode(capi.FP64_DFMA)
+        code, x, res = ctx.qmr_cx(b, 500, 1e-10, ntype=capi.TAAP)
+    assert code_r > 0 and code > 0
+    assert abs(code - code_r) <= 1
+    assert rel(x, x_r) < 1e-7
+    assert rel(cx.hx(x, orc.TAAP), b) < 1e-8
+
+
+def test_errors(lib, case):
+    p, ref, e0, app, apr = case
+    x = np.zeros(p.N, dtype=np.complex128)
+    with capi.Context.from_problem(p, e0=e0) as ctx:
+        with pytest.raises(capi.ScalitError) as e:
+            ctx.hx_cx(x, capi.TAAP)                  # no absorbing potential yet
+        assert e.value.code == -104
+        ctx.set_absorbing(app, apr)
+        with pytest.raises(capi.ScalitError) as e:
+            ctx.px_cx(x, capi.TAAP)                  # no preconditioner yet
+        assert e.value.code == -104
+        bad = app.copy()
+        bad[3] = np.inf
+        with pytest.raises(capi.ScalitError) as e:
+            ctx.set_absorbing(bad)
+        assert e.value.code == -106
