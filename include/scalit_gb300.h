@@ -267,6 +267,14 @@ int scalit_qmr(scalit_ctx *ctx, int ntype, int qmrmax, double qmrtol, int precis
                const double *B, double *X, double *res, int *iters);
 int scalit_qmr_device(scalit_ctx *ctx, int ntype, int qmrmax, double qmrtol, int precision,
                       const double *dB, double *dX, double *res, int *iters);
+/* The same two solves with QMR's code in *code and 0 (or a library error) as
+ * the result: a not-converged solve of more than 100 iterations returns
+ * -iterations <= -101 from scalit_qmr, which a caller cannot tell from a
+ * library error; these keep the two apart. */
+int scalit_qmr_ex(scalit_ctx *ctx, int ntype, int qmrmax, double qmrtol, int precision, const double *B,
+                  double *X, int *code, double *res, int *iters);
+int scalit_qmr_device_ex(scalit_ctx *ctx, int ntype, int qmrmax, double qmrtol, int precision,
+                         const double *dB, double *dX, int *code, double *res, int *iters);
 
 /* ----------------------------------------------- shifts and batches -----
  * No reference counterpart: the reference solves one system per QMR call

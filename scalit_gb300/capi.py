@@ -66,6 +66,8 @@ SIGNATURES = {
     "scalit_px_noalloc_device": (C.c_int, [_vp, C.c_int, _vp, _vp]),
     "scalit_qmr": (C.c_int, [_vp, C.c_int, C.c_int, C.c_double, C.c_int, _dp, _dp, _dp, _ip]),
     "scalit_qmr_device": (C.c_int, [_vp, C.c_int, C.c_int, C.c_double, C.c_int, _vp, _vp, _dp, _ip]),
+    "scalit_qmr_ex": (C.c_int, [_vp, C.c_int, C.c_int, C.c_double, C.c_int, _dp, _dp, _ip, _dp, _ip]),
+    "scalit_qmr_device_ex": (C.c_int, [_vp, C.c_int, C.c_int, C.c_double, C.c_int, _vp, _vp, _ip, _dp, _ip]),
     "scalit_pist_default_params": (None, [_vp, C.c_int, C.c_double, C.c_double, C.c_int, C.c_int,
                                           C.c_int, C.c_int, C.c_int, C.c_double]),
     "scalit_pist": (C.c_int, [_vp, _vp, _dp, _dp, _dp, _vp]),
@@ -391,9 +393,10 @@ class Context:
         X = np.zeros_like(B) if X0 is None else _f64(X0).copy()
         res = C.c_double(0.0)
         it = C.c_int(0)
-        code = _check(self.lib.scalit_qmr(self.h, int(ntype), int(qmrmax), float(qmrtol),
-                                          int(precision), _p(B), _p(X), C.byref(res), C.byref(it)))
-        return code, X, res.value, it.value
+        code = C.c_int(0)
+        _check(self.lib.scalit_qmr_ex(self.h, int(ntype), int(qmrmax), float(qmrtol), int(precision),
+                                      _p(B), _p(X), C.byref(code), C.byref(res), C.byref(it)))
+        return code.value, X, res.value, it.value
 
     def hx_adjoint(self, X, Ybar, ntype=TA1, want=("x", "v", "h")):
         """Adjoint of H*X: returns (Xbar, Vbar, H0bar) (None for what is not wanted)."""

@@ -532,27 +532,63 @@ int scalit_qmr_device(scalit_ctx *c, int ntype, int qmrmax, double qmrtol, int p
     return r.code;
 }
 
-int scalit_qmr(scalit_ctx *c, int ntype, int qmrmax, double qmrtol, int precision, const double *B,
-               double *X, double *res, int *iters)
+int scalit_qmr_device_ex(scalit_ctx *c, int ntype, int qmrmax, double qmrtol, int precision,
+                         const double *dB, double *dX, int *code, double *res, int *iters)
 {
     CTX_CHECK(c);
+    if (!code) { set_error("code is required"); return SCALIT_EINVAL; }
+    QmrResult r{};
+    int rc = qmr_run(c, ntype, qmrmax, qmrtol, precision, dB, dX, &r);
+    if (rc) return rc;
+    *code = r.code;
+    if (res) *res = r.res;
+    if (iters) *iters = r.iters;
+    return 0;
+}
+
+// QMR on host vectors: B in, X in (start, ntype > 0) and out.
+static int qmr_host(scalit_ctx *c, int ntype, int qmrmax, double qmrtol, int precision, const double *B,
+                    double *X, QmrResult *r)
+{
     const i64 N = c->L.N;
     double *bx = nullptr;
     SC_CUDA(cudaMallocAsync(&bx, sizeof(double) * 2 * (size_t)N, c->stream));
     SC_CUDA(cudaMemcpyAsync(bx, B, sizeof(double) * N, cudaMemcpyHostToDevice, c->stream));
     if (ntype > 0) SC_CUDA(cudaMemcpyAsync(bx + N, X, sizeof(double) * N, cudaMemcpyHostToDevice, c->stream));
-    QmrResult r{};
-    int rc = qmr_run(c, ntype, qmrmax, qmrtol, precision, bx, bx + N, &r);
+    int rc = qmr_run(c, ntype, qmrmax, qmrtol, precision, bx, bx + N, r);
     if (!rc) {
         SC_CUDA(cudaMemcpyAsync(X, bx + N, sizeof(double) * N, cudaMemcpyDeviceToHost, c->stream));
         SC_CUDA(cudaStreamSynchronize(c->stream));
     }
     cudaFreeAsync(bx, c->stream);
     cudaStreamSynchronize(c->stream);
+    return rc;
+}
+
+int scalit_qmr(scalit_ctx *c, int ntype, int qmrmax, double qmrtol, int precision, const double *B,
+               double *X, double *res, int *iters)
+{
+    CTX_CHECK(c);
+    QmrResult r{};
+    int rc = qmr_host(c, ntype, qmrmax, qmrtol, precision, B, X, &r);
     if (rc) return rc;
     if (res) *res = r.res;
     if (iters) *iters = r.iters;
     return r.code;
+}
+
+int scalit_qmr_ex(scalit_ctx *c, int ntype, int qmrmax, double qmrtol, int precision, const double *B,
+                  double *X, int *code, double *res, int *iters)
+{
+    CTX_CHECK(c);
+    if (!code) { set_error("code is required"); return SCALIT_EINVAL; }
+    QmrResult r{};
+    int rc = qmr_host(c, ntype, qmrmax, qmrtol, precision, B, X, &r);
+    if (rc) return rc;
+    *code = r.code;
+    if (res) *res = r.res;
+    if (iters) *iters = r.iters;
+    return 0;
 }
 
 // ----------------------------------------------------------------- PIST --
