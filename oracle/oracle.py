@@ -728,3 +728,136 @@ def qmr_cx(hx, px, B, qmrmax, qmrtol, ntype=0, X0=None):
         code = -i
         vnrm, gamamo, thetamo = vnrmpo, gama, theta
     return code, X, res
+
+
+# ----------------------------------------------------------------------------------
+# Complex symmetric PIST (PIST_CONV_SX) and its helpers
+# ----------------------------------------------------------------------------------
+def get_op_cx(ntype, vec):
+    """getOpCX (src/libutil/serial/base/util_cx.f90:375-420): the real value a
+    complex number is compared by."""
+    v = np.asarray(vec, dtype=np.complex128)
+    re, im = v.real, v.imag
+    ops = {1: re, 2: np.abs(re), 3: im, 4: np.abs(im), 5: np.abs(re) + np.abs(im),
+           6: re ** 2 + im ** 2, 7: re + im, 8: np.abs(re + im), 9: re - im, 10: im - re,
+           11: np.abs(im - re), 12: np.abs(re) - np.abs(im), 13: np.abs(im) - np.abs(re),
+           14: np.abs(np.abs(im) - np.abs(re)), 15: np.abs(re) ** 2 - np.abs(im) ** 2}
+    return np.array(ops[int(ntype)], dtype=np.float64)
+
+
+def get_window_index(E0, vec, M):
+    """getWindow0 (util.f90:669-716) returning the picked indices."""
+    vec = np.asarray(vec, dtype=np.float64)
+    n = vec.size
+    if n < M:
+        return np.concatenate([np.arange(n), np.full(M - n, n - 1)])
+    absv = np.abs(vec - E0)
+    label = np.ones(n, dtype=bool)
+    out = np.empty(M, dtype=np.int64)
+    for i in range(M):
+        out[i] = int(np.argmin(np.where(label, absv, np.inf)))
+        label[out[i]] = False
+    return out
+
+
+def get_window_cx(E0, ntype, vec, M):
+    """getWindow_CX (util_cx.f90:301-325): the window of getWindow0 on getOpCX."""
+    vec = np.asarray(vec, dtype=np.complex128)
+    return vec[get_window_index(E0, get_op_cx(ntype, vec), M)]
+
+
+def get_diff_max_cx(ntype, v1, v2):
+    """getDiffMax_CX (util_cx.f90:33-43)."""
+    return get_diff_max(get_op_cx(ntype, v1), get_op_cx(ntype, v2))
+
+
+def reorder_cx(ntype, vec):
+    """ReOrder_CX('A', ...) (util_cx.f90:187-214): ascending by getOpCX."""
+    vec = np.asarray(vec, dtype=np.complex128)
+    return vec[np.argsort(get_op_cx(ntype, vec), kind="stable")]
+
+
+def dot_cx(x, y):
+    """DOT_CX (vector_cx.f90:227-234): the bilinear X^T Y."""
+    return complex(np.sum(np.asarray(x) * np.asarray(y)))
+
+
+def mgs_orth_sx(W, m, VJ):
+    """MGS_ORTH_SX (src/iterate/libiterate/orth/gsorth_sx.f90:47-72): modified
+    Gram-Schmidt in the bilinear product, column m of VJ (0-based) from W,
+    normalised by the principal square root of W^T W."""
+    v = np.asarray(W, dtype=np.complex128).copy()
+    for i in range(m):
+        v = v - dot_cx(VJ[:, i], v) * VJ[:, i]
+    nrm = np.sqrt(dot_cx(v, v))
+    if nrm == 0.0:
+        return False
+    VJ[:, m] = v / nrm
+    return True
+
+
+def pisth0_sx(X, m_max, m_low, m_high, h0x, linsolv, VJ, HMAT):
+    """pistH0_SX (src/iterate/libiterate/pist/pistHij_sx.f90:62-118)."""
+    if m_low < 1 or m_low >= m_high or m_high > m_max:
+        return 0
+    if m_low == 1:
+        m_start = 1
+        t = np.sqrt(dot_cx(X, X))
+        if t == 0.0:
+            return 0
+        VJ[:, 0] = np.asarray(X, dtype=np.complex128) / t
+    else:
+        m_start = m_low - 1
+    for J in range(m_start, m_high):
+        num, WJ = linsolv(VJ[:, J - 1])
+        if num <= 0:
+            return num
+        if not mgs_orth_sx(WJ, J, VJ):
+            return -J
+    for J in range(m_low, m_high + 1):
+        WJ = h0x(VJ[:, J - 1])
+        for I in range(1, m_high + 1):
+            HMAT[I - 1, J - 1] = dot_cx(VJ[:, I - 1], WJ)
+    for J in range(1, m_low):
+        WJ = h0x(VJ[:, J - 1])
+        for I in range(m_low, m_high + 1):
+            HMAT[I - 1, J - 1] = dot_cx(VJ[:, I - 1], WJ)
+    return m_high
+
+
+def pist_conv_sx(E0, etol, ntype, x, startcnt, stepcnt, stepeig, M, m_max, h0x, linsolv):
+    """PIST_CONV_SX (src/iterate/libiterate/pist/pist_sx.f90:4-96): PIST for a
+    complex symmetric operator.  The eigenvalues of HMAT come from ZGEEV
+    (numpy's eigvals is LAPACK's ZGEEV), the window and the final order use
+    the real part, the convergence test |lambda|^2 (getOpCX types 1 and 6).
+    ntype > 0 is not restated: the reference calls getSepMax_CX with five
+    arguments (an integer where a complex array is expected), which has no
+    defined result.  Returns (status, eig[M], RES)."""
+    if ntype > 0:
+        raise ValueError("PIST_CONV_SX with ntype > 0 has no defined result in the reference")
+    n_diff, n_conv = 1, 6
+    if stepeig >= m_max or startcnt > m_max or M > m_max:
+        return 0, np.zeros(M, np.complex128), 0.0
+    N = len(x)
+    VJ = np.zeros((N, m_max), np.complex128)
+    HMAT = np.zeros((m_max, m_max), np.complex128)
+    cnt_low, cnt_high = 1, max(startcnt, M, stepeig + 1)
+    status, res, eig = 0, 0.0, np.zeros(M, np.complex128)
+    while cnt_high <= m_max:
+        num = pisth0_sx(x, m_max, cnt_low, cnt_high, h0x, linsolv, VJ, HMAT)
+        if num <= 0:
+            return -cnt_high, eig, res
+        n1 = cnt_high - stepeig
+        old = get_window_cx(E0, n_diff, np.linalg.eigvals(HMAT[:n1, :n1]), M)
+        eig = get_window_cx(E0, n_diff, np.linalg.eigvals(HMAT[:cnt_high, :cnt_high]), M)
+        res = get_diff_max_cx(n_conv, eig, old)
+        if res <= etol:
+            status = cnt_high
+            break
+        status = -cnt_high
+        cnt_low = cnt_high + 1
+        if cnt_low >= m_max:
+            status = -m_max
+            break
+        cnt_high = min(cnt_high + stepcnt, m_max)
+    return status, reorder_cx(n_diff, eig), res

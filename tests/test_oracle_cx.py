@@ -1,12 +1,14 @@
 """The oracle's complex (absorbing-potential) forms against dense complex algebra (CPU).
 
 MYHX_DX (src/iterate/module/osb.hxdx.h:178-240), MYPX_DX
-(src/iterate/module/osb.mypxdx.h) and QMR_CX
-(src/iterate/libiterate/qmr/qmrcx.f90:4-175) carry no known answers in the
+(src/iterate/module/osb.mypxdx.h), QMR_CX
+(src/iterate/libiterate/qmr/qmrcx.f90:4-175) and PIST_CONV_SX
+(src/iterate/libiterate/pist/pist_sx.f90:4-96) carry no known answers in the
 reference; the restatement is pinned to its definition: H*X is the dense
-(H - E0 +- i A) X, P*X is V diag(1/(kernel)) V^T X, and QMR_CX recovers a
-known solution of a complex symmetric system (the pattern of the reference's
-real QMR driver, qmr.drv.f90:24-47).
+(H - E0 +- i A) X, P*X is V diag(1/(kernel)) V^T X, QMR_CX recovers a known
+solution of a complex symmetric system (the pattern of the reference's real
+QMR driver, qmr.drv.f90:24-47), and PIST_CONV_SX returns the eigenvalues
+ZGEEV gives for the dense operator.
 """
 import numpy as np
 import pytest
@@ -105,3 +107,50 @@ def test_cx_qmr_on_the_osb_operator(orc, cxcase, nosb):
                               lambda v: cx.px(v, nosb=nosb, ntype=orc.TAAP, de=3e-3), b, 500, 1e-10)
     assert code > 0
     assert rel(M @ x, b) < 1e-8
+
+
+def test_get_op_cx_and_window(orc):
+    z = np.array([1 - 2j, -3 + 0.5j, 0.25 + 0.25j])
+    np.testing.assert_array_equal(orc.get_op_cx(1, z), z.real)
+    np.testing.assert_array_equal(orc.get_op_cx(6, z), z.real ** 2 + z.imag ** 2)
+    np.testing.assert_array_equal(orc.get_op_cx(11, z), np.abs(z.imag - z.real))
+    np.testing.assert_array_equal(orc.get_window_cx(0.3, 1, z, 2), z[[2, 0]])
+    np.testing.assert_array_equal(orc.reorder_cx(1, z), z[[1, 2, 0]])
+
+
+def test_pist_sx_dense_known_answer(orc):
+    """PIST_CONV_SX with exact shift-and-invert solves on a complex symmetric
+    matrix returns its eigenvalues nearest E0 (by the real part), as ZGEEV does."""
+    rng = np.random.default_rng(5)
+    n = 60
+    a = rng.standard_normal((n, n))
+    M = (a + a.T) / 2 + np.diag(np.linspace(0.0, 6.0, n)) - 1j * np.diag(rng.uniform(0.01, 0.1, n))
+    E0 = 3.0
+    exact = np.linalg.eigvals(M)
+    want = np.sort_complex(exact[np.argsort(np.abs(exact.real - E0))[:5]])
+    inv = np.linalg.inv(M - E0 * np.eye(n))
+    x0 = rng.random(n) + 0j
+    st, eig, res = orc.pist_conv_sx(E0, 1e-12, 0, x0, 0, 5, 1, 5, n, lambda v: M @ v, lambda v: (1, inv @ v))
+    assert st > 0 and res <= 1e-12
+    np.testing.assert_allclose(eig[np.argsort(eig.real)], want[np.argsort(want.real)], atol=1e-9)
+    with pytest.raises(ValueError):
+        orc.pist_conv_sx(E0, 1e-12, 1, x0, 0, 5, 1, 5, n, lambda v: M @ v, lambda v: (1, inv @ v))
+
+
+def test_pist_sx_on_the_osb_operator(orc, cxcase):
+    """Complex levels of H - i AP nearest E0 through QMR_CX solves with the
+    complex OSB preconditioner (TMAP) against the dense eigenvalues."""
+    p, op, cx, V, H, e0 = cxcase
+    Heff = H - 1j * np.diag(cx.AP)
+    exact = np.linalg.eigvals(Heff)
+    want = exact[np.argsort(np.abs(exact.real - e0))[:6]]
+
+    def linsolv(v):
+        code, x, _ = orc.qmr_cx(lambda u: cx.hx(u, orc.TMAP), lambda u: cx.px(u, 1, orc.TMAP), v, 500, 1e-12)
+        return code, x
+
+    x0 = np.random.default_rng(6).random(p.N) + 0j
+    st, eig, res = orc.pist_conv_sx(e0, 1e-11, 0, x0, 0, 5, 1, 6, 150, lambda v: cx.hx(v, orc.TMAP0), linsolv)
+    assert st > 0
+    np.testing.assert_allclose(np.sort(eig.real), np.sort(want.real), atol=1e-8)
+    np.testing.assert_allclose(eig.imag[np.argsort(eig.real)], want.imag[np.argsort(want.real)], atol=1e-8)
