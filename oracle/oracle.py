@@ -861,3 +861,71 @@ def pist_conv_sx(E0, etol, ntype, x, startcnt, stepcnt, stepeig, M, m_max, h0x, 
             break
         cnt_high = min(cnt_high + stepcnt, m_max)
     return status, reorder_cx(n_diff, eig), res
+
+
+# ----------------------------------------------------------------------------------
+# Cumulative reaction probability (osbCRP, src/iterate/module/osbw.crp.h)
+# ----------------------------------------------------------------------------------
+def lan_dx(x, M, hx):
+    """LAN_DX (src/iterate/libiterate/lanczos/lan_dx.f90:299-325) with lanHij_dx
+    (lanHij_dx.f90:59-97) and LAN_MGS_ORTH_CX (orth/gsorth_cx.f90:132-160):
+    Lanczos for a Hermitian operator on complex vectors with full
+    re-orthogonalisation in the conjugated product, then DSTEV on the
+    tridiagonal.  Returns (status, eig)."""
+    from scipy.linalg import lapack
+    x = np.asarray(x, dtype=np.complex128)
+    n = x.size
+    t = np.sqrt(np.real(np.vdot(x, x)))
+    if t == 0.0:
+        return 0, None
+    VJ = np.zeros((n, M + 1), np.complex128)
+    VJ[:, 0] = x / t
+    alpha = np.zeros(M)
+    beta = np.zeros(M)
+    for J in range(1, M + 1):
+        w = hx(VJ[:, J - 1])
+        if J != 1:
+            w = w - beta[J - 2] * VJ[:, J - 2]
+        alpha[J - 1] = np.real(np.vdot(w, VJ[:, J - 1]))
+        v = w.copy()
+        for I in range(1, J + 1):
+            v = v - np.vdot(VJ[:, I - 1], v) * VJ[:, I - 1]
+        nrm = np.sqrt(np.real(np.vdot(v, v)))
+        beta[J - 1] = nrm
+        if nrm == 0.0:
+            return -J, None
+        VJ[:, J] = v / nrm
+    d, _, info = lapack.dstev(alpha, beta[:M - 1], compute_v=0)
+    if info != 0:
+        return -M, None
+    return M, d
+
+
+def crp_operator(cx, E, qmrmax, qmrtol, sap=True, conv=0):
+    """CRP_HXDX (osbw.crp.h:71-101) at energy E: y = sqrt(APR) x, solved with
+    (H - E - i AP), times APP, solved with (H - E + i AP), times sqrt(APR).
+    The preconditioner carries the absorbing potential when sAP is set
+    (sPC = TMAP / TAAP), the real kernel otherwise (sPC = TA1)."""
+    op = cx.op
+    op.set_e0(E)
+    sq = np.sqrt(cx.APR)
+    pm, pp = (TMAP, TAAP) if sap else (TA1, TA1)
+
+    def apply(x):
+        y = sq * x
+        _, t, _ = qmr_cx(lambda u: cx.hx(u, TMAP), lambda u: cx.px(u, 1, pm), y, qmrmax, qmrtol, conv)
+        y = cx.APP * t
+        _, t, _ = qmr_cx(lambda u: cx.hx(u, TAAP), lambda u: cx.px(u, 1, pp), y, qmrmax, qmrtol, conv)
+        return sq * t
+    return apply
+
+
+def osb_crp(cx, energies, NM, x0s, qmrmax, qmrtol, sap=True, conv=0):
+    """osbCRP / calOSBCRP (osbw.crp.h:6-68): N(E) = 4 sum of the NM Lanczos
+    eigenvalues of the CRP operator from the start vector x0s[i] (the
+    reference draws it with randMat_CX); 0 when the Lanczos fails."""
+    out = np.zeros(len(energies))
+    for i, E in enumerate(energies):
+        st, eig = lan_dx(x0s[i], NM, crp_operator(cx, float(E), qmrmax, qmrtol, sap, conv))
+        out[i] = 4.0 * float(np.sum(eig)) if st > 0 else 0.0
+    return out

@@ -154,3 +154,34 @@ def test_pist_sx_on_the_osb_operator(orc, cxcase):
     assert st > 0
     np.testing.assert_allclose(np.sort(eig.real), np.sort(want.real), atol=1e-8)
     np.testing.assert_allclose(eig.imag[np.argsort(eig.real)], want.imag[np.argsort(want.real)], atol=1e-8)
+
+
+def test_lan_dx_hermitian(orc):
+    """LAN_DX on a Hermitian matrix: n steps give its whole spectrum."""
+    rng = np.random.default_rng(7)
+    n = 30
+    a = rng.standard_normal((n, n)) + 1j * rng.standard_normal((n, n))
+    A = (a + a.conj().T) / 2
+    st, eig = orc.lan_dx(rng.random(n) + 1j * rng.random(n), n, lambda v: A @ v)
+    assert st == n
+    np.testing.assert_allclose(np.sort(eig), np.linalg.eigvalsh(A), atol=1e-10)
+
+
+def test_crp_equals_dense_trace(orc, cxcase):
+    """With APR on r points the CRP operator has rank <= r, so r + 1 Lanczos
+    steps give its trace: N(E) = 4 Tr[sqrt(APR) G+ APP G- sqrt(APR)]."""
+    p, op, cx0, V, H, e0 = cxcase
+    rng = np.random.default_rng(8)
+    apr = np.zeros(p.N)
+    pts = rng.choice(p.N, 12, replace=False)
+    apr[pts] = rng.uniform(1e-3, 3e-3, 12)
+    app = np.where(apr == 0.0, rng.uniform(0.0, 2e-3, p.N), 0.0)
+    cx = orc.CxOperator(op, app, apr)
+    E = e0
+    G = lambda s: np.linalg.inv(H - E * np.eye(p.N) + s * 1j * np.diag(cx.AP))
+    sq = np.diag(np.sqrt(apr))
+    dense = 4.0 * np.real(np.trace(sq @ G(1) @ np.diag(app) @ G(-1) @ sq))
+    x0 = rng.random(p.N) + 1j * rng.random(p.N)
+    got = orc.osb_crp(cx, [E], 13, [x0], 1000, 1e-13)[0]
+    assert dense > 0.0
+    assert abs(got - dense) / dense < 1e-6
