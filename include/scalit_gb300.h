@@ -251,6 +251,18 @@ int scalit_px_cx_device(scalit_ctx *ctx, int ntype, int nvec, const double *dX, 
  * library error. */
 int scalit_qmr_cx(scalit_ctx *ctx, int conv, int qmrmax, double qmrtol, int ntype, const double *B,
                   double *X, int *code, double *res);
+/* Cumulative reaction probability, osbCRP / calOSBCRP
+ * (src/iterate/module/osbw.crp.h:6-101): for each of the nenergy energies E
+ * (E0 = E during the call; the context's shift is restored afterwards),
+ * nm steps of LAN_DX (Hermitian Lanczos with full re-orthogonalisation) on
+ * sqrt(APR) (H - E + i AP)^-1 APP (H - E - i AP)^-1 sqrt(APR) from the start
+ * vector X0 + e * npoints (interleaved complex; the reference draws it with
+ * randMat_CX), each inverse a QMR_CX solve (conv, qmrmax, qmrtol) with the
+ * preconditioner's absorbing term when sap != 0 (sAP; otherwise its real
+ * kernel, sPC = TA1).  crp[e] = 4 times the sum of the Lanczos eigenvalues
+ * (the tridiagonal's trace), 0 when the Lanczos breaks down. */
+int scalit_crp(scalit_ctx *ctx, int nenergy, const double *energies, int nm, int qmrmax, double qmrtol,
+               int conv, int sap, const double *X0, double *crp);
 
 /* ------------------------------------------------------------------ QMR ---
  * OSB_QMR -> QMR / QMR_MPI (src/iterate/module/osbw.qmr.h:13-23,

@@ -58,6 +58,7 @@ SIGNATURES = {
     "scalit_px_cx": (C.c_int, [_vp, C.c_int, C.c_int, _dp, _dp]),
     "scalit_px_cx_device": (C.c_int, [_vp, C.c_int, C.c_int, _vp, _vp]),
     "scalit_qmr_cx": (C.c_int, [_vp, C.c_int, C.c_int, C.c_double, C.c_int, _dp, _dp, _ip, _dp]),
+    "scalit_crp": (C.c_int, [_vp, C.c_int, _dp, C.c_int, C.c_int, C.c_double, C.c_int, C.c_int, _dp, _dp]),
     "scalit_set_osbw": (C.c_int, [_vp, C.c_double, C.c_int, _dp, C.c_int, _dp]),
     "scalit_get_osbw": (C.c_int, [_vp, _ip, _ip, _dp]),
     "scalit_px": (C.c_int, [_vp, C.c_int, C.c_int, _dp, _dp]),
@@ -348,6 +349,19 @@ class Context:
                                       _p(Bc.view(np.float64)), _p(X.view(np.float64)), C.byref(code),
                                       C.byref(res)))
         return code.value, X, res.value
+
+    def crp(self, energies, nm, qmrmax=2000, qmrtol=1e-4, conv=0, sap=True, X0=None, seed=0):
+        """osbCRP: N(E) at each energy.  X0 (len(energies) x N complex) defaults
+        to seeded uniform real and imaginary parts, as randMat_CX draws them."""
+        E = _f64(np.atleast_1d(energies))
+        if X0 is None:
+            rng = np.random.default_rng(seed)
+            X0 = rng.random((E.size, self.N)) + 1j * rng.random((E.size, self.N))
+        Z = np.ascontiguousarray(X0, dtype=np.complex128)
+        out = np.zeros(E.size)
+        _check(self.lib.scalit_crp(self.h, E.size, _p(E), int(nm), int(qmrmax), float(qmrtol), int(conv),
+                                   int(bool(sap)), _p(Z.view(np.float64).ravel()), _p(out)))
+        return out
 
     def get_osbw(self):
         """(ind, HW): the window's grid points (0-based) and its matrix."""

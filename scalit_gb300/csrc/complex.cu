@@ -132,6 +132,21 @@ __global__ void cx_axpby_kernel(i64 n, double ar, double ai, const double *__res
     }
 }
 
+// y = a x for a real array a and a planar complex x.
+__global__ void cx_mul_real_kernel(i64 n, const double *__restrict__ a, const double *__restrict__ x,
+                                   double *__restrict__ y)
+{
+    for (i64 p = blockIdx.x * (i64)blockDim.x + threadIdx.x; p < n; p += (i64)gridDim.x * blockDim.x) {
+        y[p] = a[p] * x[p];
+        y[n + p] = a[p] * x[n + p];
+    }
+}
+
+__global__ void sqrt_kernel(i64 n, const double *__restrict__ x, double *__restrict__ y)
+{
+    for (i64 p = blockIdx.x * (i64)blockDim.x + threadIdx.x; p < n; p += (i64)gridDim.x * blockDim.x) y[p] = sqrt(x[p]);
+}
+
 __global__ void real_div_kernel(i64 n, double *__restrict__ x, double d)
 {
     for (i64 p = blockIdx.x * (i64)blockDim.x + threadIdx.x; p < n; p += (i64)gridDim.x * blockDim.x) x[p] = x[p] / d;
@@ -141,6 +156,8 @@ __global__ void real_mul_kernel(i64 n, double *__restrict__ x, double a)
 {
     for (i64 p = blockIdx.x * (i64)blockDim.x + threadIdx.x; p < n; p += (i64)gridDim.x * blockDim.x) x[p] = a * x[p];
 }
+
+static int to_planar(scalit_ctx *c, const double *Z, bool host, double *stage, double *P);
 
 // -------------------------------------------------------- planar operators --
 // MYHX_DX on a planar complex vector.
@@ -211,8 +228,8 @@ static int px_cx_planar(const scalit_ctx *c, int ntype, const double *X, double 
 // Bilinear products X^T Y (DOT_CX, vector_cx.f90:227-234) and the norms of
 // the conjugated dot_product are deterministic FP64 device reductions read
 // back per use; the scalar recurrence runs on the host as in the reference.
-static int qmr_cx_run(scalit_ctx *c, int conv, int qmrmax, double tol, int ntype, const double *B, double *X,
-                      int *code_out, double *res_out)
+static int qmr_cx_run(scalit_ctx *c, int conv, int qmrmax, double tol, int ntype, int px_ntype, const double *B,
+                      double *X, int *code_out, double *res_out)
 {
     typedef std::complex<double> cplx;
     const i64 N = c->L.N, N2 = 2 * N;
@@ -279,7 +296,7 @@ static int qmr_cx_run(scalit_ctx *c, int conv, int qmrmax, double tol, int ntype
         }
         if ((rc = nrm(B, &bnrm))) break;
         vnrm = bnrm;
-        if ((rc = px_cx_planar(c, ntype, B, Z, T, s))) break;
+        if ((rc = px_cx_planar(c, px_ntype, B, Z, T, s))) break;
         if ((rc = nrm(Z, &znrm))) break;
         code = 0;
         for (int i = 1; i <= qmrmax; ++i) {
@@ -301,7 +318,7 @@ static int qmr_cx_run(scalit_ctx *c, int conv, int qmrmax, double tol, int ntype
             if ((rc = axpby(cplx(1.0, 0.0), Sv, -beta, V, 0))) break;
             double vnrmpo;
             if ((rc = nrm(V, &vnrmpo))) break;
-            if ((rc = px_cx_planar(c, ntype, V, Z, T, s))) break;
+            if ((rc = px_cx_planar(c, px_ntype, V, Z, T, s))) break;
             if ((rc = rdiv(Z, zvrat))) break;
             if ((rc = nrm(Z, &znrm))) break;
             const double theta = vnrmpo / (gamamo * std::abs(beta));
@@ -349,6 +366,122 @@ static int qmr_cx_run(scalit_ctx *c, int conv, int qmrmax, double tol, int ntype
     *code_out = code;
     if (res_out) *res_out = res;
     return 0;
+}
+
+// ---------------------------------------------------------------------- CRP --
+// osbCRP / calOSBCRP (src/iterate/module/osbw.crp.h:6-68): at each energy E
+// (sOSBW%mE0 = E) NM steps of LAN_DX (lanczos/lan_dx.f90:299-325, lanHij_dx
+// lanHij_dx.f90:59-97, LAN_MGS_ORTH_CX orth/gsorth_cx.f90:132-160) on the
+// Hermitian operator of CRP_HXDX (:71-101): sqrt(APR) (H - E + i AP)^-1 APP
+// (H - E - i AP)^-1 sqrt(APR), each inverse a QMR_CX solve.  N(E) is 4 times
+// the sum of the tridiagonal's eigenvalues, i.e. 4 sum(alpha) (its trace);
+// the reference's DSTEV gives the same sum to rounding.  A Lanczos breakdown
+// (beta = 0) gives N(E) = 0 as LAN_DX's failure does.
+static int crp_run(scalit_ctx *c, int nE, const double *energies, int nm, int qmrmax, double tol, int conv,
+                   int sap, const double *X0, double *out)
+{
+    typedef std::complex<double> cplx;
+    const i64 N = c->L.N, N2 = 2 * N;
+    cudaStream_t s = c->stream;
+    double *w = nullptr, *dd = nullptr;
+    if (cudaMallocAsync(&w, sizeof(double) * (size_t)N2 * ((size_t)nm + 5), s) != cudaSuccess) {
+        cudaGetLastError();
+        set_error("CRP workspace (%d Lanczos vectors of %lld complex points) does not fit", nm + 5, N);
+        return SCALIT_ENOMEM;
+    }
+    if (cudaMallocAsync(&dd, sizeof(double) * 8, s) != cudaSuccess) {
+        cudaGetLastError();
+        cudaFreeAsync(w, s);
+        set_error("CRP scalars do not fit");
+        return SCALIT_ENOMEM;
+    }
+    double *SQ = w, *W = w + N2, *Y = w + 2 * N2, *Tq = w + 3 * N2, *stage = w + 4 * N2, *VJ = w + 5 * N2;
+    auto col = [&](int j) { return VJ + (i64)j * N2; };
+    const int g = cgrid(N), g2 = cgrid(N2);
+    const double e_saved = c->E0;
+    const int pm = sap ? SCALIT_TMAP : SCALIT_TA1, pp = sap ? SCALIT_TAAP : SCALIT_TA1;
+    int rc = 0;
+    // the conjugated product x^H y (Fortran dot_product)
+    auto hdot = [&](const double *x, const double *y, cplx *r) -> int {
+        int e = dot_dev<double>(c, N, x, y, dd, s);
+        if (!e) e = dot_dev<double>(c, N, x + N, y + N, dd + 1, s);
+        if (!e) e = dot_dev<double>(c, N, x, y + N, dd + 2, s);
+        if (!e) e = dot_dev<double>(c, N, x + N, y, dd + 3, s);
+        if (e) return e;
+        double h[4];
+        e = sync_read_doubles(c, dd, h, 4);
+        if (e) return e;
+        *r = cplx(h[0] + h[1], h[2] - h[3]);
+        return 0;
+    };
+    auto axpby = [&](cplx a, const double *x, cplx b, double *y, int overwrite) -> int {
+        cx_axpby_kernel<<<g, kT, 0, s>>>(N, a.real(), a.imag(), x, b.real(), b.imag(), y, overwrite);
+        SC_CHECK_LAUNCH();
+        return 0;
+    };
+    auto mulr = [&](const double *a, const double *x, double *y) -> int {
+        cx_mul_real_kernel<<<g, kT, 0, s>>>(N, a, x, y);
+        SC_CHECK_LAUNCH();
+        return 0;
+    };
+    sqrt_kernel<<<g, kT, 0, s>>>(N, c->APR, SQ);
+    if (cudaGetLastError() != cudaSuccess) { set_error("CRP sqrt launch failed"); rc = SCALIT_ECUDA; }
+    std::vector<double> alpha((size_t)nm), beta((size_t)nm);
+    for (int e = 0; e < nE && !rc; ++e) {
+        c->E0 = energies[e];
+        c->gen++;
+        out[e] = 0.0;
+        rc = to_planar(c, X0 + (i64)e * N2, true, stage, col(0));
+        if (rc) break;
+        cplx t;
+        if ((rc = hdot(col(0), col(0), &t))) break;
+        const double tn = std::sqrt(t.real());
+        if (tn == 0.0) continue;
+        real_div_kernel<<<g2, kT, 0, s>>>(N2, col(0), tn);
+        if (cudaGetLastError() != cudaSuccess) { set_error("CRP launch failed"); rc = SCALIT_ECUDA; break; }
+        bool ok = true;
+        for (int J = 1; J <= nm && !rc && ok; ++J) {
+            int code = 0;
+            // W = sqrt(APR) (H - E + i AP)^-1 APP (H - E - i AP)^-1 sqrt(APR) VJ(J)
+            if ((rc = mulr(SQ, col(J - 1), Y))) break;
+            if ((rc = qmr_cx_run(c, conv, qmrmax, tol, SCALIT_TMAP, pm, Y, Tq, &code, nullptr))) break;
+            if ((rc = mulr(c->APP, Tq, Y))) break;
+            if ((rc = qmr_cx_run(c, conv, qmrmax, tol, SCALIT_TAAP, pp, Y, Tq, &code, nullptr))) break;
+            if ((rc = mulr(SQ, Tq, W))) break;
+            if (J != 1 && (rc = axpby(cplx(-beta[(size_t)J - 2], 0.0), col(J - 2), cplx(1.0, 0.0), W, 0))) break;
+            cplx a;
+            if ((rc = hdot(W, col(J - 1), &a))) break;
+            alpha[(size_t)J - 1] = a.real();
+            for (int I = 1; I <= J; ++I) {
+                cplx d;
+                if ((rc = hdot(col(I - 1), W, &d))) break;
+                if ((rc = axpby(-d, col(I - 1), cplx(1.0, 0.0), W, 0))) break;
+            }
+            if (rc) break;
+            cplx nw;
+            if ((rc = hdot(W, W, &nw))) break;
+            const double nrm = std::sqrt(nw.real());
+            beta[(size_t)J - 1] = nrm;
+            if (nrm == 0.0) { ok = false; break; }
+            if (cudaMemcpyAsync(col(J), W, sizeof(double) * (size_t)N2, cudaMemcpyDeviceToDevice, s) != cudaSuccess) {
+                set_error("CRP copy failed");
+                rc = SCALIT_ECUDA;
+                break;
+            }
+            real_div_kernel<<<g2, kT, 0, s>>>(N2, col(J), nrm);
+            if (cudaGetLastError() != cudaSuccess) { set_error("CRP launch failed"); rc = SCALIT_ECUDA; break; }
+        }
+        if (rc || !ok) continue;
+        double sum = 0.0;
+        for (int j = 0; j < nm; ++j) sum += alpha[(size_t)j];
+        out[e] = 4.0 * sum;
+    }
+    c->E0 = e_saved;
+    c->gen++;
+    cudaFreeAsync(w, s);
+    cudaFreeAsync(dd, s);
+    cudaStreamSynchronize(s);
+    return rc;
 }
 
 // ------------------------------------------------------------------- C ABI --
@@ -476,11 +609,23 @@ int scalit_qmr_cx(scalit_ctx *c, int conv, int qmrmax, double qmrtol, int ntype,
     double *stage = w, *Bp = w + 2 * N, *Xp = w + 4 * N;
     int rc = to_planar(c, B, true, stage, Bp);
     if (!rc && conv > 0) rc = to_planar(c, X, true, stage, Xp);
-    if (!rc) rc = qmr_cx_run(c, conv, qmrmax, qmrtol, ntype, Bp, Xp, code, res);
+    if (!rc) rc = qmr_cx_run(c, conv, qmrmax, qmrtol, ntype, ntype, Bp, Xp, code, res);
     if (!rc) rc = from_planar(c, Xp, true, stage, X);
     cudaFreeAsync(w, c->stream);
     if (cudaStreamSynchronize(c->stream) != cudaSuccess && !rc) { set_error("QMR_CX failed"); rc = SCALIT_ECUDA; }
     return rc;
+}
+
+int scalit_crp(scalit_ctx *c, int nenergy, const double *energies, int nm, int qmrmax, double qmrtol, int conv,
+               int sap, const double *X0, double *crp)
+{
+    CX_CTX_CHECK(c);
+    if (!c->osb_built) { set_error("CRP needs the preconditioner: build or load it first"); return SCALIT_ESTATE; }
+    if (!c->AP) { set_error("CRP needs the absorbing potentials: call scalit_set_absorbing"); return SCALIT_ESTATE; }
+    if (nenergy < 0 || nm < 1) { set_error("CRP needs nenergy >= 0 and nm >= 1"); return SCALIT_EINVAL; }
+    if (nenergy == 0) return 0;
+    if (!energies || !X0 || !crp) { set_error("energies, X0 and crp are required"); return SCALIT_EINVAL; }
+    return crp_run(c, nenergy, energies, nm, qmrmax, qmrtol, conv, sap, X0, crp);
 }
 
 }  // extern "C"

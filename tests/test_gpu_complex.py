@@ -110,3 +110,26 @@ def test_errors(lib, case):
         with pytest.raises(capi.ScalitError) as e:
             ctx.set_absorbing(bad)
         assert e.value.code == -106
+
+
+def test_crp_matches_oracle_and_dense_trace(lib, orc, case):
+    """osbCRP: with APR on r points, r + 1 Lanczos steps give the trace
+    4 Tr[sqrt(APR) G+ APP G- sqrt(APR)] (computed densely here)."""
+    p, ref, e0, app0, apr0 = case
+    rng = np.random.default_rng(9)
+    apr = np.zeros(p.N)
+    pts = rng.choice(p.N, 10, replace=False)
+    apr[pts] = rng.uniform(1e-3, 3e-3, 10)
+    app = np.where(apr == 0.0, rng.uniform(0.0, 2e-3, p.N), 0.0)
+    cx = orc.CxOperator(ref, app, apr)
+    H = hm.dense_hamiltonian(p, shift=0.0)
+    G = lambda s: np.linalg.inv(H - e0 * np.eye(p.N) + s * 1j * np.diag(cx.AP))
+    sq = np.diag(np.sqrt(apr))
+    dense = 4.0 * np.real(np.trace(sq @ G(1) @ np.diag(app) @ G(-1) @ sq))
+    x0 = rng.random(p.N) + 1j * rng.random(p.N)
+    with context(p, ref, e0, app, apr) as ctx:
+        got = ctx.crp([e0], 11, qmrmax=2000, qmrtol=1e-12, X0=x0[None, :])[0]
+    want = orc.osb_crp(cx, [e0], 11, [x0], 2000, 1e-12)[0]
+    assert dense > 0.0
+    assert abs(got - dense) / dense < 1e-5
+    assert abs(got - want) / want < 1e-5
