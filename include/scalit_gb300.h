@@ -263,6 +263,20 @@ int scalit_qmr_cx(scalit_ctx *ctx, int conv, int qmrmax, double qmrtol, int ntyp
  * (the tridiagonal's trace), 0 when the Lanczos breaks down. */
 int scalit_crp(scalit_ctx *ctx, int nenergy, const double *energies, int nm, int qmrmax, double qmrtol,
                int conv, int sap, const double *X0, double *crp);
+/* PIST for the complex symmetric operator, PIST_CONV_SX
+ * (src/iterate/libiterate/pist/pist_sx.f90:4-96, pistHij_sx.f90:62-118,
+ * orth/gsorth_sx.f90:47-72): the Krylov basis of the QMR_CX solves
+ * (ls_ntype for H, ls_px_ntype for P, conv / qmrmax / qmrtol; the context's
+ * shift is their E0) in the bilinear product, HMAT = VJ^T H0 VJ with H0 =
+ * MYHX_DX(h0_ntype), its eigenvalues by cuSOLVER's general eigensolver (ZGEEV
+ * in the reference), the m nearest e0 by the real part, converged when the
+ * change of |lambda|^2 is <= etol.  eig receives m interleaved complex values
+ * in ascending real part, *status PIST's result (+cnt, -cnt, 0 for bad
+ * parameters).  ntype > 0 returns SCALIT_EUNSUP: the reference's call of
+ * getSepMax_CX there passes mismatched arguments. */
+int scalit_pist_cx(scalit_ctx *ctx, double e0, double etol, int ntype, const double *X0, int startcnt,
+                   int stepcnt, int stepeig, int m, int m_max, int h0_ntype, int ls_ntype, int ls_px_ntype,
+                   int conv, int qmrmax, double qmrtol, double *eig, double *res, int *status);
 
 /* ------------------------------------------------------------------ QMR ---
  * OSB_QMR -> QMR / QMR_MPI (src/iterate/module/osbw.qmr.h:13-23,

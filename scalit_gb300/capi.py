@@ -59,6 +59,9 @@ SIGNATURES = {
     "scalit_px_cx_device": (C.c_int, [_vp, C.c_int, C.c_int, _vp, _vp]),
     "scalit_qmr_cx": (C.c_int, [_vp, C.c_int, C.c_int, C.c_double, C.c_int, _dp, _dp, _ip, _dp]),
     "scalit_crp": (C.c_int, [_vp, C.c_int, _dp, C.c_int, C.c_int, C.c_double, C.c_int, C.c_int, _dp, _dp]),
+    "scalit_pist_cx": (C.c_int, [_vp, C.c_double, C.c_double, C.c_int, _dp, C.c_int, C.c_int, C.c_int,
+                                 C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_double,
+                                 _dp, _dp, _ip]),
     "scalit_set_osbw": (C.c_int, [_vp, C.c_double, C.c_int, _dp, C.c_int, _dp]),
     "scalit_get_osbw": (C.c_int, [_vp, _ip, _ip, _dp]),
     "scalit_px": (C.c_int, [_vp, C.c_int, C.c_int, _dp, _dp]),
@@ -362,6 +365,19 @@ class Context:
         _check(self.lib.scalit_crp(self.h, E.size, _p(E), int(nm), int(qmrmax), float(qmrtol), int(conv),
                                    int(bool(sap)), _p(Z.view(np.float64).ravel()), _p(out)))
         return out
+
+    def pist_cx(self, x0, m, e0, etol, m_max, startcnt=0, stepcnt=5, stepeig=1, h0_ntype=TMAP0,
+                ls_ntype=TMAP, ls_px_ntype=TMAP, conv=0, qmrmax=2000, qmrtol=1e-4, ntype=0):
+        """PIST_CONV_SX: returns (status, eig[m] complex, RES)."""
+        Z = np.ascontiguousarray(x0, dtype=np.complex128)
+        eig = np.zeros(int(m), dtype=np.complex128)
+        res = C.c_double(0.0)
+        st = C.c_int(0)
+        _check(self.lib.scalit_pist_cx(self.h, float(e0), float(etol), int(ntype), _p(Z.view(np.float64)),
+                                       int(startcnt), int(stepcnt), int(stepeig), int(m), int(m_max),
+                                       int(h0_ntype), int(ls_ntype), int(ls_px_ntype), int(conv), int(qmrmax),
+                                       float(qmrtol), _p(eig.view(np.float64)), C.byref(res), C.byref(st)))
+        return st.value, eig, res.value
 
     def get_osbw(self):
         """(ind, HW): the window's grid points (0-based) and its matrix."""

@@ -11,6 +11,8 @@
 // interleaved COMPLEX*16 arrays.
 #include "internal.cuh"
 
+#include <cusolverDn.h>
+
 #include <algorithm>
 #include <cmath>
 #include <complex>
@@ -484,6 +486,252 @@ static int crp_run(scalit_ctx *c, int nE, const double *energies, int nm, int qm
     return rc;
 }
 
+// ------------------------------------------------------------------ PIST_SX --
+// PIST_CONV_SX (src/iterate/libiterate/pist/pist_sx.f90:4-96) with pistH0_SX
+// (pistHij_sx.f90:62-118) and MGS_ORTH_SX (orth/gsorth_sx.f90:47-72): the
+// Krylov basis of the complex symmetric operator in the bilinear product,
+// HMAT(I, J) = VJ_I^T H0 VJ_J, its eigenvalues (ZGEEV in the reference;
+// cuSOLVER's general eigensolver here), windowed around E0 by the real part
+// and tested on |lambda|^2 (getOpCX types 1 and 6, util_cx.f90:375-420).
+typedef std::complex<double> cplx;
+
+static double op_cx(int type, cplx z)
+{
+    return type == 1 ? z.real() : z.real() * z.real() + z.imag() * z.imag();
+}
+
+// getWindow_CX (util_cx.f90:301-325) over getWindow0 (util.f90:669-716): the
+// M values closest to E0 in turn, ties to the lowest index; a short list is
+// padded with its last value.
+static void window_cx(double E0, int type, const std::vector<cplx> &vec, int M, std::vector<cplx> &out)
+{
+    const int n = (int)vec.size();
+    out.assign((size_t)M, cplx(0.0, 0.0));
+    if (n < M) {
+        for (int i = 0; i < M; ++i) out[(size_t)i] = vec[(size_t)std::min(i, n - 1)];
+        return;
+    }
+    std::vector<char> label((size_t)n, 1);
+    for (int i = 0; i < M; ++i) {
+        int best = -1;
+        double bv = 0.0;
+        for (int j = 0; j < n; ++j) {
+            if (!label[(size_t)j]) continue;
+            const double a = std::fabs(op_cx(type, vec[(size_t)j]) - E0);
+            if (best < 0 || a < bv) { best = j; bv = a; }
+        }
+        out[(size_t)i] = vec[(size_t)best];
+        label[(size_t)best] = 0;
+    }
+}
+
+// Eigenvalues of the leading n x n block of HMAT (column-major, leading dimension ld).
+static int geev_cx(scalit_ctx *c, int n, const std::vector<cplx> &H, int ld, std::vector<cplx> &w)
+{
+    cudaStream_t s = c->stream;
+    cusolverDnHandle_t sol = (cusolverDnHandle_t)c->cusolver;
+    if (cusolverDnSetStream(sol, s) != CUSOLVER_STATUS_SUCCESS) { set_error("cusolverDnSetStream failed"); return SCALIT_ECUDA; }
+    std::vector<cplx> A((size_t)n * n);
+    for (int j = 0; j < n; ++j)
+        for (int i = 0; i < n; ++i) A[(size_t)i + (size_t)j * n] = H[(size_t)i + (size_t)j * ld];
+    cusolverDnParams_t prm = nullptr;
+    if (cusolverDnCreateParams(&prm) != CUSOLVER_STATUS_SUCCESS) { set_error("cusolverDnCreateParams failed"); return SCALIT_ECUDA; }
+    void *dA = nullptr, *dW = nullptr, *dbuf = nullptr;
+    int *dinfo = nullptr;
+    std::vector<unsigned char> hbuf;
+    int rc = 0;
+    size_t dws = 0, hws = 0;
+    do {
+        if (cudaMallocAsync(&dA, sizeof(cplx) * A.size(), s) != cudaSuccess ||
+            cudaMallocAsync(&dW, sizeof(cplx) * (size_t)n, s) != cudaSuccess ||
+            cudaMallocAsync(&dinfo, sizeof(int), s) != cudaSuccess) {
+            cudaGetLastError();
+            set_error("eigensolver buffers do not fit");
+            rc = SCALIT_ENOMEM;
+            break;
+        }
+        if (cudaMemcpyAsync(dA, A.data(), sizeof(cplx) * A.size(), cudaMemcpyHostToDevice, s) != cudaSuccess) {
+            set_error("HMAT upload failed");
+            rc = SCALIT_ECUDA;
+            break;
+        }
+        if (cusolverDnXgeev_bufferSize(sol, prm, CUSOLVER_EIG_MODE_NOVECTOR, CUSOLVER_EIG_MODE_NOVECTOR, n, CUDA_C_64F,
+                                       dA, n, CUDA_C_64F, dW, CUDA_C_64F, nullptr, 1, CUDA_C_64F, nullptr, 1,
+                                       CUDA_C_64F, &dws, &hws) != CUSOLVER_STATUS_SUCCESS) {
+            set_error("cusolverDnXgeev_bufferSize failed");
+            rc = SCALIT_ECUDA;
+            break;
+        }
+        if (cudaMallocAsync(&dbuf, std::max<size_t>(dws, 16), s) != cudaSuccess) {
+            cudaGetLastError();
+            set_error("eigensolver workspace does not fit");
+            rc = SCALIT_ENOMEM;
+            break;
+        }
+        hbuf.resize(std::max<size_t>(hws, 16));
+        if (cudaMemsetAsync(dinfo, 0, sizeof(int), s) != cudaSuccess ||
+            cusolverDnXgeev(sol, prm, CUSOLVER_EIG_MODE_NOVECTOR, CUSOLVER_EIG_MODE_NOVECTOR, n, CUDA_C_64F, dA, n,
+                            CUDA_C_64F, dW, CUDA_C_64F, nullptr, 1, CUDA_C_64F, nullptr, 1, CUDA_C_64F, dbuf, dws,
+                            hbuf.data(), hws, dinfo) != CUSOLVER_STATUS_SUCCESS) {
+            set_error("cusolverDnXgeev failed");
+            rc = SCALIT_ECUDA;
+            break;
+        }
+        int info = -999;
+        w.assign((size_t)n, cplx(0.0, 0.0));
+        if (cudaMemcpyAsync(&info, dinfo, sizeof(int), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+            cudaMemcpyAsync(w.data(), dW, sizeof(cplx) * (size_t)n, cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+            cudaStreamSynchronize(s) != cudaSuccess) {
+            set_error("eigenvalue read-back failed");
+            rc = SCALIT_ECUDA;
+            break;
+        }
+        if (info != 0) rc = 1;   // the eigensolver's own failure: PIST reports -num
+    } while (0);
+    if (dA) cudaFreeAsync(dA, s);
+    if (dW) cudaFreeAsync(dW, s);
+    if (dbuf) cudaFreeAsync(dbuf, s);
+    if (dinfo) cudaFreeAsync(dinfo, s);
+    cudaStreamSynchronize(s);
+    cusolverDnDestroyParams(prm);
+    return rc;
+}
+
+struct PistCxArgs {
+    double e0, etol;
+    int startcnt, stepcnt, stepeig, m, m_max;
+    int h0_ntype, ls_ntype, ls_px_ntype, conv, qmrmax;
+    double qmrtol;
+};
+
+static int pist_cx_run(scalit_ctx *c, const PistCxArgs &a, const double *X0, std::vector<cplx> &eig, double *res_out,
+                       int *status_out)
+{
+    const i64 N = c->L.N, N2 = 2 * N;
+    cudaStream_t s = c->stream;
+    const int MM = a.m_max;
+    *status_out = 0;
+    eig.assign((size_t)a.m, cplx(0.0, 0.0));
+    if (a.stepeig >= MM || a.startcnt > MM || a.m > MM) return 0;
+    double *w = nullptr, *dd = nullptr;
+    if (cudaMallocAsync(&w, sizeof(double) * (size_t)N2 * ((size_t)MM + 3), s) != cudaSuccess) {
+        cudaGetLastError();
+        set_error("complex PIST basis (%d vectors of %lld complex points) does not fit", MM, N);
+        return SCALIT_ENOMEM;
+    }
+    if (cudaMallocAsync(&dd, sizeof(double) * 8, s) != cudaSuccess) {
+        cudaGetLastError();
+        cudaFreeAsync(w, s);
+        set_error("complex PIST scalars do not fit");
+        return SCALIT_ENOMEM;
+    }
+    double *Wv = w, *stage = w + N2, *Xin = w + 2 * N2, *VJ = w + 3 * N2;
+    auto col = [&](int j1) { return VJ + (i64)(j1 - 1) * N2; };   // 1-based
+    const int g = cgrid(N);
+    std::vector<cplx> H((size_t)MM * MM, cplx(0.0, 0.0));
+    auto bil = [&](const double *x, const double *y, cplx *r) -> int {
+        int e = dot_dev<double>(c, N, x, y, dd, s);
+        if (!e) e = dot_dev<double>(c, N, x + N, y + N, dd + 1, s);
+        if (!e) e = dot_dev<double>(c, N, x, y + N, dd + 2, s);
+        if (!e) e = dot_dev<double>(c, N, x + N, y, dd + 3, s);
+        if (e) return e;
+        double h[4];
+        e = sync_read_doubles(c, dd, h, 4);
+        if (e) return e;
+        *r = cplx(h[0] - h[1], h[2] + h[3]);
+        return 0;
+    };
+    auto axpby = [&](cplx al, const double *x, cplx be, double *y, int overwrite) -> int {
+        cx_axpby_kernel<<<g, kT, 0, s>>>(N, al.real(), al.imag(), x, be.real(), be.imag(), y, overwrite);
+        SC_CHECK_LAUNCH();
+        return 0;
+    };
+    // pistH0_SX: returns m_high, <= 0 from the linear solver, -J from the orthogonalisation
+    auto pisth0 = [&](int m_low, int m_high, int *ret) -> int {
+        *ret = 0;
+        if (m_low < 1 || m_low >= m_high || m_high > MM) return 0;
+        int m_start;
+        if (m_low == 1) {
+            m_start = 1;
+            cplx xx;
+            int e = bil(Xin, Xin, &xx);
+            if (e) return e;
+            const cplx t = std::sqrt(xx);
+            if (t == cplx(0.0, 0.0)) return 0;
+            if ((e = axpby(cplx(1.0, 0.0) / t, Xin, cplx(0.0, 0.0), col(1), 1))) return e;
+        } else {
+            m_start = m_low - 1;
+        }
+        for (int J = m_start; J <= m_high - 1; ++J) {
+            int num = 0;
+            int e = qmr_cx_run(c, a.conv, a.qmrmax, a.qmrtol, a.ls_ntype, a.ls_px_ntype, col(J), Wv, &num, nullptr);
+            if (e) return e;
+            if (num <= 0) { *ret = num; return 0; }
+            // MGS_ORTH_SX: column J + 1 from Wv
+            for (int I = 1; I <= J; ++I) {
+                cplx d;
+                if ((e = bil(col(I), Wv, &d))) return e;
+                if ((e = axpby(-d, col(I), cplx(1.0, 0.0), Wv, 0))) return e;
+            }
+            cplx nw;
+            if ((e = bil(Wv, Wv, &nw))) return e;
+            const cplx nrm = std::sqrt(nw);
+            if (nrm == cplx(0.0, 0.0)) { *ret = -J; return 0; }
+            if ((e = axpby(cplx(1.0, 0.0) / nrm, Wv, cplx(0.0, 0.0), col(J + 1), 1))) return e;
+        }
+        for (int J = m_low; J <= m_high; ++J) {
+            int e = hx_cx_planar(c, a.h0_ntype, col(J), Wv, s);
+            if (e) return e;
+            for (int I = 1; I <= m_high; ++I)
+                if ((e = bil(col(I), Wv, &H[(size_t)(I - 1) + (size_t)(J - 1) * MM]))) return e;
+        }
+        for (int J = 1; J <= m_low - 1; ++J) {
+            int e = hx_cx_planar(c, a.h0_ntype, col(J), Wv, s);
+            if (e) return e;
+            for (int I = m_low; I <= m_high; ++I)
+                if ((e = bil(col(I), Wv, &H[(size_t)(I - 1) + (size_t)(J - 1) * MM]))) return e;
+        }
+        *ret = m_high;
+        return 0;
+    };
+    int rc = to_planar(c, X0, true, stage, Xin);
+    int status = 0;
+    double res = 0.0;
+    int cnt_low = 1, cnt_high = std::max(std::max(a.startcnt, a.m), a.stepeig + 1);
+    std::vector<cplx> tmp, old;
+    while (!rc && cnt_high <= MM) {
+        int num = 0;
+        if ((rc = pisth0(cnt_low, cnt_high, &num))) break;
+        if (num <= 0) { status = -cnt_high; break; }
+        const int n1 = cnt_high - a.stepeig;
+        int g1 = geev_cx(c, n1, H, MM, tmp);
+        if (g1 < 0) { rc = g1; break; }
+        if (g1 > 0) { status = -n1; break; }
+        window_cx(a.e0, 1, tmp, a.m, old);
+        g1 = geev_cx(c, cnt_high, H, MM, tmp);
+        if (g1 < 0) { rc = g1; break; }
+        if (g1 > 0) { status = -cnt_high; break; }
+        window_cx(a.e0, 1, tmp, a.m, eig);
+        res = 0.0;
+        for (int i = 0; i < a.m; ++i)
+            res = std::max(res, std::fabs(op_cx(6, eig[(size_t)i]) - op_cx(6, old[(size_t)i])));
+        if (res <= a.etol) { status = cnt_high; break; }
+        status = -cnt_high;
+        cnt_low = cnt_high + 1;
+        if (cnt_low >= MM) { status = -MM; break; }
+        cnt_high = std::min(cnt_high + a.stepcnt, MM);
+    }
+    cudaFreeAsync(w, s);
+    cudaFreeAsync(dd, s);
+    cudaStreamSynchronize(s);
+    if (rc) return rc;
+    // Reorder_CX('A', 1, ...): ascending by the real part
+    std::stable_sort(eig.begin(), eig.end(), [](const cplx &x, const cplx &y) { return x.real() < y.real(); });
+    *status_out = status;
+    if (res_out) *res_out = res;
+    return 0;
+}
+
 // ------------------------------------------------------------------- C ABI --
 // Interleaved COMPLEX*16 in (host or device) -> planar device P (2N).
 static int to_planar(scalit_ctx *c, const double *Z, bool host, double *stage, double *P)
@@ -626,6 +874,29 @@ int scalit_crp(scalit_ctx *c, int nenergy, const double *energies, int nm, int q
     if (nenergy == 0) return 0;
     if (!energies || !X0 || !crp) { set_error("energies, X0 and crp are required"); return SCALIT_EINVAL; }
     return crp_run(c, nenergy, energies, nm, qmrmax, qmrtol, conv, sap, X0, crp);
+}
+
+int scalit_pist_cx(scalit_ctx *c, double e0, double etol, int ntype, const double *X0, int startcnt, int stepcnt,
+                   int stepeig, int m, int m_max, int h0_ntype, int ls_ntype, int ls_px_ntype, int conv, int qmrmax,
+                   double qmrtol, double *eig, double *res, int *status)
+{
+    CX_CTX_CHECK(c);
+    if (!c->osb_built) { set_error("complex PIST needs the preconditioner: build or load it first"); return SCALIT_ESTATE; }
+    if (!X0 || !eig || !status) { set_error("X0, eig and status are required"); return SCALIT_EINVAL; }
+    if (ntype > 0) {
+        set_error("PIST_CONV_SX with ntype > 0 has no defined result in the reference (getSepMax_CX call)");
+        return SCALIT_EUNSUP;
+    }
+    if (m < 1 || m_max < 2) { set_error("complex PIST needs m >= 1 and m_max >= 2"); return SCALIT_EINVAL; }
+    PistCxArgs a{e0, etol, startcnt, stepcnt, stepeig, m, m_max, h0_ntype, ls_ntype, ls_px_ntype, conv, qmrmax, qmrtol};
+    std::vector<cplx> ev;
+    const int rc = pist_cx_run(c, a, X0, ev, res, status);
+    if (rc) return rc;
+    for (int i = 0; i < m; ++i) {
+        eig[2 * i] = ev[(size_t)i].real();
+        eig[2 * i + 1] = ev[(size_t)i].imag();
+    }
+    return 0;
 }
 
 }  // extern "C"

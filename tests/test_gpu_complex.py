@@ -133,3 +133,28 @@ def test_crp_matches_oracle_and_dense_trace(lib, orc, case):
     assert dense > 0.0
     assert abs(got - dense) / dense < 1e-5
     assert abs(got - want) / want < 1e-5
+
+
+def test_pist_cx_levels_of_h_minus_i_ap(lib, orc, case):
+    """PIST_CONV_SX through QMR_CX solves (TMAP) returns the complex levels of
+    H - i AP nearest E0: against the dense eigenvalues and the oracle."""
+    p, ref, e0, app, apr = case
+    cx = orc.CxOperator(ref, app, apr)
+    H = hm.dense_hamiltonian(p, shift=0.0)
+    exact = np.linalg.eigvals(H - 1j * np.diag(cx.AP))
+    want = exact[np.argsort(np.abs(exact.real - e0))[:6]]
+    want = want[np.argsort(want.real)]
+    x0 = np.random.default_rng(10).random(p.N) + 0j
+    with context(p, ref, e0, app, apr) as ctx:
+        st, eig, res = ctx.pist_cx(x0, 6, e0, 1e-11, 200, qmrmax=1000, qmrtol=1e-12)
+    assert st > 0
+    np.testing.assert_allclose(eig.real, want.real, atol=1e-8)
+    np.testing.assert_allclose(eig.imag, want.imag, atol=1e-8)
+
+    def linsolv(v):
+        code, x, _ = orc.qmr_cx(lambda u: cx.hx(u, orc.TMAP), lambda u: cx.px(u, 1, orc.TMAP), v, 1000, 1e-12)
+        return code, x
+
+    st_r, eig_r, _ = orc.pist_conv_sx(e0, 1e-11, 0, x0, 0, 5, 1, 6, 200, lambda v: cx.hx(v, orc.TMAP0), linsolv)
+    assert st_r > 0
+    np.testing.assert_allclose(eig, eig_r, atol=1e-8)
