@@ -620,7 +620,7 @@ class CxOperator:
         e0 = E0 if ntype not in (TA0, TAAP0, TMAP0) else 0.0
         return e0, sign, (self._absorb(which) if sign else None)
 
-    def px(self, X, nosb=1, ntype=TA1, de=0.0, beta=0.0):
+    def px(self, X, nosb=1, ntype=TA1, de=0.0, beta=0.0, win=None):
         """MYPX_DX (src/iterate/module/osb.mypxdx.h): V^T of levels sF..1 on the
         real and imaginary parts, the complex kernel, V of levels 1..sF.
         TOSB divides by EIG0 - E0 [+-] i A; TOSBD1 clamps |EIG0 - E0| <= DE to
@@ -655,11 +655,32 @@ class CxOperator:
             alpha = -beta * DE
             inside = np.abs(ade) <= DE
             ade = np.where(inside, alpha + b1 * ade, ade)
-        elif nosb == TOSBW:
-            raise ValueError("the complex window preconditioner is not restated")
+        elif nosb == TOSBW and win is None:
+            raise ValueError("TOSBW needs the window (an OSBW object)")
         den = ade + 1j * sign * A if sign else ade
-        Y = Y / den
+        if nosb == TOSBW:
+            wy = np.linalg.solve(self.window_matrix(win, ntype, e0), Y[win.ind])
+            Y = Y / den
+            Y[win.ind] = wy
+        else:
+            Y = Y / den
         return rot(Y, False)
+
+    def window_matrix(self, win, ntype, e0):
+        """HWRCX of createWH_DXCX (src/iterate/module/osb.pij.h:63-135): the
+        window matrix HW with -E0 (nTypes that use E0) and +-i A(WIND) added
+        on the diagonal; MYPX_DX (osb.mypxdx.h) solves with it by ZGETRF /
+        ZGETRS (ZHETRF / ZHETRS for TA0, TA1).  For TA1 the reference reads the
+        diagonal from HWCX, the complex job's array, which the real job does
+        not fill; this uses HW, the evident intent."""
+        use_e0, sign, which = cx_terms(ntype)
+        A = np.array(win.HW, dtype=np.complex128)
+        d = np.diag_indices_from(A)
+        if ntype not in (TA0, TAAP0, TMAP0):
+            A[d] -= e0
+        if sign:
+            A[d] += 1j * sign * self._absorb(which)[win.ind]
+        return A
 
 
 def qmr_cx(hx, px, B, qmrmax, qmrtol, ntype=0, X0=None):

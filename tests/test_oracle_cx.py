@@ -185,3 +185,20 @@ def test_crp_equals_dense_trace(orc, cxcase):
     got = orc.osb_crp(cx, [E], 13, [x0], 1000, 1e-13)[0]
     assert dense > 0.0
     assert abs(got - dense) / dense < 1e-6
+
+
+@pytest.mark.parametrize("ntype", [1, 0, 2, 100, 201])
+def test_cx_window_px_is_dense(orc, cxcase, ntype):
+    """MYPX_DX with TOSBW: the window block of the kernel is the inverse of
+    HW - E0 +- i A(WIND) (createWH_DXCX), the rest 1/(EIG0 - E0 +- i A)."""
+    p, op, cx, V, H, e0 = cxcase
+    win = orc.OSBW(op, e0, 20, 1e-4)
+    use_e0, sign, which = orc.cx_terms(ntype)
+    A = {"AP": cx.AP, "APP": cx.APP, "APR": cx.APR}.get(which, np.zeros(p.N))
+    shift = 0.0 if ntype in (0, 2, 3) else e0
+    M = np.diag(1.0 / (op.EIG0 - shift + 1j * sign * A))
+    Wm = win.HW - shift * np.eye(20) + 1j * sign * np.diag(A[win.ind])
+    M[np.ix_(win.ind, win.ind)] = np.linalg.inv(Wm)
+    x = np.random.default_rng(11).standard_normal(p.N) + 1j * np.random.default_rng(12).standard_normal(p.N)
+    got = cx.px(x, nosb=orc.TOSBW, ntype=ntype, win=win)
+    assert rel(got, V @ M @ V.T @ x) < 1e-10
