@@ -161,6 +161,176 @@ __global__ void real_mul_kernel(i64 n, double *__restrict__ x, double a)
 
 static int to_planar(scalit_ctx *c, const double *Z, bool host, double *stage, double *P);
 
+// --------------------------------------------------------- complex window --
+__global__ void gather_real_kernel(int m, const int *__restrict__ ind, const double *__restrict__ A,
+                                   double *__restrict__ out)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < m) out[i] = A[ind[i]];
+}
+
+// w = Z(ind) for planar Z (w: m real parts, then m imaginary parts)
+__global__ void cx_window_gather_kernel(int m, const int *__restrict__ ind, const double *__restrict__ Z, i64 n,
+                                        double *__restrict__ w)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < m) {
+        w[i] = Z[ind[i]];
+        w[m + i] = Z[n + ind[i]];
+    }
+}
+
+// Z(ind(i)) = (HWRCX^-1 w)(i): one warp per window row (inv column-major,
+// interleaved complex).
+__global__ void __launch_bounds__(kT)
+cx_window_solve_kernel(int m, const double2 *__restrict__ inv, const double *__restrict__ w,
+                       const int *__restrict__ ind, double *__restrict__ Z, i64 n)
+{
+    const int row = (int)((blockIdx.x * (i64)blockDim.x + threadIdx.x) >> 5);
+    const int lane = threadIdx.x & 31;
+    if (row >= m) return;
+    double ar = 0.0, ai = 0.0;
+    for (int j = lane; j < m; j += 32) {
+        const double2 a = inv[row + (i64)j * m];
+        const double wr = w[j], wi = w[m + j];
+        ar += a.x * wr - a.y * wi;
+        ai += a.x * wi + a.y * wr;
+    }
+    #pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        ar += __shfl_xor_sync(0xffffffffu, ar, o);
+        ai += __shfl_xor_sync(0xffffffffu, ai, o);
+    }
+    if (lane == 0) {
+        Z[ind[row]] = ar;
+        Z[n + ind[row]] = ai;
+    }
+}
+
+// createWH_DXCX (src/iterate/module/osb.pij.h:63-135) for one nType: HW with
+// -E0 (nTypes that use it) and +-i A(WIND) on the diagonal, inverted by
+// cuSOLVER's LU (ZGETRF, then ZGETRS on the identity); kept until the nType,
+// E0 or the window changes.  For TA1 the reference reads the diagonal from
+// HWCX, the complex job's array, which the real job does not fill; HW is used.
+static int cx_window_prepare(scalit_ctx *c, int ntype, double e0)
+{
+    if (c->osbw_cxinv && c->osbw_cx_ntype == ntype && c->osbw_cx_e0 == e0 && c->osbw_cx_serial == c->osbw_serial)
+        return 0;
+    typedef std::complex<double> cplx;
+    const int m = c->osbw_len;
+    cudaStream_t s = c->stream;
+    CxTerms t;
+    int rc = cx_terms(c, ntype, &t);
+    if (rc) return rc;
+    std::vector<double> hw((size_t)m * m), av((size_t)m, 0.0);
+    SC_CUDA(cudaMemcpyAsync(hw.data(), c->osbw_hw, sizeof(double) * hw.size(), cudaMemcpyDeviceToHost, s));
+    double *dav = nullptr;
+    if (t.sign) {
+        SC_CUDA(cudaMallocAsync(&dav, sizeof(double) * (size_t)m, s));
+        gather_real_kernel<<<(m + kT - 1) / kT, kT, 0, s>>>(m, c->osbw_ind, t.A, dav);
+        SC_CHECK_LAUNCH();
+        SC_CUDA(cudaMemcpyAsync(av.data(), dav, sizeof(double) * (size_t)m, cudaMemcpyDeviceToHost, s));
+        cudaFreeAsync(dav, s);
+    }
+    SC_CUDA(cudaStreamSynchronize(s));
+    std::vector<cplx> A((size_t)m * m), B((size_t)m * m, cplx(0.0, 0.0));
+    for (size_t e = 0; e < A.size(); ++e) A[e] = cplx(hw[e], 0.0);
+    for (int i = 0; i < m; ++i) {
+        A[(size_t)i * (m + 1)] += cplx(-e0, (double)t.sign * av[(size_t)i]);
+        B[(size_t)i * (m + 1)] = cplx(1.0, 0.0);
+    }
+    cusolverDnHandle_t sol = (cusolverDnHandle_t)c->cusolver;
+    if (cusolverDnSetStream(sol, s) != CUSOLVER_STATUS_SUCCESS) { set_error("cusolverDnSetStream failed"); return SCALIT_ECUDA; }
+    cuDoubleComplex *dA = nullptr, *dB = nullptr, *work = nullptr;
+    int *ipiv = nullptr, *info = nullptr;
+    auto release = [&]() {
+        if (dA) cudaFreeAsync(dA, s);
+        if (dB) cudaFreeAsync(dB, s);
+        if (work) cudaFreeAsync(work, s);
+        if (ipiv) cudaFreeAsync(ipiv, s);
+        if (info) cudaFreeAsync(info, s);
+    };
+    if (cudaMallocAsync(&dA, sizeof(cplx) * A.size(), s) != cudaSuccess ||
+        cudaMallocAsync(&dB, sizeof(cplx) * B.size(), s) != cudaSuccess ||
+        cudaMallocAsync(&ipiv, sizeof(int) * (size_t)m, s) != cudaSuccess ||
+        cudaMallocAsync(&info, sizeof(int) * 2, s) != cudaSuccess) {
+        cudaGetLastError();
+        release();
+        set_error("complex window factor does not fit");
+        return SCALIT_ENOMEM;
+    }
+    int lw = 0, hinfo[2] = {0, 0};
+    do {
+        if (cudaMemcpyAsync(dA, A.data(), sizeof(cplx) * A.size(), cudaMemcpyHostToDevice, s) != cudaSuccess ||
+            cudaMemcpyAsync(dB, B.data(), sizeof(cplx) * B.size(), cudaMemcpyHostToDevice, s) != cudaSuccess ||
+            cudaMemsetAsync(info, 0, sizeof(int) * 2, s) != cudaSuccess) {
+            set_error("complex window upload failed");
+            rc = SCALIT_ECUDA;
+            break;
+        }
+        if (cusolverDnZgetrf_bufferSize(sol, m, m, dA, m, &lw) != CUSOLVER_STATUS_SUCCESS) {
+            set_error("cusolverDnZgetrf_bufferSize failed");
+            rc = SCALIT_ECUDA;
+            break;
+        }
+        if (cudaMallocAsync(&work, sizeof(cplx) * (size_t)std::max(lw, 1), s) != cudaSuccess) {
+            cudaGetLastError();
+            set_error("complex window workspace does not fit");
+            rc = SCALIT_ENOMEM;
+            break;
+        }
+        if (cusolverDnZgetrf(sol, m, m, dA, m, work, ipiv, info) != CUSOLVER_STATUS_SUCCESS ||
+            cudaMemcpyAsync(hinfo, info, sizeof(int), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+            cudaStreamSynchronize(s) != cudaSuccess) {
+            set_error("cusolverDnZgetrf failed");
+            rc = SCALIT_ECUDA;
+            break;
+        }
+        if (hinfo[0] != 0) {
+            set_error("complex window matrix is singular (ZGETRF info=%d)", hinfo[0]);
+            rc = SCALIT_EINVAL;
+            break;
+        }
+        if (cusolverDnZgetrs(sol, CUBLAS_OP_N, m, m, dA, m, ipiv, dB, m, info + 1) != CUSOLVER_STATUS_SUCCESS ||
+            cudaMemcpyAsync(hinfo + 1, info + 1, sizeof(int), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+            cudaStreamSynchronize(s) != cudaSuccess) {
+            set_error("cusolverDnZgetrs failed");
+            rc = SCALIT_ECUDA;
+            break;
+        }
+        if (hinfo[1] != 0) {
+            set_error("complex window solve failed (ZGETRS info=%d)", hinfo[1]);
+            rc = SCALIT_EINVAL;
+            break;
+        }
+        if (!c->osbw_cxinv || c->osbw_cx_serial != c->osbw_serial) {
+            if (c->osbw_cxinv) cudaFree(c->osbw_cxinv);
+            if (c->osbw_cxw) cudaFree(c->osbw_cxw);
+            c->osbw_cxinv = c->osbw_cxw = nullptr;
+            if (cudaMalloc(&c->osbw_cxinv, sizeof(cplx) * B.size()) != cudaSuccess ||
+                cudaMalloc(&c->osbw_cxw, sizeof(double) * 2 * (size_t)m) != cudaSuccess) {
+                cudaGetLastError();
+                set_error("complex window inverse does not fit");
+                rc = SCALIT_ENOMEM;
+                break;
+            }
+        }
+        if (cudaMemcpyAsync(c->osbw_cxinv, dB, sizeof(cplx) * B.size(), cudaMemcpyDeviceToDevice, s) != cudaSuccess ||
+            cudaStreamSynchronize(s) != cudaSuccess) {
+            set_error("complex window inverse copy failed");
+            rc = SCALIT_ECUDA;
+            break;
+        }
+        c->osbw_cx_ntype = ntype;
+        c->osbw_cx_e0 = e0;
+        c->osbw_cx_serial = c->osbw_serial;
+    } while (0);
+    release();
+    cudaStreamSynchronize(s);
+    if (rc) c->osbw_cx_serial = -1;
+    return rc;
+}
+
 // -------------------------------------------------------- planar operators --
 // MYHX_DX on a planar complex vector.
 static int hx_cx_planar(const scalit_ctx *c, int ntype, const double *X, double *Y, cudaStream_t s)
@@ -185,13 +355,18 @@ static int px_cx_planar(const scalit_ctx *c, int ntype, const double *X, double 
     const Layout &L = c->L;
     const i64 N = L.N;
     if (!c->osb_built) { set_error("P*X before the preconditioner was built or loaded"); return SCALIT_ESTATE; }
-    if (c->osb_kind == SCALIT_TOSBW) {
-        set_error("the complex window preconditioner (ZHETRF/ZGETRF of createWH_DXCX) is not supported");
-        return SCALIT_EUNSUP;
-    }
     CxTerms t;
     int rc = cx_terms(c, ntype, &t);
     if (rc) return rc;
+    const bool window = c->osb_kind == SCALIT_TOSBW;
+    if (window) {
+        if (!(c->osbw_len > 0 && c->osbw_valid)) {
+            set_error("TOSBW P*X without a window for the current preconditioner: call scalit_build_osbw again");
+            return SCALIT_ESTATE;
+        }
+        rc = cx_window_prepare(const_cast<scalit_ctx *>(c), ntype, cx_kernel_e0(c, ntype));
+        if (rc) return rc;
+    }
     const int S = 2 * L.nlev;
     for (int q = 0; q < 2; ++q) {
         double *buf[2] = {Y + q * N, tmp + q * N};
@@ -206,9 +381,19 @@ static int px_cx_planar(const scalit_ctx *c, int ntype, const double *X, double 
         }
     }
     double *Z = (L.nlev % 2 == 0) ? Y : tmp;   // where both halves' V^T stages ended
+    const int m = c->osbw_len;
+    if (window) {
+        cx_window_gather_kernel<<<(m + kT - 1) / kT, kT, 0, s>>>(m, c->osbw_ind, Z, N, c->osbw_cxw);
+        SC_CHECK_LAUNCH();
+    }
     cx_kernel_step<<<cgrid(N), kT, 0, s>>>(N, Z, c->EIG0, t.sign ? t.A : nullptr, cx_kernel_e0(c, ntype),
                                            (double)t.sign, c->osb_kind, c->osb_de, c->osb_beta);
     SC_CHECK_LAUNCH();
+    if (window) {
+        cx_window_solve_kernel<<<(int)(((i64)m * 32 + kT - 1) / kT), kT, 0, s>>>(
+            m, reinterpret_cast<const double2 *>(c->osbw_cxinv), c->osbw_cxw, c->osbw_ind, Z, N);
+        SC_CHECK_LAUNCH();
+    }
     for (int q = 0; q < 2; ++q) {
         double *buf[2] = {Y + q * N, tmp + q * N};
         const double *in = Z + q * N;

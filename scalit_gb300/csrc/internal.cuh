@@ -85,6 +85,13 @@ struct scalit_ctx {
     float *osbw_invf = nullptr;
     void *osbw_wy = nullptr;
     double osbw_e0 = 0.0, osbw_de = 0.0;
+    long long osbw_serial = 0;            // counts the windows made
+    // the complex window matrix's inverse for one nType and E0 (interleaved
+    // complex, hwlen x hwlen) and room for one P*X's gathered complex entries
+    double *osbw_cxinv = nullptr, *osbw_cxw = nullptr;
+    int osbw_cx_ntype = -1;
+    double osbw_cx_e0 = 0.0;
+    long long osbw_cx_serial = -1;
     // absorbing potentials of the complex forms: APP, APR and AP = APP + APR
     double *APP = nullptr, *APR = nullptr, *AP = nullptr;
     // workspace (grown on demand)

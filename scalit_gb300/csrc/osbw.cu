@@ -222,6 +222,10 @@ void osbw_free(scalit_ctx *c)
     if (c->osbw_inv) cudaFree(c->osbw_inv);
     if (c->osbw_invf) cudaFree(c->osbw_invf);
     if (c->osbw_wy) cudaFree(c->osbw_wy);
+    if (c->osbw_cxinv) cudaFree(c->osbw_cxinv);
+    if (c->osbw_cxw) cudaFree(c->osbw_cxw);
+    c->osbw_cxinv = c->osbw_cxw = nullptr;
+    c->osbw_cx_serial = -1;
     c->osbw_ind = nullptr;
     c->osbw_hw = c->osbw_inv = nullptr;
     c->osbw_invf = nullptr;
@@ -441,6 +445,7 @@ int osbw_make(scalit_ctx *c, double e0, int count, double *de, int npc, const do
     SC_CUDA(cudaStreamSynchronize(s));
     c->osbw_len = m;
     c->osbw_valid = true;
+    c->osbw_serial++;
     c->osbw_e0 = e0;
     c->osbw_de = d;
     c->osb_kind = SCALIT_TOSBW;

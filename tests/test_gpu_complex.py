@@ -158,3 +158,20 @@ def test_pist_cx_levels_of_h_minus_i_ap(lib, orc, case):
     st_r, eig_r, _ = orc.pist_conv_sx(e0, 1e-11, 0, x0, 0, 5, 1, 6, 200, lambda v: cx.hx(v, orc.TMAP0), linsolv)
     assert st_r > 0
     np.testing.assert_allclose(eig, eig_r, atol=1e-8)
+
+
+@pytest.mark.parametrize("ntype", [1, 0, 2, 100, 201])
+def test_px_cx_window_matches_oracle(lib, orc, case, ntype):
+    """MYPX_DX with TOSBW: the window's complex matrix (createWH_DXCX) inverted
+    by LU on the device against the oracle's solve."""
+    p, ref, e0, app, apr = case
+    cx = orc.CxOperator(ref, app, apr)
+    win = orc.OSBW(ref, e0, 30, 1e-4)
+    x = cvec(np.random.default_rng(13), p.N)
+    with context(p, ref, e0, app, apr) as ctx:
+        ctx.build_osbw(e0, 30, 1e-4)
+        z = ctx.px_cx(x, ntype)
+        z2 = ctx.px_cx(x, ntype)                 # the cached inverse
+    want = cx.px(x, nosb=orc.TOSBW, ntype=ntype, win=win)
+    assert rel(z, want) < 1e-9
+    np.testing.assert_array_equal(z2, z)
