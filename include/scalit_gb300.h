@@ -237,8 +237,10 @@ int scalit_hx_cx_device(scalit_ctx *ctx, int ntype, int nvec, const double *dX, 
 /* MYPX_DX (src/iterate/module/osb.mypxdx.h): V^T of every level, the kernel
  * 1/(EIG0 - E0 + sign i A) (E0 = 0 for TA0, TAAP0, TMAP0; TOSBD1 clamps
  * |EIG0 - E0| <= DE to +-DE; TOSBD2 uses alpha + (1 + beta)(EIG0 - E0) on both
- * sides of E0, as the complex reference does), V of every level.  The complex
- * window preconditioner (TOSBW) returns SCALIT_EUNSUP. */
+ * sides of E0, as the complex reference does), V of every level.  With TOSBW
+ * the window's entries take the inverse of HW - E0 +- i A(WIND)
+ * (createWH_DXCX, osb.pij.h:63-135; LU on the device, kept per nType and
+ * E0), the others the kernel above. */
 int scalit_px_cx(scalit_ctx *ctx, int ntype, int nvec, const double *X, double *Y);
 int scalit_px_cx_device(scalit_ctx *ctx, int ntype, int nvec, const double *dX, double *dY);
 /* QMR_CX (src/iterate/libiterate/qmr/qmrcx.f90:4-175): QMR for the complex
