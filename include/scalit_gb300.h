@@ -476,6 +476,18 @@ typedef void (*scalit_fortran_op)(const int *n, const double *x, double *y);
 typedef int (*scalit_fortran_linsolv)(const int *n, const double *b, double *x, double *res);
 int qmr_(const int *ntype, const int *qmrmax, const double *qmrtol, const int *n,
          const double *B, scalit_fortran_op hx, scalit_fortran_op px, double *X, double *RES);
+/* QMR_CX (src/iterate/libiterate/qmr/qmrcx.f90:4-175) and PIST_CONV_SX
+ * (src/iterate/libiterate/pist/pist_sx.f90:4-96), the complex library's
+ * externals: B, X, EIG are COMPLEX*16 arrays (interleaved) and the callbacks
+ * receive them as such; the recurrences run on the GPU.  QMR_CX returns its
+ * code (-10 when the library fails, with a message on stderr); PIST_CONV_SX
+ * its status (0 for bad parameters and for ntype > 0, whose result the
+ * reference leaves undefined). */
+int qmr_cx_(const int *ntype, const int *qmrmax, const double *qmrtol, const int *n, const double *B,
+            scalit_fortran_op hx, scalit_fortran_op px, double *X, double *RES);
+int pist_conv_sx_(const double *e0, const double *etol, const int *ntype, const int *n, const double *X,
+                  const int *startcnt, const int *stepcnt, const int *stepeig, const int *m, const int *m_max,
+                  scalit_fortran_op h0x, scalit_fortran_linsolv linsolv, double *EIG, double *RES);
 int qmr_mpi_(const int *ntype, const int *qmrmax, const double *qmrtol, const int *n,
              const double *B, scalit_fortran_op hx, scalit_fortran_op px, double *X,
              double *RES, const int *myid);

@@ -105,6 +105,8 @@ SIGNATURES = {
     "mgs_orth_": (C.c_int, [_ip, _dp, _ip, _dp]),
     "mgs_orth_mpi_": (C.c_int, [_ip, _dp, _ip, _dp, _ip]),
     "qmr_": (C.c_int, [_ip, _ip, _dp, _ip, _dp, _vp, _vp, _dp, _dp]),
+    "qmr_cx_": (C.c_int, [_ip, _ip, _dp, _ip, _dp, _vp, _vp, _dp, _dp]),
+    "pist_conv_sx_": (C.c_int, [_dp, _dp, _ip, _ip, _dp, _ip, _ip, _ip, _ip, _ip, _vp, _vp, _dp, _dp]),
     "qmr_mpi_": (C.c_int, [_ip, _ip, _dp, _ip, _dp, _vp, _vp, _dp, _dp, _ip]),
     "pist_conv_": (C.c_int, [_dp, _dp, _ip, _ip, _dp, _ip, _ip, _ip, _ip, _ip, _vp, _vp, _dp, _dp]),
     "pist_conv_mpi_": (C.c_int, [_ip, _ip, _dp, _dp, _ip, _ip, _dp, _ip, _ip, _ip, _ip, _ip, _vp, _vp,

@@ -1210,6 +1210,45 @@ int qmr_mpi_(const int *ntype, const int *qmrmax, const double *qmrtol, const in
     return qmr_fortran(*ntype, *qmrmax, *qmrtol, *n, B, hx, px, X, RES, true);
 }
 
+// QMR_CX (src/iterate/libiterate/qmr/qmrcx.f90:4-175) and PIST_CONV_SX
+// (src/iterate/libiterate/pist/pist_sx.f90:4-96), the complex library's
+// externals, with the caller's callbacks on COMPLEX*16 arrays.
+int qmr_cx_(const int *ntype, const int *qmrmax, const double *qmrtol, const int *n, const double *B,
+            scalit_fortran_op hx, scalit_fortran_op px, double *X, double *RES)
+{
+    std::lock_guard<std::mutex> lk(g_fmu);
+    *RES = 0.0;
+    scalit_ctx *c = scratch();
+    if (!c) return -10;
+    int code = 0;
+    double res = 0.0;
+    const int rc = qmr_cx_host(c, *n, hx, px, *ntype, *qmrmax, *qmrtol, B, X, &code, &res);
+    if (rc) { report("qmr_cx", rc); return -10; }
+    *RES = res;
+    return code;
+}
+
+int pist_conv_sx_(const double *e0, const double *etol, const int *ntype, const int *n, const double *X,
+                  const int *startcnt, const int *stepcnt, const int *stepeig, const int *m, const int *m_max,
+                  scalit_fortran_op h0x, scalit_fortran_linsolv linsolv, double *EIG, double *RES)
+{
+    std::lock_guard<std::mutex> lk(g_fmu);
+    *RES = 0.0;
+    if (*ntype > 0) {
+        fprintf(stderr, "scalit_gb300: pist_conv_sx with ntype > 0 has no defined result in the reference\n");
+        return 0;
+    }
+    scalit_ctx *c = scratch();
+    if (!c) return 0;
+    int status = 0;
+    double res = 0.0;
+    const int rc = pist_sx_host(c, *n, *e0, *etol, X, *startcnt, *stepcnt, *stepeig, *m, *m_max, h0x, linsolv, EIG,
+                                &res, &status);
+    if (rc) { report("pist_conv_sx", rc); return rc; }
+    *RES = res;
+    return status;
+}
+
 int pist_conv_(const double *e0, const double *etol, const int *ntype, const int *n, const double *X,
                const int *startcnt, const int *stepcnt, const int *stepeig, const int *m, const int *m_max,
                scalit_fortran_op h0x, scalit_fortran_linsolv linsolv, double *EIG, double *RES)

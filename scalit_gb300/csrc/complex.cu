@@ -17,6 +17,7 @@
 #include <cmath>
 #include <complex>
 #include <cstring>
+#include <functional>
 #include <vector>
 
 namespace sc {
@@ -159,6 +160,7 @@ __global__ void real_mul_kernel(i64 n, double *__restrict__ x, double a)
     for (i64 p = blockIdx.x * (i64)blockDim.x + threadIdx.x; p < n; p += (i64)gridDim.x * blockDim.x) x[p] = a * x[p];
 }
 
+static int to_planar_n(scalit_ctx *c, i64 N, const double *Z, bool host, double *stage, double *P);
 static int to_planar(scalit_ctx *c, const double *Z, bool host, double *stage, double *P);
 
 // --------------------------------------------------------- complex window --
@@ -415,11 +417,14 @@ static int px_cx_planar(const scalit_ctx *c, int ntype, const double *X, double 
 // Bilinear products X^T Y (DOT_CX, vector_cx.f90:227-234) and the norms of
 // the conjugated dot_product are deterministic FP64 device reductions read
 // back per use; the scalar recurrence runs on the host as in the reference.
-static int qmr_cx_run(scalit_ctx *c, int conv, int qmrmax, double tol, int ntype, int px_ntype, const double *B,
-                      double *X, int *code_out, double *res_out)
+// An operator on planar device vectors: out = Op(in), scratch: 2N doubles.
+typedef std::function<int(const double *in, double *out, double *scratch)> CxOp;
+
+static int qmr_cx_core(scalit_ctx *c, i64 N, const CxOp &hxop, const CxOp &pxop, int conv, int qmrmax, double tol,
+                       const double *B, double *X, int *code_out, double *res_out)
 {
     typedef std::complex<double> cplx;
-    const i64 N = c->L.N, N2 = 2 * N;
+    const i64 N2 = 2 * N;
     cudaStream_t s = c->stream;
     double *w = nullptr, *dd = nullptr;
     const bool full_res = std::abs(conv) == 1;
@@ -483,7 +488,7 @@ static int qmr_cx_run(scalit_ctx *c, int conv, int qmrmax, double tol, int ntype
         }
         if ((rc = nrm(B, &bnrm))) break;
         vnrm = bnrm;
-        if ((rc = px_cx_planar(c, px_ntype, B, Z, T, s))) break;
+        if ((rc = pxop(B, Z, T))) break;
         if ((rc = nrm(Z, &znrm))) break;
         code = 0;
         for (int i = 1; i <= qmrmax; ++i) {
@@ -496,7 +501,7 @@ static int qmr_cx_run(scalit_ctx *c, int conv, int qmrmax, double tol, int ntype
             if (i == 1) rc = axpby(cplx(1.0, 0.0), Z, cplx(0.0, 0.0), Q, 1);
             else rc = axpby(cplx(1.0, 0.0), Z, -(vnrm * vzdot) / qsdot, Q, 0);
             if (rc) break;
-            if ((rc = hx_cx_planar(c, ntype, Q, Sv, s))) break;
+            if ((rc = hxop(Q, Sv, T))) break;
             real_mul_kernel<<<g2, kT, 0, s>>>(N2, Sv, zvrat);
             if (cudaGetLastError() != cudaSuccess) { set_error("QMR_CX scale launch failed"); rc = SCALIT_ECUDA; break; }
             if ((rc = bil(Q, Sv, &qsdot))) break;
@@ -505,7 +510,7 @@ static int qmr_cx_run(scalit_ctx *c, int conv, int qmrmax, double tol, int ntype
             if ((rc = axpby(cplx(1.0, 0.0), Sv, -beta, V, 0))) break;
             double vnrmpo;
             if ((rc = nrm(V, &vnrmpo))) break;
-            if ((rc = px_cx_planar(c, px_ntype, V, Z, T, s))) break;
+            if ((rc = pxop(V, Z, T))) break;
             if ((rc = rdiv(Z, zvrat))) break;
             if ((rc = nrm(Z, &znrm))) break;
             const double theta = vnrmpo / (gamamo * std::abs(beta));
@@ -524,7 +529,7 @@ static int qmr_cx_run(scalit_ctx *c, int conv, int qmrmax, double tol, int ntype
             if ((rc = axpby(cplx(-1.0, 0.0), UR, cplx(1.0, 0.0), R, 0))) break;
             if (full_res) {
                 double xnrm, r1;
-                if ((rc = hx_cx_planar(c, ntype, X, HX0, s))) break;
+                if ((rc = hxop(X, HX0, T))) break;
                 if ((rc = nrm(HX0, &xnrm))) break;
                 if ((rc = axpby(cplx(-1.0, 0.0), B, cplx(1.0, 0.0), HX0, 0))) break;
                 if ((rc = nrm(HX0, &r1))) break;
@@ -553,6 +558,18 @@ static int qmr_cx_run(scalit_ctx *c, int conv, int qmrmax, double tol, int ntype
     *code_out = code;
     if (res_out) *res_out = res;
     return 0;
+}
+
+// QMR_CX on the context's own operators: H = MYHX_DX(ntype), P = MYPX_DX(sOSB, px_ntype).
+static int qmr_cx_run(scalit_ctx *c, int conv, int qmrmax, double tol, int ntype, int px_ntype, const double *B,
+                      double *X, int *code_out, double *res_out)
+{
+    cudaStream_t s = c->stream;
+    CxOp hxop = [c, ntype, s](const double *in, double *out, double *) { return hx_cx_planar(c, ntype, in, out, s); };
+    CxOp pxop = [c, px_ntype, s](const double *in, double *out, double *t) {
+        return px_cx_planar(c, px_ntype, in, out, t, s);
+    };
+    return qmr_cx_core(c, c->L.N, hxop, pxop, conv, qmrmax, tol, B, X, code_out, res_out);
 }
 
 // ---------------------------------------------------------------------- CRP --
@@ -789,10 +806,13 @@ struct PistCxArgs {
     double qmrtol;
 };
 
-static int pist_cx_run(scalit_ctx *c, const PistCxArgs &a, const double *X0, std::vector<cplx> &eig, double *res_out,
-                       int *status_out)
+// The linear solver of PIST: out = solve(in), *num its iteration code (<= 0 failed).
+typedef std::function<int(const double *in, double *out, int *num)> CxSolve;
+
+static int pist_cx_core(scalit_ctx *c, i64 N, const PistCxArgs &a, const double *X0, const CxOp &h0op,
+                        const CxSolve &lin, std::vector<cplx> &eig, double *res_out, int *status_out)
 {
-    const i64 N = c->L.N, N2 = 2 * N;
+    const i64 N2 = 2 * N;
     cudaStream_t s = c->stream;
     const int MM = a.m_max;
     *status_out = 0;
@@ -849,7 +869,7 @@ static int pist_cx_run(scalit_ctx *c, const PistCxArgs &a, const double *X0, std
         }
         for (int J = m_start; J <= m_high - 1; ++J) {
             int num = 0;
-            int e = qmr_cx_run(c, a.conv, a.qmrmax, a.qmrtol, a.ls_ntype, a.ls_px_ntype, col(J), Wv, &num, nullptr);
+            int e = lin(col(J), Wv, &num);
             if (e) return e;
             if (num <= 0) { *ret = num; return 0; }
             // MGS_ORTH_SX: column J + 1 from Wv
@@ -865,13 +885,13 @@ static int pist_cx_run(scalit_ctx *c, const PistCxArgs &a, const double *X0, std
             if ((e = axpby(cplx(1.0, 0.0) / nrm, Wv, cplx(0.0, 0.0), col(J + 1), 1))) return e;
         }
         for (int J = m_low; J <= m_high; ++J) {
-            int e = hx_cx_planar(c, a.h0_ntype, col(J), Wv, s);
+            int e = h0op(col(J), Wv, nullptr);
             if (e) return e;
             for (int I = 1; I <= m_high; ++I)
                 if ((e = bil(col(I), Wv, &H[(size_t)(I - 1) + (size_t)(J - 1) * MM]))) return e;
         }
         for (int J = 1; J <= m_low - 1; ++J) {
-            int e = hx_cx_planar(c, a.h0_ntype, col(J), Wv, s);
+            int e = h0op(col(J), Wv, nullptr);
             if (e) return e;
             for (int I = m_low; I <= m_high; ++I)
                 if ((e = bil(col(I), Wv, &H[(size_t)(I - 1) + (size_t)(J - 1) * MM]))) return e;
@@ -879,7 +899,7 @@ static int pist_cx_run(scalit_ctx *c, const PistCxArgs &a, const double *X0, std
         *ret = m_high;
         return 0;
     };
-    int rc = to_planar(c, X0, true, stage, Xin);
+    int rc = to_planar_n(c, N, X0, true, stage, Xin);
     int status = 0;
     double res = 0.0;
     int cnt_low = 1, cnt_high = std::max(std::max(a.startcnt, a.m), a.stepeig + 1);
@@ -917,11 +937,22 @@ static int pist_cx_run(scalit_ctx *c, const PistCxArgs &a, const double *X0, std
     return 0;
 }
 
+// PIST_CONV_SX on the context's own operators.
+static int pist_cx_run(scalit_ctx *c, const PistCxArgs &a, const double *X0, std::vector<cplx> &eig, double *res_out,
+                       int *status_out)
+{
+    cudaStream_t s = c->stream;
+    CxOp h0op = [c, &a, s](const double *in, double *out, double *) { return hx_cx_planar(c, a.h0_ntype, in, out, s); };
+    CxSolve lin = [c, &a](const double *in, double *out, int *num) {
+        return qmr_cx_run(c, a.conv, a.qmrmax, a.qmrtol, a.ls_ntype, a.ls_px_ntype, in, out, num, nullptr);
+    };
+    return pist_cx_core(c, c->L.N, a, X0, h0op, lin, eig, res_out, status_out);
+}
+
 // ------------------------------------------------------------------- C ABI --
 // Interleaved COMPLEX*16 in (host or device) -> planar device P (2N).
-static int to_planar(scalit_ctx *c, const double *Z, bool host, double *stage, double *P)
+static int to_planar_n(scalit_ctx *c, i64 N, const double *Z, bool host, double *stage, double *P)
 {
-    const i64 N = c->L.N;
     const double *src = Z;
     if (host) {
         SC_CUDA(cudaMemcpyAsync(stage, Z, sizeof(double) * 2 * (size_t)N, cudaMemcpyHostToDevice, c->stream));
@@ -932,14 +963,105 @@ static int to_planar(scalit_ctx *c, const double *Z, bool host, double *stage, d
     return 0;
 }
 
-static int from_planar(scalit_ctx *c, const double *P, bool host, double *stage, double *Z)
+static int to_planar(scalit_ctx *c, const double *Z, bool host, double *stage, double *P)
 {
-    const i64 N = c->L.N;
+    return to_planar_n(c, c->L.N, Z, host, stage, P);
+}
+
+static int from_planar_n(scalit_ctx *c, i64 N, const double *P, bool host, double *stage, double *Z)
+{
     double *dst = host ? stage : Z;
     cx_join_kernel<<<cgrid(N), kT, 0, c->stream>>>(N, P, P + N, dst);
     SC_CHECK_LAUNCH();
     if (host) SC_CUDA(cudaMemcpyAsync(Z, stage, sizeof(double) * 2 * (size_t)N, cudaMemcpyDeviceToHost, c->stream));
     return 0;
+}
+
+static int from_planar(scalit_ctx *c, const double *P, bool host, double *stage, double *Z)
+{
+    return from_planar_n(c, c->L.N, P, host, stage, Z);
+}
+
+// ------------------------------------------------- caller callbacks (Fortran) --
+// An operator given as a caller's host callback on interleaved COMPLEX*16
+// arrays: planar device in -> host -> callback -> device planar out.
+struct HostCx {
+    scalit_ctx *c;
+    i64 N;
+    double *stage;                       // device, 2N
+    std::vector<double> hin, hout;
+    int to_host(const double *P)
+    {
+        int rc = from_planar_n(c, N, P, false, nullptr, stage);
+        if (rc) return rc;
+        SC_CUDA(cudaMemcpyAsync(hin.data(), stage, sizeof(double) * 2 * (size_t)N, cudaMemcpyDeviceToHost, c->stream));
+        SC_CUDA(cudaStreamSynchronize(c->stream));
+        return 0;
+    }
+    int from_host(double *P) { return to_planar_n(c, N, hout.data(), true, stage, P); }
+};
+
+int qmr_cx_host(scalit_ctx *c, i64 n, scalit_fortran_op hx, scalit_fortran_op px, int conv, int qmrmax, double tol,
+                const double *B, double *X, int *code, double *res)
+{
+    const i64 N2 = 2 * n;
+    double *w = nullptr;
+    SC_CUDA(cudaMallocAsync(&w, sizeof(double) * (size_t)N2 * 3, c->stream));
+    HostCx h{c, n, w, std::vector<double>((size_t)N2), std::vector<double>((size_t)N2)};
+    double *Bp = w + N2, *Xp = w + 2 * N2;
+    const int nn = (int)n;
+    auto wrap = [&](scalit_fortran_op f) {
+        return CxOp([&h, f, nn](const double *in, double *out, double *) -> int {
+            int rc = h.to_host(in);
+            if (rc) return rc;
+            f(&nn, h.hin.data(), h.hout.data());
+            return h.from_host(out);
+        });
+    };
+    int rc = to_planar_n(c, n, B, true, w, Bp);
+    if (!rc && conv > 0) rc = to_planar_n(c, n, X, true, w, Xp);
+    if (!rc) rc = qmr_cx_core(c, n, wrap(hx), wrap(px), conv, qmrmax, tol, Bp, Xp, code, res);
+    if (!rc) rc = from_planar_n(c, n, Xp, true, w, X);
+    cudaStreamSynchronize(c->stream);
+    cudaFreeAsync(w, c->stream);
+    cudaStreamSynchronize(c->stream);
+    return rc;
+}
+
+int pist_sx_host(scalit_ctx *c, i64 n, double e0, double etol, const double *X0, int startcnt, int stepcnt,
+                 int stepeig, int m, int m_max, scalit_fortran_op h0x, scalit_fortran_linsolv linsolv, double *eig,
+                 double *res, int *status)
+{
+    const i64 N2 = 2 * n;
+    double *w = nullptr;
+    SC_CUDA(cudaMallocAsync(&w, sizeof(double) * (size_t)N2, c->stream));
+    HostCx h{c, n, w, std::vector<double>((size_t)N2), std::vector<double>((size_t)N2)};
+    const int nn = (int)n;
+    CxOp h0op = [&h, h0x, nn](const double *in, double *out, double *) -> int {
+        int rc = h.to_host(in);
+        if (rc) return rc;
+        h0x(&nn, h.hin.data(), h.hout.data());
+        return h.from_host(out);
+    };
+    CxSolve lin = [&h, linsolv, nn](const double *in, double *out, int *num) -> int {
+        int rc = h.to_host(in);
+        if (rc) return rc;
+        double r = 0.0;
+        *num = linsolv(&nn, h.hin.data(), h.hout.data(), &r);
+        return h.from_host(out);
+    };
+    PistCxArgs a{e0, etol, startcnt, stepcnt, stepeig, m, m_max, 0, 0, 0, 0, 0, 0.0};
+    std::vector<cplx> ev;
+    int rc = pist_cx_core(c, n, a, X0, h0op, lin, ev, res, status);
+    if (!rc) {
+        for (int i = 0; i < m; ++i) {
+            eig[2 * i] = ev[(size_t)i].real();
+            eig[2 * i + 1] = ev[(size_t)i].imag();
+        }
+    }
+    cudaFreeAsync(w, c->stream);
+    cudaStreamSynchronize(c->stream);
+    return rc;
 }
 
 static int cx_apply(scalit_ctx *c, int which, int ntype, int nvec, const double *X, double *Y, bool host)

@@ -239,6 +239,15 @@ void osbw_invalidate(scalit_ctx *c);
 template <class T>
 int osbw_window_apply(const scalit_ctx *c, T *Z, const T *EIG, double e0, T alpha, const int *gate, cudaStream_t s);
 
+// ------------------------------------------------- complex forms (Fortran) --
+// QMR_CX / PIST_CONV_SX with a caller's callbacks on interleaved COMPLEX*16
+// host arrays (the recurrence on the device of context c, n complex points).
+int qmr_cx_host(scalit_ctx *c, i64 n, scalit_fortran_op hx, scalit_fortran_op px, int conv, int qmrmax, double tol,
+                const double *B, double *X, int *code, double *res);
+int pist_sx_host(scalit_ctx *c, i64 n, double e0, double etol, const double *X0, int startcnt, int stepcnt,
+                 int stepeig, int m, int m_max, scalit_fortran_op h0x, scalit_fortran_linsolv linsolv, double *eig,
+                 double *res, int *status);
+
 // ------------------------------------------------------------- OSB build --
 int osb_build(scalit_ctx *c, int bjmax, double bjtol, double *stats);
 // HosbDiag on a device HOSB(ndk, mak, mak, blk): fills VOSB and EIGVAL.

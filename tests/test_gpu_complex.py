@@ -175,3 +175,63 @@ def test_px_cx_window_matches_oracle(lib, orc, case, ntype):
     want = cx.px(x, nosb=orc.TOSBW, ntype=ntype, win=win)
     assert rel(z, want) < 1e-9
     np.testing.assert_array_equal(z2, z)
+
+
+def test_fortran_externals_with_callbacks(lib, orc):
+    """qmr_cx_ and pist_conv_sx_ with caller callbacks on COMPLEX*16 arrays
+    (a dense complex symmetric matrix, the reference drivers' pattern)."""
+    import ctypes as C
+    FOP = C.CFUNCTYPE(None, C.POINTER(C.c_int), C.POINTER(C.c_double), C.POINTER(C.c_double))
+    FLIN = C.CFUNCTYPE(C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_double), C.POINTER(C.c_double),
+                       C.POINTER(C.c_double))
+    I, D, ref = C.c_int, C.c_double, C.byref
+
+    def dp(a):
+        return a.ctypes.data_as(C.POINTER(C.c_double))
+
+    def cview(ptr, k):
+        return np.ctypeslib.as_array(ptr, shape=(2 * k,)).view(np.complex128)
+
+    rng = np.random.default_rng(14)
+    n = 40
+    a = rng.standard_normal((n, n))
+    M = (a + a.T) / 2 + np.diag(np.linspace(1.0, 6.0, n)) - 1j * np.diag(rng.uniform(0.01, 0.1, n))
+    d = np.diag(M).copy()
+
+    @FOP
+    def hmult(pn, px, py):
+        k = pn[0]
+        cview(py, k)[:] = M @ cview(px, k)
+
+    @FOP
+    def pmult(pn, px, py):
+        k = pn[0]
+        cview(py, k)[:] = cview(px, k) / d
+
+    x0 = np.arange(1, n + 1).astype(np.complex128)
+    b = M @ x0
+    x = np.zeros(n, np.complex128)
+    res = D(0.0)
+    code = lib.qmr_cx_(ref(I(0)), ref(I(1000)), ref(D(1e-12)), ref(I(n)), dp(b.view(np.float64)),
+                       C.cast(hmult, C.c_void_p), C.cast(pmult, C.c_void_p), dp(x.view(np.float64)), ref(res))
+    code_r, x_r, _ = orc.qmr_cx(lambda v: M @ v, lambda v: v / d, b, 1000, 1e-12)
+    assert code > 0 and abs(code - code_r) <= 1
+    assert np.abs(x - x0).max() / n < 1e-9
+
+    E0 = 3.0
+    inv = np.linalg.inv(M - E0 * np.eye(n))
+
+    @FLIN
+    def linsolv(pn, pb, px, pres):
+        k = pn[0]
+        cview(px, k)[:] = inv @ cview(pb, k)
+        return 1
+
+    xs = rng.random(n) + 0j
+    eig = np.zeros(5, np.complex128)
+    st = lib.pist_conv_sx_(ref(D(E0)), ref(D(1e-12)), ref(I(0)), ref(I(n)), dp(xs.view(np.float64)), ref(I(0)),
+                           ref(I(5)), ref(I(1)), ref(I(5)), ref(I(n)), C.cast(hmult, C.c_void_p),
+                           C.cast(linsolv, C.c_void_p), dp(eig.view(np.float64)), ref(res))
+    st_r, eig_r, _ = orc.pist_conv_sx(E0, 1e-12, 0, xs, 0, 5, 1, 5, n, lambda v: M @ v, lambda v: (1, inv @ v))
+    assert st > 0 and st_r > 0
+    np.testing.assert_allclose(eig, eig_r, atol=1e-9)
