@@ -738,7 +738,7 @@ static int geev_cx(scalit_ctx *c, int n, const std::vector<cplx> &H, int ld, std
         for (int i = 0; i < n; ++i) A[(size_t)i + (size_t)j * n] = H[(size_t)i + (size_t)j * ld];
     cusolverDnParams_t prm = nullptr;
     if (cusolverDnCreateParams(&prm) != CUSOLVER_STATUS_SUCCESS) { set_error("cusolverDnCreateParams failed"); return SCALIT_ECUDA; }
-    void *dA = nullptr, *dW = nullptr, *dbuf = nullptr;
+    void *dA = nullptr, *dW = nullptr, *dbuf = nullptr, *dV = nullptr;   // dV: unreferenced VL / VR
     int *dinfo = nullptr;
     std::vector<unsigned char> hbuf;
     int rc = 0;
@@ -746,7 +746,8 @@ static int geev_cx(scalit_ctx *c, int n, const std::vector<cplx> &H, int ld, std
     do {
         if (cudaMallocAsync(&dA, sizeof(cplx) * A.size(), s) != cudaSuccess ||
             cudaMallocAsync(&dW, sizeof(cplx) * (size_t)n, s) != cudaSuccess ||
-            cudaMallocAsync(&dinfo, sizeof(int), s) != cudaSuccess) {
+            cudaMallocAsync(&dinfo, sizeof(int), s) != cudaSuccess ||
+            cudaMallocAsync(&dV, sizeof(cplx) * 2, s) != cudaSuccess) {
             cudaGetLastError();
             set_error("eigensolver buffers do not fit");
             rc = SCALIT_ENOMEM;
@@ -758,7 +759,7 @@ static int geev_cx(scalit_ctx *c, int n, const std::vector<cplx> &H, int ld, std
             break;
         }
         if (cusolverDnXgeev_bufferSize(sol, prm, CUSOLVER_EIG_MODE_NOVECTOR, CUSOLVER_EIG_MODE_NOVECTOR, n, CUDA_C_64F,
-                                       dA, n, CUDA_C_64F, dW, CUDA_C_64F, nullptr, 1, CUDA_C_64F, nullptr, 1,
+                                       dA, n, CUDA_C_64F, dW, CUDA_C_64F, dV, 1, CUDA_C_64F, dV, 1,
                                        CUDA_C_64F, &dws, &hws) != CUSOLVER_STATUS_SUCCESS) {
             set_error("cusolverDnXgeev_bufferSize failed");
             rc = SCALIT_ECUDA;
@@ -773,7 +774,7 @@ static int geev_cx(scalit_ctx *c, int n, const std::vector<cplx> &H, int ld, std
         hbuf.resize(std::max<size_t>(hws, 16));
         if (cudaMemsetAsync(dinfo, 0, sizeof(int), s) != cudaSuccess ||
             cusolverDnXgeev(sol, prm, CUSOLVER_EIG_MODE_NOVECTOR, CUSOLVER_EIG_MODE_NOVECTOR, n, CUDA_C_64F, dA, n,
-                            CUDA_C_64F, dW, CUDA_C_64F, nullptr, 1, CUDA_C_64F, nullptr, 1, CUDA_C_64F, dbuf, dws,
+                            CUDA_C_64F, dW, CUDA_C_64F, dV, 1, CUDA_C_64F, dV, 1, CUDA_C_64F, dbuf, dws,
                             hbuf.data(), hws, dinfo) != CUSOLVER_STATUS_SUCCESS) {
             set_error("cusolverDnXgeev failed");
             rc = SCALIT_ECUDA;
@@ -794,6 +795,7 @@ static int geev_cx(scalit_ctx *c, int n, const std::vector<cplx> &H, int ld, std
     if (dW) cudaFreeAsync(dW, s);
     if (dbuf) cudaFreeAsync(dbuf, s);
     if (dinfo) cudaFreeAsync(dinfo, s);
+    if (dV) cudaFreeAsync(dV, s);
     cudaStreamSynchronize(s);
     cusolverDnDestroyParams(prm);
     return rc;
