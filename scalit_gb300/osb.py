@@ -25,6 +25,8 @@ class OSB:
     def __init__(self, inp: refio.OSBInput, device: int = 0, precision: int = capi.PREC_FP64):
         if inp.sCX:
             raise ValueError("complex Hamiltonians (sCX) are not supported")
+        if inp.sJOB == refio.JOB_RES2:
+            raise ValueError("the conjugate complex PIST (JOB_RES2) is not supported")
         self.inp = inp
         self.device = device
         self.precision = precision
@@ -49,6 +51,12 @@ class OSB:
         DEP = refio.load_data_dir(inp.DEPFile, inp.dep_len) if inp.dep_len else None
         self.ctx = capi.Context(inp.sN[:inp.sF], inp.sDEP[:inp.sF], ndvr=inp.sNDVR, device=self.device)
         self.ctx.load(H0, RES, DEP, OUTH)
+        # absorbing potentials (osb.io.h:18-30): APP for the resonance jobs, APP and APR for CRP
+        if inp.sJOB in (refio.JOB_RES1, refio.JOB_RES2):
+            self.ctx.set_absorbing(refio.load_data_dir(inp.APPFile, inp.my_len))
+        elif inp.sJOB in (refio.JOB_CRP, refio.JOB_CRP1, refio.JOB_CRP2):
+            self.ctx.set_absorbing(refio.load_data_dir(inp.APPFile, inp.my_len),
+                                   refio.load_data_dir(inp.APRFile, inp.my_len))
         self.ctx.set_shift(inp.sOSBW[0])
         self.ctx.set_precond(inp.sOSB if inp.sOSB in (1, 2, 3) else 1, inp.sOSBW[1], inp.sOSBW[2])
         return True
@@ -109,6 +117,37 @@ class OSB:
                              gap=mGap, qmr_max=inp.sQMR[0], qmr_tol=inp.sQMR[1], qmr_ntype=-1,
                              precision=self.precision, ntype=0, verbose=verbose, basis=basis)
 
+    # setPISTConvParam (osbw.pistconv.h:303-333)
+    def pist_params(self):
+        mE0, mTol, mStart, mStep, mMax, mNum, mGap = self.inp.sConv
+        start = 2 * mNum if mStart < mNum else mStart
+        return dict(e0=mE0, etol=mTol, startcnt=start, stepcnt=5 if mStep < 1 else mStep,
+                    stepeig=1 if mGap < 1 else mGap, m_max=start + mNum if mMax < start else mMax)
+
+    # OSB_PISTCONVDX1 (osbw.pistconv.h:102-143): resonances of H - i AP by the
+    # symmetric complex PIST; QMR_CX on (H - E0 - i AP) with the preconditioner's
+    # absorbing term when sAP is set
+    def pist_resonances(self, x0=None, seed=0):
+        inp = self.inp
+        prm = self.pist_params()
+        if x0 is None:
+            rng = np.random.default_rng(seed)                     # randMat_CX
+            x0 = rng.random(inp.my_len) + 1j * rng.random(inp.my_len)
+        return self.ctx.pist_cx(x0, inp.sConv[5], prm["e0"], prm["etol"], prm["m_max"],
+                                startcnt=prm["startcnt"], stepcnt=prm["stepcnt"], stepeig=prm["stepeig"],
+                                h0_ntype=capi.TMAP0, ls_ntype=capi.TMAP,
+                                ls_px_ntype=capi.TMAP if inp.sAP else capi.TA1, conv=-1,
+                                qmrmax=inp.sQMR[0], qmrtol=inp.sQMR[1])
+
+    # the CRP job of progPistEig (osbw.progEig.h:55-63): N(E) at
+    # E = mE0 + (i - 1) mTol, i = 1..mNum, with mGap Lanczos steps
+    def crp(self, seed=0):
+        inp = self.inp
+        mE0, mTol, _, _, _, mNum, mGap = inp.sConv
+        energies = mE0 + mTol * np.arange(mNum)
+        return energies, self.ctx.crp(energies, mGap, qmrmax=inp.sQMR[0], qmrtol=inp.sQMR[1], conv=-1,
+                                      sap=inp.sAP, seed=seed)
+
     # progPistEig (osbw.progEig.h:6-98)
     def prog_pist_eig(self, log=print, **kw):
         t0 = time.perf_counter()
@@ -116,6 +155,28 @@ class OSB:
             log(" ================================================")
             log("      Get  Eigen Values Using PIST method        ")
             log(" ================================================")
+        job = self.inp.sJOB
+        if job in (refio.JOB_CRP, refio.JOB_CRP1, refio.JOB_CRP2):
+            if log:
+                log(" ------  CRP calculation for Real Version of H0  -------")
+            energies, crp = self.crp()
+            if log:
+                for i, (e, v) in enumerate(zip(energies, crp), 1):
+                    log(f"Step:{i:5d} | Energy:{e:10.6f} | CRP:{v:15.9f}")
+                log(f" Time to get PIST Eigen values:(sec) {time.perf_counter() - t0:.3f}")
+            return len(crp), crp, 0.0, {"energies": energies}
+        if job == refio.JOB_RES1:
+            if log:
+                log(" ------  Resonance states for Real Version of H0  -------")
+                log(" ------ Using Symmetric version of PIST  -------")
+            st, eig, res = self.pist_resonances()
+            if log:
+                log(f" Max Lanczos Error: {res:.15E}  Eigen Values:")
+                for e in eig:
+                    log(f"{e.real:25.15E}  {e.imag:25.15E}")
+                log(f" Time to get PIST Eigen values:(sec) {time.perf_counter() - t0:.3f}")
+            return st, eig, res, {}
+        if log:
             log(" ------  Bound states for Real Version of H0  -------")
         if self.inp.sPT != 0:
             kw = dict(kw, basis=True)

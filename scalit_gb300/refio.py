@@ -23,6 +23,7 @@ FMAX = 20
 # Preconditioner kinds (sOSB) and operator kinds (sHC/sPC): src/iterate/module/osb.data.h:10-20.
 TOSB, TOSBD1, TOSBD2, TOSBW = 1, 2, 3, 4
 JOB_BOUND = 1
+JOB_RES1, JOB_RES2, JOB_CRP, JOB_CRP1, JOB_CRP2 = 2, 3, 4, 5, 6   # osb.data.h:13-14
 TA0, TA1 = 0, 1
 
 
@@ -56,6 +57,8 @@ class OSBInput:
     VOSBFile: str = ""
     EigFile: str = ""
     HWFile: str = ""
+    APPFile: str = ""
+    APRFile: str = ""
     VXFile: str = ""
     PTFile: str = ""
 
@@ -178,10 +181,11 @@ def read_input(text: str) -> OSBInput:
         inp.RESFile = name()
     if any(inp.sDEP[:sF]):
         inp.DEPFile = name()
-    if inp.sJOB in (2, 3):
-        raise ValueError("resonance jobs (absorbing potential) are not supported")
-    if inp.sJOB in (4, 5, 6):
-        raise ValueError("CRP jobs are not supported")
+    if inp.sJOB in (JOB_RES1, JOB_RES2):                      # osb.print.h:230-231
+        inp.APPFile = name()
+    elif inp.sJOB in (JOB_CRP, JOB_CRP1, JOB_CRP2):           # osb.print.h:232-234
+        inp.APPFile = name()
+        inp.APRFile = name()
     if inp.sHOSB != 0:
         inp.HOSBFile = name()
     if inp.sVOSB != 0:
@@ -217,6 +221,10 @@ def write_input(inp: OSBInput) -> str:
     out.append(inp.OUTHFile if inp.sNDVR else inp.RESFile)
     if any(inp.sDEP[:inp.sF]):
         out.append(inp.DEPFile)
+    if inp.sJOB in (JOB_RES1, JOB_RES2):
+        out.append(inp.APPFile)
+    elif inp.sJOB in (JOB_CRP, JOB_CRP1, JOB_CRP2):
+        out.extend([inp.APPFile, inp.APRFile])
     for flag, names in ((inp.sHOSB, [inp.HOSBFile]), (inp.sVOSB, [inp.VOSBFile, inp.EigFile]),
                         (inp.sHW, [inp.HWFile]), (inp.sVX, [inp.VXFile]),
                         (inp.sPT, [inp.PTFile])):

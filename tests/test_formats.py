@@ -156,3 +156,21 @@ def test_hw_file_roundtrip(tmp_path):
     txt = tmp_path / "hw_rep.txt"                       # list-directed repeats: r*value, D exponents
     txt.write_text(" 2\n 2*1.5D0 0.25\n -3.0\n")
     np.testing.assert_array_equal(refio.load_hw(txt, 2, binary=False), [[1.5, 0.25], [1.5, -3.0]])
+
+
+@pytest.mark.parametrize("job,names", [(2, ("APP.dat",)), (3, ("APP.dat",)), (4, ("APP.dat", "APR.dat")),
+                                       (6, ("APP.dat", "APR.dat"))])
+def test_input_absorbing_potential_files(job, names):
+    """myReadOSB (osb.print.h:230-234): the resonance jobs name APPFile, the CRP
+    jobs APPFile and APRFile, after the DEP file and before the optional files."""
+    inp = refio.OSBInput(sJOB=job, sAP=True, sVOSB=1, VOSBFile="V.dat", EigFile="E.dat",
+                         APPFile=names[0], APRFile=names[1] if len(names) > 1 else "")
+    text = refio.write_input(inp)
+    lines = text.splitlines()
+    i = lines.index("DEP.dat")
+    assert tuple(lines[i + 1:i + 1 + len(names)]) == names
+    assert lines[i + 1 + len(names)] == "V.dat"
+    back = refio.read_input(text)
+    assert back.sJOB == job and back.sAP
+    assert back.APPFile == "APP.dat" and back.APRFile == (names[1] if len(names) > 1 else "")
+    assert back.VOSBFile == "V.dat" and back.EigFile == "E.dat"

@@ -235,3 +235,51 @@ def test_fortran_externals_with_callbacks(lib, orc):
     st_r, eig_r, _ = orc.pist_conv_sx(E0, 1e-12, 0, xs, 0, 5, 1, 5, n, lambda v: M @ v, lambda v: (1, inv @ v))
     assert st > 0 and st_r > 0
     np.testing.assert_allclose(eig, eig_r, atol=1e-9)
+
+
+def test_driver_resonance_and_crp_jobs(lib, tmp_path):
+    """The driver flow on reference-format files for JOB_RES1 (OSB_PISTCONVDX1:
+    resonances of H - i AP) and JOB_CRP (osbCRP at mE0 + (i-1) mTol)."""
+    from scalit_gb300 import osb, refio
+    p = hm.build_problem(hm.Grid3(12, 10, 8), hm.PES())
+    H = hm.dense_hamiltonian(p, shift=0.0)
+    rng = np.random.default_rng(15)
+    apr = np.zeros(p.N)
+    pts = rng.choice(p.N, 8, replace=False)
+    apr[pts] = rng.uniform(1e-3, 3e-3, 8)
+    app = np.where(apr == 0.0, rng.uniform(0.0, 2e-3, p.N), 0.0)
+    refio.save_data_dir(tmp_path / "APP.dat", app)
+    refio.save_data_dir(tmp_path / "APR.dat", apr)
+    exact = np.linalg.eigvals(H)
+    e0 = float(np.sort(exact.real)[12]) + 3e-4
+
+    inp = refio.OSBInput(sJOB=refio.JOB_RES1, sAP=True, sBJ=(20, 1e-4), sQMR=(1000, 1e-12),
+                         sConv=(e0, 1e-11, 0, 5, 200, 4, 1), sOSBW=(e0, 0.0, 0.0, 0),
+                         APPFile=str(tmp_path / "APP.dat"))
+    inp = refio.write_problem_files(p, tmp_path, inp)
+    o = osb.OSB.read((tmp_path / "input.txt").read_text())
+    assert o.load_init_data()
+    o.prog_diag(log=None)
+    st, eig, res, _ = o.prog_pist_eig(log=None)
+    o.close()
+    cx = np.linalg.eigvals(H - 1j * np.diag(app))
+    want = cx[np.argsort(np.abs(cx.real - e0))[:4]]
+    want = want[np.argsort(want.real)]
+    assert st > 0
+    np.testing.assert_allclose(eig, want, atol=1e-7)
+
+    inp2 = refio.OSBInput(sJOB=refio.JOB_CRP, sAP=True, sBJ=(20, 1e-4), sQMR=(2000, 1e-12),
+                          sConv=(e0, 1e-3, 0, 5, 0, 2, 9), sOSBW=(e0, 0.0, 0.0, 0),
+                          APPFile=str(tmp_path / "APP.dat"), APRFile=str(tmp_path / "APR.dat"))
+    inp2 = refio.write_problem_files(p, tmp_path, inp2)
+    o2 = osb.OSB.read((tmp_path / "input.txt").read_text())
+    assert o2.load_init_data()
+    o2.prog_diag(log=None)
+    n, crp, _, info = o2.prog_pist_eig(log=None)
+    o2.close()
+    ap = app + apr
+    sq = np.diag(np.sqrt(apr))
+    for E, got in zip(info["energies"], crp):
+        G = lambda s: np.linalg.inv(H - E * np.eye(p.N) + s * 1j * np.diag(ap))
+        dense = 4.0 * np.real(np.trace(sq @ G(1) @ np.diag(app) @ G(-1) @ sq))
+        assert abs(got - dense) / dense < 1e-5
