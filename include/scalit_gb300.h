@@ -275,10 +275,12 @@ int scalit_crp(scalit_ctx *ctx, int nenergy, const double *energies, int nm, int
  * change of |lambda|^2 is <= etol.  eig receives m interleaved complex values
  * in ascending real part, *status PIST's result (+cnt, -cnt, 0 for bad
  * parameters).  ntype > 0 returns SCALIT_EUNSUP: the reference's call of
- * getSepMax_CX there passes mismatched arguments. */
-int scalit_pist_cx(scalit_ctx *ctx, double e0, double etol, int ntype, const double *X0, int startcnt,
-                   int stepcnt, int stepeig, int m, int m_max, int h0_ntype, int ls_ntype, int ls_px_ntype,
-                   int conv, int qmrmax, double qmrtol, double *eig, double *res, int *status);
+ * getSepMax_CX there passes mismatched arguments.  conjugate != 0 runs
+ * PIST_CONV_CX (pist/pist_cx.f90) instead: the same steps in the conjugated
+ * product (MGS_ORTH_CX, HMAT = VJ^H H0 VJ), the driver's JOB_RES2. */
+int scalit_pist_cx(scalit_ctx *ctx, double e0, double etol, int ntype, int conjugate, const double *X0,
+                   int startcnt, int stepcnt, int stepeig, int m, int m_max, int h0_ntype, int ls_ntype,
+                   int ls_px_ntype, int conv, int qmrmax, double qmrtol, double *eig, double *res, int *status);
 
 /* ------------------------------------------------------------------ QMR ---
  * OSB_QMR -> QMR / QMR_MPI (src/iterate/module/osbw.qmr.h:13-23,
@@ -486,6 +488,11 @@ int qmr_(const int *ntype, const int *qmrmax, const double *qmrtol, const int *n
 int qmr_cx_(const int *ntype, const int *qmrmax, const double *qmrtol, const int *n, const double *B,
             scalit_fortran_op hx, scalit_fortran_op px, double *X, double *RES);
 int pist_conv_sx_(const double *e0, const double *etol, const int *ntype, const int *n, const double *X,
+                  const int *startcnt, const int *stepcnt, const int *stepeig, const int *m, const int *m_max,
+                  scalit_fortran_op h0x, scalit_fortran_linsolv linsolv, double *EIG, double *RES);
+/* PIST_CONV_CX (src/iterate/libiterate/pist/pist_cx.f90): PIST_CONV_SX in the
+ * conjugated product (MGS_ORTH_CX, HMAT = VJ^H H0 VJ). */
+int pist_conv_cx_(const double *e0, const double *etol, const int *ntype, const int *n, const double *X,
                   const int *startcnt, const int *stepcnt, const int *stepeig, const int *m, const int *m_max,
                   scalit_fortran_op h0x, scalit_fortran_linsolv linsolv, double *EIG, double *RES);
 int qmr_mpi_(const int *ntype, const int *qmrmax, const double *qmrtol, const int *n,

@@ -803,6 +803,19 @@ def dot_cx(x, y):
     return complex(np.sum(np.asarray(x) * np.asarray(y)))
 
 
+def mgs_orth_cx(W, m, VJ):
+    """MGS_ORTH_CX (src/iterate/libiterate/orth/gsorth_cx.f90:51-79): the same
+    in the conjugated product, normalised by the real norm."""
+    v = np.asarray(W, dtype=np.complex128).copy()
+    for i in range(m):
+        v = v - np.vdot(VJ[:, i], v) * VJ[:, i]
+    nrm = np.sqrt(np.real(np.vdot(v, v)))
+    if nrm == 0.0:
+        return False
+    VJ[:, m] = v / nrm
+    return True
+
+
 def mgs_orth_sx(W, m, VJ):
     """MGS_ORTH_SX (src/iterate/libiterate/orth/gsorth_sx.f90:47-72): modified
     Gram-Schmidt in the bilinear product, column m of VJ (0-based) from W,
@@ -817,13 +830,16 @@ def mgs_orth_sx(W, m, VJ):
     return True
 
 
-def pisth0_sx(X, m_max, m_low, m_high, h0x, linsolv, VJ, HMAT):
-    """pistH0_SX (src/iterate/libiterate/pist/pistHij_sx.f90:62-118)."""
+def pisth0_sx(X, m_max, m_low, m_high, h0x, linsolv, VJ, HMAT, conj=False):
+    """pistH0_SX (src/iterate/libiterate/pist/pistHij_sx.f90:62-118); with conj,
+    pistH0_CX (pistHij_cx.f90) in the conjugated product."""
+    dot = (lambda a, b: complex(np.vdot(a, b))) if conj else dot_cx
+    orth = mgs_orth_cx if conj else mgs_orth_sx
     if m_low < 1 or m_low >= m_high or m_high > m_max:
         return 0
     if m_low == 1:
         m_start = 1
-        t = np.sqrt(dot_cx(X, X))
+        t = np.sqrt(np.real(np.vdot(X, X))) if conj else np.sqrt(dot_cx(X, X))
         if t == 0.0:
             return 0
         VJ[:, 0] = np.asarray(X, dtype=np.complex128) / t
@@ -833,27 +849,28 @@ def pisth0_sx(X, m_max, m_low, m_high, h0x, linsolv, VJ, HMAT):
         num, WJ = linsolv(VJ[:, J - 1])
         if num <= 0:
             return num
-        if not mgs_orth_sx(WJ, J, VJ):
+        if not orth(WJ, J, VJ):
             return -J
     for J in range(m_low, m_high + 1):
         WJ = h0x(VJ[:, J - 1])
         for I in range(1, m_high + 1):
-            HMAT[I - 1, J - 1] = dot_cx(VJ[:, I - 1], WJ)
+            HMAT[I - 1, J - 1] = dot(VJ[:, I - 1], WJ)
     for J in range(1, m_low):
         WJ = h0x(VJ[:, J - 1])
         for I in range(m_low, m_high + 1):
-            HMAT[I - 1, J - 1] = dot_cx(VJ[:, I - 1], WJ)
+            HMAT[I - 1, J - 1] = dot(VJ[:, I - 1], WJ)
     return m_high
 
 
-def pist_conv_sx(E0, etol, ntype, x, startcnt, stepcnt, stepeig, M, m_max, h0x, linsolv):
+def pist_conv_sx(E0, etol, ntype, x, startcnt, stepcnt, stepeig, M, m_max, h0x, linsolv, conj=False):
     """PIST_CONV_SX (src/iterate/libiterate/pist/pist_sx.f90:4-96): PIST for a
     complex symmetric operator.  The eigenvalues of HMAT come from ZGEEV
     (numpy's eigvals is LAPACK's ZGEEV), the window and the final order use
     the real part, the convergence test |lambda|^2 (getOpCX types 1 and 6).
     ntype > 0 is not restated: the reference calls getSepMax_CX with five
     arguments (an integer where a complex array is expected), which has no
-    defined result.  Returns (status, eig[M], RES)."""
+    defined result.  With conj this is PIST_CONV_CX (pist/pist_cx.f90): the
+    same steps in the conjugated product.  Returns (status, eig[M], RES)."""
     if ntype > 0:
         raise ValueError("PIST_CONV_SX with ntype > 0 has no defined result in the reference")
     n_diff, n_conv = 1, 6
@@ -865,7 +882,7 @@ def pist_conv_sx(E0, etol, ntype, x, startcnt, stepcnt, stepeig, M, m_max, h0x, 
     cnt_low, cnt_high = 1, max(startcnt, M, stepeig + 1)
     status, res, eig = 0, 0.0, np.zeros(M, np.complex128)
     while cnt_high <= m_max:
-        num = pisth0_sx(x, m_max, cnt_low, cnt_high, h0x, linsolv, VJ, HMAT)
+        num = pisth0_sx(x, m_max, cnt_low, cnt_high, h0x, linsolv, VJ, HMAT, conj)
         if num <= 0:
             return -cnt_high, eig, res
         n1 = cnt_high - stepeig

@@ -59,7 +59,7 @@ SIGNATURES = {
     "scalit_px_cx_device": (C.c_int, [_vp, C.c_int, C.c_int, _vp, _vp]),
     "scalit_qmr_cx": (C.c_int, [_vp, C.c_int, C.c_int, C.c_double, C.c_int, _dp, _dp, _ip, _dp]),
     "scalit_crp": (C.c_int, [_vp, C.c_int, _dp, C.c_int, C.c_int, C.c_double, C.c_int, C.c_int, _dp, _dp]),
-    "scalit_pist_cx": (C.c_int, [_vp, C.c_double, C.c_double, C.c_int, _dp, C.c_int, C.c_int, C.c_int,
+    "scalit_pist_cx": (C.c_int, [_vp, C.c_double, C.c_double, C.c_int, C.c_int, _dp, C.c_int, C.c_int, C.c_int,
                                  C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_double,
                                  _dp, _dp, _ip]),
     "scalit_set_osbw": (C.c_int, [_vp, C.c_double, C.c_int, _dp, C.c_int, _dp]),
@@ -107,6 +107,7 @@ SIGNATURES = {
     "qmr_": (C.c_int, [_ip, _ip, _dp, _ip, _dp, _vp, _vp, _dp, _dp]),
     "qmr_cx_": (C.c_int, [_ip, _ip, _dp, _ip, _dp, _vp, _vp, _dp, _dp]),
     "pist_conv_sx_": (C.c_int, [_dp, _dp, _ip, _ip, _dp, _ip, _ip, _ip, _ip, _ip, _vp, _vp, _dp, _dp]),
+    "pist_conv_cx_": (C.c_int, [_dp, _dp, _ip, _ip, _dp, _ip, _ip, _ip, _ip, _ip, _vp, _vp, _dp, _dp]),
     "qmr_mpi_": (C.c_int, [_ip, _ip, _dp, _ip, _dp, _vp, _vp, _dp, _dp, _ip]),
     "pist_conv_": (C.c_int, [_dp, _dp, _ip, _ip, _dp, _ip, _ip, _ip, _ip, _ip, _vp, _vp, _dp, _dp]),
     "pist_conv_mpi_": (C.c_int, [_ip, _ip, _dp, _dp, _ip, _ip, _dp, _ip, _ip, _ip, _ip, _ip, _vp, _vp,
@@ -369,13 +370,14 @@ class Context:
         return out
 
     def pist_cx(self, x0, m, e0, etol, m_max, startcnt=0, stepcnt=5, stepeig=1, h0_ntype=TMAP0,
-                ls_ntype=TMAP, ls_px_ntype=TMAP, conv=0, qmrmax=2000, qmrtol=1e-4, ntype=0):
-        """PIST_CONV_SX: returns (status, eig[m] complex, RES)."""
+                ls_ntype=TMAP, ls_px_ntype=TMAP, conv=0, qmrmax=2000, qmrtol=1e-4, ntype=0, conjugate=False):
+        """PIST_CONV_SX (PIST_CONV_CX with conjugate): returns (status, eig[m] complex, RES)."""
         Z = np.ascontiguousarray(x0, dtype=np.complex128)
         eig = np.zeros(int(m), dtype=np.complex128)
         res = C.c_double(0.0)
         st = C.c_int(0)
-        _check(self.lib.scalit_pist_cx(self.h, float(e0), float(etol), int(ntype), _p(Z.view(np.float64)),
+        _check(self.lib.scalit_pist_cx(self.h, float(e0), float(etol), int(ntype), int(bool(conjugate)),
+                                       _p(Z.view(np.float64)),
                                        int(startcnt), int(stepcnt), int(stepeig), int(m), int(m_max),
                                        int(h0_ntype), int(ls_ntype), int(ls_px_ntype), int(conv), int(qmrmax),
                                        float(qmrtol), _p(eig.view(np.float64)), C.byref(res), C.byref(st)))

@@ -1228,14 +1228,15 @@ int qmr_cx_(const int *ntype, const int *qmrmax, const double *qmrtol, const int
     return code;
 }
 
-int pist_conv_sx_(const double *e0, const double *etol, const int *ntype, const int *n, const double *X,
-                  const int *startcnt, const int *stepcnt, const int *stepeig, const int *m, const int *m_max,
-                  scalit_fortran_op h0x, scalit_fortran_linsolv linsolv, double *EIG, double *RES)
+static int pist_complex_fortran(const double *e0, const double *etol, const int *ntype, const int *n,
+                                const double *X, const int *startcnt, const int *stepcnt, const int *stepeig,
+                                const int *m, const int *m_max, scalit_fortran_op h0x, scalit_fortran_linsolv linsolv,
+                                double *EIG, double *RES, int conj)
 {
     std::lock_guard<std::mutex> lk(g_fmu);
     *RES = 0.0;
     if (*ntype > 0) {
-        fprintf(stderr, "scalit_gb300: pist_conv_sx with ntype > 0 has no defined result in the reference\n");
+        fprintf(stderr, "scalit_gb300: complex PIST with ntype > 0 has no defined result in the reference\n");
         return 0;
     }
     scalit_ctx *c = scratch();
@@ -1243,10 +1244,25 @@ int pist_conv_sx_(const double *e0, const double *etol, const int *ntype, const 
     int status = 0;
     double res = 0.0;
     const int rc = pist_sx_host(c, *n, *e0, *etol, X, *startcnt, *stepcnt, *stepeig, *m, *m_max, h0x, linsolv, EIG,
-                                &res, &status);
-    if (rc) { report("pist_conv_sx", rc); return rc; }
+                                &res, &status, conj);
+    if (rc) { report(conj ? "pist_conv_cx" : "pist_conv_sx", rc); return rc; }
     *RES = res;
     return status;
+}
+
+int pist_conv_sx_(const double *e0, const double *etol, const int *ntype, const int *n, const double *X,
+                  const int *startcnt, const int *stepcnt, const int *stepeig, const int *m, const int *m_max,
+                  scalit_fortran_op h0x, scalit_fortran_linsolv linsolv, double *EIG, double *RES)
+{
+    return pist_complex_fortran(e0, etol, ntype, n, X, startcnt, stepcnt, stepeig, m, m_max, h0x, linsolv, EIG, RES, 0);
+}
+
+// PIST_CONV_CX (src/iterate/libiterate/pist/pist_cx.f90): the conjugate-product twin.
+int pist_conv_cx_(const double *e0, const double *etol, const int *ntype, const int *n, const double *X,
+                  const int *startcnt, const int *stepcnt, const int *stepeig, const int *m, const int *m_max,
+                  scalit_fortran_op h0x, scalit_fortran_linsolv linsolv, double *EIG, double *RES)
+{
+    return pist_complex_fortran(e0, etol, ntype, n, X, startcnt, stepcnt, stepeig, m, m_max, h0x, linsolv, EIG, RES, 1);
 }
 
 int pist_conv_(const double *e0, const double *etol, const int *ntype, const int *n, const double *X,

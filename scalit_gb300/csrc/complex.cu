@@ -806,6 +806,7 @@ struct PistCxArgs {
     int startcnt, stepcnt, stepeig, m, m_max;
     int h0_ntype, ls_ntype, ls_px_ntype, conv, qmrmax;
     double qmrtol;
+    int conj;   // PIST_CONV_CX (pist/pist_cx.f90): the conjugated product throughout
 };
 
 // The linear solver of PIST: out = solve(in), *num its iteration code (<= 0 failed).
@@ -845,7 +846,8 @@ static int pist_cx_core(scalit_ctx *c, i64 N, const PistCxArgs &a, const double 
         double h[4];
         e = sync_read_doubles(c, dd, h, 4);
         if (e) return e;
-        *r = cplx(h[0] - h[1], h[2] + h[3]);
+        // bilinear x^T y, or the conjugated x^H y (Fortran dot_product) for PIST_CONV_CX
+        *r = a.conj ? cplx(h[0] + h[1], h[2] - h[3]) : cplx(h[0] - h[1], h[2] + h[3]);
         return 0;
     };
     auto axpby = [&](cplx al, const double *x, cplx be, double *y, int overwrite) -> int {
@@ -853,7 +855,9 @@ static int pist_cx_core(scalit_ctx *c, i64 N, const PistCxArgs &a, const double 
         SC_CHECK_LAUNCH();
         return 0;
     };
-    // pistH0_SX: returns m_high, <= 0 from the linear solver, -J from the orthogonalisation
+    // the norm of MGS_ORTH_SX (principal sqrt of x^T x) or MGS_ORTH_CX (sqrt of Re x^H x)
+    auto vnorm = [&](cplx d) { return a.conj ? cplx(std::sqrt(d.real()), 0.0) : std::sqrt(d); };
+    // pistH0_SX / pistH0_CX: returns m_high, <= 0 from the linear solver, -J from the orthogonalisation
     auto pisth0 = [&](int m_low, int m_high, int *ret) -> int {
         *ret = 0;
         if (m_low < 1 || m_low >= m_high || m_high > MM) return 0;
@@ -863,7 +867,7 @@ static int pist_cx_core(scalit_ctx *c, i64 N, const PistCxArgs &a, const double 
             cplx xx;
             int e = bil(Xin, Xin, &xx);
             if (e) return e;
-            const cplx t = std::sqrt(xx);
+            const cplx t = vnorm(xx);
             if (t == cplx(0.0, 0.0)) return 0;
             if ((e = axpby(cplx(1.0, 0.0) / t, Xin, cplx(0.0, 0.0), col(1), 1))) return e;
         } else {
@@ -882,7 +886,7 @@ static int pist_cx_core(scalit_ctx *c, i64 N, const PistCxArgs &a, const double 
             }
             cplx nw;
             if ((e = bil(Wv, Wv, &nw))) return e;
-            const cplx nrm = std::sqrt(nw);
+            const cplx nrm = vnorm(nw);
             if (nrm == cplx(0.0, 0.0)) { *ret = -J; return 0; }
             if ((e = axpby(cplx(1.0, 0.0) / nrm, Wv, cplx(0.0, 0.0), col(J + 1), 1))) return e;
         }
@@ -1032,7 +1036,7 @@ int qmr_cx_host(scalit_ctx *c, i64 n, scalit_fortran_op hx, scalit_fortran_op px
 
 int pist_sx_host(scalit_ctx *c, i64 n, double e0, double etol, const double *X0, int startcnt, int stepcnt,
                  int stepeig, int m, int m_max, scalit_fortran_op h0x, scalit_fortran_linsolv linsolv, double *eig,
-                 double *res, int *status)
+                 double *res, int *status, int conj)
 {
     const i64 N2 = 2 * n;
     double *w = nullptr;
@@ -1052,7 +1056,7 @@ int pist_sx_host(scalit_ctx *c, i64 n, double e0, double etol, const double *X0,
         *num = linsolv(&nn, h.hin.data(), h.hout.data(), &r);
         return h.from_host(out);
     };
-    PistCxArgs a{e0, etol, startcnt, stepcnt, stepeig, m, m_max, 0, 0, 0, 0, 0, 0.0};
+    PistCxArgs a{e0, etol, startcnt, stepcnt, stepeig, m, m_max, 0, 0, 0, 0, 0, 0.0, conj};
     std::vector<cplx> ev;
     int rc = pist_cx_core(c, n, a, X0, h0op, lin, ev, res, status);
     if (!rc) {
@@ -1185,9 +1189,9 @@ int scalit_crp(scalit_ctx *c, int nenergy, const double *energies, int nm, int q
     return crp_run(c, nenergy, energies, nm, qmrmax, qmrtol, conv, sap, X0, crp);
 }
 
-int scalit_pist_cx(scalit_ctx *c, double e0, double etol, int ntype, const double *X0, int startcnt, int stepcnt,
-                   int stepeig, int m, int m_max, int h0_ntype, int ls_ntype, int ls_px_ntype, int conv, int qmrmax,
-                   double qmrtol, double *eig, double *res, int *status)
+int scalit_pist_cx(scalit_ctx *c, double e0, double etol, int ntype, int conjugate, const double *X0, int startcnt,
+                   int stepcnt, int stepeig, int m, int m_max, int h0_ntype, int ls_ntype, int ls_px_ntype, int conv,
+                   int qmrmax, double qmrtol, double *eig, double *res, int *status)
 {
     CX_CTX_CHECK(c);
     if (!c->osb_built) { set_error("complex PIST needs the preconditioner: build or load it first"); return SCALIT_ESTATE; }
@@ -1197,7 +1201,8 @@ int scalit_pist_cx(scalit_ctx *c, double e0, double etol, int ntype, const doubl
         return SCALIT_EUNSUP;
     }
     if (m < 1 || m_max < 2) { set_error("complex PIST needs m >= 1 and m_max >= 2"); return SCALIT_EINVAL; }
-    PistCxArgs a{e0, etol, startcnt, stepcnt, stepeig, m, m_max, h0_ntype, ls_ntype, ls_px_ntype, conv, qmrmax, qmrtol};
+    PistCxArgs a{e0, etol, startcnt, stepcnt, stepeig, m, m_max, h0_ntype, ls_ntype, ls_px_ntype, conv, qmrmax,
+                 qmrtol, conjugate ? 1 : 0};
     std::vector<cplx> ev;
     const int rc = pist_cx_run(c, a, X0, ev, res, status);
     if (rc) return rc;

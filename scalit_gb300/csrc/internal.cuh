@@ -246,7 +246,7 @@ int qmr_cx_host(scalit_ctx *c, i64 n, scalit_fortran_op hx, scalit_fortran_op px
                 const double *B, double *X, int *code, double *res);
 int pist_sx_host(scalit_ctx *c, i64 n, double e0, double etol, const double *X0, int startcnt, int stepcnt,
                  int stepeig, int m, int m_max, scalit_fortran_op h0x, scalit_fortran_linsolv linsolv, double *eig,
-                 double *res, int *status);
+                 double *res, int *status, int conj);
 
 // ------------------------------------------------------------- OSB build --
 int osb_build(scalit_ctx *c, int bjmax, double bjtol, double *stats);

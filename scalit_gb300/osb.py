@@ -25,8 +25,6 @@ class OSB:
     def __init__(self, inp: refio.OSBInput, device: int = 0, precision: int = capi.PREC_FP64):
         if inp.sCX:
             raise ValueError("complex Hamiltonians (sCX) are not supported")
-        if inp.sJOB == refio.JOB_RES2:
-            raise ValueError("the conjugate complex PIST (JOB_RES2) is not supported")
         self.inp = inp
         self.device = device
         self.precision = precision
@@ -124,9 +122,10 @@ class OSB:
         return dict(e0=mE0, etol=mTol, startcnt=start, stepcnt=5 if mStep < 1 else mStep,
                     stepeig=1 if mGap < 1 else mGap, m_max=start + mNum if mMax < start else mMax)
 
-    # OSB_PISTCONVDX1 (osbw.pistconv.h:102-143): resonances of H - i AP by the
-    # symmetric complex PIST; QMR_CX on (H - E0 - i AP) with the preconditioner's
-    # absorbing term when sAP is set
+    # OSB_PISTCONVDX1 / OSB_PISTCONVDX2 (osbw.pistconv.h:102-143, 204-245):
+    # resonances of H - i AP by the symmetric (JOB_RES1) or the conjugate
+    # (JOB_RES2) complex PIST; QMR_CX on (H - E0 - i AP) with the
+    # preconditioner's absorbing term when sAP is set
     def pist_resonances(self, x0=None, seed=0):
         inp = self.inp
         prm = self.pist_params()
@@ -137,7 +136,8 @@ class OSB:
                                 startcnt=prm["startcnt"], stepcnt=prm["stepcnt"], stepeig=prm["stepeig"],
                                 h0_ntype=capi.TMAP0, ls_ntype=capi.TMAP,
                                 ls_px_ntype=capi.TMAP if inp.sAP else capi.TA1, conv=-1,
-                                qmrmax=inp.sQMR[0], qmrtol=inp.sQMR[1])
+                                qmrmax=inp.sQMR[0], qmrtol=inp.sQMR[1],
+                                conjugate=inp.sJOB == refio.JOB_RES2)
 
     # the CRP job of progPistEig (osbw.progEig.h:55-63): N(E) at
     # E = mE0 + (i - 1) mTol, i = 1..mNum, with mGap Lanczos steps
@@ -165,10 +165,11 @@ class OSB:
                     log(f"Step:{i:5d} | Energy:{e:10.6f} | CRP:{v:15.9f}")
                 log(f" Time to get PIST Eigen values:(sec) {time.perf_counter() - t0:.3f}")
             return len(crp), crp, 0.0, {"energies": energies}
-        if job == refio.JOB_RES1:
+        if job in (refio.JOB_RES1, refio.JOB_RES2):
             if log:
                 log(" ------  Resonance states for Real Version of H0  -------")
-                log(" ------ Using Symmetric version of PIST  -------")
+                log(" ------ Using Symmetric version of PIST  -------" if job == refio.JOB_RES1 else
+                    " ------ Using Conjugate version of PIST  -------")
             st, eig, res = self.pist_resonances()
             if log:
                 log(f" Max Lanczos Error: {res:.15E}  Eigen Values:")

@@ -283,3 +283,19 @@ def test_driver_resonance_and_crp_jobs(lib, tmp_path):
         G = lambda s: np.linalg.inv(H - E * np.eye(p.N) + s * 1j * np.diag(ap))
         dense = 4.0 * np.real(np.trace(sq @ G(1) @ np.diag(app) @ G(-1) @ sq))
         assert abs(got - dense) / dense < 1e-5
+
+
+def test_pist_cx_conjugate_levels(lib, orc, case):
+    """PIST_CONV_CX (JOB_RES2, the conjugated product) reaches the same complex
+    levels of H - i AP as the dense eigenvalues and the oracle."""
+    p, ref, e0, app, apr = case
+    cx = orc.CxOperator(ref, app, apr)
+    H = hm.dense_hamiltonian(p, shift=0.0)
+    exact = np.linalg.eigvals(H - 1j * np.diag(cx.AP))
+    want = exact[np.argsort(np.abs(exact.real - e0))[:4]]
+    want = want[np.argsort(want.real)]
+    x0 = np.random.default_rng(17).random(p.N) + 1j * np.random.default_rng(18).random(p.N)
+    with context(p, ref, e0, app, apr) as ctx:
+        st, eig, res = ctx.pist_cx(x0, 4, e0, 1e-11, 200, qmrmax=1000, qmrtol=1e-12, conjugate=True)
+    assert st > 0
+    np.testing.assert_allclose(eig, want, atol=1e-8)
