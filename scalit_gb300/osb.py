@@ -141,11 +141,14 @@ class OSB:
 
     # the CRP job of progPistEig (osbw.progEig.h:55-63): N(E) at
     # E = mE0 + (i - 1) mTol, i = 1..mNum, with mGap Lanczos steps
+    def crp_energies(self):
+        mE0, mTol, _, _, _, mNum, _ = self.inp.sConv
+        return mE0 + mTol * np.arange(mNum)
+
     def crp(self, seed=0):
         inp = self.inp
-        mE0, mTol, _, _, _, mNum, mGap = inp.sConv
-        energies = mE0 + mTol * np.arange(mNum)
-        return energies, self.ctx.crp(energies, mGap, qmrmax=inp.sQMR[0], qmrtol=inp.sQMR[1], conv=-1,
+        energies = self.crp_energies()
+        return energies, self.ctx.crp(energies, inp.sConv[6], qmrmax=inp.sQMR[0], qmrtol=inp.sQMR[1], conv=-1,
                                       sap=inp.sAP, seed=seed)
 
     # progPistEig (osbw.progEig.h:6-98)

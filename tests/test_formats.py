@@ -174,3 +174,16 @@ def test_input_absorbing_potential_files(job, names):
     assert back.sJOB == job and back.sAP
     assert back.APPFile == "APP.dat" and back.APRFile == (names[1] if len(names) > 1 else "")
     assert back.VOSBFile == "V.dat" and back.EigFile == "E.dat"
+
+
+def test_driver_parameters_without_a_device():
+    """setPISTConvParam (osbw.pistconv.h:303-333) and the CRP job's energy grid
+    (osbw.progEig.h:55-63) as the driver derives them."""
+    from scalit_gb300 import osb
+    o = osb.OSB(refio.OSBInput(sJOB=refio.JOB_CRP, sConv=(0.5, 0.01, 0, 0, 0, 4, 9)))
+    np.testing.assert_allclose(o.crp_energies(), [0.5, 0.51, 0.52, 0.53])
+    assert o.pist_params() == dict(e0=0.5, etol=0.01, startcnt=8, stepcnt=5, stepeig=9, m_max=12)
+    o2 = osb.OSB(refio.OSBInput(sConv=(0.1, 1e-8, 30, 7, 100, 20, 0)))
+    assert o2.pist_params() == dict(e0=0.1, etol=1e-8, startcnt=30, stepcnt=7, stepeig=1, m_max=100)
+    o2.close()
+    o.close()
