@@ -218,7 +218,9 @@ int scalit_px_f32_device(scalit_ctx *ctx, int npc, int nvec, const float *dX, fl
  * share the one array and it keeps the last call's contents (nothing in it
  * needs to start at zero: every stage overwrites it before reading), so calls
  * that overlap on the GPU -- two streams, or two contexts on one device --
- * race on it. */
+ * race on it.  The looked-up address is cached for the device's primary
+ * context: after a cudaDeviceReset in this process the variant must not be
+ * called again.  npc other than SCALIT_TA0 / SCALIT_TA1 is SCALIT_EINVAL. */
 int scalit_px_noalloc_device(scalit_ctx *ctx, int npc, const double *dX, double *dY);
 
 /* ------------------------------------------------ complex (absorbing) forms --

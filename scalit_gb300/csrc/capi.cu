@@ -553,12 +553,17 @@ static int qmr_host(scalit_ctx *c, int ntype, int qmrmax, double qmrtol, int pre
     const i64 N = c->L.N;
     double *bx = nullptr;
     SC_CUDA(cudaMallocAsync(&bx, sizeof(double) * 2 * (size_t)N, c->stream));
-    SC_CUDA(cudaMemcpyAsync(bx, B, sizeof(double) * N, cudaMemcpyHostToDevice, c->stream));
-    if (ntype > 0) SC_CUDA(cudaMemcpyAsync(bx + N, X, sizeof(double) * N, cudaMemcpyHostToDevice, c->stream));
-    int rc = qmr_run(c, ntype, qmrmax, qmrtol, precision, bx, bx + N, r);
+    // every failure below falls through to the one free of bx
+    int rc = 0;
+    cudaError_t e = cudaMemcpyAsync(bx, B, sizeof(double) * N, cudaMemcpyHostToDevice, c->stream);
+    if (e == cudaSuccess && ntype > 0)
+        e = cudaMemcpyAsync(bx + N, X, sizeof(double) * N, cudaMemcpyHostToDevice, c->stream);
+    if (e != cudaSuccess) rc = cuda_fail(e, "QMR right-hand side upload", __FILE__, __LINE__);
+    if (!rc) rc = qmr_run(c, ntype, qmrmax, qmrtol, precision, bx, bx + N, r);
     if (!rc) {
-        SC_CUDA(cudaMemcpyAsync(X, bx + N, sizeof(double) * N, cudaMemcpyDeviceToHost, c->stream));
-        SC_CUDA(cudaStreamSynchronize(c->stream));
+        e = cudaMemcpyAsync(X, bx + N, sizeof(double) * N, cudaMemcpyDeviceToHost, c->stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+        if (e != cudaSuccess) rc = cuda_fail(e, "QMR solution download", __FILE__, __LINE__);
     }
     cudaFreeAsync(bx, c->stream);
     cudaStreamSynchronize(c->stream);

@@ -588,9 +588,12 @@ static int crp_run(scalit_ctx *c, int nE, const double *energies, int nm, int qm
     const i64 N = c->L.N, N2 = 2 * N;
     cudaStream_t s = c->stream;
     double *w = nullptr, *dd = nullptr;
-    if (cudaMallocAsync(&w, sizeof(double) * (size_t)N2 * ((size_t)nm + 5), s) != cudaSuccess) {
+    // five work vectors, then VJ with nm + 1 columns: step J = nm still forms
+    // and normalises column nm (lanHij_dx declares VJ(N, M+1))
+    const size_t ncols = (size_t)nm + 6;
+    if (cudaMallocAsync(&w, sizeof(double) * (size_t)N2 * ncols, s) != cudaSuccess) {
         cudaGetLastError();
-        set_error("CRP workspace (%d Lanczos vectors of %lld complex points) does not fit", nm + 5, N);
+        set_error("CRP workspace (%d Lanczos vectors of %lld complex points) does not fit", (int)ncols, N);
         return SCALIT_ENOMEM;
     }
     if (cudaMallocAsync(&dd, sizeof(double) * 8, s) != cudaSuccess) {
@@ -667,6 +670,11 @@ static int crp_run(scalit_ctx *c, int nE, const double *energies, int nm, int qm
             const double nrm = std::sqrt(nw.real());
             beta[(size_t)J - 1] = nrm;
             if (nrm == 0.0) { ok = false; break; }
+            if ((size_t)J + 5 >= ncols) {   // VJ holds columns 0..nm
+                set_error("CRP Lanczos column %d outside the workspace", J);
+                rc = SCALIT_ECUDA;
+                break;
+            }
             if (cudaMemcpyAsync(col(J), W, sizeof(double) * (size_t)N2, cudaMemcpyDeviceToDevice, s) != cudaSuccess) {
                 set_error("CRP copy failed");
                 rc = SCALIT_ECUDA;

@@ -23,7 +23,9 @@ static __device__ __align__(256) double g_px_scratch[kNoAllocMaxPoints];
 
 // Device address of g_px_scratch per device.  In host code the symbol's name
 // is only a host-side stand-in, so the address is obtained once per device,
-// with that device current, by cudaGetSymbolAddress.
+// with that device current, by cudaGetSymbolAddress.  The cached address
+// belongs to the device's primary context: a caller that resets the device
+// (cudaDeviceReset) must not call the variant again in this process.
 static std::mutex g_scratch_mu;
 static double *g_scratch_addr[128] = {};
 
@@ -50,6 +52,10 @@ extern "C" int scalit_px_noalloc_device(scalit_ctx *c, int npc, const double *dX
     if (c->L.N > kNoAllocMaxPoints) {
         set_error("scalit_px_noalloc_device: grid of %lld points exceeds the %lld-point scratch "
                   "(use scalit_px_device)", c->L.N, kNoAllocMaxPoints);
+        return SCALIT_EINVAL;
+    }
+    if (npc != SCALIT_TA0 && npc != SCALIT_TA1) {
+        set_error("scalit_px_noalloc_device: npc %d is neither SCALIT_TA0 nor SCALIT_TA1", npc);
         return SCALIT_EINVAL;
     }
     if (!dX || !dY) { set_error("null vector"); return SCALIT_EINVAL; }
