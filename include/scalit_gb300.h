@@ -126,6 +126,13 @@ int scalit_set_precond(scalit_ctx *ctx, int osb_kind, double de, double beta);
  * X and Y must not overlap. */
 int scalit_hx(scalit_ctx *ctx, int ntype, int nvec, const double *X, double *Y);
 int scalit_hx_device(scalit_ctx *ctx, int ntype, int nvec, const double *dX, double *dY);
+/* Measurement aid, no counterpart in the reference: reps applications of
+ * scalit_hx_device (precision SCALIT_PREC_FP64, on double vectors) or
+ * scalit_hx_f32_device (SCALIT_PREC_FP32, float vectors) to nvec <= 64
+ * vectors, with a CUDA event on the context's stream before every level's
+ * launch; ms[level - 1] receives each level's average duration in ms. */
+int scalit_hx_level_times(scalit_ctx *ctx, int precision, int ntype, int nvec, const void *dX, void *dY,
+                          int reps, float *ms);
 /* One level of MYHX on device vectors: Y (+)= H_level X (level is 1-based;
  * a dependent level is scaled by its DEP factors, H1X_DEP / H2X, hpx.f90:21-35;
  * otherwise H1X_XYZ, hpx.f90:5-18).  accumulate != 0 adds into Y. */
@@ -465,6 +472,17 @@ void hosbdiag_(const int *bjmax, const double *bjtol, const int *blk, const int 
                const int *ndk, double *HOSB, double *VOSB, double *EIGVAL);
 void hosbdiag_seq_(const int *bjmax, const double *bjtol, const int *blk, const int *mak,
                    const int *ndk, double *HOSB, double *VOSB, double *EIGVAL, const int *id);
+/* HOSBDIAG_MPI (src/iterate/libiterate_mpi/diagmpi/hosbdiag_mpi.f90:5-96) on
+ * one rank: comm and id are ignored (the whole NDK stack is on the device);
+ * *ierr = 0 on success, 1 when the device step failed. */
+void hosbdiag_mpi_(const int *comm, const int *bjmax, const double *bjtol, const int *blk,
+                   const int *mak, const int *ndk, double *HOSB, double *VOSB, double *RES,
+                   int *ierr, const int *id);
+/* MJACOBI (src/iterate/libiterate/diag/jacobi.f90:2-83): one joint Jacobi
+ * rotation of the (P, Q) plane (1-based) of HOUT(NIN, NOUT, NOUT), in place;
+ * returns the rotation angle X.  The sums A, B, C and the rotation run on the
+ * device; the angle is taken on the host with the reference's branches. */
+double mjacobi_(const int *p, const int *q, const int *nout, const int *nin, double *HOUT);
 /* NORM_MPI / DOTPROD_MPI (src/libutil/parallel/p_base/vector_mpi.f90:8-27,110-124);
  * comm is ignored: one device holds the whole vector. */
 double norm_mpi_(const int *comm, const int *nin, const double *X, int *ierr);
@@ -505,6 +523,19 @@ int pist_conv_(const double *e0, const double *etol, const int *ntype, const int
                const double *X, const int *startcnt, const int *stepcnt, const int *stepeig,
                const int *m, const int *m_max, scalit_fortran_op h0x,
                scalit_fortran_linsolv linsolv, double *EIG, double *RES);
+/* pistH0 (src/iterate/libiterate/pist/pistHij.f90:70-125) and pistH0_MPI
+ * (src/iterate/libiterate_mpi/pist/pistHij_mpi.f90:83-190): the Krylov
+ * vectors m_low..m_high (from LinSolv and one modified Gram-Schmidt pass) and
+ * their HMAT columns, on the caller's VJ(N, M_HIGH) and HMAT(M_MAX, M_HIGH).
+ * Returns m_high, LinSolv's code (<= 0) when it failed, -J when the
+ * orthogonalisation failed at J, 0 for bad sizes.  *num2 (MPI form) receives
+ * the sum of LinSolv's codes.  Given scalit_hx0_ and scalit_osb_qmr_ the
+ * operators run on the module state without host staging. */
+int pisth0_(const int *n, const double *X, const int *m_max, const int *m_low, const int *m_high,
+            scalit_fortran_op h0x, scalit_fortran_linsolv linsolv, double *VJ, double *HMAT);
+int pisth0_mpi_(const int *myid, const int *rootid, const int *n, const double *X, const int *m_max,
+                const int *m_low, const int *m_high, scalit_fortran_op h0x,
+                scalit_fortran_linsolv linsolv, double *VJ, double *HMAT, int *num2);
 int pist_conv_mpi_(const int *myid, const int *rootid, const double *e0, const double *etol,
                    const int *ntype, const int *n, const double *X, const int *startcnt,
                    const int *stepcnt, const int *stepeig, const int *m, const int *m_max,

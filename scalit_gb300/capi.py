@@ -44,6 +44,8 @@ SIGNATURES = {
     "scalit_hx_device": (C.c_int, [_vp, C.c_int, C.c_int, _vp, _vp]),
     "scalit_hx_f32_device": (C.c_int, [_vp, C.c_int, C.c_int, _vp, _vp]),
     "scalit_level_device": (C.c_int, [_vp, C.c_int, C.c_int, _vp, _vp]),
+    "scalit_hx_level_times": (C.c_int, [_vp, C.c_int, C.c_int, C.c_int, _vp, _vp, C.c_int,
+                                        C.POINTER(C.c_float)]),
     "scalit_build_osb": (C.c_int, [_vp, C.c_int, C.c_double, _dp]),
     "scalit_build_times": (C.c_int, [_vp, _dp]),
     "scalit_selftest_wait": (C.c_int, [_vp, C.c_double]),
@@ -100,6 +102,8 @@ SIGNATURES = {
     "vtx_seq_": (None, [_ip, _ip, _ip, _dp, _dp]),
     "hosbdiag_": (None, [_ip, _dp, _ip, _ip, _ip, _dp, _dp, _dp]),
     "hosbdiag_seq_": (None, [_ip, _dp, _ip, _ip, _ip, _dp, _dp, _dp, _ip]),
+    "hosbdiag_mpi_": (None, [_ip, _ip, _dp, _ip, _ip, _ip, _dp, _dp, _dp, _ip, _ip]),
+    "mjacobi_": (C.c_double, [_ip, _ip, _ip, _ip, _dp]),
     "norm_mpi_": (C.c_double, [_ip, _ip, _dp, _ip]),
     "dotprod_mpi_": (C.c_double, [_ip, _ip, _dp, _dp, _ip]),
     "mgs_orth_": (C.c_int, [_ip, _dp, _ip, _dp]),
@@ -110,6 +114,8 @@ SIGNATURES = {
     "pist_conv_cx_": (C.c_int, [_dp, _dp, _ip, _ip, _dp, _ip, _ip, _ip, _ip, _ip, _vp, _vp, _dp, _dp]),
     "qmr_mpi_": (C.c_int, [_ip, _ip, _dp, _ip, _dp, _vp, _vp, _dp, _dp, _ip]),
     "pist_conv_": (C.c_int, [_dp, _dp, _ip, _ip, _dp, _ip, _ip, _ip, _ip, _ip, _vp, _vp, _dp, _dp]),
+    "pisth0_": (C.c_int, [_ip, _dp, _ip, _ip, _ip, _vp, _vp, _dp, _dp]),
+    "pisth0_mpi_": (C.c_int, [_ip, _ip, _ip, _dp, _ip, _ip, _ip, _vp, _vp, _dp, _dp, _ip]),
     "pist_conv_mpi_": (C.c_int, [_ip, _ip, _dp, _dp, _ip, _ip, _dp, _ip, _ip, _ip, _ip, _ip, _vp, _vp,
                                  _dp, _dp]),
     "scalit_fortran_device_": (None, [_ip]),
@@ -273,6 +279,15 @@ class Context:
 
     def level_device(self, level, dX, dY, accumulate=False):
         _check(self.lib.scalit_level_device(self.h, int(level), int(bool(accumulate)), _ptr(dX), _ptr(dY)))
+
+    def hx_level_times(self, dX, dY, nvec, reps=10, ntype=TA1):
+        """Average duration (ms) of each level's launch over reps H*X
+        applications to nvec device vectors (float64 or float32 tensors)."""
+        import torch
+        prec = PREC_FP64 if dX.dtype == torch.float64 else PREC_FP32
+        ms = (C.c_float * 20)()
+        _check(self.lib.scalit_hx_level_times(self.h, prec, ntype, nvec, _ptr(dX), _ptr(dY), reps, ms))
+        return [float(ms[i]) for i in range(len(self.sizes))]
 
     def hx_f32_device(self, dX, dY, nvec=1, ntype=TA1):
         _check(self.lib.scalit_hx_f32_device(self.h, int(ntype), int(nvec), _ptr(dX), _ptr(dY)))

@@ -352,6 +352,34 @@ int scalit_hx_device(scalit_ctx *c, int ntype, int nvec, const double *dX, doubl
     return hx_many<double>(c, ntype, nvec, dX, dY);
 }
 
+int scalit_hx_level_times(scalit_ctx *c, int precision, int ntype, int nvec, const void *dX, void *dY, int reps,
+                          float *ms)
+{
+    CTX_CHECK(c);
+    if (!ms || reps < 1 || nvec < 1 || nvec > 64) { set_error("level timing needs ms, reps >= 1, 1 <= nvec <= 64"); return SCALIT_EINVAL; }
+    if (precision != SCALIT_PREC_FP64 && precision != SCALIT_PREC_FP32) { set_error("unknown precision %d", precision); return SCALIT_EINVAL; }
+    const int nl = c->L.nlev;
+    cudaEvent_t ev[SCALIT_FMAX + 1];
+    for (int l = 0; l <= nl; ++l) SC_CUDA(cudaEventCreate(&ev[l]));
+    for (int l = 0; l < nl; ++l) ms[l] = 0.0f;
+    int rc = 0;
+    c->lev_ev = ev;
+    for (int r = 0; r < reps && !rc; ++r) {
+        rc = precision == SCALIT_PREC_FP64
+                 ? hx_many<double>(c, ntype, nvec, static_cast<const double *>(dX), static_cast<double *>(dY))
+                 : hx_many<float>(c, ntype, nvec, static_cast<const float *>(dX), static_cast<float *>(dY));
+        if (!rc && cudaEventSynchronize(ev[nl]) != cudaSuccess) { set_error("level timing failed"); rc = SCALIT_ECUDA; }
+        for (int l = 0; l < nl && !rc; ++l) {
+            float t = 0.0f;
+            if (cudaEventElapsedTime(&t, ev[l], ev[l + 1]) != cudaSuccess) { set_error("level timing failed"); rc = SCALIT_ECUDA; }
+            ms[l] += t / reps;
+        }
+    }
+    c->lev_ev = nullptr;
+    for (int l = 0; l <= nl; ++l) cudaEventDestroy(ev[l]);
+    return rc;
+}
+
 int scalit_level_device(scalit_ctx *c, int level, int accumulate, const double *dX, double *dY)
 {
     CTX_CHECK(c);
@@ -1093,26 +1121,31 @@ void vtx_seq_(const int *nin, const int *nout, const int *blk, const double *VOU
     vtx_(nin, nout, blk, VOUT, X);
 }
 
-static void hosbdiag_host(int bjmax, double bjtol, int blk, int mak, int ndk, double *HOSB, double *VOSB,
-                          double *EIG)
+static int hosbdiag_host(int bjmax, double bjtol, int blk, int mak, int ndk, double *HOSB, double *VOSB,
+                         double *EIG)
 {
     scalit_ctx *c = scratch();
-    if (!c) return;
+    if (!c) return SCALIT_ECUDA;
     const i64 nh = (i64)ndk * mak * mak * blk, nv = (i64)mak * mak * blk, ne = (i64)ndk * mak * blk;
     Scoped sb(c->stream);
     double *dH = sb.get<double>(nh), *dV = sb.get<double>(nv), *dE = sb.get<double>(ne);
-    if (!dH || !dV || !dE) { report("hosbdiag", SCALIT_ENOMEM); return; }
+    if (!dH || !dV || !dE) { report("hosbdiag", SCALIT_ENOMEM); return SCALIT_ENOMEM; }
     cudaMemcpyAsync(dH, HOSB, sizeof(double) * nh, cudaMemcpyHostToDevice, c->stream);
     double stats[5];
     int rc = hosbdiag_device(c, bjmax, bjtol, blk, mak, ndk, dH, dV, dE, stats, c->stream);
-    if (rc) { report("hosbdiag", rc); return; }
+    if (rc) { report("hosbdiag", rc); return rc; }
     cudaMemcpyAsync(HOSB, dH, sizeof(double) * nh, cudaMemcpyDeviceToHost, c->stream);
     cudaMemcpyAsync(VOSB, dV, sizeof(double) * nv, cudaMemcpyDeviceToHost, c->stream);
     cudaMemcpyAsync(EIG, dE, sizeof(double) * ne, cudaMemcpyDeviceToHost, c->stream);
-    cudaStreamSynchronize(c->stream);
+    if (cudaStreamSynchronize(c->stream) != cudaSuccess) {
+        set_error("hosbdiag: download failed");
+        report("hosbdiag", SCALIT_ECUDA);
+        return SCALIT_ECUDA;
+    }
     // the reference's summary lines (hosbdiag.f90:67-71)
     printf(" Aver. # of Sweeps:%10.5f.    Aver. OffDiag/Diag:%10.6f\n", stats[4] / blk, stats[2] / stats[4]);
     printf(" Jacobi Effi: Min:%10.5f,   Max:%10.5f,  Mean:%10.5f\n", stats[0], stats[1], stats[2] / blk);
+    return 0;
 }
 
 void hosbdiag_(const int *bjmax, const double *bjtol, const int *blk, const int *mak, const int *ndk,
@@ -1126,6 +1159,44 @@ void hosbdiag_seq_(const int *bjmax, const double *bjtol, const int *blk, const 
 {
     (void)id;
     hosbdiag_host(*bjmax, *bjtol, *blk, *mak, *ndk, HOSB, VOSB, EIGVAL);
+}
+
+// HOSBDIAG_MPI (src/iterate/libiterate_mpi/diagmpi/hosbdiag_mpi.f90:5-96) on
+// one rank: the whole NDK stack is local, so it is HosbDiag with IERR = 0.
+void hosbdiag_mpi_(const int *comm, const int *bjmax, const double *bjtol, const int *blk, const int *mak,
+                   const int *ndk, double *HOSB, double *VOSB, double *RES, int *ierr, const int *id)
+{
+    (void)comm; (void)id;
+    const int rc = hosbdiag_host(*bjmax, *bjtol, *blk, *mak, *ndk, HOSB, VOSB, RES);
+    if (ierr) *ierr = rc ? 1 : 0;
+}
+
+// MJACOBI (src/iterate/libiterate/diag/jacobi.f90:2-83): one joint rotation of
+// the (P, Q) plane of HOUT(NIN, NOUT, NOUT) in place; returns the angle.
+double mjacobi_(const int *p, const int *q, const int *nout, const int *nin, double *HOUT)
+{
+    std::lock_guard<std::mutex> lk(g_fmu);
+    const int P = *p, Q = *q, no = *nout, ni = *nin;
+    if (P < 1 || Q < 1 || P > no || Q > no || P == Q || ni < 1) {
+        set_error("mjacobi: plane (%d, %d) outside 1..%d or nin %d", P, Q, no, ni);
+        report("mjacobi", SCALIT_EINVAL);
+        return 0.0;
+    }
+    scalit_ctx *c = scratch();
+    if (!c) return 0.0;
+    const i64 n = (i64)ni * no * no;
+    Scoped sb(c->stream);
+    double *dH = sb.get<double>(n), *dabc = sb.get<double>(4);
+    if (!dH || !dabc) { report("mjacobi", SCALIT_ENOMEM); return 0.0; }
+    double x = 0.0;
+    int rc = cudaMemcpyAsync(dH, HOUT, sizeof(double) * (size_t)n, cudaMemcpyHostToDevice, c->stream) == cudaSuccess
+                 ? 0 : SCALIT_ECUDA;
+    if (!rc) rc = mjacobi_device(P, Q, no, ni, dH, dabc, &x, c->stream);
+    if (!rc && (cudaMemcpyAsync(HOUT, dH, sizeof(double) * (size_t)n, cudaMemcpyDeviceToHost, c->stream) != cudaSuccess ||
+                cudaStreamSynchronize(c->stream) != cudaSuccess))
+        rc = SCALIT_ECUDA;
+    if (rc) { report("mjacobi", rc); return 0.0; }
+    return x;
 }
 
 static double dot_host(int n, const double *X, const double *Y, int *ierr)
@@ -1268,6 +1339,63 @@ int pist_conv_cx_(const double *e0, const double *etol, const int *ntype, const 
                   scalit_fortran_op h0x, scalit_fortran_linsolv linsolv, double *EIG, double *RES)
 {
     return pist_complex_fortran(e0, etol, ntype, n, X, startcnt, stepcnt, stepeig, m, m_max, h0x, linsolv, EIG, RES, 1);
+}
+
+// pistH0 (src/iterate/libiterate/pist/pistHij.f90:70-125) and pistH0_MPI
+// (src/iterate/libiterate_mpi/pist/pistHij_mpi.f90:83-190): one block of
+// Krylov vectors m_low..m_high and their HMAT columns, with the caller's
+// callbacks, on the caller's VJ(N, M_HIGH) and HMAT(M_MAX, M_HIGH).
+static int pisth0_fortran(int n, const double *X, int m_max, int m_low, int m_high, scalit_fortran_op h0x,
+                          scalit_fortran_linsolv linsolv, double *VJ, double *HMAT, bool mpi, int *num2)
+{
+    // no lock held here: the callbacks may be this library's own externals
+    if (num2) *num2 = 0;
+    if (m_low < 1 || m_low >= m_high || m_high > m_max || n < 1) return 0;
+    const bool own = (h0x == scalit_hx0_ && linsolv == scalit_osb_qmr_ && g_fctx && g_fctx->L.N == n);
+    scalit_ctx *c = own ? g_fctx : scratch();
+    if (!c) return 0;
+    if (cudaSetDevice(c->device) != cudaSuccess) return 0;
+    int ret = 0, rc = 0;
+    if (own) {
+        // the module's own operators stay on the device: HX0 = MYHX(TA0), LinSolv = OSB_QMR
+        struct OwnOps : PistOps {
+            scalit_ctx *c;
+            int h0x(const double *dX, double *dY) override { return scalit_hx_device(c, SCALIT_TA0, 1, dX, dY); }
+            int linsolv(const double *dB, double *dX, int *num) override
+            {
+                double res = 0.0;
+                int it = 0, code = 0;
+                const int r = scalit_qmr_device_ex(c, g_fq.ntype, g_fq.qmrmax, g_fq.tol, g_fq.precision, dB, dX,
+                                                   &code, &res, &it);
+                if (r) return r;
+                *num = code;
+                return 0;
+            }
+        } ops;
+        ops.c = c;
+        rc = pisth0_host(c, n, X, m_max, m_low, m_high, ops, VJ, HMAT, mpi, num2, &ret);
+    } else {
+        HostPistOps ops;
+        ops.c = c; ops.n = n; ops.fh0x = h0x; ops.flin = linsolv;
+        ops.hin.resize(n); ops.hout.resize(n);
+        rc = pisth0_host(c, n, X, m_max, m_low, m_high, ops, VJ, HMAT, mpi, num2, &ret);
+    }
+    if (rc) { report(mpi ? "pisth0_mpi" : "pisth0", rc); return 0; }
+    return ret;
+}
+
+int pisth0_(const int *n, const double *X, const int *m_max, const int *m_low, const int *m_high,
+            scalit_fortran_op h0x, scalit_fortran_linsolv linsolv, double *VJ, double *HMAT)
+{
+    return pisth0_fortran(*n, X, *m_max, *m_low, *m_high, h0x, linsolv, VJ, HMAT, false, nullptr);
+}
+
+int pisth0_mpi_(const int *myid, const int *rootid, const int *n, const double *X, const int *m_max,
+                const int *m_low, const int *m_high, scalit_fortran_op h0x, scalit_fortran_linsolv linsolv,
+                double *VJ, double *HMAT, int *num2)
+{
+    (void)myid; (void)rootid;
+    return pisth0_fortran(*n, X, *m_max, *m_low, *m_high, h0x, linsolv, VJ, HMAT, true, num2);
 }
 
 int pist_conv_(const double *e0, const double *etol, const int *ntype, const int *n, const double *X,

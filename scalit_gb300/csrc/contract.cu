@@ -304,6 +304,7 @@ int hx_batch(const scalit_ctx *c, const T *X, T *Y, int nvec, T shift, T alpha, 
         first = 1;
     }
     for (int l = 0; l < L.nlev; ++l) {
+        if (c->lev_ev) cudaEventRecord(c->lev_ev[l], s);
         const bool fuse_diag = (l == 0 && !first);
         if constexpr (std::is_same<T, double>::value) {
             if (c->fp64_mode == SCALIT_FP64_TENSOR && tc_usable(c, l)) {
@@ -324,6 +325,7 @@ int hx_batch(const scalit_ctx *c, const T *X, T *Y, int nvec, T shift, T alpha, 
                             fuse_diag ? RES : nullptr, shift, alpha, gate, s, nvec, shiftv, vgate, vstride);
         if (rc) return rc;
     }
+    if (c->lev_ev) cudaEventRecord(c->lev_ev[L.nlev], s);
     return 0;
 }
 

@@ -114,6 +114,9 @@ struct scalit_ctx {
     // digit planes of the preconditioner's rotations, levels >= 2: [level][VX, VTX]
     TcLevelData pxtc[SCALIT_FMAX][2];
     int *tc_err = nullptr;
+    // Measurement aid: when set, hx_batch records lev_ev[l] before level l's
+    // launch and lev_ev[nlev] after the last (scalit_hx_level_times).
+    cudaEvent_t *lev_ev = nullptr;
     // Captured QMR iteration batches (one per precision); `gen` changes whenever
     // anything baked into the captured launches changes (shift, preconditioner,
     // engine, workspace), which invalidates them.
@@ -251,6 +254,7 @@ int pist_sx_host(scalit_ctx *c, i64 n, double e0, double etol, const double *X0,
 // ------------------------------------------------------------- OSB build --
 int osb_build(scalit_ctx *c, int bjmax, double bjtol, double *stats);
 // HosbDiag on a device HOSB(ndk, mak, mak, blk): fills VOSB and EIGVAL.
+int mjacobi_device(int P, int Q, int nout, int nin, double *dH, double *dabc, double *angle, cudaStream_t s);
 int hosbdiag_device(scalit_ctx *c, int bjmax, double bjtol, int blk, int mak, int ndk,
                     double *HOSB, double *VOSB, double *EIG, double *stats5, cudaStream_t s);
 
@@ -330,6 +334,8 @@ struct PistBasisOut { int *cnt = nullptr; double *ritz = nullptr, *hmat = nullpt
 int pist_core(scalit_ctx *c, i64 N, const scalit_pist_params *p, const double *dx0, PistOps &ops,
               double *eig, double *res, scalit_pist_info *info, double *vectors_host = nullptr,
               const PistBasisOut *basis = nullptr, double *resid = nullptr);
+int pisth0_host(scalit_ctx *c, i64 N, const double *X, int m_max, int m_low, int m_high, PistOps &ops, double *VJ,
+                double *HMAT, bool mpi, int *num2, int *ret);
 int pist_ctx(scalit_ctx *c, const scalit_pist_params *p, const double *dx0, double *eig,
              double *res, scalit_pist_info *info, double *vectors_host = nullptr,
              const PistBasisOut *basis = nullptr, double *resid = nullptr);

@@ -798,6 +798,103 @@ int hosbdiag_device(scalit_ctx *c, int bjmax, double bjtol, int blk, int mak, in
     return rc;
 }
 
+// MJACOBI (src/iterate/libiterate/diag/jacobi.f90:2-83) as the external
+// mjacobi_: one joint rotation of the (P, Q) plane (1-based) of all nin
+// stacked nout x nout matrices HOUT(nin, nout, nout) on the device.  One CTA
+// forms A = sum o^2, B = 2 sum o d, C = sum d^2 (o = HOUT(:, P, Q),
+// d = (HOUT(:, P, P) - HOUT(:, Q, Q)) / 2) in a fixed order; the host takes the
+// angle X from them with the reference's branches (atan of the host C
+// library) and the rotation kernel updates the P and Q rows and columns with
+// the reference's formulas.  *angle receives X, MJACOBI's result.
+static constexpr int kMjT = 1024;
+__global__ void __launch_bounds__(kMjT)
+mjacobi_abc_kernel(int p, int q, int nout, int nin, const double *__restrict__ H, double *__restrict__ abc)
+{
+    const double *hpp = H + (i64)nin * (p + (i64)nout * p), *hqq = H + (i64)nin * (q + (i64)nout * q);
+    const double *hpq = H + (i64)nin * (p + (i64)nout * q);
+    double a = 0.0, b = 0.0, cc = 0.0;
+    for (int k = threadIdx.x; k < nin; k += kMjT) {
+        const double o = hpq[k], d = 0.5 * hpp[k] - 0.5 * hqq[k];
+        a = fma(o, o, a);
+        b = fma(o, d, b);
+        cc = fma(d, d, cc);
+    }
+    __shared__ double red[3][kMjT / 32];
+    #pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        a += __shfl_xor_sync(0xffffffffu, a, o);
+        b += __shfl_xor_sync(0xffffffffu, b, o);
+        cc += __shfl_xor_sync(0xffffffffu, cc, o);
+    }
+    if ((threadIdx.x & 31) == 0) {
+        red[0][threadIdx.x >> 5] = a;
+        red[1][threadIdx.x >> 5] = b;
+        red[2][threadIdx.x >> 5] = cc;
+    }
+    __syncthreads();
+    if (threadIdx.x < 3) {
+        double t = 0.0;
+        for (int w = 0; w < kMjT / 32; ++w) t += red[threadIdx.x][w];
+        abc[threadIdx.x] = (threadIdx.x == 1) ? 2.0 * t : t;
+    }
+}
+
+__global__ void mjacobi_rotate_kernel(int p, int q, int nout, int nin, double cs, double sn, double *__restrict__ H)
+{
+    const double c2 = cs * cs, s2 = sn * sn, sc = sn * cs;
+    const i64 total = (i64)nin * nout;
+    for (i64 e = blockIdx.x * (i64)blockDim.x + threadIdx.x; e < total; e += (i64)gridDim.x * blockDim.x) {
+        const int k = (int)(e % nin), r = (int)(e / nin);
+        if (r == p) {
+            // the intersection block (p, p), (q, q), (p, q), (q, p)
+            double *hpp = H + (i64)nin * (p + (i64)nout * p) + k, *hqq = H + (i64)nin * (q + (i64)nout * q) + k;
+            double *hpq = H + (i64)nin * (p + (i64)nout * q) + k, *hqp = H + (i64)nin * (q + (i64)nout * p) + k;
+            const double o = *hpq, d = 0.5 * *hpp - 0.5 * *hqq;
+            const double np_ = c2 * *hpp + s2 * *hqq - 2 * sc * o;
+            const double nq_ = c2 * *hqq + s2 * *hpp + 2 * sc * o;
+            const double nqp = (c2 - s2) * o + 2 * sc * d;
+            *hpp = np_;
+            *hqq = nq_;
+            *hpq = nqp;
+            *hqp = nqp;
+        } else if (r != q) {
+            double *hrp = H + (i64)nin * (r + (i64)nout * p) + k, *hrq = H + (i64)nin * (r + (i64)nout * q) + k;
+            double *hpr = H + (i64)nin * (p + (i64)nout * r) + k, *hqr = H + (i64)nin * (q + (i64)nout * r) + k;
+            const double np_ = cs * *hrp - sn * *hrq;
+            const double nq_ = cs * *hrq + sn * *hrp;
+            *hrp = np_;
+            *hpr = np_;
+            *hrq = nq_;
+            *hqr = nq_;
+        }
+    }
+}
+
+int mjacobi_device(int P, int Q, int nout, int nin, double *dH, double *dabc, double *angle, cudaStream_t s)
+{
+    const double PIE = 3.14159265358979323846264338328;
+    const int p = P - 1, q = Q - 1;
+    mjacobi_abc_kernel<<<1, kMjT, 0, s>>>(p, q, nout, nin, dH, dabc);
+    SC_CHECK_LAUNCH();
+    double abc[3];
+    SC_CUDA(cudaMemcpyAsync(abc, dabc, sizeof(abc), cudaMemcpyDeviceToHost, s));
+    SC_CUDA(cudaStreamSynchronize(s));
+    const double A = abc[0], B = abc[1], C = abc[2];
+    double X;
+    if (A == C) {
+        X = (B == 0.0) ? 0.0 : -std::copysign(PIE / 8.0, B);
+    } else {
+        X = std::atan(B / (A - C)) / 4.0;
+        if (A > C) X = (X < 0.0) ? X + PIE / 4.0 : X - PIE / 4.0;
+    }
+    const i64 total = (i64)nin * nout;
+    const int grid = (int)std::max<i64>(1, std::min<i64>((total + 255) / 256, 152 * 8));
+    mjacobi_rotate_kernel<<<grid, 256, 0, s>>>(p, q, nout, nin, std::cos(X), std::sin(X), dH);
+    SC_CHECK_LAUNCH();
+    *angle = X;
+    return 0;
+}
+
 int osb_build(scalit_ctx *c, int bjmax, double bjtol, double *stats)
 {
     const Layout &L = c->L;

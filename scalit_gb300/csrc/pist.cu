@@ -906,6 +906,145 @@ int pist_core(scalit_ctx *c, i64 N, const scalit_pist_params *p, const double *d
     return rc ? rc : status;
 }
 
+// pistH0 (pistHij.f90:70-125) / pistH0_MPI (pistHij_mpi.f90:83-190) on the
+// caller's host arrays, as the Fortran externals pisth0_ / pisth0_mpi_ need:
+// VJ(N, m_high) and HMAT(m_max, m_high), column-major, both in and out.
+// Columns 1..m_low-1 of VJ (the earlier basis) are uploaded once; the new
+// columns come from LinSolv and the reference's single modified Gram-Schmidt
+// pass (MGS_ORTH, or MGS_ORTH_MPI with mpi = true: no initial norm test), in
+// its order; column J of HMAT is V^T (H0 v_J), written with its mirror in the
+// reference's order (the later column's value wins), for J = m_low..m_high.
+// *num2 (may be null) receives the sum of the linear solver's codes, as
+// pistH0_MPI's trailing argument.  Returns m_high, the solver's code (<= 0)
+// when it failed, -J when MGS_ORTH failed at J, or 0 for bad sizes / a zero
+// start vector; columns written before a failure are copied back.
+int pisth0_host(scalit_ctx *c, i64 N, const double *X, int m_max, int m_low, int m_high, PistOps &ops, double *VJ,
+                double *HMAT, bool mpi, int *num2, int *ret)
+{
+    *ret = 0;
+    if (num2) *num2 = 0;
+    if (m_low < 1 || m_low >= m_high || m_high > m_max || N < 1) return 0;
+    cudaStream_t s = c->stream;
+    const int nchunk = (int)((N + kGemvChunk - 1) / kGemvChunk);
+    const int gr = egrid(N);
+    double *dV = nullptr, *W = nullptr, *D = nullptr, *part = nullptr, *hcol = nullptr;
+    unsigned int *counter = nullptr;
+    auto fail_alloc = [&]() {
+        cudaGetLastError();
+        set_error("pistH0 workspace (%d vectors of %lld points) does not fit", m_high + 1, N);
+        return SCALIT_ENOMEM;
+    };
+    int rc = 0;
+    if (cudaMallocAsync(&dV, sizeof(double) * (size_t)N * m_high, s) != cudaSuccess) return fail_alloc();
+    if (cudaMallocAsync(&W, sizeof(double) * (size_t)N, s) != cudaSuccess ||
+        cudaMallocAsync(&D, sizeof(double) * ((size_t)m_high + 8), s) != cudaSuccess ||
+        cudaMallocAsync(&part, sizeof(double) * std::max((size_t)nchunk * m_high, (size_t)kT * 152 * 4), s) != cudaSuccess ||
+        cudaMallocAsync(&hcol, sizeof(double) * (size_t)m_high * (m_high - m_low + 1), s) != cudaSuccess ||
+        cudaMallocAsync(&counter, sizeof(unsigned int), s) != cudaSuccess)
+        rc = fail_alloc();
+    auto vcol = [&](int J1) { return dV + (i64)(J1 - 1) * N; };
+    double *dnorm = D + m_high;
+    int m_start = 1, done_high = 0;   // columns 1..done_high of dV hold the caller's or new vectors
+    if (!rc) rc = cudaMemsetAsync(counter, 0, sizeof(unsigned int), s) == cudaSuccess ? 0 : SCALIT_ECUDA;
+    if (!rc && m_low == 1) {
+        double *dx = W;   // the start vector, staged in W
+        if (cudaMemcpyAsync(dx, X, sizeof(double) * (size_t)N, cudaMemcpyHostToDevice, s) != cudaSuccess) {
+            rc = SCALIT_ECUDA;
+        } else {
+            mgs_kernel<<<gr, kT, 0, s>>>(N, dx, nullptr, nullptr, nullptr, dnorm, part, counter);
+            double h = 0.0;
+            if (cudaMemcpyAsync(&h, dnorm, sizeof(double), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+                cudaStreamSynchronize(s) != cudaSuccess) {
+                rc = SCALIT_ECUDA;
+            } else if (h != 0.0) {
+                copy_scaled_kernel<<<gr, kT, 0, s>>>(N, dx, vcol(1), dnorm);
+                done_high = 1;
+                *ret = m_high;
+            }
+        }
+    } else if (!rc) {
+        m_start = m_low - 1;
+        if (cudaMemcpyAsync(dV, VJ, sizeof(double) * (size_t)N * (m_low - 1), cudaMemcpyHostToDevice, s) != cudaSuccess)
+            rc = SCALIT_ECUDA;
+        done_high = m_low - 1;
+        *ret = m_high;
+    }
+    if (rc == SCALIT_ECUDA) set_error("pistH0 upload failed");
+    int sum = 0;
+    for (int J = m_start; !rc && *ret == m_high && J <= m_high - 1; ++J) {
+        int num = 0;
+        rc = ops.linsolv(vcol(J), W, &num);
+        if (rc) break;
+        sum += num;
+        if (num <= 0) { *ret = num; break; }
+        // MGS_ORTH(N, WJ, J, VJ): column J+1 = W less its projections, in order
+        double *v = vcol(J + 1);
+        if (cudaMemcpyAsync(v, W, sizeof(double) * (size_t)N, cudaMemcpyDeviceToDevice, s) != cudaSuccess) {
+            set_error("pistH0 copy failed");
+            rc = SCALIT_ECUDA;
+            break;
+        }
+        mgs_kernel<<<gr, kT, 0, s>>>(N, v, nullptr, nullptr, nullptr, dnorm, part, counter);
+        for (int i = 1; i <= J; ++i)
+            mgs_kernel<<<gr, kT, 0, s>>>(N, v, (i > 1) ? vcol(i - 1) : nullptr, D + (i > 1 ? i - 2 : 0), vcol(i),
+                                         D + (i - 1), part, counter);
+        mgs_kernel<<<gr, kT, 0, s>>>(N, v, vcol(J), D + (J - 1), nullptr, dnorm + 1, part, counter);
+        if (cudaGetLastError() != cudaSuccess) { set_error("pistH0 launch failed"); rc = SCALIT_ECUDA; break; }
+        double h[2];
+        if (cudaMemcpyAsync(h, dnorm, 2 * sizeof(double), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+            cudaStreamSynchronize(s) != cudaSuccess) {
+            set_error("pistH0 norm read failed");
+            rc = SCALIT_ECUDA;
+            break;
+        }
+        done_high = J + 1;
+        if ((!mpi && h[0] == 0.0) || h[1] == 0.0) { *ret = -J; break; }
+        scale_inv_sqrt_kernel<<<gr, kT, 0, s>>>(N, v, dnorm + 1);
+    }
+    if (num2) *num2 = sum;
+    if (!rc && *ret == m_high) {
+        for (int J = m_low; J <= m_high && !rc; ++J) {
+            rc = ops.h0x(vcol(J), W);
+            if (rc) break;
+            gemvt_partial_kernel<<<dim3(nchunk, m_high), kT, 0, s>>>(N, m_high, dV, W, part, nchunk);
+            gemvt_vec_kernel<<<(m_high + 127) / 128, 128, 0, s>>>(m_high, nchunk, part,
+                                                                 hcol + (i64)(J - m_low) * m_high);
+            if (cudaGetLastError() != cudaSuccess) { set_error("pistH0 launch failed"); rc = SCALIT_ECUDA; }
+        }
+        if (!rc) {
+            std::vector<double> h((size_t)m_high * (m_high - m_low + 1));
+            if (cudaMemcpyAsync(h.data(), hcol, sizeof(double) * h.size(), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+                cudaStreamSynchronize(s) != cudaSuccess) {
+                set_error("pistH0 HMAT read failed");
+                rc = SCALIT_ECUDA;
+            } else {
+                for (int J = m_low; J <= m_high; ++J)
+                    for (int I = 1; I <= m_high; ++I) {
+                        const double v = h[(size_t)(J - m_low) * m_high + (I - 1)];
+                        HMAT[(I - 1) + (i64)m_max * (J - 1)] = v;
+                        HMAT[(J - 1) + (i64)m_max * (I - 1)] = v;
+                    }
+            }
+        }
+    }
+    // the columns this call wrote: 1 (m_low == 1) or m_low.., up to the last one formed
+    const int first = (m_low == 1) ? 1 : m_low;
+    if (!rc && done_high >= first &&
+        cudaMemcpyAsync(VJ + (i64)(first - 1) * N, vcol(first), sizeof(double) * (size_t)N * (done_high - first + 1),
+                        cudaMemcpyDeviceToHost, s) != cudaSuccess) {
+        set_error("pistH0 basis download failed");
+        rc = SCALIT_ECUDA;
+    }
+    if (dV) cudaFreeAsync(dV, s);
+    if (W) cudaFreeAsync(W, s);
+    if (D) cudaFreeAsync(D, s);
+    if (part) cudaFreeAsync(part, s);
+    if (hcol) cudaFreeAsync(hcol, s);
+    if (counter) cudaFreeAsync(counter, s);
+    if (cudaStreamSynchronize(s) != cudaSuccess && !rc) { set_error("pistH0 failed on the device"); rc = SCALIT_ECUDA; }
+    return rc;
+}
+
 // Device-resident operators of the context: HX0 = MYHX(TA0), LinSolv = OSB_QMR.
 struct CtxOps : PistOps {
     scalit_ctx *c;

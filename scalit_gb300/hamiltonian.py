@@ -293,3 +293,60 @@ def dense_hamiltonian(p: Problem, shift: float = 0.0) -> np.ndarray:
     H += np.diag(np.tile(p.DEP, n_t)) @ np.kron(Kt, np.eye(n_r * n_R))
     H += np.diag(p.RES - shift)
     return H
+
+
+@dataclasses.dataclass
+class NdvrProblem:
+    """A problem in the sNDVR form: the outermost (theta) layer is given as
+    per-point matrices OUTH(n_r n_R, n_theta, n_theta) instead of a level
+    matrix, as the JA3 H0GM output (src/ham/ja3/module/ja3.hgmij:6-62) feeds
+    H3X (src/libutil/serial/base/matrix.f90:188-203)."""
+
+    sizes: tuple
+    dep: tuple
+    H0: np.ndarray      # K_r, K_R only (the outer level has no H0 block)
+    RES: np.ndarray     # the diagonal kept outside OUTH
+    DEP: np.ndarray     # empty: no dependent level
+    OUTH: np.ndarray    # (n_r n_R) x n_theta x n_theta, column-major, point index fastest
+
+    @property
+    def N(self) -> int:
+        return int(np.prod(self.sizes))
+
+
+def ndvr_problem(p: Problem, coupling: float = 1e-4, seed: int = 0) -> NdvrProblem:
+    """The same Hamiltonian with its angular layer moved into per-point
+    matrices: OUTH(a, :, :) = c(a) K_theta + diag(V(a, :)) + coupling * S_a,
+    S_a a seeded symmetric matrix per (r, R) point (a per-point angular term
+    no level matrix can express).  RES is zero, since V sits inside OUTH: the
+    outer level's block-Jacobi blocks are then OUTH itself, as myDiagInit
+    copies it (osb.diag.h:19-30)."""
+    n_r, n_R, n_t = p.sizes
+    nin = n_r * n_R
+    Kt = p.level_matrix(3)
+    c = p.DEP[:nin]
+    V = p.RES.reshape(nin, n_t, order="F")
+    rng = np.random.default_rng(seed)
+    S = rng.standard_normal((nin, n_t, n_t))
+    S = 0.5 * (S + S.transpose(0, 2, 1))
+    A = c[:, None, None] * Kt[None, :, :] + coupling * S
+    A[:, np.arange(n_t), np.arange(n_t)] += V
+    OUTH = np.ascontiguousarray(A.transpose(2, 1, 0)).ravel()   # a fastest, then i, then j
+    H0 = np.concatenate([p.level_matrix(1).ravel(order="F"), p.level_matrix(2).ravel(order="F")])
+    return NdvrProblem(sizes=p.sizes, dep=(False, False, False), H0=H0, RES=np.zeros(p.N),
+                       DEP=np.zeros(0), OUTH=OUTH)
+
+
+def dense_ndvr(q: NdvrProblem) -> np.ndarray:
+    """Explicit N x N matrix of an sNDVR problem (small problems only)."""
+    n_r, n_R, n_t = q.sizes
+    nin = n_r * n_R
+    Kr = q.H0[:n_r * n_r].reshape(n_r, n_r, order="F")
+    KR = q.H0[n_r * n_r:].reshape(n_R, n_R, order="F")
+    H = np.kron(np.eye(n_t), np.kron(np.eye(n_R), Kr)) + np.kron(np.eye(n_t), np.kron(KR, np.eye(n_r)))
+    A = q.OUTH.reshape(n_t, n_t, nin).transpose(2, 1, 0)      # A[a, i, j]
+    for i in range(n_t):
+        for j in range(n_t):
+            H[i * nin:(i + 1) * nin, j * nin:(j + 1) * nin] += np.diag(A[:, i, j])
+    H += np.diag(q.RES)
+    return H

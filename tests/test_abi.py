@@ -38,7 +38,8 @@ def test_every_header_symbol_bound(lib):
 
 def test_fortran_names_are_lowercase_underscored():
     for n in ("h1x_xyz_", "h1x_dep_", "vx_", "vtx_", "hosbdiag_", "qmr_", "qmr_mpi_", "pist_conv_",
-              "pist_conv_mpi_", "mgs_orth_", "norm_mpi_", "dotprod_mpi_"):
+              "pist_conv_mpi_", "mgs_orth_", "norm_mpi_", "dotprod_mpi_", "pisth0_", "pisth0_mpi_",
+              "hosbdiag_mpi_", "mjacobi_"):
         assert n in capi.SIGNATURES
 
 

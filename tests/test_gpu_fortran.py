@@ -98,6 +98,130 @@ def test_hosbdiag(lib, orc):
     del p
 
 
+def test_hosbdiag_mpi(lib, orc):
+    """HOSBDIAG_MPI on one rank equals HosbDiag (hosbdiag_mpi.f90:5-96), IERR = 0."""
+    blk, mak, ndk = 3, 5, 40
+    rng = np.random.default_rng(21)
+    H1 = rng.standard_normal((mak, mak))
+    H1 = ((H1 + H1.T) / 2).ravel(order="F")
+    res = rng.standard_normal(ndk * mak * blk)
+    hosb = np.zeros(ndk * mak * mak * blk)
+    orc.lib().orc_hosbinit_xyz(blk, mak, ndk, orc._p(H1), orc._p(res), orc._p(hosb))
+    h_ref, v_ref, e_ref = hosb.copy(), np.zeros(mak * mak * blk), np.zeros(ndk * mak * blk)
+    orc.lib().orc_hosbdiag(20, 1e-8, blk, mak, ndk, orc._p(h_ref), orc._p(v_ref), orc._p(e_ref), None, None)
+    h, v, e = hosb.copy(), np.zeros_like(v_ref), np.zeros_like(e_ref)
+    ierr = I(-5)
+    lib.hosbdiag_mpi_(ref(I(0)), ref(I(20)), ref(D(1e-8)), ref(I(blk)), ref(I(mak)), ref(I(ndk)), dp(h), dp(v),
+                      dp(e), ref(ierr), ref(I(0)))
+    assert ierr.value == 0
+    assert rel(e, e_ref) < 1e-12
+    assert rel(v, v_ref) < 1e-10
+
+
+@pytest.mark.parametrize("p,q,nout,nin", [(1, 2, 4, 1), (2, 5, 6, 300), (3, 1, 5, 7), (4, 4 + 3, 9, 25600)])
+def test_mjacobi(lib, orc, p, q, nout, nin):
+    """MJACOBI (jacobi.f90:2-83): the rotated stack and the returned angle equal the oracle's."""
+    rng = np.random.default_rng(p * 10 + q)
+    H = np.zeros((nin, nout, nout), order="F")
+    for a in range(nin):
+        m = rng.standard_normal((nout, nout))
+        H[a] = (m + m.T) / 2
+    flat = np.asfortranarray(H).ravel(order="F").copy()
+    want = flat.copy()
+    work = np.zeros(2 * nin)
+    x_ref = orc.lib().orc_mjacobi(p, q, nout, nin, orc._p(want), orc._p(work))
+    x = lib.mjacobi_(ref(I(p)), ref(I(q)), ref(I(nout)), ref(I(nin)), dp(flat))
+    assert abs(x - x_ref) <= 1e-12 * max(1.0, abs(x_ref))
+    assert np.abs(flat - want).max() <= 1e-12 * np.abs(want).max()
+
+
+def _pisth0_case(n=400, m_max=12, seed=31):
+    rng = np.random.default_rng(seed)
+    a = rng.standard_normal((n, n))
+    H = (a + a.T) / 2 + np.diag(np.linspace(0.0, 3.0, n))
+    E0 = 0.7
+    x = rng.random(n)
+    return H, E0, x
+
+
+def _oracle_pisth0(H, E0, x, m_max, blocks):
+    """pistH0 (pistHij.f90:70-125) on the oracle's MGS_ORTH, block after block."""
+    n = x.size
+    VJ = np.zeros((n, m_max), order="F")
+    HM = np.zeros((m_max, m_max), order="F")
+    out = []
+    for m_low, m_high in blocks:
+        if m_low == 1:
+            VJ[:, 0] = x / np.sqrt(orc_dot(x, x))
+        for J in range(1 if m_low == 1 else m_low - 1, m_high):
+            w = np.linalg.solve(H - E0 * np.eye(n), VJ[:, J - 1])
+            assert ORC.mgs_orth(w, J, VJ)
+        for J in range(m_low, m_high + 1):
+            w = H @ VJ[:, J - 1]
+            for I_ in range(1, m_high + 1):
+                HM[I_ - 1, J - 1] = orc_dot(np.ascontiguousarray(VJ[:, I_ - 1]), w)
+                HM[J - 1, I_ - 1] = HM[I_ - 1, J - 1]
+        out.append(m_high)
+    return VJ, HM, out
+
+
+ORC = None
+
+
+def orc_dot(a, b):
+    return ORC.lib().orc_dot(a.size, ORC._p(np.ascontiguousarray(a)), ORC._p(np.ascontiguousarray(b)))
+
+
+@pytest.mark.parametrize("mpi", [False, True])
+def test_pisth0(lib, orc, mpi):
+    """pistH0 / pistH0_MPI with caller callbacks: the basis and HMAT of two
+    successive blocks (1..6, then 7..10) equal the oracle's."""
+    global ORC
+    ORC = orc
+    H, E0, x = _pisth0_case()
+    n, m_max = x.size, 12
+    nsolve = {"n": 0}
+
+    @FOP
+    def h0x(pn, px, py):
+        k = pn[0]
+        np.ctypeslib.as_array(py, shape=(k,))[:] = H @ np.ctypeslib.as_array(px, shape=(k,))
+
+    @FLIN
+    def linsolv(pn, pb, px, pres):
+        k = pn[0]
+        np.ctypeslib.as_array(px, shape=(k,))[:] = np.linalg.solve(H - E0 * np.eye(k),
+                                                                   np.ctypeslib.as_array(pb, shape=(k,)))
+        pres[0] = 0.0
+        nsolve["n"] += 1
+        return 3
+
+    blocks = [(1, 6), (7, 10)]
+    VJ_r, HM_r, out_r = _oracle_pisth0(H, E0, x, m_max, blocks)
+    VJ = np.zeros(n * m_max)
+    HM = np.zeros(m_max * m_max)
+    for (m_low, m_high), want in zip(blocks, out_r):
+        num2 = I(-1)
+        if mpi:
+            got = lib.pisth0_mpi_(ref(I(0)), ref(I(0)), ref(I(n)), dp(x), ref(I(m_max)), ref(I(m_low)),
+                                  ref(I(m_high)), C.cast(h0x, C.c_void_p), C.cast(linsolv, C.c_void_p), dp(VJ),
+                                  dp(HM), ref(num2))
+            first = 1 if m_low == 1 else m_low - 1
+            assert num2.value == 3 * (m_high - first)
+        else:
+            got = lib.pisth0_(ref(I(n)), dp(x), ref(I(m_max)), ref(I(m_low)), ref(I(m_high)),
+                              C.cast(h0x, C.c_void_p), C.cast(linsolv, C.c_void_p), dp(VJ), dp(HM))
+        assert got == want
+    V = VJ.reshape((n, m_max), order="F")[:, :10]
+    assert np.abs(V - VJ_r[:, :10]).max() < 1e-10
+    Hm = HM.reshape((m_max, m_max), order="F")[:10, :10]
+    assert np.abs(Hm - HM_r[:10, :10]).max() < 1e-10 * np.abs(HM_r).max()
+    assert nsolve["n"] == 9
+    # bad sizes return 0 without touching anything
+    assert lib.pisth0_(ref(I(n)), dp(x), ref(I(m_max)), ref(I(5)), ref(I(5)),
+                       C.cast(h0x, C.c_void_p), C.cast(linsolv, C.c_void_p), dp(VJ), dp(HM)) == 0
+
+
 def test_norm_dot(lib):
     rng = np.random.default_rng(6)
     x, y = rng.standard_normal(10001), rng.standard_normal(10001)

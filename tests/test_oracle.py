@@ -130,3 +130,22 @@ def test_window_and_convergence_helpers(orc):
     assert orc.get_sep_max([0.0, 1.0], [0.1, 0.95, 3.0]) == pytest.approx(0.1)
     p = orc.pist_params(20, (0.0, 1e-8, 0, 0, 0, 20, 0))
     assert (p["startcnt"], p["stepcnt"], p["stepeig"], p["m_max"]) == (40, 5, 1, 60)
+
+
+def test_oracle_ndvr_matches_dense(orc):
+    """The oracle's sNDVR path (H3X as the outer level, OUTH as the outer
+    block-Jacobi blocks) equals the explicit matrix, and one more level of the
+    same Hamiltonian in per-point form changes nothing when the coupling is 0."""
+    from scalit_gb300 import hamiltonian as hm
+    p = hm.build_problem(hm.Grid3(8, 7, 6), hm.PES())
+    q0 = hm.ndvr_problem(p, coupling=0.0)
+    H0 = hm.dense_ndvr(q0)
+    assert np.abs(H0 - hm.dense_hamiltonian(p)).max() < 1e-15
+    q = hm.ndvr_problem(p, coupling=2e-4, seed=3)
+    op = orc.Operator(q.sizes, q.dep, q.H0, q.RES, None, E0=0.0, ndvr=True, OUTH=q.OUTH)
+    x = np.random.default_rng(4).standard_normal(q.N)
+    H = hm.dense_ndvr(q)
+    assert np.linalg.norm(op.hx(x, 0) - H @ x) / np.linalg.norm(H @ x) < 1e-14
+    # the build's outer blocks are OUTH: with one level left, P*X is (H - E0)^-1 on it
+    op.build_osb(50, 1e-14)
+    assert np.all(np.isfinite(op.EIG0))
