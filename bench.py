@@ -1,16 +1,20 @@
-"""Benchmark of the H*X hot path on GB300.
+"""Benchmark of the H*X / PIST hot path on GB300.
 
 One step = one FP64 H*X application (MYHX, TA1) to a block of 16 vectors on
-the 96 x 96 x 64 Jacobi-DVR grid (589,824 points) -- the "bare FP64 H*X on 1
-and 16 vectors" of the plain-FP64 GPU workload.  Inputs are seeded N(0,1)
-vectors already resident in HBM; two input/output sets (2 x 151 MB, larger
-than the 129 MB L2) alternate between steps.  `e2e` repeats the measurement
-through the host-buffer C ABI (scalit_hx), host<->device copies included.
+the 160 x 160 x 120 Jacobi-DVR grid (3,072,000 points), the grid the metric's
+PIST leg is quoted on.  Inputs are seeded N(0,1) vectors already resident in
+HBM; two input/output sets (2 x 786 MB, far larger than the 129 MB L2)
+alternate between steps.  `e2e` repeats the measurement through the
+host-buffer C ABI (scalit_hx), host<->device copies included.  The roofline
+object describes the dominant level launch of that same 16-vector step, timed
+with CUDA events on the context's stream; `hx_fp32` does the same for the FP32
+H*X of the precision form (both FP32 engines).
 
-The PIST leg (default: the 200 lowest levels of the 160 x 160 x 120 problem,
-3,072,000 points) times preconditioner build + PIST to convergence + the FP64
-residual check twice: FP64 inner solves, and the mixed path (FP32 inner solves,
-FP32 first Gram-Schmidt pass), and reports every level's difference.
+Legs (each reported in the JSON line): P*X FP64/FP32; PIST on 24x32x20 (20
+levels) and 96x96x64 (100 levels) against the oracle's level fixtures in
+tests/golden; PIST on 160x160x120 (200 levels) with FP64 and with mixed inner
+solves, per-level differences; the batched shifted QMR over 48 uneven
+problems; the CPU baseline (the oracle's MYHX and PIST on the host cores).
 
 N > 1 (torchrun): replicas -- every rank runs the same workload on its own GPU,
 no collective on the data path; value = all ranks' applications / slowest rank.
@@ -38,6 +42,10 @@ sys.path.insert(0, ROOT)
 
 METRIC = "H*X apps/s & %roofline; PIST time to 200 levels (mixed vs FP64 GPU)"
 
+# FP32 H*X engines timed by the bench, and the kernel each runs
+FP32_ENGINES = (("simt", 0), ("tensor_bf16x3", 1))
+FP32_KERNEL = {"simt": "gemm_kernel<float>", "tensor_bf16x3": "tc32_level_kernel"}
+
 
 def parse():
     ap = argparse.ArgumentParser()
@@ -45,7 +53,7 @@ def parse():
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="tri-96x96x64")
+    ap.add_argument("--workload", default="tri-160x160x120")
     ap.add_argument("--nvec", type=int, default=16)
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -56,8 +64,10 @@ def parse():
                     help="PIST arms to run: fp64 (FP64 inner solves), fp32 (mixed)")
     ap.add_argument("--pist-warmup", type=int, default=1,
                     help="untimed small-grid PIST before the timed arms (0 skips it)")
-    ap.add_argument("--batch-problems", type=int, default=0,
+    ap.add_argument("--batch-problems", type=int, default=48,
                     help="shifted-QMR leg over this many uneven problems (0 skips it)")
+    ap.add_argument("--golden-pist", default="tri-24x32x20,tri-96x96x64",
+                    help="PIST legs compared with the oracle's level fixtures ('none' skips them)")
     ap.add_argument("--batch-shifts", type=int, default=16)
     return ap.parse_args()
 
@@ -142,29 +152,31 @@ def load_peaks():
         return 6800.0, 1900.0, "fallback"
 
 
-def profiled_traffic(workload, level):
-    """DRAM bytes per single-vector launch of the tensor-core level kernel, from
-    the committed ncu summary of this workload (None when not profiled)."""
+def profiled_traffic(kernel, workload, level, nvec):
+    """DRAM bytes (read + write) of one nvec-vector launch of a level kernel,
+    from the committed ncu summary of this workload: the summary lists the
+    bytes of one vector's share (a smaller capture scaled by its vectors),
+    multiplied here by nvec (None when not profiled)."""
     import re
-    path = os.path.join(ROOT, "profiles", f"tc_level_kernel_{workload}.md")
+    path = os.path.join(ROOT, "profiles", f"{kernel}_{workload}.md")
     try:
         with open(path) as f:
-            m = re.search(rf"traffic_per_launch_level{level}_nvec1:\s*(\d+)", f.read())
-        return int(m.group(1)) if m else None
+            m = re.search(rf"traffic_per_vector_level{level}:\s*(\d+)", f.read())
+        return int(m.group(1)) * nvec if m else None
     except OSError:
         return None
 
 
-def hx_units(sizes):
-    """Algorithmic flops and bytes of one FP64 H*X application, and per level.
+def hx_units(sizes, w=8):
+    """Algorithmic flops and bytes of one H*X application (one vector), and per level.
 
     flops: 2 N n_l per level plus the diagonal (V - E0) X and the level sums (5N).
     bytes of a level launch: read X, write Y, and read Y when accumulating
     (levels 2..sF), plus the small level matrix; DEP and V where used.
+    w: bytes per value (8 FP64, 4 FP32).
     """
     n = list(sizes)
     N = int(np.prod(n))
-    w = 8
     levels = []
     for l, nl in enumerate(n):
         flops = 2.0 * N * nl
@@ -181,25 +193,68 @@ def hx_units(sizes):
     return total_flops, total_bytes, levels
 
 
+def hx_config(p, nvec, operator="MYHX TA1 (H - E0) X", world=1):
+    """The `config` of both arms' JSON lines (identical by construction)."""
+    return {"workload": f"tri-{p.sizes[0]}x{p.sizes[1]}x{p.sizes[2]}", "grid": list(p.sizes), "npoints": p.N,
+            "vectors_per_step": nvec, "operator": operator, "parallelism": f"replicas{world}",
+            "l2": "inputs larger than the 129 MB L2 (16 FP64 vectors of 24.6 MB per block)"}
+
+
 # ------------------------------------------------------------- reference --
-def cpu_baseline(problem, e0, seconds, nvec_cap=64):
-    """The oracle's MYHX on the host cores: applications per second on a bounded sample."""
-    from oracle import oracle as orc
-    op = orc.Operator.from_problem(problem, E0=e0)
-    x = np.random.default_rng(0).standard_normal(problem.N)
+def cpu_hx_rate(op, N, seconds, cap=64):
+    """The oracle's MYHX (TA1) applications per second on a bounded sample."""
+    x = np.random.default_rng(0).standard_normal(N)
     op.hx(x, 1)
     t0 = time.perf_counter()
     op.hx(x, 1)
     one = time.perf_counter() - t0
-    reps = max(1, min(nvec_cap, int(seconds / max(one, 1e-6))))
+    reps = max(1, min(cap, int(seconds / max(one, 1e-6))))
     t0 = time.perf_counter()
     for _ in range(reps):
         op.hx(x, 1)
-    dt = time.perf_counter() - t0
-    return {"value": reps / dt, "unit": "H*X apps/s", "cores": orc.num_threads(), "kind": "port",
-            "sample": f"{reps} FP64 H*X applications (TA1) on the {problem.sizes[0]}x"
-                      f"{problem.sizes[1]}x{problem.sizes[2]} grid, oracle C restatement of MYHX "
-                      f"(osb.hx.h:71-110), OpenMP over blocks"}
+    return reps, reps / (time.perf_counter() - t0)
+
+
+def cpu_pist_baseline(hm, seconds_capped=8.0):
+    """The oracle's PIST on the host cores: the 24x32x20 problem in full (20
+    levels, its level fixture's parameters), and on 96x96x64 the rates of a
+    capped run -- QMR iterations per second and seconds per Krylov step (QMR
+    solve + re-orthogonalised Gram-Schmidt + HMAT column) -- next to the
+    committed fixture's full CPU run (tests/golden)."""
+    from oracle import oracle as orc
+    out = {"cores": orc.num_threads(), "kind": "port"}
+    p = hm.workload("tri-24x32x20")
+    e0 = float(p.RES.min())
+    op = orc.Operator.from_problem(p, E0=e0)
+    t0 = time.perf_counter()
+    op.build_osb(20, 1e-4)
+    t1 = time.perf_counter()
+    x0 = orc.start_vector(p.N, 0)
+
+    def lin(v):
+        rc, X, _, _ = op.qmr(v, 2000, 1e-4)
+        return rc, X
+
+    st, eig, _, _ = orc.pist_conv(e0, 1e-11, 0, x0, 40, 5, 1, 20, 400, lambda v: op.hx(v, 0), lin, orth=1)
+    t2 = time.perf_counter()
+    out["tri-24x32x20"] = {"levels": 20, "status": int(st), "build_s": t1 - t0, "pist_s": t2 - t1,
+                           "seconds": t2 - t0, "levels_per_s": 20 / (t2 - t0)}
+    return out
+
+
+def cpu_baseline(problem, e0, seconds, hm, with_pist=True):
+    """The oracle on the host cores: MYHX applications per second on a bounded
+    sample of the bench's grid, and the PIST baseline."""
+    from oracle import oracle as orc
+    op = orc.Operator.from_problem(problem, E0=e0)
+    reps, value = cpu_hx_rate(op, problem.N, seconds)
+    out = {"value": value, "unit": "H*X apps/s", "cores": orc.num_threads(), "kind": "port",
+           "sample": f"{reps} FP64 H*X applications (TA1) on the {problem.sizes[0]}x"
+                     f"{problem.sizes[1]}x{problem.sizes[2]} grid, oracle C restatement of MYHX "
+                     f"(osb.hx.h:71-110), OpenMP over blocks"}
+    if with_pist:
+        out["pist"] = cpu_pist_baseline(hm)
+    return out
 
 
 def run_reference(args):
@@ -216,9 +271,9 @@ def run_reference(args):
     t0 = time.perf_counter()
     op.hx(x, 1)
     one = time.perf_counter() - t0
-    # each step is a bounded sample: nvec applications, capped so the run stays short
-    per_step = max(1, min(args.nvec, int(6.0 / max(one, 1e-6))))
-    for _ in range(args.warmup):
+    # each step is a bounded sample of the nvec-vector step, capped so the run stays short
+    per_step = max(1, min(args.nvec, int(2.0 / max(one, 1e-6))))
+    for _ in range(min(args.warmup, 3)):
         op.hx(x, 1)
     t0 = time.perf_counter()
     for _ in range(args.steps):
@@ -231,11 +286,11 @@ def run_reference(args):
         "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": dt / args.steps * 1e3, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": args.workload, "grid": list(p.sizes), "npoints": p.N,
-                   "vectors_per_step": per_step, "operator": "MYHX TA1"},
+        "config": hx_config(p, args.nvec, world=world),
         "cpu_baseline": {"value": value, "unit": "H*X apps/s", "cores": orc.num_threads(),
                          "kind": "port",
-                         "sample": f"{per_step} applications per step, oracle C restatement of MYHX"},
+                         "sample": f"{per_step} of the step's {args.nvec} applications per step, oracle C "
+                                   f"restatement of MYHX (osb.hx.h:71-110)"},
         "e2e": {"value": value, "unit": "H*X apps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -295,7 +350,15 @@ def pist_leg(workload, levels, device, capi, hm, arms=("fp64", "fp32"), warmup=T
                      "qmr_iterations": info["qmr_total"], "qmr_solves": info["qmr_solves"],
                      "t_qmr": info["t_qmr"], "t_orth": info["t_orth"], "t_hmat": info["t_hmat"],
                      "t_ritz": info["t_ritz"], "t_resid": info["t_resid"],
-                     "max_residual_eh": float(np.max(info["resid"]))}
+                     "max_residual_eh": float(np.max(info["resid"])),
+                     "residuals_eh": [float(f"{r:.3g}") for r in info["resid"]]}
+    fx = load_fixture(workload)
+    if fx is not None and fx.get("levels") == levels:
+        ref = np.array(fx["eigenvalues_eh"])
+        for name, eig in eigs.items():
+            err = np.abs(eig - ref) * hm.HARTREE_CM
+            out[name]["max_err_vs_oracle_cm"] = float(err.max())
+            out[name]["per_level_err_vs_oracle_cm"] = [float(f"{d:.3g}") for d in err]
     if "fp64" in eigs and "fp32" in eigs:
         out["speedup_fp32_inner"] = out["fp64"]["seconds"] / out["fp32"]["seconds"]
         out["speedup_excluding_build"] = out["fp64"]["pist_s"] / out["fp32"]["pist_s"]
@@ -303,6 +366,45 @@ def pist_leg(workload, levels, device, capi, hm, arms=("fp64", "fp32"), warmup=T
         out["max_abs_diff_cm"] = float(diff.max())
         out["per_level_diff_cm"] = [float(f"{d:.3g}") for d in diff]
     out["lowest_eigenvalues_eh"] = [float(v) for v in next(iter(eigs.values()))[:5]] if eigs else []
+    return out
+
+
+def load_fixture(workload):
+    path = os.path.join(ROOT, "tests", "golden", f"pist_{workload}.json")
+    try:
+        with open(path) as f:
+            return json.load(f)
+    except OSError:
+        return None
+
+
+def golden_pist_leg(workload, device, capi, hm):
+    """PIST with FP64 and with mixed inner solves on a workload whose oracle
+    levels are committed (tests/golden), with the fixture's parameters: wall
+    time from the build, levels/s and the largest level error against the
+    FP64 oracle, next to the oracle's own CPU time for the same solve."""
+    fx = load_fixture(workload)
+    if fx is None:
+        return None
+    p = hm.workload(workload)
+    x0 = np.random.default_rng(fx["seed"]).random(p.N)
+    out = {"levels": fx["levels"], "oracle_krylov": fx["status"], "oracle_qmr_iterations": fx["qmr_iterations"],
+           "oracle_cpu_seconds": fx["build_s"] + fx["pist_s"], "oracle_cpu_threads": fx["threads"]}
+    ref = np.array(fx["eigenvalues_eh"])
+    for name, prec, orth in (("fp64", capi.PREC_FP64, 1), ("fp32", capi.PREC_FP32, 2)):
+        with capi.Context.from_problem(p, e0=fx["e0"], device=device) as ctx:
+            if prec == capi.PREC_FP32:
+                ctx.set_fp32_mode(capi.FP32_TENSOR_PX)
+            t0 = time.perf_counter()
+            ctx.build_osb(20, 1e-4)
+            st, eig, _, info = ctx.pist(x0, fx["levels"], fx["e0"], fx["etol"], startcnt=fx["startcnt"],
+                                        stepcnt=fx["stepcnt"], m_max=fx["m_max"], qmr_max=fx["qmr_max"],
+                                        qmr_tol=fx["qmr_tol"], precision=prec, orth=orth, residuals=True)
+            dt = time.perf_counter() - t0
+        err = np.abs(eig - ref) * hm.HARTREE_CM
+        out[name] = {"status": st, "seconds": dt, "levels_per_s": fx["levels"] / dt,
+                     "qmr_iterations": info["qmr_total"], "max_err_vs_oracle_cm": float(err.max()),
+                     "max_residual_eh": float(np.max(info["resid"]))}
     return out
 
 
@@ -395,25 +497,16 @@ def run_ours(args):
     ms_max = reduce_max(ms, world)
     value = replicas_value(args.steps * nvec, world, ms_max / 1e3)
 
-    # per-level kernel timing (the strided GEMM launches of one application)
-    total_flops, total_bytes, lv = hx_units(p.sizes)
-    level_ms = []
-    reps = 20
-    for l in range(len(p.sizes)):
-        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        with torch.cuda.stream(stream):
-            for i in range(3):
-                ctx.level_device(l + 1, X[i % 2][i], Y[i % 2][i], accumulate=l > 0)
-            a.record(stream)
-            for i in range(reps):
-                ctx.level_device(l + 1, X[i % 2][i % nvec], Y[i % 2][i % nvec], accumulate=l > 0)
-            b.record(stream)
-        torch.cuda.synchronize()
-        level_ms.append(a.elapsed_time(b) / reps)
+    # the dominant level launch of the same 16-vector step: CUDA events between
+    # the step's level launches on the context's stream (the 16-vector block
+    # of 393 MB does not fit the 129 MB L2, so every launch streams from HBM)
+    total_flops, total_bytes, lv = hx_units(p.sizes, 8)
+    level_ms = ctx.hx_level_times(X[0], Y[0], nvec, reps=10)
     dom = int(np.argmax(level_ms))
     hbm, bf16, peak_src = load_peaks()
-    ach_gbs = lv[dom]["bytes"] / (level_ms[dom] / 1e3) / 1e9
-    ach_tf = lv[dom]["flops"] / (level_ms[dom] / 1e3) / 1e12
+    dom_bytes = nvec * lv[dom]["bytes"]
+    ach_gbs = dom_bytes / (level_ms[dom] / 1e3) / 1e9
+    ach_tf = nvec * lv[dom]["flops"] / (level_ms[dom] / 1e3) / 1e12
 
     # FP64 reference rate: cuBLAS DGEMM measured live (the FP64 unit this path runs on)
     fp64_peak = None
@@ -435,11 +528,12 @@ def run_ours(args):
     except Exception:
         fp64_peak = None
 
-    # FP32 (the inner-solve arithmetic) on the same block, both FP32 engines
+    # FP32 H*X of the precision form (the QMR inner solves' arithmetic) on the
+    # same block, both FP32 engines, with the dominant level's HBM roofline
     X32 = [x.float() for x in X]
     Y32 = [torch.empty_like(x) for x in X32]
 
-    def time_f32(fn):
+    def time_f32(fn, steps=args.steps):
         with torch.cuda.stream(stream):
             for i in range(3):
                 fn(X32[i % 2], Y32[i % 2], nvec, capi.TA1)
@@ -447,18 +541,31 @@ def run_ours(args):
         a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         with torch.cuda.stream(stream):
             a.record(stream)
-            for i in range(args.steps):
+            for i in range(steps):
                 fn(X32[i % 2], Y32[i % 2], nvec, capi.TA1)
             b.record(stream)
         torch.cuda.synchronize()
-        return args.steps * nvec / (a.elapsed_time(b) / 1e3)
+        return steps * nvec / (a.elapsed_time(b) / 1e3)
 
-    fp32_engines = {}
-    for name, mode in (("simt", capi.FP32_SIMT), ("tensor_bf16x3", capi.FP32_TENSOR)):
+    _, bytes32, lv32 = hx_units(p.sizes, 4)
+    fp32 = {"dtype": "f32", "engines_apps_per_s": {}, "engines_level_ms": {}}
+    for name, mode in FP32_ENGINES:
         ctx.set_fp32_mode(mode)
-        fp32_engines[name] = time_f32(ctx.hx_f32_device)
+        fp32["engines_apps_per_s"][name] = time_f32(ctx.hx_f32_device)
+        fp32["engines_level_ms"][name] = ctx.hx_level_times(X32[0], Y32[0], nvec, reps=10)
+    best = max(fp32["engines_apps_per_s"], key=fp32["engines_apps_per_s"].get)
+    lms = fp32["engines_level_ms"][best]
+    d32 = int(np.argmax(lms))
+    a32 = nvec * lv32[d32]["bytes"] / (lms[d32] / 1e3) / 1e9
+    fp32.update({"apps_per_s": fp32["engines_apps_per_s"][best], "engine": best,
+                 "hbm_fraction_whole_step": fp32["engines_apps_per_s"][best] * bytes32 / 1e9 / hbm,
+                 "roofline": {"bound": "hbm", "achieved": a32, "peak": hbm, "unit": "GB/s", "frac": a32 / hbm,
+                              "kernel": f"{FP32_KERNEL[best]} level {d32 + 1}",
+                              "algorithmic_bytes_per_launch": nvec * lv32[d32]["bytes"], "launch_ms": lms[d32],
+                              "traffic": profiled_traffic(FP32_KERNEL[best].split("<")[0], args.workload,
+                                                          d32 + 1, nvec),
+                              "peak_source": peak_src}})
     ctx.set_fp32_mode(capi.FP32_SIMT)
-    fp32_apps = max(fp32_engines.values())
 
     # P*X (MYPX, TA1) of the same block in FP64 and FP32, after one preconditioner build
     t0 = time.perf_counter()
@@ -468,19 +575,20 @@ def run_ours(args):
     px_apps = {}
     for name, xs, ys, fn in (("fp64", X, Y, ctx.px_device), ("fp32", X32, Y32, ctx.px_f32_device)):
         with torch.cuda.stream(stream):
-            for i in range(3):
+            for i in range(2):
                 fn(xs[i % 2], ys[i % 2], nvec, capi.TA1)
         torch.cuda.synchronize()
         a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        reps = max(2, args.steps // 4)
         with torch.cuda.stream(stream):
             a.record(stream)
-            for i in range(args.steps):
+            for i in range(reps):
                 fn(xs[i % 2], ys[i % 2], nvec, capi.TA1)
             b.record(stream)
         torch.cuda.synchronize()
-        px_apps[name] = args.steps * nvec / (a.elapsed_time(b) / 1e3)
-    ctx.set_fp32_mode(capi.FP32_TENSOR)
-    px_apps["fp32_tensor_bf16x3"] = time_f32(ctx.px_f32_device)
+        px_apps[name] = reps * nvec / (a.elapsed_time(b) / 1e3)
+    ctx.set_fp32_mode(capi.FP32_TENSOR_PX)
+    px_apps["fp32_tensor_rotations"] = time_f32(ctx.px_f32_device, max(2, args.steps // 4))
     ctx.set_fp32_mode(capi.FP32_SIMT)
     del X32, Y32
 
@@ -488,7 +596,7 @@ def run_ours(args):
     Xh = X[0].cpu().pin_memory()
     Yh = torch.empty_like(Xh).pin_memory()
     xh, yh = Xh.numpy(), Yh.numpy()
-    ctx.hx(xh, capi.TA1)
+    ctx.hx(xh, capi.TA1, out=yh)
     e2e_steps = max(3, args.steps // 4)
     t0 = time.perf_counter()
     for _ in range(e2e_steps):
@@ -496,10 +604,19 @@ def run_ours(args):
     e2e_s = time.perf_counter() - t0
     e2e_s = reduce_max(e2e_s, world)
     e2e_value = replicas_value(e2e_steps * nvec, world, e2e_s)
+    ctx.close()
+    del X, Y, Xh, Yh
+    torch.cuda.empty_cache()
 
     base = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
-        base = cpu_baseline(p, e0, args.cpu_seconds)
+        base = cpu_baseline(p, e0, args.cpu_seconds, hm)
+    golden = {}
+    if args.golden_pist != "none":
+        for wl in (w.strip() for w in args.golden_pist.split(",") if w.strip()):
+            g = golden_pist_leg(wl, local, capi, hm)
+            if g is not None:
+                golden[wl] = g
     pist = None
     if args.pist_workload != "none" and args.pist_levels > 0:
         pist = pist_leg(args.pist_workload, args.pist_levels, local, capi, hm,
@@ -514,23 +631,21 @@ def run_ours(args):
             "steps": args.steps, "warmup": max(args.warmup, 3), "ms_per_step": ms_max / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
             "data": "synthetic",
-            "config": {"workload": args.workload, "grid": list(p.sizes), "npoints": N,
-                       "vectors_per_step": nvec, "operator": "MYHX TA1 (H - E0) X",
-                       "parallelism": f"replicas{world}",
-                       "l2": "two alternating 2x151 MB input/output sets (> 129 MB L2)"},
+            "config": hx_config(p, nvec, world=world),
             "roofline": {"bound": "hbm", "achieved": ach_gbs, "peak": hbm, "unit": "GB/s",
-                         "frac": ach_gbs / hbm, "traffic": profiled_traffic(args.workload, dom + 1),
+                         "frac": ach_gbs / hbm, "traffic": profiled_traffic("tc_level_kernel", args.workload,
+                                                                           dom + 1, nvec),
                          "kernel": f"tc_level_kernel level {dom + 1}",
                          "peak_source": peak_src,
-                         "algorithmic_bytes_per_launch": lv[dom]["bytes"],
-                         "launch_ms": level_ms[dom]},
+                         "algorithmic_bytes_per_launch": dom_bytes,
+                         "launch_ms": level_ms[dom], "vectors_per_launch": nvec},
             "fp64_roofline": {"bound": "fp64", "achieved": ach_tf, "unit": "TFLOP/s",
                               "peak": fp64_peak, "frac": (ach_tf / fp64_peak) if fp64_peak else None,
                               "peak_source": "cuBLAS DGEMM 4096^3 measured in this run",
-                              "algorithmic_flops_per_launch": lv[dom]["flops"]},
+                              "algorithmic_flops_per_launch": nvec * lv[dom]["flops"]},
             "level_ms": level_ms,
             "hx_flops_per_app": total_flops, "hx_bytes_per_app": total_bytes,
-            "fp32_apps_per_s": fp32_apps, "fp32_engines_apps_per_s": fp32_engines,
+            "hx_fp32": fp32,
             "px_apps_per_s": px_apps,
             "osb_build": {"seconds": build_s, "levels_s": build_levels},
             "e2e": {"value": e2e_value, "unit": "H*X apps/s",
@@ -540,12 +655,13 @@ def run_ours(args):
         }
         if base is not None:
             line["cpu_baseline"] = base
+        if golden:
+            line["pist_vs_oracle"] = golden
         if pist is not None:
             line["pist"] = pist
         if batch is not None:
             line["batch"] = batch
         print(json.dumps(line), flush=True)
-    ctx.close()
     if world > 1:
         torch.distributed.destroy_process_group()
     return 0
