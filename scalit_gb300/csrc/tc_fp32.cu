@@ -281,7 +281,46 @@ tc32_level_kernel(Tc32Args g)
         for (int b = 0; b < 2; ++b) mbar_wait(&mbar[b], 0) || mbar_wait(&mbar[b], 1);
     }
     fence_after();
-    if (ok) {
+    if (g.c_sn == 1) {
+        // Output rows contiguous along n (a level with nin == 1): a thread owns
+        // one row, so storing straight from TMEM would give every warp store 32
+        // rows a row length apart.  The scaled accumulator tile goes through
+        // shared memory instead (the B tile and A planes, free once the last
+        // MMA completed; padded stride NT + 1), and each warp then finishes
+        // whole rows with the lanes along n: the diagonal term's loads, the
+        // accumulated output and the stores are all coalesced.
+        float *stage = reinterpret_cast<float *>(smem);
+        const int ld = NT + 1;
+        const float rs = (g.rowscale && mvalid) ? g.rowscale[m % g.Mi] : 1.0f;
+        const float sc = g.alpha * rs;
+        const uint32_t lane_base = (uint32_t)((warp & 3) * 32) << 16;
+        const int cq = NT / 4;
+        const int cbeg = (warp >> 2) * cq, cend = cbeg + cq;
+        for (int c0 = cbeg; c0 < cend && ok; c0 += 4) {
+            float v[4];
+            tmem_ld4(tbase + lane_base + (uint32_t)c0, v);
+            asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+            #pragma unroll
+            for (int j = 0; j < 4; ++j) stage[row * ld + c0 + j] = sc * v[j];
+        }
+        // every cutting thread arrives here, whatever its wait results were
+        asm volatile("bar.sync 1, %0;" :: "n"(kThreads32) : "memory");
+        const float shift = g.shiftv ? g.shiftv[z] : g.shift;
+        const int lane = tid & 31;
+        for (int r = warp; r < kBM32 && ok; r += kThreads32 / 32) {
+            if (m0 + r >= mlim) break;
+            const i64 ro = row_off(m0 + r);
+            for (int cc = lane; cc < NT; cc += 32) {
+                const int n = ntile * NT + cc;
+                if (n >= g.N) break;
+                const i64 p = ro + n;
+                float out = stage[r * ld + cc];
+                if (g.diagV) out = fmaf(g.alpha * (g.diagV[p] - shift), g.diagX[p + (i64)z * g.dx_sz], out);
+                if (g.accumulate) out += C[p];
+                C[p] = out;
+            }
+        }
+    } else if (ok) {
         // warp w reads TMEM lanes 32 (w % 4) .. (its rows) and the column quarter w / 4
         const float rs = (g.rowscale && mvalid) ? g.rowscale[m % g.Mi] : 1.0f;
         const float sc = g.alpha * rs;
@@ -434,6 +473,11 @@ static int launch32(const Tc32Args &g, i64 gx, int ntiles, int nvec, cudaStream_
     const int resident = (g.KS <= kStages32 || smem_bytes(g.NT, g.KS, g.KS, slab) <= 220 * 1024) ? 1 : 0;
     const size_t smem = smem_bytes(g.NT, g.KS, resident ? g.KS : kStages32, slab);
     if (smem > 220 * 1024) { set_error("tensor-core FP32 tile too large"); return SCALIT_EUNSUP; }
+    // the staged epilogue of row-contiguous outputs reuses the B tile and A planes
+    if (g.c_sn == 1 && (size_t)kBM32 * (g.NT + 1) * 4 > (size_t)g.KS * 2 * g.NT * 32 + 2 * (size_t)kAStep32) {
+        set_error("tensor-core FP32 output stage does not fit");
+        return SCALIT_EUNSUP;
+    }
     static int configured = -1;
     int dev = 0;
     cudaGetDevice(&dev);

@@ -326,6 +326,16 @@ tc_level_kernel(TcArgs g)
     }
     fence_after();
 
+    // Output rows contiguous along n (a level with nin == 1): the recombined
+    // values go through shared memory (the A and B digit buffers, free once the
+    // last MMA completed; padded stride NT + 1) and each warp then finishes
+    // whole rows with the lanes along n, so the diagonal term's loads, the
+    // accumulated output and the stores are coalesced instead of every warp
+    // store touching 32 rows a row length apart.
+    double *stage = reinterpret_cast<double *>(smem);
+    const bool staged = (g.c_sn == 1);
+    const int sld = NT + 1;
+
     if (ok) {
         // epilogue: thread tid holds TMEM lane tid = grid row m.  The exact group
         // sums are recombined in 64-bit integers: T = sum_{g<=5} G_g 2^(7(5-g))
@@ -358,6 +368,7 @@ tc_level_kernel(TcArgs g)
                     val = __longlong_as_double(__double_as_longlong(val) + ((long long)bexp[n] << 52));
                 const i64 p = moff + (i64)n * g.c_sn;
                 double out = sc * val;
+                if (staged) { outv[j] = out; continue; }
                 if (g.diagV) out = fma(g.alpha * (g.diagV[p] - (g.shiftv ? g.shiftv[z] : g.shift)),
                                        g.diagX[p + (i64)z * g.dx_sz], out);
                 if (g.accumulate) out += C[p];
@@ -366,7 +377,28 @@ tc_level_kernel(TcArgs g)
             #pragma unroll
             for (int j = 0; j < 4; ++j) {
                 const int n = ntile * NT + c0 + j;
-                if (n < g.N) C[moff + (i64)n * g.c_sn] = outv[j];
+                if (staged) stage[row * sld + c0 + j] = outv[j];
+                else if (n < g.N) C[moff + (i64)n * g.c_sn] = outv[j];
+            }
+        }
+    }
+    if (staged) {
+        // every cutting thread arrives here, whatever its wait results were
+        asm volatile("bar.sync 1, %0;" :: "n"(kThreadsTC) : "memory");
+        const double shift = g.shiftv ? g.shiftv[z] : g.shift;
+        const int lane = tid & 31;
+        for (int r = warp; r < kBM && ok; r += kThreadsTC / 32) {
+            const int mm = m0 + r;
+            if (mm >= mlim) break;
+            const i64 ro = (i64)(mm % g.Mi) * g.s1 + (i64)(mm / g.Mi) * g.s2;
+            for (int cc = lane; cc < NT; cc += 32) {
+                const int n = ntile * NT + cc;
+                if (n >= g.N) break;
+                const i64 p = ro + n;
+                double out = stage[r * sld + cc];
+                if (g.diagV) out = fma(g.alpha * (g.diagV[p] - shift), g.diagX[p + (i64)z * g.dx_sz], out);
+                if (g.accumulate) out += C[p];
+                C[p] = out;
             }
         }
     }
