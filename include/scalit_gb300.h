@@ -71,6 +71,10 @@ extern "C" {
 /* arithmetic of the QMR inner solves */
 #define SCALIT_PREC_FP64 0
 #define SCALIT_PREC_FP32 1
+/* FP32 QMR solves under FP64 iterative refinement: x += QMR32(b - (H - E0) x)
+ * with the residual formed by an FP64 H*X, until the FP64 residual meets the
+ * tolerance (QMR solves only, not the shifted batches) */
+#define SCALIT_PREC_FP32_REFINED 2
 
 typedef struct scalit_ctx scalit_ctx;
 
@@ -299,9 +303,15 @@ int scalit_pist_cx(scalit_ctx *ctx, double e0, double etol, int ntype, int conju
  * convergence test: |1| uses |HX - B|/|HX| (one extra H*X per iteration),
  * |2| the max of three ratios, otherwise |R|/|B|.  Returns the reference's
  * QMR_MPI code; *res receives RES and *iters (may be NULL) the iteration
- * count.  precision = SCALIT_PREC_FP64 or SCALIT_PREC_FP32 (vectors, H*X
+ * count.  precision = SCALIT_PREC_FP64, SCALIT_PREC_FP32 (vectors, H*X
  * and P*X in FP32, reductions accumulated in FP64; B and X stay FP64 at the
- * boundary). */
+ * boundary) or SCALIT_PREC_FP32_REFINED: FP32 solves of the current FP64
+ * residual r = B - (H - E0) X added to X (at most 5 rounds, each solved to
+ * max(1e-4, qmrtol |B - r| / |r|) and capped by the iterations left), until
+ * |r| <= qmrtol |B - r| -- the type -1 measure in FP64 -- so a tolerance the
+ * FP32 recurrence cannot attain is still reached (no counterpart in the
+ * reference, an extension of QMR for the mixed-precision solve); the code is
+ * the total iteration count, negative when the tolerance was not reached. */
 int scalit_qmr(scalit_ctx *ctx, int ntype, int qmrmax, double qmrtol, int precision,
                const double *B, double *X, double *res, int *iters);
 int scalit_qmr_device(scalit_ctx *ctx, int ntype, int qmrmax, double qmrtol, int precision,
@@ -370,6 +380,11 @@ typedef struct {
                       /*    its (tiny) coefficients, split into two FP32 */
                       /*    parts, over the FP32 copy: orthonormal to    */
                       /*    FP64 round-off                               */
+                      /* 3: as 2 with the first pass's update over the   */
+                      /*    FP64 basis: the FP32 copy's rounding adds    */
+                      /*    ~6e-8 |c| outside the basis' span in mode 2, */
+                      /*    which sets a residual floor of ~3e-8 Eh      */
+                      /*    (use 3 with a residual target)               */
 } scalit_pist_params;
 
 typedef struct {
@@ -424,6 +439,23 @@ int scalit_pist_vectors(scalit_ctx *ctx, const scalit_pist_params *p, const doub
  * The reference reports no residuals (pist.f90 returns eigenvalues only). */
 int scalit_pist_residuals(scalit_ctx *ctx, const scalit_pist_params *p, const double *x0, double *eig,
                           double *res, scalit_pist_info *info, double *resid);
+
+/* PIST with a residual-based continuation, no counterpart in the reference
+ * (whose stopping test is the eigenvalue change alone, getDiffMax,
+ * util.f90:84-100): once that test passes, the FP64 residuals
+ * |H psi_k - theta_k psi_k|_2 of the window's Ritz pairs are checked, and
+ * while one is above resid_tol (Eh) the Krylov basis grows by
+ * max(stepcnt, K/20) vectors and the check repeats, at most max_steps times
+ * and up to m_max vectors.  The residual floor is set by the inner solves'
+ * accuracy: a 1e-8 Eh target wants p->qmr_tol <= 1e-6, in FP64 or
+ * SCALIT_PREC_FP32_REFINED.  eig receives the window's Ritz values of the
+ * final basis (ascending), resid their residuals, vectors (m x npoints, may be
+ * NULL) the Ritz vectors, *steps (may be NULL) the number of extensions; the
+ * result is the final Krylov size (or the usual failure codes).
+ * info->t_resid includes the checks and the extensions' solves. */
+int scalit_pist_refined(scalit_ctx *ctx, const scalit_pist_params *p, const double *x0, double *eig,
+                        double *res, scalit_pist_info *info, double resid_tol, int max_steps,
+                        double *resid, double *vectors, int *steps);
 
 /* PIST followed by the output of PISTF_CONV (src/iterate/libiterate/pist/pistf.f90:98-104):
  * on success *cnt receives the final Krylov size, ritz the cnt Ritz values of

@@ -17,7 +17,7 @@ TOSB, TOSBD1, TOSBD2, TOSBW = 1, 2, 3, 4
 # nType codes of the complex forms (osb.data.h:18-22)
 TAAP0, TMAP0, TAAP, TAAPP, TAAPR, TMAP, TMAPP, TMAPR = 2, 3, 100, 101, 102, 200, 201, 202
 FP32_SIMT, FP32_TENSOR, FP32_TENSOR_PX = 0, 1, 2
-PREC_FP64, PREC_FP32 = 0, 1
+PREC_FP64, PREC_FP32, PREC_FP32_REFINED = 0, 1, 2
 FP64_DFMA, FP64_TENSOR = 0, 1
 FMAX = 20
 
@@ -44,6 +44,7 @@ SIGNATURES = {
     "scalit_hx_device": (C.c_int, [_vp, C.c_int, C.c_int, _vp, _vp]),
     "scalit_hx_f32_device": (C.c_int, [_vp, C.c_int, C.c_int, _vp, _vp]),
     "scalit_level_device": (C.c_int, [_vp, C.c_int, C.c_int, _vp, _vp]),
+    "scalit_pist_refined": (C.c_int, [_vp, _vp, _dp, _dp, _dp, _vp, C.c_double, C.c_int, _dp, _dp, _ip]),
     "scalit_hx_level_times": (C.c_int, [_vp, C.c_int, C.c_int, C.c_int, _vp, _vp, C.c_int,
                                         C.POINTER(C.c_float)]),
     "scalit_build_osb": (C.c_int, [_vp, C.c_int, C.c_double, _dp]),
@@ -475,7 +476,7 @@ class Context:
 
     def pist(self, x0, m, e0, etol, startcnt=0, stepcnt=5, m_max=0, gap=1, qmr_max=2000,
              qmr_tol=1e-4, qmr_ntype=-1, precision=PREC_FP64, ntype=0, verbose=False, orth=1,
-             vectors=False, basis=False, residuals=False):
+             vectors=False, basis=False, residuals=False, refine_tol=0.0, refine_steps=4):
         """OSB_PISTCONV: returns (status, eig[m], RES, info dict); with vectors=True the
         info dict also holds the m Ritz vectors ("vectors", m x N); with residuals=True
         it holds the FP64 residual norms |H psi - E psi| of the levels ("resid", m)."""
@@ -504,6 +505,20 @@ class Context:
             return st, eig, res.value, dict(info.as_dict(), m_max=p.m_max, startcnt=p.startcnt, cnt=k,
                                             ritz=ritz[:k], hmat=hmat[:k * k].reshape(k, k, order="F"),
                                             vj=vj[:k * self.N].reshape(self.N, k, order="F"))
+        if refine_tol != 0.0:
+            resid = np.zeros(int(m))
+            vec = np.zeros((int(m), self.N)) if vectors else None
+            steps = C.c_int(0)
+            st = _check(self.lib.scalit_pist_refined(self.h, C.byref(p), _p(x0), _p(eig), C.byref(res),
+                                                     C.byref(info), float(refine_tol), int(refine_steps),
+                                                     _p(resid), _p(vec) if vec is not None else None,
+                                                     C.byref(steps)))
+            out = dict(info.as_dict(), m_max=p.m_max, startcnt=p.startcnt, resid=resid, refine_steps=steps.value)
+            if st > 0:
+                out["krylov"] = st
+            if vec is not None:
+                out["vectors"] = vec
+            return st, eig, res.value, out
         if residuals:
             resid = np.zeros(int(m))
             st = _check(self.lib.scalit_pist_residuals(self.h, C.byref(p), _p(x0), _p(eig), C.byref(res),

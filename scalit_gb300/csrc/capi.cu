@@ -709,6 +709,23 @@ int scalit_pist_residuals(scalit_ctx *c, const scalit_pist_params *p, const doub
     return rc;
 }
 
+int scalit_pist_refined(scalit_ctx *c, const scalit_pist_params *p, const double *x0, double *eig, double *res,
+                        scalit_pist_info *info, double resid_tol, int max_steps, double *resid, double *vectors,
+                        int *steps)
+{
+    CTX_CHECK(c);
+    if (!p || !x0 || !eig || !res || !resid) { set_error("null argument"); return SCALIT_EINVAL; }
+    if (!(resid_tol > 0.0) || max_steps < 0) { set_error("refinement needs resid_tol > 0 and max_steps >= 0"); return SCALIT_EINVAL; }
+    const i64 N = c->L.N;
+    double *dx = nullptr;
+    SC_CUDA(cudaMallocAsync(&dx, sizeof(double) * (size_t)N, c->stream));
+    SC_CUDA(cudaMemcpyAsync(dx, x0, sizeof(double) * N, cudaMemcpyHostToDevice, c->stream));
+    int rc = pist_ctx(c, p, dx, eig, res, info, vectors, nullptr, resid, resid_tol, max_steps, steps);
+    cudaFreeAsync(dx, c->stream);
+    cudaStreamSynchronize(c->stream);
+    return rc;
+}
+
 // ------------------------------------------------ shifts and batches ---
 int scalit_qmr_shifts_device(scalit_ctx *c, int nrhs, const double *shifts, int ntype, int qmrmax, double qmrtol,
                              int precision, const double *dB, double *dX, int *codes, double *res)

@@ -333,11 +333,13 @@ struct PistOps {
 struct PistBasisOut { int *cnt = nullptr; double *ritz = nullptr, *hmat = nullptr, *vj = nullptr; };
 int pist_core(scalit_ctx *c, i64 N, const scalit_pist_params *p, const double *dx0, PistOps &ops,
               double *eig, double *res, scalit_pist_info *info, double *vectors_host = nullptr,
-              const PistBasisOut *basis = nullptr, double *resid = nullptr);
+              const PistBasisOut *basis = nullptr, double *resid = nullptr, double refine_tol = 0.0,
+              int refine_max = 0, int *refine_steps = nullptr);
 int pisth0_host(scalit_ctx *c, i64 N, const double *X, int m_max, int m_low, int m_high, PistOps &ops, double *VJ,
                 double *HMAT, bool mpi, int *num2, int *ret);
 int pist_ctx(scalit_ctx *c, const scalit_pist_params *p, const double *dx0, double *eig,
              double *res, scalit_pist_info *info, double *vectors_host = nullptr,
-             const PistBasisOut *basis = nullptr, double *resid = nullptr);
+             const PistBasisOut *basis = nullptr, double *resid = nullptr, double refine_tol = 0.0,
+             int refine_max = 0, int *refine_steps = nullptr);
 
 }  // namespace sc

@@ -475,7 +475,7 @@ resid_partial_kernel(i64 n, const double *Psi, const double *HPsi, const double 
 // pairs into resid (M, may be null).
 static int ritz_vectors(scalit_ctx *c, i64 N, const double *VJ, const double *HMAT, int ld, int num, double e0,
                         int M, double *A, double *EV, double *work, int lwork, int *devinfo, double *out_host,
-                        double *resid = nullptr)
+                        double *resid = nullptr, double *eig_out = nullptr)
 {
     cudaStream_t s = c->stream;
     cusolverDnHandle_t sol = (cusolverDnHandle_t)c->cusolver;
@@ -532,6 +532,8 @@ static int ritz_vectors(scalit_ctx *c, i64 N, const double *VJ, const double *HM
         g.alpha = 1.0;
         rc = launch_gemm<double>(g, s);
     }
+    if (eig_out)
+        for (int j = 0; j < Msel; ++j) eig_out[j] = ev[idx[j]];
     if (!rc && out_host)
         SC_CUDA(cudaMemcpyAsync(out_host, Psi, sizeof(double) * (size_t)N * Msel, cudaMemcpyDeviceToHost, s));
     if (!rc && resid) {
@@ -571,13 +573,13 @@ static double now()
 
 int pist_core(scalit_ctx *c, i64 N, const scalit_pist_params *p, const double *dx0, PistOps &ops,
               double *eig, double *res, scalit_pist_info *info, double *vectors_host,
-              const PistBasisOut *basis, double *resid)
+              const PistBasisOut *basis, double *resid, double refine_tol, int refine_max, int *refine_steps)
 {
     cudaStream_t s = c->stream;
     const int M = p->m, MM = p->m_max;
     scalit_pist_info inf{};
     *res = 0.0;
-    if (p->orth < 0 || p->orth > 2) { set_error("unknown orthogonalisation mode %d", p->orth); return SCALIT_EINVAL; }
+    if (p->orth < 0 || p->orth > 3) { set_error("unknown orthogonalisation mode %d", p->orth); return SCALIT_EINVAL; }
     if (p->stepeig >= MM || p->startcnt > MM || M > MM || M < 1) {
         if (info) *info = inf;
         return 0;
@@ -593,7 +595,7 @@ int pist_core(scalit_ctx *c, i64 N, const scalit_pist_params *p, const double *d
     }
     SC_CUDA(cudaMallocAsync(&W, sizeof(double) * (size_t)N, s));
     float *VJf = nullptr, *Wf = nullptr;   // FP32 copies for the mixed first pass (orth == 2)
-    if (p->orth == 2) {
+    if (p->orth >= 2) {
         if (cudaMallocAsync(&VJf, sizeof(float) * (size_t)N * MM, s) != cudaSuccess ||
             cudaMallocAsync(&Wf, sizeof(float) * (size_t)N, s) != cudaSuccess) {
             cudaGetLastError();
@@ -658,7 +660,7 @@ int pist_core(scalit_ctx *c, i64 N, const scalit_pist_params *p, const double *d
             mgs_kernel<<<gr, kT, 0, s>>>(N, v, vcol(J), D + (J - 1), nullptr, dnorm + 1, partial, counter);
         } else {
             for (int pass = 0; pass < 2; ++pass) {
-                if (pass == 0 && p->orth == 2) {
+                if (pass == 0 && p->orth >= 2) {
                     int r2 = to_f32(v, Wf, N, s);
                     if (r2) return r2;
                     if (vec4) {
@@ -668,7 +670,12 @@ int pist_core(scalit_ctx *c, i64 N, const scalit_pist_params *p, const double *d
                         gemvt_partial_f32_kernel<<<dim3(nchunk, J), kT, 0, s>>>(N, VJf, Wf, partial, nchunk);
                     }
                     gemvt_vec_kernel<<<(J + 127) / 128, 128, 0, s>>>(J, nchunk, partial, D);
-                    if (vec4) {
+                    if (p->orth == 3) {
+                        // the update over the FP64 basis: the FP32 copy's rounding
+                        // (~6e-8 |c|) would add a component outside span(V) that
+                        // the second pass cannot remove
+                        gemv_sub_kernel<<<gr, kT, 0, s>>>(N, J, VJ, D, v);
+                    } else if (vec4) {
                         gemv_sub_f32x4_kernel<false><<<(int)((N / 4 + kT - 1) / kT), kT, 0, s>>>(N, J, VJf, D, v);
                     } else {
                         gemv_sub_f32_kernel<false><<<gr, kT, 0, s>>>(N, J, VJf, D, v);
@@ -677,9 +684,9 @@ int pist_core(scalit_ctx *c, i64 N, const scalit_pist_params *p, const double *d
                 }
                 gemvt_partial_kernel<<<dim3(nchunk, J), kT, 0, s>>>(N, J, VJ, v, partial, nchunk);
                 gemvt_vec_kernel<<<(J + 127) / 128, 128, 0, s>>>(J, nchunk, partial, D);
-                if (p->orth == 2 && vec4) {
+                if (p->orth >= 2 && vec4) {
                     gemv_sub_f32x4_kernel<true><<<(int)((N / 4 + kT - 1) / kT), kT, 0, s>>>(N, J, VJf, D, v);
-                } else if (p->orth == 2) {
+                } else if (p->orth >= 2) {
                     gemv_sub_f32_kernel<true><<<gr, kT, 0, s>>>(N, J, VJf, D, v);
                 } else {
                     gemv_sub_kernel<<<gr, kT, 0, s>>>(N, J, VJ, D, v);
@@ -844,11 +851,13 @@ int pist_core(scalit_ctx *c, i64 N, const scalit_pist_params *p, const double *d
     };
 
     int cnt_low = 1, cnt_high = std::max(std::max(p->startcnt, M), p->stepeig + 1);
+    int built_high = 0;   // largest Krylov size whose vectors and HMAT columns are complete
     while (true) {
         int ret = 0;
         bool stop = false;
         rc = pisth0(cnt_low, cnt_high, &ret);
         if (rc) break;
+        if (ret == cnt_high) built_high = cnt_high;
         if (pend_high) {
             rc = ritz_settle(&stop);
             if (rc || stop) break;
@@ -886,7 +895,41 @@ int pist_core(scalit_ctx *c, i64 N, const scalit_pist_params *p, const double *d
         cudaStreamSynchronize(s);
         if (rc) set_error("copying the PIST basis out failed");
     }
-    if ((vectors_host || resid) && rc == 0 && status > 0) {
+    if (refine_steps) *refine_steps = 0;
+    if (refine_tol > 0.0 && resid && rc == 0 && status > 0) {
+        // Residual-based continuation: after the eigenvalue-change test, the
+        // FP64 residuals |H psi - theta psi| of the window's Ritz pairs are
+        // checked (Ritz vectors and one batched FP64 H*X); while one is above
+        // refine_tol the basis grows by max(stepcnt, K / 20) more vectors
+        // (pistH0's block step) and the check repeats, at most refine_max
+        // times and up to m_max vectors.  The basis already holds the batch
+        // generated while the converged check ran, so K starts there.
+        const double t0 = now();
+        cusolverDnSetStream(sol, s);
+        int K = std::max(status, built_high), rounds = 0;
+        std::vector<double> ecur((size_t)M, 0.0);
+        while (true) {
+            rc = ritz_vectors(c, N, VJ, HMAT, MM, K, p->e0, M, A, EV, work, lwork, devinfo, vectors_host, resid,
+                              ecur.data());
+            if (rc) break;
+            std::copy(ecur.begin(), ecur.end(), cur.begin());
+            status = K;
+            inf.krylov = K;
+            double rmax = 0.0;
+            for (int i = 0; i < M; ++i) rmax = std::max(rmax, resid[i]);
+            if (p->verbose) printf(" Cnt= %d  max FP64 residual= %.6e\n", K, rmax);
+            if (rmax <= refine_tol || rounds >= refine_max || K + 1 >= MM) break;
+            const int hi = std::min(MM, K + std::max(p->stepcnt, K / 20));
+            int ret = 0;
+            rc = pisth0(K + 1, hi, &ret);
+            if (rc) break;
+            if (ret != hi) break;   // the linear solver or the orthogonalisation failed: keep K
+            K = hi;
+            ++rounds;
+        }
+        if (refine_steps) *refine_steps = rounds;
+        inf.t_resid += now() - t0;
+    } else if ((vectors_host || resid) && rc == 0 && status > 0) {
         const double t0 = now();
         cusolverDnSetStream(sol, s);
         int r2 = ritz_vectors(c, N, VJ, HMAT, MM, status, p->e0, M, A, EV, work, lwork, devinfo, vectors_host,
@@ -1064,13 +1107,15 @@ struct CtxOps : PistOps {
 };
 
 int pist_ctx(scalit_ctx *c, const scalit_pist_params *p, const double *dx0, double *eig, double *res,
-             scalit_pist_info *info, double *vectors_host, const PistBasisOut *basis, double *resid)
+             scalit_pist_info *info, double *vectors_host, const PistBasisOut *basis, double *resid,
+             double refine_tol, int refine_max, int *refine_steps)
 {
     if (!c->osb_built) { set_error("PIST needs the preconditioner: build or load it first"); return SCALIT_ESTATE; }
     CtxOps ops;
     ops.c = c;
     ops.p = p;
-    return pist_core(c, c->L.N, p, dx0, ops, eig, res, info, vectors_host, basis, resid);
+    return pist_core(c, c->L.N, p, dx0, ops, eig, res, info, vectors_host, basis, resid, refine_tol, refine_max,
+                     refine_steps);
 }
 
 }  // namespace sc

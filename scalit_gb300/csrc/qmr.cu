@@ -769,6 +769,86 @@ template <class T> struct CtxQmrOps : QmrOps<T> {
     }
 };
 
+// Mixed-precision iterative refinement around the FP32 QMR: X = 0, r = B;
+// each round solves (H - E0) d = r in FP32 (the context's FP32 operators, the
+// QMR's own test with tolerance max(1e-4, qmrtol |B - r| / |r|), x0 = 0),
+// adds d to X in FP64 and forms r = B - (H - E0) X with an FP64 H*X.  It stops
+// when |r| <= qmrtol |B - r| (the type -1 measure |HX - B| / |HX| in FP64),
+// after 5 rounds, or when the rounds have used qmrmax iterations.  The code
+// is the total iteration count, negated when the tolerance was not reached;
+// an FP32 round that breaks down ends the solve with its code.
+static int qmr_refined(scalit_ctx *c, int ntype, int qmrmax, double qmrtol, const double *dB, double *dX,
+                       QmrResult *out)
+{
+    const i64 n = c->L.N;
+    cudaStream_t s = c->stream;
+    double *r = nullptr, *d = nullptr, *dd = nullptr;
+    float *bx = nullptr;
+    int rc = 0;
+    if (cudaMallocAsync(&r, sizeof(double) * (size_t)n, s) != cudaSuccess ||
+        cudaMallocAsync(&d, sizeof(double) * (size_t)n, s) != cudaSuccess ||
+        cudaMallocAsync(&dd, sizeof(double) * 4, s) != cudaSuccess ||
+        cudaMallocAsync(&bx, sizeof(float) * 2 * (size_t)n, s) != cudaSuccess) {
+        cudaGetLastError();
+        set_error("refined QMR workspace does not fit");
+        rc = SCALIT_ENOMEM;
+    }
+    auto norm2 = [&](const double *x, double *h) -> int {
+        int e = dot_dev<double>(c, n, x, x, dd, s);
+        if (!e) e = sync_read_doubles(c, dd, h, 1);
+        return e;
+    };
+    double nb = 0.0;
+    if (!rc) rc = norm2(dB, &nb);
+    if (!rc && cudaMemsetAsync(dX, 0, sizeof(double) * (size_t)n, s) != cudaSuccess) rc = SCALIT_ECUDA;
+    if (!rc && cudaMemcpyAsync(r, dB, sizeof(double) * (size_t)n, cudaMemcpyDeviceToDevice, s) != cudaSuccess)
+        rc = SCALIT_ECUDA;
+    QmrResult res{};
+    int total = 0;
+    bool converged = false;
+    double rel = 1.0, nr2 = nb;
+    CtxQmrOps<float> ops;
+    ops.c = c;
+    for (int round = 0; round < 5 && !rc && !converged && total < qmrmax; ++round) {
+        if (nr2 == 0.0) { converged = true; break; }
+        const double tin = std::min(0.5, std::max(1e-4, qmrtol / std::max(rel, 1e-300)));
+        QmrResult q{};
+        rc = to_f32(r, bx, n, s);
+        if (!rc) rc = qmr_core<float>(c, n, ops, ntype > 0 ? -1 : ntype, qmrmax - total, tin, bx, bx + n, &q);
+        if (rc) break;
+        total += q.iters;
+        res.breakdown = q.breakdown;
+        if (q.breakdown) { res.code = q.code; break; }
+        rc = to_f64(bx + n, d, n, s);
+        if (!rc) rc = axpy_dev(n, 1.0, d, dX, s);
+        // r = B - (H - E0) X in FP64
+        if (!rc) rc = hx_vec<double>(c, dX, r, c->E0, -1.0, nullptr, s);
+        if (!rc) rc = axpy_dev(n, 1.0, dB, r, s);
+        double hx2 = 0.0;
+        if (!rc) rc = norm2(r, &nr2);
+        if (rc) break;
+        // |HX|^2 = |B - r|^2
+        if (cudaMemcpyAsync(d, dB, sizeof(double) * (size_t)n, cudaMemcpyDeviceToDevice, s) != cudaSuccess) {
+            rc = SCALIT_ECUDA;
+            break;
+        }
+        rc = axpy_dev(n, -1.0, r, d, s);
+        if (!rc) rc = norm2(d, &hx2);
+        if (rc) break;
+        rel = (hx2 > 0.0) ? std::sqrt(nr2 / hx2) : 1.0;
+        res.res = rel;
+        converged = rel <= qmrtol;
+    }
+    if (!rc && !res.breakdown) res.code = converged ? std::max(total, 1) : -std::max(total, 1);
+    res.iters = total;
+    if (r) cudaFreeAsync(r, s);
+    if (d) cudaFreeAsync(d, s);
+    if (dd) cudaFreeAsync(dd, s);
+    if (bx) cudaFreeAsync(bx, s);
+    if (!rc && out) *out = res;
+    return rc;
+}
+
 int qmr_run(scalit_ctx *c, int ntype, int qmrmax, double qmrtol, int precision,
             const double *dB, double *dX, QmrResult *out)
 {
@@ -779,6 +859,7 @@ int qmr_run(scalit_ctx *c, int ntype, int qmrmax, double qmrtol, int precision,
         ops.c = c;
         return qmr_core<double>(c, n, ops, ntype, qmrmax, qmrtol, dB, dX, out);
     }
+    if (precision == SCALIT_PREC_FP32_REFINED) return qmr_refined(c, ntype, qmrmax, qmrtol, dB, dX, out);
     if (precision != SCALIT_PREC_FP32) { set_error("unknown precision %d", precision); return SCALIT_EINVAL; }
     float *bx = nullptr;
     SC_CUDA(cudaMallocAsync(&bx, sizeof(float) * 2 * (size_t)n, c->stream));

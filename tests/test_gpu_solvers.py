@@ -129,7 +129,7 @@ def test_pist_long_run_orthogonality(lib, orc):
 ORTH_TOL = 3e-15   # max |V^T V - I|: FP64 round-off; an FP32-rounded update coefficient gives ~1e-14
 
 
-@pytest.mark.parametrize("orth", [1, 2])
+@pytest.mark.parametrize("orth", [1, 2, 3])
 def test_pist_basis_orthogonality(lib, orc, c0, orth):
     """The Krylov basis after classical Gram-Schmidt twice is orthonormal to FP64
     round-off, in FP64 (orth=1) and in the mixed form (orth=2: FP32 first pass,
@@ -172,7 +172,7 @@ def test_pist_bad_params(lib, c0):
         assert st == 0
         assert info["qmr_solves"] == 0
         with pytest.raises(capi.ScalitError):
-            ctx.pist(np.ones(c0.N), 5, 0.0, 1e-8, m_max=100, orth=3)
+            ctx.pist(np.ones(c0.N), 5, 0.0, 1e-8, m_max=100, orth=4)
 
 
 def test_qmr_matches_oracle_iteration_for_iteration(lib, orc, c0):
