@@ -50,6 +50,7 @@ REFINE_TOL, REFINE_STEPS, PIST_QMR_TOL = 1e-8, 20, 1e-6
 # FP32 H*X engines timed by the bench, and the kernel each runs
 FP32_ENGINES = (("simt", 0), ("tensor_bf16x3", 1))
 FP32_KERNEL = {"simt": "gemm_kernel<float>", "tensor_bf16x3": "tc32_level_kernel"}
+FP32_PROFILE = {"simt": "gemm_kernel_f32", "tensor_bf16x3": "tc32_level_kernel"}
 
 
 def parse():
@@ -494,10 +495,12 @@ def run_ours(args):
     ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     with ClockSampler(local) as clk:
         with torch.cuda.stream(stream):
+            torch.cuda.nvtx.range_push("hx_fp64_step")    # names the launches for ncu --nvtx-include
             ev0.record(stream)
             for i in range(args.steps):
                 step(i)
             ev1.record(stream)
+            torch.cuda.nvtx.range_pop()
         torch.cuda.synchronize()
     if world > 1:
         torch.distributed.barrier()
@@ -541,17 +544,19 @@ def run_ours(args):
     X32 = [x.float() for x in X]
     Y32 = [torch.empty_like(x) for x in X32]
 
-    def time_f32(fn, steps=args.steps):
+    def time_f32(fn, steps=args.steps, label="fp32"):
         with torch.cuda.stream(stream):
             for i in range(3):
                 fn(X32[i % 2], Y32[i % 2], nvec, capi.TA1)
         torch.cuda.synchronize()
         a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         with torch.cuda.stream(stream):
+            torch.cuda.nvtx.range_push(label)
             a.record(stream)
             for i in range(steps):
                 fn(X32[i % 2], Y32[i % 2], nvec, capi.TA1)
             b.record(stream)
+            torch.cuda.nvtx.range_pop()
         torch.cuda.synchronize()
         return steps * nvec / (a.elapsed_time(b) / 1e3)
 
@@ -559,7 +564,7 @@ def run_ours(args):
     fp32 = {"dtype": "f32", "engines_apps_per_s": {}, "engines_level_ms": {}}
     for name, mode in FP32_ENGINES:
         ctx.set_fp32_mode(mode)
-        fp32["engines_apps_per_s"][name] = time_f32(ctx.hx_f32_device)
+        fp32["engines_apps_per_s"][name] = time_f32(ctx.hx_f32_device, label=f"hx_fp32_{name}")
         fp32["engines_level_ms"][name] = ctx.hx_level_times(X32[0], Y32[0], nvec, reps=10)
     best = max(fp32["engines_apps_per_s"], key=fp32["engines_apps_per_s"].get)
     lms = fp32["engines_level_ms"][best]
@@ -570,8 +575,7 @@ def run_ours(args):
                  "roofline": {"bound": "hbm", "achieved": a32, "peak": hbm, "unit": "GB/s", "frac": a32 / hbm,
                               "kernel": f"{FP32_KERNEL[best]} level {d32 + 1}",
                               "algorithmic_bytes_per_launch": nvec * lv32[d32]["bytes"], "launch_ms": lms[d32],
-                              "traffic": profiled_traffic(FP32_KERNEL[best].split("<")[0], args.workload,
-                                                          d32 + 1, nvec),
+                              "traffic": profiled_traffic(FP32_PROFILE[best], args.workload, d32 + 1, nvec),
                               "peak_source": peak_src}})
     ctx.set_fp32_mode(capi.FP32_SIMT)
 
