@@ -102,8 +102,9 @@ WORKLOADS = {
     "tri-96x96x64": (Grid3(96, 96, 64), PES()),
     # 3,072,000 points, P2 amplitude 0.005 Eh: the precision form, 200 levels.
     "tri-160x160x120": (Grid3(160, 160, 120), PES(amp2=0.005)),
-    # 1,572,864 points: the differentiation form.
-    "tri-128x128x96": (Grid3(128, 128, 96), PES()),
+    # 1,572,864 points: the differentiation form (all three anisotropy terms on,
+    # so every one of the 12 parameters moves the levels).
+    "tri-128x128x96": (Grid3(128, 128, 96), PES(amp1=0.001, amp3=0.0005, width1=1.2, width3=0.8)),
 }
 
 

@@ -113,3 +113,78 @@ def test_hellmann_feynman_vs_finite_differences(lib):
         pm[j] -= h
         fd = (levels(pes.with_params(pp))[0] - levels(pes.with_params(pm))[0]) / (2 * h)
         np.testing.assert_allclose(g[:, j], fd, rtol=2e-3, atol=2e-7)
+
+
+@pytest.mark.slow
+def test_differentiation_form_128x128x96(lib, orc):
+    """The differentiation workload at its stated size (1,572,864 points).
+
+    Adjoint H*X with respect to X, the V grid and K_R, K_r, K_theta in FP64
+    against the FP64 CPU reference gradient (the oracle's H applied to Ybar,
+    Ybar * X, and the contractions of Ybar with X per level), and in FP32
+    against the FP64 result; then Hellmann-Feynman dE_k/dp for the 50 lowest
+    levels and all 12 PES parameters against central differences of the
+    levels with relative step 1e-6 (levels taken to an FP64 residual of 1e-9
+    Eh, so their error, ~r^2/gap, is far below the differences)."""
+    torch = pytest.importorskip("torch")
+    p = hm.workload("tri-128x128x96")
+    n_r, n_R, n_t = p.sizes
+    rng = np.random.default_rng(12)
+    x, yb = rng.standard_normal(p.N), rng.standard_normal(p.N)
+    e0 = float(p.RES.min())
+    ref = orc.Operator.from_problem(p, E0=e0)
+    X = x.reshape(p.sizes, order="F")
+    Yb = yb.reshape(p.sizes, order="F")
+    c = p.DEP.reshape(n_r, n_R, order="F")
+    with capi.Context.from_problem(p, e0=e0) as ctx:
+        xb, vb, hb = ctx.hx_adjoint(x, yb, capi.TA1)
+        dx = torch.tensor(x, dtype=torch.float32, device="cuda")
+        dy = torch.tensor(yb, dtype=torch.float32, device="cuda")
+        dxb, dvb = torch.empty_like(dx), torch.empty_like(dx)
+        dhb = torch.empty(hb.size, dtype=torch.float32, device="cuda")
+        ctx.hx_adjoint_device(dx, dy, dxb, dvb, dhb, f32=True)
+        torch.cuda.ExternalStream(ctx.stream).synchronize()
+    assert rel(xb, ref.hx(yb, 1)) < 1e-12           # H - E0 is symmetric: Xbar = (H - E0) Ybar
+    np.testing.assert_allclose(vb, yb * x, rtol=1e-14)
+    off = [0, n_r ** 2, n_r ** 2 + n_R ** 2]
+    gKr = np.einsum("ibt,jbt->ij", Yb, X)
+    gKR = np.einsum("aib,ajb->ij", Yb, X)
+    gKt = np.einsum("ab,abi,abj->ij", c, Yb, X)
+    assert rel(hb[off[0]:off[1]].reshape(n_r, n_r, order="F"), gKr) < 1e-12
+    assert rel(hb[off[1]:off[2]].reshape(n_R, n_R, order="F"), gKR) < 1e-12
+    assert rel(hb[off[2]:].reshape(n_t, n_t, order="F"), gKt) < 1e-12
+    assert rel(dxb.double().cpu().numpy(), xb) < 2e-6
+    assert rel(dvb.double().cpu().numpy(), vb) < 1e-6
+    assert rel(dhb.double().cpu().numpy(), hb) < 1e-4
+
+    # Hellmann-Feynman, 50 levels x 12 parameters
+    M = 50
+    grid, pes = hm.WORKLOADS["tri-128x128x96"]
+    rr, RR, cth = p.grids["r"], p.grids["R"], p.grids["cos_theta"]
+    dv = hm.potential_grad(rr[:, None, None], RR[None, :, None], cth[None, None, :], pes)
+    dvdp = np.stack([np.ascontiguousarray(g).ravel(order="F") for g in dv])
+    x0 = np.random.default_rng(0).random(p.N)
+
+    def levels(pp, vectors=False):
+        prob = hm.build_problem(grid, pp)
+        with capi.Context.from_problem(prob, e0=e0) as cx:
+            cx.build_osb(20, 1e-4)
+            st, eig, _, info = cx.pist(x0, M, e0, 1e-12, m_max=800, qmr_max=2000, qmr_tol=1e-7,
+                                       refine_tol=1e-9, refine_steps=20, vectors=vectors)
+            assert st > 0 and np.max(info["resid"]) <= 1e-9
+            g = cx.hf_gradients(info["vectors"], dvdp) if vectors else None
+        return eig, g
+
+    eig0, g = levels(pes, vectors=True)
+    base = pes.params()
+    worst = 0.0
+    for j in range(12):
+        h = 1e-6 * abs(base[j])
+        pp, pm = base.copy(), base.copy()
+        pp[j] += h
+        pm[j] -= h
+        fd = (levels(pes.with_params(pp))[0] - levels(pes.with_params(pm))[0]) / (2 * h)
+        err = np.abs(g[:, j] - fd) / (np.abs(fd) + 1e-6 * np.abs(fd).max() + 1e-12)
+        worst = max(worst, float(err.max()))
+        np.testing.assert_allclose(g[:, j], fd, rtol=1e-3, atol=1e-5 * np.abs(fd).max() + 1e-9)
+    print(f"HF vs central differences, 50 levels x 12 parameters: worst relative difference {worst:.2e}")
