@@ -67,6 +67,11 @@ extern "C" {
                                    QMR's attainable residual), the preconditioner, whose
                                    accuracy only sets the convergence rate, takes the
                                    faster engine                                         */
+#define SCALIT_FP32_TENSOR16 3 /* H*X levels in split-FP16 x3 on the tensor cores with
+                                  exponent scaling (per vector and per matrix column;
+                                  ~22 significant bits, the accuracy of the CUDA-core
+                                  GEMM), persistent pipelined kernels; preconditioner
+                                  rotations in split-BF16 x3                          */
 
 /* arithmetic of the QMR inner solves */
 #define SCALIT_PREC_FP64 0
@@ -111,10 +116,12 @@ int scalit_set_stream(scalit_ctx *ctx, void *stream);
  * the FP64 pipe. */
 int scalit_set_fp64_mode(scalit_ctx *ctx, int mode);
 /* Engine of the FP32 level products and preconditioner rotations
- * (SCALIT_FP32_SIMT, SCALIT_FP32_TENSOR or SCALIT_FP32_TENSOR_PX; levels above
- * 256 points stay on the CUDA cores).  Split-BF16 x3 carries ~16 significant
- * bits (H*X relative error ~4e-6 against ~2e-7 on the CUDA cores).  No
- * reference counterpart: the reference has no FP32 path. */
+ * (SCALIT_FP32_SIMT, SCALIT_FP32_TENSOR, SCALIT_FP32_TENSOR_PX or
+ * SCALIT_FP32_TENSOR16; levels above 256 points stay on the CUDA cores, and
+ * SCALIT_FP32_TENSOR16 levels whose matrix does not fit one persistent tile
+ * too).  Split-BF16 x3 carries ~16 significant bits (H*X relative error ~4e-6
+ * against ~2e-7 on the CUDA cores); split-FP16 x3 with exponent scaling
+ * carries ~22.  No reference counterpart: the reference has no FP32 path. */
 int scalit_set_fp32_mode(scalit_ctx *ctx, int mode);
 /* sOSBW%mE0: the shift of (H - E0) and of the preconditioner. */
 int scalit_set_shift(scalit_ctx *ctx, double e0);

@@ -16,7 +16,7 @@ TA0, TA1 = 0, 1
 TOSB, TOSBD1, TOSBD2, TOSBW = 1, 2, 3, 4
 # nType codes of the complex forms (osb.data.h:18-22)
 TAAP0, TMAP0, TAAP, TAAPP, TAAPR, TMAP, TMAPP, TMAPR = 2, 3, 100, 101, 102, 200, 201, 202
-FP32_SIMT, FP32_TENSOR, FP32_TENSOR_PX = 0, 1, 2
+FP32_SIMT, FP32_TENSOR, FP32_TENSOR_PX, FP32_TENSOR16 = 0, 1, 2, 3
 PREC_FP64, PREC_FP32, PREC_FP32_REFINED = 0, 1, 2
 FP64_DFMA, FP64_TENSOR = 0, 1
 FMAX = 20

@@ -166,7 +166,7 @@ void scalit_destroy(scalit_ctx *c)
     for (int l = 0; l < SCALIT_FMAX; ++l) {
         if (c->tc[l].dig) cudaFree(c->tc[l].dig);
         if (c->tc[l].exps) cudaFree(c->tc[l].exps);
-        if (l == 0) { tc_free_px(c); tc32_free(c, true, true); }
+        if (l == 0) { tc_free_px(c); tc32_free(c, true, true); tc16_free(c); }
     }
     if (c->tc_err) cudaFree(c->tc_err);
     osbw_free(c);
@@ -263,6 +263,7 @@ int scalit_load(scalit_ctx *c, const double *H0, const double *RES, const double
     SC_CUDA(cudaStreamSynchronize(s));
     rc = tc_prepare(c);
     if (!rc) rc = tc32_prepare(c, false);
+    if (!rc) rc = tc16_prepare(c);
     if (rc) return rc;
     memset(c->tile_pick, -1, sizeof(c->tile_pick));
     rc = gemm_autotune(c, 16);
@@ -297,7 +298,8 @@ int scalit_set_fp64_mode(scalit_ctx *c, int mode)
 int scalit_set_fp32_mode(scalit_ctx *c, int mode)
 {
     if (!c) { set_error("null context"); return SCALIT_EINVAL; }
-    if (mode != SCALIT_FP32_SIMT && mode != SCALIT_FP32_TENSOR && mode != SCALIT_FP32_TENSOR_PX) {
+    if (mode != SCALIT_FP32_SIMT && mode != SCALIT_FP32_TENSOR && mode != SCALIT_FP32_TENSOR_PX &&
+        mode != SCALIT_FP32_TENSOR16) {
         set_error("unknown FP32 mode %d", mode);
         return SCALIT_EINVAL;
     }

@@ -293,6 +293,28 @@ int hx_batch(const scalit_ctx *c, const T *X, T *Y, int nvec, T shift, T alpha, 
     const T *OUTH = pick<T>(c, c->OUTH, c->OUTHf);
     int rc;
     int first = 0;
+    // FP32 tensor-core forms: the persistent pipelined level kernel wherever
+    // it applies (split-FP16 x3 needs the vectors' scales first)
+    bool p16 = false, pbf = false;
+    if constexpr (std::is_same<T, float>::value) {
+        const bool aligned = !(reinterpret_cast<uintptr_t>(X) & 15) && !(reinterpret_cast<uintptr_t>(Y) & 15);
+        p16 = aligned && c->fp32_mode == SCALIT_FP32_TENSOR16;
+        pbf = aligned && c->fp32_mode == SCALIT_FP32_TENSOR;
+        bool any16 = false;
+        for (int l = 0; l < L.nlev && p16; ++l) any16 = any16 || tc32p_usable(c, l, true);
+        if (any16) {
+            rc = tc16_scales(c, X, nvec, gate, s, vgate, vstride);
+            if (rc) return rc;
+        } else {
+            p16 = false;
+        }
+    }
+    // The diagonal term rides on the first level's epilogue, except on the
+    // persistent kernel: there the last level (grid points contiguous per
+    // column, its output already read for the accumulation) takes it, so the
+    // first level's epilogue loads nothing.
+    int diag_level = 0;
+    if ((p16 || pbf) && L.nlev > 1 && tc32p_usable(c, L.nlev - 1, p16)) diag_level = L.nlev - 1;
     if (L.ndvr && L.nlev == 1) {
         const int threads = 256;
         if (shiftv) { set_error("per-vector shifts with a single outer layer"); return SCALIT_EUNSUP; }
@@ -305,7 +327,7 @@ int hx_batch(const scalit_ctx *c, const T *X, T *Y, int nvec, T shift, T alpha, 
     }
     for (int l = 0; l < L.nlev; ++l) {
         if (c->lev_ev) cudaEventRecord(c->lev_ev[l], s);
-        const bool fuse_diag = (l == 0 && !first);
+        const bool fuse_diag = (l == diag_level && !first);
         if constexpr (std::is_same<T, double>::value) {
             if (c->fp64_mode == SCALIT_FP64_TENSOR && tc_usable(c, l)) {
                 rc = tc_level_apply(c, l, X, Y, l > 0 || first, fuse_diag ? RES : nullptr, shift, alpha,
@@ -314,6 +336,12 @@ int hx_batch(const scalit_ctx *c, const T *X, T *Y, int nvec, T shift, T alpha, 
                 continue;
             }
         } else {
+            if ((p16 || pbf) && tc32p_usable(c, l, p16)) {
+                rc = tc32p_level_apply(c, l, p16, X, Y, l > 0 || first, fuse_diag ? RES : nullptr, shift, alpha,
+                                       gate, s, nvec, shiftv, vgate, vstride);
+                if (rc) return rc;
+                continue;
+            }
             if (tc32_usable(c, l)) {
                 rc = tc32_level_apply(c, l, X, Y, l > 0 || first, fuse_diag ? RES : nullptr, shift, alpha,
                                       gate, s, nvec, shiftv, vgate, vstride);

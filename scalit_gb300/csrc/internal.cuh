@@ -53,6 +53,7 @@ template <class T> struct DevBuf {
 struct TcLevelData {
     uint16_t *dig = nullptr;   // [ntiles][KS][7][NT x 16] BF16 bits
     int *exps = nullptr;       // [ntiles * NT] column exponents
+    float *cscale = nullptr;   // [NT] inverse column scales (FP16 planes)
     int NT = 0, ntiles = 0, KS = 0, usable = 0;
 };
 
@@ -113,6 +114,10 @@ struct scalit_ctx {
     TcLevelData tc[SCALIT_FMAX];
     // digit planes of the preconditioner's rotations, levels >= 2: [level][VX, VTX]
     TcLevelData pxtc[SCALIT_FMAX][2];
+    // FP16 hi/lo planes of the level matrices with their column scales
+    // (SCALIT_FP32_TENSOR16) and the per-vector scale slots of one launch
+    TcLevelData tc16[SCALIT_FMAX];
+    unsigned *xmax = nullptr;
     int *tc_err = nullptr;
     // Measurement aid: when set, hx_batch records lev_ev[l] before level l's
     // launch and lev_ev[nlev] after the last (scalit_hx_level_times).
@@ -212,6 +217,14 @@ int tc32_level_apply(const scalit_ctx *c, int level, const float *X, float *Y, i
                      const float *shiftv = nullptr, const int *vgate = nullptr, int vstride = 0);
 int tc32_rot_apply(const scalit_ctx *c, int level, int transpose, const float *X, float *Y, const int *gate,
                    cudaStream_t s, int nvec = 1, const int *vgate = nullptr, int vstride = 0);
+int tc16_prepare(scalit_ctx *c);
+void tc16_free(scalit_ctx *c);
+bool tc32p_usable(const scalit_ctx *c, int level, bool f16);
+int tc16_scales(const scalit_ctx *c, const float *X, int nvec, const int *gate, cudaStream_t s,
+                const int *vgate = nullptr, int vstride = 0);
+int tc32p_level_apply(const scalit_ctx *c, int level, bool f16, const float *X, float *Y, int accumulate,
+                      const float *diagV, float shift, float alpha, const int *gate, cudaStream_t s, int nvec,
+                      const float *shiftv = nullptr, const int *vgate = nullptr, int vstride = 0);
 int tc_prepare(scalit_ctx *c);
 int tc_prepare_px(scalit_ctx *c);
 void tc_free_px(scalit_ctx *c);

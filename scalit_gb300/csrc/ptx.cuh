@@ -80,6 +80,20 @@ __device__ __forceinline__ bool mbar_wait_timed(uint64_t *mbar, uint32_t parity,
     }
 }
 
+// Wait for warps that idle most of the time: a back-off sleep between polls
+// leaves the issue slots to the working warps (bounded by the global timer).
+__device__ __forceinline__ bool mbar_wait_sleep(uint64_t *mbar, uint32_t parity, uint32_t sleep_ns,
+                                                uint64_t limit_ns = kMbarWaitNs)
+{
+    if (mbar_try(mbar, parity)) return true;
+    const uint64_t t0 = globaltimer_ns();
+    for (;;) {
+        __nanosleep(sleep_ns);
+        if (mbar_try(mbar, parity)) return true;
+        if (globaltimer_ns() - t0 > limit_ns) return false;
+    }
+}
+
 // One arrival that also announces `bytes` of transaction count.
 __device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t *mbar, uint32_t bytes)
 {
@@ -110,6 +124,12 @@ __device__ __forceinline__ void bulk_g2s(void *dst, const void *src, uint32_t by
         :: "r"(smem_addr(dst)), "l"(src), "r"(bytes), "r"(smem_addr(mbar)) : "memory");
 }
 
+// Bulk prefetch of `bytes` (a multiple of 16, 16-byte aligned) into L2.
+__device__ __forceinline__ void prefetch_l2_bulk(const void *src, uint32_t bytes)
+{
+    asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" :: "l"(src), "r"(bytes) : "memory");
+}
+
 // ------------------------------------------------------------ tcgen05 --
 // Shared-memory matrix descriptor, K-major, no swizzle: start address, the
 // byte distance between core matrices along K (LBO) and along M/N (SBO).
@@ -127,6 +147,12 @@ __device__ __forceinline__ uint64_t smem_desc(uint32_t saddr, uint32_t lbo, uint
 __host__ __device__ constexpr uint32_t idesc_bf16(int n, int m = 128)
 {
     return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(n >> 3) << 17) | ((uint32_t)(m >> 4) << 24);
+}
+
+// Instruction descriptor, kind::f16: D = F32, A = B = F16, both K-major, M x n.
+__host__ __device__ constexpr uint32_t idesc_f16(int n, int m = 128)
+{
+    return (1u << 4) | ((uint32_t)(n >> 3) << 17) | ((uint32_t)(m >> 4) << 24);
 }
 
 __device__ __forceinline__ void tc_mma(uint32_t d_tmem, uint64_t adesc, uint64_t bdesc, uint32_t idesc,
@@ -166,6 +192,19 @@ __device__ __forceinline__ void tmem_ld8(uint32_t taddr, float (&v)[8])
         : "r"(taddr));
     #pragma unroll
     for (int i = 0; i < 8; ++i) v[i] = __uint_as_float(r[i]);
+}
+
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float (&v)[16])
+{
+    uint32_t r[16];
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, "
+        "%14, %15}, [%16];"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+          "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+        : "r"(taddr));
+    #pragma unroll
+    for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
 }
 
 }  // namespace sc

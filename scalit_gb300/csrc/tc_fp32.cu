@@ -505,7 +505,8 @@ bool tc32_usable(const scalit_ctx *c, int l)
 
 bool tc32_px_usable(const scalit_ctx *c, int l)
 {
-    return (c->fp32_mode == SCALIT_FP32_TENSOR || c->fp32_mode == SCALIT_FP32_TENSOR_PX) &&
+    return (c->fp32_mode == SCALIT_FP32_TENSOR || c->fp32_mode == SCALIT_FP32_TENSOR_PX ||
+            c->fp32_mode == SCALIT_FP32_TENSOR16) &&
            c->pxtc32[l][0].usable && c->pxtc32[l][1].usable;
 }
 
