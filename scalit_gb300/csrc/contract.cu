@@ -314,7 +314,7 @@ int hx_batch(const scalit_ctx *c, const T *X, T *Y, int nvec, T shift, T alpha, 
     // column, its output already read for the accumulation) takes it, so the
     // first level's epilogue loads nothing.
     int diag_level = 0;
-    if ((p16 || pbf) && L.nlev > 1 && tc32p_usable(c, L.nlev - 1, p16)) diag_level = L.nlev - 1;
+    if ((p16 || pbf) && L.nlev > 1 && tc32p_usable(c, L.nlev - 1, p16, true)) diag_level = L.nlev - 1;
     if (L.ndvr && L.nlev == 1) {
         const int threads = 256;
         if (shiftv) { set_error("per-vector shifts with a single outer layer"); return SCALIT_EUNSUP; }
@@ -336,7 +336,7 @@ int hx_batch(const scalit_ctx *c, const T *X, T *Y, int nvec, T shift, T alpha, 
                 continue;
             }
         } else {
-            if ((p16 || pbf) && tc32p_usable(c, l, p16)) {
+            if ((p16 || pbf) && tc32p_usable(c, l, p16, fuse_diag)) {
                 rc = tc32p_level_apply(c, l, p16, X, Y, l > 0 || first, fuse_diag ? RES : nullptr, shift, alpha,
                                        gate, s, nvec, shiftv, vgate, vstride);
                 if (rc) return rc;

@@ -219,7 +219,7 @@ int tc32_rot_apply(const scalit_ctx *c, int level, int transpose, const float *X
                    cudaStream_t s, int nvec = 1, const int *vgate = nullptr, int vstride = 0);
 int tc16_prepare(scalit_ctx *c);
 void tc16_free(scalit_ctx *c);
-bool tc32p_usable(const scalit_ctx *c, int level, bool f16);
+bool tc32p_usable(const scalit_ctx *c, int level, bool f16, bool diag = false);
 int tc16_scales(const scalit_ctx *c, const float *X, int nvec, const int *gate, cudaStream_t s,
                 const int *vgate = nullptr, int vstride = 0);
 int tc32p_level_apply(const scalit_ctx *c, int level, bool f16, const float *X, float *Y, int accumulate,

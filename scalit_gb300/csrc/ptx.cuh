@@ -38,6 +38,18 @@ __device__ __forceinline__ bool mbar_try(uint64_t *mbar, uint32_t parity)
     return ok != 0;
 }
 
+// Non-blocking test of a phase (for a thread that polls several barriers).
+__device__ __forceinline__ bool mbar_test(uint64_t *mbar, uint32_t parity)
+{
+    uint32_t ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.test_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.b32 %0, 1, 0, p;\n\t}\n"
+        : "=r"(ok) : "r"(smem_addr(mbar)), "r"(parity) : "memory");
+    return ok != 0;
+}
+
 __device__ __forceinline__ bool mbar_wait(uint64_t *mbar, uint32_t parity, long long limit = kMbarWaitLimit)
 {
     for (long long i = 0; i < limit; ++i)

@@ -2,17 +2,19 @@
 //
 // One CTA per SM walks a strided sequence of 128-row tiles of the grid
 // operand (all vectors of the launch), with the level matrix held in shared
-// memory for the whole launch.  Three groups of warps run a pipeline:
+// memory for the whole launch.  Four roles run a pipeline:
 //
-//   converters (warps 0-7)  load 16-wide K slabs of the FP32 grid operand into
-//                           a ring of shared-memory slots (16-byte cp.async,
-//                           kPDepth slabs in flight), cut each slab into its
-//                           hi/lo planes (K-major canonical layout) in a second
-//                           ring, and arrive on the plane's mbarrier;
-//   MMA warp (warp 16)      issues the three products of every K step into one
-//                           of two TMEM accumulators and commits them to the
+//   load lane (warp 17)     requests 16-wide K slabs of the FP32 grid operand
+//                           by TMA tensor copies into a ring of shared-memory
+//                           slots (6-7 deep; slot "full" and "empty"
+//                           mbarriers);
+//   MMA lane (warp 16)      issues the three products of every K step into one
+//                           of two TMEM accumulators, committing them to the
 //                           plane's "free" barrier and, after a tile's last K
 //                           step, to the accumulator's "full" barrier;
+//   converters (warps 0-7)  cut each landed slab into its hi/lo planes
+//                           (K-major canonical layout) in a second ring, two K
+//                           steps per pass, and release the slot;
 //   epilogue (warps 8-15)   drain a full accumulator (scales, DEP row factor,
 //                           fused diagonal term, accumulation) while the next
 //                           tile's products run in the other accumulator.
@@ -29,19 +31,23 @@
 //
 // Operand mapping (as in tc_fp32.cu): A(m, k) is the grid vector seen
 // through the level's strides, B(k, n) = H(n, k), C written with the level's
-// epilogue.  Rows contiguous along k (level 1, a_sk == 1) give outputs
-// contiguous along n: each epilogue warp stages a 32 x 16 block in shared
-// memory and stores it as whole 64-byte row pieces.  Otherwise (a_sk > 1)
-// a warp's 32 TMEM lanes are 32 consecutive grid points of one column and
-// its loads and stores are coalesced as they come.
+// epilogue.  Rows contiguous along k (level 1): the slab is one 2-D box
+// (16 k x 128 rows, 64-byte swizzle) of the view [vector][row][k]; the
+// outputs, contiguous along n, leave through a 32 x 16 stage per epilogue
+// warp, stored by TMA in the same swizzle.  Otherwise (the grid point index
+// fastest within blocks of Mi points, Mi % 32 == 0) the slab is four boxes
+// of 32 points x 16 k of the view [vector][block][k][point], and a warp's 32
+// TMEM lanes are 32 consecutive grid points of one output column, so its
+// loads and stores are coalesced as they come.
 //
 // Every mbarrier wait is bounded; an expired wait raises a shared abort flag
-// after which no role waits again, the converters keep meeting at their
-// named barrier, the MMA warp stops issuing, the error word is set and the
-// CTA frees its TMEM and returns.
+// after which no role waits again, the load and MMA lanes stop issuing and
+// let the copies and products in flight complete, the error word is set and
+// the CTA frees its TMEM and returns.
 #include "internal.cuh"
 #include "ptx.cuh"
 
+#include <cuda.h>
 #include <cuda_bf16.h>
 #include <cuda_fp16.h>
 
@@ -50,14 +56,17 @@ namespace sc {
 static constexpr int kPM = 128;                       // grid rows per tile = TMEM lanes
 static constexpr int kPConv = 256;                    // converter threads
 static constexpr int kPEpiWarps = 8;                  // two per TMEM lane quarter
-static constexpr int kPThreads = kPConv + 32 * kPEpiWarps + 32;
-static constexpr int kPMmaWarp = kPConv / 32 + kPEpiWarps;
-static constexpr int kPDepth = 6;                     // K slabs in flight
-static constexpr int kPSlots = kPDepth + 2;           // FP32 slab slots
+static constexpr int kPThreads = kPConv + 32 * kPEpiWarps + 96;
+static constexpr int kPMmaWarp = kPConv / 32 + kPEpiWarps;     // the MMA lane
+static constexpr int kPLoadWarp = kPMmaWarp + 1;               // the TMA load lane
+static constexpr int kPELoadWarp = kPMmaWarp + 2;              // the epilogue operands' load lane
+static constexpr int kPERingMax = 8;                           // epilogue operand chunks in flight
+static constexpr int kPSlotsMax = 7;                  // FP32 slab slots (rows along k: 7; else 6)
+static constexpr int kPSlotsM = 6;
 static constexpr int kPPlanes = 4;                    // hi/lo plane slots
 static constexpr int kPSlab = kPM * 16 * 4;           // one FP32 slab: 8 KB
 static constexpr int kPPlane = kPM * 16 * 2 * 2;      // hi + lo planes: 8 KB
-static constexpr int kPStage = 32 * 16;               // floats per epilogue warp stage
+static constexpr int kPStage = 32 * 16;               // floats per epilogue stage (2 per warp)
 static constexpr int kPAccCols = 256;                 // TMEM columns per accumulator
 static constexpr int kPMaxSmem = 227 * 1024;
 static constexpr int kPMaxVec = 4096;                 // vectors per launch (scale slots)
@@ -66,7 +75,6 @@ struct Tc32pArgs {
     int M, K, KS, NT, N;       // rows per vector, contraction, K steps, tile columns, output columns
     int mtiles, tiles;         // M tiles per vector, M tiles x vectors
     i64 Mi, s1, s2, a_sk, c_sn;
-    const float *A; i64 a_sz;
     float *C; i64 c_sz;
     const float *rowscale;
     int accumulate;
@@ -81,12 +89,24 @@ struct Tc32pArgs {
     const uint4 *bsplit;       // [KS][hi, lo][NT x 16] canonical K-major
     const float *binv;         // per output column: 2^-e_n (FP16 form)
     const unsigned *xmax;      // per vector: bits of max |x| (FP16 form)
+    int tstore;                // outputs contiguous along n, nothing to add: TMA stores
+    int ering, echunk;         // points fastest: epilogue operand ring slots and bytes per slot
+    int nslots;                // FP32 slab slots
 };
 
-static size_t p_smem_bytes(int NT, int KS)
+// Shared memory: B, slab slots, plane slots, the epilogue region (level 1:
+// two 32 x 16 stages per epilogue warp; otherwise the operand ring), column
+// scales, barriers.
+static size_t p_fixed_bytes(int NT, int KS, int nslots)
 {
-    return (size_t)KS * 2 * NT * 32 + (size_t)kPSlots * kPSlab + (size_t)kPPlanes * kPPlane +
-           (size_t)kPEpiWarps * kPStage * 4 + 256 * 4 + (2 * kPPlanes + 5) * 8 + 16;
+    return (size_t)KS * 2 * NT * 32 + (size_t)nslots * kPSlab + (size_t)kPPlanes * kPPlane + 256 * 4 +
+           (2 * kPSlotsMax + 2 * kPPlanes + 2 * kPERingMax + 6) * 8 + 16;
+}
+static constexpr size_t kPStageBytes = (size_t)kPEpiWarps * 2 * kPStage * 4;
+
+static size_t p_smem_bytes(int NT, int KS, int nslots, size_t ebytes)
+{
+    return p_fixed_bytes(NT, KS, nslots) + (ebytes > kPStageBytes ? ebytes : kPStageBytes);
 }
 
 // Scale exponent e with max|v| 2^e in [2^14, 2^15) from the bits of max|v|
@@ -123,30 +143,71 @@ __device__ __forceinline__ void p_cut2(float x0, float x1, float xs, uint32_t &h
     }
 }
 
+__device__ __forceinline__ void tma_load_3d(void *dst, const CUtensorMap *map, int c0, int c1, int c2, uint64_t *mbar)
+{
+    asm volatile(
+        "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], [%5];"
+        :: "r"(smem_addr(dst)), "l"(reinterpret_cast<uint64_t>(map)), "r"(c0), "r"(c1), "r"(c2), "r"(smem_addr(mbar))
+        : "memory");
+}
+
+__device__ __forceinline__ void tma_load_4d(void *dst, const CUtensorMap *map, int c0, int c1, int c2, int c3,
+                                            uint64_t *mbar)
+{
+    asm volatile(
+        "cp.async.bulk.tensor.4d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4, %5}], [%6];"
+        :: "r"(smem_addr(dst)), "l"(reinterpret_cast<uint64_t>(map)), "r"(c0), "r"(c1), "r"(c2), "r"(c3),
+           "r"(smem_addr(mbar))
+        : "memory");
+}
+
+__device__ __forceinline__ void tma_store_3d(const CUtensorMap *map, const void *src, int c0, int c1, int c2)
+{
+    asm volatile("cp.async.bulk.tensor.3d.global.shared::cta.tile.bulk_group [%0, {%1, %2, %3}], [%4];"
+                 :: "l"(reinterpret_cast<uint64_t>(map)), "r"(c0), "r"(c1), "r"(c2), "r"(smem_addr(src))
+                 : "memory");
+}
+
+__device__ __forceinline__ void tma_store_4d(const CUtensorMap *map, const void *src, int c0, int c1, int c2, int c3)
+{
+    asm volatile("cp.async.bulk.tensor.4d.global.shared::cta.tile.bulk_group [%0, {%1, %2, %3, %4}], [%5];"
+                 :: "l"(reinterpret_cast<uint64_t>(map)), "r"(c0), "r"(c1), "r"(c2), "r"(c3), "r"(smem_addr(src))
+                 : "memory");
+}
+
 template <bool F16>
 __global__ void __launch_bounds__(kPThreads, 1)
-tc32p_level_kernel(Tc32pArgs g)
+tc32p_level_kernel(Tc32pArgs g, const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmC,
+                   const __grid_constant__ CUtensorMap tmV)
 {
     if (g.gate && *g.gate) return;
     extern __shared__ __align__(1024) unsigned char smem[];
     const int NT = g.NT, KS = g.KS;
     const int bstep = 2 * NT * 32;                              // bytes of one K step of B (hi + lo)
     unsigned char *Bs = smem;
-    unsigned char *slots = Bs + (size_t)KS * bstep;
-    unsigned char *planes = slots + kPSlots * kPSlab;
-    float *stage = reinterpret_cast<float *>(planes + kPPlanes * kPPlane);
-    float *binv_s = stage + kPEpiWarps * kPStage;
-    uint64_t *pfull = reinterpret_cast<uint64_t *>(binv_s + 256);
+    unsigned char *slots = Bs + (size_t)KS * bstep;             // 1024-byte aligned (NT % 16 == 0)
+    const int S = g.nslots;
+    unsigned char *planes = slots + S * kPSlab;
+    float *stage = reinterpret_cast<float *>(planes + kPPlanes * kPPlane);     // the epilogue region
+    const size_t ebytes = (size_t)g.ering * g.echunk;
+    float *binv_s = stage + (ebytes > kPStageBytes ? ebytes : kPStageBytes) / 4;
+    uint64_t *full = reinterpret_cast<uint64_t *>(binv_s + 256);
+    uint64_t *empty = full + kPSlotsMax;
+    uint64_t *pfull = empty + kPSlotsMax;
     uint64_t *pfree = pfull + kPPlanes;
     uint64_t *accfull = pfree + kPPlanes;
     uint64_t *accempty = accfull + 2;
-    uint64_t *bready = accempty + 2;
-    volatile int *abort_flag = reinterpret_cast<volatile int *>(bready + 1);
-    uint32_t *tslot = reinterpret_cast<uint32_t *>(bready + 1) + 1;
+    uint64_t *efull = accempty + 2;
+    uint64_t *eempty = efull + kPERingMax;
+    uint64_t *bready = eempty + kPERingMax;
+    uint64_t *drain = bready + 1;                               // products in flight at an abort
+    volatile int *abort_flag = reinterpret_cast<volatile int *>(drain + 1);
+    uint32_t *tslot = reinterpret_cast<uint32_t *>(drain + 1) + 1;
 
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const int G = gridDim.x;
     const int niter = (g.tiles - (int)blockIdx.x + G - 1) / G;  // tiles of this CTA
+    const int nsteps = niter * KS;
     const bool kmajor = (g.a_sk == 1);
     const int Mi32 = (int)g.Mi;
     auto rowoff = [&](int m) -> i64 {
@@ -154,11 +215,20 @@ tc32p_level_kernel(Tc32pArgs g)
         return (i64)(m - mq * Mi32) * g.s1 + (i64)mq * g.s2;
     };
     auto vgated = [&](int z) -> bool { return g.vgate && g.vgate[(i64)z * g.vgate_stride]; };
+    auto fail = [&]() {
+        *abort_flag = 1;
+        if (g.err) atomicExch(g.err, 5);
+    };
 
     if (tid == 0) {
+        // the 64-byte swizzle of the boxes repeats every 512 bytes of shared memory
+        if (smem_addr(slots) & 511) { if (g.err) atomicExch(g.err, 5); }
+        for (int i = 0; i < S; ++i) { mbar_init(&full[i], 1); mbar_init(&empty[i], kPConv); }
         for (int i = 0; i < kPPlanes; ++i) { mbar_init(&pfull[i], kPConv); mbar_init(&pfree[i], 1); }
         for (int b = 0; b < 2; ++b) { mbar_init(&accfull[b], 1); mbar_init(&accempty[b], 32 * kPEpiWarps); }
+        for (int i = 0; i < kPERingMax; ++i) { mbar_init(&efull[i], 1); mbar_init(&eempty[i], 4); }
         mbar_init(bready, 1);
+        mbar_init(drain, 1);
         *abort_flag = 0;
         mbar_init_fence();
         mbar_arrive_expect_tx(bready, (uint32_t)(KS * bstep));
@@ -176,212 +246,204 @@ tc32p_level_kernel(Tc32pArgs g)
     fence_after();
     const uint32_t tbase = *tslot;
 
-    if (warp < 8) {
+    if (warp < kPConv / 32) {
         // ------------------------------------------------------ converters --
-        const int nsteps = niter * KS;
-        // Load cursor: the tile and K step of the next slab to request, this
-        // thread's two 16-byte pieces (source bases at k = 0, validity) and
-        // their fixed destinations in a slot; advanced one step per call.
-        int ci = 0, cks = 0;
-        const float *cbase[2];
-        bool cval[2];
-        uint32_t coff[2];
-        int ck[2];                                  // the piece's own k offset within a slab
-        #pragma unroll
-        for (int r = 0; r < 2; ++r) {
-            const int e = tid + r * kPConv;
-            if (kmajor) {
-                const int row = e >> 2, c = e & 3;
-                coff[r] = row * 64 + 16 * (c ^ ((row >> 1) & 3));
-                ck[r] = 4 * c;
-            } else {
-                const int kk = e >> 5, c = e & 31;
-                coff[r] = kk * 512 + c * 16;
-                ck[r] = kk;
-            }
-        }
-        auto tile_bases = [&](int it) {
-            const int tau = (int)blockIdx.x + it * G;
-            const int z = tau / g.mtiles, m0 = (tau - z * g.mtiles) * kPM;
-            const bool skip = vgated(z);
-            const float *A = g.A + (i64)z * g.a_sz;
-            #pragma unroll
-            for (int r = 0; r < 2; ++r) {
-                const int e = tid + r * kPConv;
-                const int m = kmajor ? m0 + (e >> 2) : m0 + 4 * (e & 31);
-                cval[r] = !skip && m < g.M;
-                cbase[r] = cval[r] ? A + rowoff(m) + (kmajor ? (i64)ck[r] : (i64)ck[r] * g.a_sk) : g.A;
-            }
-        };
-        if (nsteps > 0) tile_bases(0);
-        int qi = 0;                                 // steps requested so far
-        auto issue = [&]() {
-            if (qi < nsteps) {
-                const uint32_t st = smem_addr(slots + (qi % kPSlots) * kPSlab);
-                const int k0 = cks * 16;
-                #pragma unroll
-                for (int r = 0; r < 2; ++r) {
-                    const bool v = cval[r] && k0 + ck[r] < g.K;
-                    const float *src = v ? cbase[r] + (kmajor ? (i64)k0 : (i64)k0 * g.a_sk) : g.A;
-                    asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;"
-                                 :: "r"(st + coff[r]), "l"(src), "r"(v ? 16u : 0u) : "memory");
-                }
-                ++qi;
-                if (++cks == KS) {
-                    cks = 0;
-                    if (++ci < niter) tile_bases(ci);
-                }
-            }
-            asm volatile("cp.async.commit_group;" ::: "memory");
-        };
-        for (int q = 0; q < kPDepth; ++q) issue();
         const int row = tid & (kPM - 1), h = tid >> 7;
         const int poff = (row >> 3) * 256 + h * 128 + (row & 7) * 16;
         const int sw = (row >> 1) & 3;
         int ks = 0, it = 0;
         float xs = 1.0f;
         if (F16 && nsteps > 0) xs = p_pow2(p_scale_exp(g.xmax[(int)blockIdx.x / g.mtiles]));
-        int slot = 0, p = 0;
-        uint32_t pphase = 0;
-        // Two K steps per pass: one wait, one barrier and one fence for both,
-        // so their fixed latencies are paid once per pair.  The two slots
-        // refilled after the barrier held the previous pass's steps, which
-        // every converter has finished reading once it reaches the barrier.
+        int fs = 0, p = 0;                      // slot and plane of the next step
+        uint32_t fph = 0, pphase = 0;
+        // two K steps per pass: one fence and one round of arrivals for both
         for (int q = 0; q < nsteps; q += 2) {
-            asm volatile("cp.async.wait_group %0;" :: "n"(kPDepth - 2) : "memory");
-            asm volatile("bar.sync 1, %0;" :: "n"(kPConv) : "memory");
             const int nu = (q + 1 < nsteps) ? 2 : 1;
             uint32_t hw[2][4], lw[2][4];
+            int used[2];
             #pragma unroll
             for (int u = 0; u < 2; ++u) {
                 if (u >= nu) break;
-                const unsigned char *st = slots + (slot + u < kPSlots ? slot + u : slot + u - kPSlots) * kPSlab;
+                if (!*abort_flag && !mbar_wait(&full[fs], fph)) fail();
+                const unsigned char *st = slots + fs * kPSlab;
                 float x[8];
                 if (kmajor) {
+                    // the box's 64-byte swizzle: 16-byte piece c of row r at c ^ ((r >> 1) & 3)
                     const float4 a = *reinterpret_cast<const float4 *>(st + row * 64 + 16 * ((2 * h) ^ sw));
                     const float4 b = *reinterpret_cast<const float4 *>(st + row * 64 + 16 * ((2 * h + 1) ^ sw));
                     x[0] = a.x; x[1] = a.y; x[2] = a.z; x[3] = a.w;
                     x[4] = b.x; x[5] = b.y; x[6] = b.z; x[7] = b.w;
                 } else {
-                    const float *sf = reinterpret_cast<const float *>(st);
+                    // four boxes [16 k][32 points]
+                    const float *sf = reinterpret_cast<const float *>(st) + (row >> 5) * 512 + (row & 31);
                     #pragma unroll
-                    for (int j = 0; j < 8; ++j) x[j] = sf[(8 * h + j) * kPM + row];
+                    for (int j = 0; j < 8; ++j) x[j] = sf[(8 * h + j) * 32];
                 }
                 #pragma unroll
                 for (int j = 0; j < 4; ++j) p_cut2<F16>(x[2 * j], x[2 * j + 1], xs, hw[u][j], lw[u][j]);
+                used[u] = fs;
+                if (++fs == S) { fs = 0; fph ^= 1u; }
                 if (++ks == KS) {
                     ks = 0;
                     ++it;
                     if (F16 && it < niter) xs = p_pow2(p_scale_exp(g.xmax[((int)blockIdx.x + it * G) / g.mtiles]));
                 }
             }
-            issue();
-            issue();
+            #pragma unroll
+            for (int u = 0; u < 2; ++u)
+                if (u < nu) mbar_arrive(&empty[used[u]]);
             #pragma unroll
             for (int u = 0; u < 2; ++u) {
                 if (u >= nu) break;
-                if (q + u >= kPPlanes && !*abort_flag) {
-                    if (!mbar_wait(&pfree[p], pphase ^ 1u)) {
-                        *abort_flag = 1;
-                        if (g.err) atomicExch(g.err, 5);
-                    }
-                }
+                if (q + u >= kPPlanes && !*abort_flag && !mbar_wait(&pfree[p], pphase ^ 1u)) fail();
                 unsigned char *pl = planes + p * kPPlane;
                 *reinterpret_cast<uint4 *>(pl + poff) = make_uint4(hw[u][0], hw[u][1], hw[u][2], hw[u][3]);
                 *reinterpret_cast<uint4 *>(pl + kPPlane / 2 + poff) = make_uint4(lw[u][0], lw[u][1], lw[u][2], lw[u][3]);
                 if (++p == kPPlanes) { p = 0; pphase ^= 1u; }
             }
             fence_proxy_async_smem();
-            {
-                int pa = p - nu;
-                if (pa < 0) pa += kPPlanes;
-                for (int u = 0; u < nu; ++u) {
-                    mbar_arrive(&pfull[pa]);
-                    if (++pa == kPPlanes) pa = 0;
-                }
+            int pa = p - nu;
+            if (pa < 0) pa += kPPlanes;
+            for (int u = 0; u < nu; ++u) {
+                mbar_arrive(&pfull[pa]);
+                if (++pa == kPPlanes) pa = 0;
             }
-            slot += 2;
-            if (slot >= kPSlots) slot -= kPSlots;
         }
-        asm volatile("cp.async.wait_all;" ::: "memory");
-    } else if (warp == kPMmaWarp) {
-        // -------------------------------------------------------- MMA warp --
-        const uint32_t idesc = F16 ? idesc_f16(NT) : idesc_bf16(NT);
-        if (!mbar_wait_timed(bready, 0)) { *abort_flag = 1; if (g.err) atomicExch(g.err, 5); }
-        int q = 0;
-        for (int it = 0; it < niter; ++it) {
-            const int b = it & 1;
-            if (it >= 2 && !*abort_flag && !mbar_wait_sleep(&accempty[b], (uint32_t)(((it >> 1) - 1) & 1), 64)) {
-                *abort_flag = 1;
-                if (g.err) atomicExch(g.err, 5);
-            }
-            fence_after();
-            for (int ks = 0; ks < KS; ++ks, ++q) {
-                const int p = q % kPPlanes;
-                if (!*abort_flag && !mbar_wait_sleep(&pfull[p], (uint32_t)((q / kPPlanes) & 1), 32)) {
-                    *abort_flag = 1;
-                    if (g.err) atomicExch(g.err, 5);
+    } else if (warp == kPLoadWarp) {
+        // ------------------------------------------------------ load lane --
+        if (lane == 0) {
+            int pit = 0, pks = 0, pz = 0, pm0 = 0;
+            bool pskip = false;
+            auto ptile = [&]() {
+                const int tau = (int)blockIdx.x + pit * G;
+                pz = tau / g.mtiles;
+                pm0 = (tau - pz * g.mtiles) * kPM;
+                pskip = vgated(pz);
+            };
+            if (nsteps > 0) ptile();
+            int prod = 0;
+            for (; prod < nsteps && !*abort_flag; ++prod) {
+                const int sl = prod % S;
+                if (prod >= S && !mbar_wait(&empty[sl], (uint32_t)(((prod / S) - 1) & 1))) {
+                    fail();
+                    break;
                 }
-                fence_after();
-                if (lane == 0) {
-                    if (!*abort_flag) {
-                        const unsigned char *Ab = planes + p * kPPlane;
-                        const uint64_t a_hi = smem_desc(smem_addr(Ab), 128, 256);
-                        const uint64_t a_lo = smem_desc(smem_addr(Ab + kPPlane / 2), 128, 256);
-                        const unsigned char *Bk = Bs + (size_t)ks * bstep;
-                        const uint64_t b_hi = smem_desc(smem_addr(Bk), 128, 256);
-                        const uint64_t b_lo = smem_desc(smem_addr(Bk + NT * 32), 128, 256);
-                        const uint32_t d = tbase + (uint32_t)(b * kPAccCols);
-                        tc_mma(d, a_hi, b_hi, idesc, ks > 0 ? 1u : 0u);
-                        tc_mma(d, a_hi, b_lo, idesc, 1u);
-                        tc_mma(d, a_lo, b_hi, idesc, 1u);
+                unsigned char *dst = slots + sl * kPSlab;
+                if (pskip) {
+                    mbar_arrive(&full[sl]);   // a stopped vector: nothing to load
+                } else {
+                    mbar_arrive_expect_tx(&full[sl], (uint32_t)kPSlab);
+                    if (kmajor) {
+                        tma_load_3d(dst, &tmA, pks * 16, pm0, pz, &full[sl]);
+                    } else {
+                        #pragma unroll
+                        for (int j = 0; j < 4; ++j) {
+                            const int m = pm0 + 32 * j;
+                            tma_load_4d(dst + j * 2048, &tmA, m % Mi32, pks * 16, m / Mi32, pz, &full[sl]);
+                        }
                     }
-                    tc_commit(&pfree[p]);
                 }
-                __syncwarp();
+                if (++pks == KS) {
+                    pks = 0;
+                    if (++pit < niter) ptile();
+                }
             }
-            if (lane == 0) tc_commit(&accfull[b]);
-            __syncwarp();
+            // the copies in flight land before the shared memory goes
+            for (int q = prod - S < 0 ? 0 : prod - S; q < prod; ++q)
+                mbar_wait_timed(&full[q % S], (uint32_t)((q / S) & 1), 200000000ull);
         }
-        // every commit has arrived before the TMEM goes (the epilogue waited for
-        // the last accumulators; this covers an abort)
-        if (niter > 0) {
-            mbar_wait_timed(&accfull[(niter - 1) & 1], (uint32_t)(((niter - 1) >> 1) & 1), 200000000ull);
+        __syncwarp();
+    } else if (warp == kPELoadWarp) {
+        // ---------------------------------------- epilogue operands' lane --
+        // points fastest: per tile and 16-column chunk, the accumulated output
+        // (and for the diagonal term V and X) as four 32-point boxes each
+        if (lane == 0 && g.ering > 0) {
+            const int nch = (g.N + 15) / 16;
+            const bool dg = g.diagV != nullptr;
+            const uint32_t piece = 4 * 2048;
+            int cc = 0;
+            for (int it = 0; it < niter && !*abort_flag; ++it) {
+                const int tau = (int)blockIdx.x + it * G;
+                const int z = tau / g.mtiles, m0 = (tau - z * g.mtiles) * kPM;
+                const bool skip = vgated(z);
+                for (int ch = 0; ch < nch; ++ch, ++cc) {
+                    const int sl = cc % g.ering;
+                    if (cc >= g.ering && !mbar_wait(&eempty[sl], (uint32_t)(((cc / g.ering) - 1) & 1))) {
+                        fail();
+                        break;
+                    }
+                    unsigned char *dst = reinterpret_cast<unsigned char *>(stage) + (size_t)sl * g.echunk;
+                    if (skip || (!g.accumulate && !dg)) {
+                        mbar_arrive(&efull[sl]);
+                        continue;
+                    }
+                    mbar_arrive_expect_tx(&efull[sl], (g.accumulate ? piece : 0u) + (dg ? 2 * piece : 0u));
+                    #pragma unroll
+                    for (int j = 0; j < 4; ++j) {
+                        const int m = m0 + 32 * j;
+                        const int c0 = m % Mi32, c2 = m / Mi32;
+                        if (g.accumulate) tma_load_4d(dst + j * 2048, &tmC, c0, ch * 16, c2, z, &efull[sl]);
+                        if (dg) {
+                            tma_load_3d(dst + piece + j * 2048, &tmV, c0, ch * 16, c2, &efull[sl]);
+                            tma_load_4d(dst + 2 * piece + j * 2048, &tmA, c0, ch * 16, c2, z, &efull[sl]);
+                        }
+                    }
+                }
+            }
+            // the copies in flight land before the shared memory goes
+            for (int q = cc - g.ering < 0 ? 0 : cc - g.ering; q < cc; ++q)
+                mbar_wait_timed(&efull[q % g.ering], (uint32_t)((q / g.ering) & 1), 200000000ull);
         }
+        __syncwarp();
+    } else if (warp == kPMmaWarp) {
+        // -------------------------------------------------------- MMA lane --
+        if (lane == 0) {
+            const uint32_t idesc = F16 ? idesc_f16(NT) : idesc_bf16(NT);
+            if (!mbar_wait_timed(bready, 0)) fail();
+            int q = 0, it = 0;
+            for (; it < niter && !*abort_flag; ++it) {
+                const int b = it & 1;
+                if (it >= 2 && !mbar_wait(&accempty[b], (uint32_t)(((it >> 1) - 1) & 1))) { fail(); break; }
+                for (int ks = 0; ks < KS; ++ks, ++q) {
+                    const int pp = q % kPPlanes;
+                    if (!mbar_wait(&pfull[pp], (uint32_t)((q / kPPlanes) & 1))) { fail(); break; }
+                    fence_after();
+                    const unsigned char *Ab = planes + pp * kPPlane;
+                    const uint64_t a_hi = smem_desc(smem_addr(Ab), 128, 256);
+                    const uint64_t a_lo = smem_desc(smem_addr(Ab + kPPlane / 2), 128, 256);
+                    const unsigned char *Bk = Bs + (size_t)ks * bstep;
+                    const uint64_t b_hi = smem_desc(smem_addr(Bk), 128, 256);
+                    const uint64_t b_lo = smem_desc(smem_addr(Bk + NT * 32), 128, 256);
+                    const uint32_t d = tbase + (uint32_t)(b * kPAccCols);
+                    tc_mma(d, a_hi, b_hi, idesc, ks > 0 ? 1u : 0u);
+                    tc_mma(d, a_hi, b_lo, idesc, 1u);
+                    tc_mma(d, a_lo, b_hi, idesc, 1u);
+                    tc_commit(&pfree[pp]);
+                }
+                if (*abort_flag) break;
+                tc_commit(&accfull[b]);
+            }
+            // every product has completed before the TMEM and the planes go
+            tc_commit(drain);
+            mbar_wait_timed(drain, 0, 200000000ull);
+        }
+        __syncwarp();
     } else {
         // -------------------------------------------------------- epilogue --
         const int qd = warp & 3;                 // TMEM lanes 32 qd .. 32 qd + 31 (warp % 4)
         const int ew = warp - kPConv / 32;       // 0 .. kPEpiWarps - 1
         const int hc = ew >> 2;                  // this warp's half of the columns
-        float *stg = stage + ew * kPStage;
+        float *stg0 = stage + ew * 2 * kPStage;
         const int nch = (g.N + 15) / 16;
         const uint32_t lane_base = (uint32_t)(qd * 32) << 16;
+        int nstore = 0;                          // TMA stores issued by this warp
         for (int it = 0; it < niter; ++it) {
             const int b = it & 1;
             const int tau = (int)blockIdx.x + it * G;
             const int z = tau / g.mtiles, m0 = (tau - z * g.mtiles) * kPM;
-            // the next tile's accumulated output (columns of 128 consecutive
-            // grid points) is pulled into L2 while this tile's products run,
-            // so the epilogue's loads of it hit L2
-            if (g.accumulate && g.c_sn > 1 && it + 1 < niter) {
-                const int tn = tau + G;
-                const int zn = tn / g.mtiles, mn0 = (tn - zn * g.mtiles) * kPM;
-                if (!vgated(zn)) {
-                    const int mend = min(mn0 + kPM, g.M);
-                    for (int n = ew * 32 + lane; n < g.N; n += 32 * kPEpiWarps) {
-                        const float *Cn = g.C + (i64)zn * g.c_sz + (i64)n * g.c_sn;
-                        for (int a = mn0; a < mend;) {
-                            const int bend = min(mend, (a / Mi32 + 1) * Mi32);
-                            prefetch_l2_bulk(Cn + rowoff(a), (uint32_t)(bend - a) * 4u);
-                            a = bend;
-                        }
-                    }
-                }
-            }
             bool ok = !*abort_flag;
             if (ok && !mbar_wait_sleep(&accfull[b], (uint32_t)((it >> 1) & 1), 256)) {
-                *abort_flag = 1;
-                if (g.err) atomicExch(g.err, 5);
+                fail();
                 ok = false;
             }
             ok = __all_sync(0xffffffffu, ok);
@@ -396,21 +458,44 @@ tc32p_level_kernel(Tc32pArgs g)
                 const int m = m0 + r;
                 const float rs = (g.rowscale && m < g.M) ? g.rowscale[m % Mi32] : 1.0f;
                 const float sc = g.alpha * rs * xinv;
-                if (g.c_sn == 1) {
-                    // rows contiguous along n: 32 x 16 blocks through the warp's
-                    // stage (row scale applied going in, column scale coming out),
-                    // stored as 64-byte row pieces; the diagonal term and the
-                    // accumulated output, when given, are loaded the same way
+                if (g.tstore) {
+                    // rows contiguous along n, nothing to add: each 32 x 16 block
+                    // is scaled into one of the warp's two stages (64-byte
+                    // swizzle) and stored by one TMA copy; rows past the vector's
+                    // last are clipped by the copy
+                    const int sw = (lane >> 1) & 3;
+                    const bool rows_in = m0 + qd * 32 < g.M;
+                    for (int ch = hc; ch < nch; ch += 2) {
+                        float v[16];
+                        tmem_ld16(tbase + lane_base + (uint32_t)(b * kPAccCols + ch * 16), v);
+                        asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+                        float *stg = stg0 + (nstore & 1) * kPStage;
+                        if (nstore >= 2) {
+                            if (lane == 0) asm volatile("cp.async.bulk.wait_group.read 1;" ::: "memory");
+                            __syncwarp();
+                        }
+                        #pragma unroll
+                        for (int j4 = 0; j4 < 4; ++j4) {
+                            const float *cs = binv_s + ch * 16 + 4 * j4;
+                            *reinterpret_cast<float4 *>(stg + lane * 16 + 4 * (j4 ^ sw)) =
+                                make_float4(sc * cs[0] * v[4 * j4], sc * cs[1] * v[4 * j4 + 1],
+                                            sc * cs[2] * v[4 * j4 + 2], sc * cs[3] * v[4 * j4 + 3]);
+                        }
+                        fence_proxy_async_smem();
+                        __syncwarp();
+                        if (lane == 0 && rows_in) {
+                            tma_store_3d(&tmC, stg, ch * 16, m0 + qd * 32, z);
+                            asm volatile("cp.async.bulk.commit_group;" ::: "memory");
+                        }
+                        ++nstore;
+                    }
+                } else if (g.c_sn == 1) {
+                    // rows contiguous along n with a diagonal term or an output
+                    // to add: 32 x 16 blocks through the warp's stage, finished
+                    // as 64-byte row pieces
                     const int f = lane & 3;
                     const int sw = (lane >> 1) & 3;
-                    i64 rbase[4];
-                    bool rval[4];
-                    #pragma unroll
-                    for (int u = 0; u < 4; ++u) {
-                        const int mm = m0 + qd * 32 + 8 * u + (lane >> 2);
-                        rval[u] = mm < g.M;
-                        rbase[u] = rval[u] ? rowoff(mm) : 0;
-                    }
+                    float *stg = stg0;
                     for (int ch = hc; ch < nch; ch += 2) {
                         float v[16];
                         tmem_ld16(tbase + lane_base + (uint32_t)(b * kPAccCols + ch * 16), v);
@@ -422,86 +507,94 @@ tc32p_level_kernel(Tc32pArgs g)
                         __syncwarp();
                         const int n = ch * 16 + 4 * f;
                         const float4 cs = *reinterpret_cast<const float4 *>(binv_s + n);
-                        const bool nval = n < g.N;
-                        if (!Vd && !g.accumulate) {
-                            #pragma unroll
-                            for (int u = 0; u < 4; ++u) {
-                                const int rr = 8 * u + (lane >> 2);
-                                const float4 o = *reinterpret_cast<const float4 *>(stg + rr * 16 + 4 * (f ^ ((rr >> 1) & 3)));
-                                if (rval[u] && nval)
-                                    *reinterpret_cast<float4 *>(C + rbase[u] + n) =
-                                        make_float4(o.x * cs.x, o.y * cs.y, o.z * cs.z, o.w * cs.w);
+                        #pragma unroll
+                        for (int u = 0; u < 4; ++u) {
+                            const int rr = 8 * u + (lane >> 2);
+                            const float4 o = *reinterpret_cast<const float4 *>(stg + rr * 16 + 4 * (f ^ ((rr >> 1) & 3)));
+                            const int mm = m0 + qd * 32 + rr;
+                            if (mm >= g.M || n >= g.N) continue;
+                            const i64 pp = rowoff(mm) + n;
+                            float4 out = make_float4(o.x * cs.x, o.y * cs.y, o.z * cs.z, o.w * cs.w);
+                            if (Vd) {
+                                const float4 dv = __ldg(reinterpret_cast<const float4 *>(Vd + pp));
+                                const float4 dx = __ldg(reinterpret_cast<const float4 *>(Xd + pp));
+                                out.x = fmaf(g.alpha * (dv.x - shift), dx.x, out.x);
+                                out.y = fmaf(g.alpha * (dv.y - shift), dx.y, out.y);
+                                out.z = fmaf(g.alpha * (dv.z - shift), dx.z, out.z);
+                                out.w = fmaf(g.alpha * (dv.w - shift), dx.w, out.w);
                             }
-                        } else {
-                            #pragma unroll
-                            for (int u = 0; u < 4; ++u) {
-                                const int rr = 8 * u + (lane >> 2);
-                                const float4 o = *reinterpret_cast<const float4 *>(stg + rr * 16 + 4 * (f ^ ((rr >> 1) & 3)));
-                                if (!rval[u] || !nval) continue;
-                                const i64 pp = rbase[u] + n;
-                                float4 out = make_float4(o.x * cs.x, o.y * cs.y, o.z * cs.z, o.w * cs.w);
-                                if (Vd) {
-                                    const float4 dv = __ldg(reinterpret_cast<const float4 *>(Vd + pp));
-                                    const float4 dx = __ldg(reinterpret_cast<const float4 *>(Xd + pp));
-                                    out.x = fmaf(g.alpha * (dv.x - shift), dx.x, out.x);
-                                    out.y = fmaf(g.alpha * (dv.y - shift), dx.y, out.y);
-                                    out.z = fmaf(g.alpha * (dv.z - shift), dx.z, out.z);
-                                    out.w = fmaf(g.alpha * (dv.w - shift), dx.w, out.w);
-                                }
-                                if (g.accumulate) {
-                                    const float4 cy = *reinterpret_cast<const float4 *>(C + pp);
-                                    out.x += cy.x; out.y += cy.y; out.z += cy.z; out.w += cy.w;
-                                }
-                                *reinterpret_cast<float4 *>(C + pp) = out;
+                            if (g.accumulate) {
+                                const float4 cy = *reinterpret_cast<const float4 *>(C + pp);
+                                out.x += cy.x; out.y += cy.y; out.z += cy.z; out.w += cy.w;
                             }
+                            *reinterpret_cast<float4 *>(C + pp) = out;
                         }
                         __syncwarp();
                     }
                 } else {
-                    // a lane owns grid row m; per column the warp's 32 lanes are
-                    // 32 consecutive points; groups of 8 columns of this warp's
-                    // half, every load of a group (accumulated output, diagonal
-                    // term) issued together with the group's TMEM load
-                    const bool mval = m < g.M;
-                    const i64 moff = mval ? rowoff(m) : 0;
+                    // points fastest: per 16-column chunk of this warp's half, the
+                    // operands wait in the ring as [16 n][32 points] per quarter;
+                    // the result overwrites the output's box, which one TMA copy
+                    // stores (points past the vector's last are clipped); the slot
+                    // is released once that copy has read it
+                    const float *cs = binv_s;
+                    const bool rows_in = m0 + qd * 32 < g.M;
                     for (int ch = hc; ch < nch; ch += 2) {
+                        const int cc = it * nch + ch;
+                        const int sl = cc % g.ering;
+                        float v[16];
+                        tmem_ld16(tbase + lane_base + (uint32_t)(b * kPAccCols + ch * 16), v);
+                        bool eok = !*abort_flag && mbar_wait(&efull[sl], (uint32_t)((cc / g.ering) & 1));
+                        eok = __all_sync(0xffffffffu, eok);
+                        asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+                        if (!eok) { fail(); break; }
+                        float *cb = stage + (size_t)sl * (g.echunk / 4) + qd * 512;
                         #pragma unroll
-                        for (int hf = 0; hf < 2; ++hf) {
-                            const int c0 = ch * 16 + 8 * hf;
-                            float v[8], cy[8], dv[8], dx[8];
-                            tmem_ld8(tbase + lane_base + (uint32_t)(b * kPAccCols + c0), v);
-                            #pragma unroll
-                            for (int t = 0; t < 8; ++t) {
-                                const int n = c0 + t;
-                                const bool in = mval && n < g.N;
-                                const i64 p = moff + (i64)n * g.c_sn;
-                                cy[t] = (in && g.accumulate) ? C[p] : 0.0f;
-                                dv[t] = (in && Vd) ? Vd[p] : 0.0f;
-                                dx[t] = (in && Vd) ? Xd[p] : 0.0f;
-                            }
-                            asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-                            if (!mval) continue;
-                            #pragma unroll
-                            for (int t = 0; t < 8; ++t) {
-                                const int n = c0 + t;
-                                if (n >= g.N) break;
-                                float out = v[t] * (sc * binv_s[n]) + cy[t];
-                                if (Vd) out = fmaf(g.alpha * (dv[t] - shift), dx[t], out);
-                                C[moff + (i64)n * g.c_sn] = out;
-                            }
+                        for (int j = 0; j < 16; ++j) {
+                            const int n = ch * 16 + j;
+                            const int idx = j * 32 + lane;
+                            float out = v[j] * (sc * cs[n < 256 ? n : 0]);
+                            if (g.accumulate) out += cb[idx];
+                            if (Vd) out = fmaf(g.alpha * (cb[2048 + idx] - shift), cb[4096 + idx], out);
+                            cb[idx] = out;
                         }
+                        fence_proxy_async_smem();
+                        __syncwarp();
+                        if (lane == 0) {
+                            if (rows_in) {
+                                const int mq = m0 + qd * 32;
+                                tma_store_4d(&tmC, cb, mq % Mi32, ch * 16, mq / Mi32, z);
+                                asm volatile("cp.async.bulk.commit_group;" ::: "memory");
+                                asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory");
+                                ++nstore;
+                            }
+                            mbar_arrive(&eempty[sl]);
+                        }
+                        __syncwarp();
                     }
                 }
-            } else if (ok) {
-                // a stopped vector: the accumulator is released unread
+            } else if (ok && g.ering > 0) {
+                // a stopped vector: its ring chunks are released unread
+                for (int ch = hc; ch < nch; ch += 2) {
+                    const int cc = it * nch + ch;
+                    const int sl = cc % g.ering;
+                    if (lane == 0) {
+                        if (mbar_wait(&efull[sl], (uint32_t)((cc / g.ering) & 1))) mbar_arrive(&eempty[sl]);
+                        else fail();
+                    }
+                    __syncwarp();
+                }
             }
             fence_before();
             mbar_arrive(&accempty[b]);
         }
+        // the stage buffers are read and the stores complete before the CTA ends
+        if (lane == 0 && nstore > 0) asm volatile("cp.async.bulk.wait_group 0;" ::: "memory");
+        __syncwarp();
     }
 
     // B copies have landed before the shared memory goes (an abort may skip
-    // the MMA warp's wait on them)
+    // the load lane's wait on them)
     if (tid == 0) mbar_wait_timed(bready, 0, 200000000ull);
     fence_before();
     __syncthreads();
@@ -581,7 +674,25 @@ __global__ void split_b16_kernel(int nout, int NT, const float *__restrict__ H, 
 
 // ------------------------------------------------------------------ host --
 
-static bool p_fits(int NT, int KS) { return p_smem_bytes(NT, KS) <= (size_t)kPMaxSmem; }
+// Epilogue operand ring of a points-fastest level: slots of 8 KB per operand
+// (the output, and V and X for the diagonal term), as many as fit (at most
+// kPERingMax, at least two).
+static int p_ring(int NT, int KS, bool diag, int *echunk)
+{
+    const size_t fixed = p_fixed_bytes(NT, KS, kPSlotsM);
+    const int chunk = 8192 * (diag ? 3 : 1);
+    if (echunk) *echunk = chunk;
+    if (fixed >= (size_t)kPMaxSmem) return 0;
+    const size_t room = (size_t)kPMaxSmem - fixed;
+    int r = (int)(room / chunk);
+    return r > kPERingMax ? kPERingMax : r;
+}
+
+static bool p_fits(int NT, int KS, bool kmajor, bool diag)
+{
+    if (kmajor) return p_smem_bytes(NT, KS, kPSlotsMax, 0) <= (size_t)kPMaxSmem;
+    return p_ring(NT, KS, diag, nullptr) >= 2;
+}
 
 void tc16_free(scalit_ctx *c)
 {
@@ -604,7 +715,7 @@ int tc16_prepare(scalit_ctx *c)
         if (L.ndvr && l == L.nlev - 1) continue;
         const int nout = L.n[l];
         const int NT = (nout + 15) / 16 * 16, KS = (nout + 15) / 16;
-        if (NT > 256 || !p_fits(NT, KS)) continue;
+        if (NT > 256 || !p_fits(NT, KS, L.dim[l] == 1, false)) continue;
         TcLevelData &t = c->tc16[l];
         const size_t nel = (size_t)KS * 2 * NT * 16;
         SC_CUDA(cudaMalloc(&t.dig, nel * sizeof(uint16_t)));
@@ -621,18 +732,52 @@ int tc16_prepare(scalit_ctx *c)
 // The persistent kernel applies to level l when one tile holds the level
 // matrix (single N tile, shared memory) and the operand's rows allow 16-byte
 // copies.  f16 selects the FP16 planes, else the BF16 planes of tc_fp32.cu.
-bool tc32p_usable(const scalit_ctx *c, int l, bool f16)
+bool tc32p_usable(const scalit_ctx *c, int l, bool f16, bool diag)
 {
     const Layout &L = c->L;
     if (L.ndvr && l == L.nlev - 1) return false;
     const TcLevelData &t = f16 ? c->tc16[l] : c->tc32[l];
-    if (!t.usable || t.ntiles != 1 || !p_fits(t.NT, t.KS)) return false;
+    if (!t.usable || t.ntiles != 1 || !p_fits(t.NT, t.KS, L.dim[l] == 1, diag)) return false;
     if (f16 && !c->xmax) return false;
     const int nout = L.n[l];
     const i64 nin = L.dim[l], N = L.N;
     if (N % 4 || nout % 4) return false;
-    if (nin > 1 && nin % 4) return false;
+    // grid points fastest within blocks of nin: 32-point boxes stay in a block
+    if (nin > 1 && nin % 32) return false;
     return true;
+}
+
+// cuTensorMapEncodeTiled from the driver (no link against libcuda).
+typedef CUresult (*EncodeTiledFn)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *, const cuuint64_t *,
+                                  const cuuint64_t *, const cuuint32_t *, const cuuint32_t *, CUtensorMapInterleave,
+                                  CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+static EncodeTiledFn encode_fn()
+{
+    static EncodeTiledFn fn = nullptr;
+    if (!fn) {
+        void *p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+                cudaSuccess && q == cudaDriverEntryPointSuccess)
+            fn = reinterpret_cast<EncodeTiledFn>(p);
+    }
+    return fn;
+}
+
+// FP32 tensor map of rank r over base with the given extents (elements),
+// strides of dimensions 1.. (bytes) and box; zero fill outside.
+static int encode_map(CUtensorMap *map, const float *base, int rank, const cuuint64_t *dims,
+                      const cuuint64_t *strides, const cuuint32_t *box, CUtensorMapSwizzle swz)
+{
+    EncodeTiledFn fn = encode_fn();
+    if (!fn) { set_error("cuTensorMapEncodeTiled unavailable"); return SCALIT_ECUDA; }
+    const cuuint32_t estr[5] = {1, 1, 1, 1, 1};
+    const CUresult r = fn(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, (cuuint32_t)rank, const_cast<float *>(base), dims,
+                          strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, swz,
+                          CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) { set_error("cuTensorMapEncodeTiled failed (%d)", (int)r); return SCALIT_ECUDA; }
+    return 0;
 }
 
 // Per-vector scales of X (FP16 form): zero the slots, then one max pass.
@@ -657,7 +802,10 @@ int tc32p_level_apply(const scalit_ctx *c, int l, bool f16, const float *X, floa
 {
     const Layout &L = c->L;
     const TcLevelData &t = f16 ? c->tc16[l] : c->tc32[l];
-    if (!tc32p_usable(c, l, f16)) { set_error("level %d has no persistent tensor-core plan", l + 1); return SCALIT_EUNSUP; }
+    if (!tc32p_usable(c, l, f16, diagV != nullptr)) {
+        set_error("level %d has no persistent tensor-core plan", l + 1);
+        return SCALIT_EUNSUP;
+    }
     if ((reinterpret_cast<uintptr_t>(X) & 15) || (reinterpret_cast<uintptr_t>(Y) & 15)) {
         set_error("persistent tensor-core operands not 16-byte aligned");
         return SCALIT_EINVAL;
@@ -680,7 +828,7 @@ int tc32p_level_apply(const scalit_ctx *c, int l, bool f16, const float *X, floa
     const i64 tiles = (i64)g.mtiles * nvec;
     if (tiles > 2147483647LL) { set_error("level %d: too many tiles", l + 1); return SCALIT_EINVAL; }
     g.tiles = (int)tiles;
-    g.A = X; g.a_sz = N; g.C = Y; g.c_sz = N;
+    g.C = Y; g.c_sz = N;
     g.accumulate = accumulate; g.alpha = alpha;
     g.diagV = diagV; g.diagX = X; g.dx_sz = N; g.shift = shift; g.shiftv = shiftv;
     g.vgate = vgate; g.vgate_stride = vstride;
@@ -688,6 +836,36 @@ int tc32p_level_apply(const scalit_ctx *c, int l, bool f16, const float *X, floa
     g.bsplit = reinterpret_cast<const uint4 *>(t.dig);
     g.binv = f16 ? t.cscale : nullptr;
     g.xmax = f16 ? c->xmax : nullptr;
+    g.tstore = (g.c_sn == 1 && !accumulate && !diagV) ? 1 : 0;
+
+    // the grid operand: [vector][row][k] boxes of 16 k x 128 rows (64-byte
+    // swizzle) or [vector][block][k][point] boxes of 32 points x 16 k; the
+    // level-1 output for TMA stores: [vector][row][n] boxes of 16 n x 32 rows
+    CUtensorMap tmA, tmC, tmV;
+    int rc;
+    if (nin == 1) {
+        const cuuint64_t dims[3] = {(cuuint64_t)nout, (cuuint64_t)blk, (cuuint64_t)nvec};
+        const cuuint64_t str[2] = {(cuuint64_t)nout * 4, (cuuint64_t)N * 4};
+        const cuuint32_t box[3] = {16, kPM, 1};
+        rc = encode_map(&tmA, X, 3, dims, str, box, CU_TENSOR_MAP_SWIZZLE_64B);
+        if (!rc && g.tstore) {
+            const cuuint32_t boxc[3] = {16, 32, 1};
+            rc = encode_map(&tmC, Y, 3, dims, str, boxc, CU_TENSOR_MAP_SWIZZLE_64B);
+        }
+    } else {
+        const cuuint64_t dims[4] = {(cuuint64_t)nin, (cuuint64_t)nout, (cuuint64_t)blk, (cuuint64_t)nvec};
+        const cuuint64_t str[3] = {(cuuint64_t)nin * 4, (cuuint64_t)nin * nout * 4, (cuuint64_t)N * 4};
+        const cuuint32_t box[4] = {32, 16, 1, 1};
+        rc = encode_map(&tmA, X, 4, dims, str, box, CU_TENSOR_MAP_SWIZZLE_NONE);
+        // the output (loaded to accumulate, stored back) in the same boxes, V
+        // without the vector dimension
+        if (!rc) rc = encode_map(&tmC, Y, 4, dims, str, box, CU_TENSOR_MAP_SWIZZLE_NONE);
+        if (!rc && diagV) rc = encode_map(&tmV, diagV, 3, dims, str, box, CU_TENSOR_MAP_SWIZZLE_NONE);
+        g.ering = p_ring(g.NT, g.KS, diagV != nullptr, &g.echunk);
+    }
+    if (rc) return rc;
+    if (nin == 1 && !g.tstore) tmC = tmA;
+    if (!(nin > 1 && diagV)) tmV = tmA;
 
     static int sms = 0, configured = -1;
     int dev = 0;
@@ -699,9 +877,10 @@ int tc32p_level_apply(const scalit_ctx *c, int l, bool f16, const float *X, floa
         configured = dev;
     }
     const int grid = (int)(tiles < sms ? tiles : sms);
-    const size_t smem = p_smem_bytes(g.NT, g.KS);
-    if (f16) tc32p_level_kernel<true><<<grid, kPThreads, smem, s>>>(g);
-    else tc32p_level_kernel<false><<<grid, kPThreads, smem, s>>>(g);
+    g.nslots = nin == 1 ? kPSlotsMax : kPSlotsM;
+    const size_t smem = p_smem_bytes(g.NT, g.KS, g.nslots, (size_t)g.ering * g.echunk);
+    if (f16) tc32p_level_kernel<true><<<grid, kPThreads, smem, s>>>(g, tmA, tmC, tmV);
+    else tc32p_level_kernel<false><<<grid, kPThreads, smem, s>>>(g, tmA, tmC, tmV);
     SC_CHECK_LAUNCH();
     return 0;
 }

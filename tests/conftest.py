@@ -30,7 +30,7 @@ def orc():
 # GPU modules whose device path has not yet passed on a GB300 run after the
 # others, so that under -x a failure in one of them does not hide the rest;
 # test_zz_no_alloc.py stays last (its docstring says why).
-_NOT_YET_VALIDATED = ("test_gpu_window.py", "test_gpu_complex.py", "test_gpu_tc16.py")
+_NOT_YET_VALIDATED = ("test_gpu_window.py", "test_gpu_complex.py")
 
 
 def pytest_collection_modifyitems(config, items):

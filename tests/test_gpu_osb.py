@@ -127,7 +127,7 @@ def test_fp32_tensor_px_mode(lib):
     with capi.Context.from_problem(p, e0=float(p.RES.min()) - 1e-3) as ctx:
         ctx.build_osb(20, 1e-4)
         dx = torch.tensor(x, dtype=torch.float32, device="cuda")
-        for mode in (capi.FP32_SIMT, capi.FP32_TENSOR, capi.FP32_TENSOR_PX):
+        for mode in (capi.FP32_SIMT, capi.FP32_TENSOR, capi.FP32_TENSOR_PX, capi.FP32_TENSOR16):
             ctx.set_fp32_mode(mode)
             hy, pz = torch.empty_like(dx), torch.empty_like(dx)
             ctx.hx_f32_device(dx, hy)
@@ -135,7 +135,9 @@ def test_fp32_tensor_px_mode(lib):
             torch.cuda.synchronize()
             out[mode] = (hy.cpu(), pz.cpu())
         with pytest.raises(capi.ScalitError):
-            ctx.set_fp32_mode(3)
+            ctx.set_fp32_mode(4)
     assert torch.equal(out[capi.FP32_TENSOR_PX][0], out[capi.FP32_SIMT][0])
+    # SCALIT_FP32_TENSOR16 rotates with the same split-BF16 x3 rotations
+    assert torch.equal(out[capi.FP32_TENSOR16][1], out[capi.FP32_TENSOR][1])
     assert torch.equal(out[capi.FP32_TENSOR_PX][1], out[capi.FP32_TENSOR][1])
     assert not torch.equal(out[capi.FP32_TENSOR][1], out[capi.FP32_SIMT][1])

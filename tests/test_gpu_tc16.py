@@ -1,5 +1,9 @@
 """FP32 H*X on the persistent tensor-core level kernel (csrc/tc_fp32p.cu).
 
+Grids whose inner blocks are multiples of 32 points (32x24x20, 64x20x12,
+96x96x64) run every level on it, partial tiles included; the others run
+their first level on it and the rest on the earlier engines.
+
 Split-FP16 x3 with exponent scaling (SCALIT_FP32_TENSOR16) must carry the
 accuracy of the FP32 CUDA-core GEMM: H*X within 2e-6 norm-wise of the FP64
 oracle (MYHX, osb.hx.h:71-110), for vectors of any scale (the per-vector
@@ -32,7 +36,7 @@ def _hx32(ctx, X, ntype):
     return dy.double().cpu().numpy()
 
 
-@pytest.mark.parametrize("sizes", [(24, 32, 20), (20, 12, 8), (36, 44, 28)])
+@pytest.mark.parametrize("sizes", [(24, 32, 20), (20, 12, 8), (36, 44, 28), (32, 24, 20), (64, 20, 12)])
 @pytest.mark.parametrize("mode,tol", [(capi.FP32_TENSOR16, TOL_F16X3), (capi.FP32_TENSOR, TOL_BF16X3)])
 def test_hx_f32_persistent(lib, orc, sizes, mode, tol):
     """Both split forms against the FP64 oracle; vectors scaled by 1e-30 ..
