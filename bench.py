@@ -48,9 +48,15 @@ METRIC = "H*X apps/s & %roofline; PIST time to 200 levels (mixed vs FP64 GPU)"
 REFINE_TOL, REFINE_STEPS, PIST_QMR_TOL = 1e-8, 20, 1e-6
 
 # FP32 H*X engines timed by the bench, and the kernel each runs
-FP32_ENGINES = (("simt", 0), ("tensor_bf16x3", 1))
-FP32_KERNEL = {"simt": "gemm_kernel<float>", "tensor_bf16x3": "tc32_level_kernel"}
-FP32_PROFILE = {"simt": "gemm_kernel_f32", "tensor_bf16x3": "tc32_level_kernel"}
+FP32_ENGINES = (("simt", 0), ("tensor_bf16x3", 1), ("tensor_f16x3", 3))
+FP32_KERNEL = {"simt": "gemm_kernel<float>", "tensor_bf16x3": "tc32p_level_kernel<false>",
+               "tensor_f16x3": "tc32p_level_kernel<true>"}
+FP32_PROFILE = {"simt": "gemm_kernel_f32", "tensor_bf16x3": "tc32p_level_kernel",
+                "tensor_f16x3": "tc32p_level_kernel"}
+# the engine of the mixed arms' FP32 inner solves: H*X in split-FP16 x3 on the
+# tensor cores (the accuracy of the CUDA-core GEMM), the preconditioner's
+# rotations in split-BF16 x3
+MIXED_FP32_MODE = 3
 
 
 def parse():
@@ -173,12 +179,14 @@ def profiled_traffic(kernel, workload, level, nvec):
         return None
 
 
-def hx_units(sizes, w=8):
+def hx_units(sizes, w=8, diag_level=0):
     """Algorithmic flops and bytes of one H*X application (one vector), and per level.
 
     flops: 2 N n_l per level plus the diagonal (V - E0) X and the level sums (5N).
     bytes of a level launch: read X, write Y, and read Y when accumulating
-    (levels 2..sF), plus the small level matrix; DEP and V where used.
+    (levels 2..sF), plus the small level matrix; DEP and V where used (V on
+    the level that carries the diagonal term: the first on the FP64 engines,
+    the last on the persistent FP32 kernel).
     w: bytes per value (8 FP64, 4 FP32).
     """
     n = list(sizes)
@@ -187,7 +195,7 @@ def hx_units(sizes, w=8):
     for l, nl in enumerate(n):
         flops = 2.0 * N * nl
         byts = (2 + (1 if l > 0 else 0)) * N * w + nl * nl * w
-        if l == 0:
+        if l == diag_level:
             byts += N * w            # V for the fused diagonal term
             flops += 3.0 * N
         if l == len(n) - 1:
@@ -317,7 +325,7 @@ def pist_leg(workload, levels, device, capi, hm, arms=("fp64", "fp32"), warmup=T
         with capi.Context.from_problem(pw, e0=float(pw.RES.min()), device=device) as ctx:
             ctx.build_osb(20, 1e-4)
             if prec != capi.PREC_FP64:
-                ctx.set_fp32_mode(capi.FP32_TENSOR_PX)
+                ctx.set_fp32_mode(MIXED_FP32_MODE)
             ctx.pist(np.random.default_rng(0).random(pw.N), levels, float(pw.RES.min()), 1e-11,
                      m_max=max(8 * levels, 400), qmr_max=2000, qmr_tol=PIST_QMR_TOL, precision=prec, orth=orth,
                      refine_tol=REFINE_TOL, refine_steps=REFINE_STEPS)
@@ -326,7 +334,7 @@ def pist_leg(workload, levels, device, capi, hm, arms=("fp64", "fp32"), warmup=T
     x0 = np.random.default_rng(0).random(p.N)
     out = {"workload": workload, "levels": levels}
     eigs = {}
-    # mixed leg: FP32 inner solves (H*X on the CUDA cores, the preconditioner's
+    # mixed leg: FP32 inner solves (H*X in split-FP16 x3 and the preconditioner's
     # rotations in split-BF16 x3 on the tensor cores) and an FP32 first
     # Gram-Schmidt pass (the re-orthogonalisation's projections, HMAT and the
     # Ritz solves stay FP64; its update streams the basis' FP32 copy with
@@ -336,7 +344,7 @@ def pist_leg(workload, levels, device, capi, hm, arms=("fp64", "fp32"), warmup=T
             continue
         with capi.Context.from_problem(p, e0=e0, device=device) as ctx:
             if prec != capi.PREC_FP64:
-                ctx.set_fp32_mode(capi.FP32_TENSOR_PX)
+                ctx.set_fp32_mode(MIXED_FP32_MODE)
             t0 = time.perf_counter()
             stats = ctx.build_osb(20, 1e-4)
             t1 = time.perf_counter()
@@ -347,8 +355,8 @@ def pist_leg(workload, levels, device, capi, hm, arms=("fp64", "fp32"), warmup=T
             t2 = time.perf_counter()
         eigs[name] = eig
         out[name] = {"status": st, "orth": orth, "seconds": t2 - t0, "build_s": t1 - t0, "pist_s": t2 - t1,
-                     "inner_solves": ("FP32 QMR under FP64 iterative refinement (H*X CUDA cores, "
-                                      "preconditioner rotations split-BF16 x3 tensor cores)"
+                     "inner_solves": ("FP32 QMR under FP64 iterative refinement (H*X split-FP16 x3 "
+                                      "tensor cores, preconditioner rotations split-BF16 x3 tensor cores)"
                                       if prec != capi.PREC_FP64 else "FP64 QMR"),
                      "qmr_tol": PIST_QMR_TOL,
                      "build_levels_s": build_levels,
@@ -403,7 +411,7 @@ def golden_pist_leg(workload, device, capi, hm):
     for name, prec, orth in (("fp64", capi.PREC_FP64, 1), ("fp32", capi.PREC_FP32, 2)):
         with capi.Context.from_problem(p, e0=fx["e0"], device=device) as ctx:
             if prec == capi.PREC_FP32:
-                ctx.set_fp32_mode(capi.FP32_TENSOR_PX)
+                ctx.set_fp32_mode(MIXED_FP32_MODE)
             t0 = time.perf_counter()
             ctx.build_osb(20, 1e-4)
             st, eig, _, info = ctx.pist(x0, fx["levels"], fx["e0"], fx["etol"], startcnt=fx["startcnt"],
@@ -560,13 +568,15 @@ def run_ours(args):
         torch.cuda.synchronize()
         return steps * nvec / (a.elapsed_time(b) / 1e3)
 
-    _, bytes32, lv32 = hx_units(p.sizes, 4)
+    _, bytes32, lv32 = hx_units(p.sizes, 4, diag_level=len(p.sizes) - 1)
     fp32 = {"dtype": "f32", "engines_apps_per_s": {}, "engines_level_ms": {}}
     for name, mode in FP32_ENGINES:
         ctx.set_fp32_mode(mode)
         fp32["engines_apps_per_s"][name] = time_f32(ctx.hx_f32_device, label=f"hx_fp32_{name}")
         fp32["engines_level_ms"][name] = ctx.hx_level_times(X32[0], Y32[0], nvec, reps=10)
-    best = max(fp32["engines_apps_per_s"], key=fp32["engines_apps_per_s"].get)
+    # the roofline of the engine the mixed arms' inner solves run (split-FP16 x3:
+    # the CUDA-core GEMM's accuracy); the split-BF16 x3 rate is listed beside it
+    best = "tensor_f16x3"
     lms = fp32["engines_level_ms"][best]
     d32 = int(np.argmax(lms))
     a32 = nvec * lv32[d32]["bytes"] / (lms[d32] / 1e3) / 1e9
