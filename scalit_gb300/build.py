@@ -14,7 +14,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 OUT_DIR = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT_DIR, "libscalit_gb300.so")
-SOURCES = ["contract.cu", "px.cu", "osb.cu", "osbw.cu", "complex.cu", "qmr.cu", "pist.cu", "capi.cu", "noalloc.cu", "tc_fp64.cu", "adjoint.cu", "multi.cu", "tc_fp32.cu", "tc_fp32p.cu"]
+SOURCES = ["contract.cu", "px.cu", "osb.cu", "osbw.cu", "complex.cu", "qmr.cu", "pist.cu", "capi.cu", "noalloc.cu", "tc_fp64.cu", "adjoint.cu", "multi.cu", "tc_fp32.cu", "tc_fp32p.cu", "tc_fp64p.cu"]
 HEADERS = ["internal.cuh", "ptx.cuh"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr"]

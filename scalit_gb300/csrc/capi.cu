@@ -169,6 +169,7 @@ void scalit_destroy(scalit_ctx *c)
         if (l == 0) { tc_free_px(c); tc32_free(c, true, true); tc16_free(c); }
     }
     if (c->tc_err) cudaFree(c->tc_err);
+    if (c->xmax64) cudaFree(c->xmax64);
     osbw_free(c);
     double *aptrs[] = {c->APP, c->APR, c->AP};
     for (double *p : aptrs) if (p) cudaFree(p);
@@ -264,6 +265,7 @@ int scalit_load(scalit_ctx *c, const double *H0, const double *RES, const double
     rc = tc_prepare(c);
     if (!rc) rc = tc32_prepare(c, false);
     if (!rc) rc = tc16_prepare(c);
+    if (!rc) rc = tc64p_prepare(c);
     if (rc) return rc;
     memset(c->tile_pick, -1, sizeof(c->tile_pick));
     rc = gemm_autotune(c, 16);

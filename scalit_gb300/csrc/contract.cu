@@ -295,7 +295,19 @@ int hx_batch(const scalit_ctx *c, const T *X, T *Y, int nvec, T shift, T alpha, 
     int first = 0;
     // FP32 tensor-core forms: the persistent pipelined level kernel wherever
     // it applies (split-FP16 x3 needs the vectors' scales first)
-    bool p16 = false, pbf = false;
+    bool p16 = false, pbf = false, p64 = false;
+    if constexpr (std::is_same<T, double>::value) {
+        // FP64 digit engine: the persistent kernel wherever it applies, after
+        // the vectors' exponents
+        const bool aligned = !(reinterpret_cast<uintptr_t>(X) & 15) && !(reinterpret_cast<uintptr_t>(Y) & 15);
+        if (aligned && c->fp64_mode == SCALIT_FP64_TENSOR) {
+            for (int l = 0; l < L.nlev; ++l) p64 = p64 || tc64p_usable(c, l);
+            if (p64) {
+                rc = tc64p_scales(c, X, nvec, gate, s, vgate, vstride);
+                if (rc) return rc;
+            }
+        }
+    }
     if constexpr (std::is_same<T, float>::value) {
         const bool aligned = !(reinterpret_cast<uintptr_t>(X) & 15) && !(reinterpret_cast<uintptr_t>(Y) & 15);
         p16 = aligned && c->fp32_mode == SCALIT_FP32_TENSOR16;
@@ -315,6 +327,7 @@ int hx_batch(const scalit_ctx *c, const T *X, T *Y, int nvec, T shift, T alpha, 
     // first level's epilogue loads nothing.
     int diag_level = 0;
     if ((p16 || pbf) && L.nlev > 1 && tc32p_usable(c, L.nlev - 1, p16, true)) diag_level = L.nlev - 1;
+    if (p64 && L.nlev > 1 && tc64p_usable(c, L.nlev - 1)) diag_level = L.nlev - 1;
     if (L.ndvr && L.nlev == 1) {
         const int threads = 256;
         if (shiftv) { set_error("per-vector shifts with a single outer layer"); return SCALIT_EUNSUP; }
@@ -329,6 +342,12 @@ int hx_batch(const scalit_ctx *c, const T *X, T *Y, int nvec, T shift, T alpha, 
         if (c->lev_ev) cudaEventRecord(c->lev_ev[l], s);
         const bool fuse_diag = (l == diag_level && !first);
         if constexpr (std::is_same<T, double>::value) {
+            if (p64 && tc64p_usable(c, l)) {
+                rc = tc64p_level_apply(c, l, X, Y, l > 0 || first, fuse_diag ? RES : nullptr, shift, alpha,
+                                       gate, s, nvec, shiftv, vgate, vstride);
+                if (rc) return rc;
+                continue;
+            }
             if (c->fp64_mode == SCALIT_FP64_TENSOR && tc_usable(c, l)) {
                 rc = tc_level_apply(c, l, X, Y, l > 0 || first, fuse_diag ? RES : nullptr, shift, alpha,
                                     gate, s, nvec, shiftv, vgate, vstride);

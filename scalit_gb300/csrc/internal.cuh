@@ -1,6 +1,7 @@
 // Internal declarations shared by the translation units of libscalit_gb300.
 #pragma once
 
+#include <cuda.h>
 #include <cuda_runtime.h>
 #include <cstdint>
 #include <cstdio>
@@ -118,6 +119,7 @@ struct scalit_ctx {
     // (SCALIT_FP32_TENSOR16) and the per-vector scale slots of one launch
     TcLevelData tc16[SCALIT_FMAX];
     unsigned *xmax = nullptr;
+    unsigned long long *xmax64 = nullptr;   // per-vector max |x| bits (persistent FP64 engine)
     int *tc_err = nullptr;
     // Measurement aid: when set, hx_batch records lev_ev[l] before level l's
     // launch and lev_ev[nlev] after the last (scalit_hx_level_times).
@@ -217,7 +219,16 @@ int tc32_level_apply(const scalit_ctx *c, int level, const float *X, float *Y, i
                      const float *shiftv = nullptr, const int *vgate = nullptr, int vstride = 0);
 int tc32_rot_apply(const scalit_ctx *c, int level, int transpose, const float *X, float *Y, const int *gate,
                    cudaStream_t s, int nvec = 1, const int *vgate = nullptr, int vstride = 0);
+int tma_encode(CUtensorMap *map, const void *base, bool f64, int rank, const cuuint64_t *dims,
+               const cuuint64_t *strides, const cuuint32_t *box, CUtensorMapSwizzle swz);
 int tc16_prepare(scalit_ctx *c);
+int tc64p_prepare(scalit_ctx *c);
+bool tc64p_usable(const scalit_ctx *c, int level);
+int tc64p_scales(const scalit_ctx *c, const double *X, int nvec, const int *gate, cudaStream_t s,
+                 const int *vgate = nullptr, int vstride = 0);
+int tc64p_level_apply(const scalit_ctx *c, int level, const double *X, double *Y, int accumulate,
+                      const double *diagV, double shift, double alpha, const int *gate, cudaStream_t s, int nvec,
+                      const double *shiftv = nullptr, const int *vgate = nullptr, int vstride = 0);
 void tc16_free(scalit_ctx *c);
 bool tc32p_usable(const scalit_ctx *c, int level, bool f16, bool diag = false);
 int tc16_scales(const scalit_ctx *c, const float *X, int nvec, const int *gate, cudaStream_t s,

@@ -143,38 +143,6 @@ __device__ __forceinline__ void p_cut2(float x0, float x1, float xs, uint32_t &h
     }
 }
 
-__device__ __forceinline__ void tma_load_3d(void *dst, const CUtensorMap *map, int c0, int c1, int c2, uint64_t *mbar)
-{
-    asm volatile(
-        "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], [%5];"
-        :: "r"(smem_addr(dst)), "l"(reinterpret_cast<uint64_t>(map)), "r"(c0), "r"(c1), "r"(c2), "r"(smem_addr(mbar))
-        : "memory");
-}
-
-__device__ __forceinline__ void tma_load_4d(void *dst, const CUtensorMap *map, int c0, int c1, int c2, int c3,
-                                            uint64_t *mbar)
-{
-    asm volatile(
-        "cp.async.bulk.tensor.4d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4, %5}], [%6];"
-        :: "r"(smem_addr(dst)), "l"(reinterpret_cast<uint64_t>(map)), "r"(c0), "r"(c1), "r"(c2), "r"(c3),
-           "r"(smem_addr(mbar))
-        : "memory");
-}
-
-__device__ __forceinline__ void tma_store_3d(const CUtensorMap *map, const void *src, int c0, int c1, int c2)
-{
-    asm volatile("cp.async.bulk.tensor.3d.global.shared::cta.tile.bulk_group [%0, {%1, %2, %3}], [%4];"
-                 :: "l"(reinterpret_cast<uint64_t>(map)), "r"(c0), "r"(c1), "r"(c2), "r"(smem_addr(src))
-                 : "memory");
-}
-
-__device__ __forceinline__ void tma_store_4d(const CUtensorMap *map, const void *src, int c0, int c1, int c2, int c3)
-{
-    asm volatile("cp.async.bulk.tensor.4d.global.shared::cta.tile.bulk_group [%0, {%1, %2, %3, %4}], [%5];"
-                 :: "l"(reinterpret_cast<uint64_t>(map)), "r"(c0), "r"(c1), "r"(c2), "r"(c3), "r"(smem_addr(src))
-                 : "memory");
-}
-
 template <bool F16>
 __global__ void __launch_bounds__(kPThreads, 1)
 tc32p_level_kernel(Tc32pArgs g, const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmC,
@@ -765,19 +733,27 @@ static EncodeTiledFn encode_fn()
     return fn;
 }
 
-// FP32 tensor map of rank r over base with the given extents (elements),
-// strides of dimensions 1.. (bytes) and box; zero fill outside.
-static int encode_map(CUtensorMap *map, const float *base, int rank, const cuuint64_t *dims,
-                      const cuuint64_t *strides, const cuuint32_t *box, CUtensorMapSwizzle swz)
+// Tensor map (FP32 or FP64 elements) of rank r over base with the given
+// extents (elements), strides of dimensions 1.. (bytes) and box; zero fill
+// outside.
+int tma_encode(CUtensorMap *map, const void *base, bool f64, int rank, const cuuint64_t *dims,
+               const cuuint64_t *strides, const cuuint32_t *box, CUtensorMapSwizzle swz)
 {
     EncodeTiledFn fn = encode_fn();
     if (!fn) { set_error("cuTensorMapEncodeTiled unavailable"); return SCALIT_ECUDA; }
     const cuuint32_t estr[5] = {1, 1, 1, 1, 1};
-    const CUresult r = fn(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, (cuuint32_t)rank, const_cast<float *>(base), dims,
-                          strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, swz,
-                          CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    const CUresult r = fn(map, f64 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT64 : CU_TENSOR_MAP_DATA_TYPE_FLOAT32,
+                          (cuuint32_t)rank, const_cast<void *>(base), dims, strides, box, estr,
+                          CU_TENSOR_MAP_INTERLEAVE_NONE, swz, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                          CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
     if (r != CUDA_SUCCESS) { set_error("cuTensorMapEncodeTiled failed (%d)", (int)r); return SCALIT_ECUDA; }
     return 0;
+}
+
+static int encode_map(CUtensorMap *map, const float *base, int rank, const cuuint64_t *dims,
+                      const cuuint64_t *strides, const cuuint32_t *box, CUtensorMapSwizzle swz)
+{
+    return tma_encode(map, base, false, rank, dims, strides, box, swz);
 }
 
 // Per-vector scales of X (FP16 form): zero the slots, then one max pass.

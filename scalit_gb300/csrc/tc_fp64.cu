@@ -742,9 +742,10 @@ int tc_check_error(scalit_ctx *c)
     if (h) {
         static const char *what[] = {"", "FP64 tensor-core level product", "level-1 P*X stream",
                                      "FP32 tensor-core level product", "bounded-wait self-test",
-                                     "persistent FP32 tensor-core level product"};
+                                     "persistent FP32 tensor-core level product",
+                                     "persistent FP64 tensor-core level product"};
         set_error("%s: an mbarrier wait ran out (kernel aborted, context usable)",
-                  (h >= 1 && h <= 5) ? what[h] : "device kernel");
+                  (h >= 1 && h <= 6) ? what[h] : "device kernel");
         cudaMemsetAsync(c->tc_err, 0, sizeof(int), c->stream);
         return SCALIT_ECUDA;
     }

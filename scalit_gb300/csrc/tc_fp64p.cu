@@ -1,0 +1,598 @@
+// Persistent FP64 level products of H*X on the tcgen05 digit engine.
+//
+// The arithmetic is the digit scheme of tc_fp64.cu: with e_x the binary
+// exponent of max|x| over the vector and e_n that of column n of B,
+//   A(m, k) = 2^e_x sum_{s=0..6} a_s 2^-7(s+1),  B(k, n) = 2^e_n sum_t b_t 2^-7(t+1),
+// |a_s|, |b_t| <= 127 integers (exact in BF16), and the 28 digit pairs with
+// s + t <= 6 accumulate into 7 FP32 group accumulators in TMEM (exact for
+// groups 0..5 with K <= 160), recombined in 64-bit integers in the epilogue.
+// One exponent per vector (instead of per grid row) lets every K slab be cut
+// as it arrives; it leaves an error of ~2^-46 max|x| |B| per product.
+//
+// The pipeline is that of tc_fp32p.cu: one CTA per SM walks tiles of 128
+// grid rows x one N tile of at most 64 columns (7 x 64 TMEM columns), N tile
+// fastest so that neighbouring CTAs share the grid operand's tile in L2.
+//   load lane (warp 17)     per K step, a TMA tensor copy of the FP64 slab
+//                           (16 k x 128 rows, 128-byte swizzle, or four 32-point
+//                           x 16 k boxes when points are fastest) and a bulk copy
+//                           of the step's 7 B digit planes, into one of
+//                           kQSlots step slots ("full" / "empty" mbarriers; a slot
+//                           is empty once the converters read its slab and the
+//                           step's products read its B planes);
+//   converters (warps 0-7)  cut the slab into 7 BF16 digit planes (K-major
+//                           canonical layout) in one of kQPlanes plane slots;
+//   MMA lane (warp 16)      issues the step's 28 products;
+//   epilogue (warps 8-15)   recombine the groups, scale, add the diagonal term
+//                           and the accumulated output, store; level-1 outputs
+//                           leave by TMA from swizzled 32 x 8 stages.
+// The accumulator is single (448 of 512 columns), so a tile's products start
+// once the previous tile's epilogue has read it; loads and cuts run ahead.
+// Every wait is bounded as in tc_fp32p.cu.
+#include "internal.cuh"
+#include "ptx.cuh"
+
+#include <cuda_bf16.h>
+
+namespace sc {
+
+static constexpr int kQM = 128;
+static constexpr int kQConv = 256;
+static constexpr int kQEpiWarps = 8;
+static constexpr int kQThreads = kQConv + 32 * kQEpiWarps + 64;
+static constexpr int kQMmaWarp = kQConv / 32 + kQEpiWarps;
+static constexpr int kQLoadWarp = kQMmaWarp + 1;
+static constexpr int kQDig = 7;
+static constexpr int kQNTMax = 64;
+static constexpr int kQSlabA = kQM * 16 * 8;                   // FP64 slab: 16 KB
+static constexpr int kQBStepMax = kQDig * kQNTMax * 32;        // B digits of a K step: <= 14 KB
+static constexpr int kQSlot = kQSlabA + kQBStepMax;            // 30 KB (a multiple of 1 KB)
+static constexpr int kQSlots = 3;
+static constexpr int kQPlane = kQDig * kQM * 32;               // A digit planes of a K step: 28 KB
+static constexpr int kQPlanes = 3;
+static constexpr int kQStage = 32 * 8;                         // doubles per epilogue stage (2 per warp)
+static constexpr int kQMaxVec = 4096;
+
+struct Tc64pArgs {
+    int M, K, KS, N, NT, ntn;   // rows per vector, contraction, K steps, output columns, N tile, N tiles
+    int mtiles, tiles;          // M tiles per vector; tiles = mtiles x ntn x vectors
+    i64 Mi, s1, s2, a_sk, c_sn;
+    double *C; i64 c_sz;
+    const double *rowscale;
+    int accumulate;
+    double alpha;
+    const double *diagV;
+    const double *diagX; i64 dx_sz;
+    double shift;
+    const double *shiftv;
+    const int *vgate; int vgate_stride;
+    const int *gate;
+    int *err;
+    const uint16_t *bdig;       // [ntile][ks][digit][NT x 16] canonical K-major
+    const int *bexp;            // [ntile * NT] column exponents
+    const unsigned long long *xmax;   // per vector: bits of max |x|
+    int tstore;                 // outputs contiguous along n, nothing to add: TMA stores
+};
+
+static size_t q_smem_bytes()
+{
+    return (size_t)kQSlots * kQSlot + (size_t)kQPlanes * kQPlane + (size_t)kQEpiWarps * 2 * kQStage * 8 +
+           (2 * kQSlots + 2 * kQPlanes + 4) * 8 + 16;
+}
+
+// Binary exponent e with |x| < 2^e (frexp's) from the bits of |x|; 0 for zero.
+__device__ __forceinline__ int q_exp(unsigned long long bits)
+{
+    const int ex = (int)((bits >> 52) & 0x7FF);
+    if (ex) return ex - 1022;
+    const unsigned long long m = bits & 0x000FFFFFFFFFFFFFULL;
+    return m ? (64 - __clzll(m)) - 1074 : 0;
+}
+
+// 49-bit fixed-point magnitude of |x| 2^(49 - e) (truncated), e >= exponent of x.
+__device__ __forceinline__ unsigned long long q_fixed49(unsigned long long bits, int e)
+{
+    const int ex = (int)((bits >> 52) & 0x7FF);
+    const unsigned long long m = (bits & 0x000FFFFFFFFFFFFFULL) | (ex ? (1ULL << 52) : 0ULL);
+    const int sh = (ex ? ex : 1) - 1075 + 49 - e;   // <= -4
+    return (sh <= -64) ? 0ULL : (m >> (-sh));
+}
+
+
+__global__ void __launch_bounds__(kQThreads, 1)
+tc64p_level_kernel(Tc64pArgs g, const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmC)
+{
+    if (g.gate && *g.gate) return;
+    extern __shared__ __align__(1024) unsigned char smem[];
+    const int NT = g.NT, KS = g.KS;
+    const int bstep = kQDig * NT * 32;
+    unsigned char *slots = smem;                                     // 1024-byte aligned
+    unsigned char *planes = slots + kQSlots * kQSlot;
+    double *stage = reinterpret_cast<double *>(planes + kQPlanes * kQPlane);
+    uint64_t *full = reinterpret_cast<uint64_t *>(stage + kQEpiWarps * 2 * kQStage);
+    uint64_t *empty = full + kQSlots;
+    uint64_t *pfull = empty + kQSlots;
+    uint64_t *pfree = pfull + kQPlanes;
+    uint64_t *accfull = pfree + kQPlanes;
+    uint64_t *accempty = accfull + 1;
+    uint64_t *drain = accempty + 1;
+    volatile int *abort_flag = reinterpret_cast<volatile int *>(drain + 1);
+    uint32_t *tslot = reinterpret_cast<uint32_t *>(drain + 1) + 1;
+
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int G = gridDim.x;
+    const int niter = (g.tiles - (int)blockIdx.x + G - 1) / G;
+    const int nsteps = niter * KS;
+    const bool kmajor = (g.a_sk == 1);
+    const int Mi32 = (int)g.Mi;
+    const int per_vec = g.mtiles * g.ntn;
+    auto rowoff = [&](int m) -> i64 {
+        const int mq = m / Mi32;
+        return (i64)(m - mq * Mi32) * g.s1 + (i64)mq * g.s2;
+    };
+    auto vgated = [&](int z) -> bool { return g.vgate && g.vgate[(i64)z * g.vgate_stride]; };
+    auto fail = [&]() {
+        *abort_flag = 1;
+        if (g.err) atomicExch(g.err, 6);
+    };
+    // tile -> vector, first row, N tile
+    auto tile_of = [&](int it, int &z, int &m0, int &nt) {
+        const int tau = (int)blockIdx.x + it * G;
+        z = tau / per_vec;
+        const int r = tau - z * per_vec;
+        const int mt = r / g.ntn;
+        nt = r - mt * g.ntn;
+        m0 = mt * kQM;
+    };
+
+    if (tid == 0) {
+        if (smem_addr(slots) & 1023) { if (g.err) atomicExch(g.err, 6); }
+        for (int i = 0; i < kQSlots; ++i) { mbar_init(&full[i], 1); mbar_init(&empty[i], kQConv + 1); }
+        for (int i = 0; i < kQPlanes; ++i) { mbar_init(&pfull[i], kQConv); mbar_init(&pfree[i], 1); }
+        mbar_init(accfull, 1);
+        mbar_init(accempty, 32 * kQEpiWarps);
+        mbar_init(drain, 1);
+        *abort_flag = 0;
+        mbar_init_fence();
+    }
+    if (warp == kQMmaWarp) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;"
+                     :: "r"(smem_addr(tslot)), "r"(512) : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    fence_before();
+    __syncthreads();
+    fence_after();
+    const uint32_t tbase = *tslot;
+
+    if (warp < kQConv / 32) {
+        // ------------------------------------------------------ converters --
+        const int row = tid & (kQM - 1), h = tid >> 7;
+        const int poff = (row >> 3) * 256 + h * 128 + (row & 7) * 16;
+        int ks = 0, it = 0, fs = 0, p = 0;
+        uint32_t fph = 0, pph = 0;
+        int e = 0;
+        if (nsteps > 0) {
+            int z, m0, nt;
+            tile_of(0, z, m0, nt);
+            e = q_exp(g.xmax[z]);
+        }
+        for (int q = 0; q < nsteps; ++q) {
+            if (!*abort_flag && !mbar_wait(&full[fs], fph)) fail();
+            const unsigned char *st = slots + fs * kQSlot;
+            unsigned long long xb[8];
+            if (kmajor) {
+                // the box's 128-byte swizzle: 16-byte piece c of row r at c ^ (r & 7)
+                #pragma unroll
+                for (int i = 0; i < 4; ++i) {
+                    const ulonglong2 v = *reinterpret_cast<const ulonglong2 *>(st + row * 128 + 16 * ((4 * h + i) ^ (row & 7)));
+                    xb[2 * i] = v.x;
+                    xb[2 * i + 1] = v.y;
+                }
+            } else {
+                const unsigned long long *sd = reinterpret_cast<const unsigned long long *>(st) + (row >> 5) * 512 + (row & 31);
+                #pragma unroll
+                for (int j = 0; j < 8; ++j) xb[j] = sd[(8 * h + j) * 32];
+            }
+            mbar_arrive(&empty[fs]);
+            // the 49-bit magnitudes as 28 + 21 bits; digit s = bits 42-7s .. 48-7s
+            uint32_t Fh[8], Fl[8], sg[8];
+            #pragma unroll
+            for (int j = 0; j < 8; ++j) {
+                const unsigned long long F = q_fixed49(xb[j], e);
+                Fh[j] = (uint32_t)(F >> 21);
+                Fl[j] = (uint32_t)F & 0x1FFFFFu;
+                sg[j] = (uint32_t)(xb[j] >> 32) & 0x80000000u;
+            }
+            if (q >= kQPlanes && !*abort_flag && !mbar_wait(&pfree[p], pph ^ 1u)) fail();
+            unsigned char *pl = planes + p * kQPlane;
+            #pragma unroll
+            for (int s = 0; s < kQDig; ++s) {
+                uint32_t w[4];
+                #pragma unroll
+                for (int j = 0; j < 8; j += 2) {
+                    const uint32_t d0 = s < 4 ? (Fh[j] >> (21 - 7 * s)) & 127u : (Fl[j] >> (42 - 7 * s)) & 127u;
+                    const uint32_t d1 = s < 4 ? (Fh[j + 1] >> (21 - 7 * s)) & 127u : (Fl[j + 1] >> (42 - 7 * s)) & 127u;
+                    // the digit as an exact float (2^23 + d - 2^23) with x's sign; its
+                    // upper 16 bits are the BF16 digit
+                    const uint32_t f0 = __float_as_uint(__uint_as_float(0x4B000000u | d0) - 8388608.0f) | sg[j];
+                    const uint32_t f1 = __float_as_uint(__uint_as_float(0x4B000000u | d1) - 8388608.0f) | sg[j + 1];
+                    w[j >> 1] = __byte_perm(f0, f1, 0x7632);
+                }
+                *reinterpret_cast<uint4 *>(pl + s * (kQM * 32) + poff) = make_uint4(w[0], w[1], w[2], w[3]);
+            }
+            fence_proxy_async_smem();
+            mbar_arrive(&pfull[p]);
+            if (++fs == kQSlots) { fs = 0; fph ^= 1u; }
+            if (++p == kQPlanes) { p = 0; pph ^= 1u; }
+            if (++ks == KS) {
+                ks = 0;
+                if (++it < niter) {
+                    int z, m0, nt;
+                    tile_of(it, z, m0, nt);
+                    e = q_exp(g.xmax[z]);
+                }
+            }
+        }
+    } else if (warp == kQLoadWarp) {
+        // ------------------------------------------------------ load lane --
+        if (lane == 0) {
+            int pit = 0, pks = 0, pz = 0, pm0 = 0, pnt = 0;
+            bool pskip = false;
+            if (nsteps > 0) { tile_of(0, pz, pm0, pnt); pskip = vgated(pz); }
+            int prod = 0;
+            for (; prod < nsteps && !*abort_flag; ++prod) {
+                const int sl = prod % kQSlots;
+                if (prod >= kQSlots && !mbar_wait(&empty[sl], (uint32_t)(((prod / kQSlots) - 1) & 1))) { fail(); break; }
+                unsigned char *dst = slots + sl * kQSlot;
+                if (pskip) {
+                    mbar_arrive(&full[sl]);
+                } else {
+                    mbar_arrive_expect_tx(&full[sl], (uint32_t)(kQSlabA + bstep));
+                    if (kmajor) {
+                        tma_load_3d(dst, &tmA, pks * 16, pm0, pz, &full[sl]);
+                    } else {
+                        #pragma unroll
+                        for (int j = 0; j < 4; ++j) {
+                            const int m = pm0 + 32 * j;
+                            tma_load_4d(dst + j * 4096, &tmA, m % Mi32, pks * 16, m / Mi32, pz, &full[sl]);
+                        }
+                    }
+                    bulk_g2s(dst + kQSlabA, g.bdig + ((size_t)pnt * KS + pks) * kQDig * NT * 16, (uint32_t)bstep,
+                             &full[sl]);
+                }
+                if (++pks == KS) {
+                    pks = 0;
+                    if (++pit < niter) { tile_of(pit, pz, pm0, pnt); pskip = vgated(pz); }
+                }
+            }
+            for (int q = prod - kQSlots < 0 ? 0 : prod - kQSlots; q < prod; ++q)
+                mbar_wait_timed(&full[q % kQSlots], (uint32_t)((q / kQSlots) & 1), 200000000ull);
+        }
+        __syncwarp();
+    } else if (warp == kQMmaWarp) {
+        // -------------------------------------------------------- MMA lane --
+        if (lane == 0) {
+            // group accumulator g at TMEM column g NT, the B digit planes of a step
+            // consecutive: one MMA of A_s with the planes t .. t+c-1 (N = c NT <= 256)
+            // writes the groups s+t .. s+t+c-1 at once
+            const int per = (256 / NT) < kQDig ? 256 / NT : kQDig;
+            int q = 0, it = 0, fs = 0, p = 0;
+            uint32_t fph = 0, pph = 0;
+            for (; it < niter && !*abort_flag; ++it) {
+                if (it >= 1 && !mbar_wait(accempty, (uint32_t)((it - 1) & 1))) { fail(); break; }
+                for (int ks = 0; ks < KS; ++ks, ++q) {
+                    if (!mbar_wait(&pfull[p], pph) || !mbar_wait(&full[fs], fph)) { fail(); break; }
+                    fence_after();
+                    const unsigned char *Ab = planes + p * kQPlane;
+                    const unsigned char *Bb = slots + fs * kQSlot + kQSlabA;
+                    #pragma unroll 1
+                    for (int s = 0; s < kQDig; ++s) {
+                        const uint64_t ad = smem_desc(smem_addr(Ab + s * (kQM * 32)), 128, 256);
+                        #pragma unroll 1
+                        for (int t = 0; t + s < kQDig; t += per) {
+                            const int cnt = (kQDig - s - t) < per ? (kQDig - s - t) : per;
+                            const uint64_t bd = smem_desc(smem_addr(Bb + t * (NT * 32)), 128, 256);
+                            tc_mma(tbase + (uint32_t)((s + t) * NT), ad, bd, idesc_bf16(cnt * NT),
+                                   (ks > 0 || s > 0) ? 1u : 0u);
+                        }
+                    }
+                    tc_commit(&pfree[p]);
+                    tc_commit(&empty[fs]);
+                    if (++fs == kQSlots) { fs = 0; fph ^= 1u; }
+                    if (++p == kQPlanes) { p = 0; pph ^= 1u; }
+                }
+                if (*abort_flag) break;
+                tc_commit(accfull);
+            }
+            tc_commit(drain);
+            mbar_wait_timed(drain, 0, 200000000ull);
+        }
+        __syncwarp();
+    } else {
+        // -------------------------------------------------------- epilogue --
+        const int qd = warp & 3;                 // TMEM lanes 32 qd .. 32 qd + 31
+        const int ew = warp - kQConv / 32;
+        const int hc = ew >> 2;                  // this warp's half of the N tile
+        double *stg0 = stage + ew * 2 * kQStage;
+        const uint32_t lane_base = (uint32_t)(qd * 32) << 16;
+        const int half = NT / 2;                 // a multiple of 8
+        int nstore = 0;
+        for (int it = 0; it < niter; ++it) {
+            int z, m0, nt;
+            tile_of(it, z, m0, nt);
+            bool ok = !*abort_flag;
+            if (ok && !mbar_wait_sleep(accfull, (uint32_t)(it & 1), 256)) { fail(); ok = false; }
+            ok = __all_sync(0xffffffffu, ok);
+            fence_after();
+            if (ok && !vgated(z)) {
+                const int ex = q_exp(g.xmax[z]);
+                const double shift = g.shiftv ? g.shiftv[z] : g.shift;
+                const double *Vd = g.diagV;
+                const double *Xd = g.diagX + (i64)z * g.dx_sz;
+                double *C = g.C + (i64)z * g.c_sz;
+                const int r = qd * 32 + lane;
+                const int m = m0 + r;
+                const bool mval = m < g.M;
+                const i64 moff = mval ? rowoff(m) : 0;
+                const double rs = (g.rowscale && mval) ? g.rowscale[m % Mi32] : 1.0;
+                const int sw = (lane >> 1) & 3;
+                const bool rows_in = m0 + qd * 32 < g.M;
+                // exact group sums -> 64-bit integer -> FP64, times 2^e_n (an
+                // exponent add on the bits) and the row's scale
+                // T 2^(e_x + e_n - 49), |T| < 2^60, rounded to nearest even and
+                // assembled from integer operations (the FP64 pipe is the scarce
+                // one); then the row's scale when it is not 1
+                const bool unit = (g.alpha * rs == 1.0);
+                auto recombine = [&](const float *gq, int n) -> double {
+                    long long T = ((long long)__float2int_rn(gq[kQDig - 1])) >> 7;
+                    #pragma unroll
+                    for (int k = kQDig - 2; k >= 0; --k)
+                        T += (long long)__float2int_rn(gq[k]) << (7 * (kQDig - 2 - k));
+                    if (T == 0 || n >= g.N) return 0.0;
+                    const unsigned long long sgn = (unsigned long long)T & 0x8000000000000000ULL;
+                    const unsigned long long a = T < 0 ? (unsigned long long)(-T) : (unsigned long long)T;
+                    const int lz = __clzll((long long)a);
+                    const unsigned long long top = a << lz;              // leading one at bit 63
+                    unsigned long long mant = top >> 11;                   // 53 bits
+                    const unsigned long long low = top & 0x7FFULL;
+                    if (low > 0x400ULL || (low == 0x400ULL && (mant & 1ULL))) ++mant;
+                    int ef = 1023 + 63 - lz + ex - 49 + g.bexp[n];
+                    if (mant >> 53) { mant >>= 1; ++ef; }
+                    double val;
+                    if (ef > 0 && ef < 2047)
+                        val = __longlong_as_double((long long)(sgn | ((unsigned long long)ef << 52) |
+                                                               (mant & 0x000FFFFFFFFFFFFFULL)));
+                    else
+                        val = ldexp((double)T, ex - 49 + g.bexp[n]);   // outside the normal range
+                    return unit ? val : val * (g.alpha * rs);
+                };
+                if (g.tstore) {
+                    // rows along n, nothing to add: 32 x 8 blocks through a
+                    // 64-byte-swizzled stage, one TMA store each (rows and
+                    // columns past the level's last are clipped)
+                    for (int c0 = hc * half; c0 < hc * half + half; c0 += 8) {
+                        float gv[kQDig][8];
+                        #pragma unroll
+                        for (int gq = 0; gq < kQDig; ++gq)
+                            tmem_ld8(tbase + lane_base + (uint32_t)(gq * NT + c0), gv[gq]);
+                        asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+                        double *stg = stg0 + (nstore & 1) * kQStage;
+                        if (nstore >= 2) {
+                            if (lane == 0) asm volatile("cp.async.bulk.wait_group.read 1;" ::: "memory");
+                            __syncwarp();
+                        }
+                        #pragma unroll
+                        for (int c2 = 0; c2 < 4; ++c2) {
+                            float g0[kQDig], g1[kQDig];
+                            #pragma unroll
+                            for (int gq = 0; gq < kQDig; ++gq) { g0[gq] = gv[gq][2 * c2]; g1[gq] = gv[gq][2 * c2 + 1]; }
+                            const int n = nt * NT + c0 + 2 * c2;
+                            *reinterpret_cast<double2 *>(stg + lane * 8 + 2 * (c2 ^ sw)) =
+                                make_double2(recombine(g0, n), recombine(g1, n + 1));
+                        }
+                        fence_proxy_async_smem();
+                        __syncwarp();
+                        if (lane == 0 && rows_in) {
+                            tma_store_3d(&tmC, stg, nt * NT + c0, m0 + qd * 32, z);
+                            asm volatile("cp.async.bulk.commit_group;" ::: "memory");
+                        }
+                        ++nstore;
+                    }
+                } else {
+                    // a lane owns grid row m; groups of 4 columns, every load of a
+                    // group (accumulated output, diagonal term) issued with its
+                    // TMEM loads (points fastest: 32 consecutive points a column)
+                    for (int c0 = hc * half; c0 < hc * half + half; c0 += 4) {
+                        float gv[kQDig][4];
+                        #pragma unroll
+                        for (int gq = 0; gq < kQDig; ++gq)
+                            tmem_ld4(tbase + lane_base + (uint32_t)(gq * NT + c0), gv[gq]);
+                        double cy[4], dv[4], dx[4];
+                        #pragma unroll
+                        for (int j = 0; j < 4; ++j) {
+                            const int n = nt * NT + c0 + j;
+                            const bool in = mval && n < g.N;
+                            const i64 pp = moff + (i64)n * g.c_sn;
+                            cy[j] = (in && g.accumulate) ? C[pp] : 0.0;
+                            dv[j] = (in && Vd) ? Vd[pp] : 0.0;
+                            dx[j] = (in && Vd) ? Xd[pp] : 0.0;
+                        }
+                        asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+                        if (!mval) continue;
+                        #pragma unroll
+                        for (int j = 0; j < 4; ++j) {
+                            const int n = nt * NT + c0 + j;
+                            if (n >= g.N) break;
+                            float gj[kQDig];
+                            #pragma unroll
+                            for (int gq = 0; gq < kQDig; ++gq) gj[gq] = gv[gq][j];
+                            double o = recombine(gj, n);
+                            if (Vd) o = fma(g.alpha * (dv[j] - shift), dx[j], o);
+                            C[moff + (i64)n * g.c_sn] = o + cy[j];
+                        }
+                    }
+                }
+            }
+            fence_before();
+            mbar_arrive(accempty);
+        }
+        if (lane == 0 && nstore > 0) asm volatile("cp.async.bulk.wait_group 0;" ::: "memory");
+        __syncwarp();
+    }
+
+    fence_before();
+    __syncthreads();
+    if (warp == kQMmaWarp)
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" :: "r"(tbase), "r"(512) : "memory");
+}
+
+// Per-vector max |x| as FP64 bits; out[] must be zero before the launch.
+__global__ void absmax64_kernel(const double *__restrict__ X, i64 n, i64 vstride, unsigned long long *out,
+                                const int *gate, const int *vgate, int vgstride)
+{
+    if (gate && *gate) return;
+    const int z = blockIdx.y;
+    if (vgate && vgate[(i64)z * vgstride]) return;
+    const double *x = X + (i64)z * vstride;
+    unsigned long long mx = 0;
+    const i64 n2 = n / 2;
+    const double2 *x2 = reinterpret_cast<const double2 *>(x);
+    for (i64 i = blockIdx.x * (i64)blockDim.x + threadIdx.x; i < n2; i += (i64)gridDim.x * blockDim.x) {
+        const double2 v = __ldg(x2 + i);
+        const unsigned long long a = (unsigned long long)__double_as_longlong(fabs(v.x));
+        const unsigned long long b = (unsigned long long)__double_as_longlong(fabs(v.y));
+        mx = max(mx, max(a, b));
+    }
+    for (i64 i = 2 * n2 + blockIdx.x * (i64)blockDim.x + threadIdx.x; i < n; i += (i64)gridDim.x * blockDim.x)
+        mx = max(mx, (unsigned long long)__double_as_longlong(fabs(x[i])));
+    #pragma unroll
+    for (int o = 16; o > 0; o >>= 1) mx = max(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+    __shared__ unsigned long long red[32];
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = mx;
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        mx = threadIdx.x < (blockDim.x >> 5) ? red[threadIdx.x] : 0ULL;
+        #pragma unroll
+        for (int o = 16; o > 0; o >>= 1) mx = max(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+        if (threadIdx.x == 0) atomicMax(out + z, mx);
+    }
+}
+
+// ------------------------------------------------------------------ host --
+
+int tc64p_prepare(scalit_ctx *c)
+{
+    if (!c->xmax64) SC_CUDA(cudaMalloc(&c->xmax64, sizeof(unsigned long long) * kQMaxVec));
+    return 0;
+}
+
+// The persistent FP64 kernel applies to level l when the digit engine holds a
+// plan for it (N tile <= 64 columns) and the operand's rows allow the tensor
+// copies: rows along k of an even length, or points fastest in blocks of a
+// multiple of 32.
+bool tc64p_usable(const scalit_ctx *c, int l)
+{
+    const Layout &L = c->L;
+    if (L.ndvr && l == L.nlev - 1) return false;
+    const TcLevelData &t = c->tc[l];
+    if (!t.usable || t.NT > kQNTMax || t.NT % 16 || !c->xmax64) return false;
+    const int nout = L.n[l];
+    const i64 nin = L.dim[l];
+    if (L.N % 2 || nout % 2 || nout > 160) return false;
+    if (nin > 1 && nin % 32) return false;
+    return true;
+}
+
+int tc64p_scales(const scalit_ctx *c, const double *X, int nvec, const int *gate, cudaStream_t s, const int *vgate,
+                 int vstride)
+{
+    if (nvec > kQMaxVec) { set_error("more than %d vectors in one FP64 tensor-core launch", kQMaxVec); return SCALIT_EINVAL; }
+    if (reinterpret_cast<uintptr_t>(X) & 15) { set_error("FP64 tensor-core operand not 16-byte aligned"); return SCALIT_EINVAL; }
+    SC_CUDA(cudaMemsetAsync(c->xmax64, 0, sizeof(unsigned long long) * nvec, s));
+    const i64 n2 = c->L.N / 2;
+    int bx = (int)((n2 + 255) / 256);
+    const int cap = 152 * 8 / (nvec < 8 ? nvec : 8) + 1;
+    if (bx > cap) bx = cap;
+    absmax64_kernel<<<dim3(bx, nvec), 256, 0, s>>>(X, c->L.N, c->L.N, c->xmax64, gate, vgate, vstride);
+    SC_CHECK_LAUNCH();
+    return 0;
+}
+
+int tc64p_level_apply(const scalit_ctx *c, int l, const double *X, double *Y, int accumulate, const double *diagV,
+                      double shift, double alpha, const int *gate, cudaStream_t s, int nvec, const double *shiftv,
+                      const int *vgate, int vstride)
+{
+    const Layout &L = c->L;
+    const TcLevelData &t = c->tc[l];
+    if (!tc64p_usable(c, l)) { set_error("level %d has no persistent FP64 tensor-core plan", l + 1); return SCALIT_EUNSUP; }
+    if ((reinterpret_cast<uintptr_t>(X) & 15) || (reinterpret_cast<uintptr_t>(Y) & 15)) {
+        set_error("persistent FP64 tensor-core operands not 16-byte aligned");
+        return SCALIT_EINVAL;
+    }
+    if (nvec > kQMaxVec) { set_error("more than %d vectors in one persistent launch", kQMaxVec); return SCALIT_EINVAL; }
+    const int nout = L.n[l];
+    const i64 nin = L.dim[l], blk = L.blk[l], N = L.N;
+    Tc64pArgs g{};
+    g.N = nout; g.K = nout; g.KS = t.KS; g.NT = t.NT; g.ntn = t.ntiles;
+    if (nin == 1) {
+        g.M = (int)blk; g.Mi = blk; g.s1 = nout; g.s2 = 0; g.a_sk = 1; g.c_sn = 1;
+        g.rowscale = nullptr;
+    } else {
+        const i64 M = nin * blk;
+        if (M > 2147483647LL) { set_error("level %d too large", l + 1); return SCALIT_EINVAL; }
+        g.M = (int)M; g.Mi = nin; g.s1 = 1; g.s2 = nin * nout; g.a_sk = nin; g.c_sn = nin;
+        g.rowscale = L.dep[l] ? c->DEP + L.deps[l] : nullptr;
+    }
+    g.mtiles = (g.M + kQM - 1) / kQM;
+    const i64 tiles = (i64)g.mtiles * g.ntn * nvec;
+    if (tiles > 2147483647LL) { set_error("level %d: too many tiles", l + 1); return SCALIT_EINVAL; }
+    g.tiles = (int)tiles;
+    g.C = Y; g.c_sz = N;
+    g.accumulate = accumulate; g.alpha = alpha;
+    g.diagV = diagV; g.diagX = X; g.dx_sz = N; g.shift = shift; g.shiftv = shiftv;
+    g.vgate = vgate; g.vgate_stride = vstride;
+    g.gate = gate; g.err = c->tc_err;
+    g.bdig = t.dig;
+    g.bexp = t.exps;
+    g.xmax = c->xmax64;
+    g.tstore = (g.c_sn == 1 && !accumulate && !diagV) ? 1 : 0;
+
+    // the grid operand: [vector][row][k] boxes of 16 k x 128 rows (128-byte
+    // swizzle) or [vector][block][k][point] boxes of 32 points x 16 k; the
+    // level-1 output for TMA stores: [vector][row][n] boxes of 8 n x 32 rows
+    CUtensorMap tmA, tmC;
+    int rc;
+    if (nin == 1) {
+        const cuuint64_t dims[3] = {(cuuint64_t)nout, (cuuint64_t)blk, (cuuint64_t)nvec};
+        const cuuint64_t str[2] = {(cuuint64_t)nout * 8, (cuuint64_t)N * 8};
+        const cuuint32_t box[3] = {16, kQM, 1};
+        rc = tma_encode(&tmA, X, true, 3, dims, str, box, CU_TENSOR_MAP_SWIZZLE_128B);
+        if (!rc && g.tstore) {
+            const cuuint32_t boxc[3] = {8, 32, 1};
+            rc = tma_encode(&tmC, Y, true, 3, dims, str, boxc, CU_TENSOR_MAP_SWIZZLE_64B);
+        }
+    } else {
+        const cuuint64_t dims[4] = {(cuuint64_t)nin, (cuuint64_t)nout, (cuuint64_t)blk, (cuuint64_t)nvec};
+        const cuuint64_t str[3] = {(cuuint64_t)nin * 8, (cuuint64_t)nin * nout * 8, (cuuint64_t)N * 8};
+        const cuuint32_t box[4] = {32, 16, 1, 1};
+        rc = tma_encode(&tmA, X, true, 4, dims, str, box, CU_TENSOR_MAP_SWIZZLE_NONE);
+    }
+    if (rc) return rc;
+    if (!g.tstore) tmC = tmA;
+
+    static int sms = 0, configured = -1;
+    int dev = 0;
+    cudaGetDevice(&dev);
+    if (configured != dev) {
+        SC_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+        SC_CUDA(cudaFuncSetAttribute(tc64p_level_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)q_smem_bytes()));
+        configured = dev;
+    }
+    const int grid = (int)(tiles < sms ? tiles : sms);
+    tc64p_level_kernel<<<grid, kQThreads, q_smem_bytes(), s>>>(g, tmA, tmC);
+    SC_CHECK_LAUNCH();
+    return 0;
+}
+
+}  // namespace sc
