@@ -169,7 +169,7 @@ void scalit_destroy(scalit_ctx *c)
         if (l == 0) { tc_free_px(c); tc32_free(c, true, true); tc16_free(c); }
     }
     if (c->tc_err) cudaFree(c->tc_err);
-    if (c->xmax64) cudaFree(c->xmax64);
+    if (c->rexp) cudaFree(c->rexp);
     osbw_free(c);
     double *aptrs[] = {c->APP, c->APR, c->AP};
     for (double *p : aptrs) if (p) cudaFree(p);

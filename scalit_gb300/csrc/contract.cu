@@ -300,10 +300,11 @@ int hx_batch(const scalit_ctx *c, const T *X, T *Y, int nvec, T shift, T alpha, 
         // FP64 digit engine: the persistent kernel wherever it applies, after
         // the vectors' exponents
         const bool aligned = !(reinterpret_cast<uintptr_t>(X) & 15) && !(reinterpret_cast<uintptr_t>(Y) & 15);
-        if (aligned && c->fp64_mode == SCALIT_FP64_TENSOR) {
-            for (int l = 0; l < L.nlev; ++l) p64 = p64 || tc64p_usable(c, l);
-            if (p64) {
-                rc = tc64p_scales(c, X, nvec, gate, s, vgate, vstride);
+        if (aligned && c->fp64_mode == SCALIT_FP64_TENSOR && nvec <= tc64p_vectors_max()) {
+            for (int l = 0; l < L.nlev; ++l) {
+                if (!tc64p_usable(c, l)) continue;
+                p64 = true;
+                rc = tc64p_rowexp(c, l, X, nvec, gate, s, vgate, vstride);
                 if (rc) return rc;
             }
         }

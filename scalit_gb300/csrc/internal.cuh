@@ -119,7 +119,8 @@ struct scalit_ctx {
     // (SCALIT_FP32_TENSOR16) and the per-vector scale slots of one launch
     TcLevelData tc16[SCALIT_FMAX];
     unsigned *xmax = nullptr;
-    unsigned long long *xmax64 = nullptr;   // per-vector max |x| bits (persistent FP64 engine)
+    int *rexp = nullptr;                    // row exponents of the persistent FP64 engine's levels
+    i64 rexp_off[SCALIT_FMAX] = {};
     int *tc_err = nullptr;
     // Measurement aid: when set, hx_batch records lev_ev[l] before level l's
     // launch and lev_ev[nlev] after the last (scalit_hx_level_times).
@@ -224,7 +225,8 @@ int tma_encode(CUtensorMap *map, const void *base, bool f64, int rank, const cuu
 int tc16_prepare(scalit_ctx *c);
 int tc64p_prepare(scalit_ctx *c);
 bool tc64p_usable(const scalit_ctx *c, int level);
-int tc64p_scales(const scalit_ctx *c, const double *X, int nvec, const int *gate, cudaStream_t s,
+int tc64p_vectors_max();
+int tc64p_rowexp(const scalit_ctx *c, int level, const double *X, int nvec, const int *gate, cudaStream_t s,
                  const int *vgate = nullptr, int vstride = 0);
 int tc64p_level_apply(const scalit_ctx *c, int level, const double *X, double *Y, int accumulate,
                       const double *diagV, double shift, double alpha, const int *gate, cudaStream_t s, int nvec,

@@ -157,7 +157,10 @@ tc_level_kernel(TcArgs g)
         __syncthreads();
         fence_after();
         const uint32_t tbase = *tslot;
-        const uint32_t idesc = idesc_bf16(NT);
+        // group g at TMEM column g NT and the step's B digit planes consecutive:
+        // one product of A_s with the planes t .. t+c-1 (N = c NT <= 256) writes
+        // the groups s+t .. s+t+c-1 at once
+        const int per = (256 / NT) < kDigits ? 256 / NT : kDigits;
         const int lane = tid & 31;
         for (int ks = 0; ks < KS; ++ks) {
             const int buf = ks & 1;
@@ -170,10 +173,11 @@ tc_level_kernel(TcArgs g)
                 for (int s = 0; s < kDigits; ++s) {
                     const uint64_t ad = smem_desc(smem_addr(Ab + s * (kBM * 32)), 128, 256);
                     #pragma unroll 1
-                    for (int t = 0; t + s < kGroups; ++t) {
+                    for (int t = 0; t + s < kGroups; t += per) {
+                        const int cnt = (kGroups - s - t) < per ? (kGroups - s - t) : per;
                         const uint64_t bd = smem_desc(smem_addr(Bb + t * (NT * 32)), 128, 256);
                         const uint32_t acc = (ks > 0 || s > 0) ? 1u : 0u;
-                        tc_mma(tbase + (uint32_t)((s + t) * NT), ad, bd, idesc, acc);
+                        tc_mma(tbase + (uint32_t)((s + t) * NT), ad, bd, idesc_bf16(cnt * NT), acc);
                     }
                 }
                 tc_commit(&mbar[buf]);

@@ -1,13 +1,14 @@
 // Persistent FP64 level products of H*X on the tcgen05 digit engine.
 //
-// The arithmetic is the digit scheme of tc_fp64.cu: with e_x the binary
-// exponent of max|x| over the vector and e_n that of column n of B,
-//   A(m, k) = 2^e_x sum_{s=0..6} a_s 2^-7(s+1),  B(k, n) = 2^e_n sum_t b_t 2^-7(t+1),
+// The arithmetic is the digit scheme of tc_fp64.cu: with e_m the binary
+// exponent of the largest |x| of grid row m and e_n that of column n of B,
+//   A(m, k) = 2^e_m sum_{s=0..6} a_s 2^-7(s+1),  B(k, n) = 2^e_n sum_t b_t 2^-7(t+1),
 // |a_s|, |b_t| <= 127 integers (exact in BF16), and the 28 digit pairs with
 // s + t <= 6 accumulate into 7 FP32 group accumulators in TMEM (exact for
 // groups 0..5 with K <= 160), recombined in 64-bit integers in the epilogue.
-// One exponent per vector (instead of per grid row) lets every K slab be cut
-// as it arrives; it leaves an error of ~2^-46 max|x| |B| per product.
+// The row exponents come from one pass over each level's rows before the
+// level (rowexp_kernel), so every K slab can be cut as it arrives; the digits
+// are those of tc_fp64.cu.
 //
 // The pipeline is that of tc_fp32p.cu: one CTA per SM walks tiles of 128
 // grid rows x one N tile of at most 64 columns (7 x 64 TMEM columns), N tile
@@ -38,9 +39,11 @@ namespace sc {
 static constexpr int kQM = 128;
 static constexpr int kQConv = 256;
 static constexpr int kQEpiWarps = 8;
-static constexpr int kQThreads = kQConv + 32 * kQEpiWarps + 64;
+static constexpr int kQThreads = kQConv + 32 * kQEpiWarps + 96;
 static constexpr int kQMmaWarp = kQConv / 32 + kQEpiWarps;
 static constexpr int kQLoadWarp = kQMmaWarp + 1;
+static constexpr int kQELoadWarp = kQMmaWarp + 2;              // the epilogue operands' load lane
+static constexpr int kQERingMax = 8;
 static constexpr int kQDig = 7;
 static constexpr int kQNTMax = 64;
 static constexpr int kQSlabA = kQM * 16 * 8;                   // FP64 slab: 16 KB
@@ -50,7 +53,6 @@ static constexpr int kQSlots = 3;
 static constexpr int kQPlane = kQDig * kQM * 32;               // A digit planes of a K step: 28 KB
 static constexpr int kQPlanes = 3;
 static constexpr int kQStage = 32 * 8;                         // doubles per epilogue stage (2 per warp)
-static constexpr int kQMaxVec = 4096;
 
 struct Tc64pArgs {
     int M, K, KS, N, NT, ntn;   // rows per vector, contraction, K steps, output columns, N tile, N tiles
@@ -69,14 +71,31 @@ struct Tc64pArgs {
     int *err;
     const uint16_t *bdig;       // [ntile][ks][digit][NT x 16] canonical K-major
     const int *bexp;            // [ntile * NT] column exponents
-    const unsigned long long *xmax;   // per vector: bits of max |x|
+    const int *rexp;            // per row of every vector (z M + m): binary exponent of the row's max |x|
     int tstore;                 // outputs contiguous along n, nothing to add: TMA stores
+    int ering, echunk;          // points fastest: epilogue operand ring slots and bytes per slot
 };
 
-static size_t q_smem_bytes()
+// Shared memory: step slots, plane slots, the epilogue region (level 1: two
+// 32 x 8 stages per epilogue warp; otherwise the operand ring), barriers.
+static constexpr size_t kQStageBytes = (size_t)kQEpiWarps * 2 * kQStage * 8;
+static constexpr size_t kQFixed = (size_t)kQSlots * kQSlot + (size_t)kQPlanes * kQPlane +
+                                  (2 * kQSlots + 2 * kQPlanes + 2 * kQERingMax + 4) * 8 + 16;
+static constexpr int kQMaxSmem = 227 * 1024;
+
+static size_t q_smem_bytes(size_t ebytes)
 {
-    return (size_t)kQSlots * kQSlot + (size_t)kQPlanes * kQPlane + (size_t)kQEpiWarps * 2 * kQStage * 8 +
-           (2 * kQSlots + 2 * kQPlanes + 4) * 8 + 16;
+    return kQFixed + (ebytes > kQStageBytes ? ebytes : kQStageBytes);
+}
+
+// Epilogue operand ring of a points-fastest level: 8 KB per operand and
+// 8-column chunk (the output, and V and X for the diagonal term).
+static int q_ring(bool diag, int *echunk)
+{
+    const int chunk = 8192 * (diag ? 3 : 1);
+    if (echunk) *echunk = chunk;
+    int r = (int)(((size_t)kQMaxSmem - kQFixed) / chunk);
+    return r > kQERingMax ? kQERingMax : r;
 }
 
 // Binary exponent e with |x| < 2^e (frexp's) from the bits of |x|; 0 for zero.
@@ -99,7 +118,8 @@ __device__ __forceinline__ unsigned long long q_fixed49(unsigned long long bits,
 
 
 __global__ void __launch_bounds__(kQThreads, 1)
-tc64p_level_kernel(Tc64pArgs g, const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmC)
+tc64p_level_kernel(Tc64pArgs g, const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmC,
+                   const __grid_constant__ CUtensorMap tmV, const __grid_constant__ CUtensorMap tmX)
 {
     if (g.gate && *g.gate) return;
     extern __shared__ __align__(1024) unsigned char smem[];
@@ -108,13 +128,17 @@ tc64p_level_kernel(Tc64pArgs g, const __grid_constant__ CUtensorMap tmA, const _
     unsigned char *slots = smem;                                     // 1024-byte aligned
     unsigned char *planes = slots + kQSlots * kQSlot;
     double *stage = reinterpret_cast<double *>(planes + kQPlanes * kQPlane);
-    uint64_t *full = reinterpret_cast<uint64_t *>(stage + kQEpiWarps * 2 * kQStage);
+    const size_t ebytes = (size_t)g.ering * g.echunk;
+    uint64_t *full = reinterpret_cast<uint64_t *>(reinterpret_cast<unsigned char *>(stage) +
+                                                  (ebytes > kQStageBytes ? ebytes : kQStageBytes));
     uint64_t *empty = full + kQSlots;
     uint64_t *pfull = empty + kQSlots;
     uint64_t *pfree = pfull + kQPlanes;
     uint64_t *accfull = pfree + kQPlanes;
     uint64_t *accempty = accfull + 1;
-    uint64_t *drain = accempty + 1;
+    uint64_t *efull = accempty + 1;
+    uint64_t *eempty = efull + kQERingMax;
+    uint64_t *drain = eempty + kQERingMax;
     volatile int *abort_flag = reinterpret_cast<volatile int *>(drain + 1);
     uint32_t *tslot = reinterpret_cast<uint32_t *>(drain + 1) + 1;
 
@@ -150,6 +174,7 @@ tc64p_level_kernel(Tc64pArgs g, const __grid_constant__ CUtensorMap tmA, const _
         for (int i = 0; i < kQPlanes; ++i) { mbar_init(&pfull[i], kQConv); mbar_init(&pfree[i], 1); }
         mbar_init(accfull, 1);
         mbar_init(accempty, 32 * kQEpiWarps);
+        for (int i = 0; i < kQERingMax; ++i) { mbar_init(&efull[i], 1); mbar_init(&eempty[i], 4); }
         mbar_init(drain, 1);
         *abort_flag = 0;
         mbar_init_fence();
@@ -170,12 +195,14 @@ tc64p_level_kernel(Tc64pArgs g, const __grid_constant__ CUtensorMap tmA, const _
         const int poff = (row >> 3) * 256 + h * 128 + (row & 7) * 16;
         int ks = 0, it = 0, fs = 0, p = 0;
         uint32_t fph = 0, pph = 0;
-        int e = 0;
-        if (nsteps > 0) {
+        // this thread's grid row's exponent (the digits are the row's 49-bit
+        // fixed-point magnitudes, as in tc_fp64.cu)
+        auto row_exp = [&](int it) -> int {
             int z, m0, nt;
-            tile_of(0, z, m0, nt);
-            e = q_exp(g.xmax[z]);
-        }
+            tile_of(it, z, m0, nt);
+            return (m0 + row < g.M) ? g.rexp[(i64)z * g.M + m0 + row] : 0;
+        };
+        int e = nsteps > 0 ? row_exp(0) : 0;
         for (int q = 0; q < nsteps; ++q) {
             if (!*abort_flag && !mbar_wait(&full[fs], fph)) fail();
             const unsigned char *st = slots + fs * kQSlot;
@@ -226,13 +253,48 @@ tc64p_level_kernel(Tc64pArgs g, const __grid_constant__ CUtensorMap tmA, const _
             if (++p == kQPlanes) { p = 0; pph ^= 1u; }
             if (++ks == KS) {
                 ks = 0;
-                if (++it < niter) {
-                    int z, m0, nt;
-                    tile_of(it, z, m0, nt);
-                    e = q_exp(g.xmax[z]);
-                }
+                if (++it < niter) e = row_exp(it);
             }
         }
+    } else if (warp == kQELoadWarp) {
+        // ---------------------------------------- epilogue operands' lane --
+        // points fastest: per tile and 8-column chunk, the accumulated output
+        // (and for the diagonal term V and X) as four 32-point boxes each
+        if (lane == 0 && g.ering > 0) {
+            const int nck = NT / 8;
+            const bool dg = g.diagV != nullptr;
+            const uint32_t piece = 4 * 2048;
+            int cc = 0;
+            for (int it = 0; it < niter && !*abort_flag; ++it) {
+                int z, m0, nt;
+                tile_of(it, z, m0, nt);
+                const bool skip = vgated(z);
+                for (int ch = 0; ch < nck; ++ch, ++cc) {
+                    const int sl = cc % g.ering;
+                    if (cc >= g.ering && !mbar_wait(&eempty[sl], (uint32_t)(((cc / g.ering) - 1) & 1))) { fail(); break; }
+                    unsigned char *dst = reinterpret_cast<unsigned char *>(stage) + (size_t)sl * g.echunk;
+                    if (skip || (!g.accumulate && !dg)) {
+                        mbar_arrive(&efull[sl]);
+                        continue;
+                    }
+                    mbar_arrive_expect_tx(&efull[sl], (g.accumulate ? piece : 0u) + (dg ? 2 * piece : 0u));
+                    const int n0 = nt * NT + ch * 8;
+                    #pragma unroll
+                    for (int j = 0; j < 4; ++j) {
+                        const int m = m0 + 32 * j;
+                        const int c0 = m % Mi32, c2 = m / Mi32;
+                        if (g.accumulate) tma_load_4d(dst + j * 2048, &tmC, c0, n0, c2, z, &efull[sl]);
+                        if (dg) {
+                            tma_load_3d(dst + piece + j * 2048, &tmV, c0, n0, c2, &efull[sl]);
+                            tma_load_4d(dst + 2 * piece + j * 2048, &tmX, c0, n0, c2, z, &efull[sl]);
+                        }
+                    }
+                }
+            }
+            for (int q = cc - g.ering < 0 ? 0 : cc - g.ering; q < cc; ++q)
+                mbar_wait_timed(&efull[q % g.ering], (uint32_t)((q / g.ering) & 1), 200000000ull);
+        }
+        __syncwarp();
     } else if (warp == kQLoadWarp) {
         // ------------------------------------------------------ load lane --
         if (lane == 0) {
@@ -325,7 +387,7 @@ tc64p_level_kernel(Tc64pArgs g, const __grid_constant__ CUtensorMap tmA, const _
             ok = __all_sync(0xffffffffu, ok);
             fence_after();
             if (ok && !vgated(z)) {
-                const int ex = q_exp(g.xmax[z]);
+                const int ex = (m0 + qd * 32 + lane < g.M) ? g.rexp[(i64)z * g.M + m0 + qd * 32 + lane] : 0;
                 const double shift = g.shiftv ? g.shiftv[z] : g.shift;
                 const double *Vd = g.diagV;
                 const double *Xd = g.diagX + (i64)z * g.dx_sz;
@@ -344,10 +406,11 @@ tc64p_level_kernel(Tc64pArgs g, const __grid_constant__ CUtensorMap tmA, const _
                 // one); then the row's scale when it is not 1
                 const bool unit = (g.alpha * rs == 1.0);
                 auto recombine = [&](const float *gq, int n) -> double {
-                    long long T = ((long long)__float2int_rn(gq[kQDig - 1])) >> 7;
-                    #pragma unroll
-                    for (int k = kQDig - 2; k >= 0; --k)
-                        T += (long long)__float2int_rn(gq[k]) << (7 * (kQDig - 2 - k));
+                    // three 32-bit partial sums (each below 2^31), two 64-bit steps
+                    const int hi = (__float2int_rn(gq[0]) << 7) + __float2int_rn(gq[1]);
+                    const int md = (__float2int_rn(gq[2]) << 7) + __float2int_rn(gq[3]);
+                    const int lo = (__float2int_rn(gq[4]) << 7) + __float2int_rn(gq[5]) + (__float2int_rn(gq[6]) >> 7);
+                    const long long T = ((long long)hi << 28) + ((long long)md << 14) + lo;
                     if (T == 0 || n >= g.N) return 0.0;
                     const unsigned long long sgn = (unsigned long long)T & 0x8000000000000000ULL;
                     const unsigned long long a = T < 0 ? (unsigned long long)(-T) : (unsigned long long)T;
@@ -398,25 +461,61 @@ tc64p_level_kernel(Tc64pArgs g, const __grid_constant__ CUtensorMap tmA, const _
                         }
                         ++nstore;
                     }
+                } else if (g.ering > 0) {
+                    // points fastest: per 8-column chunk (this warp's: every
+                    // other one), the operands wait in the ring as [8 n][32
+                    // points] per quarter; the result overwrites the output's box,
+                    // which one TMA copy stores (points past the vector's last
+                    // are clipped); the slot is released once the copy read it
+                    const int nck = NT / 8;
+                    for (int ch = hc; ch < nck; ch += 2) {
+                        const int cc = it * nck + ch;
+                        const int sl = cc % g.ering;
+                        const int c0 = ch * 8;
+                        float gv[kQDig][8];
+                        #pragma unroll
+                        for (int gq = 0; gq < kQDig; ++gq)
+                            tmem_ld8(tbase + lane_base + (uint32_t)(gq * NT + c0), gv[gq]);
+                        bool eok = !*abort_flag && mbar_wait(&efull[sl], (uint32_t)((cc / g.ering) & 1));
+                        eok = __all_sync(0xffffffffu, eok);
+                        asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+                        if (!eok) { fail(); break; }
+                        double *cb = reinterpret_cast<double *>(reinterpret_cast<unsigned char *>(stage) +
+                                                                (size_t)sl * g.echunk) + qd * 256;
+                        #pragma unroll
+                        for (int j = 0; j < 8; ++j) {
+                            const int n = nt * NT + c0 + j;
+                            const int idx = j * 32 + lane;
+                            float gj[kQDig];
+                            #pragma unroll
+                            for (int gq = 0; gq < kQDig; ++gq) gj[gq] = gv[gq][j];
+                            double o = recombine(gj, n);
+                            if (Vd) o = fma(g.alpha * (cb[1024 + idx] - shift), cb[2048 + idx], o);
+                            if (g.accumulate) o += cb[idx];
+                            cb[idx] = o;
+                        }
+                        fence_proxy_async_smem();
+                        __syncwarp();
+                        if (lane == 0) {
+                            if (rows_in) {
+                                const int mq = m0 + qd * 32;
+                                tma_store_4d(&tmC, cb, mq % Mi32, nt * NT + c0, mq / Mi32, z);
+                                asm volatile("cp.async.bulk.commit_group;" ::: "memory");
+                                asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory");
+                                ++nstore;
+                            }
+                            mbar_arrive(&eempty[sl]);
+                        }
+                        __syncwarp();
+                    }
                 } else {
-                    // a lane owns grid row m; groups of 4 columns, every load of a
-                    // group (accumulated output, diagonal term) issued with its
-                    // TMEM loads (points fastest: 32 consecutive points a column)
+                    // rows along n with a diagonal term or an output to add (rare):
+                    // direct loads and stores, 4 columns at a time
                     for (int c0 = hc * half; c0 < hc * half + half; c0 += 4) {
                         float gv[kQDig][4];
                         #pragma unroll
                         for (int gq = 0; gq < kQDig; ++gq)
                             tmem_ld4(tbase + lane_base + (uint32_t)(gq * NT + c0), gv[gq]);
-                        double cy[4], dv[4], dx[4];
-                        #pragma unroll
-                        for (int j = 0; j < 4; ++j) {
-                            const int n = nt * NT + c0 + j;
-                            const bool in = mval && n < g.N;
-                            const i64 pp = moff + (i64)n * g.c_sn;
-                            cy[j] = (in && g.accumulate) ? C[pp] : 0.0;
-                            dv[j] = (in && Vd) ? Vd[pp] : 0.0;
-                            dx[j] = (in && Vd) ? Xd[pp] : 0.0;
-                        }
                         asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
                         if (!mval) continue;
                         #pragma unroll
@@ -426,11 +525,25 @@ tc64p_level_kernel(Tc64pArgs g, const __grid_constant__ CUtensorMap tmA, const _
                             float gj[kQDig];
                             #pragma unroll
                             for (int gq = 0; gq < kQDig; ++gq) gj[gq] = gv[gq][j];
+                            const i64 pp = moff + (i64)n * g.c_sn;
                             double o = recombine(gj, n);
-                            if (Vd) o = fma(g.alpha * (dv[j] - shift), dx[j], o);
-                            C[moff + (i64)n * g.c_sn] = o + cy[j];
+                            if (Vd) o = fma(g.alpha * (Vd[pp] - shift), Xd[pp], o);
+                            if (g.accumulate) o += C[pp];
+                            C[pp] = o;
                         }
                     }
+                }
+            } else if (ok && g.ering > 0) {
+                // a stopped vector: its ring chunks are released unread
+                const int nck = NT / 8;
+                for (int ch = hc; ch < nck; ch += 2) {
+                    const int cc = it * nck + ch;
+                    const int sl = cc % g.ering;
+                    if (lane == 0) {
+                        if (mbar_wait(&efull[sl], (uint32_t)((cc / g.ering) & 1))) mbar_arrive(&eempty[sl]);
+                        else fail();
+                    }
+                    __syncwarp();
                 }
             }
             fence_before();
@@ -446,56 +559,67 @@ tc64p_level_kernel(Tc64pArgs g, const __grid_constant__ CUtensorMap tmA, const _
         asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" :: "r"(tbase), "r"(512) : "memory");
 }
 
-// Per-vector max |x| as FP64 bits; out[] must be zero before the launch.
-__global__ void absmax64_kernel(const double *__restrict__ X, i64 n, i64 vstride, unsigned long long *out,
-                                const int *gate, const int *vgate, int vgstride)
+// Binary exponent of the largest |x| of every row of a level, for rows of
+// all vectors (out[z M + m]): rows along k (a_sk == 1) one warp per row,
+// otherwise one thread per row (consecutive rows, consecutive points).
+__global__ void rowexp_kernel(const double *__restrict__ X, i64 N, int M, int K, i64 Mi, i64 s1, i64 s2, i64 a_sk,
+                              int nvec, int *__restrict__ out, const int *gate, const int *vgate, int vgstride)
 {
     if (gate && *gate) return;
-    const int z = blockIdx.y;
-    if (vgate && vgate[(i64)z * vgstride]) return;
-    const double *x = X + (i64)z * vstride;
-    unsigned long long mx = 0;
-    const i64 n2 = n / 2;
-    const double2 *x2 = reinterpret_cast<const double2 *>(x);
-    for (i64 i = blockIdx.x * (i64)blockDim.x + threadIdx.x; i < n2; i += (i64)gridDim.x * blockDim.x) {
-        const double2 v = __ldg(x2 + i);
-        const unsigned long long a = (unsigned long long)__double_as_longlong(fabs(v.x));
-        const unsigned long long b = (unsigned long long)__double_as_longlong(fabs(v.y));
-        mx = max(mx, max(a, b));
-    }
-    for (i64 i = 2 * n2 + blockIdx.x * (i64)blockDim.x + threadIdx.x; i < n; i += (i64)gridDim.x * blockDim.x)
-        mx = max(mx, (unsigned long long)__double_as_longlong(fabs(x[i])));
-    #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) mx = max(mx, __shfl_xor_sync(0xffffffffu, mx, o));
-    __shared__ unsigned long long red[32];
-    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = mx;
-    __syncthreads();
-    if (threadIdx.x < 32) {
-        mx = threadIdx.x < (blockDim.x >> 5) ? red[threadIdx.x] : 0ULL;
+    const i64 rows = (i64)M * nvec;
+    if (a_sk == 1) {
+        const i64 w = (blockIdx.x * (i64)blockDim.x + threadIdx.x) >> 5;
+        const int lane = threadIdx.x & 31;
+        if (w >= rows) return;
+        const int z = (int)(w / M), m = (int)(w - (i64)z * M);
+        if (vgate && vgate[(i64)z * vgstride]) return;
+        const double *x = X + (i64)z * N + (i64)(m % Mi) * s1 + (i64)(m / Mi) * s2;
+        unsigned long long mx = 0;
+        for (int k = lane; k < K; k += 32) mx = max(mx, (unsigned long long)__double_as_longlong(fabs(x[k])));
         #pragma unroll
         for (int o = 16; o > 0; o >>= 1) mx = max(mx, __shfl_xor_sync(0xffffffffu, mx, o));
-        if (threadIdx.x == 0) atomicMax(out + z, mx);
+        if (lane == 0) out[w] = q_exp(mx);
+    } else {
+        const i64 t = blockIdx.x * (i64)blockDim.x + threadIdx.x;
+        if (t >= rows) return;
+        const int z = (int)(t / M), m = (int)(t - (i64)z * M);
+        if (vgate && vgate[(i64)z * vgstride]) return;
+        const double *x = X + (i64)z * N + (i64)(m % Mi) * s1 + (i64)(m / Mi) * s2;
+        unsigned long long mx = 0;
+        for (int k = 0; k < K; ++k) mx = max(mx, (unsigned long long)__double_as_longlong(fabs(x[(i64)k * a_sk])));
+        out[t] = q_exp(mx);
     }
 }
 
 // ------------------------------------------------------------------ host --
 
+// Row exponents of every level the persistent kernel takes, for up to
+// kQRexpVec vectors (one region per level).
+static constexpr int kQRexpVec = 32;
+
 int tc64p_prepare(scalit_ctx *c)
 {
-    if (!c->xmax64) SC_CUDA(cudaMalloc(&c->xmax64, sizeof(unsigned long long) * kQMaxVec));
+    const Layout &L = c->L;
+    if (c->rexp) { cudaFree(c->rexp); c->rexp = nullptr; }
+    i64 total = 0;
+    for (int l = 0; l < L.nlev; ++l) {
+        c->rexp_off[l] = total;
+        total += (L.N / L.n[l]) * kQRexpVec;
+    }
+    SC_CUDA(cudaMalloc(&c->rexp, sizeof(int) * (size_t)total));
     return 0;
 }
 
 // The persistent FP64 kernel applies to level l when the digit engine holds a
-// plan for it (N tile <= 64 columns) and the operand's rows allow the tensor
-// copies: rows along k of an even length, or points fastest in blocks of a
-// multiple of 32.
+// plan for it (N tile <= 64 columns, K <= 160) and the operand's rows allow
+// the tensor copies: rows along k of an even length, or points fastest in
+// blocks of a multiple of 32.
 bool tc64p_usable(const scalit_ctx *c, int l)
 {
     const Layout &L = c->L;
     if (L.ndvr && l == L.nlev - 1) return false;
     const TcLevelData &t = c->tc[l];
-    if (!t.usable || t.NT > kQNTMax || t.NT % 16 || !c->xmax64) return false;
+    if (!t.usable || t.NT > kQNTMax || t.NT % 16 || !c->rexp) return false;
     const int nout = L.n[l];
     const i64 nin = L.dim[l];
     if (L.N % 2 || nout % 2 || nout > 160) return false;
@@ -503,17 +627,23 @@ bool tc64p_usable(const scalit_ctx *c, int l)
     return true;
 }
 
-int tc64p_scales(const scalit_ctx *c, const double *X, int nvec, const int *gate, cudaStream_t s, const int *vgate,
-                 int vstride)
+int tc64p_vectors_max() { return kQRexpVec; }
+
+// The row exponents of level l's rows for nvec vectors of X.
+int tc64p_rowexp(const scalit_ctx *c, int l, const double *X, int nvec, const int *gate, cudaStream_t s,
+                 const int *vgate, int vstride)
 {
-    if (nvec > kQMaxVec) { set_error("more than %d vectors in one FP64 tensor-core launch", kQMaxVec); return SCALIT_EINVAL; }
-    if (reinterpret_cast<uintptr_t>(X) & 15) { set_error("FP64 tensor-core operand not 16-byte aligned"); return SCALIT_EINVAL; }
-    SC_CUDA(cudaMemsetAsync(c->xmax64, 0, sizeof(unsigned long long) * nvec, s));
-    const i64 n2 = c->L.N / 2;
-    int bx = (int)((n2 + 255) / 256);
-    const int cap = 152 * 8 / (nvec < 8 ? nvec : 8) + 1;
-    if (bx > cap) bx = cap;
-    absmax64_kernel<<<dim3(bx, nvec), 256, 0, s>>>(X, c->L.N, c->L.N, c->xmax64, gate, vgate, vstride);
+    const Layout &L = c->L;
+    if (nvec > kQRexpVec) { set_error("more than %d vectors in one FP64 tensor-core launch", kQRexpVec); return SCALIT_EINVAL; }
+    const int nout = L.n[l];
+    const i64 nin = L.dim[l], blk = L.blk[l];
+    const i64 M = nin == 1 ? blk : nin * blk;
+    const i64 Mi = nin == 1 ? blk : nin, s1 = nin == 1 ? nout : 1, s2 = nin == 1 ? 0 : nin * nout;
+    const i64 a_sk = nin == 1 ? 1 : nin;
+    const i64 rows = M * nvec;
+    const i64 threads = a_sk == 1 ? rows * 32 : rows;
+    rowexp_kernel<<<(unsigned)((threads + 255) / 256), 256, 0, s>>>(X, L.N, (int)M, nout, Mi, s1, s2, a_sk, nvec,
+                                                                    c->rexp + c->rexp_off[l], gate, vgate, vstride);
     SC_CHECK_LAUNCH();
     return 0;
 }
@@ -529,7 +659,7 @@ int tc64p_level_apply(const scalit_ctx *c, int l, const double *X, double *Y, in
         set_error("persistent FP64 tensor-core operands not 16-byte aligned");
         return SCALIT_EINVAL;
     }
-    if (nvec > kQMaxVec) { set_error("more than %d vectors in one persistent launch", kQMaxVec); return SCALIT_EINVAL; }
+    if (nvec > kQRexpVec) { set_error("more than %d vectors in one persistent launch", kQRexpVec); return SCALIT_EINVAL; }
     const int nout = L.n[l];
     const i64 nin = L.dim[l], blk = L.blk[l], N = L.N;
     Tc64pArgs g{};
@@ -554,13 +684,13 @@ int tc64p_level_apply(const scalit_ctx *c, int l, const double *X, double *Y, in
     g.gate = gate; g.err = c->tc_err;
     g.bdig = t.dig;
     g.bexp = t.exps;
-    g.xmax = c->xmax64;
+    g.rexp = c->rexp + c->rexp_off[l];
     g.tstore = (g.c_sn == 1 && !accumulate && !diagV) ? 1 : 0;
 
     // the grid operand: [vector][row][k] boxes of 16 k x 128 rows (128-byte
     // swizzle) or [vector][block][k][point] boxes of 32 points x 16 k; the
     // level-1 output for TMA stores: [vector][row][n] boxes of 8 n x 32 rows
-    CUtensorMap tmA, tmC;
+    CUtensorMap tmA, tmC, tmV, tmX;
     int rc;
     if (nin == 1) {
         const cuuint64_t dims[3] = {(cuuint64_t)nout, (cuuint64_t)blk, (cuuint64_t)nvec};
@@ -576,21 +706,31 @@ int tc64p_level_apply(const scalit_ctx *c, int l, const double *X, double *Y, in
         const cuuint64_t str[3] = {(cuuint64_t)nin * 8, (cuuint64_t)nin * nout * 8, (cuuint64_t)N * 8};
         const cuuint32_t box[4] = {32, 16, 1, 1};
         rc = tma_encode(&tmA, X, true, 4, dims, str, box, CU_TENSOR_MAP_SWIZZLE_NONE);
+        // the epilogue's operands in 32-point x 8-column boxes: the output (loaded
+        // to accumulate, stored back), X and V (without the vector dimension)
+        const cuuint32_t boxe[4] = {32, 8, 1, 1};
+        if (!rc) rc = tma_encode(&tmC, Y, true, 4, dims, str, boxe, CU_TENSOR_MAP_SWIZZLE_NONE);
+        if (!rc && diagV) rc = tma_encode(&tmX, X, true, 4, dims, str, boxe, CU_TENSOR_MAP_SWIZZLE_NONE);
+        if (!rc && diagV) rc = tma_encode(&tmV, diagV, true, 3, dims, str, boxe, CU_TENSOR_MAP_SWIZZLE_NONE);
+        g.ering = q_ring(diagV != nullptr, &g.echunk);
+        if (g.ering < 2) { set_error("level %d: no room for the epilogue ring", l + 1); return SCALIT_EUNSUP; }
     }
     if (rc) return rc;
-    if (!g.tstore) tmC = tmA;
+    if (nin == 1 && !g.tstore) tmC = tmA;
+    if (!(nin > 1 && diagV)) { tmV = tmA; tmX = tmA; }
 
     static int sms = 0, configured = -1;
     int dev = 0;
     cudaGetDevice(&dev);
     if (configured != dev) {
         SC_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
-        SC_CUDA(cudaFuncSetAttribute(tc64p_level_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                     (int)q_smem_bytes()));
+        SC_CUDA(cudaFuncSetAttribute(tc64p_level_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kQMaxSmem));
         configured = dev;
     }
     const int grid = (int)(tiles < sms ? tiles : sms);
-    tc64p_level_kernel<<<grid, kQThreads, q_smem_bytes(), s>>>(g, tmA, tmC);
+    const size_t smem = q_smem_bytes((size_t)g.ering * g.echunk);
+    if (smem > (size_t)kQMaxSmem) { set_error("persistent FP64 tile too large"); return SCALIT_EUNSUP; }
+    tc64p_level_kernel<<<grid, kQThreads, smem, s>>>(g, tmA, tmC, tmV, tmX);
     SC_CHECK_LAUNCH();
     return 0;
 }
