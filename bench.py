@@ -673,7 +673,8 @@ def run_ours(args):
             "osb_build": {"seconds": build_s, "levels_s": build_levels},
             "e2e": {"value": e2e_value, "unit": "H*X apps/s",
                     "h2d_bytes_per_step": int(nvec * N * 8), "d2h_bytes_per_step": int(nvec * N * 8)},
-            "gpu_launches": args.steps * len(p.sizes),
+            # per level: the row-exponent pass and the level product
+            "gpu_launches": args.steps * 2 * len(p.sizes),
             "clocks": clk.summary(),
         }
         if base is not None:

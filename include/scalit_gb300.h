@@ -254,6 +254,22 @@ int scalit_set_absorbing(scalit_ctx *ctx, const double *APP, const double *APR);
  * unknown codes act as TA1, as the reference's default does). */
 int scalit_hx_cx(scalit_ctx *ctx, int ntype, int nvec, const double *X, double *Y);
 int scalit_hx_cx_device(scalit_ctx *ctx, int ntype, int nvec, const double *dX, double *dY);
+/* The complex-Hamiltonian job (sCX; loadH0 / loadInitData with H0CX, DEPCX,
+ * OUTHCX: osb.io.h:49-60, osb.init.h:109-125): complex level matrices H0CX
+ * (the concatenation of H0's layout, interleaved COMPLEX*16), complex
+ * dependent-level factors DEPCX (may be null) and complex outer per-point
+ * matrices OUTHCX (sNDVR; else null), real RES.  Loads their real parts as
+ * scalit_load does and keeps the imaginary parts, after which every complex
+ * form (scalit_hx_cx, QMR_CX, the complex PISTs, the CRP) applies MYHX_CX
+ * (osb.hxcx.h:191-261, H1X_XYZ_CX / H1X_DEP_CX / H3X_CX: hpx_cx.f90:6-34,
+ * matrix_cx.f90:97-208): Y = D X + sum_level H_level X with complex H_level.
+ * The OSB preconditioner is built from the real parts (the reference's
+ * HosbDiagDX rotates the stacked real and imaginary parts of HOSBCX; not
+ * provided), which changes the inner solves' convergence, not their
+ * solutions.  The real entry points (scalit_hx, scalit_qmr, scalit_pist) see
+ * the real parts. */
+int scalit_load_cx(scalit_ctx *ctx, const double *H0CX, const double *RES, const double *DEPCX,
+                   const double *OUTHCX);
 /* MYPX_DX (src/iterate/module/osb.mypxdx.h): V^T of every level, the kernel
  * 1/(EIG0 - E0 + sign i A) (E0 = 0 for TA0, TAAP0, TMAP0; TOSBD1 clamps
  * |EIG0 - E0| <= DE to +-DE; TOSBD2 uses alpha + (1 + beta)(EIG0 - E0) on both

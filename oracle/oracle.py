@@ -591,15 +591,69 @@ def cx_terms(ntype):
     return _CX_DIAG.get(int(ntype), (True, 0, None))
 
 
+def cx_levels(sizes, dep, ndvr, H0CX, DEPCX, OUTHCX, X):
+    """The level sum of MYHX_CX (osb.hxcx.h:244-260) with complex level
+    matrices: H1X_XYZ_CX / H1X_DEP_CX (hpx_cx.f90:6-34) through H1X_CX /
+    H2X_CX (matrix_cx.f90:97-112, 144-159), and H3X_CX (matrix_cx.f90:194-208)
+    for the outer per-point layer when sNDVR; in the reference's loop order
+    (j = 1..NOUT accumulated per output column i)."""
+    sizes = tuple(int(n) for n in sizes)
+    nlev = len(sizes)
+    N = int(np.prod(sizes))
+    X = np.asarray(X, dtype=np.complex128)
+    Y = np.zeros(N, dtype=np.complex128)
+    h0 = 0
+    dp = 0
+    for l, nout in enumerate(sizes):
+        nin = int(np.prod(sizes[:l], dtype=np.int64))
+        blk = int(np.prod(sizes[l + 1:], dtype=np.int64))
+        Xl = X.reshape((nin, nout, blk), order="F")
+        T = np.zeros((nin, nout, blk), dtype=np.complex128)
+        if ndvr and l == nlev - 1:
+            A = np.asarray(OUTHCX, dtype=np.complex128).reshape((nin, nout, nout), order="F")
+            for i in range(nout):
+                acc = A[:, i, 0] * Xl[:, 0, 0]
+                for j in range(1, nout):
+                    acc = acc + A[:, i, j] * Xl[:, j, 0]
+                T[:, i, 0] = acc
+        else:
+            H = np.asarray(H0CX[h0:h0 + nout * nout], dtype=np.complex128).reshape((nout, nout), order="F")
+            h0 += nout * nout
+            if dep[l]:
+                cor = np.asarray(DEPCX[dp:dp + nin], dtype=np.complex128)
+                dp += nin
+            for b in range(blk):
+                for i in range(nout):
+                    if dep[l]:
+                        acc = H[i, 0] * cor * Xl[:, 0, b]
+                        for j in range(1, nout):
+                            acc = acc + H[i, j] * cor * Xl[:, j, b]
+                    else:
+                        acc = H[i, 0] * Xl[:, 0, b]
+                        for j in range(1, nout):
+                            acc = acc + H[i, j] * Xl[:, j, b]
+                    T[:, i, b] = acc
+        Y = Y + T.reshape(N, order="F")
+    return Y
+
+
 class CxOperator:
     """The real operator with absorbing potentials: AP = APP (JOB_RES1/2,
-    APR = 0) or APP + APR (JOB_CRP) (loadInitData, osb.io.h:18-30,92-112)."""
+    APR = 0) or APP + APR (JOB_CRP) (loadInitData, osb.io.h:18-30,92-112).
+    With set_complex_h0 the level matrices (and DEP, OUTH) are complex: the
+    complex-Hamiltonian job (sCX)."""
 
     def __init__(self, op, APP, APR=None):
         self.op = op
         self.APP = _f64(APP)
         self.APR = np.zeros_like(self.APP) if APR is None else _f64(APR)
         self.AP = self.APP + self.APR if APR is not None else self.APP.copy()
+        self.cxh = None
+
+    def set_complex_h0(self, H0CX, DEPCX=None, OUTHCX=None):
+        self.cxh = (np.asarray(H0CX, dtype=np.complex128),
+                    None if DEPCX is None else np.asarray(DEPCX, dtype=np.complex128),
+                    None if OUTHCX is None else np.asarray(OUTHCX, dtype=np.complex128))
 
     def _absorb(self, which):
         return {"AP": self.AP, "APP": self.APP, "APR": self.APR}[which]
@@ -610,7 +664,13 @@ class CxOperator:
         use_e0, sign, which = cx_terms(ntype)
         X = np.asarray(X, dtype=np.complex128)
         nt = 1 if use_e0 else 0
-        Y = self.op.hx(X.real.copy(), nt) + 1j * self.op.hx(X.imag.copy(), nt)
+        if self.cxh is not None:
+            # MYHX_CX (osb.hxcx.h:191-261): the real diagonal, then the complex levels
+            op = self.op
+            Y = (op.RES - (op.E0 if use_e0 else 0.0)) * X
+            Y = Y + cx_levels(op.sizes, op.dep, op.ndvr, self.cxh[0], self.cxh[1], self.cxh[2], X)
+        else:
+            Y = self.op.hx(X.real.copy(), nt) + 1j * self.op.hx(X.imag.copy(), nt)
         if sign:
             Y = Y + 1j * sign * self._absorb(which) * X
         return Y

@@ -57,6 +57,7 @@ SIGNATURES = {
     "scalit_build_osbw": (C.c_int, [_vp, C.c_double, C.c_int, _dp, C.c_int, _ip]),
     "scalit_set_absorbing": (C.c_int, [_vp, _dp, _dp]),
     "scalit_hx_cx": (C.c_int, [_vp, C.c_int, C.c_int, _dp, _dp]),
+    "scalit_load_cx": (C.c_int, [_vp, _dp, _dp, _dp, _dp]),
     "scalit_hx_cx_device": (C.c_int, [_vp, C.c_int, C.c_int, _vp, _vp]),
     "scalit_px_cx": (C.c_int, [_vp, C.c_int, C.c_int, _dp, _dp]),
     "scalit_px_cx_device": (C.c_int, [_vp, C.c_int, C.c_int, _vp, _vp]),
@@ -352,6 +353,16 @@ class Context:
         zf, of = Z.view(np.float64), out.view(np.float64)
         _check(fn(self.h, int(ntype), nvec, _p(zf), _p(of)))
         return out
+
+    def load_cx(self, H0CX, RES, DEPCX=None, OUTHCX=None):
+        """The complex-Hamiltonian job (sCX): complex level matrices, DEP
+        factors and outer per-point matrices, real RES."""
+        def cx(a):
+            return None if a is None else np.ascontiguousarray(np.asarray(a, dtype=np.complex128)).view(np.float64)
+        h, d, o = cx(H0CX), cx(DEPCX), cx(OUTHCX)
+        res = _f64(RES)
+        _check(self.lib.scalit_load_cx(self.h, _p(h), _p(res), _p(d) if d is not None else None,
+                                       _p(o) if o is not None else None))
 
     def hx_cx(self, X, ntype=TAAP):
         """MYHX_DX on complex vectors (N or nvec x N)."""

@@ -171,7 +171,7 @@ void scalit_destroy(scalit_ctx *c)
     if (c->tc_err) cudaFree(c->tc_err);
     if (c->rexp) cudaFree(c->rexp);
     osbw_free(c);
-    double *aptrs[] = {c->APP, c->APR, c->AP};
+    double *aptrs[] = {c->APP, c->APR, c->AP, c->H0i, c->DEPi, c->OUTHi};
     for (double *p : aptrs) if (p) cudaFree(p);
     for (int i = 0; i < 2; ++i) if (c->qg[i].exec) cudaGraphExecDestroy(c->qg[i].exec);
     if (c->red_counter) cudaFree(c->red_counter);
@@ -244,6 +244,7 @@ int scalit_load(scalit_ctx *c, const double *H0, const double *RES, const double
     if (!RES) { set_error("RES is required"); return SCALIT_EINVAL; }
     if (L.deplen > 0 && !DEP) { set_error("DEP is required: a level depends on the coordinates"); return SCALIT_EINVAL; }
     if (L.outhlen > 0 && !OUTH) { set_error("OUTH is required when the outer layer is per point"); return SCALIT_EINVAL; }
+    c->cxh = false;   // a complex Hamiltonian's imaginary parts apply again only through scalit_load_cx
     if (!all_finite(H0, L.h0len) || !all_finite(RES, L.N) || (L.deplen && !all_finite(DEP, L.deplen)) ||
         (L.outhlen && !all_finite(OUTH, L.outhlen))) {
         set_error("non-finite value in the Hamiltonian input");

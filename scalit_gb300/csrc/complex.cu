@@ -334,7 +334,48 @@ static int cx_window_prepare(scalit_ctx *c, int ntype, double e0)
 }
 
 // -------------------------------------------------------- planar operators --
-// MYHX_DX on a planar complex vector.
+// The imaginary parts of a complex Hamiltonian's levels (sCX), added to the
+// real parts' products: with H = Hr + i Hi, D = Dr + i Di (dependent level)
+// and X = Xr + i Xi,
+//   H X       : Yr += -Hi Xi,                       Yi += Hi Xr
+//   D (H X)   : Yr += -Dr(Hi Xi) - Di(Hr Xi) - Di(Hi Xr),
+//               Yi +=  Dr(Hi Xr) + Di(Hr Xr) - Di(Hi Xi)
+//   outer (sNDVR, per-point A = Ar + i Ai): Yr += -Ai Xi, Yi += Ai Xr
+// each a level product on the FP64 pipe with the given matrix, factors and sign.
+static int hx_cx_imag_terms(const scalit_ctx *c, const double *X, double *Y, cudaStream_t s)
+{
+    const Layout &L = c->L;
+    const i64 N = L.N;
+    const double *Xr = X, *Xi = X + N;
+    double *Yr = Y, *Yi = Y + N;
+    struct Term { const double *H, *D, *O, *x; double *y; double a; };
+    for (int l = 0; l < L.nlev; ++l) {
+        Term terms[6];
+        int nt = 0;
+        if (L.ndvr && l == L.nlev - 1) {
+            terms[nt++] = {c->H0, c->DEP, c->OUTHi, Xi, Yr, -1.0};
+            terms[nt++] = {c->H0, c->DEP, c->OUTHi, Xr, Yi, 1.0};
+        } else if (!L.dep[l]) {
+            terms[nt++] = {c->H0i, c->DEP, c->OUTH, Xi, Yr, -1.0};
+            terms[nt++] = {c->H0i, c->DEP, c->OUTH, Xr, Yi, 1.0};
+        } else {
+            terms[nt++] = {c->H0i, c->DEP, c->OUTH, Xi, Yr, -1.0};
+            terms[nt++] = {c->H0, c->DEPi, c->OUTH, Xi, Yr, -1.0};
+            terms[nt++] = {c->H0i, c->DEPi, c->OUTH, Xr, Yr, -1.0};
+            terms[nt++] = {c->H0i, c->DEP, c->OUTH, Xr, Yi, 1.0};
+            terms[nt++] = {c->H0, c->DEPi, c->OUTH, Xr, Yi, 1.0};
+            terms[nt++] = {c->H0i, c->DEPi, c->OUTH, Xi, Yi, -1.0};
+        }
+        for (int i = 0; i < nt; ++i) {
+            int rc = level_apply<double>(c, l, terms[i].H, terms[i].D, terms[i].O, terms[i].x, terms[i].y,
+                                         /*accumulate=*/1, nullptr, 0.0, terms[i].a, nullptr, s);
+            if (rc) return rc;
+        }
+    }
+    return 0;
+}
+
+// MYHX_DX (MYHX_CX with a complex Hamiltonian) on a planar complex vector.
 static int hx_cx_planar(const scalit_ctx *c, int ntype, const double *X, double *Y, cudaStream_t s)
 {
     CxTerms t;
@@ -342,6 +383,10 @@ static int hx_cx_planar(const scalit_ctx *c, int ntype, const double *X, double 
     if (rc) return rc;
     rc = hx_batch<double>(c, X, Y, 2, t.use_e0 ? c->E0 : 0.0, 1.0, nullptr, s);
     if (rc) return rc;
+    if (c->cxh) {
+        rc = hx_cx_imag_terms(c, X, Y, s);
+        if (rc) return rc;
+    }
     if (t.sign) {
         cx_absorb_kernel<<<cgrid(c->L.N), kT, 0, s>>>(c->L.N, X, Y, t.A, (double)t.sign);
         SC_CHECK_LAUNCH();
@@ -1139,6 +1184,47 @@ int scalit_set_absorbing(scalit_ctx *c, const double *APP, const double *APR)
     else SC_CUDA(cudaMemsetAsync(c->APR, 0, sizeof(double) * (size_t)N, c->stream));
     SC_CUDA(cudaMemcpyAsync(c->AP, ap.data(), sizeof(double) * (size_t)N, cudaMemcpyHostToDevice, c->stream));
     SC_CUDA(cudaStreamSynchronize(c->stream));
+    return 0;
+}
+
+int scalit_load_cx(scalit_ctx *c, const double *H0CX, const double *RES, const double *DEPCX, const double *OUTHCX)
+{
+    CX_CTX_CHECK(c);
+    if (!H0CX || !RES) { set_error("H0CX and RES are required"); return SCALIT_EINVAL; }
+    const Layout &L = c->L;
+    bool anydep = false;
+    for (int l = 0; l < L.nlev; ++l) anydep = anydep || L.dep[l];
+    if (anydep && !DEPCX) { set_error("a dependent level needs DEPCX"); return SCALIT_EINVAL; }
+    if (L.ndvr && !OUTHCX) { set_error("sNDVR needs OUTHCX"); return SCALIT_EINVAL; }
+    auto split = [](const double *z, i64 n, std::vector<double> &re, std::vector<double> &im) {
+        re.resize((size_t)n);
+        im.resize((size_t)n);
+        for (i64 i = 0; i < n; ++i) { re[(size_t)i] = z[2 * i]; im[(size_t)i] = z[2 * i + 1]; }
+    };
+    std::vector<double> h0r, h0i, dr, di, orr, oi;
+    split(H0CX, L.h0len, h0r, h0i);
+    if (anydep) split(DEPCX, L.deplen, dr, di);
+    if (L.ndvr) split(OUTHCX, L.outhlen, orr, oi);
+    for (double v : h0i) if (!std::isfinite(v)) { set_error("non-finite H0CX"); return SCALIT_ENONFINITE; }
+    for (double v : di) if (!std::isfinite(v)) { set_error("non-finite DEPCX"); return SCALIT_ENONFINITE; }
+    for (double v : oi) if (!std::isfinite(v)) { set_error("non-finite OUTHCX"); return SCALIT_ENONFINITE; }
+    c->cxh = false;
+    int rc = scalit_load(c, h0r.data(), RES, anydep ? dr.data() : nullptr, L.ndvr ? orr.data() : nullptr);
+    if (rc) return rc;
+    auto up = [&](double **d, const std::vector<double> &h) -> int {
+        if (*d) { cudaFree(*d); *d = nullptr; }
+        if (h.empty()) return 0;
+        SC_CUDA(cudaMalloc(d, sizeof(double) * h.size()));
+        SC_CUDA(cudaMemcpyAsync(*d, h.data(), sizeof(double) * h.size(), cudaMemcpyHostToDevice, c->stream));
+        return 0;
+    };
+    rc = up(&c->H0i, h0i);
+    if (!rc) rc = up(&c->DEPi, di);
+    if (!rc) rc = up(&c->OUTHi, oi);
+    if (rc) return rc;
+    SC_CUDA(cudaStreamSynchronize(c->stream));
+    c->cxh = true;
+    c->gen++;
     return 0;
 }
 

@@ -96,6 +96,10 @@ struct scalit_ctx {
     long long osbw_cx_serial = -1;
     // absorbing potentials of the complex forms: APP, APR and AP = APP + APR
     double *APP = nullptr, *APR = nullptr, *AP = nullptr;
+    // the complex-Hamiltonian job (sCX): imaginary parts of H0CX, DEPCX, OUTHCX
+    // (the real parts are H0, DEP, OUTH); cxh is set while they apply
+    double *H0i = nullptr, *DEPi = nullptr, *OUTHi = nullptr;
+    bool cxh = false;
     // workspace (grown on demand)
     void *work = nullptr;
     size_t work_bytes = 0;

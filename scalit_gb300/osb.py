@@ -23,8 +23,6 @@ class OSB:
     """Module state: the parameter record plus the device context."""
 
     def __init__(self, inp: refio.OSBInput, device: int = 0, precision: int = capi.PREC_FP64):
-        if inp.sCX:
-            raise ValueError("complex Hamiltonians (sCX) are not supported")
         self.inp = inp
         self.device = device
         self.precision = precision
@@ -39,16 +37,25 @@ class OSB:
     # loadInitData (osb.io.h:2-42)
     def load_init_data(self) -> bool:
         inp = self.inp
-        H0 = refio.load_data(inp.H0File, inp.h0_len)
+        # sCX (loadH0 / loadDEP / loadOutH, osb.io.h:46-54,211-238): H0, DEP and
+        # OUTH are COMPLEX*16 records of the same lengths (loadData_CX,
+        # loadDataDir_CX); RES stays real
+        def cxv(a):
+            return a.view(np.complex128)
+        mult = 2 if inp.sCX else 1
+        H0 = refio.load_data(inp.H0File, mult * inp.h0_len)
         OUTH = None
         if inp.sNDVR:
-            OUTH = refio.load_data_dir(inp.OUTHFile, inp.sN[inp.sF - 1] * inp.my_len)
+            OUTH = refio.load_data_dir(inp.OUTHFile, mult * inp.sN[inp.sF - 1] * inp.my_len)
             RES = np.zeros(inp.my_len)
         else:
             RES = refio.load_data_dir(inp.RESFile, inp.my_len)
-        DEP = refio.load_data_dir(inp.DEPFile, inp.dep_len) if inp.dep_len else None
+        DEP = refio.load_data_dir(inp.DEPFile, mult * inp.dep_len) if inp.dep_len else None
         self.ctx = capi.Context(inp.sN[:inp.sF], inp.sDEP[:inp.sF], ndvr=inp.sNDVR, device=self.device)
-        self.ctx.load(H0, RES, DEP, OUTH)
+        if inp.sCX:
+            self.ctx.load_cx(cxv(H0), RES, None if DEP is None else cxv(DEP), None if OUTH is None else cxv(OUTH))
+        else:
+            self.ctx.load(H0, RES, DEP, OUTH)
         # absorbing potentials (osb.io.h:18-30): APP for the resonance jobs, APP and APR for CRP
         if inp.sJOB in (refio.JOB_RES1, refio.JOB_RES2):
             self.ctx.set_absorbing(refio.load_data_dir(inp.APPFile, inp.my_len))

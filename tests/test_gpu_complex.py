@@ -299,3 +299,128 @@ def test_pist_cx_conjugate_levels(lib, orc, case):
         st, eig, res = ctx.pist_cx(x0, 4, e0, 1e-11, 200, qmrmax=1000, qmrtol=1e-12, conjugate=True)
     assert st > 0
     np.testing.assert_allclose(eig, want, atol=1e-8)
+
+
+def _cx_hamiltonian(p, seed):
+    rng = np.random.default_rng(seed)
+    parts = []
+    for l, n in enumerate(p.sizes):
+        K = p.level_matrix(l + 1)
+        S = rng.standard_normal((n, n)) * 1e-4
+        parts.append((K + 1j * (S + S.T)).ravel(order="F"))
+    return np.concatenate(parts), p.DEP * (1.0 + 1j * rng.uniform(-0.05, 0.05, p.DEP.size))
+
+
+@pytest.mark.parametrize("sizes", [(12, 10, 8), (32, 24, 20)])
+def test_complex_hamiltonian_hx(lib, orc, sizes):
+    """The complex-Hamiltonian job (sCX): MYHX_CX with complex level matrices
+    and complex DEP (osb.hxcx.h:191-261) against the oracle, 1e-12, for the
+    plain, shifted and absorbing forms; the real entry points see the real
+    parts, and a real load drops the imaginary ones."""
+    p = hm.build_problem(hm.Grid3(*sizes), hm.PES())
+    e0 = float(p.RES.min()) + 1e-3
+    ref = orc.Operator.from_problem(p, E0=e0)
+    app = np.random.default_rng(5).uniform(0.0, 2e-3, p.N)
+    cx = orc.CxOperator(ref, app)
+    H0CX, DEPCX = _cx_hamiltonian(p, 6)
+    cx.set_complex_h0(H0CX, DEPCX)
+    X = cvec(np.random.default_rng(7), (2, p.N))
+    with capi.Context(p.sizes, p.dep) as ctx:
+        ctx.load_cx(H0CX, p.RES, DEPCX)
+        ctx.set_shift(e0)
+        ctx.set_absorbing(app)
+        for ntype in (capi.TA0, capi.TA1, capi.TMAP):
+            Y = ctx.hx_cx(X, ntype)
+            for v in range(2):
+                assert rel(Y[v], cx.hx(X[v], ntype)) < 1e-12, (ntype, v)
+        # the real H*X of the same context: the real parts
+        xr = X[0].real.copy()
+        real = orc.Operator(p.sizes, p.dep, H0CX.real, p.RES, DEPCX.real, E0=e0)
+        assert rel(ctx.hx(xr, capi.TA1), real.hx(xr, 1)) < 1e-12
+        ctx.load(p.H0, p.RES, p.DEP)
+        ctx.set_absorbing(app)
+        plain = orc.CxOperator(ref, app)
+        assert rel(ctx.hx_cx(X[0], capi.TA1), plain.hx(X[0], capi.TA1)) < 1e-12
+
+
+def test_complex_hamiltonian_qmr_and_pist(lib, orc):
+    """QMR_CX and the complex symmetric PIST on a complex Hamiltonian: the
+    solution of (H - E0 - i AP) x = b against the dense solve, and the levels
+    of H - i AP nearest E0 against the dense eigenvalues (the preconditioner
+    is built from the real parts: it sets the convergence, not the result)."""
+    p = hm.build_problem(hm.Grid3(12, 10, 8), hm.PES())
+    H0CX, DEPCX = _cx_hamiltonian(p, 8)
+    app = np.random.default_rng(9).uniform(0.0, 2e-3, p.N)
+    sizes, N = p.sizes, p.N
+    H = np.diag(p.RES).astype(np.complex128)
+    h0, dp = 0, 0
+    for l, n in enumerate(sizes):
+        nin = int(np.prod(sizes[:l], dtype=np.int64))
+        blk = int(np.prod(sizes[l + 1:], dtype=np.int64))
+        Hl = H0CX[h0:h0 + n * n].reshape((n, n), order="F")
+        h0 += n * n
+        D = np.diag(DEPCX[dp:dp + nin]) if p.dep[l] else np.eye(nin)
+        dp += nin if p.dep[l] else 0
+        H = H + np.kron(np.eye(blk), np.kron(Hl, D))
+    Hm = H - 1j * np.diag(app)
+    ev = np.linalg.eigvals(Hm)
+    e0 = float(np.sort(ev.real)[12]) + 3e-4
+    b = cvec(np.random.default_rng(10), N)
+    with capi.Context(p.sizes, p.dep) as ctx:
+        ctx.load_cx(H0CX, p.RES, DEPCX)
+        ctx.set_shift(e0)
+        ctx.set_absorbing(app)
+        ctx.build_osb(20, 1e-4)
+        code, x, res = ctx.qmr_cx(b, 2000, 1e-10, ntype=capi.TMAP)
+        assert code > 0
+        x_dense = np.linalg.solve(Hm - e0 * np.eye(N), b)
+        assert rel(x, x_dense) < 1e-7
+        x0 = np.random.default_rng(11).random(N) + 1j * np.random.default_rng(12).random(N)
+        st, eig, res = ctx.pist_cx(x0, 4, e0, 1e-11, 200, qmrmax=1000, qmrtol=1e-12)
+    assert st > 0
+    want = ev[np.argsort(np.abs(ev.real - e0))[:4]]
+    want = want[np.argsort(want.real)]
+    np.testing.assert_allclose(np.sort_complex(eig), np.sort_complex(want), atol=1e-8)
+
+
+def test_driver_complex_hamiltonian_job(lib, tmp_path):
+    """The driver flow with sCX: H0 and DEP as COMPLEX*16 files (loadData_CX,
+    loadDataDir_CX; osb.io.h:46-54,211-222), JOB_RES1: the levels of
+    H_complex - i AP nearest E0 against the dense eigenvalues."""
+    import dataclasses
+    from scalit_gb300 import osb, refio
+    p = hm.build_problem(hm.Grid3(12, 10, 8), hm.PES())
+    H0CX, DEPCX = _cx_hamiltonian(p, 13)
+    app = np.random.default_rng(14).uniform(0.0, 2e-3, p.N)
+    sizes = p.sizes
+    H = np.diag(p.RES).astype(np.complex128)
+    h0, dp = 0, 0
+    for l, n in enumerate(sizes):
+        nin = int(np.prod(sizes[:l], dtype=np.int64))
+        blk = int(np.prod(sizes[l + 1:], dtype=np.int64))
+        Hl = H0CX[h0:h0 + n * n].reshape((n, n), order="F")
+        h0 += n * n
+        D = np.diag(DEPCX[dp:dp + nin]) if p.dep[l] else np.eye(nin)
+        dp += nin if p.dep[l] else 0
+        H = H + np.kron(np.eye(blk), np.kron(Hl, D))
+    ev = np.linalg.eigvals(H - 1j * np.diag(app))
+    e0 = float(np.sort(ev.real)[12]) + 3e-4
+    refio.save_data_dir(tmp_path / "APP.dat", app)
+    inp = refio.OSBInput(sJOB=refio.JOB_RES1, sAP=True, sBJ=(20, 1e-4), sQMR=(1000, 1e-12),
+                         sConv=(e0, 1e-11, 0, 5, 200, 4, 1), sOSBW=(e0, 0.0, 0.0, 0),
+                         APPFile=str(tmp_path / "APP.dat"))
+    inp = refio.write_problem_files(p, tmp_path, inp)
+    refio.save_data(inp.H0File, np.ascontiguousarray(H0CX).view(np.float64))
+    refio.save_data_dir(inp.DEPFile, np.ascontiguousarray(DEPCX).view(np.float64))
+    inp = dataclasses.replace(inp, sCX=True)
+    (tmp_path / "input.txt").write_text(refio.write_input(inp))
+    o = osb.OSB.read((tmp_path / "input.txt").read_text())
+    assert o.inp.sCX
+    assert o.load_init_data()
+    o.prog_diag(log=None)
+    st, eig, res, _ = o.prog_pist_eig(log=None)
+    o.close()
+    want = ev[np.argsort(np.abs(ev.real - e0))[:4]]
+    want = want[np.argsort(want.real)]
+    assert st > 0
+    np.testing.assert_allclose(eig, want, atol=1e-7)

@@ -221,3 +221,55 @@ def test_pist_cx_conjugate_dense(orc):
                                     conj=True)
     assert st > 0
     np.testing.assert_allclose(eig, want, atol=1e-9)
+
+
+def _complex_hamiltonian(p, seed):
+    """Complex symmetric level matrices K_l + i S_l (small symmetric S_l),
+    complex DEP factors, for the complex-Hamiltonian job (sCX)."""
+    rng = np.random.default_rng(seed)
+    parts = []
+    for l, n in enumerate(p.sizes):
+        K = p.level_matrix(l + 1)
+        S = rng.standard_normal((n, n)) * 1e-4
+        parts.append((K + 1j * (S + S.T)).ravel(order="F"))
+    H0CX = np.concatenate(parts)
+    DEPCX = p.DEP * (1.0 + 1j * rng.uniform(-0.05, 0.05, p.DEP.size))
+    return H0CX, DEPCX
+
+
+def _dense_cx(p, H0CX, DEPCX, RES, shift=0.0):
+    sizes = p.sizes
+    N = int(np.prod(sizes))
+    H = np.diag(RES - shift).astype(np.complex128)
+    h0, dp = 0, 0
+    for l, n in enumerate(sizes):
+        nin = int(np.prod(sizes[:l], dtype=np.int64))
+        blk = int(np.prod(sizes[l + 1:], dtype=np.int64))
+        Hl = H0CX[h0:h0 + n * n].reshape((n, n), order="F")
+        h0 += n * n
+        if p.dep[l]:
+            D = np.diag(DEPCX[dp:dp + nin])
+            dp += nin
+        else:
+            D = np.eye(nin)
+        H = H + np.kron(np.eye(blk), np.kron(Hl, D))
+    assert H.shape == (N, N)
+    return H
+
+
+@pytest.mark.parametrize("ntype", [0, 1, 201])
+def test_cx_hamiltonian_hx_is_dense(orc, ntype):
+    """MYHX_CX (osb.hxcx.h:191-261) with complex level matrices and DEP: the
+    oracle's level sum equals the dense complex Kronecker sum."""
+    p = hm.build_problem(hm.Grid3(6, 5, 4), hm.PES())
+    op = orc.Operator.from_problem(p, E0=1e-3)
+    app = np.random.default_rng(1).uniform(0.0, 2e-3, p.N)
+    cx = orc.CxOperator(op, app)
+    H0CX, DEPCX = _complex_hamiltonian(p, 2)
+    cx.set_complex_h0(H0CX, DEPCX)
+    shift = op.E0 if ntype != 0 else 0.0
+    H = _dense_cx(p, H0CX, DEPCX, p.RES, shift)
+    if ntype == 201:                                   # TMAP: H - i AP - E0
+        H = H - 1j * np.diag(app)
+    x = np.random.default_rng(3).standard_normal(p.N) + 1j * np.random.default_rng(4).standard_normal(p.N)
+    assert rel(cx.hx(x, ntype), H @ x) < 1e-13
