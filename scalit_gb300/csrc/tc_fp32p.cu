@@ -35,10 +35,16 @@
 // (16 k x 128 rows, 64-byte swizzle) of the view [vector][row][k]; the
 // outputs, contiguous along n, leave through a 32 x 16 stage per epilogue
 // warp, stored by TMA in the same swizzle.  Otherwise (the grid point index
-// fastest within blocks of Mi points, Mi % 32 == 0) the slab is four boxes
-// of 32 points x 16 k of the view [vector][block][k][point], and a warp's 32
-// TMEM lanes are 32 consecutive grid points of one output column, so its
-// loads and stores are coalesced as they come.
+// fastest within blocks of Mi points, Mi % 32 == 0) a tile's 128 rows are
+// four groups of 32 points; the groups of one block form a run, moved as one
+// box of 32 points x w groups x 16 k of the view
+// [vector][block][k][group][point] (one box per tile when the blocks hold
+// whole tiles, two when a tile straddles a block boundary: each TMA
+// instruction costs its issuing thread about 0.2 us, so fewer and larger
+// boxes keep the load lanes ahead), and a warp's 32 TMEM lanes are 32
+// consecutive grid points of one output column.  The epilogue writes its
+// results over the accumulated output's place in the ring; once the four
+// quarters of a chunk are written, one lane stores the chunk's runs.
 //
 // Every mbarrier wait is bounded; an expired wait raises a shared abort flag
 // after which no role waits again, the load and MMA lanes stop issuing and
@@ -92,6 +98,15 @@ struct Tc32pArgs {
     int tstore;                // outputs contiguous along n, nothing to add: TMA stores
     int ering, echunk;         // points fastest: epilogue operand ring slots and bytes per slot
     int nslots;                // FP32 slab slots
+    int gp, nblk;              // points fastest: groups of 32 points per block, blocks per vector
+};
+
+// Tensor maps of one launch.  Rows along k: a[0] (the grid operand) and c[0]
+// (level-1 output stores).  Points fastest: entry w - 1 holds boxes of
+// 32 points x w groups of 32 points x 16 k (or n), w = 1..4, for the grid
+// operand (a), the output (c) and V (v).
+struct Tc32pMaps {
+    CUtensorMap a[4], c[4], v[4];
 };
 
 // Shared memory: B, slab slots, plane slots, the epilogue region (level 1:
@@ -100,7 +115,7 @@ struct Tc32pArgs {
 static size_t p_fixed_bytes(int NT, int KS, int nslots)
 {
     return (size_t)KS * 2 * NT * 32 + (size_t)nslots * kPSlab + (size_t)kPPlanes * kPPlane + 256 * 4 +
-           (2 * kPSlotsMax + 2 * kPPlanes + 2 * kPERingMax + 6) * 8 + 16;
+           (2 * kPSlotsMax + 2 * kPPlanes + 3 * kPERingMax + 6) * 8 + 16;
 }
 static constexpr size_t kPStageBytes = (size_t)kPEpiWarps * 2 * kPStage * 4;
 
@@ -143,10 +158,44 @@ __device__ __forceinline__ void p_cut2(float x0, float x1, float xs, uint32_t &h
     }
 }
 
+// Points fastest: a tile's 128 rows are the groups of 32 points G0 .. G0 + 3
+// (G0 = first row / 32); the groups that share a block form a run, moved as
+// one box and held in shared memory as [k][w][32] from position pos (in
+// groups).  Run of the tile's group q: its position and width.
+__device__ __forceinline__ void p_run(int G0, int q, int gp, int &pos, int &w)
+{
+    const int gg = (G0 + q) % gp;             // group within its block
+    pos = q > gg ? q - gg : 0;
+    const int gs = gg - (q - pos);            // the run's first group within the block
+    w = min(4 - pos, gp - gs);
+}
+
+// The runs of one tile: a run starts at the tile's first group and at every
+// group that opens a block; on[q] marks a run starting at group q that lies
+// in the vector (blocks past the last are not moved).
+struct PRuns {
+    bool on[4];
+    int w[4], gg[4], c2[4];
+    uint32_t bytes;                           // bytes of one operand's boxes
+};
+
+__device__ __forceinline__ void p_runs(int G0, int gp, int nblk, PRuns &r)
+{
+    r.bytes = 0;
+    #pragma unroll
+    for (int q = 0; q < 4; ++q) {
+        const int Gq = G0 + q, c2 = Gq / gp, gg = Gq - c2 * gp;
+        r.on[q] = (q == 0 || gg == 0) && c2 < nblk;
+        r.w[q] = min(4 - q, gp - gg);
+        r.gg[q] = gg;
+        r.c2[q] = c2;
+        if (r.on[q]) r.bytes += (uint32_t)r.w[q] * 2048u;
+    }
+}
+
 template <bool F16>
 __global__ void __launch_bounds__(kPThreads, 1)
-tc32p_level_kernel(Tc32pArgs g, const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmC,
-                   const __grid_constant__ CUtensorMap tmV)
+tc32p_level_kernel(Tc32pArgs g, const __grid_constant__ Tc32pMaps mp)
 {
     if (g.gate && *g.gate) return;
     extern __shared__ __align__(1024) unsigned char smem[];
@@ -167,7 +216,8 @@ tc32p_level_kernel(Tc32pArgs g, const __grid_constant__ CUtensorMap tmA, const _
     uint64_t *accempty = accfull + 2;
     uint64_t *efull = accempty + 2;
     uint64_t *eempty = efull + kPERingMax;
-    uint64_t *bready = eempty + kPERingMax;
+    uint64_t *sready = eempty + kPERingMax;                     // a chunk's four quarters written
+    uint64_t *bready = sready + kPERingMax;
     uint64_t *drain = bready + 1;                               // products in flight at an abort
     volatile int *abort_flag = reinterpret_cast<volatile int *>(drain + 1);
     uint32_t *tslot = reinterpret_cast<uint32_t *>(drain + 1) + 1;
@@ -183,6 +233,18 @@ tc32p_level_kernel(Tc32pArgs g, const __grid_constant__ CUtensorMap tmA, const _
         return (i64)(m - mq * Mi32) * g.s1 + (i64)mq * g.s2;
     };
     auto vgated = [&](int z) -> bool { return g.vgate && g.vgate[(i64)z * g.vgate_stride]; };
+    // points fastest: the runs of a tile (computed once per tile, so the
+    // lanes that move boxes spend no divisions per box), their bytes, and
+    // the boxes of one operand at k (or n) offset kk
+    auto run_boxes = [&](unsigned char *dst, const PRuns &r, const CUtensorMap *maps, bool vec, int kk, int z,
+                         uint64_t *bar) {
+        #pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            if (!r.on[q]) continue;
+            if (vec) tma_load_5d(dst + q * 2048, &maps[r.w[q] - 1], 0, r.gg[q], kk, r.c2[q], z, bar);
+            else tma_load_4d(dst + q * 2048, &maps[r.w[q] - 1], 0, r.gg[q], kk, r.c2[q], bar);
+        }
+    };
     auto fail = [&]() {
         *abort_flag = 1;
         if (g.err) atomicExch(g.err, 5);
@@ -194,7 +256,11 @@ tc32p_level_kernel(Tc32pArgs g, const __grid_constant__ CUtensorMap tmA, const _
         for (int i = 0; i < S; ++i) { mbar_init(&full[i], 1); mbar_init(&empty[i], kPConv); }
         for (int i = 0; i < kPPlanes; ++i) { mbar_init(&pfull[i], kPConv); mbar_init(&pfree[i], 1); }
         for (int b = 0; b < 2; ++b) { mbar_init(&accfull[b], 1); mbar_init(&accempty[b], 32 * kPEpiWarps); }
-        for (int i = 0; i < kPERingMax; ++i) { mbar_init(&efull[i], 1); mbar_init(&eempty[i], 4); }
+        for (int i = 0; i < kPERingMax; ++i) {
+            mbar_init(&efull[i], 1);
+            mbar_init(&eempty[i], 1);
+            mbar_init(&sready[i], 4);
+        }
         mbar_init(bready, 1);
         mbar_init(drain, 1);
         *abort_flag = 0;
@@ -222,6 +288,17 @@ tc32p_level_kernel(Tc32pArgs g, const __grid_constant__ CUtensorMap tmA, const _
         int ks = 0, it = 0;
         float xs = 1.0f;
         if (F16 && nsteps > 0) xs = p_pow2(p_scale_exp(g.xmax[(int)blockIdx.x / g.mtiles]));
+        // points fastest: this row's place in the slab's runs
+        int coff = 0, kstr = 0;
+        auto crun = [&](int i) {
+            if (kmajor) return;
+            const int tau = (int)blockIdx.x + i * G, z = tau / g.mtiles;
+            int pos, w;
+            p_run(((tau - z * g.mtiles) * kPM) >> 5, row >> 5, g.gp, pos, w);
+            coff = pos * 512 + ((row >> 5) - pos) * 32 + (row & 31);
+            kstr = w * 32;
+        };
+        if (nsteps > 0) crun(0);
         int fs = 0, p = 0;                      // slot and plane of the next step
         uint32_t fph = 0, pphase = 0;
         // two K steps per pass: one fence and one round of arrivals for both
@@ -242,10 +319,10 @@ tc32p_level_kernel(Tc32pArgs g, const __grid_constant__ CUtensorMap tmA, const _
                     x[0] = a.x; x[1] = a.y; x[2] = a.z; x[3] = a.w;
                     x[4] = b.x; x[5] = b.y; x[6] = b.z; x[7] = b.w;
                 } else {
-                    // four boxes [16 k][32 points]
-                    const float *sf = reinterpret_cast<const float *>(st) + (row >> 5) * 512 + (row & 31);
+                    // runs [16 k][w][32 points]
+                    const float *sf = reinterpret_cast<const float *>(st) + coff;
                     #pragma unroll
-                    for (int j = 0; j < 8; ++j) x[j] = sf[(8 * h + j) * 32];
+                    for (int j = 0; j < 8; ++j) x[j] = sf[(8 * h + j) * kstr];
                 }
                 #pragma unroll
                 for (int j = 0; j < 4; ++j) p_cut2<F16>(x[2 * j], x[2 * j + 1], xs, hw[u][j], lw[u][j]);
@@ -255,6 +332,7 @@ tc32p_level_kernel(Tc32pArgs g, const __grid_constant__ CUtensorMap tmA, const _
                     ks = 0;
                     ++it;
                     if (F16 && it < niter) xs = p_pow2(p_scale_exp(g.xmax[((int)blockIdx.x + it * G) / g.mtiles]));
+                    if (it < niter) crun(it);
                 }
             }
             #pragma unroll
@@ -282,17 +360,19 @@ tc32p_level_kernel(Tc32pArgs g, const __grid_constant__ CUtensorMap tmA, const _
         if (lane == 0) {
             int pit = 0, pks = 0, pz = 0, pm0 = 0;
             bool pskip = false;
+            PRuns pr;
             auto ptile = [&]() {
                 const int tau = (int)blockIdx.x + pit * G;
                 pz = tau / g.mtiles;
                 pm0 = (tau - pz * g.mtiles) * kPM;
                 pskip = vgated(pz);
+                if (!kmajor) p_runs(pm0 >> 5, g.gp, g.nblk, pr);
             };
             if (nsteps > 0) ptile();
-            int prod = 0;
+            int prod = 0, sl = 0;
+            uint32_t rnd = 0;                 // parity of the ring round
             for (; prod < nsteps && !*abort_flag; ++prod) {
-                const int sl = prod % S;
-                if (prod >= S && !mbar_wait(&empty[sl], (uint32_t)(((prod / S) - 1) & 1))) {
+                if (prod >= S && !mbar_wait(&empty[sl], rnd ^ 1u)) {
                     fail();
                     break;
                 }
@@ -300,17 +380,15 @@ tc32p_level_kernel(Tc32pArgs g, const __grid_constant__ CUtensorMap tmA, const _
                 if (pskip) {
                     mbar_arrive(&full[sl]);   // a stopped vector: nothing to load
                 } else {
-                    mbar_arrive_expect_tx(&full[sl], (uint32_t)kPSlab);
                     if (kmajor) {
-                        tma_load_3d(dst, &tmA, pks * 16, pm0, pz, &full[sl]);
+                        mbar_arrive_expect_tx(&full[sl], (uint32_t)kPSlab);
+                        tma_load_3d(dst, &mp.a[0], pks * 16, pm0, pz, &full[sl]);
                     } else {
-                        #pragma unroll
-                        for (int j = 0; j < 4; ++j) {
-                            const int m = pm0 + 32 * j;
-                            tma_load_4d(dst + j * 2048, &tmA, m % Mi32, pks * 16, m / Mi32, pz, &full[sl]);
-                        }
+                        mbar_arrive_expect_tx(&full[sl], pr.bytes);
+                        run_boxes(dst, pr, mp.a, true, pks * 16, pz, &full[sl]);
                     }
                 }
+                if (++sl == S) { sl = 0; rnd ^= 1u; }
                 if (++pks == KS) {
                     pks = 0;
                     if (++pit < niter) ptile();
@@ -324,38 +402,37 @@ tc32p_level_kernel(Tc32pArgs g, const __grid_constant__ CUtensorMap tmA, const _
     } else if (warp == kPELoadWarp) {
         // ---------------------------------------- epilogue operands' lane --
         // points fastest: per tile and 16-column chunk, the accumulated output
-        // (and for the diagonal term V and X) as four 32-point boxes each
+        // (and for the diagonal term V and X) as the tile's runs
         if (lane == 0 && g.ering > 0) {
             const int nch = (g.N + 15) / 16;
             const bool dg = g.diagV != nullptr;
             const uint32_t piece = 4 * 2048;
-            int cc = 0;
+            int cc = 0, sl = 0;
+            uint32_t rnd = 0;
+            PRuns er;
             for (int it = 0; it < niter && !*abort_flag; ++it) {
                 const int tau = (int)blockIdx.x + it * G;
                 const int z = tau / g.mtiles, m0 = (tau - z * g.mtiles) * kPM;
                 const bool skip = vgated(z);
+                p_runs(m0 >> 5, g.gp, g.nblk, er);
+                const uint32_t tx = (g.accumulate ? er.bytes : 0u) + (dg ? 2 * er.bytes : 0u);
                 for (int ch = 0; ch < nch; ++ch, ++cc) {
-                    const int sl = cc % g.ering;
-                    if (cc >= g.ering && !mbar_wait(&eempty[sl], (uint32_t)(((cc / g.ering) - 1) & 1))) {
+                    if (cc >= g.ering && !mbar_wait(&eempty[sl], rnd ^ 1u)) {
                         fail();
                         break;
                     }
                     unsigned char *dst = reinterpret_cast<unsigned char *>(stage) + (size_t)sl * g.echunk;
                     if (skip || (!g.accumulate && !dg)) {
                         mbar_arrive(&efull[sl]);
-                        continue;
-                    }
-                    mbar_arrive_expect_tx(&efull[sl], (g.accumulate ? piece : 0u) + (dg ? 2 * piece : 0u));
-                    #pragma unroll
-                    for (int j = 0; j < 4; ++j) {
-                        const int m = m0 + 32 * j;
-                        const int c0 = m % Mi32, c2 = m / Mi32;
-                        if (g.accumulate) tma_load_4d(dst + j * 2048, &tmC, c0, ch * 16, c2, z, &efull[sl]);
+                    } else {
+                        mbar_arrive_expect_tx(&efull[sl], tx);
+                        if (g.accumulate) run_boxes(dst, er, mp.c, true, ch * 16, z, &efull[sl]);
                         if (dg) {
-                            tma_load_3d(dst + piece + j * 2048, &tmV, c0, ch * 16, c2, &efull[sl]);
-                            tma_load_4d(dst + 2 * piece + j * 2048, &tmA, c0, ch * 16, c2, z, &efull[sl]);
+                            run_boxes(dst + piece, er, mp.v, false, ch * 16, z, &efull[sl]);
+                            run_boxes(dst + 2 * piece, er, mp.a, true, ch * 16, z, &efull[sl]);
                         }
                     }
+                    if (++sl == g.ering) { sl = 0; rnd ^= 1u; }
                 }
             }
             // the copies in flight land before the shared memory goes
@@ -452,7 +529,7 @@ tc32p_level_kernel(Tc32pArgs g, const __grid_constant__ CUtensorMap tmA, const _
                         fence_proxy_async_smem();
                         __syncwarp();
                         if (lane == 0 && rows_in) {
-                            tma_store_3d(&tmC, stg, ch * 16, m0 + qd * 32, z);
+                            tma_store_3d(&mp.c[0], stg, ch * 16, m0 + qd * 32, z);
                             asm volatile("cp.async.bulk.commit_group;" ::: "memory");
                         }
                         ++nstore;
@@ -501,26 +578,36 @@ tc32p_level_kernel(Tc32pArgs g, const __grid_constant__ CUtensorMap tmA, const _
                     }
                 } else {
                     // points fastest: per 16-column chunk of this warp's half, the
-                    // operands wait in the ring as [16 n][32 points] per quarter;
-                    // the result overwrites the output's box, which one TMA copy
-                    // stores (points past the vector's last are clipped); the slot
-                    // is released once that copy has read it
+                    // operands wait in the ring as the tile's runs [16 n][w][32
+                    // points]; the result overwrites the output's place and, once
+                    // the four quarters are written, the first quarter's lane 0
+                    // stores the runs (blocks past the last are not stored) and
+                    // releases the slot when the copies have read it
                     const float *cs = binv_s;
-                    const bool rows_in = m0 + qd * 32 < g.M;
+                    const int G0 = m0 >> 5;
+                    int pos, w;
+                    p_run(G0, qd, g.gp, pos, w);
+                    const int ebase = pos * 512 + (qd - pos) * 32 + lane, nstr = w * 32;
+                    PRuns er;
+                    if (qd == 0) p_runs(G0, g.gp, g.nblk, er);
+                    const int cc0 = it * nch, q0 = cc0 / g.ering, r0 = cc0 - q0 * g.ering;
                     for (int ch = hc; ch < nch; ch += 2) {
-                        const int cc = it * nch + ch;
-                        const int sl = cc % g.ering;
+                        // ring slot and round of chunk it * nch + ch
+                        int sl = r0 + ch, rq = q0;
+                        while (sl >= g.ering) { sl -= g.ering; ++rq; }
+                        const uint32_t par = (uint32_t)(rq & 1);
                         float v[16];
                         tmem_ld16(tbase + lane_base + (uint32_t)(b * kPAccCols + ch * 16), v);
-                        bool eok = !*abort_flag && mbar_wait(&efull[sl], (uint32_t)((cc / g.ering) & 1));
+                        bool eok = !*abort_flag && mbar_wait(&efull[sl], par);
                         eok = __all_sync(0xffffffffu, eok);
                         asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
                         if (!eok) { fail(); break; }
-                        float *cb = stage + (size_t)sl * (g.echunk / 4) + qd * 512;
+                        float *cbuf = stage + (size_t)sl * (g.echunk / 4);
+                        float *cb = cbuf + ebase;
                         #pragma unroll
                         for (int j = 0; j < 16; ++j) {
                             const int n = ch * 16 + j;
-                            const int idx = j * 32 + lane;
+                            const int idx = j * nstr;
                             float out = v[j] * (sc * cs[n < 256 ? n : 0]);
                             if (g.accumulate) out += cb[idx];
                             if (Vd) out = fmaf(g.alpha * (cb[2048 + idx] - shift), cb[4096 + idx], out);
@@ -529,26 +616,42 @@ tc32p_level_kernel(Tc32pArgs g, const __grid_constant__ CUtensorMap tmA, const _
                         fence_proxy_async_smem();
                         __syncwarp();
                         if (lane == 0) {
-                            if (rows_in) {
-                                const int mq = m0 + qd * 32;
-                                tma_store_4d(&tmC, cb, mq % Mi32, ch * 16, mq / Mi32, z);
-                                asm volatile("cp.async.bulk.commit_group;" ::: "memory");
-                                asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory");
-                                ++nstore;
+                            mbar_arrive(&sready[sl]);
+                            if (qd == 0) {
+                                if (!mbar_wait(&sready[sl], par)) {
+                                    fail();
+                                } else {
+                                    #pragma unroll
+                                    for (int q = 0; q < 4; ++q) {
+                                        if (!er.on[q]) continue;
+                                        tma_store_5d(&mp.c[er.w[q] - 1], cbuf + q * 512, 0, er.gg[q], ch * 16,
+                                                     er.c2[q], z);
+                                        ++nstore;
+                                    }
+                                    asm volatile("cp.async.bulk.commit_group;" ::: "memory");
+                                    asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory");
+                                    mbar_arrive(&eempty[sl]);
+                                }
                             }
-                            mbar_arrive(&eempty[sl]);
                         }
                         __syncwarp();
+                        if (*abort_flag) break;
                     }
                 }
             } else if (ok && g.ering > 0) {
-                // a stopped vector: its ring chunks are released unread
+                // a stopped vector: its ring chunks are released unread (the
+                // quarters still mark each chunk so the phases stay in step)
+                const int cc0 = it * nch, q0 = cc0 / g.ering, r0 = cc0 - q0 * g.ering;
                 for (int ch = hc; ch < nch; ch += 2) {
-                    const int cc = it * nch + ch;
-                    const int sl = cc % g.ering;
+                    int sl = r0 + ch, rq = q0;
+                    while (sl >= g.ering) { sl -= g.ering; ++rq; }
+                    const uint32_t par = (uint32_t)(rq & 1);
                     if (lane == 0) {
-                        if (mbar_wait(&efull[sl], (uint32_t)((cc / g.ering) & 1))) mbar_arrive(&eempty[sl]);
-                        else fail();
+                        mbar_arrive(&sready[sl]);
+                        if (qd == 0) {
+                            if (mbar_wait(&sready[sl], par) && mbar_wait(&efull[sl], par)) mbar_arrive(&eempty[sl]);
+                            else fail();
+                        }
                     }
                     __syncwarp();
                 }
@@ -710,7 +813,7 @@ bool tc32p_usable(const scalit_ctx *c, int l, bool f16, bool diag)
     const int nout = L.n[l];
     const i64 nin = L.dim[l], N = L.N;
     if (N % 4 || nout % 4) return false;
-    // grid points fastest within blocks of nin: 32-point boxes stay in a block
+    // grid points fastest within blocks of nin: 32-point groups stay in a block
     if (nin > 1 && nin % 32) return false;
     return true;
 }
@@ -815,33 +918,38 @@ int tc32p_level_apply(const scalit_ctx *c, int l, bool f16, const float *X, floa
     g.tstore = (g.c_sn == 1 && !accumulate && !diagV) ? 1 : 0;
 
     // the grid operand: [vector][row][k] boxes of 16 k x 128 rows (64-byte
-    // swizzle) or [vector][block][k][point] boxes of 32 points x 16 k; the
-    // level-1 output for TMA stores: [vector][row][n] boxes of 16 n x 32 rows
-    CUtensorMap tmA, tmC, tmV;
-    int rc;
+    // swizzle), the level-1 output for TMA stores: [vector][row][n] boxes of
+    // 16 n x 32 rows; points fastest: the grid operand, the output (loaded to
+    // accumulate, stored back) and V (no vector dimension) as
+    // [vector][block][k][group][point] boxes of 32 points x w groups x 16 k
+    Tc32pMaps mp;
+    memset(&mp, 0, sizeof(mp));
+    int rc = 0;
     if (nin == 1) {
         const cuuint64_t dims[3] = {(cuuint64_t)nout, (cuuint64_t)blk, (cuuint64_t)nvec};
         const cuuint64_t str[2] = {(cuuint64_t)nout * 4, (cuuint64_t)N * 4};
         const cuuint32_t box[3] = {16, kPM, 1};
-        rc = encode_map(&tmA, X, 3, dims, str, box, CU_TENSOR_MAP_SWIZZLE_64B);
+        rc = encode_map(&mp.a[0], X, 3, dims, str, box, CU_TENSOR_MAP_SWIZZLE_64B);
         if (!rc && g.tstore) {
             const cuuint32_t boxc[3] = {16, 32, 1};
-            rc = encode_map(&tmC, Y, 3, dims, str, boxc, CU_TENSOR_MAP_SWIZZLE_64B);
+            rc = encode_map(&mp.c[0], Y, 3, dims, str, boxc, CU_TENSOR_MAP_SWIZZLE_64B);
         }
     } else {
-        const cuuint64_t dims[4] = {(cuuint64_t)nin, (cuuint64_t)nout, (cuuint64_t)blk, (cuuint64_t)nvec};
-        const cuuint64_t str[3] = {(cuuint64_t)nin * 4, (cuuint64_t)nin * nout * 4, (cuuint64_t)N * 4};
-        const cuuint32_t box[4] = {32, 16, 1, 1};
-        rc = encode_map(&tmA, X, 4, dims, str, box, CU_TENSOR_MAP_SWIZZLE_NONE);
-        // the output (loaded to accumulate, stored back) in the same boxes, V
-        // without the vector dimension
-        if (!rc) rc = encode_map(&tmC, Y, 4, dims, str, box, CU_TENSOR_MAP_SWIZZLE_NONE);
-        if (!rc && diagV) rc = encode_map(&tmV, diagV, 3, dims, str, box, CU_TENSOR_MAP_SWIZZLE_NONE);
+        const i64 gp = nin / 32;
+        g.gp = (int)gp; g.nblk = (int)blk;
+        const cuuint64_t dims[5] = {32, (cuuint64_t)gp, (cuuint64_t)nout, (cuuint64_t)blk, (cuuint64_t)nvec};
+        const cuuint64_t str[4] = {128, (cuuint64_t)nin * 4, (cuuint64_t)nin * nout * 4, (cuuint64_t)N * 4};
+        // every run is 4 groups wide when the blocks hold whole tiles
+        const int wmin = (gp % 4 == 0) ? 4 : 1, wmax = gp < 4 ? (int)gp : 4;
+        for (int w = wmin; w <= wmax && !rc; ++w) {
+            const cuuint32_t box[5] = {32, (cuuint32_t)w, 16, 1, 1};
+            rc = encode_map(&mp.a[w - 1], X, 5, dims, str, box, CU_TENSOR_MAP_SWIZZLE_NONE);
+            if (!rc) rc = encode_map(&mp.c[w - 1], Y, 5, dims, str, box, CU_TENSOR_MAP_SWIZZLE_NONE);
+            if (!rc && diagV) rc = encode_map(&mp.v[w - 1], diagV, 4, dims, str, box, CU_TENSOR_MAP_SWIZZLE_NONE);
+        }
         g.ering = p_ring(g.NT, g.KS, diagV != nullptr, &g.echunk);
     }
     if (rc) return rc;
-    if (nin == 1 && !g.tstore) tmC = tmA;
-    if (!(nin > 1 && diagV)) tmV = tmA;
 
     static int sms = 0, configured = -1;
     int dev = 0;
@@ -855,8 +963,8 @@ int tc32p_level_apply(const scalit_ctx *c, int l, bool f16, const float *X, floa
     const int grid = (int)(tiles < sms ? tiles : sms);
     g.nslots = nin == 1 ? kPSlotsMax : kPSlotsM;
     const size_t smem = p_smem_bytes(g.NT, g.KS, g.nslots, (size_t)g.ering * g.echunk);
-    if (f16) tc32p_level_kernel<true><<<grid, kPThreads, smem, s>>>(g, tmA, tmC, tmV);
-    else tc32p_level_kernel<false><<<grid, kPThreads, smem, s>>>(g, tmA, tmC, tmV);
+    if (f16) tc32p_level_kernel<true><<<grid, kPThreads, smem, s>>>(g, mp);
+    else tc32p_level_kernel<false><<<grid, kPThreads, smem, s>>>(g, mp);
     SC_CHECK_LAUNCH();
     return 0;
 }

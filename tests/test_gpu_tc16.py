@@ -36,11 +36,15 @@ def _hx32(ctx, X, ntype):
     return dy.double().cpu().numpy()
 
 
-@pytest.mark.parametrize("sizes", [(24, 32, 20), (20, 12, 8), (36, 44, 28), (32, 24, 20), (64, 20, 12)])
+@pytest.mark.parametrize("sizes", [(24, 32, 20), (20, 12, 8), (36, 44, 28), (32, 24, 20), (64, 20, 12),
+                                   (160, 12, 8), (224, 12, 4), (96, 12, 8), (160, 12, 7)])
 @pytest.mark.parametrize("mode,tol", [(capi.FP32_TENSOR16, TOL_F16X3), (capi.FP32_TENSOR, TOL_BF16X3)])
 def test_hx_f32_persistent(lib, orc, sizes, mode, tol):
     """Both split forms against the FP64 oracle; vectors scaled by 1e-30 ..
-    1e+30 exercise the FP16 form's per-vector exponent."""
+    1e+30 exercise the FP16 form's per-vector exponent.  Blocks of 32, 64,
+    96, 160 and 224 points put a tile's four 32-point groups in 1 to 4 runs
+    of one to four groups, and short last blocks leave rows past the
+    vector's end."""
     pytest.importorskip("torch")
     p = hm.build_problem(hm.Grid3(*sizes), hm.PES())
     e0 = float(p.RES.min())
