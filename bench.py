@@ -323,9 +323,10 @@ def pist_leg(workload, levels, device, capi, hm, arms=("fp64", "fp32"), warmup=T
     pw = hm.workload("tri-24x32x20")
     for prec, orth in ((capi.PREC_FP64, 1), (capi.PREC_FP32_REFINED, 3)) if warmup else ():
         with capi.Context.from_problem(pw, e0=float(pw.RES.min()), device=device) as ctx:
-            ctx.build_osb(20, 1e-4)
             if prec != capi.PREC_FP64:
                 ctx.set_fp32_mode(MIXED_FP32_MODE)
+                ctx.set_build_precision(capi.PREC_FP32)
+            ctx.build_osb(20, 1e-4)
             ctx.pist(np.random.default_rng(0).random(pw.N), levels, float(pw.RES.min()), 1e-11,
                      m_max=max(8 * levels, 400), qmr_max=2000, qmr_tol=PIST_QMR_TOL, precision=prec, orth=orth,
                      refine_tol=REFINE_TOL, refine_steps=REFINE_STEPS)
@@ -335,16 +336,18 @@ def pist_leg(workload, levels, device, capi, hm, arms=("fp64", "fp32"), warmup=T
     out = {"workload": workload, "levels": levels}
     eigs = {}
     # mixed leg: FP32 inner solves (H*X in split-FP16 x3 and the preconditioner's
-    # rotations in split-BF16 x3 on the tensor cores) and an FP32 first
-    # Gram-Schmidt pass (the re-orthogonalisation's projections, HMAT and the
-    # Ritz solves stay FP64; its update streams the basis' FP32 copy with
-    # coefficients split into two FP32 parts)
+    # rotations in split-BF16 x3 on the tensor cores) on a preconditioner whose
+    # first-level Jacobi sweeps run in FP32 (it only feeds those solves), and
+    # an FP32 first Gram-Schmidt pass (the re-orthogonalisation's projections,
+    # HMAT and the Ritz solves stay FP64; its update streams the basis' FP32
+    # copy with coefficients split into two FP32 parts)
     for name, prec, orth in (("fp64", capi.PREC_FP64, 1), ("fp32", capi.PREC_FP32_REFINED, 3)):
         if name not in arms:
             continue
         with capi.Context.from_problem(p, e0=e0, device=device) as ctx:
             if prec != capi.PREC_FP64:
                 ctx.set_fp32_mode(MIXED_FP32_MODE)
+                ctx.set_build_precision(capi.PREC_FP32)
             t0 = time.perf_counter()
             stats = ctx.build_osb(20, 1e-4)
             t1 = time.perf_counter()
@@ -355,6 +358,7 @@ def pist_leg(workload, levels, device, capi, hm, arms=("fp64", "fp32"), warmup=T
             t2 = time.perf_counter()
         eigs[name] = eig
         out[name] = {"status": st, "orth": orth, "seconds": t2 - t0, "build_s": t1 - t0, "pist_s": t2 - t1,
+                     "build_sweeps": "FP32 on the first level" if prec != capi.PREC_FP64 else "FP64",
                      "inner_solves": ("FP32 QMR under FP64 iterative refinement (H*X split-FP16 x3 "
                                       "tensor cores, preconditioner rotations split-BF16 x3 tensor cores)"
                                       if prec != capi.PREC_FP64 else "FP64 QMR"),
@@ -412,6 +416,7 @@ def golden_pist_leg(workload, device, capi, hm):
         with capi.Context.from_problem(p, e0=fx["e0"], device=device) as ctx:
             if prec == capi.PREC_FP32:
                 ctx.set_fp32_mode(MIXED_FP32_MODE)
+                ctx.set_build_precision(capi.PREC_FP32)
             t0 = time.perf_counter()
             ctx.build_osb(20, 1e-4)
             st, eig, _, info = ctx.pist(x0, fx["levels"], fx["e0"], fx["etol"], startcnt=fx["startcnt"],

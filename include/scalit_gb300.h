@@ -123,6 +123,14 @@ int scalit_set_fp64_mode(scalit_ctx *ctx, int mode);
  * against ~2e-7 on the CUDA cores); split-FP16 x3 with exponent scaling
  * carries ~22.  No reference counterpart: the reference has no FP32 path. */
 int scalit_set_fp32_mode(scalit_ctx *ctx, int mode);
+/* Precision of the Jacobi sweeps of the next scalit_build_osb calls on the
+ * levels whose blocks hold one matrix each (the grid's first level, where
+ * the build spends most of its time): SCALIT_PREC_FP64 (default, the
+ * reference's HosbDiag/MJACOBI) or SCALIT_PREC_FP32 (angles, rotations and V
+ * in FP32; EIG0, the rotated HOSB and the sweep test in FP64) for a
+ * preconditioner that only feeds FP32 inner solves.  The outer levels' sweeps
+ * stay FP64.  No reference counterpart. */
+int scalit_set_build_precision(scalit_ctx *ctx, int precision);
 /* sOSBW%mE0: the shift of (H - E0) and of the preconditioner. */
 int scalit_set_shift(scalit_ctx *ctx, double e0);
 /* sOSB kernel kind with sOSBW%mDE and sOSBW%mBeta.  SCALIT_TOSBW needs a

@@ -51,6 +51,7 @@ SIGNATURES = {
     "scalit_build_times": (C.c_int, [_vp, _dp]),
     "scalit_selftest_wait": (C.c_int, [_vp, C.c_double]),
     "scalit_set_fp32_mode": (C.c_int, [_vp, C.c_int]),
+    "scalit_set_build_precision": (C.c_int, [_vp, C.c_int]),
     "scalit_tile_picks": (C.c_int, [_vp, _ip]),
     "scalit_get_osb": (C.c_int, [_vp, _dp, _dp]),
     "scalit_set_osb": (C.c_int, [_vp, _dp, _dp]),
@@ -261,6 +262,11 @@ class Context:
 
     def set_fp32_mode(self, mode):
         _check(self.lib.scalit_set_fp32_mode(self.h, int(mode)))
+
+    def set_build_precision(self, precision):
+        """PREC_FP64 (default) or PREC_FP32: precision of the next builds'
+        Jacobi sweeps on one-matrix blocks."""
+        _check(self.lib.scalit_set_build_precision(self.h, int(precision)))
 
     def set_shift(self, e0):
         _check(self.lib.scalit_set_shift(self.h, float(e0)))

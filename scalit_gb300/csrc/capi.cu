@@ -298,6 +298,17 @@ int scalit_set_fp64_mode(scalit_ctx *c, int mode)
     return 0;
 }
 
+int scalit_set_build_precision(scalit_ctx *c, int precision)
+{
+    if (!c) { set_error("null context"); return SCALIT_EINVAL; }
+    if (precision != SCALIT_PREC_FP64 && precision != SCALIT_PREC_FP32) {
+        set_error("unknown build precision %d", precision);
+        return SCALIT_EINVAL;
+    }
+    c->build_prec = precision;
+    return 0;
+}
+
 int scalit_set_fp32_mode(scalit_ctx *c, int mode)
 {
     if (!c) { set_error("null context"); return SCALIT_EINVAL; }

@@ -114,6 +114,9 @@ struct scalit_ctx {
     // FP32 engine: SCALIT_FP32_SIMT (CUDA cores), SCALIT_FP32_TENSOR (split-BF16 x3)
     // or SCALIT_FP32_TENSOR_PX (split-BF16 x3 for the preconditioner's rotations only)
     int fp32_mode = SCALIT_FP32_SIMT;
+    // precision of the preconditioner build's one-matrix Jacobi sweeps
+    // (SCALIT_PREC_FP64, or SCALIT_PREC_FP32 for FP32 inner solves)
+    int build_prec = SCALIT_PREC_FP64;
     TcLevelData tc32[SCALIT_FMAX];           // hi/lo planes of the level matrices
     TcLevelData pxtc32[SCALIT_FMAX][2];      // of the preconditioner's rotations [VX, VTX]
     TcLevelData tc[SCALIT_FMAX];
@@ -285,8 +288,10 @@ int pist_sx_host(scalit_ctx *c, i64 n, double e0, double etol, const double *X0,
 int osb_build(scalit_ctx *c, int bjmax, double bjtol, double *stats);
 // HosbDiag on a device HOSB(ndk, mak, mak, blk): fills VOSB and EIGVAL.
 int mjacobi_device(int P, int Q, int nout, int nin, double *dH, double *dabc, double *angle, cudaStream_t s);
+// f32: one-matrix blocks run their sweeps in FP32 (a preconditioner built for
+// FP32 inner solves); every other block and caller runs them in FP64.
 int hosbdiag_device(scalit_ctx *c, int bjmax, double bjtol, int blk, int mak, int ndk,
-                    double *HOSB, double *VOSB, double *EIG, double *stats5, cudaStream_t s);
+                    double *HOSB, double *VOSB, double *EIG, double *stats5, cudaStream_t s, bool f32 = false);
 
 // ------------------------------------------------------------ vector ops --
 // Deterministic FP64-accumulated dot product; writes the result to *out (device).

@@ -39,37 +39,39 @@ namespace sc {
 
 static constexpr int kThreads = 256;
 
-// cos and sin of the MJACOBI angle (jacobi.f90:42-60).
-__device__ void jacobi_angle(double A, double B, double C, double *cs, double *sn)
+// cos and sin of the MJACOBI angle (jacobi.f90:42-60), in the precision of
+// the sweep (FP64, or FP32 for a preconditioner built in single precision).
+template <typename R>
+__device__ void jacobi_angle(R A, R B, R C, R *cs, R *sn)
 {
-    const double INV_SQRT2 = 0.70710678118654752440;
+    const R INV_SQRT2 = R(0.70710678118654752440), one = R(1), half = R(0.5), two = R(2);
     if (A == C) {
-        if (B == 0.0) { *cs = 1.0; *sn = 0.0; return; }
+        if (B == R(0)) { *cs = one; *sn = R(0); return; }
         // X = -sign(pi/8, B)
-        const double c8 = sqrt(0.5 * (1.0 + INV_SQRT2));
-        const double s8 = sqrt(0.5 * (1.0 - INV_SQRT2));
+        const R c8 = sqrt(half * (one + INV_SQRT2));
+        const R s8 = sqrt(half * (one - INV_SQRT2));
         *cs = c8;
-        *sn = (B > 0.0) ? -s8 : s8;
+        *sn = (B > R(0)) ? -s8 : s8;
         return;
     }
-    const double T = B / (A - C);
-    double c4, s4;   // cos, sin of atan(T)
-    if (fabs(T) > 1.0) {
-        const double r = 1.0 / T;
-        const double h = sqrt(1.0 + r * r);
+    const R T = B / (A - C);
+    R c4, s4;   // cos, sin of atan(T)
+    if (fabs(T) > one) {
+        const R r = one / T;
+        const R h = sqrt(one + r * r);
         c4 = fabs(r) / h;
-        s4 = (T > 0.0 ? 1.0 : -1.0) / h;
+        s4 = (T > R(0) ? one : -one) / h;
     } else {
-        c4 = 1.0 / sqrt(1.0 + T * T);
+        c4 = one / sqrt(one + T * T);
         s4 = T * c4;
     }
-    const double c2 = sqrt(0.5 * (1.0 + c4));
-    const double s2 = s4 / (2.0 * c2);
-    double c = sqrt(0.5 * (1.0 + c2));
-    double s = s2 / (2.0 * c);
+    const R c2 = sqrt(half * (one + c4));
+    const R s2 = s4 / (two * c2);
+    R c = sqrt(half * (one + c2));
+    R s = s2 / (two * c);
     if (A > C) {
-        double nc, ns;
-        if (s < 0.0) {        // X + pi/4  (X < 0 <=> s < 0)
+        R nc, ns;
+        if (s < R(0)) {       // X + pi/4  (X < 0 <=> s < 0)
             nc = (c - s) * INV_SQRT2;
             ns = (s + c) * INV_SQRT2;
         } else {              // X - pi/4
@@ -221,15 +223,16 @@ __device__ __forceinline__ void batch_item(double *H, int ndk_, int mak, int ldr
 
 // VUPDATE (vupdate.f90:21-36) of item u = (t, row), rows fastest: columns
 // p_t, q_t of V.
-__device__ __forceinline__ void batch_vitem(double *V, int mak, int a, int i,
-                                            const double *__restrict__ cs, const double *__restrict__ sn,
+template <typename R>
+__device__ __forceinline__ void batch_vitem(R *V, int mak, int a, int i,
+                                            const R *__restrict__ cs, const R *__restrict__ sn,
                                             int u, float rmak)
 {
     int row;
     const int t = quot_small(u, mak, rmak, row);
-    double *vp = V + (i64)(a + t) * mak + row, *vq = V + (i64)(a + i + t) * mak + row;
-    const double c = cs[t], sv = sn[t];
-    const double x = *vp, y = *vq;
+    R *vp = V + (i64)(a + t) * mak + row, *vq = V + (i64)(a + i + t) * mak + row;
+    const R c = cs[t], sv = sn[t];
+    const R x = *vp, y = *vq;
     *vp = c * x - sv * y;
     *vq = c * y + sv * x;
 }
@@ -386,8 +389,9 @@ jacobi_block_kernel(int bjmax, double bjtol, int blk, int mak, int ndk,
 __device__ __forceinline__ int pk(int r, int c) { return ((c * (c + 1)) >> 1) + r; }   // r <= c
 __device__ __forceinline__ int pks(int a, int b) { return a <= b ? pk(a, b) : pk(b, a); }
 
-__device__ __forceinline__ void packed_item(double *H, int mak, int a, int i, int m,
-                                            const double *__restrict__ cs, const double *__restrict__ sn,
+template <typename R>
+__device__ __forceinline__ void packed_item(R *H, int mak, int a, int i, int m,
+                                            const R *__restrict__ cs, const R *__restrict__ sn,
                                             int u, float rm)
 {
     const int nfree = (mak - 2 * m) * m;
@@ -396,8 +400,8 @@ __device__ __forceinline__ void packed_item(double *H, int mak, int a, int i, in
         const int f = quot_small(u, m, rm, t), r = free_row(f, a, i, m);
         const int p = a + t, q = a + i + t;
         const int ip = pks(r, p), iq = pks(r, q);
-        const double c = cs[t], sv = sn[t];
-        const double x = H[ip], y = H[iq];
+        const R c = cs[t], sv = sn[t];
+        const R x = H[ip], y = H[iq];
         H[ip] = c * x - sv * y;
         H[iq] = c * y + sv * x;
         return;
@@ -407,43 +411,46 @@ __device__ __forceinline__ void packed_item(double *H, int mak, int a, int i, in
     const int t = quot_small(u, m, rm, t2);
     if (t2 < t) return;
     const int p = a + t, q = a + i + t;
-    const double c = cs[t], sv = sn[t];
+    const R c = cs[t], sv = sn[t];
     if (t == t2) {
         const int pp = pk(p, p), qq = pk(q, q), pq = pk(p, q);
-        const double C2 = c * c, S2 = sv * sv, SC = sv * c;
-        const double odg = H[pq];
-        const double ddg = 0.5 * H[pp] - 0.5 * H[qq];
-        const double np_ = C2 * H[pp] + S2 * H[qq] - 2 * SC * odg;
-        const double nq_ = C2 * H[qq] + S2 * H[pp] + 2 * SC * odg;
-        const double nqp = (C2 - S2) * odg + 2 * SC * ddg;
+        const R C2 = c * c, S2 = sv * sv, SC = sv * c;
+        const R odg = H[pq];
+        const R ddg = R(0.5) * H[pp] - R(0.5) * H[qq];
+        const R np_ = C2 * H[pp] + S2 * H[qq] - R(2) * SC * odg;
+        const R nq_ = C2 * H[qq] + S2 * H[pp] + R(2) * SC * odg;
+        const R nqp = (C2 - S2) * odg + R(2) * SC * ddg;
         H[pp] = np_; H[qq] = nq_; H[pq] = nqp;
         return;
     }
     const int p2 = a + t2, q2 = a + i + t2;
     const int i00 = pks(p, p2), i01 = pks(p, q2), i10 = pks(q, p2), i11 = pks(q, q2);
-    const double x00 = H[i00], x01 = H[i01], x10 = H[i10], x11 = H[i11];
-    const double a00 = c * x00 - sv * x10, a10 = c * x10 + sv * x00;
-    const double a01 = c * x01 - sv * x11, a11 = c * x11 + sv * x01;
-    const double c2 = cs[t2], s2 = sn[t2];
+    const R x00 = H[i00], x01 = H[i01], x10 = H[i10], x11 = H[i11];
+    const R a00 = c * x00 - sv * x10, a10 = c * x10 + sv * x00;
+    const R a01 = c * x01 - sv * x11, a11 = c * x11 + sv * x01;
+    const R c2 = cs[t2], s2 = sn[t2];
     H[i00] = c2 * a00 - s2 * a01;
     H[i01] = c2 * a01 + s2 * a00;
     H[i10] = c2 * a10 - s2 * a11;
     H[i11] = c2 * a11 + s2 * a10;
 }
 
-// 2 sum over r < c of H(r, c)^2 and sum of H(c, c)^2, column by column.
-__device__ double packed_offdiag(const double *H, int mak, double *red)
+// 2 sum over r < c of H(r, c)^2 and sum of H(c, c)^2, column by column
+// (summed in FP64 for either element type).
+template <typename R>
+__device__ double packed_offdiag(const R *H, int mak, double *red)
 {
     double s = 0.0, z1 = 0.0, z2 = 0.0;
     for (int c = 1; c < mak; ++c) {
-        const double *Hc = H + pk(0, c);
+        const R *Hc = H + pk(0, c);
         for (int r = threadIdx.x; r < c; r += blockDim.x) { const double h = Hc[r]; s = fma(h, h, s); }
     }
     block_sum3(s, z1, z2, red);
     return 2.0 * s;
 }
 
-__device__ double packed_sumdiag(const double *H, int mak, double *red)
+template <typename R>
+__device__ double packed_sumdiag(const R *H, int mak, double *red)
 {
     double s = 0.0, z1 = 0.0, z2 = 0.0;
     for (int c = threadIdx.x; c < mak; c += blockDim.x) { const double h = H[pk(c, c)]; s = fma(h, h, s); }
@@ -451,28 +458,33 @@ __device__ double packed_sumdiag(const double *H, int mak, double *red)
     return s;
 }
 
+// R = float: the sweeps of a preconditioner built in single precision (its
+// products only feed FP32 inner solves): H, the angles and V in FP32 (V in
+// the first half of the block's FP64 storage, widened in place at the end),
+// the sweep sums, EIG0 and the rotated HOSB in FP64.
+template <typename R>
 __global__ void __launch_bounds__(512, 2)
 jacobi_packed_kernel(int bjmax, double bjtol, int blk, int mak, double *__restrict__ HOSB,
                      double *__restrict__ VOSB, double *__restrict__ EIG, double *__restrict__ bstats)
 {
     extern __shared__ __align__(16) double smem[];
     double *red = smem;                 // 3 * 32
-    double *cs = smem + 96;             // kMaxBatch
-    double *sn = cs + kMaxBatch;        // kMaxBatch
-    double *cs_v = sn + kMaxBatch;      // kMaxBatch: the previous batch's angles, for
-    double *sn_v = cs_v + kMaxBatch;    // kMaxBatch  its deferred V update
-    double *H = sn_v + kMaxBatch;       // upper triangle, mak (mak + 1) / 2
+    R *cs = reinterpret_cast<R *>(smem + 96);   // kMaxBatch
+    R *sn = cs + kMaxBatch;             // kMaxBatch
+    R *cs_v = sn + kMaxBatch;           // kMaxBatch: the previous batch's angles, for
+    R *sn_v = cs_v + kMaxBatch;         // kMaxBatch  its deferred V update
+    R *H = sn_v + kMaxBatch;            // upper triangle, mak (mak + 1) / 2
     const int tid = threadIdx.x, nt = blockDim.x;
     const float rmak = 1.0f / (float)mak;
     for (int b = blockIdx.x; b < blk; b += gridDim.x) {
         double *Hg = HOSB + (i64)b * mak * mak;
-        double *V = VOSB + (i64)b * mak * mak;
+        R *V = reinterpret_cast<R *>(VOSB + (i64)b * mak * mak);
         __syncthreads();
         for (int e = tid; e < mak * mak; e += nt) {
             int r;
             const int c = quot_small(e, mak, rmak, r);
-            if (r <= c) H[pk(r, c)] = Hg[e];
-            V[e] = (r == c) ? 1.0 : 0.0;
+            if (r <= c) H[pk(r, c)] = (R)Hg[e];
+            V[e] = (r == c) ? R(1) : R(0);
         }
         __syncthreads();
         const double initye = packed_offdiag(H, mak, red);
@@ -488,9 +500,9 @@ jacobi_packed_kernel(int bjmax, double bjtol, int blk, int mak, double *__restri
                     const int t0 = (m + 31) & ~31;          // t0 <= kMaxBatch < nt
                     if (tid < m) {
                         const int p = a + tid, q = a + i + tid;
-                        const double o = H[pk(p, q)];
-                        const double d = 0.5 * H[pk(p, p)] - 0.5 * H[pk(q, q)];
-                        jacobi_angle(o * o, 2.0 * (o * d), d * d, cs + tid, sn + tid);
+                        const R o = H[pk(p, q)];
+                        const R d = R(0.5) * H[pk(p, p)] - R(0.5) * H[pk(q, q)];
+                        jacobi_angle(o * o, R(2) * (o * d), d * d, cs + tid, sn + tid);
                     } else if (tid >= t0) {
                         for (int u = tid - t0; u < mak * mv; u += nt - t0)
                             batch_vitem(V, mak, av, iv, cs_v, sn_v, u, rmak);
@@ -511,12 +523,26 @@ jacobi_packed_kernel(int bjmax, double bjtol, int blk, int mak, double *__restri
         for (int u = tid; u < mak * mv; u += nt) batch_vitem(V, mak, av, iv, cs_v, sn_v, u, rmak);
         const double sd = packed_sumdiag(H, mak, red);
         __syncthreads();
-        for (int e = tid; e < mak; e += nt) EIG[e + (i64)mak * b] = H[pk(e, e)];
+        for (int e = tid; e < mak; e += nt) EIG[e + (i64)mak * b] = (double)H[pk(e, e)];
         // the rotated matrix back in full storage, its diagonal zeroed (as HOSB after HosbDiag)
         for (int e = tid; e < mak * mak; e += nt) {
             int r;
             const int c = quot_small(e, mak, rmak, r);
-            Hg[e] = (r == c) ? 0.0 : H[pks(r, c)];
+            Hg[e] = (r == c) ? 0.0 : (double)H[pks(r, c)];
+        }
+        if constexpr (sizeof(R) == sizeof(float)) {
+            // widen V in place, last chunk of nt elements first: element e's
+            // double covers floats 2e and 2e + 1, which belong to chunks
+            // already read (or, for the first chunk, to itself and the next)
+            double *Vd = VOSB + (i64)b * mak * mak;
+            const int n = mak * mak;
+            for (int j0 = ((n - 1) / nt) * nt; j0 >= 0; j0 -= nt) {
+                const int e = j0 + tid;
+                const float v = e < n ? V[e] : 0.0f;
+                __syncthreads();
+                if (e < n) Vd[e] = (double)v;
+                __syncthreads();
+            }
         }
         if (tid == 0) {
             bstats[3 * (i64)b] = (double)k;
@@ -681,7 +707,7 @@ static int gridsz(i64 items)
 }
 
 int hosbdiag_device(scalit_ctx *c, int bjmax, double bjtol, int blk, int mak, int ndk,
-                    double *HOSB, double *VOSB, double *EIG, double *stats5, cudaStream_t s)
+                    double *HOSB, double *VOSB, double *EIG, double *stats5, cudaStream_t s, bool f32)
 {
     if (blk <= 0 || mak <= 0 || ndk <= 0) { set_error("hosbdiag: bad sizes"); return SCALIT_EINVAL; }
     std::vector<double> bstats(3 * (size_t)blk);
@@ -712,15 +738,23 @@ int hosbdiag_device(scalit_ctx *c, int bjmax, double bjtol, int blk, int mak, in
         if (forced) nt = forced;
         if (ndk == 1) {
             // one matrix per block: the packed triangle, half the shared memory
-            const size_t pbytes = sizeof(double) * (size_t)mak * (mak + 1) / 2;
+            // (a quarter with FP32 sweeps)
+            const size_t pbytes = (f32 ? sizeof(float) : sizeof(double)) * (size_t)mak * (mak + 1) / 2;
             const int pctas = std::max(1, (int)((228 * 1024) / (fixed + pbytes + 1024)));
             int pnt = 256;
             while (pnt < 512 && 2 * pnt * pctas <= 512) pnt *= 2;
             if (forced) pnt = std::min(forced, 512);
-            SC_CUDA(cudaFuncSetAttribute(jacobi_packed_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         (int)(225 * 1024)));
-            jacobi_packed_kernel<<<grid, pnt, fixed + pbytes, s>>>(bjmax, bjtol, blk, mak, HOSB, VOSB, EIG,
-                                                                  d_bstats);
+            if (f32) {
+                SC_CUDA(cudaFuncSetAttribute(jacobi_packed_kernel<float>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             (int)(225 * 1024)));
+                jacobi_packed_kernel<float><<<grid, pnt, fixed + pbytes, s>>>(bjmax, bjtol, blk, mak, HOSB, VOSB,
+                                                                              EIG, d_bstats);
+            } else {
+                SC_CUDA(cudaFuncSetAttribute(jacobi_packed_kernel<double>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             (int)(225 * 1024)));
+                jacobi_packed_kernel<double><<<grid, pnt, fixed + pbytes, s>>>(bjmax, bjtol, blk, mak, HOSB, VOSB,
+                                                                               EIG, d_bstats);
+            }
         } else {
             jacobi_block_kernel<<<grid, nt, fixed + bytes, s>>>(bjmax, bjtol, blk, mak, ndk, HOSB, VOSB, EIG,
                                                                 d_bstats);
@@ -919,7 +953,7 @@ int osb_build(scalit_ctx *c, int bjmax, double bjtol, double *stats)
         }
         if (rc == 0)
             rc = hosbdiag_device(c, bjmax, bjtol, (int)blk, mak, (int)ndk, HOSB, c->VOSB + L.vs[l],
-                                 c->EIG0, stats ? stats + 5 * l : nullptr, s);
+                                 c->EIG0, stats ? stats + 5 * l : nullptr, s, c->build_prec == SCALIT_PREC_FP32);
         if (rc == 0 && cudaStreamSynchronize(s) != cudaSuccess) { set_error("osb build level %d", l + 1); rc = SCALIT_ECUDA; }
         c->build_s[l] = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
     }
