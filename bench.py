@@ -326,6 +326,7 @@ def pist_leg(workload, levels, device, capi, hm, arms=("fp64", "fp32"), warmup=T
             if prec != capi.PREC_FP64:
                 ctx.set_fp32_mode(MIXED_FP32_MODE)
                 ctx.set_build_precision(capi.PREC_FP32)
+                ctx.set_fp32_px_storage(16)
             ctx.build_osb(20, 1e-4)
             ctx.pist(np.random.default_rng(0).random(pw.N), levels, float(pw.RES.min()), 1e-11,
                      m_max=max(8 * levels, 400), qmr_max=2000, qmr_tol=PIST_QMR_TOL, precision=prec, orth=orth,
@@ -337,7 +338,8 @@ def pist_leg(workload, levels, device, capi, hm, arms=("fp64", "fp32"), warmup=T
     eigs = {}
     # mixed leg: FP32 inner solves (H*X in split-FP16 x3 and the preconditioner's
     # rotations in split-BF16 x3 on the tensor cores) on a preconditioner whose
-    # first-level Jacobi sweeps run in FP32 (it only feeds those solves), and
+    # first-level Jacobi sweeps run in FP32 and whose first-level matrices the
+    # FP32 P*X streams in FP16 (it only feeds those solves), and
     # an FP32 first Gram-Schmidt pass (the re-orthogonalisation's projections,
     # HMAT and the Ritz solves stay FP64; its update streams the basis' FP32
     # copy with coefficients split into two FP32 parts)
@@ -348,6 +350,7 @@ def pist_leg(workload, levels, device, capi, hm, arms=("fp64", "fp32"), warmup=T
             if prec != capi.PREC_FP64:
                 ctx.set_fp32_mode(MIXED_FP32_MODE)
                 ctx.set_build_precision(capi.PREC_FP32)
+                ctx.set_fp32_px_storage(16)
             t0 = time.perf_counter()
             stats = ctx.build_osb(20, 1e-4)
             t1 = time.perf_counter()
@@ -359,6 +362,7 @@ def pist_leg(workload, levels, device, capi, hm, arms=("fp64", "fp32"), warmup=T
         eigs[name] = eig
         out[name] = {"status": st, "orth": orth, "seconds": t2 - t0, "build_s": t1 - t0, "pist_s": t2 - t1,
                      "build_sweeps": "FP32 on the first level" if prec != capi.PREC_FP64 else "FP64",
+                     "px_level1_storage": "FP16" if prec != capi.PREC_FP64 else "FP64",
                      "inner_solves": ("FP32 QMR under FP64 iterative refinement (H*X split-FP16 x3 "
                                       "tensor cores, preconditioner rotations split-BF16 x3 tensor cores)"
                                       if prec != capi.PREC_FP64 else "FP64 QMR"),
@@ -417,6 +421,7 @@ def golden_pist_leg(workload, device, capi, hm):
             if prec == capi.PREC_FP32:
                 ctx.set_fp32_mode(MIXED_FP32_MODE)
                 ctx.set_build_precision(capi.PREC_FP32)
+                ctx.set_fp32_px_storage(16)
             t0 = time.perf_counter()
             ctx.build_osb(20, 1e-4)
             st, eig, _, info = ctx.pist(x0, fx["levels"], fx["e0"], fx["etol"], startcnt=fx["startcnt"],

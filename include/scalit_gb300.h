@@ -131,6 +131,16 @@ int scalit_set_fp32_mode(scalit_ctx *ctx, int mode);
  * preconditioner that only feeds FP32 inner solves.  The outer levels' sweeps
  * stay FP64.  No reference counterpart. */
 int scalit_set_build_precision(scalit_ctx *ctx, int precision);
+/* Storage of the first level's preconditioner matrices for the FP32 P*X:
+ * bits = 32 (default, FP32) or 16 (an FP16 copy, made now and after every
+ * scalit_build_osb / scalit_set_osb; first levels of a multiple of 8
+ * points).  The FP32 P*X streams those matrices once per application -- the
+ * largest array of the solve -- so FP16 halves its traffic; the rounding of
+ * the eigenvectors (~2^-11) perturbs the preconditioner, not the operator,
+ * so FP32 inner solves under FP64 refinement converge to the same result.
+ * The FP64 P*X and the batched (several shifts) P*X keep FP32/FP64.  No
+ * reference counterpart. */
+int scalit_set_fp32_px_storage(scalit_ctx *ctx, int bits);
 /* sOSBW%mE0: the shift of (H - E0) and of the preconditioner. */
 int scalit_set_shift(scalit_ctx *ctx, double e0);
 /* sOSB kernel kind with sOSBW%mDE and sOSBW%mBeta.  SCALIT_TOSBW needs a

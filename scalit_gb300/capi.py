@@ -52,6 +52,7 @@ SIGNATURES = {
     "scalit_selftest_wait": (C.c_int, [_vp, C.c_double]),
     "scalit_set_fp32_mode": (C.c_int, [_vp, C.c_int]),
     "scalit_set_build_precision": (C.c_int, [_vp, C.c_int]),
+    "scalit_set_fp32_px_storage": (C.c_int, [_vp, C.c_int]),
     "scalit_tile_picks": (C.c_int, [_vp, _ip]),
     "scalit_get_osb": (C.c_int, [_vp, _dp, _dp]),
     "scalit_set_osb": (C.c_int, [_vp, _dp, _dp]),
@@ -262,6 +263,11 @@ class Context:
 
     def set_fp32_mode(self, mode):
         _check(self.lib.scalit_set_fp32_mode(self.h, int(mode)))
+
+    def set_fp32_px_storage(self, bits):
+        """32 (default) or 16: storage of the first level's preconditioner
+        matrices for the FP32 P*X."""
+        _check(self.lib.scalit_set_fp32_px_storage(self.h, int(bits)))
 
     def set_build_precision(self, precision):
         """PREC_FP64 (default) or PREC_FP32: precision of the next builds'

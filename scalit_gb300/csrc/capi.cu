@@ -163,6 +163,7 @@ void scalit_destroy(scalit_ctx *c)
     for (double *p : dptrs) if (p) cudaFree(p);
     float *fptrs[] = {c->H0f, c->RESf, c->DEPf, c->OUTHf, c->EIG0f, c->VOSBf};
     for (float *p : fptrs) if (p) cudaFree(p);
+    if (c->VOSBh) cudaFree(c->VOSBh);
     for (int l = 0; l < SCALIT_FMAX; ++l) {
         if (c->tc[l].dig) cudaFree(c->tc[l].dig);
         if (c->tc[l].exps) cudaFree(c->tc[l].exps);
@@ -307,6 +308,15 @@ int scalit_set_build_precision(scalit_ctx *c, int precision)
     }
     c->build_prec = precision;
     return 0;
+}
+
+int scalit_set_fp32_px_storage(scalit_ctx *c, int bits)
+{
+    CTX_CHECK(c);
+    if (bits != 32 && bits != 16) { set_error("FP32 P*X storage of %d bits", bits); return SCALIT_EINVAL; }
+    c->px_bits = bits;
+    c->gen++;
+    return px_half_prepare(c);
 }
 
 int scalit_set_fp32_mode(scalit_ctx *c, int mode)
@@ -532,6 +542,7 @@ int scalit_set_osb(scalit_ctx *c, const double *VOSB, const double *EIG0)
     c->gen++;
     rc = tc_prepare_px(c);
     if (!rc) rc = tc32_prepare(c, true);
+    if (!rc) rc = px_half_prepare(c);
     return rc;
 }
 

@@ -117,6 +117,10 @@ struct scalit_ctx {
     // precision of the preconditioner build's one-matrix Jacobi sweeps
     // (SCALIT_PREC_FP64, or SCALIT_PREC_FP32 for FP32 inner solves)
     int build_prec = SCALIT_PREC_FP64;
+    // storage of the level-1 preconditioner matrices for the FP32 P*X: 32
+    // (VOSBf) or 16 (an FP16 copy, VOSBh, made by px_half_prepare)
+    int px_bits = 32;
+    void *VOSBh = nullptr;
     TcLevelData tc32[SCALIT_FMAX];           // hi/lo planes of the level matrices
     TcLevelData pxtc32[SCALIT_FMAX][2];      // of the preconditioner's rotations [VX, VTX]
     TcLevelData tc[SCALIT_FMAX];
@@ -290,6 +294,7 @@ int osb_build(scalit_ctx *c, int bjmax, double bjtol, double *stats);
 int mjacobi_device(int P, int Q, int nout, int nin, double *dH, double *dabc, double *angle, cudaStream_t s);
 // f32: one-matrix blocks run their sweeps in FP32 (a preconditioner built for
 // FP32 inner solves); every other block and caller runs them in FP64.
+int px_half_prepare(scalit_ctx *c);
 int hosbdiag_device(scalit_ctx *c, int bjmax, double bjtol, int blk, int mak, int ndk,
                     double *HOSB, double *VOSB, double *EIG, double *stats5, cudaStream_t s, bool f32 = false);
 

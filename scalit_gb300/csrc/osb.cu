@@ -965,6 +965,7 @@ int osb_build(scalit_ctx *c, int bjmax, double bjtol, double *stats)
     SC_CUDA(cudaStreamSynchronize(s));
     if (!rc) rc = tc_prepare_px(c);
     if (!rc) rc = tc32_prepare(c, true);
+    if (!rc) rc = px_half_prepare(c);
     return rc;
 }
 

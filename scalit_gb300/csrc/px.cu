@@ -11,11 +11,22 @@
 #include "internal.cuh"
 #include "ptx.cuh"
 
+#include <cuda_fp16.h>
+
 #include <algorithm>
 #include <cstdlib>
 #include <type_traits>
 
 namespace sc {
+
+// An element of a staged matrix in the compute type (the FP32 preconditioner
+// may keep its level-1 matrices in FP16).
+template <class T, class TV>
+__device__ __forceinline__ T vload(const TV &v)
+{
+    if constexpr (std::is_same<TV, __half>::value) return (T)__half2float(v);
+    else return (T)v;
+}
 
 // K^-1 of the preconditioner kernel (osb.px.h:156-189).
 template <class T>
@@ -134,10 +145,11 @@ __host__ __device__ constexpr size_t px1_stream_head(int ring)
 }
 
 // FULL: n == 32 * RPL, every lane holds RPL rows and no row test is needed.
-// CPW (2 or 4): columns per warp and chunk.
-template <class T, int RPL, bool FULL, int CPW>
+// CPW (2 or 4): columns per warp and chunk.  TV: the matrices' storage type
+// (T, or FP16 for the FP32 preconditioner: half the bytes streamed).
+template <class T, class TV, int RPL, bool FULL, int CPW>
 __global__ void __launch_bounds__(kStreamThreads, sizeof(T) == 4 ? 4 : 2)
-px_level1_stream(int n, i64 nblk, const T *__restrict__ V, const T *__restrict__ EIG,
+px_level1_stream(int n, i64 nblk, const TV *__restrict__ V, const T *__restrict__ EIG,
                  const T *__restrict__ X, T *__restrict__ Y, KernelParams kp, T alpha, int nc, int ring,
                  const int *gate, int *err)
 {
@@ -150,8 +162,8 @@ px_level1_stream(int n, i64 nblk, const T *__restrict__ V, const T *__restrict__
     int *relcnt = reinterpret_cast<int *>(full + ring);         // warps done with the slot's chunks
     int *last = relcnt + ring;                                  // the chunk last issued into the slot
     const int slot_elems = kChunkCols * n;
-    T *slots = reinterpret_cast<T *>(smem_stream + px1_stream_head(ring));
-    T *vec0 = slots + ring * slot_elems;                        // per parity: x, f, NW partials
+    TV *slots = reinterpret_cast<TV *>(smem_stream + px1_stream_head(ring));
+    T *vec0 = reinterpret_cast<T *>(slots + ring * slot_elems); // per parity: x, f, NW partials
     const int vstride = (2 + NW) * n;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const T e0 = T(kp.e0), de = T(fabs(kp.de)), rde = T(1.0 / fabs(kp.de));
@@ -165,7 +177,7 @@ px_level1_stream(int n, i64 nblk, const T *__restrict__ V, const T *__restrict__
         const int kk = g / nc, c0 = (g - kk * nc) * kChunkCols;
         const i64 b = blockIdx.x + (i64)kk * gridDim.x;
         const int cols = min(kChunkCols, n - c0);
-        const uint32_t bytes = (uint32_t)(sizeof(T) * (size_t)cols * n);
+        const uint32_t bytes = (uint32_t)(sizeof(TV) * (size_t)cols * n);
         last[slot] = g;
         mbar_arrive_expect_tx(&full[slot], bytes);
         bulk_g2s(slots + slot * slot_elems, V + b * (i64)n * n + (i64)c0 * n, bytes, &full[slot]);
@@ -210,7 +222,7 @@ px_level1_stream(int n, i64 nblk, const T *__restrict__ V, const T *__restrict__
         for (int c = 0; c < nc; ++c) {
             const int g = k * nc + c;
             if (!__all_sync(0xffffffffu, mbar_wait_timed(&full[slot], par))) { abort_flag = 1; break; }
-            const T *chunk = slots + slot * slot_elems + lane;
+            const TV *chunk = slots + slot * slot_elems + lane;
             const int c0 = c * kChunkCols, cols = min(kChunkCols, n - c0);
             // the warp's CPW columns, each element read once from shared
             // memory (columns past the block's last are zero: warp-uniform)
@@ -218,11 +230,11 @@ px_level1_stream(int n, i64 nblk, const T *__restrict__ V, const T *__restrict__
             #pragma unroll
             for (int q = 0; q < CPW; ++q) {
                 const int j = warp + q * NW;
-                const T *col = chunk + j * n;
+                const TV *col = chunk + j * n;
                 d[q] = T(0);
                 #pragma unroll
                 for (int r = 0; r < RPL; ++r) {
-                    v[q][r] = (j < cols && (FULL || lane + 32 * r < n)) ? col[32 * r] : T(0);
+                    v[q][r] = (j < cols && (FULL || lane + 32 * r < n)) ? vload<T>(col[32 * r]) : T(0);
                     d[q] = fma(v[q][r], xr[r], d[q]);
                 }
             }
@@ -387,8 +399,8 @@ static int px1_stream_shape(const void *fn, size_t chunk, int nc, size_t vecs, i
 
 // Launch of the streaming kernel; returns 1 when it does not apply (no ring
 // of two chunks fits), so the caller takes the one-CTA-per-block kernel.
-template <class T, int RPL, bool FULL, int CPW>
-static int launch_px1_stream_as(int n, i64 nblk, const T *V, const T *EIG, const T *X, T *Y, KernelParams kp,
+template <class T, class TV, int RPL, bool FULL, int CPW>
+static int launch_px1_stream_as(int n, i64 nblk, const TV *V, const T *EIG, const T *X, T *Y, KernelParams kp,
                                 T alpha, const int *gate, int *err, cudaStream_t s)
 {
     static int configured = -1;
@@ -396,18 +408,18 @@ static int launch_px1_stream_as(int n, i64 nblk, const T *V, const T *EIG, const
     int dev = 0;
     cudaGetDevice(&dev);
     if (configured != dev) {
-        SC_CUDA(cudaFuncSetAttribute(px_level1_stream<T, RPL, FULL, CPW>,
+        SC_CUDA(cudaFuncSetAttribute(px_level1_stream<T, TV, RPL, FULL, CPW>,
                                      cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kMaxDynSmem));
         for (int i = 0; i <= 256; ++i) shape_n[i] = 0;
         configured = dev;
     }
     constexpr int kChunkCols = CPW * kStreamWarps;
-    const size_t chunk = sizeof(T) * (size_t)kChunkCols * n;
+    const size_t chunk = sizeof(TV) * (size_t)kChunkCols * n;
     const int nc = (n + kChunkCols - 1) / kChunkCols;
     const size_t vecs = sizeof(T) * (size_t)n * 2 * (2 + kStreamWarps);
     if (!shape_n[n]) {
         int ring = 0;
-        shape_cta[n] = px1_stream_shape(reinterpret_cast<const void *>(px_level1_stream<T, RPL, FULL, CPW>),
+        shape_cta[n] = px1_stream_shape(reinterpret_cast<const void *>(px_level1_stream<T, TV, RPL, FULL, CPW>),
                                         chunk, nc, vecs, ring);
         shape_ring[n] = ring;
         shape_n[n] = 1;
@@ -417,22 +429,43 @@ static int launch_px1_stream_as(int n, i64 nblk, const T *V, const T *EIG, const
     if ((nblk / (152 * per_sm) + 1) * nc > 2147483647LL) return 1;   // a CTA counts its chunks in an int
     const size_t smem = px1_stream_head(ring) + (size_t)ring * chunk + vecs;
     const int grid = (int)std::min<i64>(nblk, 152 * per_sm);
-    px_level1_stream<T, RPL, FULL, CPW><<<grid, kStreamThreads, smem, s>>>(n, nblk, V, EIG, X, Y, kp, alpha,
-                                                                           nc, ring, gate, err);
+    px_level1_stream<T, TV, RPL, FULL, CPW><<<grid, kStreamThreads, smem, s>>>(n, nblk, V, EIG, X, Y, kp, alpha,
+                                                                               nc, ring, gate, err);
     SC_CHECK_LAUNCH();
     return 0;
 }
 
-template <class T, int RPL>
-static int launch_px1_stream(int n, i64 nblk, const T *V, const T *EIG, const T *X, T *Y, KernelParams kp,
+template <class T, class TV, int RPL>
+static int launch_px1_stream(int n, i64 nblk, const TV *V, const T *EIG, const T *X, T *Y, KernelParams kp,
                              T alpha, const int *gate, int *err, cudaStream_t s)
 {
     // four columns per warp halve the per-chunk overhead; two keep the
     // register footprint of long columns in bounds
     constexpr int CPW = RPL <= 5 ? 4 : 2;
     if (n == 32 * RPL)
-        return launch_px1_stream_as<T, RPL, true, CPW>(n, nblk, V, EIG, X, Y, kp, alpha, gate, err, s);
-    return launch_px1_stream_as<T, RPL, false, CPW>(n, nblk, V, EIG, X, Y, kp, alpha, gate, err, s);
+        return launch_px1_stream_as<T, TV, RPL, true, CPW>(n, nblk, V, EIG, X, Y, kp, alpha, gate, err, s);
+    return launch_px1_stream_as<T, TV, RPL, false, CPW>(n, nblk, V, EIG, X, Y, kp, alpha, gate, err, s);
+}
+
+// The streaming kernel with matrices stored as TV; returns 1 when it does
+// not apply (chunks and bases must be 16-byte aligned).
+template <class T, class TV>
+static int launch_px1_streamed(int n, i64 nblk, const TV *V, const T *EIG, const T *X, T *Y,
+                               KernelParams kp, T alpha, const int *gate, int *err, cudaStream_t s)
+{
+    const bool aligned = ((reinterpret_cast<uintptr_t>(V) & 15) == 0) && ((sizeof(TV) * (size_t)n * n) % 16 == 0) &&
+                         ((sizeof(TV) * (size_t)n) % 16 == 0 || sizeof(TV) == sizeof(T));
+    if (!(n >= 1 && n <= 256 && nblk >= 1 && aligned)) return 1;
+    switch ((n + 31) / 32) {
+    case 1: return launch_px1_stream<T, TV, 1>(n, nblk, V, EIG, X, Y, kp, alpha, gate, err, s);
+    case 2: return launch_px1_stream<T, TV, 2>(n, nblk, V, EIG, X, Y, kp, alpha, gate, err, s);
+    case 3: return launch_px1_stream<T, TV, 3>(n, nblk, V, EIG, X, Y, kp, alpha, gate, err, s);
+    case 4: return launch_px1_stream<T, TV, 4>(n, nblk, V, EIG, X, Y, kp, alpha, gate, err, s);
+    case 5: return launch_px1_stream<T, TV, 5>(n, nblk, V, EIG, X, Y, kp, alpha, gate, err, s);
+    case 6: return launch_px1_stream<T, TV, 6>(n, nblk, V, EIG, X, Y, kp, alpha, gate, err, s);
+    case 7: return launch_px1_stream<T, TV, 7>(n, nblk, V, EIG, X, Y, kp, alpha, gate, err, s);
+    default: return launch_px1_stream<T, TV, 8>(n, nblk, V, EIG, X, Y, kp, alpha, gate, err, s);
+    }
 }
 
 template <class T>
@@ -440,19 +473,8 @@ static int launch_px1(int n, i64 nblk, const T *V, const T *EIG, const T *X, T *
                       KernelParams kp, T alpha, const int *gate, int *err, cudaStream_t s)
 {
     // the streaming kernel: chunks and bases 16-byte aligned
-    const bool aligned = ((reinterpret_cast<uintptr_t>(V) & 15) == 0) && ((sizeof(T) * (size_t)n * n) % 16 == 0);
-    if (n >= 1 && n <= 256 && nblk >= 1 && aligned) {
-        int rc = 1;
-        switch ((n + 31) / 32) {
-        case 1: rc = launch_px1_stream<T, 1>(n, nblk, V, EIG, X, Y, kp, alpha, gate, err, s); break;
-        case 2: rc = launch_px1_stream<T, 2>(n, nblk, V, EIG, X, Y, kp, alpha, gate, err, s); break;
-        case 3: rc = launch_px1_stream<T, 3>(n, nblk, V, EIG, X, Y, kp, alpha, gate, err, s); break;
-        case 4: rc = launch_px1_stream<T, 4>(n, nblk, V, EIG, X, Y, kp, alpha, gate, err, s); break;
-        case 5: rc = launch_px1_stream<T, 5>(n, nblk, V, EIG, X, Y, kp, alpha, gate, err, s); break;
-        case 6: rc = launch_px1_stream<T, 6>(n, nblk, V, EIG, X, Y, kp, alpha, gate, err, s); break;
-        case 7: rc = launch_px1_stream<T, 7>(n, nblk, V, EIG, X, Y, kp, alpha, gate, err, s); break;
-        default: rc = launch_px1_stream<T, 8>(n, nblk, V, EIG, X, Y, kp, alpha, gate, err, s); break;
-        }
+    {
+        const int rc = launch_px1_streamed<T, T>(n, nblk, V, EIG, X, Y, kp, alpha, gate, err, s);
         if (rc <= 0) return rc;
     }
     const size_t vec = sizeof(T) * 2 * (size_t)n;
@@ -566,7 +588,14 @@ int px_vec(const scalit_ctx *c, int npc, const T *X, T *Y, T *tmp, T alpha, cons
     ++stage;
     {
         T *out = buf[(S - stage) % 2];
-        rc = launch_px1<T>(L.n[0], L.blk[0], V + L.vs[0], EIG, in, out, kp, alpha, gate, c->tc_err, s);
+        rc = 1;
+        if constexpr (std::is_same<T, float>::value) {
+            // level-1 matrices in FP16 (scalit_set_fp32_px_storage): half the bytes
+            if (c->VOSBh)
+                rc = launch_px1_streamed<float, __half>(L.n[0], L.blk[0], static_cast<const __half *>(c->VOSBh), EIG,
+                                                        in, out, kp, alpha, gate, c->tc_err, s);
+        }
+        if (rc > 0) rc = launch_px1<T>(L.n[0], L.blk[0], V + L.vs[0], EIG, in, out, kp, alpha, gate, c->tc_err, s);
         if (rc) return rc;
         in = out;
     }
@@ -581,6 +610,32 @@ int px_vec(const scalit_ctx *c, int npc, const T *X, T *Y, T *tmp, T alpha, cons
 }
 
 template int px_vec<double>(const scalit_ctx *, int, const double *, double *, double *, double, const int *, cudaStream_t);
+
+__global__ void f64_to_f16_kernel(i64 n, const double *__restrict__ x, __half *__restrict__ y)
+{
+    for (i64 i = blockIdx.x * (i64)blockDim.x + threadIdx.x; i < n; i += (i64)gridDim.x * blockDim.x)
+        y[i] = __double2half(x[i]);
+}
+
+// The FP16 copy of the level-1 matrices for the FP32 P*X, made from the FP64
+// preconditioner when the context asks for it (after every build or load),
+// freed otherwise.
+int px_half_prepare(scalit_ctx *c)
+{
+    const Layout &L = c->L;
+    const bool want = c->px_bits == 16 && c->osb_built && L.n[0] % 8 == 0;
+    if (!want) {
+        if (c->VOSBh) { cudaFree(c->VOSBh); c->VOSBh = nullptr; }
+        return 0;
+    }
+    const i64 n = L.blk[0] * (i64)L.n[0] * L.n[0];
+    if (!c->VOSBh) SC_CUDA(cudaMalloc(&c->VOSBh, sizeof(__half) * (size_t)n));
+    const int grid = (int)std::min<i64>((n + 255) / 256, 152 * 16);
+    f64_to_f16_kernel<<<grid, 256, 0, c->stream>>>(n, c->VOSB + L.vs[0], static_cast<__half *>(c->VOSBh));
+    SC_CHECK_LAUNCH();
+    SC_CUDA(cudaStreamSynchronize(c->stream));
+    return 0;
+}
 // P*X of nvec vectors (stride N) at once, vector v with its own kernel shift
 // e0v[v] (device): the level-1 matrices are staged once per block for all the
 // vectors, and the outer rotations fold the vectors into the GEMM rows.

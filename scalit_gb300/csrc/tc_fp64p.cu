@@ -561,13 +561,42 @@ tc64p_level_kernel(Tc64pArgs g, const __grid_constant__ CUtensorMap tmA, const _
 
 // Binary exponent of the largest |x| of every row of a level, for rows of
 // all vectors (out[z M + m]): rows along k (a_sk == 1) one warp per row,
-// otherwise one thread per row (consecutive rows, consecutive points).
+// otherwise 32 consecutive rows (consecutive points) per block, each of its
+// kRexpSlices warps taking every kRexpSlices-th k, the slices' maxima
+// combined in shared memory (enough blocks for one vector to fill the GPU).
+static constexpr int kRexpSlices = 8;
 __global__ void rowexp_kernel(const double *__restrict__ X, i64 N, int M, int K, i64 Mi, i64 s1, i64 s2, i64 a_sk,
                               int nvec, int *__restrict__ out, const int *gate, const int *vgate, int vgstride)
 {
     if (gate && *gate) return;
     const i64 rows = (i64)M * nvec;
-    if (a_sk == 1) {
+    if (a_sk != 1) {
+        __shared__ unsigned long long red[kRexpSlices][32];
+        const int lane = threadIdx.x & 31, slice = threadIdx.x >> 5;
+        const i64 t = blockIdx.x * (i64)32 + lane;
+        unsigned long long mx = 0;
+        bool on = t < rows;
+        int z = 0, m = 0;
+        if (on) {
+            z = (int)(t / M);
+            m = (int)(t - (i64)z * M);
+            on = !(vgate && vgate[(i64)z * vgstride]);
+        }
+        if (on) {
+            const double *x = X + (i64)z * N + (i64)(m % Mi) * s1 + (i64)(m / Mi) * s2;
+            for (int k = slice; k < K; k += kRexpSlices)
+                mx = max(mx, (unsigned long long)__double_as_longlong(fabs(x[(i64)k * a_sk])));
+        }
+        red[slice][lane] = mx;
+        __syncthreads();
+        if (slice == 0 && on) {
+            #pragma unroll
+            for (int q = 1; q < kRexpSlices; ++q) mx = max(mx, red[q][lane]);
+            out[t] = q_exp(mx);
+        }
+        return;
+    }
+    {
         const i64 w = (blockIdx.x * (i64)blockDim.x + threadIdx.x) >> 5;
         const int lane = threadIdx.x & 31;
         if (w >= rows) return;
@@ -579,15 +608,6 @@ __global__ void rowexp_kernel(const double *__restrict__ X, i64 N, int M, int K,
         #pragma unroll
         for (int o = 16; o > 0; o >>= 1) mx = max(mx, __shfl_xor_sync(0xffffffffu, mx, o));
         if (lane == 0) out[w] = q_exp(mx);
-    } else {
-        const i64 t = blockIdx.x * (i64)blockDim.x + threadIdx.x;
-        if (t >= rows) return;
-        const int z = (int)(t / M), m = (int)(t - (i64)z * M);
-        if (vgate && vgate[(i64)z * vgstride]) return;
-        const double *x = X + (i64)z * N + (i64)(m % Mi) * s1 + (i64)(m / Mi) * s2;
-        unsigned long long mx = 0;
-        for (int k = 0; k < K; ++k) mx = max(mx, (unsigned long long)__double_as_longlong(fabs(x[(i64)k * a_sk])));
-        out[t] = q_exp(mx);
     }
 }
 
@@ -641,9 +661,11 @@ int tc64p_rowexp(const scalit_ctx *c, int l, const double *X, int nvec, const in
     const i64 Mi = nin == 1 ? blk : nin, s1 = nin == 1 ? nout : 1, s2 = nin == 1 ? 0 : nin * nout;
     const i64 a_sk = nin == 1 ? 1 : nin;
     const i64 rows = M * nvec;
-    const i64 threads = a_sk == 1 ? rows * 32 : rows;
-    rowexp_kernel<<<(unsigned)((threads + 255) / 256), 256, 0, s>>>(X, L.N, (int)M, nout, Mi, s1, s2, a_sk, nvec,
-                                                                    c->rexp + c->rexp_off[l], gate, vgate, vstride);
+    // rows along k: a warp per row; points fastest: 32 rows per block of
+    // 32 x kRexpSlices threads
+    const i64 blocks = a_sk == 1 ? (rows * 32 + 255) / 256 : (rows + 31) / 32;
+    rowexp_kernel<<<(unsigned)blocks, a_sk == 1 ? 256 : 32 * kRexpSlices, 0, s>>>(
+        X, L.N, (int)M, nout, Mi, s1, s2, a_sk, nvec, c->rexp + c->rexp_off[l], gate, vgate, vstride);
     SC_CHECK_LAUNCH();
     return 0;
 }

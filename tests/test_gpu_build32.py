@@ -9,7 +9,12 @@ uses, since its preconditioner only feeds FP32 inner solves.
   residual refinement to 1e-8 Eh, as the bench's mixed arm runs) reproduces
   the oracle's committed 24x32x20 levels within 1e-4 cm^-1 and meets the
   residual target;
-* an unknown precision is refused.
+* the FP32 P*X with the first level's matrices stored in FP16
+  (scalit_set_fp32_px_storage(16)) stays within the FP16 rounding of the
+  FP32 P*X, and returns to it bit for bit when the storage goes back to 32;
+  mixed PIST with both (the bench's mixed arm) still meets the fixture and
+  the residual target;
+* an unknown precision or storage is refused.
 """
 import json
 import os
@@ -46,7 +51,30 @@ def test_fp32_build_matches_fp64(lib, sizes):
     assert abs(s32[0, 4] - s64[0, 4]) <= 0.25 * s64[0, 4] + blk0
 
 
-def test_mixed_pist_on_fp32_build(lib):
+def test_fp16_px_storage(lib):
+    torch = pytest.importorskip("torch")
+    p = hm.workload("tri-24x32x20")
+    with capi.Context.from_problem(p, e0=float(p.RES.min()) - 1e-3) as ctx:
+        ctx.build_osb(20, 1e-4)
+        X = torch.randn(3, p.N, dtype=torch.float32, device="cuda")
+        Y32, Y16, Yb = (torch.empty_like(X) for _ in range(3))
+        ctx.px_f32_device(X, Y32, 3)
+        ctx.set_fp32_px_storage(16)
+        ctx.px_f32_device(X, Y16, 3)
+        ctx.set_fp32_px_storage(32)
+        ctx.px_f32_device(X, Yb, 3)
+        torch.cuda.synchronize()
+        with pytest.raises(capi.ScalitError):
+            ctx.set_fp32_px_storage(8)
+    a, b = Y32.double().cpu().numpy(), Y16.double().cpu().numpy()
+    for v in range(3):
+        r = np.linalg.norm(a[v] - b[v]) / np.linalg.norm(a[v])
+        assert 1e-6 < r < 3e-3, (v, r)       # the FP16 copy is used, and only rounds
+    assert torch.equal(Y32, Yb)
+
+
+@pytest.mark.parametrize("bits", [32, 16])
+def test_mixed_pist_on_fp32_build(lib, bits):
     with open(os.path.join(os.path.dirname(__file__), "golden", "pist_tri-24x32x20.json")) as f:
         fx = json.load(f)
     p = hm.workload(fx["workload"])
@@ -54,6 +82,7 @@ def test_mixed_pist_on_fp32_build(lib):
     with capi.Context.from_problem(p, e0=fx["e0"]) as ctx:
         ctx.set_fp32_mode(capi.FP32_TENSOR16)
         ctx.set_build_precision(capi.PREC_FP32)
+        ctx.set_fp32_px_storage(bits)
         ctx.build_osb(20, 1e-4)
         st, eig, res, info = ctx.pist(x0, fx["levels"], fx["e0"], fx["etol"], startcnt=fx["startcnt"],
                                       m_max=fx["m_max"], qmr_max=fx["qmr_max"], qmr_tol=1e-6,
