@@ -123,13 +123,14 @@ int scalit_set_fp64_mode(scalit_ctx *ctx, int mode);
  * against ~2e-7 on the CUDA cores); split-FP16 x3 with exponent scaling
  * carries ~22.  No reference counterpart: the reference has no FP32 path. */
 int scalit_set_fp32_mode(scalit_ctx *ctx, int mode);
-/* Precision of the Jacobi sweeps of the next scalit_build_osb calls on the
- * levels whose blocks hold one matrix each (the grid's first level, where
- * the build spends most of its time): SCALIT_PREC_FP64 (default, the
- * reference's HosbDiag/MJACOBI) or SCALIT_PREC_FP32 (angles, rotations and V
- * in FP32; EIG0, the rotated HOSB and the sweep test in FP64) for a
- * preconditioner that only feeds FP32 inner solves.  The outer levels' sweeps
- * stay FP64.  No reference counterpart. */
+/* Precision of the Jacobi sweeps of the next scalit_build_osb calls:
+ * SCALIT_PREC_FP64 (default, the reference's HosbDiag/MJACOBI) or
+ * SCALIT_PREC_FP32 for a preconditioner that only feeds FP32 inner solves.
+ * With FP32, the levels whose blocks hold one matrix each (the grid's first
+ * level, where the build spends most of its time) sweep with angles,
+ * rotations and V in FP32, and the outer levels' stacked matrices are
+ * rotated in FP32 with their angles and V in FP64; EIG0 and the sweep test
+ * are FP64 throughout.  No reference counterpart. */
 int scalit_set_build_precision(scalit_ctx *ctx, int precision);
 /* Storage of the first level's preconditioner matrices for the FP32 P*X:
  * bits = 32 (default, FP32) or 16 (an FP16 copy, made now and after every

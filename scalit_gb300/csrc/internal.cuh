@@ -292,8 +292,9 @@ int pist_sx_host(scalit_ctx *c, i64 n, double e0, double etol, const double *X0,
 int osb_build(scalit_ctx *c, int bjmax, double bjtol, double *stats);
 // HosbDiag on a device HOSB(ndk, mak, mak, blk): fills VOSB and EIGVAL.
 int mjacobi_device(int P, int Q, int nout, int nin, double *dH, double *dabc, double *angle, cudaStream_t s);
-// f32: one-matrix blocks run their sweeps in FP32 (a preconditioner built for
-// FP32 inner solves); every other block and caller runs them in FP64.
+// f32: one-matrix blocks and the stacks of the spread schedule run their
+// sweeps in FP32 (a preconditioner built for FP32 inner solves); stacks that
+// fit one CTA's shared memory and every other caller run them in FP64.
 int px_half_prepare(scalit_ctx *c);
 int hosbdiag_device(scalit_ctx *c, int bjmax, double bjtol, int blk, int mak, int ndk,
                     double *HOSB, double *VOSB, double *EIG, double *stats5, cudaStream_t s, bool f32 = false);

@@ -164,8 +164,8 @@ __device__ __forceinline__ int free_row(int f, int a, int i, int m)
 
 // MJACOBI's update (jacobi.f90:62-80) of work item u of stacked matrix k.
 // ONE: a single matrix per block (ndk == 1) with 32-bit offsets.
-template <bool ONE>
-__device__ __forceinline__ void batch_item(double *H, int ndk_, int mak, int ldr, int a, int i, int m,
+template <bool ONE, typename R = double>
+__device__ __forceinline__ void batch_item(R *H, int ndk_, int mak, int ldr, int a, int i, int m,
                                            const double *__restrict__ cs, const double *__restrict__ sn,
                                            int u, int k, float rm)
 {
@@ -173,17 +173,17 @@ __device__ __forceinline__ void batch_item(double *H, int ndk_, int mak, int ldr
     const I ndk = ONE ? 1 : (I)ndk_;
     const int nfree = (mak - 2 * m) * m;
     const I ld = ndk * (I)ldr;
-    double *Hk = H + (ONE ? 0 : k);
+    R *Hk = H + (ONE ? 0 : k);
     if (u < nfree) {
         int t;
         const int f = quot_small(u, m, rm, t), r = free_row(f, a, i, m);
         const int p = a + t, q = a + i + t;
-        double *hrp = Hk + ndk * r + ld * p, *hrq = Hk + ndk * r + ld * q;
-        double *hpr = Hk + ndk * p + ld * r, *hqr = Hk + ndk * q + ld * r;
-        const double c = cs[t], sv = sn[t];
-        const double x = *hrp, y = *hrq;
-        const double np_ = c * x - sv * y;
-        const double nq_ = c * y + sv * x;
+        R *hrp = Hk + ndk * r + ld * p, *hrq = Hk + ndk * r + ld * q;
+        R *hpr = Hk + ndk * p + ld * r, *hqr = Hk + ndk * q + ld * r;
+        const R c = (R)cs[t], sv = (R)sn[t];
+        const R x = *hrp, y = *hrq;
+        const R np_ = c * x - sv * y;
+        const R nq_ = c * y + sv * x;
         *hrp = np_; *hpr = np_; *hrq = nq_; *hqr = nq_;
         return;
     }
@@ -192,30 +192,30 @@ __device__ __forceinline__ void batch_item(double *H, int ndk_, int mak, int ldr
     const int t = quot_small(u, m, rm, t2);
     if (t2 < t) return;
     const int p = a + t, q = a + i + t;
-    const double c = cs[t], sv = sn[t];
+    const R c = (R)cs[t], sv = (R)sn[t];
     if (t == t2) {
-        double *hpp = Hk + ndk * p + ld * p, *hqq = Hk + ndk * q + ld * q;
-        double *hpq = Hk + ndk * p + ld * q, *hqp = Hk + ndk * q + ld * p;
-        const double C2 = c * c, S2 = sv * sv, SC = sv * c;
-        const double odg = *hpq;
-        const double ddg = 0.5 * *hpp - 0.5 * *hqq;
-        const double np_ = C2 * *hpp + S2 * *hqq - 2 * SC * odg;
-        const double nq_ = C2 * *hqq + S2 * *hpp + 2 * SC * odg;
-        const double nqp = (C2 - S2) * odg + 2 * SC * ddg;
+        R *hpp = Hk + ndk * p + ld * p, *hqq = Hk + ndk * q + ld * q;
+        R *hpq = Hk + ndk * p + ld * q, *hqp = Hk + ndk * q + ld * p;
+        const R C2 = c * c, S2 = sv * sv, SC = sv * c;
+        const R odg = *hpq;
+        const R ddg = R(0.5) * *hpp - R(0.5) * *hqq;
+        const R np_ = C2 * *hpp + S2 * *hqq - R(2) * SC * odg;
+        const R nq_ = C2 * *hqq + S2 * *hpp + R(2) * SC * odg;
+        const R nqp = (C2 - S2) * odg + R(2) * SC * ddg;
         *hpp = np_; *hqq = nq_; *hpq = nqp; *hqp = nqp;
         return;
     }
     const int p2 = a + t2, q2 = a + i + t2;
-    double *h00 = Hk + ndk * p + ld * p2, *h01 = Hk + ndk * p + ld * q2;
-    double *h10 = Hk + ndk * q + ld * p2, *h11 = Hk + ndk * q + ld * q2;
+    R *h00 = Hk + ndk * p + ld * p2, *h01 = Hk + ndk * p + ld * q2;
+    R *h10 = Hk + ndk * q + ld * p2, *h11 = Hk + ndk * q + ld * q2;
     // rotation t acts on rows p2 and q2 as rows outside its plane ...
-    const double x00 = *h00, x01 = *h01, x10 = *h10, x11 = *h11;
-    const double a00 = c * x00 - sv * x10, a10 = c * x10 + sv * x00;
-    const double a01 = c * x01 - sv * x11, a11 = c * x11 + sv * x01;
+    const R x00 = *h00, x01 = *h01, x10 = *h10, x11 = *h11;
+    const R a00 = c * x00 - sv * x10, a10 = c * x10 + sv * x00;
+    const R a01 = c * x01 - sv * x11, a11 = c * x11 + sv * x01;
     // ... then rotation t2 on rows p and q
-    const double c2 = cs[t2], s2 = sn[t2];
-    const double b00 = c2 * a00 - s2 * a01, b01 = c2 * a01 + s2 * a00;
-    const double b10 = c2 * a10 - s2 * a11, b11 = c2 * a11 + s2 * a10;
+    const R c2 = (R)cs[t2], s2 = (R)sn[t2];
+    const R b00 = c2 * a00 - s2 * a01, b01 = c2 * a01 + s2 * a00;
+    const R b10 = c2 * a10 - s2 * a11, b11 = c2 * a11 + s2 * a10;
     *h00 = b00; *h01 = b01; *h10 = b10; *h11 = b11;
     Hk[ndk * p2 + ld * p] = b00; Hk[ndk * q2 + ld * p] = b01;
     Hk[ndk * p2 + ld * q] = b10; Hk[ndk * q2 + ld * q] = b11;
@@ -556,18 +556,21 @@ jacobi_packed_kernel(int bjmax, double bjtol, int blk, int mak, double *__restri
 // Per-block state of the sweep loop: [initye, ye, dye, k, done, sumdiag].
 struct SweepState { double initye, ye, dye; int k, done; double sumdiag; };
 
+// R: the element type of the stacked matrices (FP64, or FP32 for a
+// preconditioner built in single precision); sums, angles and V in FP64.
+template <typename R>
 __global__ void __launch_bounds__(kThreads)
-gpu_partial_kernel(int mode, int mak, int ndk, const double *__restrict__ HOSB, double *__restrict__ partial)
+gpu_partial_kernel(int mode, int mak, int ndk, const R *__restrict__ HOSB, double *__restrict__ partial)
 {
     // mode 1: sumOffDiag; mode 2: sumDiag.
     __shared__ double red[96];
     const int b = blockIdx.y;
-    const double *H = HOSB + (i64)b * ndk * mak * mak;
+    const R *H = HOSB + (i64)b * ndk * mak * mak;
     double sA = 0.0, sB = 0.0, sC = 0.0;
     if (mode == 1) {
         // upper triangles: column col holds rows 0..col-1 contiguously (ndk * col numbers)
         for (int col = 1 + blockIdx.x; col < mak; col += gridDim.x) {
-            const double *Hc = H + (i64)ndk * mak * col;
+            const R *Hc = H + (i64)ndk * mak * col;
             const int cnt = ndk * col;
             for (int e = threadIdx.x; e < cnt; e += blockDim.x) { const double h = Hc[e]; sA = fma(h, h, sA); }
         }
@@ -588,8 +591,9 @@ gpu_partial_kernel(int mode, int mak, int ndk, const double *__restrict__ HOSB, 
 
 // One CTA per (plane t of the batch, block b): A, B, C over the stack, the
 // angle, and V's columns p_t, q_t.
+template <typename R>
 __global__ void __launch_bounds__(kThreads)
-gpu_batch_angle_kernel(int mak, int ndk, int a, int i, int blk, int ms, const double *__restrict__ HOSB,
+gpu_batch_angle_kernel(int mak, int ndk, int a, int i, int blk, int ms, const R *__restrict__ HOSB,
                        double *__restrict__ rcs, double *__restrict__ rsn, double *__restrict__ VOSB,
                        const SweepState *__restrict__ st)
 {
@@ -598,7 +602,7 @@ gpu_batch_angle_kernel(int mak, int ndk, int a, int i, int blk, int ms, const do
     const int t = blockIdx.x, p = a + t, q = a + i + t;
     for (int b = blockIdx.y; b < blk; b += gridDim.y) {
         if (st[b].done) continue;
-        const double *H = HOSB + (i64)b * ndk * mak * mak;
+        const R *H = HOSB + (i64)b * ndk * mak * mak;
         double sA = 0.0, sB = 0.0, sC = 0.0;
         for (int kk = threadIdx.x; kk < ndk; kk += blockDim.x) {
             const double o = H[kk + (i64)ndk * (p + (i64)mak * q)];
@@ -626,8 +630,9 @@ gpu_batch_angle_kernel(int mak, int ndk, int a, int i, int blk, int ms, const do
     }
 }
 
+template <typename R>
 __global__ void __launch_bounds__(kThreads)
-gpu_batch_rotate_kernel(int mak, int ndk, int a, int i, int m, int blk, int ms, double *__restrict__ HOSB,
+gpu_batch_rotate_kernel(int mak, int ndk, int a, int i, int m, int blk, int ms, R *__restrict__ HOSB,
                         const double *__restrict__ rcs, const double *__restrict__ rsn,
                         const SweepState *__restrict__ st)
 {
@@ -635,11 +640,11 @@ gpu_batch_rotate_kernel(int mak, int ndk, int a, int i, int m, int blk, int ms, 
     const float rm = 1.0f / (float)m;
     for (int b = blockIdx.y; b < blk; b += gridDim.y) {
         if (st[b].done) continue;
-        double *H = HOSB + (i64)b * ndk * mak * mak;
+        R *H = HOSB + (i64)b * ndk * mak * mak;
         const double *cs = rcs + (i64)b * ms, *sn = rsn + (i64)b * ms;
         for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < total; e += gridDim.x * blockDim.x) {
             const int u = e / ndk;
-            batch_item<false>(H, ndk, mak, mak, a, i, m, cs, sn, u, e - u * ndk, rm);
+            batch_item<false, R>(H, ndk, mak, mak, a, i, m, cs, sn, u, e - u * ndk, rm);
         }
     }
 }
@@ -666,7 +671,8 @@ __global__ void gpu_sweep_kernel(int mode, int nchunk, int bjmax, double bjtol,
     S.done = !(fabs(S.dye) > S.initye * bjtol && S.k <= bjmax);
 }
 
-__global__ void gpu_finish_kernel(int nchunk, int blk, int mak, int ndk, double *__restrict__ HOSB,
+template <typename R>
+__global__ void gpu_finish_kernel(int nchunk, int blk, int mak, int ndk, R *__restrict__ HOSB,
                                   double *__restrict__ EIG, const double *__restrict__ partial,
                                   SweepState *__restrict__ st, double *__restrict__ bstats)
 {
@@ -679,13 +685,13 @@ __global__ void gpu_finish_kernel(int nchunk, int blk, int mak, int ndk, double 
         bstats[3 * (i64)b + 1] = fabs(1.0 - S.ye / S.initye);
         bstats[3 * (i64)b + 2] = s;
     }
-    double *H = HOSB + (i64)b * ndk * mak * mak;
+    R *H = HOSB + (i64)b * ndk * mak * mak;
     const i64 total = (i64)ndk * mak;
     for (i64 e = blockIdx.x * (i64)blockDim.x + threadIdx.x; e < total; e += (i64)gridDim.x * blockDim.x) {
         const int kk = (int)(e % ndk), i = (int)(e / ndk);
         const i64 di = kk + (i64)ndk * (i + (i64)mak * i);
-        EIG[kk + (i64)ndk * (i + (i64)mak * b)] = H[di];
-        H[di] = 0.0;
+        EIG[kk + (i64)ndk * (i + (i64)mak * b)] = (double)H[di];
+        H[di] = R(0);
     }
 }
 
@@ -704,6 +710,69 @@ static int gridsz(i64 items)
     if (g > 152 * 32) g = 152 * 32;
     if (g < 1) g = 1;
     return (int)g;
+}
+
+// The spread schedule's sweeps of one level on stacked matrices H (element
+// type R) in global memory: V, the sums and the angles in FP64.
+template <typename R>
+static int spread_sweeps(int bjmax, double bjtol, int blk, int mak, int ndk, R *H, double *VOSB, double *EIG,
+                         double *d_bstats, cudaStream_t s)
+{
+    int rc = 0;
+    const int gy = std::min(blk, 65535);
+    const int npart_off = std::max(1, std::min(64, (int)(((i64)ndk * mak * mak + kThreads * 8 - 1) / (kThreads * 8))));
+    const int ms = std::max(1, mak / 2);
+    double *partial = nullptr, *rcs = nullptr;
+    SweepState *st = nullptr;
+    SC_CUDA(cudaMallocAsync(&partial, sizeof(double) * 3 * (size_t)npart_off * blk, s));
+    SC_CUDA(cudaMallocAsync(&rcs, sizeof(double) * 2 * (size_t)ms * blk, s));
+    SC_CUDA(cudaMallocAsync(&st, sizeof(SweepState) * (size_t)blk, s));
+    double *rsn = rcs + (size_t)ms * blk;
+    identity_kernel<<<gridsz((i64)mak * mak * blk), kThreads, 0, s>>>(mak, blk, VOSB);
+    if (blk > 65535) { set_error("hosbdiag: %d blocks too many for the spread schedule", blk); rc = SCALIT_EINVAL; }
+    if ((i64)ndk * mak * mak > 2147483647LL) { set_error("hosbdiag: a block of %d x %d x %d is too large", ndk, mak, mak); rc = SCALIT_EINVAL; }
+    const dim3 goff(npart_off, blk);
+    if (!rc) {
+        gpu_partial_kernel<R><<<goff, kThreads, 0, s>>>(1, mak, ndk, H, partial);
+        gpu_sweep_kernel<<<(blk + 127) / 128, 128, 0, s>>>(0, npart_off, bjmax, bjtol, partial, st, blk);
+        SC_CHECK_LAUNCH();
+    }
+    std::vector<SweepState> hst(blk);
+    const int max_ctas = 152 * 16;
+    for (int sweep = 0; !rc && sweep <= bjmax + 1; ++sweep) {
+        SC_CUDA(cudaMemcpyAsync(hst.data(), st, sizeof(SweepState) * blk, cudaMemcpyDeviceToHost, s));
+        SC_CUDA(cudaStreamSynchronize(s));
+        bool any = false;
+        for (int b = 0; b < blk; ++b) any |= !hst[b].done;
+        if (!any) break;
+        for (int i = 1; i <= mak - 1; ++i) {
+            for (int a = 0; a < mak - i; a += i) {
+                const int m = std::min(i, mak - i - a);
+                const i64 items = (i64)ndk * ((i64)(mak - 2 * m) * m + (i64)m * m);
+                const int gx = (int)std::max<i64>(1, std::min<i64>((items + kThreads - 1) / kThreads,
+                                                                   std::max(1, max_ctas / gy)));
+                gpu_batch_angle_kernel<R><<<dim3(m, gy), kThreads, 0, s>>>(mak, ndk, a, i, blk, ms, H, rcs, rsn,
+                                                                        VOSB, st);
+                gpu_batch_rotate_kernel<R><<<dim3(gx, gy), kThreads, 0, s>>>(mak, ndk, a, i, m, blk, ms, H,
+                                                                          rcs, rsn, st);
+            }
+        }
+        SC_CHECK_LAUNCH();
+        gpu_partial_kernel<R><<<goff, kThreads, 0, s>>>(1, mak, ndk, H, partial);
+        gpu_sweep_kernel<<<(blk + 127) / 128, 128, 0, s>>>(1, npart_off, bjmax, bjtol, partial, st, blk);
+        SC_CHECK_LAUNCH();
+    }
+    if (!rc) {
+        const i64 items = (i64)ndk * mak;
+        const int grot = (int)std::min<i64>((items + kThreads - 1) / kThreads, 152 * 8);
+        gpu_partial_kernel<R><<<goff, kThreads, 0, s>>>(2, mak, ndk, H, partial);
+        gpu_finish_kernel<R><<<dim3(grot, blk), kThreads, 0, s>>>(npart_off, blk, mak, ndk, H, EIG, partial, st, d_bstats);
+        SC_CHECK_LAUNCH();
+    }
+    cudaFreeAsync(partial, s);
+    cudaFreeAsync(rcs, s);
+    cudaFreeAsync(st, s);
+    return rc;
 }
 
 int hosbdiag_device(scalit_ctx *c, int bjmax, double bjtol, int blk, int mak, int ndk,
@@ -760,60 +829,17 @@ int hosbdiag_device(scalit_ctx *c, int bjmax, double bjtol, int blk, int mak, in
                                                                 d_bstats);
         }
         SC_CHECK_LAUNCH();
+    } else if (f32) {
+        // FP32 sweeps on an FP32 copy of the stacks (the FP64 HOSB is left as
+        // it came: the build reads only EIG0 and V after a level)
+        float *Hf = nullptr;
+        SC_CUDA(cudaMallocAsync(&Hf, sizeof(float) * (size_t)ndk * mak * mak * blk, s));
+        rc = to_f32(HOSB, Hf, (i64)ndk * mak * mak * blk, s);
+        if (!rc) rc = spread_sweeps<float>(bjmax, bjtol, blk, mak, ndk, Hf, VOSB, EIG, d_bstats, s);
+        cudaFreeAsync(Hf, s);
+        if (rc) { cudaFreeAsync(d_bstats, s); return rc; }
     } else {
-        const int gy = std::min(blk, 65535);
-        const int npart_off = std::max(1, std::min(64, (int)(((i64)ndk * mak * mak + kThreads * 8 - 1) / (kThreads * 8))));
-        const int ms = std::max(1, mak / 2);
-        double *partial = nullptr, *rcs = nullptr;
-        SweepState *st = nullptr;
-        SC_CUDA(cudaMallocAsync(&partial, sizeof(double) * 3 * (size_t)npart_off * blk, s));
-        SC_CUDA(cudaMallocAsync(&rcs, sizeof(double) * 2 * (size_t)ms * blk, s));
-        SC_CUDA(cudaMallocAsync(&st, sizeof(SweepState) * (size_t)blk, s));
-        double *rsn = rcs + (size_t)ms * blk;
-        identity_kernel<<<gridsz((i64)mak * mak * blk), kThreads, 0, s>>>(mak, blk, VOSB);
-        if (blk > 65535) { set_error("hosbdiag: %d blocks too many for the spread schedule", blk); rc = SCALIT_EINVAL; }
-        if ((i64)ndk * mak * mak > 2147483647LL) { set_error("hosbdiag: a block of %d x %d x %d is too large", ndk, mak, mak); rc = SCALIT_EINVAL; }
-        const dim3 goff(npart_off, blk);
-        if (!rc) {
-            gpu_partial_kernel<<<goff, kThreads, 0, s>>>(1, mak, ndk, HOSB, partial);
-            gpu_sweep_kernel<<<(blk + 127) / 128, 128, 0, s>>>(0, npart_off, bjmax, bjtol, partial, st, blk);
-            SC_CHECK_LAUNCH();
-        }
-        std::vector<SweepState> hst(blk);
-        const int max_ctas = 152 * 16;
-        for (int sweep = 0; !rc && sweep <= bjmax + 1; ++sweep) {
-            SC_CUDA(cudaMemcpyAsync(hst.data(), st, sizeof(SweepState) * blk, cudaMemcpyDeviceToHost, s));
-            SC_CUDA(cudaStreamSynchronize(s));
-            bool any = false;
-            for (int b = 0; b < blk; ++b) any |= !hst[b].done;
-            if (!any) break;
-            for (int i = 1; i <= mak - 1; ++i) {
-                for (int a = 0; a < mak - i; a += i) {
-                    const int m = std::min(i, mak - i - a);
-                    const i64 items = (i64)ndk * ((i64)(mak - 2 * m) * m + (i64)m * m);
-                    const int gx = (int)std::max<i64>(1, std::min<i64>((items + kThreads - 1) / kThreads,
-                                                                       std::max(1, max_ctas / gy)));
-                    gpu_batch_angle_kernel<<<dim3(m, gy), kThreads, 0, s>>>(mak, ndk, a, i, blk, ms, HOSB, rcs, rsn,
-                                                                            VOSB, st);
-                    gpu_batch_rotate_kernel<<<dim3(gx, gy), kThreads, 0, s>>>(mak, ndk, a, i, m, blk, ms, HOSB,
-                                                                              rcs, rsn, st);
-                }
-            }
-            SC_CHECK_LAUNCH();
-            gpu_partial_kernel<<<goff, kThreads, 0, s>>>(1, mak, ndk, HOSB, partial);
-            gpu_sweep_kernel<<<(blk + 127) / 128, 128, 0, s>>>(1, npart_off, bjmax, bjtol, partial, st, blk);
-            SC_CHECK_LAUNCH();
-        }
-        if (!rc) {
-            const i64 items = (i64)ndk * mak;
-            const int grot = (int)std::min<i64>((items + kThreads - 1) / kThreads, 152 * 8);
-            gpu_partial_kernel<<<goff, kThreads, 0, s>>>(2, mak, ndk, HOSB, partial);
-            gpu_finish_kernel<<<dim3(grot, blk), kThreads, 0, s>>>(npart_off, blk, mak, ndk, HOSB, EIG, partial, st, d_bstats);
-            SC_CHECK_LAUNCH();
-        }
-        cudaFreeAsync(partial, s);
-        cudaFreeAsync(rcs, s);
-        cudaFreeAsync(st, s);
+        rc = spread_sweeps<double>(bjmax, bjtol, blk, mak, ndk, HOSB, VOSB, EIG, d_bstats, s);
         if (rc) { cudaFreeAsync(d_bstats, s); return rc; }
     }
     SC_CUDA(cudaMemcpyAsync(bstats.data(), d_bstats, sizeof(double) * 3 * (size_t)blk, cudaMemcpyDeviceToHost, s));

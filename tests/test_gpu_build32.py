@@ -1,10 +1,11 @@
-"""Preconditioner build with FP32 Jacobi sweeps on the one-matrix blocks
+"""Preconditioner build with FP32 Jacobi sweeps
 (scalit_set_build_precision(SCALIT_PREC_FP32)): the build the mixed PIST arm
 uses, since its preconditioner only feeds FP32 inner solves.
 
 * EIG0 equals the FP64 build's (the same rotation order, FP32 rounding), the
-  first level's V blocks are orthogonal to FP32 accuracy, and the outer
-  levels (FP64 sweeps in both builds) follow from them;
+  first level's V blocks are orthogonal to FP32 accuracy; the grids put the
+  outer levels on both the one-CTA stacks (FP64 in both builds) and the
+  spread schedule (FP32 stacks);
 * mixed PIST on the FP32-built preconditioner (QMR tolerance 1e-6, FP64
   residual refinement to 1e-8 Eh, as the bench's mixed arm runs) reproduces
   the oracle's committed 24x32x20 levels within 1e-4 cm^-1 and meets the
