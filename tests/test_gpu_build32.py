@@ -74,6 +74,23 @@ def test_fp16_px_storage(lib):
     assert torch.equal(Y32, Yb)
 
 
+def test_fp16_px_storage_needs_blocks_of_eight(lib):
+    """First levels of a length that is not a multiple of 8 keep the FP32
+    matrices (the FP16 chunks would not be 16-byte aligned): storage 16 then
+    gives the FP32 P*X bit for bit."""
+    torch = pytest.importorskip("torch")
+    p = hm.build_problem(hm.Grid3(20, 12, 8), hm.PES())
+    with capi.Context.from_problem(p, e0=float(p.RES.min()) - 1e-3) as ctx:
+        ctx.build_osb(20, 1e-4)
+        X = torch.randn(2, p.N, dtype=torch.float32, device="cuda")
+        Y32, Y16 = torch.empty_like(X), torch.empty_like(X)
+        ctx.px_f32_device(X, Y32, 2)
+        ctx.set_fp32_px_storage(16)
+        ctx.px_f32_device(X, Y16, 2)
+        torch.cuda.synchronize()
+    assert torch.equal(Y32, Y16)
+
+
 @pytest.mark.parametrize("bits", [32, 16])
 def test_mixed_pist_on_fp32_build(lib, bits):
     with open(os.path.join(os.path.dirname(__file__), "golden", "pist_tri-24x32x20.json")) as f:
