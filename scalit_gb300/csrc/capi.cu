@@ -430,19 +430,38 @@ int scalit_hx(scalit_ctx *c, int ntype, int nvec, const double *X, double *Y)
     if (!c->loaded) { set_error("H*X before scalit_load"); return SCALIT_ESTATE; }
     // Chunks of vectors in two device buffer sets; the copy-in of chunk k+1 and
     // the copy-out of chunk k-1 overlap the product of chunk k (three streams).
+    // The chunks grow 1, 2, 4 .. up to G vectors and shrink the same way at the
+    // end, so only one vector's copy-in and one vector's copy-out are exposed
+    // (a copy of a vector takes about half its product's time) while the
+    // middle chunks run the product on several vectors at once.
     const i64 N = c->L.N;
-    const i64 target = (64LL << 20) / (8 * N);
-    int G = (int)std::max<i64>(1, std::min<i64>(target, 64));
-    if (nvec >= 2) G = std::min(G, (nvec + 1) / 2);
-    G = std::min(G, nvec);
+    const i64 target = (256LL << 20) / (8 * N);
+    const int G = (int)std::max<i64>(1, std::min<i64>(std::min<i64>(target, 4), nvec));
+    std::vector<int> sizes;
+    {
+        std::vector<int> up;
+        for (int g = 1; g < G; g *= 2) up.push_back(g);
+        int su = 0;
+        for (int g : up) su += g;
+        if (2 * su >= nvec) {
+            sizes.push_back(1);
+            int rem = nvec - 1;
+            while (rem > 1) { const int g = std::min(2, rem - 1); sizes.push_back(g); rem -= g; }
+            if (rem == 1) sizes.push_back(1);
+        } else {
+            sizes = up;
+            for (int mid = nvec - 2 * su; mid > 0;) { const int g = std::min(G, mid); sizes.push_back(g); mid -= g; }
+            for (auto it = up.rbegin(); it != up.rend(); ++it) sizes.push_back(*it);
+        }
+    }
     double *w = nullptr;
     int rc = work_get(c, sizeof(double) * 4 * (size_t)G * N, (void **)&w);
     if (rc) return rc;
     double *Xd[2] = {w, w + (i64)G * N}, *Yd[2] = {w + 2 * (i64)G * N, w + 3 * (i64)G * N};
     cudaEvent_t *ev = c->ev;   // [in0, in1, comp0, comp1, out0, out1]
-    for (int v0 = 0, k = 0; v0 < nvec; v0 += G, ++k) {
+    for (int v0 = 0, k = 0; v0 < nvec; v0 += sizes[k], ++k) {
         const int b = k & 1;
-        const int nb = std::min(G, nvec - v0);
+        const int nb = sizes[k];
         const size_t bytes = sizeof(double) * (size_t)nb * N;
         SC_CUDA(cudaStreamWaitEvent(c->s_in, ev[2 + b], 0));
         SC_CUDA(cudaMemcpyAsync(Xd[b], X + (i64)v0 * N, bytes, cudaMemcpyHostToDevice, c->s_in));
