@@ -271,7 +271,8 @@ tc64p_level_kernel(Tc64pArgs g, const __grid_constant__ CUtensorMap tmA, const _
                 const bool skip = vgated(z);
                 for (int ch = 0; ch < nck; ++ch, ++cc) {
                     const int sl = cc % g.ering;
-                    if (cc >= g.ering && !mbar_wait(&eempty[sl], (uint32_t)(((cc / g.ering) - 1) & 1))) { fail(); break; }
+                    // one thread: its waits suspend on the barrier (as in tc_fp32p.cu)
+                    if (cc >= g.ering && !mbar_wait_timed(&eempty[sl], (uint32_t)(((cc / g.ering) - 1) & 1))) { fail(); break; }
                     unsigned char *dst = reinterpret_cast<unsigned char *>(stage) + (size_t)sl * g.echunk;
                     if (skip || (!g.accumulate && !dg)) {
                         mbar_arrive(&efull[sl]);
@@ -304,7 +305,7 @@ tc64p_level_kernel(Tc64pArgs g, const __grid_constant__ CUtensorMap tmA, const _
             int prod = 0;
             for (; prod < nsteps && !*abort_flag; ++prod) {
                 const int sl = prod % kQSlots;
-                if (prod >= kQSlots && !mbar_wait(&empty[sl], (uint32_t)(((prod / kQSlots) - 1) & 1))) { fail(); break; }
+                if (prod >= kQSlots && !mbar_wait_timed(&empty[sl], (uint32_t)(((prod / kQSlots) - 1) & 1))) { fail(); break; }
                 unsigned char *dst = slots + sl * kQSlot;
                 if (pskip) {
                     mbar_arrive(&full[sl]);
